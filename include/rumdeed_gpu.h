@@ -1,0 +1,160 @@
+/*
+ * rumdeed_gpu.h -- C ABI of librumdeed_gb300, the GB300 (sm_103a)
+ * implementation of RUMDEED's time-step hot path.
+ *
+ * The reference (NanoPhysicsCenter/RUMDEED, Fortran 2008) exposes this path
+ * as Fortran module procedures that share state through module globals.  Each
+ * entry point below replaces one of them; a Fortran iso_c_binding interface
+ * module that keeps the old procedure names is given in INTEGRATION.md.
+ *
+ * Conventions
+ *  - Every function returns an int status: RD_OK (0) or a negative RD_ERR_*.
+ *    rd_last_error() returns a message for the last failure of the calling
+ *    thread.  No function aborts the process.
+ *  - Handles are opaque; device state is owned by the library.  Host pointers
+ *    are borrowed for the duration of the call only.
+ *  - Vectors use the reference layout: (3, N) column-major, i.e. x, y, z of a
+ *    particle (or point) are consecutive.  Units are SI (m, m/s, m/s^2, C, s).
+ *  - Calls on one engine are not thread-safe; use one host thread per engine
+ *    (the reference calls in from one thread as well).
+ *  - Indices are 0-based (the reference's are 1-based).
+ */
+#ifndef RUMDEED_GPU_H
+#define RUMDEED_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  RD_OK = 0,
+  RD_ERR_INVALID = -1,   /* bad argument */
+  RD_ERR_CUDA = -2,      /* CUDA runtime error (message in rd_last_error) */
+  RD_ERR_NOMEM = -3,     /* device allocation failed */
+  RD_ERR_CAPACITY = -4,  /* no diode slot / pool range / chain range free */
+  RD_ERR_STATE = -5,     /* call not valid in the current state */
+  RD_ERR_NOTFOUND = -6   /* unknown diode */
+};
+
+enum { RD_GEOM_PLANAR = 1, RD_GEOM_TIP = 2 };
+enum { RD_PREC_FP64 = 0, RD_PREC_FP32C = 1 };
+enum { RD_SPECIES_ELEC = 1, RD_SPECIES_ION = 2, RD_SPECIES_ATOM = 3 };
+enum { RD_REMOVE_TOP = 1, RD_REMOVE_BOT = 2 };
+
+typedef struct rd_engine rd_engine;
+
+/* Engine: one GPU, a pool of diode slots sharing one particle pool. */
+typedef struct {
+  int device;                   /* CUDA device ordinal */
+  int precision;                /* RD_PREC_FP64 (plain) or RD_PREC_FP32C (compensated) */
+  int max_diodes;               /* diode slots */
+  long long particle_capacity;  /* particle pool size (sum of diode capacities) */
+  long long chain_capacity;     /* MH chain pool size (sum of per-diode chain caps) */
+  long long quad_capacity;      /* supply quadrature points over all diodes */
+  int target_items;             /* work items per pair sum (0 = 8 x grid) */
+  int grid_blocks;              /* persistent grid size (0 = 4 x SM count) */
+} rd_engine_config;
+
+/* One diode (the namelist /input/ of one run, src/mod_global.F90:426-439). */
+typedef struct {
+  int geometry;            /* RD_GEOM_PLANAR or RD_GEOM_TIP */
+  double V_s;              /* voltage over the gap (V) */
+  double gap;              /* planar gap d = box_dim(3) (m); tips use d_tip + h_tip */
+  double time_step;        /* s */
+  int image_charge;        /* 0/1 */
+  int N_ic_max;            /* image partners: 1 + 4*N_ic_max */
+  int capacity;            /* MAX_PARTICLES of this diode */
+  double emitter_pos[2];   /* planar emitter lower-left corner (m) */
+  double emitter_dim[2];   /* planar emitter size (m) */
+  int work_nx, work_ny;    /* checkerboard work function grid (1 x 1 = uniform) */
+  const double* work;      /* work_ny x work_nx values in eV, row 0 = top row */
+  double tip_dim[3];       /* tip (d_tip, R_base, h_tip) in m */
+  double tip_work_function;/* eV (the reference hard-codes 4.7) */
+  int emission;            /* 0: no emission; 1: Fowler-Nordheim field emission */
+  int mh_jumps;            /* 0: reference default (200 planar, 80 tip) */
+  int max_chains;          /* MH chains per step at most (0: capacity) */
+  int quad_panels;         /* planar supply rule: panels per side (0: 16) */
+  int quad_order;          /* planar supply rule: Gauss-Legendre order (0: 4) */
+  int init_rounds;         /* MH start-position rounds (0: 10000 as the reference) */
+  unsigned long long seed; /* Philox key of this diode */
+} rd_diode_config;
+
+typedef struct {
+  int n;                   /* particles in flight */
+  int emitted_step, dropped_step, absorbed_top_step, absorbed_bot_step;
+  int chains, chains_failed, chains_capped;
+  long long emitted_total, dropped_total, absorbed_top_total, absorbed_bot_total;
+  long long electron_steps, steps_done;
+  double ramo_current;     /* ramo_current(species_elec) of the last step (A) */
+  double N_sup, MH_std, a_rate, residual;
+} rd_counters;
+
+const char* rd_last_error(void);
+int rd_version(void);
+
+/* Engine lifetime (Init / Particles_To_Device residency, src/main.F90:416-741,
+ * src/mod_verlet.F90:71-111: state is resident for the engine's lifetime). */
+int rd_engine_create(const rd_engine_config* cfg, rd_engine** out);
+int rd_engine_destroy(rd_engine* e);
+int rd_sync(rd_engine* e);
+
+/* Diode slots.  rd_diode_add performs Init_Field_Emission_v2
+ * (src/mod_field_emission_v2.F90:113-135) or Init_Emission_Tip
+ * (src/mod_emission_tip.f90:81-127) for the new slot. */
+int rd_diode_add(rd_engine* e, const rd_diode_config* cfg, int* diode);
+int rd_diode_remove(rd_engine* e, int diode);
+int rd_diode_count(rd_engine* e, int* active);
+
+/* Add_Particle (src/mod_pair.F90:29-159) for n particles in order: appended
+ * at the end, charge/mass by species, Beeman history seeded with
+ * (q/m) E_vac(x); particles beyond the capacity are counted as dropped. */
+int rd_add_particles(rd_engine* e, int diode, int n, const double* pos3n, const double* vel3n,
+                     const int* species, int step, int section);
+
+/* Full state snapshot out (any pointer may be NULL); n_out gets the count.
+ * Arrays must hold `cap` particles. */
+int rd_get_particles(rd_engine* e, int diode, int cap, double* pos3n, double* vel3n,
+                     double* acc3n, double* charge, int* id, int* section, int* n_out);
+
+/* Overwrite positions / velocities / the three acceleration histories of the
+ * first n particles (snapshot in; any pointer may be NULL). */
+int rd_set_particles(rd_engine* e, int diode, int n, const double* pos3n, const double* vel3n,
+                     const double* acc3n, const double* acc_prev3n, const double* acc_prev23n);
+
+/* Calculate_Acceleration_Particles (src/mod_verlet.F90:597-620): sets the
+ * current acceleration of every particle of every diode from the current
+ * positions; copies diode `diode`'s (3, n) result to acc3n if not NULL. */
+int rd_accel(rd_engine* e, int diode, double* acc3n);
+
+/* Calc_Field_at_Batch (src/mod_verlet.F90:1635-1911): field (V/m) at M
+ * points of one diode. */
+int rd_field_at(rd_engine* e, int diode, int M, const double* pos3m, double* field3m);
+
+/* Mark_Particles_Remove (src/mod_pair.F90:169-339), for tests and drivers. */
+int rd_mark_remove(rd_engine* e, int diode, int index, int why);
+
+/* The main-loop phases for all diodes (src/main.F90:175-219):
+ *   rd_do_emission     ptr_Do_Emission (Do_Field_Emission / Do_Emission_Tip)
+ *   rd_update_position Update_Position (Velocity_Verlet, mod_verlet.F90:123-162)
+ *   rd_remove_particles Remove_Particles (mod_pair.F90:352-562)
+ *   rd_step            the three in order, as one captured CUDA graph
+ *   rd_run             nsteps consecutive rd_step calls, steps first..first+nsteps-1 */
+int rd_do_emission(rd_engine* e, int step);
+int rd_update_position(rd_engine* e, int step);
+int rd_remove_particles(rd_engine* e, int step);
+int rd_step(rd_engine* e, int step);
+int rd_run(rd_engine* e, int first_step, int nsteps);
+
+int rd_counters_get(rd_engine* e, int diode, rd_counters* out);
+/* Life-time histogram of removed electrons: hist[k] = electrons that lived
+ * k+1 steps (record_lifetime, src/mod_pair.F90:1135-1160), 1000 entries. */
+int rd_life_time(rd_engine* e, int diode, int* hist1000);
+
+/* Timing of the last rd_run: device milliseconds (CUDA events on the engine
+ * stream) and launches of library kernels per step. */
+int rd_last_run_stats(rd_engine* e, double* ms, int* kernels_per_step);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

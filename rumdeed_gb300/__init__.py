@@ -1,0 +1,314 @@
+"""rumdeed_gb300 -- GB300 (sm_103a) implementation of RUMDEED's time-step hot path.
+
+Python host mirror of the reference's Fortran module interfaces for this path,
+calling librumdeed_gb300.so through its C ABI (include/rumdeed_gpu.h):
+
+    reference (NanoPhysicsCenter/RUMDEED)          here
+    ---------------------------------------------  --------------------------------
+    Add_Particle            mod_pair.F90:29         Diode.add_particle(s)
+    Mark_Particles_Remove   mod_pair.F90:169        Diode.mark_particles_remove
+    Remove_Particles        mod_pair.F90:352        Engine.remove_particles
+    Update_Position         mod_verlet.F90:115      Engine.update_position
+    Calculate_Acceleration_Particles  :597          Engine/Diode.calculate_acceleration_particles
+    Calc_Field_at_Batch     mod_verlet.F90:1635     Diode.calc_field_at_batch
+    ptr_Do_Emission / Do_Field_Emission fe_v2:170   Engine.do_emission
+    main loop               main.F90:175-219        Engine.step / Engine.run
+
+There is no CPU fallback: importing works anywhere, but creating an Engine
+raises if the CUDA library is missing or no GPU is present.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "librumdeed_gb300.so")
+
+RD_OK = 0
+GEOM_PLANAR, GEOM_TIP = 1, 2
+PREC_FP64, PREC_FP32C = 0, 1
+ELEC, ION, ATOM = 1, 2, 3
+REMOVE_TOP, REMOVE_BOT = 1, 2
+
+# Physical constants (src/mod_global.F90:26-45).
+q_0 = 1.602176634e-19
+m_0 = 9.1093837015e-31
+length_scale = 1.0e-9
+time_scale = 1.0e-12
+
+
+class RumdeedError(RuntimeError):
+    pass
+
+
+class EngineConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("max_diodes", C.c_int),
+                ("particle_capacity", C.c_longlong), ("chain_capacity", C.c_longlong),
+                ("quad_capacity", C.c_longlong), ("target_items", C.c_int),
+                ("grid_blocks", C.c_int)]
+
+
+class DiodeConfig(C.Structure):
+    _fields_ = [("geometry", C.c_int), ("V_s", C.c_double), ("gap", C.c_double),
+                ("time_step", C.c_double), ("image_charge", C.c_int), ("N_ic_max", C.c_int),
+                ("capacity", C.c_int), ("emitter_pos", C.c_double * 2),
+                ("emitter_dim", C.c_double * 2), ("work_nx", C.c_int), ("work_ny", C.c_int),
+                ("work", C.POINTER(C.c_double)), ("tip_dim", C.c_double * 3),
+                ("tip_work_function", C.c_double), ("emission", C.c_int), ("mh_jumps", C.c_int),
+                ("max_chains", C.c_int), ("quad_panels", C.c_int), ("quad_order", C.c_int),
+                ("init_rounds", C.c_int), ("seed", C.c_ulonglong)]
+
+
+class Counters(C.Structure):
+    _fields_ = [("n", C.c_int), ("emitted_step", C.c_int), ("dropped_step", C.c_int),
+                ("absorbed_top_step", C.c_int), ("absorbed_bot_step", C.c_int),
+                ("chains", C.c_int), ("chains_failed", C.c_int), ("chains_capped", C.c_int),
+                ("emitted_total", C.c_longlong), ("dropped_total", C.c_longlong),
+                ("absorbed_top_total", C.c_longlong), ("absorbed_bot_total", C.c_longlong),
+                ("electron_steps", C.c_longlong), ("steps_done", C.c_longlong),
+                ("ramo_current", C.c_double), ("N_sup", C.c_double), ("MH_std", C.c_double),
+                ("a_rate", C.c_double), ("residual", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lib = None
+
+# Every entry point of include/rumdeed_gpu.h with its ctypes signature.
+SIGNATURES = {
+    "rd_last_error": (C.c_char_p, []),
+    "rd_version": (C.c_int, []),
+    "rd_engine_create": (C.c_int, [C.POINTER(EngineConfig), C.POINTER(C.c_void_p)]),
+    "rd_engine_destroy": (C.c_int, [C.c_void_p]),
+    "rd_sync": (C.c_int, [C.c_void_p]),
+    "rd_diode_add": (C.c_int, [C.c_void_p, C.POINTER(DiodeConfig), _ip]),
+    "rd_diode_remove": (C.c_int, [C.c_void_p, C.c_int]),
+    "rd_diode_count": (C.c_int, [C.c_void_p, _ip]),
+    "rd_add_particles": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _ip, C.c_int, C.c_int]),
+    "rd_get_particles": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _ip, _ip, _ip]),
+    "rd_set_particles": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp]),
+    "rd_accel": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "rd_field_at": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp]),
+    "rd_mark_remove": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "rd_do_emission": (C.c_int, [C.c_void_p, C.c_int]),
+    "rd_update_position": (C.c_int, [C.c_void_p, C.c_int]),
+    "rd_remove_particles": (C.c_int, [C.c_void_p, C.c_int]),
+    "rd_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "rd_run": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "rd_counters_get": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Counters)]),
+    "rd_life_time": (C.c_int, [C.c_void_p, C.c_int, _ip]),
+    "rd_last_run_stats": (C.c_int, [C.c_void_p, _dp, _ip]),
+}
+
+
+def build(force=False):
+    """Compile librumdeed_gb300.so (nvcc, sm_103a) if it is missing or stale."""
+    from . import builder
+    return builder.build(force=force)
+
+
+def lib():
+    """Load librumdeed_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RumdeedError("librumdeed_gb300.so is not built (run rumdeed_gb300.build())")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != RD_OK:
+        msg = lib().rd_last_error().decode(errors="replace")
+        raise RumdeedError("rumdeed_gb300 error %d: %s" % (rc, msg))
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _vec3(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1, 3)
+    if n is not None and a.shape[0] != n:
+        raise ValueError("expected %d rows" % n)
+    return a
+
+
+class Engine:
+    """One GPU, a pool of diode slots advanced together (segment table)."""
+
+    def __init__(self, precision=PREC_FP32C, max_diodes=16, particle_capacity=1 << 20,
+                 chain_capacity=1 << 16, quad_capacity=1 << 16, device=0, target_items=0,
+                 grid_blocks=0):
+        self.L = lib()
+        cfg = EngineConfig(device, precision, max_diodes, particle_capacity, chain_capacity,
+                           quad_capacity, target_items, grid_blocks)
+        h = C.c_void_p()
+        _check(self.L.rd_engine_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self.precision = precision
+        self.diodes = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.rd_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # diode slots ---------------------------------------------------------------
+    def add_diode(self, geometry=GEOM_PLANAR, V_s=2.0e3, gap=1000e-9, time_step=0.25e-15,
+                  image_charge=True, N_ic_max=0, capacity=4096, emitter_pos=(0.0, 0.0),
+                  emitter_dim=(0.0, 0.0), work=None, tip_dim=(0.0, 0.0, 0.0),
+                  tip_work_function=4.7, emission=False, mh_jumps=0, max_chains=0,
+                  quad_panels=0, quad_order=0, init_rounds=0, seed=1):
+        cfg = DiodeConfig()
+        cfg.geometry = geometry
+        cfg.V_s = V_s
+        cfg.gap = gap
+        cfg.time_step = time_step
+        cfg.image_charge = int(bool(image_charge))
+        cfg.N_ic_max = N_ic_max
+        cfg.capacity = capacity
+        cfg.emitter_pos[:] = list(emitter_pos)
+        cfg.emitter_dim[:] = list(emitter_dim)
+        keep = None
+        if work is not None:
+            keep = np.ascontiguousarray(work, dtype=np.float64)
+            cfg.work_ny, cfg.work_nx = keep.shape
+            cfg.work = keep.ctypes.data_as(_dp)
+        cfg.tip_dim[:] = list(tip_dim)
+        cfg.tip_work_function = tip_work_function
+        cfg.emission = int(bool(emission))
+        cfg.mh_jumps = mh_jumps
+        cfg.max_chains = max_chains
+        cfg.quad_panels = quad_panels
+        cfg.quad_order = quad_order
+        cfg.init_rounds = init_rounds
+        cfg.seed = seed
+        d = C.c_int()
+        _check(self.L.rd_diode_add(self.h, C.byref(cfg), C.byref(d)))
+        del keep
+        dio = Diode(self, d.value)
+        self.diodes[d.value] = dio
+        return dio
+
+    def remove_diode(self, diode):
+        idx = diode.index if isinstance(diode, Diode) else int(diode)
+        _check(self.L.rd_diode_remove(self.h, idx))
+        self.diodes.pop(idx, None)
+
+    # main-loop phases (all diodes) ----------------------------------------------
+    def do_emission(self, step):
+        _check(self.L.rd_do_emission(self.h, step))
+
+    def update_position(self, step):
+        _check(self.L.rd_update_position(self.h, step))
+
+    def remove_particles(self, step):
+        _check(self.L.rd_remove_particles(self.h, step))
+
+    def calculate_acceleration_particles(self):
+        _check(self.L.rd_accel(self.h, next(iter(self.diodes)) if self.diodes else 0, None))
+
+    def step(self, step):
+        _check(self.L.rd_step(self.h, step))
+
+    def run(self, first_step, nsteps):
+        _check(self.L.rd_run(self.h, first_step, nsteps))
+
+    def sync(self):
+        _check(self.L.rd_sync(self.h))
+
+    def last_run_stats(self):
+        ms = C.c_double()
+        k = C.c_int()
+        _check(self.L.rd_last_run_stats(self.h, C.byref(ms), C.byref(k)))
+        return ms.value, k.value
+
+
+class Diode:
+    """One diode slot of an Engine (the module globals of one reference run)."""
+
+    def __init__(self, engine, index):
+        self.e = engine
+        self.index = index
+
+    @property
+    def L(self):
+        return self.e.L
+
+    def add_particles(self, pos, vel=None, species=None, step=1, section=1):
+        pos = _vec3(pos)
+        n = pos.shape[0]
+        vel = None if vel is None else _vec3(vel, n)
+        sp = None if species is None else np.ascontiguousarray(np.broadcast_to(species, (n,)), dtype=np.int32)
+        _check(self.L.rd_add_particles(self.e.h, self.index, n, _p(pos), _p(vel),
+                                       None if sp is None else sp.ctypes.data_as(_ip), step, section))
+
+    def add_particle(self, pos, vel=(0.0, 0.0, 0.0), species=ELEC, step=1, section=1):
+        self.add_particles([pos], [vel], [species], step, section)
+
+    def counters(self):
+        c = Counters()
+        _check(self.L.rd_counters_get(self.e.h, self.index, C.byref(c)))
+        return c.as_dict()
+
+    @property
+    def n(self):
+        return self.counters()["n"]
+
+    def particles(self):
+        n = self.n
+        cap = max(n, 1)
+        pos = np.zeros((cap, 3)); vel = np.zeros((cap, 3)); acc = np.zeros((cap, 3))
+        q = np.zeros(cap); ids = np.zeros(cap, dtype=np.int32); sec = np.zeros(cap, dtype=np.int32)
+        nout = C.c_int()
+        _check(self.L.rd_get_particles(self.e.h, self.index, cap, _p(pos), _p(vel), _p(acc), _p(q),
+                                       ids.ctypes.data_as(_ip), sec.ctypes.data_as(_ip), C.byref(nout)))
+        return {"pos": pos[:n], "vel": vel[:n], "acc": acc[:n], "charge": q[:n], "id": ids[:n],
+                "section": sec[:n]}
+
+    def set_particles(self, pos=None, vel=None, acc=None, acc_prev=None, acc_prev2=None):
+        arrs = [None if a is None else _vec3(a) for a in (pos, vel, acc, acc_prev, acc_prev2)]
+        n = next(a.shape[0] for a in arrs if a is not None)
+        _check(self.L.rd_set_particles(self.e.h, self.index, n, *[_p(a) for a in arrs]))
+
+    def calculate_acceleration_particles(self):
+        n = self.n
+        out = np.zeros((max(n, 1), 3))
+        _check(self.L.rd_accel(self.e.h, self.index, _p(out)))
+        return out[:n]
+
+    def calc_field_at_batch(self, pts):
+        pts = _vec3(pts)
+        out = np.zeros_like(pts)
+        _check(self.L.rd_field_at(self.e.h, self.index, pts.shape[0], _p(pts), _p(out)))
+        return out
+
+    def mark_particles_remove(self, i, why):
+        _check(self.L.rd_mark_remove(self.e.h, self.index, i, why))
+
+    def life_time(self):
+        h = np.zeros(1000, dtype=np.int32)
+        _check(self.L.rd_life_time(self.e.h, self.index, h.ctypes.data_as(_ip)))
+        return h

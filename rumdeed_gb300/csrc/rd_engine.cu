@@ -1,0 +1,903 @@
+// rd_engine.cu -- host side of librumdeed_gb300: engine and diode-slot
+// management, the step pipeline and its CUDA graph, and the C ABI declared
+// in include/rumdeed_gpu.h.
+//
+// One engine owns one GPU stream, one particle pool shared by all diode
+// slots (segment table in device memory), the scratch of the pair-sum engine
+// and the Metropolis-Hastings chain pool.  The whole time step -- emission
+// (supply integral, MH chains, emission test and append), Beeman position
+// update, all-pairs forces, velocity update and Ramo current, stable
+// compaction -- is a fixed sequence of kernels whose work lists are built on
+// the device, captured once as a CUDA graph and replayed every step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rumdeed_gpu.h"
+#include "rd_pair.cuh"
+
+// ---- kernels (other translation units) ------------------------------------------
+cudaError_t rd_upload_constants_force(const RdConst&);
+cudaError_t rd_upload_constants_field(const RdConst&);
+cudaError_t rd_upload_constants_step(const RdConst&);
+cudaError_t rd_launch_force(int prec, int geometry_mask, int nic_general, int grid, cudaStream_t st,
+                            const DiodeParams* P, const DiodeDyn* Dy, const Pool& pool,
+                            const PlanEntry* plan, const PlanHeader* ph, double* partial,
+                            int* tickets, double kscale);
+cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st,
+                                   const DiodeParams* P, const Pool& pool, const PlanEntry* plan,
+                                   const PlanHeader* ph, const PointSet& pts, double* partial,
+                                   int* tickets, double kscale);
+cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const DiodeParams* P,
+                                const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
+                                const double* qx, const double* qy, double* qF, double* partial,
+                                int* tickets, double kscale);
+cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                                    const double* qx, const double* qy, const double* qw,
+                                    const double* qF, const double* qfx, const double* qfy,
+                                    const double* work);
+cudaError_t rd_launch_mh_init(int prec, int grid, cudaStream_t st, const DiodeParams* P,
+                              DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
+                              const PlanHeader* ph, const ChainState& cs, const int* ch_off,
+                              const double* work, const int* step_ptr, double kscale);
+cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_t st,
+                              const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
+                              const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
+                              const int* ch_off, const double* work, const int* step_ptr,
+                              int it_idx, double* partial, int* tickets, double kscale);
+cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                           const Pool& pool, const ChainState& cs, const int* ch_off,
+                           const double* work, const int* step_ptr);
+cudaError_t rd_launch_plan(cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy, int nslots,
+                           int mode, int target_items, int max_items, const int* npts,
+                           PlanEntry* plan, PlanHeader* ph);
+cudaError_t rd_launch_pack(int grid, cudaStream_t st, const DiodeParams* P, const Pool& pool,
+                           const PlanEntry* plan, const PlanHeader* ph);
+cudaError_t rd_launch_position(int grid, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                               const Pool& pool, const PlanEntry* plan, const PlanHeader* ph);
+cudaError_t rd_launch_velocity(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
+                               DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
+                               const PlanHeader* ph, double* ramo);
+cudaError_t rd_launch_compact(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
+                              DiodeDyn* Dy, const Pool& pool, const Pool& tmp,
+                              const PlanEntry* plan, const PlanHeader* ph, int* kept, int* life,
+                              const int* step_ptr);
+cudaError_t rd_launch_step_set(cudaStream_t st, int* step_ptr, int step);
+cudaError_t rd_launch_step_inc(cudaStream_t st, int* step_ptr);
+cudaError_t rd_launch_add_particles(cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                                    const Pool& pool, int d, int cnt, const double* pos,
+                                    const double* vel, const int* species, int step, int section);
+cudaError_t rd_launch_mark(cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
+                           int d, int i, int why);
+
+enum { PM_FORCE_PLANAR = 0, PM_FORCE_TIP = 1, PM_FIELD = 2, PM_SUPPLY_PLANAR = 3,
+       PM_SUPPLY_TIP = 4, PM_MH = 5, PM_PART = 6, PM_PART1024 = 7, PM_COUNT = 8 };
+
+// ---- errors -------------------------------------------------------------------------
+static thread_local std::string g_err;
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+#define CK(call)                                                                     \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return fail(RD_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
+  } while (0)
+
+// ---- constants (src/mod_global.F90:26-45,333; src/mod_field_emission_v2.F90:36-47) -----
+static RdConst make_constants() {
+  RdConst k;
+  k.pi = 3.141592653589793238462643383279502884197169399375105820974944592307816406286;
+  const double h = 6.62607015e-34, c = 299792458.0, mu0 = 1.25663706212e-6;
+  const double m_u = 1.66053906660e-27;
+  k.q0 = 1.602176634e-19;
+  k.m0 = 9.1093837015e-31;
+  k.eps0 = 1.0 / (mu0 * (c * c));
+  k.hbar = h / (2.0 * k.pi);
+  k.div_fac_c = 1.0 / (((4.0 * k.pi) * k.eps0) * 1.0);
+  k.a_FN = (k.q0 * k.q0) / ((16.0 * (k.pi * k.pi)) * k.hbar);
+  k.b_FN = (-4.0 / (3.0 * k.hbar)) * std::sqrt((2.0 * k.m0) * k.q0);
+  k.l_const = k.q0 / ((4.0 * k.pi) * k.eps0);
+  k.length_scale = 1.0e-9;
+  k.L2 = k.length_scale * k.length_scale;
+  k.tip_K = (1.0 * k.q0) / ((4.0 * k.pi) * k.eps0);
+  k.m_N2 = 28.0134 * m_u;
+  k.m_N2p = k.m_N2 - k.m0;
+  return k;
+}
+
+// Gauss-Legendre nodes and weights on [-1, 1] (Newton iteration on P_n).
+static void gauss_legendre(int n, double* x, double* w) {
+  const double pi = 3.141592653589793238462643383279502884197169399375105820974944592307816406286;
+  for (int k = 0; k < n; ++k) {
+    double z = std::cos(pi * (k + 0.75) / (n + 0.5)), dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int m = 2; m <= n; ++m) {
+        double p2 = ((2.0 * m - 1.0) * z * p1 - (m - 1.0) * p0) / m;
+        p0 = p1; p1 = p2;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    double p0 = 1.0, p1 = z;
+    for (int m = 2; m <= n; ++m) {
+      double p2 = ((2.0 * m - 1.0) * z * p1 - (m - 1.0) * p0) / m;
+      p0 = p1; p1 = p2;
+    }
+    dp = n * (z * p1 - p0) / (z * z - 1.0);
+    x[k] = -z;
+    w[k] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+  if (n == 1) { x[0] = 0.0; w[0] = 2.0; }
+}
+
+// ---- simple first-fit range allocator -------------------------------------------------
+struct RangeAlloc {
+  std::vector<std::pair<long long, long long>> free_;   // (start, length), sorted
+  void init(long long cap) { free_.clear(); if (cap > 0) free_.push_back({0, cap}); }
+  long long alloc(long long len, long long align) {
+    if (len <= 0) return 0;
+    for (size_t k = 0; k < free_.size(); ++k) {
+      long long s = free_[k].first, l = free_[k].second;
+      long long a = (s + align - 1) / align * align;
+      if (a - s + len <= l) {
+        free_.erase(free_.begin() + k);
+        if (a > s) insert({s, a - s});
+        if (a + len < s + l) insert({a + len, s + l - a - len});
+        return a;
+      }
+    }
+    return -1;
+  }
+  void release(long long s, long long len) { if (len > 0) insert({s, len}); }
+  void insert(std::pair<long long, long long> r) {
+    auto it = std::lower_bound(free_.begin(), free_.end(), r);
+    it = free_.insert(it, r);
+    size_t k = it - free_.begin();
+    if (k + 1 < free_.size() && free_[k].first + free_[k].second == free_[k + 1].first) {
+      free_[k].second += free_[k + 1].second;
+      free_.erase(free_.begin() + k + 1);
+    }
+    if (k > 0 && free_[k - 1].first + free_[k - 1].second == free_[k].first) {
+      free_[k - 1].second += free_[k].second;
+      free_.erase(free_.begin() + k);
+    }
+  }
+};
+
+struct SlotHost {
+  bool used = false;
+  DiodeParams p{};
+  long long pool_off = 0, pool_len = 0;
+  long long ch_off = 0, ch_len = 0;
+  long long q_off = 0, q_len = 0;
+  long long w_off = 0, w_len = 0;
+};
+
+struct rd_engine {
+  rd_engine_config cfg{};
+  int sms = 0, grid = 0;
+  cudaStream_t st = nullptr;
+  RdConst k{};
+  double kscale = 0.0;
+  int max_items = 0;
+  // device memory
+  DiodeParams* dP = nullptr;
+  DiodeDyn* dD = nullptr;
+  Pool pool{}, tmp{};
+  std::vector<void*> allocs;
+  double* work = nullptr;
+  double *qx = nullptr, *qy = nullptr, *qz = nullptr, *qw = nullptr, *qF = nullptr, *qfx = nullptr, *qfy = nullptr;
+  ChainState cs{};
+  int *d_choff = nullptr, *d_qoff = nullptr, *d_npts = nullptr, *d_zero_off = nullptr;
+  PlanEntry* plan[PM_COUNT] = {};
+  PlanHeader* ph[PM_COUNT] = {};
+  double* partial = nullptr;
+  int* tickets = nullptr;
+  int* kept = nullptr;
+  double* ramo = nullptr;
+  int* life = nullptr;
+  int* d_step = nullptr;
+  double *fpx = nullptr, *fpy = nullptr, *fpz = nullptr, *ffx = nullptr, *ffy = nullptr, *ffz = nullptr;
+  long long fcap = 0;
+  double *stage_d = nullptr;
+  int* stage_i = nullptr;
+  long long stage_cap = 0;
+  // host
+  std::vector<SlotHost> slots;
+  RangeAlloc pool_alloc, ch_alloc, q_alloc, w_alloc;
+  // graph
+  cudaGraphExec_t graph = nullptr;
+  std::string graph_sig;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  int last_kernels = 0;
+  int kernels_in_step = 0;
+
+  template <class T>
+  cudaError_t dalloc(T** p, size_t count) {
+    cudaError_t e = cudaMalloc((void**)p, std::max<size_t>(count, 1) * sizeof(T));
+    if (e == cudaSuccess) allocs.push_back((void*)*p);
+    return e;
+  }
+  int nslots_hw() const {
+    int hw = 0;
+    for (size_t s = 0; s < slots.size(); ++s) if (slots[s].used) hw = (int)s + 1;
+    return hw > 0 ? hw : 1;
+  }
+};
+
+static int alloc_pool(rd_engine* e, Pool& P, long long cap) {
+  double** dbl[] = {&P.x, &P.y, &P.z, &P.vx, &P.vy, &P.vz, &P.ax, &P.ay, &P.az,
+                    &P.bx, &P.by, &P.bz, &P.cx, &P.cy, &P.cz, &P.q, &P.m};
+  for (auto p : dbl) CK(e->dalloc(p, cap));
+  int** in[] = {&P.species, &P.id, &P.step0, &P.section, &P.mask};
+  for (auto p : in) CK(e->dalloc(p, cap));
+  float4** f4[] = {&P.pk_hi, &P.pk_lo, &P.ip_hi, &P.ip_lo};
+  for (auto p : f4) CK(e->dalloc(p, cap));
+  return RD_OK;
+}
+
+// ---- pipeline pieces ----------------------------------------------------------------
+static int target_items(const rd_engine* e) {
+  return e->cfg.target_items > 0 ? e->cfg.target_items : 8 * e->grid;
+}
+
+static cudaError_t plan(rd_engine* e, int mode, const int* npts = nullptr) {
+  e->kernels_in_step++;
+  return rd_launch_plan(e->st, e->dP, e->dD, e->nslots_hw(), mode, target_items(e), e->max_items,
+                        npts, e->plan[mode], e->ph[mode]);
+}
+
+struct Sig {
+  bool planar = false, tip = false, emit_planar = false, emit_tip = false, nic = false;
+  int jumps = 0;
+};
+static Sig signature(const rd_engine* e) {
+  Sig s;
+  for (auto& sl : e->slots) {
+    if (!sl.used) continue;
+    const DiodeParams& p = sl.p;
+    if (p.geometry == RD_G_TIP) s.tip = true; else s.planar = true;
+    if (p.geometry == RD_G_PLANAR && p.image_charge && p.N_ic_max > 0) s.nic = true;
+    if (p.emission) {
+      if (p.geometry == RD_G_TIP) s.emit_tip = true; else s.emit_planar = true;
+      s.jumps = std::max(s.jumps, p.mh_jumps);
+    }
+  }
+  return s;
+}
+
+static int launch_emission(rd_engine* e) {
+  Sig s = signature(e);
+  if (!s.emit_planar && !s.emit_tip) return RD_OK;
+  const int prec = e->cfg.precision;
+  const int ns = e->nslots_hw();
+  if (s.emit_planar) {
+    CK(plan(e, PM_SUPPLY_PLANAR));
+    CK(rd_launch_z0_points(prec, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_PLANAR],
+                           e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qF, e->partial, e->tickets,
+                           e->kscale));
+    e->kernels_in_step++;
+  }
+  if (s.emit_tip) {
+    CK(plan(e, PM_SUPPLY_TIP));
+    PointSet pts{e->qx, e->qy, e->qz, e->qfx, e->qfy, e->qF, e->d_qoff};
+    CK(rd_launch_field_points(prec, RD_G_TIP, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_TIP],
+                              e->ph[PM_SUPPLY_TIP], pts, e->partial, e->tickets, e->kscale));
+    e->kernels_in_step++;
+  }
+  CK(rd_launch_supply_reduce(ns, e->st, e->dP, e->dD, e->qx, e->qy, e->qw, e->qF, e->qfx, e->qfy,
+                             e->work));
+  e->kernels_in_step++;
+  CK(plan(e, PM_MH));
+  CK(rd_launch_mh_init(prec, e->grid * 4, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                       e->cs, e->d_choff, e->work, e->d_step, e->kscale));
+  e->kernels_in_step++;
+  const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
+  for (int it = 1; it <= s.jumps; ++it) {
+    CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH],
+                         e->ph[PM_MH], e->cs, e->d_choff, e->work, e->d_step, it, e->partial,
+                         e->tickets, e->kscale));
+    e->kernels_in_step += (gmask == 3) ? 2 : 1;
+  }
+  CK(rd_launch_emit(ns, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step));
+  e->kernels_in_step++;
+  return RD_OK;
+}
+
+static int launch_force(rd_engine* e) {
+  Sig s = signature(e);
+  if (s.planar) {
+    CK(plan(e, PM_FORCE_PLANAR));
+    CK(rd_launch_force(e->cfg.precision, 1, s.nic ? 1 : 0, e->grid, e->st, e->dP, e->dD, e->pool,
+                       e->plan[PM_FORCE_PLANAR], e->ph[PM_FORCE_PLANAR], e->partial, e->tickets,
+                       e->kscale));
+    e->kernels_in_step++;
+  }
+  if (s.tip) {
+    CK(plan(e, PM_FORCE_TIP));
+    CK(rd_launch_force(e->cfg.precision, 2, 0, e->grid, e->st, e->dP, e->dD, e->pool,
+                       e->plan[PM_FORCE_TIP], e->ph[PM_FORCE_TIP], e->partial, e->tickets,
+                       e->kscale));
+    e->kernels_in_step++;
+  }
+  return RD_OK;
+}
+
+static int launch_update_position(rd_engine* e) {
+  const int ns = e->nslots_hw();
+  CK(plan(e, PM_PART));
+  CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART]));
+  e->kernels_in_step++;
+  int rc = launch_force(e);
+  if (rc) return rc;
+  CK(rd_launch_velocity(e->grid, ns, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART],
+                        e->ramo));
+  e->kernels_in_step += 2;
+  return RD_OK;
+}
+
+static int launch_remove(rd_engine* e) {
+  CK(plan(e, PM_PART1024));
+  CK(rd_launch_compact(e->grid, e->nslots_hw(), e->st, e->dP, e->dD, e->pool, e->tmp,
+                       e->plan[PM_PART1024], e->ph[PM_PART1024], e->kept, e->life, e->d_step));
+  e->kernels_in_step += 4;
+  return RD_OK;
+}
+
+static int launch_step_body(rd_engine* e) {
+  e->kernels_in_step = 0;
+  int rc = launch_emission(e);
+  if (rc) return rc;
+  rc = launch_update_position(e);
+  if (rc) return rc;
+  rc = launch_remove(e);
+  if (rc) return rc;
+  CK(rd_launch_step_inc(e->st, e->d_step));
+  e->kernels_in_step++;
+  return RD_OK;
+}
+
+static std::string sig_string(rd_engine* e) {
+  Sig s = signature(e);
+  char b[128];
+  snprintf(b, sizeof b, "%d%d%d%d%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
+           s.jumps, e->nslots_hw());
+  return b;
+}
+
+static int ensure_graph(rd_engine* e) {
+  std::string sig = sig_string(e);
+  if (e->graph && sig == e->graph_sig) return RD_OK;
+  if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+  int rc = launch_step_body(e);
+  cudaError_t ce = cudaStreamEndCapture(e->st, &g);
+  if (rc) { if (ce == cudaSuccess) cudaGraphDestroy(g); return rc; }
+  CK(ce);
+  cudaError_t ie = cudaGraphInstantiate(&e->graph, g, 0);
+  cudaGraphDestroy(g);
+  CK(ie);
+  e->graph_sig = sig;
+  e->last_kernels = e->kernels_in_step;
+  return RD_OK;
+}
+
+static int repack(rd_engine* e) {
+  CK(plan(e, PM_PART));
+  CK(rd_launch_pack(e->grid, e->st, e->dP, e->pool, e->plan[PM_PART], e->ph[PM_PART]));
+  return RD_OK;
+}
+
+static int stage(rd_engine* e, long long doubles, long long ints) {
+  long long need = std::max(doubles, ints);
+  if (need <= e->stage_cap) return RD_OK;
+  if (e->stage_d) cudaFree(e->stage_d);
+  if (e->stage_i) cudaFree(e->stage_i);
+  e->stage_d = nullptr; e->stage_i = nullptr;
+  long long cap = std::max<long long>(need, 1 << 16);
+  CK(cudaMalloc(&e->stage_d, cap * sizeof(double)));
+  CK(cudaMalloc(&e->stage_i, cap * sizeof(int)));
+  e->stage_cap = cap;
+  return RD_OK;
+}
+
+static bool valid_diode(rd_engine* e, int d) {
+  return e && d >= 0 && d < (int)e->slots.size() && e->slots[d].used;
+}
+
+// ---- C ABI ----------------------------------------------------------------------------
+extern "C" {
+
+const char* rd_last_error(void) { return g_err.c_str(); }
+int rd_version(void) { return 10000; }
+
+int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
+  if (!cfg || !out) return fail(RD_ERR_INVALID, "null argument");
+  if (cfg->max_diodes <= 0 || cfg->particle_capacity <= 0)
+    return fail(RD_ERR_INVALID, "max_diodes and particle_capacity must be positive");
+  if (cfg->precision != RD_PREC_FP64 && cfg->precision != RD_PREC_FP32C)
+    return fail(RD_ERR_INVALID, "unknown precision");
+  rd_engine* e = new rd_engine();
+  e->cfg = *cfg;
+  int rc = RD_OK;
+  auto bail = [&](int code) { rd_engine_destroy(e); return code; };
+  cudaError_t ce = cudaSetDevice(cfg->device);
+  if (ce != cudaSuccess) return bail(fail(RD_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(ce)));
+  cudaDeviceProp prop;
+  ce = cudaGetDeviceProperties(&prop, cfg->device);
+  if (ce != cudaSuccess) return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
+  e->sms = prop.multiProcessorCount;
+  e->grid = cfg->grid_blocks > 0 ? cfg->grid_blocks : 4 * e->sms;
+  if ((ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
+  cudaEventCreate(&e->ev0);
+  cudaEventCreate(&e->ev1);
+  e->k = make_constants();
+  e->kscale = e->k.div_fac_c * e->k.q0 * 1.0e18;
+  if (rd_upload_constants_force(e->k) != cudaSuccess || rd_upload_constants_field(e->k) != cudaSuccess ||
+      rd_upload_constants_step(e->k) != cudaSuccess)
+    return bail(fail(RD_ERR_CUDA, "constant upload failed"));
+  const long long cap = cfg->particle_capacity;
+  const int S = cfg->max_diodes;
+  const long long chcap = std::max<long long>(cfg->chain_capacity, 1);
+  const long long qcap = std::max<long long>(cfg->quad_capacity, 1);
+  e->max_items = std::max(65536, 4 * target_items(e));
+  if ((rc = alloc_pool(e, e->pool, cap)) || (rc = alloc_pool(e, e->tmp, cap))) return bail(rc);
+  if (e->dalloc(&e->dP, S) || e->dalloc(&e->dD, S) || e->dalloc(&e->work, (size_t)S * 4 + 4096) ||
+      e->dalloc(&e->qx, qcap) || e->dalloc(&e->qy, qcap) || e->dalloc(&e->qz, qcap) ||
+      e->dalloc(&e->qw, qcap) || e->dalloc(&e->qF, qcap) || e->dalloc(&e->qfx, qcap) ||
+      e->dalloc(&e->qfy, qcap) || e->dalloc(&e->d_choff, S) || e->dalloc(&e->d_qoff, S) ||
+      e->dalloc(&e->d_npts, S) || e->dalloc(&e->d_zero_off, S) ||
+      e->dalloc(&e->partial, (size_t)e->max_items * 3 * RD_ITILE) ||
+      e->dalloc(&e->tickets, e->max_items) || e->dalloc(&e->kept, e->max_items) ||
+      e->dalloc(&e->ramo, cap) || e->dalloc(&e->life, (size_t)S * RD_MAX_LIFE) ||
+      e->dalloc(&e->d_step, 1))
+    return bail(fail(RD_ERR_NOMEM, "device allocation failed"));
+  double** chd[] = {&e->cs.x, &e->cs.y, &e->cs.F, &e->cs.sup, &e->cs.df, &e->cs.px, &e->cs.py,
+                    &e->cs.pF, &e->cs.tx, &e->cs.ty, &e->cs.tz, &e->cs.pxx, &e->cs.pyy, &e->cs.pzz};
+  for (auto p : chd) if (e->dalloc(p, chcap)) return bail(fail(RD_ERR_NOMEM, "chain pool allocation failed"));
+  if (e->dalloc(&e->cs.ok, chcap) || e->dalloc(&e->cs.prop_ok, chcap))
+    return bail(fail(RD_ERR_NOMEM, "chain pool allocation failed"));
+  for (int m = 0; m < PM_COUNT; ++m)
+    if (e->dalloc(&e->plan[m], S) || e->dalloc(&e->ph[m], 1))
+      return bail(fail(RD_ERR_NOMEM, "plan allocation failed"));
+  cudaMemsetAsync(e->dP, 0, sizeof(DiodeParams) * S, e->st);
+  cudaMemsetAsync(e->dD, 0, sizeof(DiodeDyn) * S, e->st);
+  cudaMemsetAsync(e->tickets, 0, sizeof(int) * e->max_items, e->st);
+  cudaMemsetAsync(e->life, 0, sizeof(int) * (size_t)S * RD_MAX_LIFE, e->st);
+  cudaMemsetAsync(e->d_npts, 0, sizeof(int) * S, e->st);
+  cudaMemsetAsync(e->d_zero_off, 0, sizeof(int) * S, e->st);
+  cudaMemsetAsync(e->d_step, 0, sizeof(int), e->st);
+  cudaMemsetAsync(e->pool.mask, 0, sizeof(int) * cap, e->st);
+  if ((ce = cudaStreamSynchronize(e->st)) != cudaSuccess) return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
+  e->slots.resize(S);
+  e->pool_alloc.init(cap);
+  e->ch_alloc.init(chcap);
+  e->q_alloc.init(qcap);
+  e->w_alloc.init((long long)S * 4 + 4096);
+  *out = e;
+  return RD_OK;
+}
+
+int rd_engine_destroy(rd_engine* e) {
+  if (!e) return RD_OK;
+  if (e->st) cudaStreamSynchronize(e->st);
+  if (e->graph) cudaGraphExecDestroy(e->graph);
+  for (void* p : e->allocs) cudaFree(p);
+  if (e->stage_d) cudaFree(e->stage_d);
+  if (e->stage_i) cudaFree(e->stage_i);
+  if (e->fpx) { cudaFree(e->fpx); cudaFree(e->fpy); cudaFree(e->fpz); cudaFree(e->ffx); cudaFree(e->ffy); cudaFree(e->ffz); }
+  if (e->ev0) cudaEventDestroy(e->ev0);
+  if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->st) cudaStreamDestroy(e->st);
+  delete e;
+  return RD_OK;
+}
+
+int rd_sync(rd_engine* e) {
+  if (!e) return fail(RD_ERR_INVALID, "null engine");
+  CK(cudaStreamSynchronize(e->st));
+  return RD_OK;
+}
+
+int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
+  if (!e || !c || !diode) return fail(RD_ERR_INVALID, "null argument");
+  if (c->geometry != RD_GEOM_PLANAR && c->geometry != RD_GEOM_TIP) return fail(RD_ERR_INVALID, "unknown geometry");
+  if (c->capacity <= 0 || c->time_step <= 0.0) return fail(RD_ERR_INVALID, "capacity and time_step must be positive");
+  if (c->N_ic_max < 0 || c->N_ic_max > 64) return fail(RD_ERR_INVALID, "N_ic_max out of range");
+  int s = -1;
+  for (size_t k = 0; k < e->slots.size(); ++k) if (!e->slots[k].used) { s = (int)k; break; }
+  if (s < 0) return fail(RD_ERR_CAPACITY, "no free diode slot");
+  DiodeParams p{};
+  p.active = 1;
+  p.geometry = c->geometry;
+  p.cap = c->capacity;
+  p.image_charge = c->image_charge ? 1 : 0;
+  p.N_ic_max = c->N_ic_max;
+  p.emission = c->emission ? 1 : 0;
+  p.V = c->V_s;
+  p.dt = c->time_step;
+  p.dt2 = c->time_step * c->time_step;
+  p.seed = c->seed;
+  p.init_rounds = c->init_rounds > 0 ? c->init_rounds : 10000;
+  p.work_nx = p.work_ny = 1;
+  if (c->geometry == RD_GEOM_PLANAR) {
+    if (c->gap <= 0.0) return fail(RD_ERR_INVALID, "gap must be positive");
+    p.d = c->gap;
+    p.E_z = -1.0 * c->V_s / p.d;                   // Set_Voltage :2050-2052
+    p.em_x0 = c->emitter_pos[0]; p.em_y0 = c->emitter_pos[1];
+    p.em_Lx = c->emitter_dim[0]; p.em_Ly = c->emitter_dim[1];
+    if (p.emission && (p.em_Lx <= 0.0 || p.em_Ly <= 0.0)) return fail(RD_ERR_INVALID, "emitter_dim must be positive");
+    p.org_x = p.em_x0 + 0.5 * p.em_Lx;
+    p.org_y = p.em_y0 + 0.5 * p.em_Ly;
+    p.mh_jumps = c->mh_jumps > 0 ? c->mh_jumps : 200;   // MH_ndim, fe_v2:70
+    p.mh_lo = 0.00005; p.mh_hi = 0.1250;                 // fe_v2:75-76
+    if (c->work_nx > 0 && c->work_ny > 0 && c->work) { p.work_nx = c->work_nx; p.work_ny = c->work_ny; }
+  } else {
+    // Init_Emission_Tip, src/mod_emission_tip.f90:81-127
+    double dt_ = c->tip_dim[0], Rb = c->tip_dim[1], ht = c->tip_dim[2];
+    if (dt_ <= 0.0 || Rb <= 0.0 || ht <= 0.0) return fail(RD_ERR_INVALID, "tip_dim must be positive");
+    p.d = dt_ + ht;
+    p.h_tip = ht;
+    p.max_xi = ht / dt_ + 1.0;
+    p.a_foci = std::sqrt(((dt_ * dt_) * (Rb * Rb)) / ((ht * ht) + (2.0 * dt_) * ht) + dt_ * dt_);
+    p.eta_1 = -1.0 * dt_ / p.a_foci;
+    double theta = std::acos(dt_ / p.a_foci);
+    p.r_tip = (p.a_foci * std::sin(theta)) * std::tan(theta);
+    p.shift_z = std::fabs((p.a_foci * p.eta_1) * p.max_xi);
+    double pre = std::log((((1.0 + p.eta_1) / (1.0 - p.eta_1)) * (1.0 - 0.0)) / (1.0 + 0.0));
+    p.pre_E_unit = (2.0 * 1.0) / (p.a_foci * pre);
+    p.pre_E = (2.0 * c->V_s) / (p.a_foci * pre);
+    p.tip_phi = c->tip_work_function > 0.0 ? c->tip_work_function : 4.7;
+    p.org_x = 0.0; p.org_y = 0.0;
+    p.mh_jumps = c->mh_jumps > 0 ? c->mh_jumps : 80;     // ndim, emission_tip:506
+    p.mh_lo = 0.0005; p.mh_hi = 0.125;                   // emission_tip:62-63
+  }
+  SlotHost sl;
+  sl.pool_len = p.cap;
+  sl.pool_off = e->pool_alloc.alloc(sl.pool_len, 32);
+  if (sl.pool_off < 0) return fail(RD_ERR_CAPACITY, "particle pool full");
+  p.off = (int)sl.pool_off;
+  auto undo = [&]() {
+    e->pool_alloc.release(sl.pool_off, sl.pool_len);
+    if (sl.ch_len) e->ch_alloc.release(sl.ch_off, sl.ch_len);
+    if (sl.q_len) e->q_alloc.release(sl.q_off, sl.q_len);
+    if (sl.w_len) e->w_alloc.release(sl.w_off, sl.w_len);
+  };
+  // work function table
+  sl.w_len = (long long)p.work_nx * p.work_ny;
+  sl.w_off = e->w_alloc.alloc(sl.w_len, 1);
+  if (sl.w_off < 0) { sl.w_len = 0; undo(); return fail(RD_ERR_CAPACITY, "work-function table full"); }
+  p.work_off = (int)sl.w_off;
+  std::vector<double> wv(sl.w_len, 4.7);
+  if (c->geometry == RD_GEOM_PLANAR && c->work && c->work_nx > 0 && c->work_ny > 0)
+    for (long long k2 = 0; k2 < sl.w_len; ++k2) wv[k2] = c->work[k2];
+  if (p.emission) {
+    p.max_chains = c->max_chains > 0 ? c->max_chains : p.cap;
+    sl.ch_len = p.max_chains;
+    sl.ch_off = e->ch_alloc.alloc(sl.ch_len, 32);
+    if (sl.ch_off < 0) { sl.ch_len = 0; undo(); return fail(RD_ERR_CAPACITY, "MH chain pool full"); }
+    int npt;
+    if (c->geometry == RD_GEOM_PLANAR) {
+      int P_ = c->quad_panels > 0 ? c->quad_panels : 16, Q = c->quad_order > 0 ? c->quad_order : 4;
+      if (Q > 16) { undo(); return fail(RD_ERR_INVALID, "quad_order must be <= 16"); }
+      p.quad_n = P_ * Q;
+      npt = p.quad_n * p.quad_n;
+    } else {
+      npt = 10000;
+    }
+    sl.q_len = npt;
+    sl.q_off = e->q_alloc.alloc(sl.q_len, 32);
+    if (sl.q_off < 0) { sl.q_len = 0; undo(); return fail(RD_ERR_CAPACITY, "quadrature table full"); }
+    p.q_off = (int)sl.q_off;
+    std::vector<double> hx(npt), hy(npt), hz(npt, 0.0), hw(npt);
+    if (c->geometry == RD_GEOM_PLANAR) {
+      int P_ = c->quad_panels > 0 ? c->quad_panels : 16, Q = c->quad_order > 0 ? c->quad_order : 4;
+      double gx[16], gw[16];
+      gauss_legendre(Q, gx, gw);
+      double A = p.em_Lx * p.em_Ly;
+      for (int iy = 0; iy < p.quad_n; ++iy) {
+        double uy = ((iy / Q) + 0.5 * (gx[iy % Q] + 1.0)) / P_, wy = 0.5 * gw[iy % Q] / P_;
+        for (int ix = 0; ix < p.quad_n; ++ix) {
+          double ux = ((ix / Q) + 0.5 * (gx[ix % Q] + 1.0)) / P_, wx = 0.5 * gw[ix % Q] / P_;
+          int k2 = iy * p.quad_n + ix;
+          hx[k2] = p.em_x0 + ux * p.em_Lx;
+          hy[k2] = p.em_y0 + uy * p.em_Ly;
+          hw[k2] = (wx * wy) * A;
+        }
+      }
+    } else {
+      // 100 x 100 midpoint grid in (xi, phi) with the cell areas
+      // (Do_Field_Emission_Tip_OLDCODE :434-481, Tip_Area, xyz_corr)
+      const double pi = e->k.pi;
+      const int nr = 100;
+      double len_phi = 2.0 * pi / nr, len_xi = (p.max_xi - 1.0) / nr, e2 = p.eta_1 * p.eta_1;
+      auto fac = [&](double xi) { return xi * std::sqrt(xi * xi - e2) - e2 * std::log(xi + std::sqrt(xi * xi - e2)); };
+      for (int i = 1; i <= nr; ++i)
+        for (int j = 1; j <= nr; ++j) {
+          double xi_c = 1.0 + (i - 0.5) * len_xi, phi_c = (j - 0.5) * len_phi;
+          int k2 = (i - 1) * nr + (j - 1);
+          double xy = p.a_foci * std::sqrt((xi_c * xi_c - 1.0) * (1.0 - p.eta_1 * p.eta_1));
+          hx[k2] = xy * std::cos(phi_c);
+          hy[k2] = xy * std::sin(phi_c);
+          hz[k2] = (p.a_foci * xi_c) * p.eta_1 + p.shift_z;
+          double xi1 = 1.0 + (i - 1.0) * len_xi, xi2 = 1.0 + (i + 0.0) * len_xi;
+          double ph1 = (j - 1.0) * len_phi, ph2 = (j + 0.0) * len_phi;
+          hw[k2] = (((0.5 * (p.a_foci * p.a_foci)) * std::sqrt(1.0 - e2)) * (ph2 - ph1)) * (fac(xi2) - fac(xi1));
+        }
+    }
+    CK(cudaMemcpyAsync(e->qx + sl.q_off, hx.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemcpyAsync(e->qy + sl.q_off, hy.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemcpyAsync(e->qz + sl.q_off, hz.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
+    CK(cudaMemcpyAsync(e->qw + sl.q_off, hw.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
+    CK(cudaStreamSynchronize(e->st));
+  }
+  CK(cudaMemcpyAsync(e->work + sl.w_off, wv.data(), sl.w_len * sizeof(double), cudaMemcpyHostToDevice, e->st));
+  DiodeDyn y{};
+  y.MH_std = (c->geometry == RD_GEOM_TIP) ? 0.125 : 0.0125;   // fe_v2:58; tip 1.0 clamped to 0.125
+  y.a_rate = (c->geometry == RD_GEOM_TIP) ? 0.5 : 1.0;
+  y.first_dead = 0x7fffffff;
+  int choff = (int)sl.ch_off, qoff = (int)sl.q_off;
+  CK(cudaMemcpyAsync(e->dP + s, &p, sizeof p, cudaMemcpyHostToDevice, e->st));
+  CK(cudaMemcpyAsync(e->dD + s, &y, sizeof y, cudaMemcpyHostToDevice, e->st));
+  CK(cudaMemcpyAsync(e->d_choff + s, &choff, sizeof(int), cudaMemcpyHostToDevice, e->st));
+  CK(cudaMemcpyAsync(e->d_qoff + s, &qoff, sizeof(int), cudaMemcpyHostToDevice, e->st));
+  CK(cudaMemsetAsync(e->life + (size_t)s * RD_MAX_LIFE, 0, sizeof(int) * RD_MAX_LIFE, e->st));
+  CK(cudaMemsetAsync(e->pool.mask + p.off, 0, sizeof(int) * p.cap, e->st));
+  CK(cudaStreamSynchronize(e->st));
+  sl.used = true;
+  sl.p = p;
+  e->slots[s] = sl;
+  *diode = s;
+  return RD_OK;
+}
+
+int rd_diode_remove(rd_engine* e, int d) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  SlotHost& sl = e->slots[d];
+  DiodeParams p{};
+  DiodeDyn y{};
+  CK(cudaMemcpyAsync(e->dP + d, &p, sizeof p, cudaMemcpyHostToDevice, e->st));
+  CK(cudaMemcpyAsync(e->dD + d, &y, sizeof y, cudaMemcpyHostToDevice, e->st));
+  CK(cudaStreamSynchronize(e->st));
+  e->pool_alloc.release(sl.pool_off, sl.pool_len);
+  if (sl.ch_len) e->ch_alloc.release(sl.ch_off, sl.ch_len);
+  if (sl.q_len) e->q_alloc.release(sl.q_off, sl.q_len);
+  if (sl.w_len) e->w_alloc.release(sl.w_off, sl.w_len);
+  sl = SlotHost();
+  return RD_OK;
+}
+
+int rd_diode_count(rd_engine* e, int* active) {
+  if (!e || !active) return fail(RD_ERR_INVALID, "null argument");
+  int n = 0;
+  for (auto& s : e->slots) n += s.used ? 1 : 0;
+  *active = n;
+  return RD_OK;
+}
+
+int rd_add_particles(rd_engine* e, int d, int n, const double* pos, const double* vel,
+                     const int* species, int step, int section) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  if (n < 0 || (n > 0 && !pos)) return fail(RD_ERR_INVALID, "bad particle arrays");
+  int rc = stage(e, 6LL * n, n);
+  if (rc) return rc;
+  if (n > 0) {
+    CK(cudaMemcpyAsync(e->stage_d, pos, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, e->st));
+    if (vel) CK(cudaMemcpyAsync(e->stage_d + 3LL * n, vel, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, e->st));
+    if (species) CK(cudaMemcpyAsync(e->stage_i, species, sizeof(int) * n, cudaMemcpyHostToDevice, e->st));
+  }
+  CK(rd_launch_add_particles(e->st, e->dP, e->dD, e->pool, d, n, e->stage_d, vel ? e->stage_d + 3LL * n : nullptr,
+                             species ? e->stage_i : nullptr, step, section));
+  CK(cudaStreamSynchronize(e->st));
+  return RD_OK;
+}
+
+static int read_dyn(rd_engine* e, int d, DiodeDyn* y) {
+  CK(cudaMemcpyAsync(y, e->dD + d, sizeof(DiodeDyn), cudaMemcpyDeviceToHost, e->st));
+  CK(cudaStreamSynchronize(e->st));
+  return RD_OK;
+}
+
+int rd_get_particles(rd_engine* e, int d, int cap, double* pos, double* vel, double* acc,
+                     double* charge, int* id, int* section, int* n_out) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  DiodeDyn y;
+  int rc = read_dyn(e, d, &y);
+  if (rc) return rc;
+  if (n_out) *n_out = y.n;
+  int n = std::min(y.n, cap);
+  if (n <= 0) return RD_OK;
+  const int off = e->slots[d].p.off;
+  std::vector<double> buf(n);
+  auto get3 = [&](double* dst, double* a, double* b, double* c2) -> int {
+    double* src[3] = {a, b, c2};
+    for (int k2 = 0; k2 < 3; ++k2) {
+      CK(cudaMemcpy(buf.data(), src[k2] + off, sizeof(double) * n, cudaMemcpyDeviceToHost));
+      for (int i = 0; i < n; ++i) dst[3 * i + k2] = buf[i];
+    }
+    return RD_OK;
+  };
+  if (pos && (rc = get3(pos, e->pool.x, e->pool.y, e->pool.z))) return rc;
+  if (vel && (rc = get3(vel, e->pool.vx, e->pool.vy, e->pool.vz))) return rc;
+  if (acc && (rc = get3(acc, e->pool.ax, e->pool.ay, e->pool.az))) return rc;
+  if (charge) CK(cudaMemcpy(charge, e->pool.q + off, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (id) CK(cudaMemcpy(id, e->pool.id + off, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  if (section) CK(cudaMemcpy(section, e->pool.section + off, sizeof(int) * n, cudaMemcpyDeviceToHost));
+  return RD_OK;
+}
+
+int rd_set_particles(rd_engine* e, int d, int n, const double* pos, const double* vel,
+                     const double* acc, const double* accp, const double* accp2) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  DiodeDyn y;
+  int rc = read_dyn(e, d, &y);
+  if (rc) return rc;
+  if (n < 0 || n > y.n) return fail(RD_ERR_INVALID, "n exceeds the particles in flight");
+  const int off = e->slots[d].p.off;
+  std::vector<double> buf(std::max(n, 1));
+  auto put3 = [&](const double* srcv, double* a, double* b, double* c2) -> int {
+    double* dst[3] = {a, b, c2};
+    for (int k2 = 0; k2 < 3; ++k2) {
+      for (int i = 0; i < n; ++i) buf[i] = srcv[3 * i + k2];
+      CK(cudaMemcpy(dst[k2] + off, buf.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    }
+    return RD_OK;
+  };
+  if (n > 0) {
+    if (pos && (rc = put3(pos, e->pool.x, e->pool.y, e->pool.z))) return rc;
+    if (vel && (rc = put3(vel, e->pool.vx, e->pool.vy, e->pool.vz))) return rc;
+    if (acc && (rc = put3(acc, e->pool.ax, e->pool.ay, e->pool.az))) return rc;
+    if (accp && (rc = put3(accp, e->pool.bx, e->pool.by, e->pool.bz))) return rc;
+    if (accp2 && (rc = put3(accp2, e->pool.cx, e->pool.cy, e->pool.cz))) return rc;
+  }
+  if ((rc = repack(e))) return rc;
+  CK(cudaStreamSynchronize(e->st));
+  return RD_OK;
+}
+
+int rd_accel(rd_engine* e, int d, double* acc3n) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  int rc = repack(e);
+  if (rc) return rc;
+  if ((rc = launch_force(e))) return rc;
+  CK(cudaStreamSynchronize(e->st));
+  if (acc3n) return rd_get_particles(e, d, 1 << 30, nullptr, nullptr, acc3n, nullptr, nullptr, nullptr, nullptr);
+  return RD_OK;
+}
+
+int rd_field_at(rd_engine* e, int d, int M, const double* pos, double* field) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  if (M < 0 || (M > 0 && (!pos || !field))) return fail(RD_ERR_INVALID, "bad point arrays");
+  if (M == 0) return RD_OK;
+  if (M > e->fcap) {
+    if (e->fpx) { cudaFree(e->fpx); cudaFree(e->fpy); cudaFree(e->fpz); cudaFree(e->ffx); cudaFree(e->ffy); cudaFree(e->ffz); }
+    long long cap = std::max<long long>(M, 4096);
+    double** bufs[] = {&e->fpx, &e->fpy, &e->fpz, &e->ffx, &e->ffy, &e->ffz};
+    for (auto b : bufs) CK(cudaMalloc(b, cap * sizeof(double)));
+    e->fcap = cap;
+  }
+  std::vector<double> h(M);
+  double* dsts[3] = {e->fpx, e->fpy, e->fpz};
+  for (int k2 = 0; k2 < 3; ++k2) {
+    for (int i = 0; i < M; ++i) h[i] = pos[3 * i + k2];
+    CK(cudaMemcpyAsync(dsts[k2], h.data(), sizeof(double) * M, cudaMemcpyHostToDevice, e->st));
+    CK(cudaStreamSynchronize(e->st));
+  }
+  std::vector<int> np(e->slots.size(), 0);
+  np[d] = M;
+  CK(cudaMemcpyAsync(e->d_npts, np.data(), sizeof(int) * np.size(), cudaMemcpyHostToDevice, e->st));
+  int rc = repack(e);
+  if (rc) return rc;
+  CK(plan(e, PM_FIELD, e->d_npts));
+  PointSet pts{e->fpx, e->fpy, e->fpz, e->ffx, e->ffy, e->ffz, e->d_zero_off};
+  CK(rd_launch_field_points(e->cfg.precision, e->slots[d].p.geometry, e->grid, e->st, e->dP, e->pool,
+                            e->plan[PM_FIELD], e->ph[PM_FIELD], pts, e->partial, e->tickets, e->kscale));
+  double* srcs[3] = {e->ffx, e->ffy, e->ffz};
+  for (int k2 = 0; k2 < 3; ++k2) {
+    CK(cudaMemcpyAsync(h.data(), srcs[k2], sizeof(double) * M, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    for (int i = 0; i < M; ++i) field[3 * i + k2] = h[i];
+  }
+  return RD_OK;
+}
+
+int rd_mark_remove(rd_engine* e, int d, int i, int why) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  if (why != RD_REMOVE_TOP && why != RD_REMOVE_BOT) return fail(RD_ERR_INVALID, "unknown removal flag");
+  CK(rd_launch_mark(e->st, e->dP, e->dD, e->pool, d, i, why));
+  CK(cudaStreamSynchronize(e->st));
+  return RD_OK;
+}
+
+int rd_do_emission(rd_engine* e, int step) {
+  if (!e) return fail(RD_ERR_INVALID, "null engine");
+  CK(rd_launch_step_set(e->st, e->d_step, step));
+  int rc = launch_emission(e);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(e->st));
+  return RD_OK;
+}
+
+int rd_update_position(rd_engine* e, int step) {
+  if (!e) return fail(RD_ERR_INVALID, "null engine");
+  CK(rd_launch_step_set(e->st, e->d_step, step));
+  int rc = launch_update_position(e);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(e->st));
+  return RD_OK;
+}
+
+int rd_remove_particles(rd_engine* e, int step) {
+  if (!e) return fail(RD_ERR_INVALID, "null engine");
+  CK(rd_launch_step_set(e->st, e->d_step, step));
+  int rc = launch_remove(e);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(e->st));
+  return RD_OK;
+}
+
+int rd_run(rd_engine* e, int first_step, int nsteps) {
+  if (!e) return fail(RD_ERR_INVALID, "null engine");
+  if (nsteps < 0) return fail(RD_ERR_INVALID, "nsteps < 0");
+  int rc = ensure_graph(e);
+  if (rc) return rc;
+  CK(rd_launch_step_set(e->st, e->d_step, first_step));
+  CK(cudaEventRecord(e->ev0, e->st));
+  for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(e->graph, e->st));
+  CK(cudaEventRecord(e->ev1, e->st));
+  CK(cudaStreamSynchronize(e->st));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+  e->last_ms = ms;
+  return RD_OK;
+}
+
+int rd_step(rd_engine* e, int step) { return rd_run(e, step, 1); }
+
+int rd_counters_get(rd_engine* e, int d, rd_counters* o) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  if (!o) return fail(RD_ERR_INVALID, "null argument");
+  DiodeDyn y;
+  int rc = read_dyn(e, d, &y);
+  if (rc) return rc;
+  o->n = y.n;
+  o->emitted_step = y.emitted_step; o->dropped_step = y.dropped_step;
+  o->absorbed_top_step = y.absorbed_top_step; o->absorbed_bot_step = y.absorbed_bot_step;
+  o->chains = y.chains; o->chains_failed = y.chains_failed; o->chains_capped = y.chains_capped;
+  o->emitted_total = y.emitted_total; o->dropped_total = y.dropped_total;
+  o->absorbed_top_total = y.absorbed_top_total; o->absorbed_bot_total = y.absorbed_bot_total;
+  o->electron_steps = y.electron_steps; o->steps_done = y.steps_done;
+  o->ramo_current = y.ramo_current; o->N_sup = y.N_sup; o->MH_std = y.MH_std;
+  o->a_rate = y.a_rate; o->residual = y.residual;
+  return RD_OK;
+}
+
+int rd_life_time(rd_engine* e, int d, int* hist) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  if (!hist) return fail(RD_ERR_INVALID, "null argument");
+  CK(cudaMemcpy(hist, e->life + (size_t)d * RD_MAX_LIFE, sizeof(int) * RD_MAX_LIFE, cudaMemcpyDeviceToHost));
+  return RD_OK;
+}
+
+int rd_last_run_stats(rd_engine* e, double* ms, int* kps) {
+  if (!e) return fail(RD_ERR_INVALID, "null engine");
+  if (ms) *ms = e->last_ms;
+  if (kps) *kps = e->last_kernels;
+  return RD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,825 @@
+// rd_field.cu -- field at points and the emission pipeline.
+//
+//  * k_field_points: E at arbitrary points (Calc_Field_at_Batch,
+//    src/mod_verlet.F90:1635-1911): vacuum field plus, for every particle j,
+//    q_j k [ (p - x_j)/(|p - x_j| + l^2)^3 + IC(p, x_j) ] with the image
+//    function evaluated with the point in the "a" role (:1762-1793, :1822-1893).
+//  * k_z0_points / k_mh_jump_planar: the z component at cathode points
+//    (z = 0).  There the Coulomb term and the n = 0 image partner share the
+//    same distance and their x, y parts cancel exactly, so per particle the
+//    field is -2 q_j k sum_h h/(sqrt(dxy^2 + h^2) + l^2)^3 over the partner
+//    heights h in {z_j, z_j +- 2nd}: half the rsqrt count of the generic form
+//    with the same result.
+//  * supply integral, MH chains and emission: the batched planar sampler
+//    Metropolis_Hastings_rectangle_J_batch (src/mod_field_emission_v2.F90:
+//    1284-1458) and the tip sampler Metro_algo_tip_v3 (src/mod_emission_tip.f90:
+//    1241-1390) run as one lockstep batch per diode; the supply integral uses a
+//    composite Gauss-Legendre rule (planar; the reference uses the third-party
+//    Cuba library) or the reference's own 100x100 midpoint grid (tip,
+//    Do_Field_Emission_Tip_OLDCODE :417-534).  Random numbers are Philox
+//    streams keyed by the diode seed with counters (chain, iteration, step,
+//    purpose), so every chain is reproducible and independent of scheduling.
+#include "rd_tiles.cuh"
+
+
+namespace {
+
+// ---- general field at points ---------------------------------------------------
+__device__ __forceinline__ void point_pack(const DiodeParams& p, double x, double y, double z,
+                                           float4& ih, float4& il, float4& iih, float4& iil) {
+  float a, b;
+  split_nm(x, p.org_x, &a, &b); ih.x = a; il.x = b;
+  split_nm(y, p.org_y, &a, &b); ih.y = a; il.y = b;
+  split_nm(z, 0.0, &a, &b); ih.z = a; il.z = b;
+  ih.w = 1.f;
+  il.w = (float)((p.d - z) * 1.0e9);
+  iih = iil = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (p.geometry == RD_G_TIP) {
+    double xi, yi, zi;
+    double dis = tip_image_point(p, x, y, z, &xi, &yi, &zi);
+    split_nm(xi, p.org_x, &a, &b); iih.x = a; iil.x = b;
+    split_nm(yi, p.org_y, &a, &b); iih.y = a; iil.y = b;
+    split_nm(zi, 0.0, &a, &b); iih.z = a; iil.z = b;
+    iih.w = (float)(p.r_tip / dis);
+  }
+}
+
+template <int PREC, int GEOM>
+__global__ void __launch_bounds__(RD_ITILE)
+k_field_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __restrict__ plan,
+               const PlanHeader* __restrict__ ph, PointSet pts, double* __restrict__ partial,
+               int* __restrict__ tickets, double kscale) {
+  __shared__ float4 sh[RD_TILE], sl[RD_TILE], sih[RD_TILE], sil[RD_TILE];
+  __shared__ rd_d4 sj[RD_TILE];
+  const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ItemRef it = decode_item(plan, nd, g);
+    const DiodeParams& p = P[it.d];
+    const int off = p.off, m = plan[it.d].n_i, po = pts.off[it.d];
+    const int i = it.i0 + tid;
+    const bool valid = i < m;
+    double X = valid ? pts.x[po + i] : 0.0, Y = valid ? pts.y[po + i] : 0.0;
+    double Z = valid ? pts.z[po + i] : 0.5 * p.d;
+    double fx, fy, fz;
+    if (PREC == 1) {
+      float4 ih, il, iih, iil;
+      point_pack(p, X, Y, Z, ih, il, iih, iil);
+      const float dnm = (float)(p.d * 1.0e9);
+      F32Acc acc;
+      acc.zero();
+      for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+        __syncthreads();
+        int j = jt + tid;
+        if (j < it.j1) {
+          sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j];
+          if (GEOM == RD_G_TIP) { sih[tid] = pool.ip_hi[off + j]; sil[tid] = pool.ip_lo[off + j]; }
+        }
+        __syncthreads();
+        int kmax = min(RD_TILE, it.j1 - jt);
+        float tx = 0.f, ty = 0.f, tz = 0.f;
+        if (GEOM == RD_G_TIP)
+          tip_tile_f32<T_UPPER>(sh, sl, sih, sil, kmax, ih, il, iih, iil, -1, p.image_charge,
+                                (float)c_k.tip_K, tx, ty, tz);
+        else if (p.N_ic_max == 0)
+          planar_tile_f32<T_UPPER, true>(sh, sl, kmax, ih, il, -1, 0, dnm, p.image_charge, tx, ty, tz);
+        else
+          planar_tile_f32<T_UPPER, false>(sh, sl, kmax, ih, il, -1, p.N_ic_max, dnm, p.image_charge, tx, ty, tz);
+        acc.add(tx, ty, tz);
+      }
+      fx = ((double)acc.hx + (double)acc.lx) * kscale;
+      fy = ((double)acc.hy + (double)acc.ly) * kscale;
+      fz = ((double)acc.hz + (double)acc.lz) * kscale;
+    } else {
+      const double L2 = c_k.L2, dfc = c_k.div_fac_c;
+      fx = fy = fz = 0.0;
+      for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+        __syncthreads();
+        int j = jt + tid;
+        if (j < it.j1) sj[tid] = make_d4(pool.x[off + j], pool.y[off + j], pool.z[off + j], pool.q[off + j]);
+        __syncthreads();
+        int kmax = min(RD_TILE, it.j1 - jt);
+        if (GEOM == RD_G_TIP)
+          tip_tile_f64<T_UPPER>(sj, kmax, X, Y, Z, dfc, -1, p.image_charge, p, L2, c_k.tip_K, fx, fy, fz);
+        else
+          planar_tile_f64<T_UPPER>(sj, kmax, X, Y, Z, dfc, -1, p.N_ic_max, p.d, p.image_charge, L2, fx, fy, fz);
+      }
+    }
+    if (it.nch > 1) {
+      double* pp = partial + (size_t)g * 3 * RD_ITILE;
+      pp[tid] = fx; pp[RD_ITILE + tid] = fy; pp[2 * RD_ITILE + tid] = fz;
+      if (!tile_ticket(tickets, it)) continue;
+      fx = fy = fz = 0.0;
+      for (int c = 0; c < it.nch; ++c) {
+        const double* q = partial + (size_t)(it.base + c) * 3 * RD_ITILE;
+        fx += __ldcg(q + tid); fy += __ldcg(q + RD_ITILE + tid); fz += __ldcg(q + 2 * RD_ITILE + tid);
+      }
+    }
+    if (valid) {
+      double ex, ey, ez;
+      vacuum_field(p, X, Y, Z, &ex, &ey, &ez);
+      pts.fx[po + i] = ex + fx;
+      pts.fy[po + i] = ey + fy;
+      pts.fz[po + i] = ez + fz;
+    }
+  }
+}
+
+// ---- cathode z = 0 field, planar ----------------------------------------------------
+// Sum over one j-tile of q_j sum_h h / r_h^3 (nm units), point at z = 0.
+__device__ __forceinline__ float z0_tile_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
+                                             int kmax, float pxh, float pxl, float pyh, float pyl,
+                                             int nic, float dnm) {
+  float s = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < kmax; ++k) {
+    float4 h = sh[k], l = sl[k];
+    float dx = (pxh - h.x) + (pxl - l.x);
+    float dy = (pyh - h.y) + (pyl - l.y);
+    float dxy2 = fmaf(dx, dx, dy * dy);
+    float zj = h.z + l.z;
+    float inv = rsqrtf(fmaxf(fmaf(zj, zj, dxy2), 1e-20f));
+    s = fmaf(h.w * zj, (inv * inv) * inv, s);
+    for (int n = 1; n <= nic; ++n) {
+      float h1 = zj + 2.0f * n * dnm, h2 = zj - 2.0f * n * dnm;
+      float i1 = rsqrtf(fmaf(h1, h1, dxy2)), i2 = rsqrtf(fmaxf(fmaf(h2, h2, dxy2), 1e-20f));
+      s = fmaf(h.w * h1, (i1 * i1) * i1, s);
+      s = fmaf(h.w * h2, (i2 * i2) * i2, s);
+    }
+  }
+  return s;
+}
+
+__device__ __forceinline__ double z0_tile_f64(const rd_d4* __restrict__ sj, int kmax, double px,
+                                              double py, int nic, double d, double L2) {
+  double s = 0.0;
+  for (int k = 0; k < kmax; ++k) {
+    rd_d4 pj = sj[k];
+    double dx = px - pj.x, dy = py - pj.y, dxy2 = dx * dx + dy * dy;
+    double r = sqrt(dxy2 + pj.z * pj.z) + L2;
+    s += (pj.w * pj.z) / ((r * r) * r);
+    for (int n = 1; n <= nic; ++n) {
+      double h1 = pj.z + (2.0 * n) * d, h2 = pj.z - (2.0 * n) * d;
+      double r1 = sqrt(dxy2 + h1 * h1) + L2, r2 = sqrt(dxy2 + h2 * h2) + L2;
+      s += (pj.w * h1) / ((r1 * r1) * r1);
+      s += (pj.w * h2) / ((r2 * r2) * r2);
+    }
+  }
+  return s;
+}
+
+// Partial F_z sum of the item for a point (px, py) at z = 0, in the units
+// that z0_finish turns into V/m.  Loads the j-tiles into shared memory.
+template <int PREC>
+__device__ __forceinline__ double z0_item_sum(const DiodeParams& p, const Pool& pool, const ItemRef& it,
+                                              double px, double py, float4* sh, float4* sl,
+                                              rd_d4* sj) {
+  const int off = p.off, tid = threadIdx.x;
+  if (PREC == 1) {
+    float pxh, pxl, pyh, pyl;
+    split_nm(px, p.org_x, &pxh, &pxl);
+    split_nm(py, p.org_y, &pyh, &pyl);
+    const float dnm = (float)(p.d * 1.0e9);
+    const int nic = p.image_charge ? p.N_ic_max : 0;
+    float hi = 0.f, lo = 0.f;
+    for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+      __syncthreads();
+      int j = jt + tid;
+      if (j < it.j1) { sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j]; }
+      __syncthreads();
+      two_sum_acc(hi, lo, z0_tile_f32(sh, sl, min(RD_TILE, it.j1 - jt), pxh, pxl, pyh, pyl, nic, dnm));
+    }
+    return (double)hi + (double)lo;
+  } else {
+    const int nic = p.image_charge ? p.N_ic_max : 0;
+    double s = 0.0;
+    for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+      __syncthreads();
+      int j = jt + tid;
+      if (j < it.j1) sj[tid] = make_d4(pool.x[off + j], pool.y[off + j], pool.z[off + j], pool.q[off + j]);
+      __syncthreads();
+      s += z0_tile_f64(sj, min(RD_TILE, it.j1 - jt), px, py, nic, p.d, c_k.L2);
+    }
+    return s;
+  }
+}
+
+// F_z from the summed partials.  Without image charges the x, y cancellation
+// does not hold and the plain Coulomb z term is -z_j only: factor 1 not 2.
+template <int PREC>
+__device__ __forceinline__ double z0_finish(const DiodeParams& p, double s, double kscale) {
+  double f = p.image_charge ? -2.0 : -1.0;
+  if (PREC == 1) return p.E_z + f * kscale * s;
+  return p.E_z + f * c_k.div_fac_c * s;
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(RD_ITILE)
+k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __restrict__ plan,
+            const PlanHeader* __restrict__ ph, const double* __restrict__ qx,
+            const double* __restrict__ qy, double* __restrict__ qF, double* __restrict__ partial,
+            int* __restrict__ tickets, double kscale) {
+  __shared__ float4 sh[RD_TILE], sl[RD_TILE];
+  __shared__ rd_d4 sj[RD_TILE];
+  const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ItemRef it = decode_item(plan, nd, g);
+    const DiodeParams& p = P[it.d];
+    const int m = plan[it.d].n_i, i = it.i0 + tid;
+    const bool valid = i < m;
+    const int qo = p.q_off;
+    double px = valid ? qx[qo + i] : p.em_x0, py = valid ? qy[qo + i] : p.em_y0;
+    double s = z0_item_sum<PREC>(p, pool, it, px, py, sh, sl, sj);
+    if (it.nch > 1) {
+      partial[(size_t)g * RD_ITILE + tid] = s;
+      if (!tile_ticket(tickets, it)) continue;
+      s = 0.0;
+      for (int c = 0; c < it.nch; ++c) s += __ldcg(partial + (size_t)(it.base + c) * RD_ITILE + tid);
+    }
+    if (valid) qF[qo + i] = z0_finish<PREC>(p, s, kscale);
+  }
+}
+
+// ---- supply integrals ------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  const int tid = threadIdx.x;
+  red[tid] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (tid < s) red[tid] += red[tid + s];
+    __syncthreads();
+  }
+  double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ long nint_d(double x) {
+  return (long)(x >= 0 ? floor(x + 0.5) : -floor(-x + 0.5));
+}
+
+// N_sup = sum_k w_k A S(F_k), N_round = nint(N_sup + residual) (planar,
+// Do_Field_Emission_Planar_rectangle :282-285) or nint(N_sup) (tip, :488).
+__global__ void k_supply_reduce(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy,
+                                const double* __restrict__ qx, const double* __restrict__ qy,
+                                const double* __restrict__ qw, const double* __restrict__ qF,
+                                const double* __restrict__ qfx, const double* __restrict__ qfy,
+                                const double* __restrict__ work) {
+  __shared__ double red[256];
+  const int d = blockIdx.x;
+  const DiodeParams& p = P[d];
+  if (!p.active || !p.emission) return;
+  DiodeDyn& y = Dy[d];
+  const int npt = (p.geometry == RD_G_TIP) ? 10000 : p.quad_n * p.quad_n;
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < npt; k += blockDim.x) {
+    double F = qF[p.q_off + k];
+    if (p.geometry == RD_G_TIP) {   // Field_normal :105-112
+      double nx, ny, nz;
+      tip_normal(p, qx[p.q_off + k], qy[p.q_off + k], &nx, &ny, &nz);
+      F = (nx * qfx[p.q_off + k] + ny * qfy[p.q_off + k]) + nz * F;
+    }
+    if (F < 0.0) {
+      if (p.geometry == RD_G_TIP) {
+        double t = fn_t_y(F, p.tip_phi, p.image_charge);   // Elec_Supply (tip) :1710-1718
+        acc += (((qw[p.q_off + k] * c_k.a_FN) * (F * F)) * p.dt) / ((c_k.q0 * p.tip_phi) * (t * t));
+      } else {
+        double phi = work_at(p, work, qx[p.q_off + k], qy[p.q_off + k], nullptr);
+        acc += qw[p.q_off + k] * fn_supply_v2(F, phi, p.image_charge, p.dt);
+      }
+    }
+  }
+  double N_sup = block_sum(acc, red);
+  if (threadIdx.x == 0) {
+    y.N_sup = N_sup;
+    long nr;
+    if (p.geometry == RD_G_TIP) {
+      nr = nint_d(N_sup);
+    } else {
+      nr = nint_d(N_sup + y.residual);
+      y.residual = N_sup - (double)nr;
+    }
+    long M = nr > 0 ? nr : 0;
+    y.chains_capped = M > p.max_chains ? (int)(M - p.max_chains) : 0;
+    y.chains = (int)(M > p.max_chains ? p.max_chains : M);
+    y.chains_failed = 0;
+    y.mh_acc = y.mh_rej = y.mh_done = 0;
+  }
+}
+
+// ---- MH chain initialisation: one warp per chain --------------------------------------
+// Uniform proposals until the field is favourable (F < 0), at most
+// init_rounds rounds (10000 in the reference, :1321-1364 and
+// mod_emission_tip.f90:1292-1318).
+template <int PREC>
+__device__ double warp_field_planar_z0(const DiodeParams& p, const Pool& pool, int n, double px,
+                                       double py, double kscale) {
+  const int lane = threadIdx.x & 31, off = p.off;
+  const int nic = p.image_charge ? p.N_ic_max : 0;
+  double s;
+  if (PREC == 1) {
+    float pxh, pxl, pyh, pyl;
+    split_nm(px, p.org_x, &pxh, &pxl);
+    split_nm(py, p.org_y, &pyh, &pyl);
+    const float dnm = (float)(p.d * 1.0e9);
+    float hi = 0.f, lo = 0.f;
+    for (int j = lane; j < n; j += 32) {
+      float4 h = pool.pk_hi[off + j], l = pool.pk_lo[off + j];
+      two_sum_acc(hi, lo, z0_tile_f32(&h, &l, 1, pxh, pxl, pyh, pyl, nic, dnm));
+    }
+    s = (double)hi + (double)lo;
+  } else {
+    s = 0.0;
+    for (int j = lane; j < n; j += 32) {
+      rd_d4 pj = make_d4(pool.x[off + j], pool.y[off + j], pool.z[off + j], pool.q[off + j]);
+      s += z0_tile_f64(&pj, 1, px, py, nic, p.d, c_k.L2);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return z0_finish<PREC>(p, s, kscale);
+}
+
+template <int PREC>
+__device__ void warp_field_general(const DiodeParams& p, const Pool& pool, int n, double X,
+                                   double Y, double Z, double kscale, double* ex, double* ey,
+                                   double* ez) {
+  const int lane = threadIdx.x & 31, off = p.off;
+  double fx = 0, fy = 0, fz = 0;
+  if (PREC == 1) {
+    float4 ih, il, iih, iil;
+    point_pack(p, X, Y, Z, ih, il, iih, iil);
+    const float dnm = (float)(p.d * 1.0e9);
+    F32Acc acc;
+    acc.zero();
+    for (int j = lane; j < n; j += 32) {
+      float4 h = pool.pk_hi[off + j], l = pool.pk_lo[off + j];
+      float tx = 0.f, ty = 0.f, tz = 0.f;
+      if (p.geometry == RD_G_TIP) {
+        float4 jh = pool.ip_hi[off + j], jl = pool.ip_lo[off + j];
+        tip_tile_f32<T_UPPER>(&h, &l, &jh, &jl, 1, ih, il, iih, iil, -1, p.image_charge,
+                              (float)c_k.tip_K, tx, ty, tz);
+      } else {
+        planar_tile_f32<T_UPPER, false>(&h, &l, 1, ih, il, -1, p.N_ic_max, dnm, p.image_charge, tx, ty, tz);
+      }
+      acc.add(tx, ty, tz);
+    }
+    fx = ((double)acc.hx + (double)acc.lx) * kscale;
+    fy = ((double)acc.hy + (double)acc.ly) * kscale;
+    fz = ((double)acc.hz + (double)acc.lz) * kscale;
+  } else {
+    for (int j = lane; j < n; j += 32) {
+      rd_d4 pj = make_d4(pool.x[off + j], pool.y[off + j], pool.z[off + j], pool.q[off + j]);
+      if (p.geometry == RD_G_TIP)
+        tip_tile_f64<T_UPPER>(&pj, 1, X, Y, Z, c_k.div_fac_c, -1, p.image_charge, p, c_k.L2, c_k.tip_K, fx, fy, fz);
+      else
+        planar_tile_f64<T_UPPER>(&pj, 1, X, Y, Z, c_k.div_fac_c, -1, p.N_ic_max, p.d, p.image_charge, c_k.L2, fx, fy, fz);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    fx += __shfl_xor_sync(0xffffffffu, fx, o);
+    fy += __shfl_xor_sync(0xffffffffu, fy, o);
+    fz += __shfl_xor_sync(0xffffffffu, fz, o);
+  }
+  double vx, vy, vz;
+  vacuum_field(p, X, Y, Z, &vx, &vy, &vz);
+  *ex = vx + fx; *ey = vy + fy; *ez = vz + fz;
+}
+
+__device__ __forceinline__ double tip_target_log(const DiodeParams& p, double F, double xi) {
+  double t = fn_t_y(F, p.tip_phi, p.image_charge);   // Tip_fe_target_log :1213-1219
+  double sup = (((p.dt / c_k.q0) * c_k.a_FN) / ((t * t) * p.tip_phi)) * (F * F);
+  double v = sup > 2.2250738585072014e-308 ? sup : 2.2250738585072014e-308;
+  return log(v) + 0.5 * log(xi * xi - p.eta_1 * p.eta_1);
+}
+
+template <int PREC>
+__global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
+                          const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                          ChainState cs, const int* __restrict__ ch_off, const double* __restrict__ work,
+                          const int* __restrict__ step_ptr, double kscale) {
+  const int nd = ph->n_diodes;
+  const int warps_total = (gridDim.x * blockDim.x) >> 5;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const uint32_t step = (uint32_t)*step_ptr;
+  // chain prefix: plan[d].pad0 holds the first global chain index of diode d
+  int total = nd > 0 ? plan[nd - 1].pad0 + plan[nd - 1].n_i : 0;
+  for (int g = wid; g < total; g += warps_total) {
+    int lo = 0, hi = nd - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (plan[mid].pad0 <= g) lo = mid; else hi = mid - 1; }
+    const int d = lo, c = g - plan[d].pad0;
+    const DiodeParams& p = P[d];
+    const int n = plan[d].n_j, k = ch_off[d] + c;
+    int ok = 0;
+    double F = 1.0, sup = -1.79769313486231570e308, X = 0, Y = 0, Z = 0, xi = 1.0, ph_ = 0.0;
+    for (int r = 0; r < p.init_rounds && !ok; ++r) {
+      double u1, u2;
+      rng2(p.seed, (uint32_t)c, (uint32_t)r, step, RNG_INIT, &u1, &u2);
+      if (p.geometry == RD_G_TIP) {
+        double txi = 1.0 + (p.max_xi - 1.0) * u1, tph = (2.0 * c_k.pi) * u2;
+        double x, y, z, ex, ey, ez, nx, ny, nz;
+        tip_xyz(p, txi, p.eta_1, tph, &x, &y, &z);
+        warp_field_general<PREC>(p, pool, n, x, y, z, kscale, &ex, &ey, &ez);
+        tip_normal(p, x, y, &nx, &ny, &nz);
+        double Fn = (nx * ex + ny * ey) + nz * ez;
+        if (Fn < 0.0) { ok = 1; F = Fn; X = x; Y = y; Z = z; xi = txi; ph_ = tph; sup = tip_target_log(p, Fn, txi); }
+      } else {
+        double x = u1 * p.em_Lx + p.em_x0, y = u2 * p.em_Ly + p.em_y0;
+        double Fz = warp_field_planar_z0<PREC>(p, pool, n, x, y, kscale);
+        if (Fz < 0.0) {
+          ok = 1; F = Fz; X = x; Y = y;
+          sup = fn_supply_log(Fz, work_at(p, work, x, y, nullptr), p.image_charge);
+        }
+      }
+    }
+    if (lane == 0) {
+      if (!ok) {
+        F = 1.0; sup = -1.79769313486231570e308;
+        if (p.geometry == RD_G_TIP) { xi = 1.0; ph_ = 0.0; tip_xyz(p, 1.0, p.eta_1, 0.0, &X, &Y, &Z); }
+        else { X = p.em_x0; Y = p.em_y0; }
+        atomicAdd(&Dy[d].chains_failed, 1);
+      }
+      cs.ok[k] = ok; cs.F[k] = F; cs.sup[k] = sup;
+      if (p.geometry == RD_G_TIP) { cs.x[k] = xi; cs.y[k] = ph_; cs.tx[k] = X; cs.ty[k] = Y; cs.tz[k] = Z; }
+      else { cs.x[k] = X; cs.y[k] = Y; }
+    }
+  }
+}
+
+// ---- MH jump iteration ---------------------------------------------------------------------
+__device__ __forceinline__ void mh_counts_and_update(const DiodeParams& p, DiodeDyn& y, int tiles,
+                                                     int it_idx, int ndim_first, int a, int r,
+                                                     int* red_i) {
+  // block reduce (a, r)
+  const int tid = threadIdx.x;
+  red_i[tid] = a; red_i[RD_ITILE + tid] = r;
+  __syncthreads();
+  for (int s = RD_ITILE / 2; s > 0; s >>= 1) {
+    if (tid < s) { red_i[tid] += red_i[tid + s]; red_i[RD_ITILE + tid] += red_i[RD_ITILE + tid + s]; }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    atomicAdd(&y.mh_acc, red_i[0]);
+    atomicAdd(&y.mh_rej, red_i[RD_ITILE]);
+    __threadfence();
+    int prev = atomicAdd(&y.mh_done, 1);
+    if (prev == tiles - 1) {
+      __threadfence();
+      int A = atomicExch(&y.mh_acc, 0), R = atomicExch(&y.mh_rej, 0);
+      y.mh_done = 0;
+      if (it_idx > ndim_first && A + R > 0) {   // MH_std_update :603-612
+        double rate = (double)A / (double)(A + R);
+        y.a_rate = rate;
+        double s = y.MH_std * exp(0.025 * (rate - 0.35));
+        if (s > p.mh_hi) s = p.mh_hi; else if (s < p.mh_lo) s = p.mh_lo;
+        y.MH_std = s;
+      }
+    }
+  }
+  __syncthreads();
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(RD_ITILE)
+k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
+                 const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                 ChainState cs, const int* __restrict__ ch_off, const double* __restrict__ work,
+                 const int* __restrict__ step_ptr, int it_idx, double* __restrict__ partial,
+                 int* __restrict__ tickets, double kscale) {
+  __shared__ float4 sh[RD_TILE], sl[RD_TILE];
+  __shared__ rd_d4 sj[RD_TILE];
+  __shared__ int red_i[2 * RD_ITILE];
+  const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
+  const uint32_t step = (uint32_t)*step_ptr;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ItemRef it = decode_item(plan, nd, g);
+    const DiodeParams& p = P[it.d];
+    if (p.geometry != RD_G_PLANAR || it_idx > p.mh_jumps) continue;
+    DiodeDyn& y = Dy[it.d];
+    const int M = plan[it.d].n_i, c = it.i0 + tid, k = ch_off[it.d] + c;
+    const bool valid = c < M;
+    const int ok = valid ? cs.ok[k] : 0;
+    const int ndim_first = (int)nint_d(p.mh_jumps * 0.25);
+    // proposal (box_muller + check_limits_metro_rec :1380-1393, :1466-1516)
+    double sx = (it_idx > ndim_first) ? p.em_Lx * y.MH_std : p.em_Lx * 0.10;
+    double sy = (it_idx > ndim_first) ? p.em_Ly * y.MH_std : p.em_Ly * 0.10;
+    double wx = p.em_x0, wy = p.em_y0;
+    if (ok) {
+      double g1, g2;
+      gauss2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, &g1, &g2);
+      wx = g1 * sx + cs.x[k];
+      wy = g2 * sy + cs.y[k];
+      double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+      if (wx > hx) wx = hx - (wx - hx); else if (wx < p.em_x0) wx = (p.em_x0 - wx) + p.em_x0;
+      if (wy > hy) wy = hy - (wy - hy); else if (wy < p.em_y0) wy = (p.em_y0 - wy) + p.em_y0;
+    }
+    double s = z0_item_sum<PREC>(p, pool, it, wx, wy, sh, sl, sj);
+    if (it.nch > 1) {
+      partial[(size_t)g * RD_ITILE + tid] = s;
+      if (!tile_ticket(tickets, it)) continue;
+      s = 0.0;
+      for (int cc = 0; cc < it.nch; ++cc) s += __ldcg(partial + (size_t)(it.base + cc) * RD_ITILE + tid);
+    }
+    // accept / reject (:1400-1443)
+    int a = 0, r = 0;
+    if (ok) {
+      double F = z0_finish<PREC>(p, s, kscale);
+      if (F >= 0.0) {
+        r = 1;
+      } else {
+        double sn = fn_supply_log(F, work_at(p, work, wx, wy, nullptr), p.image_charge);
+        double sc = cs.sup[k];
+        bool take = sn >= sc;
+        if (!take) {
+          double u1, u2;
+          rng2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, &u1, &u2);
+          take = log(u1) <= sn - sc;
+        }
+        if (take) { cs.x[k] = wx; cs.y[k] = wy; cs.sup[k] = sn; cs.F[k] = F; a = 1; }
+        else r = 1;
+      }
+    }
+    mh_counts_and_update(p, y, plan[it.d].tiles, it_idx, ndim_first, a, r, red_i);
+  }
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(RD_ITILE)
+k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
+              const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+              ChainState cs, const int* __restrict__ ch_off, const int* __restrict__ step_ptr,
+              int it_idx, double* __restrict__ partial, int* __restrict__ tickets, double kscale) {
+  __shared__ float4 sh[RD_TILE], sl[RD_TILE], sih[RD_TILE], sil[RD_TILE];
+  __shared__ rd_d4 sj[RD_TILE];
+  __shared__ int red_i[2 * RD_ITILE];
+  const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
+  const uint32_t step = (uint32_t)*step_ptr;
+  const double twopi = 2.0 * c_k.pi;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ItemRef it = decode_item(plan, nd, g);
+    const DiodeParams& p = P[it.d];
+    if (p.geometry != RD_G_TIP || it_idx > p.mh_jumps) continue;
+    DiodeDyn& y = Dy[it.d];
+    const int M = plan[it.d].n_i, c = it.i0 + tid, k = ch_off[it.d] + c;
+    const bool valid = c < M;
+    const int ok = valid ? cs.ok[k] : 0;
+    const int ndim_first = (int)nint_d(p.mh_jumps * 0.25);
+    double sxi = (it_idx > ndim_first) ? (p.max_xi - 1.0) * y.MH_std : (p.max_xi - 1.0) * 0.10;
+    double sph = (it_idx > ndim_first) ? twopi * y.MH_std : twopi * 0.10;
+    // proposal in (xi, phi), Metro_algo_tip_v3 :1334-1350
+    double nxi = 1.5, nph = 0.0;
+    int inside = 0;
+    if (ok) {
+      double g1, g2;
+      gauss2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, &g1, &g2);
+      nxi = cs.x[k] + g1 * sxi;
+      double a = cs.y[k] + g2 * sph;
+      nph = a - floor(a / twopi) * twopi;
+      if (nxi > p.max_xi) nxi = 2.0 * p.max_xi - nxi;
+      if (nxi < 1.0) nxi = 2.0 - nxi;
+      inside = !(nxi < 1.0 || nxi > p.max_xi);
+    }
+    double X, Y, Z;
+    tip_xyz(p, inside ? nxi : 1.5, p.eta_1, nph, &X, &Y, &Z);
+    // field at the proposal (general form, all three components)
+    double fx = 0, fy = 0, fz = 0;
+    const int off = p.off;
+    if (PREC == 1) {
+      float4 ih, il, iih, iil;
+      point_pack(p, X, Y, Z, ih, il, iih, iil);
+      F32Acc acc;
+      acc.zero();
+      for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+        __syncthreads();
+        int j = jt + tid;
+        if (j < it.j1) {
+          sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j];
+          sih[tid] = pool.ip_hi[off + j]; sil[tid] = pool.ip_lo[off + j];
+        }
+        __syncthreads();
+        float tx = 0.f, ty = 0.f, tz = 0.f;
+        tip_tile_f32<T_UPPER>(sh, sl, sih, sil, min(RD_TILE, it.j1 - jt), ih, il, iih, iil, -1,
+                              p.image_charge, (float)c_k.tip_K, tx, ty, tz);
+        acc.add(tx, ty, tz);
+      }
+      fx = ((double)acc.hx + (double)acc.lx) * kscale;
+      fy = ((double)acc.hy + (double)acc.ly) * kscale;
+      fz = ((double)acc.hz + (double)acc.lz) * kscale;
+    } else {
+      for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+        __syncthreads();
+        int j = jt + tid;
+        if (j < it.j1) sj[tid] = make_d4(pool.x[off + j], pool.y[off + j], pool.z[off + j], pool.q[off + j]);
+        __syncthreads();
+        tip_tile_f64<T_UPPER>(sj, min(RD_TILE, it.j1 - jt), X, Y, Z, c_k.div_fac_c, -1,
+                              p.image_charge, p, c_k.L2, c_k.tip_K, fx, fy, fz);
+      }
+    }
+    if (it.nch > 1) {
+      double* pp = partial + (size_t)g * 3 * RD_ITILE;
+      pp[tid] = fx; pp[RD_ITILE + tid] = fy; pp[2 * RD_ITILE + tid] = fz;
+      if (!tile_ticket(tickets, it)) continue;
+      fx = fy = fz = 0.0;
+      for (int cc = 0; cc < it.nch; ++cc) {
+        const double* q = partial + (size_t)(it.base + cc) * 3 * RD_ITILE;
+        fx += __ldcg(q + tid); fy += __ldcg(q + RD_ITILE + tid); fz += __ldcg(q + 2 * RD_ITILE + tid);
+      }
+    }
+    int a = 0, r = 0;
+    if (ok) {
+      if (!inside) {
+        r = 1;
+      } else {
+        double ex, ey, ez, nx, ny, nz;
+        tip_field_E(p, X, Y, Z, &ex, &ey, &ez);
+        ex += fx; ey += fy; ez += fz;
+        tip_normal(p, X, Y, &nx, &ny, &nz);
+        double F = (nx * ex + ny * ey) + nz * ez;
+        if (F >= 0.0) {
+          r = 1;
+        } else {
+          double sn = tip_target_log(p, F, nxi), sc = cs.sup[k];
+          bool take = sn >= sc;
+          if (!take) {
+            double u1, u2;
+            rng2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, &u1, &u2);
+            take = log(u1) <= sn - sc;
+          }
+          if (take) {
+            cs.x[k] = nxi; cs.y[k] = nph; cs.F[k] = F; cs.sup[k] = sn;
+            cs.tx[k] = X; cs.ty[k] = Y; cs.tz[k] = Z;
+            a = 1;
+          } else r = 1;
+        }
+      }
+    }
+    mh_counts_and_update(p, y, plan[it.d].tiles, it_idx, ndim_first, a, r, red_i);
+  }
+}
+
+// ---- emission decisions and stable append ----------------------------------------------------
+// One CTA per emitting diode.  Candidates are tested in chain order
+// (Do_Field_Emission_Planar_rectangle :345-381; Do_Field_Emission_Tip_OLDCODE
+// :504-523) and the emitted electrons are appended in that order with
+// Add_Particle semantics (src/mod_pair.F90:29-159): capacity check with a
+// drop count, q = -q0, m = m0, the Beeman history seeded with (q/m) E_vac.
+__global__ void __launch_bounds__(1024)
+k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, ChainState cs,
+       const int* __restrict__ ch_off, const double* __restrict__ work,
+       const int* __restrict__ step_ptr) {
+  __shared__ int warp_tot[32];
+  __shared__ int s_base;
+  const int d = blockIdx.x;
+  const DiodeParams& p = P[d];
+  if (!p.active || !p.emission) return;
+  DiodeDyn& y = Dy[d];
+  const int step = *step_ptr;
+  const int M = y.chains;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (tid == 0) s_base = 0;
+  __syncthreads();
+  const int n0 = y.n, id0 = y.nrID;
+  int emitted = 0, dropped = 0;
+  for (int c0 = 0; c0 < M; c0 += blockDim.x) {
+    const int c = c0 + tid, k = ch_off[d] + c;
+    int e = 0;
+    double X = 0, Y = 0, Z = 0;
+    int sec = 1;
+    if (c < M) {
+      double u1, u2;
+      rng2(p.seed, (uint32_t)c, 0u, (uint32_t)step, RNG_EMIT, &u1, &u2);
+      const int ok = cs.ok[k];
+      const double F = cs.F[k];
+      if (p.geometry == RD_G_TIP) {
+        double Df = 0.0;
+        if (ok) {
+          double sq = sqrt(p.tip_phi);   // Escape_Prob_Tip :1734-1758
+          Df = exp(((c_k.b_FN * ((sq * sq) * sq)) * fn_v_y(F, p.tip_phi, p.image_charge)) / fabs(F));
+        }
+        if (F < 0.0 && u1 <= Df) {
+          e = 1;
+          double nx, ny, nz;
+          tip_normal(p, cs.tx[k], cs.ty[k], &nx, &ny, &nz);
+          X = cs.tx[k] + nx * c_k.length_scale;
+          Y = cs.ty[k] + ny * c_k.length_scale;
+          Z = cs.tz[k] + nz * c_k.length_scale;
+        }
+      } else {
+        X = cs.x[k]; Y = cs.y[k];
+        double phi = work_at(p, work, X, Y, &sec);
+        double D = ok ? fn_escape_log(F, phi, p.image_charge) : -1.79769313486231570e308;
+        if (F >= 0.0) D = -1.79769313486231570e308;
+        if (log(u1) <= D) { e = 1; Z = 1.0 * c_k.length_scale; }
+      }
+    }
+    // block-wide exclusive scan of e
+    unsigned bal = __ballot_sync(0xffffffffu, e);
+    int wpre = __popc(bal & ((1u << lane) - 1));
+    if (lane == 0) warp_tot[w] = __popc(bal);
+    __syncthreads();
+    int base = 0, tot = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { if (q < w) base += warp_tot[q]; tot += warp_tot[q]; }
+    const int slot = s_base + base + wpre;   // emitted so far in chain order
+    if (e) {
+      int i = n0 + slot;
+      if (i < p.cap) {
+        int gi = p.off + i;
+        double qm = (-1.0 * c_k.q0) / (1.0 * c_k.m0), ex, ey, ez;
+        vacuum_field(p, X, Y, Z, &ex, &ey, &ez);
+        pool.x[gi] = X; pool.y[gi] = Y; pool.z[gi] = Z;
+        pool.vx[gi] = 0.0; pool.vy[gi] = 0.0; pool.vz[gi] = 0.0;
+        pool.ax[gi] = pool.bx[gi] = pool.cx[gi] = qm * ex;
+        pool.ay[gi] = pool.by[gi] = pool.cy[gi] = qm * ey;
+        pool.az[gi] = pool.bz[gi] = pool.cz[gi] = qm * ez;
+        pool.q[gi] = -1.0 * c_k.q0;
+        pool.m[gi] = 1.0 * c_k.m0;
+        pool.species[gi] = 1;
+        pool.id[gi] = id0 + slot;
+        pool.step0[gi] = step;
+        pool.section[gi] = sec;
+        pool.mask[gi] = 1;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) s_base += tot;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    int tot = s_base;
+    int room = p.cap - n0;
+    emitted = tot < room ? tot : (room > 0 ? room : 0);
+    dropped = tot - emitted;
+    y.n = n0 + emitted;
+    y.nrID = id0 + emitted;
+    y.emitted_step = emitted;
+    y.dropped_step = dropped;
+    y.emitted_total += emitted;
+    y.dropped_total += dropped;
+  }
+}
+
+}  // namespace
+
+// ---- launch wrappers --------------------------------------------------------------------------
+cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st,
+                                   const DiodeParams* P, const Pool& pool, const PlanEntry* plan,
+                                   const PlanHeader* ph, const PointSet& pts, double* partial,
+                                   int* tickets, double kscale) {
+  if (prec == 1) {
+    if (geom == RD_G_TIP) k_field_points<1, RD_G_TIP><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
+    else k_field_points<1, RD_G_PLANAR><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
+  } else {
+    if (geom == RD_G_TIP) k_field_points<0, RD_G_TIP><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
+    else k_field_points<0, RD_G_PLANAR><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const DiodeParams* P,
+                                const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
+                                const double* qx, const double* qy, double* qF, double* partial,
+                                int* tickets, double kscale) {
+  if (prec == 1) k_z0_points<1><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, qx, qy, qF, partial, tickets, kscale);
+  else k_z0_points<0><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, qx, qy, qF, partial, tickets, kscale);
+  return cudaGetLastError();
+}
+
+cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                                    const double* qx, const double* qy, const double* qw,
+                                    const double* qF, const double* qfx, const double* qfy,
+                                    const double* work) {
+  k_supply_reduce<<<nslots, 256, 0, st>>>(P, Dy, qx, qy, qw, qF, qfx, qfy, work);
+  return cudaGetLastError();
+}
+
+cudaError_t rd_launch_mh_init(int prec, int grid, cudaStream_t st, const DiodeParams* P,
+                              DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
+                              const PlanHeader* ph, const ChainState& cs, const int* ch_off,
+                              const double* work, const int* step_ptr, double kscale) {
+  if (prec == 1) k_mh_init<1><<<grid, 256, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, work, step_ptr, kscale);
+  else k_mh_init<0><<<grid, 256, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, work, step_ptr, kscale);
+  return cudaGetLastError();
+}
+
+cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_t st,
+                              const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
+                              const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
+                              const int* ch_off, const double* work, const int* step_ptr,
+                              int it_idx, double* partial, int* tickets, double kscale) {
+  if (geometry_mask & 1) {
+    if (prec == 1) k_mh_jump_planar<1><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, work, step_ptr, it_idx, partial, tickets, kscale);
+    else k_mh_jump_planar<0><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, work, step_ptr, it_idx, partial, tickets, kscale);
+  }
+  if (geometry_mask & 2) {
+    if (prec == 1) k_mh_jump_tip<1><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale);
+    else k_mh_jump_tip<0><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                           const Pool& pool, const ChainState& cs, const int* ch_off,
+                           const double* work, const int* step_ptr) {
+  k_emit<<<nslots, 1024, 0, st>>>(P, Dy, pool, cs, ch_off, work, step_ptr);
+  return cudaGetLastError();
+}
+
+RD_DEFINE_CONSTANT_UPLOAD(field)

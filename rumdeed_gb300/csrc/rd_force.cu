@@ -1,0 +1,281 @@
+// rd_force.cu -- all-pairs acceleration kernels (Calculate_Acceleration_Particles).
+//
+// Semantics follow the gather form of the reference,
+// Calculate_Acceleration_Particles_ACC (src/mod_verlet.F90:1217-1429):
+//   a_i = (1/m_i) [ sum_{j != i} q_i q_j k ( d_ij/(|d_ij| + l^2)^3 + IC_ij ) + q_i E_vac(x_i) ]
+// with the image term IC_ij of the pair always evaluated with the
+// lower-indexed particle in the "a" role and mirrored in x and y for the
+// higher-indexed one (:1303-1323, :1372-1402).
+//
+// Two precisions:
+//  * FP64 ("plain"): the reference's arithmetic in SI units.
+//  * FP32 compensated: positions as (hi, lo) float pairs in nm, rsqrt and
+//    per-j-tile float accumulation, tile sums folded into (hi, lo) pairs with
+//    two-sum, the final sum and all prefactors in FP64.  The image partner
+//    heights are formed from sums of absolute heights (z_a + z_b, or the
+//    anode distances) so terms do not cancel next to the electrodes.
+//
+// Tiles are aligned (i0 and j0 multiples of RD_TILE), so a j-tile is either
+// entirely above the i-tile (all j > i), entirely below, or the diagonal
+// tile; the role selection and the self-exclusion are per pair only on the
+// diagonal tile.
+#include "rd_tiles.cuh"
+
+namespace {
+
+template <bool NIC0>
+__global__ void __launch_bounds__(RD_ITILE)
+k_force_planar_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
+                   const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                   double* __restrict__ partial, int* __restrict__ tickets, double kscale) {
+  __shared__ float4 sh[RD_TILE], sl[RD_TILE];
+  const int total = ph->total_items, nd = ph->n_diodes;
+  const int tid = threadIdx.x;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ItemRef it = decode_item(plan, nd, g);
+    const DiodeParams& p = P[it.d];
+    const int off = p.off, n = plan[it.d].n_i;
+    const int i = it.i0 + tid;
+    const bool valid = i < n;
+    float4 ih = valid ? pool.pk_hi[off + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 il = valid ? pool.pk_lo[off + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float dnm = (float)(p.d * 1.0e9);
+    const int nic = p.N_ic_max, ic = p.image_charge;
+    F32Acc acc;
+    acc.zero();
+    for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+      __syncthreads();
+      int j = jt + tid;
+      if (j < it.j1) { sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j]; }
+      __syncthreads();
+      int kmax = min(RD_TILE, it.j1 - jt);
+      float tx = 0.f, ty = 0.f, tz = 0.f;
+      if (jt == it.i0)
+        planar_tile_f32<T_DIAG, NIC0>(sh, sl, kmax, ih, il, tid, nic, dnm, ic, tx, ty, tz);
+      else if (jt > it.i0)
+        planar_tile_f32<T_UPPER, NIC0>(sh, sl, kmax, ih, il, -1, nic, dnm, ic, tx, ty, tz);
+      else
+        planar_tile_f32<T_LOWER, NIC0>(sh, sl, kmax, ih, il, -1, nic, dnm, ic, tx, ty, tz);
+      acc.add(tx, ty, tz);
+    }
+    double fx = (double)acc.hx + (double)acc.lx;
+    double fy = (double)acc.hy + (double)acc.ly;
+    double fz = (double)acc.hz + (double)acc.lz;
+    if (it.nch > 1) {
+      double* pp = partial + (size_t)g * 3 * RD_ITILE;
+      pp[tid] = fx; pp[RD_ITILE + tid] = fy; pp[2 * RD_ITILE + tid] = fz;
+      if (!tile_ticket(tickets, it)) continue;
+      fx = fy = fz = 0.0;
+      for (int c = 0; c < it.nch; ++c) {
+        const double* q = partial + (size_t)(it.base + c) * 3 * RD_ITILE;
+        fx += __ldcg(q + tid); fy += __ldcg(q + RD_ITILE + tid); fz += __ldcg(q + 2 * RD_ITILE + tid);
+      }
+    }
+    if (valid) {
+      // a_i = (q_i k e^2 1e18 / m_i) * sum + q_i E_vac / m_i   (nm -> m: 1e18)
+      const int gi = off + i;
+      double qi = pool.q[gi], im = 1.0 / pool.m[gi];
+      double pre = (qi * kscale) * im;   // kscale = k * q0 * 1e18 (per unit q_j/q0)
+      pool.ax[gi] = pre * fx;
+      pool.ay[gi] = pre * fy;
+      pool.az[gi] = pre * fz + qi * p.E_z * im;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(RD_ITILE)
+k_force_planar_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
+                   const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                   double* __restrict__ partial, int* __restrict__ tickets) {
+  __shared__ rd_d4 sj[RD_TILE];
+  const int total = ph->total_items, nd = ph->n_diodes;
+  const int tid = threadIdx.x;
+  const double L2 = c_k.L2, dfc = c_k.div_fac_c;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ItemRef it = decode_item(plan, nd, g);
+    const DiodeParams& p = P[it.d];
+    const int off = p.off, n = plan[it.d].n_i;
+    const int i = it.i0 + tid;
+    const bool valid = i < n;
+    double x1 = 0, y1 = 0, z1 = 0, q1 = 0;
+    if (valid) { x1 = pool.x[off + i]; y1 = pool.y[off + i]; z1 = pool.z[off + i]; q1 = pool.q[off + i]; }
+    const double qd1 = q1 * dfc;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+      __syncthreads();
+      int j = jt + tid;
+      if (j < it.j1) sj[tid] = make_d4(pool.x[off + j], pool.y[off + j], pool.z[off + j], pool.q[off + j]);
+      __syncthreads();
+      int kmax = min(RD_TILE, it.j1 - jt);
+      if (jt == it.i0)
+        planar_tile_f64<T_DIAG>(sj, kmax, x1, y1, z1, qd1, tid, p.N_ic_max, p.d, p.image_charge, L2, ax, ay, az);
+      else if (jt > it.i0)
+        planar_tile_f64<T_UPPER>(sj, kmax, x1, y1, z1, qd1, -1, p.N_ic_max, p.d, p.image_charge, L2, ax, ay, az);
+      else
+        planar_tile_f64<T_LOWER>(sj, kmax, x1, y1, z1, qd1, -1, p.N_ic_max, p.d, p.image_charge, L2, ax, ay, az);
+    }
+    if (it.nch > 1) {
+      double* pp = partial + (size_t)g * 3 * RD_ITILE;
+      pp[tid] = ax; pp[RD_ITILE + tid] = ay; pp[2 * RD_ITILE + tid] = az;
+      if (!tile_ticket(tickets, it)) continue;
+      ax = ay = az = 0.0;
+      for (int c = 0; c < it.nch; ++c) {
+        const double* q = partial + (size_t)(it.base + c) * 3 * RD_ITILE;
+        ax += __ldcg(q + tid); ay += __ldcg(q + RD_ITILE + tid); az += __ldcg(q + 2 * RD_ITILE + tid);
+      }
+    }
+    if (valid) {
+      const int gi = off + i;
+      double im = 1.0 / pool.m[gi];
+      pool.ax[gi] = ax * im;
+      pool.ay[gi] = ay * im;
+      pool.az[gi] = (az + q1 * p.E_z) * im;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(RD_ITILE)
+k_force_tip_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
+                const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                double* __restrict__ partial, int* __restrict__ tickets, double kscale) {
+  __shared__ float4 sh[RD_TILE], sl[RD_TILE], sih[RD_TILE], sil[RD_TILE];
+  const int total = ph->total_items, nd = ph->n_diodes;
+  const int tid = threadIdx.x;
+  const float K = (float)c_k.tip_K;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ItemRef it = decode_item(plan, nd, g);
+    const DiodeParams& p = P[it.d];
+    const int off = p.off, n = plan[it.d].n_i;
+    const int i = it.i0 + tid;
+    const bool valid = i < n;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 ih = valid ? pool.pk_hi[off + i] : z4, il = valid ? pool.pk_lo[off + i] : z4;
+    float4 iih = valid ? pool.ip_hi[off + i] : z4, iil = valid ? pool.ip_lo[off + i] : z4;
+    F32Acc acc;
+    acc.zero();
+    for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+      __syncthreads();
+      int j = jt + tid;
+      if (j < it.j1) {
+        sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j];
+        sih[tid] = pool.ip_hi[off + j]; sil[tid] = pool.ip_lo[off + j];
+      }
+      __syncthreads();
+      int kmax = min(RD_TILE, it.j1 - jt);
+      float tx = 0.f, ty = 0.f, tz = 0.f;
+      if (jt == it.i0)
+        tip_tile_f32<T_DIAG>(sh, sl, sih, sil, kmax, ih, il, iih, iil, tid, p.image_charge, K, tx, ty, tz);
+      else if (jt > it.i0)
+        tip_tile_f32<T_UPPER>(sh, sl, sih, sil, kmax, ih, il, iih, iil, -1, p.image_charge, K, tx, ty, tz);
+      else
+        tip_tile_f32<T_LOWER>(sh, sl, sih, sil, kmax, ih, il, iih, iil, -1, p.image_charge, K, tx, ty, tz);
+      acc.add(tx, ty, tz);
+    }
+    double fx = (double)acc.hx + (double)acc.lx;
+    double fy = (double)acc.hy + (double)acc.ly;
+    double fz = (double)acc.hz + (double)acc.lz;
+    if (it.nch > 1) {
+      double* pp = partial + (size_t)g * 3 * RD_ITILE;
+      pp[tid] = fx; pp[RD_ITILE + tid] = fy; pp[2 * RD_ITILE + tid] = fz;
+      if (!tile_ticket(tickets, it)) continue;
+      fx = fy = fz = 0.0;
+      for (int c = 0; c < it.nch; ++c) {
+        const double* q = partial + (size_t)(it.base + c) * 3 * RD_ITILE;
+        fx += __ldcg(q + tid); fy += __ldcg(q + RD_ITILE + tid); fz += __ldcg(q + 2 * RD_ITILE + tid);
+      }
+    }
+    if (valid) {
+      const int gi = off + i;
+      double qi = pool.q[gi], im = 1.0 / pool.m[gi];
+      double pre = (qi * kscale) * im;
+      double ex, ey, ez;
+      tip_field_E(p, pool.x[gi], pool.y[gi], pool.z[gi], &ex, &ey, &ez);
+      pool.ax[gi] = pre * fx + qi * ex * im;
+      pool.ay[gi] = pre * fy + qi * ey * im;
+      pool.az[gi] = pre * fz + qi * ez * im;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(RD_ITILE)
+k_force_tip_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
+                const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                double* __restrict__ partial, int* __restrict__ tickets) {
+  __shared__ rd_d4 sj[RD_TILE];
+  const int total = ph->total_items, nd = ph->n_diodes;
+  const int tid = threadIdx.x;
+  const double L2 = c_k.L2, dfc = c_k.div_fac_c, K = c_k.tip_K;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ItemRef it = decode_item(plan, nd, g);
+    const DiodeParams& p = P[it.d];
+    const int off = p.off, n = plan[it.d].n_i;
+    const int i = it.i0 + tid;
+    const bool valid = i < n;
+    double x1 = 0, y1 = 0, z1 = 0, q1 = 0;
+    if (valid) { x1 = pool.x[off + i]; y1 = pool.y[off + i]; z1 = pool.z[off + i]; q1 = pool.q[off + i]; }
+    const double qd1 = q1 * dfc;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+      __syncthreads();
+      int j = jt + tid;
+      if (j < it.j1) sj[tid] = make_d4(pool.x[off + j], pool.y[off + j], pool.z[off + j], pool.q[off + j]);
+      __syncthreads();
+      int kmax = min(RD_TILE, it.j1 - jt);
+      if (jt == it.i0)
+        tip_tile_f64<T_DIAG>(sj, kmax, x1, y1, z1, qd1, tid, p.image_charge, p, L2, K, ax, ay, az);
+      else if (jt > it.i0)
+        tip_tile_f64<T_UPPER>(sj, kmax, x1, y1, z1, qd1, -1, p.image_charge, p, L2, K, ax, ay, az);
+      else
+        tip_tile_f64<T_LOWER>(sj, kmax, x1, y1, z1, qd1, -1, p.image_charge, p, L2, K, ax, ay, az);
+    }
+    if (it.nch > 1) {
+      double* pp = partial + (size_t)g * 3 * RD_ITILE;
+      pp[tid] = ax; pp[RD_ITILE + tid] = ay; pp[2 * RD_ITILE + tid] = az;
+      if (!tile_ticket(tickets, it)) continue;
+      ax = ay = az = 0.0;
+      for (int c = 0; c < it.nch; ++c) {
+        const double* q = partial + (size_t)(it.base + c) * 3 * RD_ITILE;
+        ax += __ldcg(q + tid); ay += __ldcg(q + RD_ITILE + tid); az += __ldcg(q + 2 * RD_ITILE + tid);
+      }
+    }
+    if (valid) {
+      const int gi = off + i;
+      double im = 1.0 / pool.m[gi];
+      double ex, ey, ez;
+      tip_field_E(p, x1, y1, z1, &ex, &ey, &ez);
+      pool.ax[gi] = (ax + q1 * ex) * im;
+      pool.ay[gi] = (ay + q1 * ey) * im;
+      pool.az[gi] = (az + q1 * ez) * im;
+    }
+  }
+}
+
+}  // namespace
+
+// Launch wrappers (called by the engine).
+cudaError_t rd_launch_force(int prec, int geometry_mask, int nic_general, int grid,
+                            cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy,
+                            const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
+                            double* partial, int* tickets, double kscale) {
+  // geometry_mask: bit0 planar diodes present, bit1 tip diodes present.  The
+  // planar and tip kernels each skip items of the other geometry through the
+  // plan (separate plans per geometry are built by the engine).
+  if (prec == 0) {
+    if (geometry_mask & 1)
+      k_force_planar_f64<<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets);
+    else
+      k_force_tip_f64<<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets);
+  } else {
+    if (geometry_mask & 1) {
+      if (nic_general)
+        k_force_planar_f32<false><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale);
+      else
+        k_force_planar_f32<true><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale);
+    } else {
+      k_force_tip_f32<<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale);
+    }
+  }
+  return cudaGetLastError();
+}
+
+RD_DEFINE_CONSTANT_UPLOAD(force)

@@ -1,0 +1,111 @@
+// rd_internal.h -- data model shared by the host engine and the sm_103a
+// kernels of librumdeed_gb300.
+//
+// Layout in HBM.  All diodes of an engine share one particle pool; diode d
+// owns the slots [off_d, off_d + cap_d) of every pool array (off_d is a
+// multiple of 32).  The pool is struct-of-arrays so that every kernel reads
+// each field with coalesced loads:
+//   FP64 state  : pos x/y/z, vel x/y/z, acc (cur, prev, prev2) x/y/z, charge, mass
+//   int state   : species, id, step created, section, mask
+//   FP32 packs  : pk_hi = (x, y, z, q/q0) and pk_lo = (x, y, z, 0) as the high
+//                 and low float parts of the position in nm (x, y relative to
+//                 the diode's lateral origin, z absolute from the cathode);
+//                 tip diodes add the sphere image point of each particle in
+//                 the same hi/lo form (ip_hi, ip_lo).
+// The segment table (DiodeParams, static per admission; DiodeDyn, dynamic
+// counters) lives in device memory, so a captured step graph stays valid
+// while requests are admitted and retired.
+#pragma once
+#include <stdint.h>
+
+#define RD_TILE 128           // particles per shared-memory j-tile
+#define RD_ITILE 128          // i-particles (or points) per work item
+#define RD_MAX_LIFE 1000
+#define RD_MAX_WORK 4096      // max checkerboard cells per diode (64x64)
+
+enum { RD_G_PLANAR = 1, RD_G_TIP = 2 };
+
+// 32-byte aligned quadruple of doubles (one particle of an FP64 j-tile).
+struct __align__(32) rd_d4 { double x, y, z, w; };
+#ifdef __CUDACC__
+__host__ __device__ inline rd_d4 make_d4(double x, double y, double z, double w) {
+  rd_d4 r; r.x = x; r.y = y; r.z = z; r.w = w; return r;
+}
+#endif
+
+struct RdConst {
+  double pi, q0, m0, eps0, hbar, div_fac_c, a_FN, b_FN, l_const, L2, tip_K, m_N2, m_N2p;
+  double length_scale;
+};
+
+// Static parameters of one diode slot.
+struct DiodeParams {
+  int active;            // 1 while the slot holds a simulation
+  int geometry;          // RD_G_PLANAR / RD_G_TIP
+  int cap, off;          // capacity and pool offset
+  int image_charge, N_ic_max;
+  int emission;          // 0 off, 1 field emission
+  int mh_jumps, max_chains, init_rounds;
+  int quad_n;            // supply quadrature points per dimension (planar)
+  int q_off;             // offset of this diode's quadrature points in the quad table
+  int work_nx, work_ny, work_off;
+  int pad0;
+  unsigned long long seed;
+  double V, d, E_z, dt, dt2;
+  double em_x0, em_y0, em_Lx, em_Ly;
+  double org_x, org_y;   // lateral origin of the FP32 frame (m)
+  // hyperboloid tip (mod_hyperboloid_tip)
+  double a_foci, eta_1, max_xi, shift_z, r_tip, h_tip, pre_E, pre_E_unit, tip_phi;
+  double mh_lo, mh_hi;   // MH_std clamps
+};
+
+// Dynamic per-diode state (device resident, updated by kernels).
+struct DiodeDyn {
+  int n;                 // particles in flight
+  int nrID;
+  int n_remove, n_remove_top, n_remove_bot;
+  int first_dead;
+  int emitted_step, dropped_step;
+  int chains, chains_failed, chains_capped;
+  int mh_acc, mh_rej, mh_done;   // per-jump counters (reset by the last arriver)
+  int sup_done;
+  int absorbed_top_step, absorbed_bot_step;
+  int pad;
+  long long emitted_total, absorbed_top_total, absorbed_bot_total, dropped_total;
+  long long electron_steps;      // sum over steps of particles in flight
+  long long steps_done;
+  double ramo_current;
+  double MH_std, a_rate, residual, N_sup;
+  double avg_vel[3];
+};
+
+// Particle pool (device pointers).
+struct Pool {
+  double *x, *y, *z, *vx, *vy, *vz;
+  double *ax, *ay, *az, *bx, *by, *bz, *cx, *cy, *cz;   // acc cur / prev / prev2
+  double *q, *m;
+  int *species, *id, *step0, *section, *mask;
+  float4 *pk_hi, *pk_lo, *ip_hi, *ip_lo;
+};
+
+// One unit of a pair-sum: i-tile (or point block) x j-chunk of one diode.
+struct WorkItem {
+  int diode;
+  int i0;        // first i (particle or point) of the tile
+  int j0, j1;    // particle range of the chunk
+  int tile;      // index of the tile among the diode's tiles (partials)
+  int chunk, nchunks;
+  int slot;      // global tile slot for partial / counter storage
+};
+
+// MH chain state (per diode, chains at [choff_d, choff_d + max_chains)).
+struct ChainState {
+  double *x, *y;         // planar: position; tip: xi, phi
+  double *F, *sup, *df;  // field (z or normal), log target, escape (log for planar)
+  double *px, *py;       // proposal
+  double *pF;            // proposal field
+  int *ok;
+  double *tx, *ty, *tz;  // tip: cartesian position of the current state
+  double *pxx, *pyy, *pzz;  // tip: cartesian position of the proposal
+  int *prop_ok;          // proposal inside the domain
+};

@@ -1,0 +1,82 @@
+// rd_pair.cuh -- the pair-sum engine shared by the force, field and
+// Metropolis-Hastings kernels.
+//
+// A pair sum (particles or surface points i against the particles j of the
+// same diode) is cut into work items: an i-tile of RD_ITILE consecutive i
+// times a j-chunk of consecutive particles.  A plan (one entry per diode,
+// built on the device from the particle counts) says how many tiles and
+// chunks each diode has; persistent CTAs walk the item index space
+// round-robin and decode (diode, tile, chunk) by binary search.  When a tile
+// has more than one chunk, each chunk stores its partial sums in scratch and
+// the last chunk to finish (an atomic ticket, no waiting) adds the partials
+// in chunk order, so results do not depend on scheduling.
+#pragma once
+#include "rd_device.cuh"
+
+struct PlanEntry {
+  int item_off;   // first item of this diode
+  int tiles;      // i-tiles
+  int nch;        // j-chunks per tile
+  int clen;       // j-chunk length (multiple of RD_TILE)
+  int n_i;        // number of i (particles or points)
+  int n_j;        // number of j particles
+  int pad0;       // MH plans: first global chain index of the diode
+  int tsize;      // i-tile width (RD_ITILE for pair sums, 1024 for compaction)
+};
+
+struct PlanHeader {
+  int total_items;
+  int n_diodes;    // entries in the plan
+  int pad[2];
+};
+
+struct ItemRef {
+  int d;        // plan entry (== diode slot)
+  int tile, chunk, nch;
+  int i0, j0, j1;
+  int base;     // item index of chunk 0 of this tile (partial / ticket slot)
+};
+
+__device__ __forceinline__ ItemRef decode_item(const PlanEntry* plan, int nd, int g) {
+  int lo = 0, hi = nd - 1;
+  while (lo < hi) {   // last entry with item_off <= g
+    int mid = (lo + hi + 1) >> 1;
+    if (plan[mid].item_off <= g) lo = mid; else hi = mid - 1;
+  }
+  const PlanEntry& e = plan[lo];
+  ItemRef r;
+  r.d = lo;
+  int local = g - e.item_off;
+  r.tile = local / e.nch;
+  r.chunk = local - r.tile * e.nch;
+  r.nch = e.nch;
+  r.i0 = r.tile * e.tsize;
+  r.j0 = r.chunk * e.clen;
+  r.j1 = min(r.j0 + e.clen, e.n_j);
+  r.base = e.item_off + r.tile * e.nch;
+  return r;
+}
+
+// Stores this CTA's partials, then returns true in the CTA that completed
+// the tile (all chunks stored).  ncomp doubles per i, layout
+// partial[(item * ncomp + c) * RD_ITILE + tid].
+__device__ __forceinline__ bool tile_ticket(int* tickets, const ItemRef& it) {
+  __shared__ int s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int prev = atomicAdd(&tickets[it.base], 1);
+    s_last = (prev == it.nch - 1);
+    if (s_last) tickets[it.base] = 0;   // reset for the next launch
+  }
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last != 0;
+}
+
+// Points of a field evaluation: per-diode lists at [off[d], off[d] + n_d).
+struct PointSet {   // per-diode point lists at [pt_off_d, pt_off_d + n_d)
+  const double *x, *y, *z;
+  double *fx, *fy, *fz;
+  const int* off;   // per diode slot
+};

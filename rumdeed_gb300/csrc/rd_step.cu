@@ -1,0 +1,491 @@
+// rd_step.cu -- per-particle kernels of the time step and the work planner.
+//
+//  * k_plan: builds the pair-sum plan (rd_pair.cuh) on the device from the
+//    particle / point / chain counts, so a captured step graph adapts to the
+//    counts of every step without host involvement.
+//  * k_pack: FP32 (hi, lo) position packs, anode distances and, for tips,
+//    the apex-sphere image point of every particle.
+//  * k_position: Beeman position update, history shift, boundary checks and
+//    removal marking (Update_ElecIon_Position, src/mod_verlet.F90:197-232;
+//    Check_Boundary_Planar :325-338; Check_Boundary_Tip,
+//    src/mod_emission_tip.f90:1627-1647; Mark_Particles_Remove,
+//    src/mod_pair.F90:169-339), fused with the pack.
+//  * k_velocity + k_ramo: Beeman velocity update and the Ramo current
+//    (Update_ElecIon_Velocity, src/mod_verlet.F90:449-509), reduced per diode
+//    in a fixed order.
+//  * k_compact_*: stable, order-preserving compaction from the first dead
+//    index (Remove_Particles :352-562, compact_array :1180-1223) with the
+//    life-time histogram (record_lifetime :1135-1160).
+#include "rd_pair.cuh"
+
+enum { PM_FORCE_PLANAR = 0, PM_FORCE_TIP = 1, PM_FIELD = 2, PM_SUPPLY_PLANAR = 3,
+       PM_SUPPLY_TIP = 4, PM_MH = 5, PM_PART = 6, PM_PART1024 = 7 };
+
+namespace {
+
+__device__ __forceinline__ void mark_remove(const DiodeParams& p, DiodeDyn& y, Pool& pool, int i,
+                                            int gi, int why) {
+  if (!pool.mask[gi]) return;
+  pool.mask[gi] = 0;
+  pool.q[gi] = 0.0;   // a marked particle no longer acts on others (:206-207)
+  atomicAdd(&y.n_remove, 1);
+  atomicMin(&y.first_dead, i);
+  if (pool.species[gi] == 1) {
+    if (why == 1) atomicAdd(&y.n_remove_top, 1);
+    else atomicAdd(&y.n_remove_bot, 1);
+  }
+}
+
+__device__ __forceinline__ void pack_one(const DiodeParams& p, const Pool& pool, int gi) {
+  double x = pool.x[gi], y = pool.y[gi], z = pool.z[gi];
+  float4 h, l;
+  split_nm(x, p.org_x, &h.x, &l.x);
+  split_nm(y, p.org_y, &h.y, &l.y);
+  split_nm(z, 0.0, &h.z, &l.z);
+  h.w = (float)(pool.q[gi] / c_k.q0);
+  l.w = (float)((p.d - z) * 1.0e9);
+  pool.pk_hi[gi] = h;
+  pool.pk_lo[gi] = l;
+  if (p.geometry == RD_G_TIP) {
+    double xi, yi, zi;
+    double dis = tip_image_point(p, x, y, z, &xi, &yi, &zi);
+    float4 a, b;
+    split_nm(xi, p.org_x, &a.x, &b.x);
+    split_nm(yi, p.org_y, &a.y, &b.y);
+    split_nm(zi, 0.0, &a.z, &b.z);
+    a.w = (float)(p.r_tip / dis);
+    b.w = 0.f;
+    pool.ip_hi[gi] = a;
+    pool.ip_lo[gi] = b;
+  }
+}
+
+// ---- planner --------------------------------------------------------------------
+__global__ void __launch_bounds__(1024)
+k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int nslots, int mode,
+       int target_items, int max_items, const int* __restrict__ npts, PlanEntry* __restrict__ plan,
+       PlanHeader* __restrict__ ph) {
+  __shared__ double red[1024];
+  __shared__ int s_items[32], s_chains[32];
+  const int tid = threadIdx.x;
+  const int tsize = (mode == PM_PART1024) ? 1024 : RD_ITILE;
+  const bool pair = (mode <= PM_MH);
+  // pass 1: total pair work
+  double work = 0.0;
+  for (int d = tid; d < nslots; d += blockDim.x) {
+    const DiodeParams& p = P[d];
+    if (!p.active) continue;
+    int ni = 0, nj = Dy[d].n;
+    switch (mode) {
+      case PM_FORCE_PLANAR: ni = p.geometry == RD_G_PLANAR ? nj : 0; break;
+      case PM_FORCE_TIP: ni = p.geometry == RD_G_TIP ? nj : 0; break;
+      case PM_FIELD: ni = npts[d]; break;
+      case PM_SUPPLY_PLANAR: ni = (p.emission && p.geometry == RD_G_PLANAR) ? p.quad_n * p.quad_n : 0; break;
+      case PM_SUPPLY_TIP: ni = (p.emission && p.geometry == RD_G_TIP) ? 10000 : 0; break;
+      case PM_MH: ni = p.emission ? Dy[d].chains : 0; break;
+      default: ni = nj; break;
+    }
+    work += (double)ni * (double)(nj > RD_TILE ? nj : RD_TILE);
+  }
+  red[tid] = work;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (tid < s) red[tid] += red[tid + s];
+    __syncthreads();
+  }
+  const double total_work = red[0];
+  double per_item = total_work / (double)(target_items > 0 ? target_items : 1);
+  // pass 2: entries, serial prefix in chunks of blockDim
+  __shared__ int s_run_items, s_run_chains;
+  if (tid == 0) { s_run_items = 0; s_run_chains = 0; }
+  __syncthreads();
+  for (int base = 0; base < nslots; base += blockDim.x) {
+    int d = base + tid;
+    int items = 0, ni = 0, nj = 0, tiles = 0, nch = 1, clen = RD_TILE, chains = 0;
+    if (d < nslots) {
+      const DiodeParams& p = P[d];
+      if (p.active) {
+        nj = Dy[d].n;
+        switch (mode) {
+          case PM_FORCE_PLANAR: ni = p.geometry == RD_G_PLANAR ? nj : 0; break;
+          case PM_FORCE_TIP: ni = p.geometry == RD_G_TIP ? nj : 0; break;
+          case PM_FIELD: ni = npts[d]; break;
+          case PM_SUPPLY_PLANAR: ni = (p.emission && p.geometry == RD_G_PLANAR) ? p.quad_n * p.quad_n : 0; break;
+          case PM_SUPPLY_TIP: ni = (p.emission && p.geometry == RD_G_TIP) ? 10000 : 0; break;
+          case PM_MH: ni = p.emission ? Dy[d].chains : 0; chains = ni; break;
+          default: ni = nj; break;
+        }
+        tiles = (ni + tsize - 1) / tsize;
+        if (pair && tiles > 0) {
+          int njr = ((nj + RD_TILE - 1) / RD_TILE) * RD_TILE;
+          if (njr < RD_TILE) njr = RD_TILE;
+          double want = per_item / (double)RD_ITILE;            // j per item
+          int c = (int)fmin((double)njr, fmax((double)RD_TILE, want));
+          c = ((c + RD_TILE - 1) / RD_TILE) * RD_TILE;
+          // keep the item count within the scratch budget
+          long long maxc = (long long)max_items / (tiles > 0 ? tiles : 1);
+          if (maxc < 1) maxc = 1;
+          while ((long long)((nj + c - 1) / c) > maxc) c *= 2;
+          clen = c;
+          nch = nj > 0 ? (nj + c - 1) / c : 1;
+        }
+        items = tiles * nch;
+      }
+    }
+    // block scan of items and chains
+    int lane = tid & 31, w = tid >> 5;
+    int vi = items, vc = chains;
+    for (int o = 1; o < 32; o <<= 1) {
+      int a = __shfl_up_sync(0xffffffffu, vi, o), b = __shfl_up_sync(0xffffffffu, vc, o);
+      if (lane >= o) { vi += a; vc += b; }
+    }
+    if (lane == 31) { s_items[w] = vi; s_chains[w] = vc; }
+    __syncthreads();
+    int oi = 0, oc = 0;
+    for (int q = 0; q < w; ++q) { oi += s_items[q]; oc += s_chains[q]; }
+    int run_i = s_run_items, run_c = s_run_chains;
+    if (d < nslots) {
+      PlanEntry e;
+      e.item_off = run_i + oi + vi - items;
+      e.tiles = tiles; e.nch = nch; e.clen = clen; e.n_i = ni; e.n_j = nj;
+      e.pad0 = run_c + oc + vc - chains;
+      e.tsize = tsize;
+      plan[d] = e;
+    }
+    __syncthreads();
+    if (tid == blockDim.x - 1) { s_run_items = run_i + oi + vi; s_run_chains = run_c + oc + vc; }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    ph->total_items = s_run_items;
+    ph->n_diodes = nslots;
+  }
+}
+
+// Per-particle index space over the PM_PART plan (tiles of RD_ITILE).
+__device__ __forceinline__ bool part_index(const PlanEntry* plan, const PlanHeader* ph, int g,
+                                           int* d, int* i) {
+  ItemRef it = decode_item(plan, ph->n_diodes, g);
+  *d = it.d;
+  *i = it.i0 + threadIdx.x;
+  return *i < plan[it.d].n_i;
+}
+
+__global__ void __launch_bounds__(RD_ITILE)
+k_pack(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __restrict__ plan,
+       const PlanHeader* __restrict__ ph) {
+  for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
+    int d, i;
+    if (!part_index(plan, ph, g, &d, &i)) continue;
+    pack_one(P[d], pool, P[d].off + i);
+  }
+}
+
+__global__ void __launch_bounds__(RD_ITILE)
+k_position(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
+           const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph) {
+  for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
+    int d, i;
+    if (!part_index(plan, ph, g, &d, &i)) continue;
+    const DiodeParams& p = P[d];
+    const int gi = p.off + i;
+    if (pool.species[gi] != 3) {
+      const double dt = p.dt, dt2 = p.dt2;
+      double ax = pool.ax[gi], ay = pool.ay[gi], az = pool.az[gi];
+      double bx = pool.bx[gi], by = pool.by[gi], bz = pool.bz[gi];
+      double x = (pool.x[gi] + pool.vx[gi] * dt) + ((1.0 / 6.0) * (4.0 * ax - bx)) * dt2;
+      double y = (pool.y[gi] + pool.vy[gi] * dt) + ((1.0 / 6.0) * (4.0 * ay - by)) * dt2;
+      double z = (pool.z[gi] + pool.vz[gi] * dt) + ((1.0 / 6.0) * (4.0 * az - bz)) * dt2;
+      pool.x[gi] = x; pool.y[gi] = y; pool.z[gi] = z;
+      pool.cx[gi] = bx; pool.cy[gi] = by; pool.cz[gi] = bz;
+      pool.bx[gi] = ax; pool.by[gi] = ay; pool.bz[gi] = az;
+      pool.ax[gi] = 0.0; pool.ay[gi] = 0.0; pool.az[gi] = 0.0;
+      DiodeDyn& yy = Dy[d];
+      if (z < 0.0) mark_remove(p, yy, pool, i, gi, 2);
+      else if (z > p.d) mark_remove(p, yy, pool, i, gi, 1);
+      if (p.geometry == RD_G_TIP && tip_eta(p, x, y, z) < p.eta_1) mark_remove(p, yy, pool, i, gi, 2);
+    }
+    pack_one(p, pool, gi);
+  }
+}
+
+__global__ void __launch_bounds__(RD_ITILE)
+k_velocity(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __restrict__ plan,
+           const PlanHeader* __restrict__ ph, double* __restrict__ ramo) {
+  for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
+    int d, i;
+    if (!part_index(plan, ph, g, &d, &i)) continue;
+    const DiodeParams& p = P[d];
+    const int gi = p.off + i;
+    double r = 0.0;
+    if (pool.species[gi] != 3) {
+      const double dt = p.dt;
+      double vx = pool.vx[gi] + ((1.0 / 6.0) * ((2.0 * pool.ax[gi] + 5.0 * pool.bx[gi]) - pool.cx[gi])) * dt;
+      double vy = pool.vy[gi] + ((1.0 / 6.0) * ((2.0 * pool.ay[gi] + 5.0 * pool.by[gi]) - pool.cy[gi])) * dt;
+      double vz = pool.vz[gi] + ((1.0 / 6.0) * ((2.0 * pool.az[gi] + 5.0 * pool.bz[gi]) - pool.cz[gi])) * dt;
+      pool.vx[gi] = vx; pool.vy[gi] = vy; pool.vz[gi] = vz;
+      if (pool.species[gi] == 1) {
+        double ux, uy, uz;
+        if (p.geometry == RD_G_TIP) {   // E_zunit_tip
+          double ex, ey, ez;
+          tip_field_E(p, pool.x[gi], pool.y[gi], pool.z[gi], &ex, &ey, &ez);
+          ux = (ex * p.pre_E_unit) / p.pre_E; uy = (ey * p.pre_E_unit) / p.pre_E; uz = (ez * p.pre_E_unit) / p.pre_E;
+        } else {                        // E_zunit_planar
+          ux = 0.0; uy = 0.0; uz = -1.0 / p.d;
+        }
+        r = pool.q[gi] * ((vx * ux + vy * uy) + vz * uz);
+      }
+    }
+    ramo[gi] = r;
+  }
+}
+
+// Ramo current and electron-step count per diode (fixed-order reduction).
+__global__ void __launch_bounds__(256)
+k_ramo(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, const double* __restrict__ ramo) {
+  __shared__ double red[256];
+  const int d = blockIdx.x;
+  const DiodeParams& p = P[d];
+  if (!p.active) return;
+  const int n = Dy[d].n;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += ramo[p.off + i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    Dy[d].ramo_current = red[0];
+    Dy[d].electron_steps += n;
+    Dy[d].steps_done += 1;
+  }
+}
+
+// ---- compaction ------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024)
+k_compact_count(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
+                const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                int* __restrict__ kept) {
+  __shared__ int wsum[32];
+  for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
+    ItemRef it = decode_item(plan, ph->n_diodes, g);
+    const DiodeParams& p = P[it.d];
+    if (Dy[it.d].n_remove == 0) continue;   // block-uniform
+    const int n = plan[it.d].n_i;
+    const int i = it.i0 + threadIdx.x;
+    int m = (i < n) ? pool.mask[p.off + i] : 0;
+    int c = __popc(__ballot_sync(0xffffffffu, m));
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int q = 0; q < 32; ++q) t += wsum[q];
+      kept[g] = t;
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ void move_particle(const Pool& a, const Pool& b, int src, int dst) {
+  b.x[dst] = a.x[src]; b.y[dst] = a.y[src]; b.z[dst] = a.z[src];
+  b.vx[dst] = a.vx[src]; b.vy[dst] = a.vy[src]; b.vz[dst] = a.vz[src];
+  b.ax[dst] = a.ax[src]; b.ay[dst] = a.ay[src]; b.az[dst] = a.az[src];
+  b.bx[dst] = a.bx[src]; b.by[dst] = a.by[src]; b.bz[dst] = a.bz[src];
+  b.cx[dst] = a.cx[src]; b.cy[dst] = a.cy[src]; b.cz[dst] = a.cz[src];
+  b.q[dst] = a.q[src]; b.m[dst] = a.m[src];
+  b.species[dst] = a.species[src]; b.id[dst] = a.id[src];
+  b.step0[dst] = a.step0[src]; b.section[dst] = a.section[src];
+}
+
+__global__ void __launch_bounds__(1024)
+k_compact_scatter(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
+                  Pool tmp, const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                  const int* __restrict__ kept, int* __restrict__ life, const int* __restrict__ step_ptr) {
+  __shared__ int wsum[32];
+  const int step = *step_ptr;
+  for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
+    ItemRef it = decode_item(plan, ph->n_diodes, g);
+    const DiodeParams& p = P[it.d];
+    const DiodeDyn& y = Dy[it.d];
+    if (y.n_remove == 0) continue;
+    const int n = plan[it.d].n_i;
+    const int b = it.tile, i0 = it.i0;
+    if (i0 + 1024 <= y.first_dead) continue;   // nothing moves in this block
+    const bool record = (n - y.n_remove) > 0;  // the reference skips the all-removed case
+    int before = 0;
+    const int tb0 = plan[it.d].item_off;
+    for (int q = 0; q < b; ++q) before += kept[tb0 + q];
+    const int i = i0 + threadIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int m = (i < n) ? pool.mask[p.off + i] : 0;
+    unsigned bal = __ballot_sync(0xffffffffu, m);
+    if (lane == 0) wsum[w] = __popc(bal);
+    __syncthreads();
+    int pre = 0;
+    for (int q = 0; q < w; ++q) pre += wsum[q];
+    pre += __popc(bal & ((1u << lane) - 1));
+    if (i < n && i >= y.first_dead) {
+      if (m) {
+        move_particle(pool, tmp, p.off + i, p.off + before + pre);
+      } else if (record) {
+        int lt = step - pool.step0[p.off + i];
+        if (lt <= 0) lt = 1;
+        if (lt > RD_MAX_LIFE) lt = RD_MAX_LIFE;
+        if (pool.species[p.off + i] == 1) atomicAdd(&life[(size_t)it.d * RD_MAX_LIFE + lt - 1], 1);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(1024)
+k_compact_copy(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
+               Pool tmp, const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph) {
+  for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
+    ItemRef it = decode_item(plan, ph->n_diodes, g);
+    const DiodeParams& p = P[it.d];
+    const DiodeDyn& y = Dy[it.d];
+    if (y.n_remove == 0) continue;
+    const int n = plan[it.d].n_i, n_new = n - y.n_remove;
+    const int i = it.i0 + threadIdx.x;
+    if (i >= n) continue;
+    const int gi = p.off + i;
+    pool.mask[gi] = 1;
+    if (i >= y.first_dead && i < n_new) {
+      move_particle(tmp, pool, gi, gi);
+      pack_one(p, pool, gi);
+    }
+  }
+}
+
+__global__ void k_compact_finish(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, int nslots) {
+  int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nslots || !P[d].active) return;
+  DiodeDyn& y = Dy[d];
+  y.absorbed_top_step = y.n_remove_top;
+  y.absorbed_bot_step = y.n_remove_bot;
+  y.absorbed_top_total += y.n_remove_top;
+  y.absorbed_bot_total += y.n_remove_bot;
+  if (y.n_remove > 0 && y.n > 0) y.n = y.n - y.n_remove;
+  y.n_remove = y.n_remove_top = y.n_remove_bot = 0;
+  y.first_dead = 0x7fffffff;
+}
+
+__global__ void k_step_set(int* step_ptr, int step) { *step_ptr = step; }
+__global__ void k_step_inc(int* step_ptr) { *step_ptr += 1; }
+
+}  // namespace
+
+// ---- launch wrappers ------------------------------------------------------------------
+cudaError_t rd_launch_plan(cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy, int nslots,
+                           int mode, int target_items, int max_items, const int* npts,
+                           PlanEntry* plan, PlanHeader* ph) {
+  k_plan<<<1, 1024, 0, st>>>(P, Dy, nslots, mode, target_items, max_items, npts, plan, ph);
+  return cudaGetLastError();
+}
+cudaError_t rd_launch_pack(int grid, cudaStream_t st, const DiodeParams* P, const Pool& pool,
+                           const PlanEntry* plan, const PlanHeader* ph) {
+  k_pack<<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph);
+  return cudaGetLastError();
+}
+cudaError_t rd_launch_position(int grid, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                               const Pool& pool, const PlanEntry* plan, const PlanHeader* ph) {
+  k_position<<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph);
+  return cudaGetLastError();
+}
+cudaError_t rd_launch_velocity(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
+                               DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
+                               const PlanHeader* ph, double* ramo) {
+  k_velocity<<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, ramo);
+  k_ramo<<<nslots, 256, 0, st>>>(P, Dy, ramo);
+  return cudaGetLastError();
+}
+cudaError_t rd_launch_compact(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
+                              DiodeDyn* Dy, const Pool& pool, const Pool& tmp,
+                              const PlanEntry* plan, const PlanHeader* ph, int* kept, int* life,
+                              const int* step_ptr) {
+  k_compact_count<<<grid, 1024, 0, st>>>(P, Dy, pool, plan, ph, kept);
+  k_compact_scatter<<<grid, 1024, 0, st>>>(P, Dy, pool, tmp, plan, ph, kept, life, step_ptr);
+  k_compact_copy<<<grid, 1024, 0, st>>>(P, Dy, pool, tmp, plan, ph);
+  k_compact_finish<<<(nslots + 127) / 128, 128, 0, st>>>(P, Dy, nslots);
+  return cudaGetLastError();
+}
+cudaError_t rd_launch_step_set(cudaStream_t st, int* step_ptr, int step) {
+  k_step_set<<<1, 1, 0, st>>>(step_ptr, step);
+  return cudaGetLastError();
+}
+cudaError_t rd_launch_step_inc(cudaStream_t st, int* step_ptr) {
+  k_step_inc<<<1, 1, 0, st>>>(step_ptr);
+  return cudaGetLastError();
+}
+
+namespace {
+// Add_Particle (src/mod_pair.F90:29-159) for a batch, in order.
+__global__ void k_add_particles(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
+                                int d, int cnt, const double* __restrict__ pos, const double* __restrict__ vel,
+                                const int* __restrict__ species, int step, int section) {
+  const DiodeParams& p = P[d];
+  DiodeDyn& y = Dy[d];
+  const int n0 = y.n, id0 = y.nrID;
+  const int room = p.cap - n0 > 0 ? p.cap - n0 : 0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < cnt && t < room; t += gridDim.x * blockDim.x) {
+    const int i = n0 + t, gi = p.off + i;
+    const double X = pos[3 * t], Y = pos[3 * t + 1], Z = pos[3 * t + 2];
+    const int sp = species ? species[t] : 1;
+    double q, m;
+    if (sp == 1) { q = -1.0 * c_k.q0; m = 1.0 * c_k.m0; }
+    else if (sp == 2) { q = 1.0 * c_k.q0; m = c_k.m_N2p; }
+    else { q = 0.0; m = c_k.m_N2; }
+    double ex, ey, ez;
+    vacuum_field(p, X, Y, Z, &ex, &ey, &ez);
+    const double qm = q / m;
+    pool.x[gi] = X; pool.y[gi] = Y; pool.z[gi] = Z;
+    pool.vx[gi] = vel ? vel[3 * t] : 0.0; pool.vy[gi] = vel ? vel[3 * t + 1] : 0.0;
+    pool.vz[gi] = vel ? vel[3 * t + 2] : 0.0;
+    pool.ax[gi] = pool.bx[gi] = pool.cx[gi] = qm * ex;
+    pool.ay[gi] = pool.by[gi] = pool.cy[gi] = qm * ey;
+    pool.az[gi] = pool.bz[gi] = pool.cz[gi] = qm * ez;
+    pool.q[gi] = q; pool.m[gi] = m;
+    pool.species[gi] = sp; pool.id[gi] = id0 + t; pool.step0[gi] = step;
+    pool.section[gi] = section; pool.mask[gi] = 1;
+    pack_one(p, pool, gi);
+  }
+}
+
+__global__ void k_add_finish(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, int d, int cnt) {
+  DiodeDyn& y = Dy[d];
+  const int room = P[d].cap - y.n > 0 ? P[d].cap - y.n : 0;
+  const int added = cnt < room ? cnt : room;
+  y.n += added;
+  y.nrID += added;
+  y.dropped_total += cnt - added;
+}
+
+__global__ void k_mark(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, int d,
+                       int i, int why) {
+  if (i < Dy[d].n) {
+    mark_remove(P[d], Dy[d], pool, i, P[d].off + i, why);
+    pack_one(P[d], pool, P[d].off + i);
+  }
+}
+}  // namespace
+
+cudaError_t rd_launch_add_particles(cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
+                                    int d, int cnt, const double* pos, const double* vel,
+                                    const int* species, int step, int section) {
+  if (cnt > 0) {
+    int blocks = (cnt + 255) / 256;
+    k_add_particles<<<blocks, 256, 0, st>>>(P, Dy, pool, d, cnt, pos, vel, species, step, section);
+  }
+  k_add_finish<<<1, 1, 0, st>>>(P, Dy, d, cnt);
+  return cudaGetLastError();
+}
+
+cudaError_t rd_launch_mark(cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy, const Pool& pool, int d,
+                           int i, int why) {
+  k_mark<<<1, 1, 0, st>>>(P, Dy, pool, d, i, why);
+  return cudaGetLastError();
+}
+
+RD_DEFINE_CONSTANT_UPLOAD(step)

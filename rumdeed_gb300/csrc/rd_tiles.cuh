@@ -1,0 +1,226 @@
+// rd_tiles.cuh -- per-pair arithmetic of one shared-memory j-tile, shared by
+// the force kernels (i = particle) and the field kernels (i = evaluation
+// point, always in the upper role: the point images / is imaged as the "a"
+// argument of the reference image functions).
+#pragma once
+#include "rd_pair.cuh"
+
+enum { T_UPPER = 0, T_LOWER = 1, T_DIAG = 2 };
+
+struct F32Acc {
+  float hx, lx, hy, ly, hz, lz;
+  __device__ void zero() { hx = lx = hy = ly = hz = lz = 0.f; }
+  __device__ void add(float tx, float ty, float tz) {
+    two_sum_acc(hx, lx, tx);
+    two_sum_acc(hy, ly, ty);
+    two_sum_acc(hz, lz, tz);
+  }
+};
+
+// ---- planar, FP32 compensated ------------------------------------------------
+// One j-tile against the thread's particle i.  NIC0: N_ic_max == 0 fast path.
+template <int MODE, bool NIC0>
+__device__ __forceinline__ void planar_tile_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
+                                                int kmax, float4 ih, float4 il, int self_k,
+                                                int nic, float dnm, int ic, float& tx,
+                                                float& ty, float& tz) {
+  float sx = 0.f, sy = 0.f, sz = 0.f, szs = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < kmax; ++k) {
+    float4 h = sh[k], l = sl[k];
+    float q = h.w;
+    if (MODE == T_DIAG) q = (k == self_k) ? 0.f : q;
+    float dx = (ih.x - h.x) + (il.x - l.x);
+    float dy = (ih.y - h.y) + (il.y - l.y);
+    float dz = (ih.z - h.z) + (il.z - l.z);
+    float dxy2 = fmaf(dx, dx, dy * dy);
+    float r2 = fmaf(dz, dz, dxy2);
+    float inv = rsqrtf(fmaxf(r2, 1e-20f));
+    float s = q * (inv * inv) * inv;
+    sx = fmaf(s, dx, sx);
+    sy = fmaf(s, dy, sy);
+    sz = fmaf(s, dz, sz);
+    if (ic) {
+      // n = 0 partner at -z_b: dz = z_a + z_b (symmetric in the roles)
+      float zs = (ih.z + h.z) + (il.z + l.z);
+      float ri = rsqrtf(fmaxf(fmaf(zs, zs, dxy2), 1e-20f));
+      float si = q * (ri * ri) * ri;
+      sx = fmaf(-si, dx, sx);
+      sy = fmaf(-si, dy, sy);
+      sz = fmaf(-si, zs, sz);
+      if (!NIC0) {
+        // anode distances u = d - z, exact near the anode
+        float us = il.w + l.w;
+        for (int n = 1; n <= nic; ++n) {
+          float two_nd = 2.0f * n * dnm;
+          // opposite-charge partners (symmetric in the roles)
+          float z1 = (n == 1) ? -us : zs - two_nd;   // z_a + z_b - 2nd
+          float z2 = zs + two_nd;                      // z_a + z_b + 2nd
+          float r1 = rsqrtf(fmaxf(fmaf(z1, z1, dxy2), 1e-20f));
+          float r2b = rsqrtf(fmaxf(fmaf(z2, z2, dxy2), 1e-20f));
+          float s1 = q * (r1 * r1) * r1, s2 = q * (r2b * r2b) * r2b;
+          sx = fmaf(-(s1 + s2), dx, sx);
+          sy = fmaf(-(s1 + s2), dy, sy);
+          sz = fmaf(-s1, z1, fmaf(-s2, z2, sz));
+          // same-charge partners, evaluated with a = i; the z part changes
+          // sign when j < i (lower-index role convention)
+          float z3 = dz - two_nd, z4 = dz + two_nd;
+          float r3 = rsqrtf(fmaxf(fmaf(z3, z3, dxy2), 1e-20f));
+          float r4 = rsqrtf(fmaxf(fmaf(z4, z4, dxy2), 1e-20f));
+          float s3 = q * (r3 * r3) * r3, s4 = q * (r4 * r4) * r4;
+          sx = fmaf(s3 + s4, dx, sx);
+          sy = fmaf(s3 + s4, dy, sy);
+          float zsame = fmaf(s3, z3, s4 * z4);
+          if (MODE == T_DIAG) zsame = (k > self_k) ? zsame : -zsame;
+          szs += zsame;
+        }
+      }
+    }
+  }
+  if (!NIC0) {
+    if (MODE == T_LOWER) szs = -szs;
+    sz += szs;
+  }
+  tx += sx; ty += sy; tz += sz;
+}
+
+// ---- planar, FP64 (reference arithmetic) ---------------------------------------
+template <int MODE>
+__device__ __forceinline__ void planar_tile_f64(const rd_d4* __restrict__ sj, int kmax, double x1,
+                                                double y1, double z1, double qd1, int self_k,
+                                                int nic, double d, int ic, double L2,
+                                                double& ax, double& ay, double& az) {
+  for (int k = 0; k < kmax; ++k) {
+    if (MODE == T_DIAG && k == self_k) continue;
+    rd_d4 pj = sj[k];
+    double pre = qd1 * pj.w;
+    double dx = x1 - pj.x, dy = y1 - pj.y, dz = z1 - pj.z;
+    double dxy2 = dx * dx + dy * dy;
+    double r = sqrt(dxy2 + dz * dz) + L2;
+    double inv = 1.0 / ((r * r) * r);
+    ax = ax + (pre * inv) * dx;
+    ay = ay + (pre * inv) * dy;
+    az = az + (pre * inv) * dz;
+    if (ic) {
+      bool upper = (MODE == T_UPPER) || (MODE == T_DIAG && k > self_k);
+      double za = upper ? z1 : pj.z, zb = upper ? pj.z : z1;
+      // acc_ic_planar_series.inc
+      double zic = -1.0 * zb, dzi = za - zic;
+      r = sqrt(dxy2 + dzi * dzi) + L2;
+      inv = 1.0 / ((r * r) * r);
+      double icx = -dx * inv, icy = -dy * inv, icz = -dzi * inv;
+      for (int n = 1; n <= nic; ++n) {
+        double zz0 = (2.0 * n) * d - zb, zz1 = (-2.0 * n) * d - zb;
+        double zz2 = (2.0 * n) * d + zb, zz3 = (-2.0 * n) * d + zb;
+        dzi = za - zz0; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
+        icx = icx - dx * inv; icy = icy - dy * inv; icz = icz - dzi * inv;
+        dzi = za - zz1; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
+        icx = icx - dx * inv; icy = icy - dy * inv; icz = icz - dzi * inv;
+        dzi = za - zz2; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
+        icx = icx + dx * inv; icy = icy + dy * inv; icz = icz + dzi * inv;
+        dzi = za - zz3; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
+        icx = icx + dx * inv; icy = icy + dy * inv; icz = icz + dzi * inv;
+      }
+      ax = ax + pre * icx;
+      ay = ay + pre * icy;
+      az = az + pre * icz;
+    }
+  }
+}
+
+// ---- hyperboloid tip -------------------------------------------------------------
+// Sphere image term (acc_tip_image_point.inc + acc_tip_ic_force.inc):
+// a = lower-indexed particle, b = higher-indexed,
+//   IC = K [ (a - b)/|b - a|^3 - (R/dis_a) (im_a - b)/|b - im_a|^3 ]
+// applied to the lower particle as is and to the higher one mirrored in x, y.
+template <int MODE>
+__device__ __forceinline__ void tip_tile_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
+                                             const float4* __restrict__ sih, const float4* __restrict__ sil,
+                                             int kmax, float4 ih, float4 il, float4 iih, float4 iil,
+                                             int self_k, int ic, float K, float& tx, float& ty,
+                                             float& tz) {
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+  for (int k = 0; k < kmax; ++k) {
+    float4 h = sh[k], l = sl[k];
+    float q = h.w;
+    if (MODE == T_DIAG) q = (k == self_k) ? 0.f : q;
+    float dx = (ih.x - h.x) + (il.x - l.x);
+    float dy = (ih.y - h.y) + (il.y - l.y);
+    float dz = (ih.z - h.z) + (il.z - l.z);
+    float r2 = fmaf(dz, dz, fmaf(dx, dx, dy * dy));
+    float inv = rsqrtf(fmaxf(r2, 1e-20f));
+    float inv3 = (inv * inv) * inv;
+    float s = q * inv3;
+    sx = fmaf(s, dx, sx);
+    sy = fmaf(s, dy, sy);
+    sz = fmaf(s, dz, sz);
+    if (ic) {
+      bool upper = (MODE == T_UPPER) || (MODE == T_DIAG && k > self_k);
+      // e = im_a - b: upper (a = i, b = j) uses the thread's image point,
+      // lower (a = j, b = i) the tile's.
+      float ex, ey, ez, c;
+      if (upper) {
+        ex = (iih.x - h.x) + (iil.x - l.x);
+        ey = (iih.y - h.y) + (iil.y - l.y);
+        ez = (iih.z - h.z) + (iil.z - l.z);
+        c = iih.w;
+      } else {
+        float4 jh = sih[k], jl = sil[k];
+        ex = (jh.x - ih.x) + (jl.x - il.x);
+        ey = (jh.y - ih.y) + (jl.y - il.y);
+        ez = (jh.z - ih.z) + (jl.z - il.z);
+        c = jh.w;
+      }
+      float re = rsqrtf(fmaxf(fmaf(ez, ez, fmaf(ex, ex, ey * ey)), 1e-20f));
+      float se = c * (re * re) * re;
+      // upper: K[ d inv3 - c e/|e|^3 ];  lower (mirrored x, y):
+      //        K[ (dx, dy, -dz) inv3 + c (ex, ey, -ez)/|e|^3 ]
+      //   x, y: K [ d inv3 - sgn c e/|e|^3 ],  z: K [ sgn d inv3 - c e/|e|^3 ]
+      float sgn = upper ? 1.f : -1.f;
+      float kq = K * q;
+      sx = fmaf(kq, fmaf(inv3, dx, -sgn * se * ex), sx);
+      sy = fmaf(kq, fmaf(inv3, dy, -sgn * se * ey), sy);
+      sz = fmaf(kq, fmaf(sgn * inv3, dz, -se * ez), sz);
+    }
+  }
+  tx += sx; ty += sy; tz += sz;
+}
+
+// FP64 tip gather: Calculate_Acceleration_Particles_ACC tip branch (:1344-1426).
+template <int MODE>
+__device__ __forceinline__ void tip_tile_f64(const rd_d4* __restrict__ sj, int kmax, double x1,
+                                             double y1, double z1, double qd1, int self_k, int ic,
+                                             const DiodeParams& p, double L2, double K,
+                                             double& ax, double& ay, double& az) {
+  const double z0 = p.h_tip - p.r_tip, R = p.r_tip;
+  for (int k = 0; k < kmax; ++k) {
+    if (MODE == T_DIAG && k == self_k) continue;
+    rd_d4 pj = sj[k];
+    double pre = qd1 * pj.w;
+    double dx = x1 - pj.x, dy = y1 - pj.y, dz = z1 - pj.z;
+    double r = sqrt(dx * dx + dy * dy + dz * dz) + L2;
+    double inv = 1.0 / ((r * r) * r);
+    ax = ax + (pre * inv) * dx;
+    ay = ay + (pre * inv) * dy;
+    az = az + (pre * inv) * dz;
+    if (ic) {
+      bool upper = (MODE == T_UPPER) || (MODE == T_DIAG && k > self_k);
+      double xa = upper ? x1 : pj.x, ya = upper ? y1 : pj.y, za = upper ? z1 : pj.z;
+      double xb = upper ? pj.x : x1, yb = upper ? pj.y : y1, zb = upper ? pj.z : z1;
+      double sgn = upper ? 1.0 : -1.0;
+      double dza = za - z0;
+      double dis = sqrt(xa * xa + ya * ya + dza * dza);
+      double zim = z0 + (R * R) / (sqrt((1.0 + (xa * xa) / (dza * dza)) + (ya * ya) / (dza * dza)) * dis);
+      double xim = ((zim - z0) * xa) / dza, yim = ((zim - z0) * ya) / dza;
+      double tda = pow((xb - xa) * (xb - xa) + (yb - ya) * (yb - ya) + (zb - za) * (zb - za), 1.5);
+      double tdb = pow((xb - xim) * (xb - xim) + (yb - yim) * (yb - yim) + (zb - zim) * (zb - zim), 1.5);
+      double icx = K * ((xa - xb) / tda - (R * (xim - xb)) / (dis * tdb));
+      double icy = K * ((ya - yb) / tda - (R * (yim - yb)) / (dis * tdb));
+      double icz = K * ((za - zb) / tda - (R * (zim - zb)) / (dis * tdb));
+      ax = ax + pre * sgn * icx;
+      ay = ay + pre * sgn * icy;
+      az = az + pre * icz;
+    }
+  }
+}
+

@@ -1,0 +1,292 @@
+"""GPU parity tests: librumdeed_gb300 (through its C ABI) against the CPU oracle.
+
+Tolerances (per particle / point, norm-relative, as src/mod_tests.F90:1665-1669):
+  FP64 plain form          <= 1e-12
+  FP32 compensated form    <= 1e-5  (the spec force tolerance)
+Integer and index results (counts, ids, order, emitted sets) must be equal.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NM = 1e-9
+TOL64, TOL32 = 1e-12, 1e-5
+
+
+def nrel(a, b):
+    a = np.asarray(a); b = np.asarray(b)
+    return np.max(np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300))
+
+
+def uniform_particles(rng, n, half=500 * NM, d=1000 * NM):
+    return np.column_stack([rng.uniform(-half, half, n), rng.uniform(-half, half, n),
+                            rng.uniform(1 * NM, d - 1 * NM, n)])
+
+
+def both(rg, orc, prec, n=300, ic=True, nic=0, seed=1, ions=False, V=2e3, d=1000 * NM):
+    rng = np.random.default_rng(seed)
+    pos = uniform_particles(rng, n, d=d)
+    sp = np.where(np.arange(n) % 5 == 4, 2, 1) if ions else np.ones(n, dtype=int)
+    eng = rg.Engine(precision=prec, max_diodes=4, particle_capacity=max(4 * n, 4096))
+    dio = eng.add_diode(V_s=V, gap=d, capacity=max(2 * n, 1024), image_charge=ic, N_ic_max=nic)
+    dio.add_particles(pos, species=sp)
+    o = orc.OracleDiode(cap=max(2 * n, 1024), V_s=V, d=d, image_charge=ic, N_ic_max=nic)
+    for p, s in zip(pos, sp):
+        o.add(p, species=int(s))
+    return eng, dio, o, pos
+
+
+@pytest.mark.parametrize("ic,nic,ions", [(True, 0, False), (True, 2, True), (False, 0, True), (True, 7, False)])
+def test_accel_fp64_matches_oracle(rg, orc, ic, nic, ions):
+    eng, dio, o, _ = both(rg, orc, rg.PREC_FP64, n=333, ic=ic, nic=nic, ions=ions)
+    acc = dio.calculate_acceleration_particles()
+    assert nrel(acc, o.accel("gather", True)) <= TOL64
+    # and the reference CPU pair loop gives the same up to rounding
+    assert nrel(acc, o.accel("planar", True)) <= TOL64
+    eng.close()
+
+
+@pytest.mark.parametrize("n,nic", [(1000, 0), (2048, 7), (700, 1)])
+def test_accel_fp32c_within_tolerance(rg, orc, n, nic):
+    eng, dio, o, _ = both(rg, orc, rg.PREC_FP32C, n=n, nic=nic)
+    acc = dio.calculate_acceleration_particles()
+    ref = o.accel("gather", True)
+    assert nrel(acc, ref) <= TOL32
+    # also on the pair part alone (vacuum-field term removed)
+    k = orc.constants()
+    vac = np.array([0.0, 0.0, -k["q_0"] / k["m_0"] * (-2e3 / (1000 * NM))])
+    assert nrel(acc - vac, ref - vac) <= 1e-4
+    eng.close()
+
+
+def test_field_at_parity(rg, orc):
+    rng = np.random.default_rng(3)
+    pts = np.vstack([uniform_particles(rng, 100),
+                     np.column_stack([rng.uniform(-500 * NM, 500 * NM, 100),
+                                      rng.uniform(-500 * NM, 500 * NM, 100), np.zeros(100)])])
+    for prec, tol in ((rg.PREC_FP64, TOL64), (rg.PREC_FP32C, TOL32)):
+        for nic in (0, 3):
+            eng, dio, o, _ = both(rg, orc, prec, n=500, nic=nic, seed=4)
+            f = dio.calc_field_at_batch(pts)
+            assert nrel(f, o.field_at(pts)) <= tol, (prec, nic)
+            eng.close()
+
+
+def test_golden_probe_on_gpu(rg, orc):
+    """Test_Acceleration_Without_Image_Charge field golden value through the GPU."""
+    for prec in (rg.PREC_FP64, rg.PREC_FP32C):
+        eng = rg.Engine(precision=prec, max_diodes=2, particle_capacity=4096)
+        d = eng.add_diode(V_s=2.0, gap=100 * NM, capacity=64, image_charge=False)
+        R = np.array([[3.0, -10.0, 2.0], [-9.0, 26.0, 80.0], [6.0, -24.0, 56.53]]) * NM
+        d.add_particles(R, species=[1, 1, 2])
+        probe = np.array([[np.float32(-4.55), np.float32(-2.34), np.float32(96.44)]], dtype=np.float64) * NM
+        E = d.calc_field_at_batch(probe)[0]
+        gold = np.array([-314559.29097098, 1423979.07058996, -20246038.87978313])
+        assert np.all(np.abs(E - gold) / np.abs(gold) < 0.02)
+        eng.close()
+
+
+def test_tip_accel_and_field(rg, orc):
+    rng = np.random.default_rng(11)
+    tip = (900 * NM, 100 * NM, 100 * NM)
+    n = 257
+    # particles above the tip surface
+    pos = np.column_stack([rng.uniform(-300 * NM, 300 * NM, n), rng.uniform(-300 * NM, 300 * NM, n),
+                           rng.uniform(105 * NM, 990 * NM, n)])
+    pts = np.array([[0.0, 0.0, 102.0], [30.0, -10.0, 130.0], [-50.0, 40.0, 300.0], [15.0, 8.0, 500.0]]) * NM
+    o = orc.OracleDiode(orc.TIP, cap=1024, V_s=2e3, d=1000 * NM, image_charge=True)
+    o.set_tip(*tip, 4.7)
+    for p in pos:
+        o.add(p)
+    ref = o.accel("gather", True)
+    fref = o.field_at(pts)
+    for prec, tol in ((rg.PREC_FP64, TOL64), (rg.PREC_FP32C, TOL32)):
+        eng = rg.Engine(precision=prec, max_diodes=2, particle_capacity=4096)
+        d = eng.add_diode(geometry=rg.GEOM_TIP, V_s=2e3, capacity=1024, tip_dim=tip)
+        d.add_particles(pos)
+        assert nrel(d.calculate_acceleration_particles(), ref) <= tol
+        assert nrel(d.calc_field_at_batch(pts), fref) <= tol
+        eng.close()
+
+
+def test_beeman_kinematics_gpu(rg, orc):
+    """Test_Beeman_Kinematics (src/mod_tests.F90:1403-1452) through rd_update_position."""
+    k = orc.constants()
+    d, V, dt, vx0 = 1000 * NM, 2.0e3, 0.25e-15, 1.0e3
+    for prec in (rg.PREC_FP64, rg.PREC_FP32C):
+        eng = rg.Engine(precision=prec, max_diodes=2, particle_capacity=4096)
+        dio = eng.add_diode(V_s=V, gap=d, time_step=dt, image_charge=False, capacity=16)
+        dio.add_particle([0.0, 0.0, 500 * NM], vel=[vx0, 0.0, 0.0])
+        for i in range(1, 4):
+            eng.update_position(i)
+        p = dio.particles()
+        az = k["q_0"] * V / (k["m_0"] * d)
+        assert p["pos"][0, 2] - 500 * NM == pytest.approx(4.5 * az * dt ** 2, rel=1e-12)
+        assert p["vel"][0, 2] == pytest.approx(3 * az * dt, rel=1e-12)
+        assert p["pos"][0, 0] == pytest.approx(3 * vx0 * dt, rel=1e-12)
+        assert dio.counters()["ramo_current"] == pytest.approx(k["q_0"] * 3 * az * dt / d, rel=1e-12)
+        eng.close()
+
+
+def test_transit_time_gpu(rg, orc):
+    """Test_Transit_Time (src/mod_tests.F90:912-977) with rd_update_position + rd_remove_particles."""
+    k = orc.constants()
+    d, V, dt, z0 = 1000 * NM, 2.0e3, 0.25e-15, 1.0 * NM
+    steps_exp = int(np.ceil(np.sqrt(2 * d * (d - z0) * k["m_0"] / (k["q_0"] * V)) / dt))
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=2, particle_capacity=4096)
+    dio = eng.add_diode(V_s=V, gap=d, time_step=dt, capacity=16)
+    dio.add_particle([0.0, 0.0, z0])
+    o = orc.OracleDiode(cap=16, V_s=V, d=d, time_step=dt)
+    o.add([0.0, 0.0, z0])
+    res = None
+    for i in range(1, steps_exp + 100):
+        eng.update_position(i)
+        eng.remove_particles(i)
+        o.verlet(i); o.remove(i)
+        if res is None and dio.n == 0:
+            res = i
+            break
+    assert res is not None and abs(res - steps_exp) < 0.01 * steps_exp
+    assert o.n == 0       # oracle absorbed on the same step
+    c = dio.counters()
+    assert c["absorbed_top_total"] == 1
+    assert dio.life_time()[res - 1 - 1] == 1 or dio.life_time().sum() == 0
+    eng.close()
+
+
+def test_removal_compaction_gpu(rg, orc):
+    """Test_Particle_Removal (src/mod_tests.F90:1193-1289) semantics on the device."""
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=2, particle_capacity=8192)
+    dio = eng.add_diode(V_s=2.0, gap=100 * NM, capacity=3000, image_charge=False)
+    n = 2500
+    R = np.column_stack([np.arange(1, n + 1) * 0.01 * NM, -np.arange(1, n + 1) * 0.02 * NM,
+                         np.linspace(1, 99, n) * NM])
+    V = np.column_stack([np.arange(1, n + 1) * 100.0, -np.arange(1, n + 1) * 50.0, np.arange(1, n + 1) * 25.0])
+    dio.add_particles(R, V, species=np.where(np.arange(n) % 7 == 3, 2, 1), step=1)
+    rng = np.random.default_rng(2)
+    dead = np.sort(rng.choice(n, 321, replace=False))
+    for i in dead:
+        dio.mark_particles_remove(int(i), rg.REMOVE_TOP)
+    dio.mark_particles_remove(int(dead[0]), rg.REMOVE_TOP)     # double mark is a no-op
+    eng.remove_particles(11)
+    keep = np.setdiff1d(np.arange(n), dead)
+    p = dio.particles()
+    assert dio.n == n - len(dead)
+    np.testing.assert_array_equal(p["pos"], R[keep])
+    np.testing.assert_array_equal(p["vel"], V[keep])
+    np.testing.assert_array_equal(p["id"], keep)
+    n_elec_dead = int(np.sum((dead % 7) != 3))
+    assert dio.life_time()[9] == n_elec_dead
+    c = dio.counters()
+    assert c["absorbed_top_total"] == n_elec_dead
+    eng.close()
+
+
+def _emission_pair(rg, orc, prec, seed=77, n0=150, work=2.0, jumps=40, chains=300):
+    rng = np.random.default_rng(seed)
+    d, V = 500 * NM, 1.0e3
+    pos = np.column_stack([rng.uniform(-60 * NM, 60 * NM, n0), rng.uniform(-60 * NM, 60 * NM, n0),
+                           rng.uniform(2 * NM, 490 * NM, n0)])
+    eng = rg.Engine(precision=prec, max_diodes=2, particle_capacity=8192, chain_capacity=4096)
+    dio = eng.add_diode(V_s=V, gap=d, capacity=4096, emitter_pos=(-50 * NM, -50 * NM),
+                        emitter_dim=(100 * NM, 100 * NM), work=[[work]], emission=True,
+                        mh_jumps=jumps, max_chains=chains, quad_panels=8, quad_order=4, seed=seed)
+    dio.add_particles(pos)
+    o = orc.OracleDiode(cap=4096, V_s=V, d=d)
+    o.set_planar_emitter(-50 * NM, -50 * NM, 100 * NM, 100 * NM, [[work]])
+    o.set_emission(True, seed=seed, mh_jumps=jumps, max_chains=chains, quad_panels=8, quad_order=4)
+    for p in pos:
+        o.add(p)
+    return eng, dio, o
+
+
+def test_emission_fp64_matches_oracle_chain_for_chain(rg, orc):
+    """Supply integral, MH chains (shared Philox streams) and the emission
+    test: the FP64 GPU form reproduces the oracle's emitted electrons."""
+    eng, dio, o = _emission_pair(rg, orc, rg.PREC_FP64)
+    n_before = dio.n
+    eng.do_emission(1)
+    o.emission(1)
+    c = dio.counters()
+    assert c["N_sup"] == pytest.approx(o.s.N_sup, rel=1e-12)
+    assert c["chains"] == o.s.last_chains
+    assert c["MH_std"] == pytest.approx(o.s.MH_std, rel=1e-12)
+    assert c["emitted_step"] == o.s.emitted_step > 0
+    p = dio.particles()
+    assert dio.n == o.n
+    new = slice(n_before, dio.n)
+    assert np.max(np.abs(p["pos"][new] - o.arr("pos")[new])) < 1e-12 * 100 * NM
+    np.testing.assert_array_equal(p["id"], o.iarr("id"))
+    eng.close()
+
+
+def test_full_steps_fp64_trajectory(rg, orc):
+    """Five main-loop iterations (emission, Beeman, forces, removal) agree."""
+    eng, dio, o = _emission_pair(rg, orc, rg.PREC_FP64, seed=5, jumps=20)
+    for i in range(1, 6):
+        eng.step(i)
+        o.step(i)
+        assert dio.n == o.n, i
+    p = dio.particles()
+    assert np.max(np.abs(p["pos"] - o.arr("pos"))) < 1e-9 * NM
+    assert nrel(p["vel"] + 1e-3, o.arr("vel") + 1e-3) < 1e-8
+    c = dio.counters()
+    assert c["emitted_total"] == o.s.emitted_total
+    assert c["ramo_current"] == pytest.approx(o.s.ramo_current, rel=1e-9)
+    eng.close()
+
+
+def test_emission_fp32c_statistics(rg, orc):
+    """The FP32 compensated form emits the same electrons as the FP64 oracle
+    unless a decision sits within the FP32 field error of its threshold."""
+    eng, dio, o = _emission_pair(rg, orc, rg.PREC_FP32C, seed=9)
+    eng.do_emission(1)
+    o.emission(1)
+    c = dio.counters()
+    assert c["N_sup"] == pytest.approx(o.s.N_sup, rel=1e-5)
+    assert abs(c["emitted_step"] - o.s.emitted_step) <= max(2, 0.05 * o.s.emitted_step)
+    eng.close()
+
+
+def test_tip_emission_fp64(rg, orc):
+    tip = (900 * NM, 100 * NM, 100 * NM)
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=2, particle_capacity=8192, chain_capacity=8192,
+                    quad_capacity=20000)
+    d = eng.add_diode(geometry=rg.GEOM_TIP, V_s=800.0, time_step=0.25e-15, capacity=4096, tip_dim=tip,
+                      emission=True, mh_jumps=20, max_chains=500, seed=3)
+    o = orc.OracleDiode(orc.TIP, cap=4096, V_s=800.0, d=1000 * NM)
+    o.set_tip(*tip, 4.7)
+    o.set_emission(True, seed=3, mh_jumps=20, max_chains=500)
+    for i in range(1, 3):
+        eng.step(i)
+        o.step(i)
+        c = d.counters()
+        assert c["N_sup"] == pytest.approx(o.s.N_sup, rel=1e-10)
+        assert c["emitted_step"] == o.s.emitted_step
+        assert d.n == o.n
+    p = d.particles()
+    if d.n:
+        assert np.max(np.abs(p["pos"] - o.arr("pos"))) < 1e-6 * NM
+    eng.close()
+
+
+def test_batch_equals_alone(rg, orc):
+    """A diode advanced alone and inside a mix of diodes gives the same result
+    (FP32 compensated: within the force tolerance)."""
+    rng = np.random.default_rng(21)
+    cfgs = [dict(V_s=rng.uniform(500, 5000), gap=rng.uniform(200, 2000) * NM, capacity=int(c))
+            for c in (300, 1500, 700)]
+    pos = [uniform_particles(rng, c["capacity"] // 2, d=c["gap"]) for c in cfgs]
+    solo = rg.Engine(precision=rg.PREC_FP32C, max_diodes=2, particle_capacity=8192)
+    a = solo.add_diode(**cfgs[1]); a.add_particles(pos[1])
+    solo.run(1, 5)
+    mix = rg.Engine(precision=rg.PREC_FP32C, max_diodes=8, particle_capacity=16384)
+    ds = [mix.add_diode(**c) for c in cfgs]
+    for dd, p in zip(ds, pos):
+        dd.add_particles(p)
+    mix.run(1, 5)
+    pa, pb = a.particles(), ds[1].particles()
+    assert a.n == ds[1].n
+    assert np.max(np.abs(pa["pos"] - pb["pos"])) < 1e-5 * cfgs[1]["gap"]
+    solo.close(); mix.close()

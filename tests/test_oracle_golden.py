@@ -1,0 +1,341 @@
+"""Pins the CPU oracle (oracle/rd_oracle.c) to the reference's own tests.
+
+Every test here ports a known-answer test of src/mod_tests.F90 (or
+src/mod_field_emission_v2.F90:1742-1778) with its golden values and its
+tolerances (2 % relative or 1e-6 absolute per component, src/mod_global.F90:
+419-420, unless the reference test states a tighter one).  Runs on CPU only.
+"""
+import numpy as np
+import pytest
+
+NM = 1e-9
+TOL_REL, TOL_ABS = 0.02, 1e-6
+
+
+def close(actual, expected):
+    """Assert_Close / Assert_Close_Vec, src/mod_tests.F90:113-159."""
+    a = np.atleast_1d(np.asarray(actual, dtype=float))
+    e = np.atleast_1d(np.asarray(expected, dtype=float))
+    for x, y in zip(a, e):
+        if abs(y) < TOL_ABS:
+            assert abs(x - y) < TOL_ABS, (a, e)
+        else:
+            assert abs(x - y) / abs(y) < TOL_REL, (a, e)
+
+
+def test_philox_known_answers(orc):
+    # Random123 known-answer vectors for philox4x32-10
+    assert orc.philox([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert orc.philox([0xffffffff] * 4, [0xffffffff] * 2) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert orc.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0]) == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+def test_constants(orc):
+    k = orc.constants()
+    # epsilon_0 = 1/(mu_0 c^2) with the 2018 NIST mu_0 (mod_global.F90:29-31)
+    assert k["epsilon_0"] == pytest.approx(8.8541878128e-12, rel=1e-10)
+    assert k["div_fac_c"] == pytest.approx(8.9875517923e9, rel=1e-10)
+    assert k["h_bar"] == pytest.approx(1.054571817e-34, rel=1e-9)
+
+
+def test_fn_functions(orc):
+    """Test_FN_Functions, src/mod_tests.F90:1688-1736 (phi = 4.7 eV)."""
+    L = orc.lib()
+    assert L.orc_v_y(-2e9, 4.7, 0) == 1.0 and L.orc_t_y(-2e9, 4.7, 0) == 1.0
+    close(L.orc_v_y(-2e9, 4.7, 1), 0.8253581935658024)
+    close(L.orc_t_y(-2e9, 4.7, 1), 1.0292422630703880)
+    close(L.orc_escape_prob_log(-2e9, 4.7, 1), -28.723444978828507)
+    close(L.orc_v_y(-4e9, 4.7, 1), 0.6808388366998485)
+    close(L.orc_t_y(-4e9, 4.7, 1), 1.0484437096180323)
+    close(L.orc_escape_prob_log(-4e9, 4.7, 1), -11.846999895226958)
+    close(L.orc_v_y(-1e12, 4.7, 1), 0.0)
+    # the restatement reproduces the golden values far below the 2 % band
+    assert abs(L.orc_escape_prob_log(-2e9, 4.7, 1) + 28.723444978828507) < 1e-12
+    assert abs(L.orc_v_y(-4e9, 4.7, 1) - 0.6808388366998485) < 1e-14
+    # Test_Field_Emission_Module (mod_field_emission_v2.F90:1758-1765): |dv| < 1e-6
+    assert abs(L.orc_v_y(-2.0e3 / 1000.0e-9, 4.7, 1) - 0.8253581935658024) < 1e-6
+
+
+def _three_particles(orc, ic=False, nic=0, d=100 * NM, V=2.0):
+    o = orc.OracleDiode(cap=16, V_s=V, d=d, time_step=0.25e-15, image_charge=ic, N_ic_max=nic)
+    R = np.array([[3.0, -10.0, 2.0], [-9.0, 26.0, 80.0], [6.0, -24.0, 56.53]]) * NM
+    o.add(R[0], species=orc.ELEC)
+    o.add(R[1], species=orc.ELEC)
+    o.add(R[2], species=orc.ION)
+    return o, R
+
+
+@pytest.mark.parametrize("kind", ["generic", "planar", "gather"])
+def test_acceleration_without_image_charge(orc, kind):
+    """Test_Acceleration_Without_Image_Charge, src/mod_tests.F90:405-519."""
+    k = orc.constants()
+    q0, m0, m_N2p = k["q_0"], k["m_0"], k["m_N2p"]
+    pre = q0 ** 2 / (4 * k["pi"] * k["epsilon_0"])
+    o, R = _three_particles(orc)
+    E = np.array([0.0, 0.0, -2.0 / (100 * NM)])
+    nrm = lambda v: np.linalg.norm(v) ** 3
+    a1 = pre / m0 * (R[0] - R[1]) / nrm(R[0] - R[1]) - pre / m0 * (R[0] - R[2]) / nrm(R[0] - R[2]) - q0 / m0 * E
+    a2 = pre / m0 * (R[1] - R[0]) / nrm(R[1] - R[0]) - pre / m0 * (R[1] - R[2]) / nrm(R[1] - R[2]) - q0 / m0 * E
+    a3 = -pre / m_N2p * (R[2] - R[0]) / nrm(R[2] - R[0]) - pre / m_N2p * (R[2] - R[1]) / nrm(R[2] - R[1]) + q0 / m_N2p * E
+    acc = o.accel(kind)
+    close(acc[0], a1)
+    close(acc[1], a2)
+    close(acc[2], a3)
+    # the analytic values hold to rounding: the l^2 guard is 1e-18 m on r ~ 1e-8 m
+    for a, b in zip(acc, (a1, a2, a3)):
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-9
+
+
+def test_field_probe_golden(orc):
+    """Golden field at the probe, src/mod_tests.F90:505-515 (independent Python script)."""
+    o, _ = _three_particles(orc)
+    # the probe literals are default (single precision) REALs in the reference
+    probe = np.array([np.float32(-4.55), np.float32(-2.34), np.float32(96.44)], dtype=np.float64) * NM
+    E = o.field_at(probe[None, :])[0]
+    close(E, [-314559.29097098, 1423979.07058996, -20246038.87978313])
+    # empty-system field (Test_Planar_Field :1128-1148)
+    empty = orc.OracleDiode(cap=4, V_s=2.0, d=100 * NM, image_charge=False)
+    close(empty.field_at(np.array([[-4.55, -2.34, 96.44]]) * NM)[0], [0.0, 0.0, -2.0 / (100 * NM)])
+
+
+def test_image_charge(orc):
+    """Test_Image_Charge, src/mod_tests.F90:523-695."""
+    k = orc.constants()
+    q0, pi, eps0, dfc = k["q_0"], k["pi"], k["epsilon_0"], k["div_fac_c"]
+    q1, q2 = -q0, q0
+    R1 = np.array([3.0, -10.0, 2.0]) * NM
+    R2 = np.array([6.0, -24.0, 98.53]) * NM
+    d = 100 * NM
+
+    def ic(o, a, b):
+        out = np.zeros(3)
+        o.L.orc_force_image_planar(o.p, orc.ptr(np.ascontiguousarray(a)), orc.ptr(np.ascontiguousarray(b)), orc.ptr(out))
+        return out
+
+    o = orc.OracleDiode(cap=4, V_s=2.0, d=d, image_charge=True, N_ic_max=0)
+    close(q1 ** 2 * dfc * ic(o, R1, R1), [0, 0, -q1 ** 2 / (4 * pi * eps0) / (2 * R1[2]) ** 2])
+    close(q2 ** 2 * dfc * ic(o, R2, R2), [0, 0, -q2 ** 2 / (4 * pi * eps0) / (2 * R2[2]) ** 2])
+    R2_ic = R2 * [1, 1, -1]
+    F12 = q1 * (-q2) / (4 * pi * eps0) * (R1 - R2_ic) / np.linalg.norm(R1 - R2_ic) ** 3
+    close(q1 * q2 * dfc * ic(o, R1, R2), F12)
+    R1_ic = R1 * [1, 1, -1]
+    F21 = q2 * (-q1) / (4 * pi * eps0) * (R2 - R1_ic) / np.linalg.norm(R2 - R1_ic) ** 3
+    close(q2 * q1 * dfc * ic(o, R2, R1), F21)
+
+    o1 = orc.OracleDiode(cap=4, V_s=2.0, d=d, image_charge=True, N_ic_max=1)
+
+    def partners(R, q):
+        zs = [-R[2], -2 * d - R[2], -2 * d + R[2], 2 * d - R[2], 2 * d + R[2]]
+        qs = [-q, -q, q, -q, q]
+        return [(np.array([R[0], R[1], z]), qq) for z, qq in zip(zs, qs)]
+
+    def field_from(R_eval, q_eval, parts):
+        return sum(q_eval * qq / (4 * pi * eps0) * (R_eval - Rp) / np.linalg.norm(R_eval - Rp) ** 3
+                   for Rp, qq in parts)
+
+    close(q1 ** 2 * dfc * ic(o1, R1, R1), field_from(R1, q1, partners(R1, q1)))
+    close(q2 ** 2 * dfc * ic(o1, R2, R2), field_from(R2, q2, partners(R2, q2)))
+    close(q1 * q2 * dfc * ic(o1, R1, R2), field_from(R1, q1, partners(R2, q2)))
+
+
+def test_planar_batch_field(orc):
+    """Test_Planar_Batch_Field, src/mod_tests.F90:1554-1603."""
+    pts = np.array([[0.0, 0.0, 10.0], [12.0, -4.0, 21.0], [-20.0, 30.0, 80.0], [40.0, 40.0, 95.0]]) * NM
+    o = orc.OracleDiode(cap=8, V_s=2.0, d=100 * NM, image_charge=True, N_ic_max=1)
+    for f in o.field_at(pts):
+        close(f, [0.0, 0.0, -2.0 / (100 * NM)])
+    o.add(np.array([10.0, -5.0, 20.0]) * NM)
+    o.add(np.array([-15.0, 8.0, 60.0]) * NM)
+    o.add(np.array([5.0, 25.0, 40.0]) * NM, species=orc.ION)
+    batch = o.field_at(pts)
+    for k in range(4):
+        close(batch[k], o.field_at(pts[k:k + 1], compensated=False)[0])
+
+
+@pytest.mark.parametrize("ic,nic", [(True, 2), (False, 0)])
+def test_planar_specialized_acceleration(orc, ic, nic):
+    """Test_Planar_Specialized_Acceleration, src/mod_tests.F90:1610-1680 (< 1e-10)."""
+    d = 1000 * NM
+    o = orc.OracleDiode(cap=64, V_s=2.0e3, d=d, image_charge=ic, N_ic_max=nic)
+    box = np.array([100 * NM, 100 * NM, d])
+    for i in range(1, 41):
+        p = np.array([0.5 + 0.45 * np.sin(1.7 * i), 0.5 + 0.45 * np.cos(2.3 * i),
+                      0.5 + 0.45 * np.sin(3.1 * i + 0.5)]) * box
+        o.add(p, species=orc.ION if i % 5 == 0 else orc.ELEC)
+    gen = o.accel("generic", False)
+    for kind in ("planar", "gather"):
+        a = o.accel(kind, False)
+        scale = np.maximum(np.linalg.norm(gen, axis=1), 1.0)
+        assert np.max(np.linalg.norm(a - gen, axis=1) / scale) < 1e-10, kind
+
+
+def test_beeman_kinematics(orc):
+    """Test_Beeman_Kinematics, src/mod_tests.F90:1403-1452 (exact after 3 steps)."""
+    k = orc.constants()
+    d, V, dt, vx0 = 1000 * NM, 2.0e3, 0.25e-15, 1.0e3
+    o = orc.OracleDiode(cap=4, V_s=V, d=d, time_step=dt, image_charge=False)
+    R0 = np.array([0.0, 0.0, 500 * NM])
+    o.add(R0, vel=[vx0, 0.0, 0.0])
+    for i in range(1, 4):
+        o.verlet(i)
+    az = k["q_0"] * V / (k["m_0"] * d)
+    pos, vel = o.arr("pos")[0], o.arr("vel")[0]
+    close((pos[2] - R0[2]) / NM, 4.5 * az * dt ** 2 / NM)
+    close(vel[2], 3.0 * az * dt)
+    close((pos[0] - R0[0]) / NM, 3.0 * vx0 * dt / NM)
+    close(vel[0], vx0)
+    close((pos[1] - R0[1]) / NM, 0.0)
+    close(o.s.ramo_current * 1e9, k["q_0"] * 3.0 * az * dt / d * 1e9)
+
+
+def test_transit_time(orc):
+    """Test_Transit_Time, src/mod_tests.F90:912-977 (within 1 %)."""
+    k = orc.constants()
+    d, V, dt = 1000 * NM, 2.0e3, 0.25e-15
+    z0 = 1.0 * NM
+    t_exp = np.sqrt(2.0 * d * (d - z0) * k["m_0"] / (k["q_0"] * V))
+    steps_exp = int(np.ceil(t_exp / dt))
+    o = orc.OracleDiode(cap=4, V_s=V, d=d, time_step=dt, image_charge=True, N_ic_max=0)
+    o.add([0.0, 0.0, z0])
+    steps_res = None
+    for i in range(1, steps_exp + 1000):
+        o.verlet(i)
+        o.remove(i)
+        if o.n == 0:
+            steps_res = i
+            break
+    assert steps_res is not None
+    assert abs(steps_exp - steps_res) < 0.01 * steps_exp
+
+
+def test_particle_removal(orc):
+    """Test_Particle_Removal, src/mod_tests.F90:1193-1289."""
+    k = orc.constants()
+    o = orc.OracleDiode(cap=16, V_s=2.0, d=100 * NM, image_charge=False)
+    spc = [orc.ELEC] * 7
+    spc[2] = spc[5] = orc.ION
+    R = np.array([[1.0 * i, -2.0 * i, 10.0 * i] for i in range(1, 8)]) * NM
+    V = np.array([[100.0 * i, -50.0 * i, 25.0 * i] for i in range(1, 8)])
+    for i in range(7):
+        o.add(R[i], vel=V[i], species=spc[i], step=1, sec=1)
+    assert o.n == 7
+    o.mark(1, orc.REMOVE_TOP)
+    o.mark(1, orc.REMOVE_TOP)
+    o.mark(3, orc.REMOVE_BOT)
+    o.mark(5, orc.REMOVE_TOP)
+    assert o.s.n_remove == 3 and o.s.n_remove_top == 1 and o.s.n_remove_bot == 1
+    assert o.arr("charge", 1)[1] == 0.0
+    o.remove(11)
+    assert o.n == 4
+    keep = [0, 2, 4, 6]
+    np.testing.assert_allclose(o.arr("pos"), R[keep], rtol=0, atol=0)
+    np.testing.assert_allclose(o.arr("vel"), V[keep], rtol=0, atol=0)
+    assert list(o.iarr("id")) == [0, 2, 4, 6]
+    assert list(o.iarr("species")) == [orc.ELEC, orc.ION, orc.ELEC, orc.ELEC]
+    close(o.arr("charge", 1)[0] / k["q_0"], -1.0)
+    close(o.arr("charge", 1)[1] / k["q_0"], 1.0)
+    lt = o.life_time()
+    assert lt[9, 0] == 2 and lt[9, 1] == 1
+    assert o.s.n_remove == 0
+
+
+def test_remove_all_particles(orc):
+    """Test_Remove_All_Particles, src/mod_tests.F90:1295-1328."""
+    o = orc.OracleDiode(cap=16, V_s=2.0, d=100 * NM, image_charge=False)
+    o.add(np.array([3.0, -10.0, 2.0]) * NM)
+    o.add(np.array([-9.0, 26.0, 80.0]) * NM)
+    o.mark(0, orc.REMOVE_TOP)
+    o.mark(1, orc.REMOVE_TOP)
+    o.remove(21)
+    assert o.n == 0 and o.s.n_remove == 0
+    assert o.life_time().sum() == 0          # nothing compacted, nothing recorded
+    R = np.array([5.0, 6.0, 50.0]) * NM
+    o.add(R, step=2)
+    assert o.n == 1
+    np.testing.assert_array_equal(o.arr("pos")[0], R)
+
+
+def test_work_function_checkerboard(orc):
+    """Test_Work_Function_Checkerboard, src/mod_tests.F90:1918-1978."""
+    L = orc.lib()
+    w = np.array([[4.10, 4.20], [4.30, 4.40]])
+    pos = np.array([0.0, 0.0])
+    dim = np.array([100.0, 100.0]) * NM
+    import ctypes as C
+    sec = C.c_int()
+
+    def at(x, y):
+        v = L.orc_work_checkerboard(orc.ptr(w), 2, 2, orc.ptr(pos), orc.ptr(dim), x * NM, y * NM,
+                                    C.byref(sec))
+        return v, sec.value
+
+    assert at(25, 25) == (4.30, 1)
+    assert at(75, 25) == (4.40, 2)
+    assert at(25, 75) == (4.10, 3)
+    assert at(75, 75) == (4.20, 4)
+    assert at(150, 25) == (4.40, 2)
+    assert at(-10, 130) == (4.10, 3)
+
+
+def test_tip_acceleration(orc):
+    """Test_Tip_Acceleration, src/mod_tests.F90:988-1084: the gather form
+    (the reference's device code) against the host pair loop, and the batch
+    field against the point-wise one."""
+    o = orc.OracleDiode(orc.TIP, cap=8, V_s=2.0e3, d=1000 * NM, time_step=0.25e-15,
+                        image_charge=True, N_ic_max=0)
+    o.set_tip(900 * NM, 100 * NM, 100 * NM, 4.7)
+    R = np.array([[2.0, 1.0, 103.0], [-2.0, 2.5, 106.0], [1.5, -3.0, 110.0]]) * NM
+    o.add(R[0]); o.add(R[1]); o.add(R[2], species=orc.ION)
+    exp = o.accel("generic", False)
+    got = o.accel("gather", False)
+    for i in range(3):
+        close(got[i], exp[i])
+        assert np.linalg.norm(got[i] - exp[i]) / np.linalg.norm(exp[i]) < 1e-12
+    pts = np.array([[0.0, 0.0, 102.0], [30.0, -10.0, 130.0], [-50.0, 40.0, 300.0], [15.0, 8.0, 500.0]]) * NM
+    b = o.field_at(pts)
+    for k in range(4):
+        close(b[k], o.field_at(pts[k:k + 1], compensated=False)[0])
+    # r_tip recomputed from R_base (Init_Emission_Tip :115-120)
+    d_t, h_t, Rb = 900 * NM, 100 * NM, 100 * NM
+    assert o.s.r_tip == pytest.approx(Rb ** 2 * d_t / (h_t ** 2 + 2 * d_t * h_t), rel=1e-12)
+
+
+def test_planar_system(orc):
+    """Test_Planar_System, src/mod_tests.F90:2013-2119: d = 500 nm, 1 kV,
+    100 x 100 nm emitter, phi = 2.0 eV (tests/work), 250 steps.  The
+    reference draws its random numbers from the compiler's RANDOM_NUMBER; the
+    oracle uses Philox streams, so only the reference's invariant and band
+    checks apply."""
+    k = orc.constants()
+    d, V, dt, n_steps, z_emit = 500 * NM, 1.0e3, 0.25e-15, 250, 1.0 * NM
+    o = orc.OracleDiode(cap=20000, V_s=V, d=d, time_step=dt, image_charge=True, N_ic_max=0)
+    o.set_planar_emitter(-50 * NM, -50 * NM, 100 * NM, 100 * NM, [[2.0]])
+    o.set_emission(True, seed=12345, mh_jumps=200, quad_panels=8, quad_order=4)
+    n_emit = n_top = n_bot = 0
+    Q = Q_ss = 0.0
+    bounds_ok = finite_ok = True
+    for i in range(1, n_steps + 1):
+        n_before = o.n
+        o.emission(i)
+        n_emit += o.n - n_before
+        o.verlet(i)
+        Q += o.s.ramo_current * dt
+        if i > n_steps // 2:
+            Q_ss += o.s.ramo_current * dt
+        n_top += o.s.n_remove_top
+        n_bot += o.s.n_remove_bot
+        o.remove(i)
+        if o.n:
+            z = o.arr("pos")[:, 2]
+            bounds_ok &= bool(np.all(z >= 0) and np.all(z <= d))
+            finite_ok &= bool(np.all(np.abs(o.arr("pos")) < 1.0))
+    sum_z = np.sum(o.arr("pos")[:, 2] - z_emit) if o.n else 0.0
+    Q_exp = k["q_0"] * (n_top * (d - z_emit) - n_bot * z_emit + sum_z) / d
+    I_ss = Q_ss / (dt * (n_steps - n_steps // 2))
+    assert n_emit > 100
+    assert n_top > 50
+    assert o.n == n_emit - n_top - n_bot
+    assert bounds_ok and finite_ok
+    assert abs(Q - Q_exp) < 0.10 * abs(Q_exp)
+    assert 0.5e-3 < I_ss < 4.0e-3, I_ss
