@@ -1,0 +1,431 @@
+#!/usr/bin/env python3
+"""Headline benchmark: electron-steps/s of the served FP32-compensated engine on
+the diode-request mix (Poisson arrivals at 20/s, per-request diodes drawn from
+the 128-diode batch distributions), against the plain FP64 one-diode-at-a-time
+GPU form and the CPU restatement of the reference path.
+
+A step is one serving iteration: admission of arrived requests, one time step
+(emission, Beeman update, all-pair forces, velocities, absorption/compaction)
+of every resident diode as one CUDA graph, per-diode counters back to the host
+and retirement of completed simulations.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NM = 1e-9
+METRIC = "electron-steps/s"
+SEED = 20261203
+
+
+# ---------------------------------------------------------------------------------
+# request stream: Poisson(20/s) arrivals; each request a planar diode with
+# peak electrons log-U[256, 32768], V U[0.5, 5] kV, gap U[200, 2000] nm,
+# work function U[2.5, 5.5] eV, square emitter side U[100, 2000] nm (centred),
+# dt = 0.25 fs, one image-charge partner, steps log-U[500, 20000], own seed.
+# Each is pre-filled with its peak electron count (x, y uniform over the
+# emitter footprint, z uniform in [1 nm, gap - 1 nm]).
+class RequestStream:
+    def __init__(self, seed=SEED, rate=20.0, horizon=300.0, rank=0):
+        self.rng = np.random.default_rng([seed, rank])
+        self.rate, self.horizon = rate, horizon
+        self.t = 0.0
+        self.k = 0
+
+    def next(self):
+        self.t += self.rng.exponential(1.0 / self.rate)
+        if self.t > self.horizon:
+            return None
+        r = self.rng
+        cap = int(round(math.exp(r.uniform(math.log(256), math.log(32768)))))
+        req = dict(arrival=self.t, index=self.k, capacity=cap,
+                   V_s=float(r.uniform(500.0, 5000.0)), gap=float(r.uniform(200.0, 2000.0)) * NM,
+                   phi=float(r.uniform(2.5, 5.5)), side=float(r.uniform(100.0, 2000.0)) * NM,
+                   steps=int(round(math.exp(r.uniform(math.log(500), math.log(20000))))),
+                   seed=int(r.integers(1, 2 ** 62)))
+        self.k += 1
+        return req
+
+
+def diode_kwargs(req, max_chains=0):
+    s = req["side"]
+    return dict(V_s=req["V_s"], gap=req["gap"], time_step=0.25e-15, image_charge=True, N_ic_max=0,
+                capacity=req["capacity"], emitter_pos=(-s / 2, -s / 2), emitter_dim=(s, s),
+                work=[[req["phi"]]], emission=True, max_chains=max_chains, seed=req["seed"])
+
+
+def prefill(req):
+    rng = np.random.default_rng(req["seed"] % (2 ** 32))
+    n, s, d = req["capacity"], req["side"], req["gap"]
+    return np.column_stack([rng.uniform(-s / 2, s / 2, n), rng.uniform(-s / 2, s / 2, n),
+                            rng.uniform(1 * NM, d - 1 * NM, n)])
+
+
+# ---------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1])); smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measure_fp32_peak():
+    """FP32 FMA throughput of this GPU: cuBLAS SGEMM with TF32 disabled."""
+    try:
+        import torch
+        torch.backends.cuda.matmul.allow_tf32 = False
+        torch.set_float32_matmul_precision("highest")
+        n = 8192
+        a = torch.randn(n, n, device="cuda")
+        b = torch.randn(n, n, device="cuda")
+        for _ in range(2):
+            a @ b
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(); a @ b; e1.record(); e1.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        return 2.0 * n ** 3 / best / 1e12
+    except Exception as exc:  # torch missing: nominal figure
+        print("fp32 peak probe failed: %s" % exc, file=sys.stderr)
+        return None
+
+
+class L2Flush:
+    """Writes a 256 MB buffer (twice the 129 MB L2) between timed iterations."""
+
+    def __init__(self):
+        self.buf = None
+        try:
+            import torch
+            self.buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        except Exception:
+            pass
+
+    def __call__(self):
+        if self.buf is not None:
+            self.buf.zero_()
+            import torch
+            torch.cuda.synchronize()
+
+
+# ---------------------------------------------------------------------------------
+def cpu_sample(stream_seed, budget_pairs=2.0e10, rank=0):
+    """The CPU restatement of the reference path (oracle, OpenMP, all host
+    threads) on a bounded sample: full time steps of the first requests of the
+    stream whose estimated cost fits the budget (the smallest diodes, which
+    favours the CPU).  Returns (electron-steps/s, sample description, cores)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import orc
+    orc.build()
+    st = RequestStream(stream_seed, rank=rank)
+    used, picked = 0.0, []
+    for _ in range(400):
+        r = st.next()
+        if r is None:
+            break
+        cost = 200.0 * r["capacity"] ** 2 + 4096.0 * r["capacity"] + r["capacity"] ** 2
+        if used + cost <= budget_pairs:
+            picked.append(r)
+            used += cost
+        if len(picked) >= 6:
+            break
+    e_steps, t_tot = 0, 0.0
+    for r in picked:
+        o = orc.OracleDiode(cap=r["capacity"], V_s=r["V_s"], d=r["gap"], time_step=0.25e-15,
+                            image_charge=True, N_ic_max=0)
+        s = r["side"]
+        o.set_planar_emitter(-s / 2, -s / 2, s, s, [[r["phi"]]])
+        o.set_emission(True, seed=r["seed"], mh_jumps=200, max_chains=r["capacity"],
+                       quad_panels=16, quad_order=4)
+        for p in prefill(r):
+            o.add(p, step=0)
+        t0 = time.perf_counter()
+        o.emission(1)
+        n = o.n
+        o.verlet(1)
+        o.remove(1)
+        t_tot += time.perf_counter() - t0
+        e_steps += n
+    cores = orc.lib().orc_omp_threads()
+    desc = ("1 full time step of each of %d stream requests (capacities %s) with the "
+            "oracle's OpenMP C restatement" % (len(picked), [r["capacity"] for r in picked]))
+    return (e_steps / t_tot if t_tot > 0 else 0.0), desc, cores, t_tot
+
+
+def plain_fp64_sample(rg, requests, budget_s=25.0):
+    """The plain FP64 GPU form, one diode at a time (own engine, rd_run per
+    diode), on a sample of the served requests."""
+    e_steps, dev_s, names = 0, 0.0, []
+    t_start = time.perf_counter()
+    for r in sorted(requests, key=lambda q: q["capacity"]):
+        if time.perf_counter() - t_start > budget_s:
+            break
+        eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=r["capacity"] + 64,
+                        chain_capacity=r["capacity"] + 64, quad_capacity=4096)
+        d = eng.add_diode(**diode_kwargs(r))
+        d.add_particles(prefill(r), step=0)
+        eng.run(1, 1)                     # first step (graph capture) untimed
+        n0 = d.counters()["electron_steps"]
+        eng.run(2, 1)
+        ms, _ = eng.last_run_stats()
+        e_steps += d.counters()["electron_steps"] - n0
+        dev_s += ms / 1e3
+        names.append(r["capacity"])
+        eng.close()
+    return (e_steps / dev_s if dev_s > 0 else 0.0), names
+
+
+# ---------------------------------------------------------------------------------
+def run_ours(args, rank, world):
+    import rumdeed_gb300 as rg
+    rg.build()
+    S = args.slots
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=S, particle_capacity=S * 32768 + 4096,
+                    chain_capacity=S * 32768 + 4096, quad_capacity=S * 4096 + 4096)
+    stream = RequestStream(SEED, rank=rank)
+    pending = stream.next()
+    submitted = {}
+    flush = L2Flush()
+    t0 = time.perf_counter()
+
+    def submit_arrived():
+        nonlocal pending
+        now = time.perf_counter() - t0
+        h2d = 0
+        while pending is not None and pending["arrival"] <= now:
+            pos = prefill(pending)
+            rid = eng.submit(pending["steps"], pos=pos, **diode_kwargs(pending))
+            submitted[rid] = pending
+            h2d += pos.nbytes
+            pending = stream.next()
+        return h2d
+
+    # warm-up: W iterations and until the slots are full (saturated server)
+    it = 0
+    while True:
+        submit_arrived()
+        st = eng.serve(1)
+        it += 1
+        if it >= args.warmup and (st["running"] >= S or pending is None):
+            break
+        if it > 100000:
+            break
+    # timed region
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    clocks.start()
+    dev_ms, wall_s, e_steps, h2d, d2h, admitted, retired = 0.0, 0.0, 0, 0, 0, 0, 0
+    step_ms = []
+    for k in range(args.steps):
+        flush()
+        w0 = time.perf_counter()
+        h2d += 0  # submissions are host-side copies into the engine's request queue
+        submit_arrived()
+        st = eng.serve(1)
+        wall_s += time.perf_counter() - w0
+        dev_ms += st["device_ms"]
+        step_ms.append(st["device_ms"])
+        e_steps += st["electron_steps"]
+        h2d += st["h2d_bytes"]
+        d2h += st["d2h_bytes"]
+        admitted += st["admitted"]
+        retired += st["retired"]
+    clk = clocks.stop()
+    running = st["running"]
+    queued = st["queued"]
+    _, kps = eng.last_run_stats()
+    # queueing delay of the requests admitted so far
+    qd = []
+    for rid in list(submitted)[:2000]:
+        s = eng.poll(rid)
+        if s["admit_s"] >= 0:
+            qd.append(s["admit_s"] - s["submit_s"])
+    # per-phase profile of one more step (dominant kernel: MH jump launches)
+    prof = eng.profile_step(eng_step := 10 ** 6)
+    resident = [submitted[r] for r in list(submitted) if eng.poll(r)["state"] == rg.REQ_RUNNING]
+    eng.close()
+
+    tot_dev = dev_ms / 1e3
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([tot_dev, wall_s, float(e_steps)], dtype=torch.float64, device="cuda")
+        mx = t.clone(); dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t.clone(); dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        tot_dev, wall_s, e_all = float(mx[0]), float(mx[1]), float(sm[2])
+    else:
+        e_all = float(e_steps)
+    value = e_all / tot_dev if tot_dev > 0 else 0.0
+    e2e = e_all / wall_s if wall_s > 0 else 0.0
+    if rank != 0:
+        return
+    # dominant kernel roofline (FP32 pipe; 20 flops per Coulomb-like term)
+    launches = max(prof["mh_jump_launches"], 1)
+    avg_ms = prof["mh_jumps_ms"] / launches
+    flops_per_launch = 20.0 * prof["mh_pair_evals"] / launches
+    achieved = flops_per_launch / (avg_ms / 1e3) / 1e12 if avg_ms > 0 else 0.0
+    peak = measure_fp32_peak()
+    peak_src = "measured: cuBLAS SGEMM 8192^3, TF32 off"
+    if peak is None:
+        peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        peak_src = "nominal: 152 SMs x 128 lanes x 2 x 2.07 GHz"
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "mh_jump_traffic.json")
+    if os.path.exists(tpath):
+        tj = json.load(open(tpath))
+        traffic = tj["dram_bytes_per_pair_eval"] * prof["mh_pair_evals"] / launches
+    plain_v, plain_caps = plain_fp64_sample(rg, resident, budget_s=args.plain_budget)
+    cpu_v, cpu_desc, cores, cpu_t = cpu_sample(SEED, rank=rank)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 pair sums (compensated) + f64 integration/FN",
+        "data": "synthetic request stream (seeded; configs[3] distributions)",
+        "config": {"workload": "serve: Poisson 20/s planar-diode requests, configs[2] distributions, "
+                               "pre-filled to peak N, MH 200 jumps, chains capped at capacity",
+                   "slots": S, "precision": "fp32c", "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "l2": "256 MB buffer written between timed iterations",
+                   "resident_diodes": running, "queued_requests": queued,
+                   "admitted_in_timed": admitted, "retired_in_timed": retired},
+        "latency": {"step_ms_p50": float(np.percentile(step_ms, 50)),
+                    "step_ms_p99": float(np.percentile(step_ms, 99)),
+                    "step_ms_max": float(max(step_ms)),
+                    "queueing_delay_s_p50": float(np.percentile(qd, 50)) if qd else None,
+                    "queueing_delay_s_p99": float(np.percentile(qd, 99)) if qd else None,
+                    "simulation_latency": "no simulation completes inside the window: "
+                                          "projected = steps x step time (>= 500 steps)"},
+        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": h2d / max(args.steps, 1),
+                "d2h_bytes_per_step": d2h / max(args.steps, 1)},
+        "plain_fp64_one_diode_at_a_time": {"value": plain_v, "unit": METRIC,
+                                           "sample_capacities": plain_caps,
+                                           "served_over_plain": value / plain_v if plain_v else None},
+        "gpu_launches": args.steps * (kps + 1) + 2 * admitted,
+        "roofline": {"bound": "fp32", "kernel": "k_mh_jump_planar<fp32c>",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": traffic,
+                     "peak_source": peak_src,
+                     "flops_convention": "20 flops per Coulomb-like term (Nyland et al.); "
+                                         "1 term per (chain, particle) at the cathode"},
+        "phase_ms": {k: prof[k] for k in ("supply_ms", "mh_init_ms", "mh_jumps_ms", "emit_ms",
+                                          "position_ms", "force_ms", "velocity_ms", "compact_ms",
+                                          "total_ms")},
+        "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cores, "kind": "port",
+                         "sample": cpu_desc, "seconds": cpu_t},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    vals, t_all = [], 0.0
+    desc, cores = "", 0
+    for k in range(args.warmup + args.steps):
+        v, desc, cores, t = cpu_sample(SEED, budget_pairs=args.ref_budget, rank=0)
+        if k >= args.warmup:
+            vals.append(v)
+            t_all += t
+    value = statistics.median(vals) if vals else 0.0
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_all / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic request stream (seeded; configs[3] distributions)",
+            "config": {"workload": "serve: Poisson 20/s planar-diode requests (bounded CPU sample)"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
+                             "sample": desc + " (the Fortran reference cannot be built here: no "
+                                              "Fortran compiler, Cuba 4.2.2 not vendored)"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--slots", type=int, default=128)
+    ap.add_argument("--plain-budget", type=float, default=20.0)
+    ap.add_argument("--ref-budget", type=float, default=1.0e10)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

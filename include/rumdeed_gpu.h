@@ -154,6 +154,64 @@ int rd_life_time(rd_engine* e, int diode, int* hist1000);
  * stream) and launches of library kernels per step. */
 int rd_last_run_stats(rd_engine* e, double* ms, int* kernels_per_step);
 
+/* ---- tracing: per-phase device times of one step --------------------------
+ * The reference has only wall-clock stamps at start and end of the run
+ * (src/main.F90:51,267).  rd_profile_step runs one main-loop iteration
+ * uncaptured with CUDA events between the phases and reports their device
+ * times and work. */
+typedef struct {
+  double supply_ms, mh_init_ms, mh_jumps_ms, emit_ms;
+  double position_ms, force_ms, velocity_ms, compact_ms, total_ms;
+  int mh_jump_launches;
+  long long mh_pair_evals;   /* sum over jump launches of chains x particles */
+  long long force_pairs;     /* sum over diodes of n (n - 1) */
+  long long supply_pair_evals;
+} rd_phase_times;
+int rd_profile_step(rd_engine* e, int step, rd_phase_times* out);
+
+/* ---- serving: continuous batching of diode simulations ---------------------
+ * The reference runs one simulation per process.  Requests queue in FIFO
+ * order; rd_serve admits the queue head whenever a diode slot, a particle-pool
+ * range of its capacity (its peak electron count, i.e. HBM) and a chain range
+ * are free, advances every admitted simulation by one time step per
+ * iteration (one graph launch), and retires simulations that completed their
+ * step count, freeing their slot for the next request.  Each simulation
+ * counts its own steps from 1, so its result does not depend on what else
+ * is resident. */
+typedef struct {
+  rd_diode_config diode;
+  int steps;               /* time steps to simulate */
+  int n_init;              /* initial electrons (copied at submit) */
+  const double* pos3n;     /* (3, n_init) positions */
+  const double* vel3n;     /* (3, n_init) velocities or NULL */
+} rd_request;
+
+enum { RD_REQ_QUEUED = 0, RD_REQ_RUNNING = 1, RD_REQ_DONE = 2, RD_REQ_CANCELLED = 3 };
+
+typedef struct {
+  int state;
+  int diode;               /* slot while running, -1 otherwise */
+  int steps;
+  double submit_s, admit_s, done_s;   /* engine clock, seconds */
+  rd_counters counters;    /* latest counters (final once done) */
+} rd_request_status;
+
+typedef struct {
+  int iterations;          /* serving iterations run by the call */
+  int admitted, retired, running, queued;
+  double device_ms;        /* sum of per-iteration device times */
+  double wall_ms;          /* host wall time of the call */
+  long long electron_steps;/* electrons in flight summed over diodes and iterations */
+  double step_ms_p50, step_ms_p99, step_ms_max;   /* per-iteration device time */
+  long long h2d_bytes, d2h_bytes;
+} rd_serve_stats;
+
+int rd_submit(rd_engine* e, const rd_request* req, long long* id);
+int rd_poll(rd_engine* e, long long id, rd_request_status* out);
+int rd_cancel(rd_engine* e, long long id);
+int rd_serve(rd_engine* e, int iterations, rd_serve_stats* out);
+int rd_clock(rd_engine* e, double* seconds);
+
 #ifdef __cplusplus
 }
 #endif

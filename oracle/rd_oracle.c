@@ -458,6 +458,7 @@ void orc_accel_planar(const orc_diode* s, double* acc, int comp) {
 void orc_accel_gather(const orc_diode* s, double* acc, int comp) {
   init_constants();
   int n = s->n;
+#pragma omp parallel for schedule(dynamic, 16)
   for (int i = 0; i < n; ++i) {
     const double* p1 = s->pos + 3 * i;
     double q1 = s->charge[i], qd1 = q1 * DIV_FAC_C;
@@ -509,6 +510,7 @@ void orc_field_at(const orc_diode* s, const double p[3], double out[3], int comp
 }
 
 void orc_field_at_batch(const orc_diode* s, int M, const double* pts, double* out, int comp) {
+#pragma omp parallel for schedule(dynamic, 4)
   for (int m = 0; m < M; ++m) orc_field_at(s, pts + 3 * m, out + 3 * m, comp);
 }
 
@@ -732,23 +734,26 @@ double orc_supply_integral_planar(orc_diode* s) {
   double gx[16], gw[16];
   gauss_legendre(Q, gx, gw);
   double A = s->em_dim[0] * s->em_dim[1];
-  nsum tot = {0, 0};
   int npt = P * Q;
-  for (int iy = 0; iy < npt; ++iy) {
+  double* val = (double*)calloc((size_t)npt * npt, sizeof(double));
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int k = 0; k < npt * npt; ++k) {
+    int iy = k / npt, ix = k % npt;
     double uy = ((iy / Q) + 0.5 * (gx[iy % Q] + 1.0)) / P;
     double wy = 0.5 * gw[iy % Q] / P;
-    for (int ix = 0; ix < npt; ++ix) {
-      double ux = ((ix / Q) + 0.5 * (gx[ix % Q] + 1.0)) / P;
-      double wx = 0.5 * gw[ix % Q] / P;
-      double p[3] = {s->em_pos[0] + ux * s->em_dim[0], s->em_pos[1] + uy * s->em_dim[1], 0.0};
-      double f[3];
-      orc_field_at(s, p, f, 1);
-      if (f[2] < 0.0) {
-        double phi = work_at(s, p[0], p[1], NULL);
-        nadd(&tot, (wx * wy) * (A * orc_elec_supply_v2(f[2], phi, s->image_charge, s->time_step)));
-      }
+    double ux = ((ix / Q) + 0.5 * (gx[ix % Q] + 1.0)) / P;
+    double wx = 0.5 * gw[ix % Q] / P;
+    double p[3] = {s->em_pos[0] + ux * s->em_dim[0], s->em_pos[1] + uy * s->em_dim[1], 0.0};
+    double f[3];
+    orc_field_at(s, p, f, 1);
+    if (f[2] < 0.0) {
+      double phi = work_at(s, p[0], p[1], NULL);
+      val[k] = (wx * wy) * (A * orc_elec_supply_v2(f[2], phi, s->image_charge, s->time_step));
     }
   }
+  nsum tot = {0, 0};
+  for (int k = 0; k < npt * npt; ++k) if (val[k] != 0.0) nadd(&tot, val[k]);
+  free(val);
   return nval(&tot);
 }
 
@@ -767,6 +772,7 @@ void orc_mh_batch_planar(orc_diode* s, int step, int M, double* df_out, double* 
   int ndim = s->mh_jumps, ndim_first = (int)nint_f(ndim * 0.25);
   double* sup = (double*)malloc(sizeof(double) * (M > 0 ? M : 1));
   double std[2] = {s->em_dim[0] * 0.10, s->em_dim[1] * 0.10};
+#pragma omp parallel for schedule(dynamic, 1)
   for (int c = 0; c < M; ++c) {
     ok[c] = 0;
     for (int r = 0; r < s->init_rounds_max; ++r) {
@@ -793,6 +799,7 @@ void orc_mh_batch_planar(orc_diode* s, int step, int M, double* df_out, double* 
   for (int it = 1; it <= ndim && any_ok; ++it) {
     if (it > ndim_first) { std[0] = s->em_dim[0] * s->MH_std; std[1] = s->em_dim[1] * s->MH_std; }
     int acc = 0, rej = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : acc, rej)
     for (int c = 0; c < M; ++c) {
       if (!ok[c]) continue;
       double g1, g2;
@@ -881,21 +888,24 @@ static double tip_supply_log_target(const orc_diode* s, double F, double xi) {
 double orc_supply_tip(orc_diode* s) {
   const int nr = 100;
   double len_phi = 2.0 * PI / nr, len_xi = (s->max_xi - 1.0) / nr;
-  nsum ns = {0, 0};
-  for (int i = 1; i <= nr; ++i) {
-    for (int j = 1; j <= nr; ++j) {
-      double xi_c = 1.0 + (i - 0.5) * len_xi, phi_c = (j - 0.5) * len_phi;
-      double p[3];
-      orc_tip_xyz(s, xi_c, s->eta_1, phi_c, p);
-      double F = field_normal(s, p);
-      if (F < 0.0) {
-        double A = orc_tip_area(s, 1.0 + (i - 1.0) * len_xi, 1.0 + (i + 0.0) * len_xi,
-                                (j - 1.0) * len_phi, (j + 0.0) * len_phi);
-        double t = orc_t_y(F, s->tip_phi, s->image_charge);       /* Elec_Supply :1710-1718 */
-        nadd(&ns, (((A * A_FN) * (F * F)) * s->time_step) / ((Q_0 * s->tip_phi) * (t * t)));
-      }
+  double* val = (double*)calloc((size_t)nr * nr, sizeof(double));
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int k = 0; k < nr * nr; ++k) {
+    int i = k / nr + 1, j = k % nr + 1;
+    double xi_c = 1.0 + (i - 0.5) * len_xi, phi_c = (j - 0.5) * len_phi;
+    double p[3];
+    orc_tip_xyz(s, xi_c, s->eta_1, phi_c, p);
+    double F = field_normal(s, p);
+    if (F < 0.0) {
+      double A = orc_tip_area(s, 1.0 + (i - 1.0) * len_xi, 1.0 + (i + 0.0) * len_xi,
+                              (j - 1.0) * len_phi, (j + 0.0) * len_phi);
+      double t = orc_t_y(F, s->tip_phi, s->image_charge);       /* Elec_Supply :1710-1718 */
+      val[k] = (((A * A_FN) * (F * F)) * s->time_step) / ((Q_0 * s->tip_phi) * (t * t));
     }
   }
+  nsum ns = {0, 0};
+  for (int k = 0; k < nr * nr; ++k) if (val[k] != 0.0) nadd(&ns, val[k]);
+  free(val);
   return nval(&ns);
 }
 
@@ -908,6 +918,7 @@ void orc_mh_batch_tip(orc_diode* s, int step, int M, double* df_out, double* F_o
   double* xi = (double*)malloc(sizeof(double) * (M > 0 ? M : 1));
   double* ph = (double*)malloc(sizeof(double) * (M > 0 ? M : 1));
   double std[2] = {(s->max_xi - 1.0) * 0.10, (2.0 * PI) * 0.10};
+#pragma omp parallel for schedule(dynamic, 1)
   for (int c = 0; c < M; ++c) {
     ok[c] = 0;
     for (int r = 0; r < s->init_rounds_max; ++r) {
@@ -934,6 +945,7 @@ void orc_mh_batch_tip(orc_diode* s, int step, int M, double* df_out, double* F_o
   for (int it = 1; it <= ndim && any_ok; ++it) {
     if (it > ndim_first) { std[0] = (s->max_xi - 1.0) * s->MH_std; std[1] = (2.0 * PI) * s->MH_std; }
     int acc = 0, rej = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : acc, rej)
     for (int c = 0; c < M; ++c) {
       if (!ok[c]) continue;
       double g1, g2;

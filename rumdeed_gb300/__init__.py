@@ -74,6 +74,48 @@ class Counters(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class PhaseTimes(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("supply_ms", "mh_init_ms", "mh_jumps_ms", "emit_ms",
+                                          "position_ms", "force_ms", "velocity_ms", "compact_ms",
+                                          "total_ms")] + \
+               [("mh_jump_launches", C.c_int), ("mh_pair_evals", C.c_longlong),
+                ("force_pairs", C.c_longlong), ("supply_pair_evals", C.c_longlong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Request(C.Structure):
+    _fields_ = [("diode", DiodeConfig), ("steps", C.c_int), ("n_init", C.c_int),
+                ("pos3n", C.POINTER(C.c_double)), ("vel3n", C.POINTER(C.c_double))]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_int), ("diode", C.c_int), ("steps", C.c_int),
+                ("submit_s", C.c_double), ("admit_s", C.c_double), ("done_s", C.c_double),
+                ("counters", Counters)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "counters"}
+        d["counters"] = self.counters.as_dict()
+        return d
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("admitted", C.c_int), ("retired", C.c_int),
+                ("running", C.c_int), ("queued", C.c_int), ("device_ms", C.c_double),
+                ("wall_ms", C.c_double), ("electron_steps", C.c_longlong),
+                ("step_ms_p50", C.c_double), ("step_ms_p99", C.c_double),
+                ("step_ms_max", C.c_double), ("h2d_bytes", C.c_longlong),
+                ("d2h_bytes", C.c_longlong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED = 0, 1, 2, 3
+
+
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _lib = None
@@ -102,6 +144,12 @@ SIGNATURES = {
     "rd_counters_get": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Counters)]),
     "rd_life_time": (C.c_int, [C.c_void_p, C.c_int, _ip]),
     "rd_last_run_stats": (C.c_int, [C.c_void_p, _dp, _ip]),
+    "rd_profile_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(PhaseTimes)]),
+    "rd_submit": (C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_longlong)]),
+    "rd_poll": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(RequestStatus)]),
+    "rd_cancel": (C.c_int, [C.c_void_p, C.c_longlong]),
+    "rd_serve": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(ServeStats)]),
+    "rd_clock": (C.c_int, [C.c_void_p, _dp]),
 }
 
 
@@ -176,35 +224,8 @@ class Engine:
         self.close()
 
     # diode slots ---------------------------------------------------------------
-    def add_diode(self, geometry=GEOM_PLANAR, V_s=2.0e3, gap=1000e-9, time_step=0.25e-15,
-                  image_charge=True, N_ic_max=0, capacity=4096, emitter_pos=(0.0, 0.0),
-                  emitter_dim=(0.0, 0.0), work=None, tip_dim=(0.0, 0.0, 0.0),
-                  tip_work_function=4.7, emission=False, mh_jumps=0, max_chains=0,
-                  quad_panels=0, quad_order=0, init_rounds=0, seed=1):
-        cfg = DiodeConfig()
-        cfg.geometry = geometry
-        cfg.V_s = V_s
-        cfg.gap = gap
-        cfg.time_step = time_step
-        cfg.image_charge = int(bool(image_charge))
-        cfg.N_ic_max = N_ic_max
-        cfg.capacity = capacity
-        cfg.emitter_pos[:] = list(emitter_pos)
-        cfg.emitter_dim[:] = list(emitter_dim)
-        keep = None
-        if work is not None:
-            keep = np.ascontiguousarray(work, dtype=np.float64)
-            cfg.work_ny, cfg.work_nx = keep.shape
-            cfg.work = keep.ctypes.data_as(_dp)
-        cfg.tip_dim[:] = list(tip_dim)
-        cfg.tip_work_function = tip_work_function
-        cfg.emission = int(bool(emission))
-        cfg.mh_jumps = mh_jumps
-        cfg.max_chains = max_chains
-        cfg.quad_panels = quad_panels
-        cfg.quad_order = quad_order
-        cfg.init_rounds = init_rounds
-        cfg.seed = seed
+    def add_diode(self, **kw):
+        cfg, keep = diode_config(**kw)
         d = C.c_int()
         _check(self.L.rd_diode_add(self.h, C.byref(cfg), C.byref(d)))
         del keep
@@ -216,6 +237,48 @@ class Engine:
         idx = diode.index if isinstance(diode, Diode) else int(diode)
         _check(self.L.rd_diode_remove(self.h, idx))
         self.diodes.pop(idx, None)
+
+    # tracing -------------------------------------------------------------------
+    def profile_step(self, step):
+        """One main-loop iteration with CUDA-event timers between the phases."""
+        t = PhaseTimes()
+        _check(self.L.rd_profile_step(self.h, step, C.byref(t)))
+        return t.as_dict()
+
+    # serving -------------------------------------------------------------------
+    def submit(self, steps, pos=None, vel=None, **diode_kw):
+        cfg, keep = diode_config(**diode_kw)
+        req = Request()
+        req.diode = cfg
+        req.steps = steps
+        p = None if pos is None else _vec3(pos)
+        v = None if vel is None else _vec3(vel)
+        req.n_init = 0 if p is None else p.shape[0]
+        req.pos3n = _p(p)
+        req.vel3n = _p(v)
+        i = C.c_longlong()
+        _check(self.L.rd_submit(self.h, C.byref(req), C.byref(i)))
+        del keep
+        return i.value
+
+    def poll(self, rid):
+        st = RequestStatus()
+        _check(self.L.rd_poll(self.h, rid, C.byref(st)))
+        return st.as_dict()
+
+    def cancel(self, rid):
+        _check(self.L.rd_cancel(self.h, rid))
+
+    def serve(self, iterations=1):
+        st = ServeStats()
+        _check(self.L.rd_serve(self.h, iterations, C.byref(st)))
+        return st.as_dict()
+
+    def clock(self):
+        t = C.c_double()
+        _check(self.L.rd_clock(self.h, C.byref(t)))
+        return t.value
+
 
     # main-loop phases (all diodes) ----------------------------------------------
     def do_emission(self, step):
@@ -244,6 +307,39 @@ class Engine:
         k = C.c_int()
         _check(self.L.rd_last_run_stats(self.h, C.byref(ms), C.byref(k)))
         return ms.value, k.value
+
+
+def diode_config(geometry=GEOM_PLANAR, V_s=2.0e3, gap=1000e-9, time_step=0.25e-15,
+             image_charge=True, N_ic_max=0, capacity=4096, emitter_pos=(0.0, 0.0),
+             emitter_dim=(0.0, 0.0), work=None, tip_dim=(0.0, 0.0, 0.0),
+             tip_work_function=4.7, emission=False, mh_jumps=0, max_chains=0,
+             quad_panels=0, quad_order=0, init_rounds=0, seed=1):
+    """rd_diode_config from keyword arguments (the /input/ namelist of one run)."""
+    cfg = DiodeConfig()
+    cfg.geometry = geometry
+    cfg.V_s = V_s
+    cfg.gap = gap
+    cfg.time_step = time_step
+    cfg.image_charge = int(bool(image_charge))
+    cfg.N_ic_max = N_ic_max
+    cfg.capacity = capacity
+    cfg.emitter_pos[:] = list(emitter_pos)
+    cfg.emitter_dim[:] = list(emitter_dim)
+    keep = None
+    if work is not None:
+        keep = np.ascontiguousarray(work, dtype=np.float64)
+        cfg.work_ny, cfg.work_nx = keep.shape
+        cfg.work = keep.ctypes.data_as(_dp)
+    cfg.tip_dim[:] = list(tip_dim)
+    cfg.tip_work_function = tip_work_function
+    cfg.emission = int(bool(emission))
+    cfg.mh_jumps = mh_jumps
+    cfg.max_chains = max_chains
+    cfg.quad_panels = quad_panels
+    cfg.quad_order = quad_order
+    cfg.init_rounds = init_rounds
+    cfg.seed = seed
+    return cfg, keep
 
 
 class Diode:

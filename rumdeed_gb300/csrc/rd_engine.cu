@@ -12,6 +12,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <deque>
+#include <map>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -223,6 +226,22 @@ struct rd_engine {
   double last_ms = 0.0;
   int last_kernels = 0;
   int kernels_in_step = 0;
+  // serving
+  struct Req {
+    rd_diode_config cfg{};
+    std::vector<double> work, pos, vel;
+    int steps = 0;
+    rd_request_status st{};
+  };
+  std::map<long long, Req> reqs;
+  std::deque<long long> queue;
+  std::map<int, long long> running;   // slot -> request id
+  long long next_id = 1;
+  int gstep = 1;                       // engine step of the next serving launch
+  std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+  double clock() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
 
   template <class T>
   cudaError_t dalloc(T** p, size_t count) {
@@ -230,11 +249,9 @@ struct rd_engine {
     if (e == cudaSuccess) allocs.push_back((void*)*p);
     return e;
   }
-  int nslots_hw() const {
-    int hw = 0;
-    for (size_t s = 0; s < slots.size(); ++s) if (slots[s].used) hw = (int)s + 1;
-    return hw > 0 ? hw : 1;
-  }
+  // Launch shapes cover every slot (inactive ones exit at once), so the
+  // captured step graph stays valid while requests come and go.
+  int nslots_hw() const { return cfg.max_diodes; }
 };
 
 static int alloc_pool(rd_engine* e, Pool& P, long long cap) {
@@ -309,7 +326,7 @@ static int launch_emission(rd_engine* e) {
     CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH],
                          e->ph[PM_MH], e->cs, e->d_choff, e->work, e->d_step, it, e->partial,
                          e->tickets, e->kscale));
-    e->kernels_in_step += (gmask == 3) ? 2 : 1;
+    e->kernels_in_step += (gmask == 3) ? 3 : 2;   // propose + jump kernel(s)
   }
   CK(rd_launch_emit(ns, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step));
   e->kernels_in_step++;
@@ -372,8 +389,7 @@ static int launch_step_body(rd_engine* e) {
 static std::string sig_string(rd_engine* e) {
   Sig s = signature(e);
   char b[128];
-  snprintf(b, sizeof b, "%d%d%d%d%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
-           s.jumps, e->nslots_hw());
+  snprintf(b, sizeof b, "%d%d%d%d%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic, s.jumps);
   return b;
 }
 
@@ -454,7 +470,12 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   const int S = cfg->max_diodes;
   const long long chcap = std::max<long long>(cfg->chain_capacity, 1);
   const long long qcap = std::max<long long>(cfg->quad_capacity, 1);
-  e->max_items = std::max(65536, 4 * target_items(e));
+  // scratch bound: the planner grows the chunk length until the items fit,
+  // and with one chunk per tile every mode has at most capacity/128 + slots tiles
+  // scratch bound: at most 8 chunks per tile (RD_NCH_MAX) and at most
+  // capacity/128 + slots tiles in any pair sum
+  e->max_items = (int)std::min<long long>(
+      1 << 26, 8LL * (std::max(cap, std::max(chcap, qcap)) / RD_ITILE + 4LL * S) + 65536);
   if ((rc = alloc_pool(e, e->pool, cap)) || (rc = alloc_pool(e, e->tmp, cap))) return bail(rc);
   if (e->dalloc(&e->dP, S) || e->dalloc(&e->dD, S) || e->dalloc(&e->work, (size_t)S * 4 + 4096) ||
       e->dalloc(&e->qx, qcap) || e->dalloc(&e->qy, qcap) || e->dalloc(&e->qz, qcap) ||
@@ -779,9 +800,20 @@ int rd_accel(rd_engine* e, int d, double* acc3n) {
   return RD_OK;
 }
 
+static int field_at_batch(rd_engine* e, int d, int M, const double* pos, double* field);
+
 int rd_field_at(rd_engine* e, int d, int M, const double* pos, double* field) {
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (M < 0 || (M > 0 && (!pos || !field))) return fail(RD_ERR_INVALID, "bad point arrays");
+  const int chunk = (e->max_items / 2) * RD_ITILE;
+  for (int m0 = 0; m0 < M; m0 += chunk) {
+    int rc = field_at_batch(e, d, std::min(chunk, M - m0), pos + 3LL * m0, field + 3LL * m0);
+    if (rc) return rc;
+  }
+  return RD_OK;
+}
+
+static int field_at_batch(rd_engine* e, int d, int M, const double* pos, double* field) {
   if (M == 0) return RD_OK;
   if (M > e->fcap) {
     if (e->fpx) { cudaFree(e->fpx); cudaFree(e->fpy); cudaFree(e->fpz); cudaFree(e->ffx); cudaFree(e->ffy); cudaFree(e->ffz); }
@@ -897,6 +929,256 @@ int rd_last_run_stats(rd_engine* e, double* ms, int* kps) {
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   if (ms) *ms = e->last_ms;
   if (kps) *kps = e->last_kernels;
+  return RD_OK;
+}
+
+static void fill_counters(const DiodeDyn& y, rd_counters* o) {
+  o->n = y.n;
+  o->emitted_step = y.emitted_step; o->dropped_step = y.dropped_step;
+  o->absorbed_top_step = y.absorbed_top_step; o->absorbed_bot_step = y.absorbed_bot_step;
+  o->chains = y.chains; o->chains_failed = y.chains_failed; o->chains_capped = y.chains_capped;
+  o->emitted_total = y.emitted_total; o->dropped_total = y.dropped_total;
+  o->absorbed_top_total = y.absorbed_top_total; o->absorbed_bot_total = y.absorbed_bot_total;
+  o->electron_steps = y.electron_steps; o->steps_done = y.steps_done;
+  o->ramo_current = y.ramo_current; o->N_sup = y.N_sup; o->MH_std = y.MH_std;
+  o->a_rate = y.a_rate; o->residual = y.residual;
+}
+
+int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
+  if (!e || !out) return fail(RD_ERR_INVALID, "null argument");
+  *out = rd_phase_times{};
+  const int S = e->cfg.max_diodes;
+  cudaEvent_t ev[9];
+  for (auto& v : ev) CK(cudaEventCreate(&v));
+  struct Guard { cudaEvent_t* v; ~Guard() { for (int k = 0; k < 9; ++k) cudaEventDestroy(v[k]); } } guard{ev};
+  Sig s = signature(e);
+  const int prec = e->cfg.precision;
+  std::vector<DiodeDyn> dyn(S);
+  CK(rd_launch_step_set(e->st, e->d_step, step));
+  CK(cudaEventRecord(ev[0], e->st));
+  if (s.emit_planar || s.emit_tip) {
+    // supply integral
+    if (s.emit_planar) {
+      CK(plan(e, PM_SUPPLY_PLANAR));
+      CK(rd_launch_z0_points(prec, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_PLANAR],
+                             e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qF, e->partial, e->tickets, e->kscale));
+    }
+    if (s.emit_tip) {
+      CK(plan(e, PM_SUPPLY_TIP));
+      PointSet pts{e->qx, e->qy, e->qz, e->qfx, e->qfy, e->qF, e->d_qoff};
+      CK(rd_launch_field_points(prec, RD_G_TIP, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_TIP],
+                                e->ph[PM_SUPPLY_TIP], pts, e->partial, e->tickets, e->kscale));
+    }
+    CK(rd_launch_supply_reduce(S, e->st, e->dP, e->dD, e->qx, e->qy, e->qw, e->qF, e->qfx, e->qfy, e->work));
+    CK(cudaEventRecord(ev[1], e->st));
+    CK(cudaMemcpyAsync(dyn.data(), e->dD, sizeof(DiodeDyn) * S, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    for (int d = 0; d < S; ++d) {
+      const SlotHost& sl = e->slots[d];
+      if (!sl.used || !sl.p.emission) continue;
+      long long npt = sl.p.geometry == RD_G_TIP ? 10000 : (long long)sl.p.quad_n * sl.p.quad_n;
+      out->supply_pair_evals += npt * dyn[d].n;
+      out->mh_pair_evals += (long long)dyn[d].chains * dyn[d].n * sl.p.mh_jumps;
+    }
+    CK(plan(e, PM_MH));
+    CK(rd_launch_mh_init(prec, e->grid * 4, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                         e->cs, e->d_choff, e->work, e->d_step, e->kscale));
+    CK(cudaEventRecord(ev[2], e->st));
+    const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
+    for (int it = 1; it <= s.jumps; ++it)
+      CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                           e->cs, e->d_choff, e->work, e->d_step, it, e->partial, e->tickets, e->kscale));
+    out->mh_jump_launches = s.jumps * ((gmask == 3) ? 2 : 1);
+    CK(cudaEventRecord(ev[3], e->st));
+    CK(rd_launch_emit(S, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step));
+  } else {
+    CK(cudaEventRecord(ev[1], e->st));
+    CK(cudaEventRecord(ev[2], e->st));
+    CK(cudaEventRecord(ev[3], e->st));
+  }
+  CK(cudaEventRecord(ev[4], e->st));
+  CK(plan(e, PM_PART));
+  CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART]));
+  CK(cudaEventRecord(ev[5], e->st));
+  int rc = launch_force(e);
+  if (rc) return rc;
+  CK(cudaEventRecord(ev[6], e->st));
+  CK(rd_launch_velocity(e->grid, S, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->ramo));
+  CK(cudaEventRecord(ev[7], e->st));
+  CK(cudaMemcpyAsync(dyn.data(), e->dD, sizeof(DiodeDyn) * S, cudaMemcpyDeviceToHost, e->st));
+  rc = launch_remove(e);
+  if (rc) return rc;
+  CK(rd_launch_step_inc(e->st, e->d_step));
+  CK(cudaEventRecord(ev[8], e->st));
+  CK(cudaStreamSynchronize(e->st));
+  for (int d = 0; d < S; ++d)
+    if (e->slots[d].used) out->force_pairs += (long long)dyn[d].n * (dyn[d].n > 0 ? dyn[d].n - 1 : 0);
+  float t[8];
+  for (int k = 0; k < 8; ++k) CK(cudaEventElapsedTime(&t[k], ev[k], ev[k + 1]));
+  out->supply_ms = t[0]; out->mh_init_ms = t[1]; out->mh_jumps_ms = t[2]; out->emit_ms = t[3];
+  out->position_ms = t[4]; out->force_ms = t[5]; out->velocity_ms = t[6]; out->compact_ms = t[7];
+  float tot;
+  CK(cudaEventElapsedTime(&tot, ev[0], ev[8]));
+  out->total_ms = tot;
+  return RD_OK;
+}
+
+// ---- serving --------------------------------------------------------------------------
+int rd_clock(rd_engine* e, double* seconds) {
+  if (!e || !seconds) return fail(RD_ERR_INVALID, "null argument");
+  *seconds = e->clock();
+  return RD_OK;
+}
+
+int rd_submit(rd_engine* e, const rd_request* req, long long* id) {
+  if (!e || !req || !id) return fail(RD_ERR_INVALID, "null argument");
+  if (req->steps <= 0 || req->n_init < 0 || (req->n_init > 0 && !req->pos3n))
+    return fail(RD_ERR_INVALID, "bad request");
+  if (req->n_init > req->diode.capacity) return fail(RD_ERR_INVALID, "n_init exceeds capacity");
+  rd_engine::Req r;
+  r.cfg = req->diode;
+  if (req->diode.work && req->diode.work_nx > 0 && req->diode.work_ny > 0) {
+    r.work.assign(req->diode.work, req->diode.work + (size_t)req->diode.work_nx * req->diode.work_ny);
+  }
+  r.cfg.work = nullptr;
+  if (req->n_init > 0) {
+    r.pos.assign(req->pos3n, req->pos3n + 3LL * req->n_init);
+    if (req->vel3n) r.vel.assign(req->vel3n, req->vel3n + 3LL * req->n_init);
+  }
+  r.steps = req->steps;
+  r.st.state = RD_REQ_QUEUED;
+  r.st.diode = -1;
+  r.st.steps = req->steps;
+  r.st.submit_s = e->clock();
+  r.st.admit_s = r.st.done_s = -1.0;
+  long long k = e->next_id++;
+  e->reqs[k] = std::move(r);
+  e->queue.push_back(k);
+  *id = k;
+  return RD_OK;
+}
+
+int rd_poll(rd_engine* e, long long id, rd_request_status* out) {
+  if (!e || !out) return fail(RD_ERR_INVALID, "null argument");
+  auto it = e->reqs.find(id);
+  if (it == e->reqs.end()) return fail(RD_ERR_NOTFOUND, "unknown request");
+  *out = it->second.st;
+  return RD_OK;
+}
+
+int rd_cancel(rd_engine* e, long long id) {
+  if (!e) return fail(RD_ERR_INVALID, "null engine");
+  auto it = e->reqs.find(id);
+  if (it == e->reqs.end()) return fail(RD_ERR_NOTFOUND, "unknown request");
+  rd_engine::Req& r = it->second;
+  if (r.st.state == RD_REQ_QUEUED) {
+    e->queue.erase(std::remove(e->queue.begin(), e->queue.end(), id), e->queue.end());
+  } else if (r.st.state == RD_REQ_RUNNING) {
+    int rc = rd_diode_remove(e, r.st.diode);
+    if (rc) return rc;
+    e->running.erase(r.st.diode);
+    r.st.diode = -1;
+  } else {
+    return RD_OK;
+  }
+  r.st.state = RD_REQ_CANCELLED;
+  r.st.done_s = e->clock();
+  return RD_OK;
+}
+
+static int serve_admit(rd_engine* e, rd_serve_stats* st) {
+  while (!e->queue.empty()) {
+    long long id = e->queue.front();
+    rd_engine::Req& r = e->reqs[id];
+    rd_diode_config cfg = r.cfg;
+    if (!r.work.empty()) cfg.work = r.work.data();
+    int slot = -1;
+    int rc = rd_diode_add(e, &cfg, &slot);
+    if (rc == RD_ERR_CAPACITY) return RD_OK;   // head of line waits for capacity
+    if (rc) {                                  // invalid request: drop it
+      r.st.state = RD_REQ_CANCELLED;
+      r.st.done_s = e->clock();
+      e->queue.pop_front();
+      continue;
+    }
+    int off = e->gstep - 1;   // the diode's first step is 1
+    CK(cudaMemcpy(&e->dD[slot].step_offset, &off, sizeof(int), cudaMemcpyHostToDevice));
+    const int n = (int)(r.pos.size() / 3);
+    if (n > 0) {
+      rc = rd_add_particles(e, slot, n, r.pos.data(), r.vel.empty() ? nullptr : r.vel.data(), nullptr, 0, 1);
+      if (rc) return rc;
+      st->h2d_bytes += (long long)(r.pos.size() + r.vel.size()) * sizeof(double);
+    }
+    r.st.state = RD_REQ_RUNNING;
+    r.st.diode = slot;
+    r.st.admit_s = e->clock();
+    e->running[slot] = id;
+    e->queue.pop_front();
+    st->admitted++;
+    std::vector<double>().swap(r.pos);
+    std::vector<double>().swap(r.vel);
+  }
+  return RD_OK;
+}
+
+int rd_serve(rd_engine* e, int iterations, rd_serve_stats* out) {
+  if (!e || !out) return fail(RD_ERR_INVALID, "null argument");
+  *out = rd_serve_stats{};
+  const double w0 = e->clock();
+  const int S = e->cfg.max_diodes;
+  std::vector<DiodeDyn> dyn(S);
+  std::vector<double> times;
+  for (int it = 0; it < iterations; ++it) {
+    int rc = serve_admit(e, out);
+    if (rc) return rc;
+    if (e->running.empty()) break;
+    if ((rc = ensure_graph(e))) return rc;
+    CK(rd_launch_step_set(e->st, e->d_step, e->gstep));
+    CK(cudaEventRecord(e->ev0, e->st));
+    CK(cudaGraphLaunch(e->graph, e->st));
+    CK(cudaEventRecord(e->ev1, e->st));
+    CK(cudaMemcpyAsync(dyn.data(), e->dD, sizeof(DiodeDyn) * S, cudaMemcpyDeviceToHost, e->st));
+    CK(cudaStreamSynchronize(e->st));
+    out->d2h_bytes += (long long)sizeof(DiodeDyn) * S;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+    times.push_back(ms);
+    out->device_ms += ms;
+    out->iterations++;
+    e->gstep++;
+    std::vector<int> done;
+    for (auto& kv : e->running) {
+      const DiodeDyn& y = dyn[kv.first];
+      rd_engine::Req& r = e->reqs[kv.second];
+      out->electron_steps += y.electron_steps - r.st.counters.electron_steps;
+      fill_counters(y, &r.st.counters);
+      if (y.steps_done >= r.steps) done.push_back(kv.first);
+    }
+    for (int slot : done) {
+      rd_engine::Req& r = e->reqs[e->running[slot]];
+      if ((rc = rd_diode_remove(e, slot))) return rc;
+      r.st.state = RD_REQ_DONE;
+      r.st.diode = -1;
+      r.st.done_s = e->clock();
+      e->running.erase(slot);
+      out->retired++;
+    }
+  }
+  out->running = (int)e->running.size();
+  out->queued = (int)e->queue.size();
+  out->wall_ms = (e->clock() - w0) * 1e3;
+  if (!times.empty()) {
+    std::vector<double> s(times);
+    std::sort(s.begin(), s.end());
+    auto pct = [&](double q) {
+      double pos = q * (s.size() - 1);
+      size_t lo = (size_t)pos, hi = std::min(lo + 1, s.size() - 1);
+      return s[lo] + (s[hi] - s[lo]) * (pos - lo);
+    };
+    out->step_ms_p50 = pct(0.50);
+    out->step_ms_p99 = pct(0.99);
+    out->step_ms_max = s.back();
+  }
   return RD_OK;
 }
 

@@ -399,7 +399,6 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
   const int nd = ph->n_diodes;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  const uint32_t step = (uint32_t)*step_ptr;
   // chain prefix: plan[d].pad0 holds the first global chain index of diode d
   int total = nd > 0 ? plan[nd - 1].pad0 + plan[nd - 1].n_i : 0;
   for (int g = wid; g < total; g += warps_total) {
@@ -408,6 +407,7 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
     const int d = lo, c = g - plan[d].pad0;
     const DiodeParams& p = P[d];
     const int n = plan[d].n_j, k = ch_off[d] + c;
+    const uint32_t step = (uint32_t)(*step_ptr - Dy[d].step_offset);
     int ok = 0;
     double F = 1.0, sup = -1.79769313486231570e308, X = 0, Y = 0, Z = 0, xi = 1.0, ph_ = 0.0;
     for (int r = 0; r < p.init_rounds && !ok; ++r) {
@@ -488,29 +488,18 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
   __shared__ rd_d4 sj[RD_TILE];
   __shared__ int red_i[2 * RD_ITILE];
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
-  const uint32_t step = (uint32_t)*step_ptr;
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     if (p.geometry != RD_G_PLANAR || it_idx > p.mh_jumps) continue;
     DiodeDyn& y = Dy[it.d];
+    const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
     const int M = plan[it.d].n_i, c = it.i0 + tid, k = ch_off[it.d] + c;
     const bool valid = c < M;
     const int ok = valid ? cs.ok[k] : 0;
     const int ndim_first = (int)nint_d(p.mh_jumps * 0.25);
-    // proposal (box_muller + check_limits_metro_rec :1380-1393, :1466-1516)
-    double sx = (it_idx > ndim_first) ? p.em_Lx * y.MH_std : p.em_Lx * 0.10;
-    double sy = (it_idx > ndim_first) ? p.em_Ly * y.MH_std : p.em_Ly * 0.10;
-    double wx = p.em_x0, wy = p.em_y0;
-    if (ok) {
-      double g1, g2;
-      gauss2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, &g1, &g2);
-      wx = g1 * sx + cs.x[k];
-      wy = g2 * sy + cs.y[k];
-      double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
-      if (wx > hx) wx = hx - (wx - hx); else if (wx < p.em_x0) wx = (p.em_x0 - wx) + p.em_x0;
-      if (wy > hy) wy = hy - (wy - hy); else if (wy < p.em_y0) wy = (p.em_y0 - wy) + p.em_y0;
-    }
+    // proposal from k_mh_propose
+    const double wx = ok ? cs.px[k] : p.em_x0, wy = ok ? cs.py[k] : p.em_y0;
     double s = z0_item_sum<PREC>(p, pool, it, wx, wy, sh, sl, sj);
     if (it.nch > 1) {
       partial[(size_t)g * RD_ITILE + tid] = s;
@@ -551,34 +540,25 @@ k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool
   __shared__ rd_d4 sj[RD_TILE];
   __shared__ int red_i[2 * RD_ITILE];
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
-  const uint32_t step = (uint32_t)*step_ptr;
-  const double twopi = 2.0 * c_k.pi;
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     if (p.geometry != RD_G_TIP || it_idx > p.mh_jumps) continue;
     DiodeDyn& y = Dy[it.d];
+    const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
     const int M = plan[it.d].n_i, c = it.i0 + tid, k = ch_off[it.d] + c;
     const bool valid = c < M;
     const int ok = valid ? cs.ok[k] : 0;
     const int ndim_first = (int)nint_d(p.mh_jumps * 0.25);
-    double sxi = (it_idx > ndim_first) ? (p.max_xi - 1.0) * y.MH_std : (p.max_xi - 1.0) * 0.10;
-    double sph = (it_idx > ndim_first) ? twopi * y.MH_std : twopi * 0.10;
-    // proposal in (xi, phi), Metro_algo_tip_v3 :1334-1350
-    double nxi = 1.5, nph = 0.0;
+    // proposal from k_mh_propose
+    double nxi = 1.5, nph = 0.0, X, Y, Z;
     int inside = 0;
     if (ok) {
-      double g1, g2;
-      gauss2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, &g1, &g2);
-      nxi = cs.x[k] + g1 * sxi;
-      double a = cs.y[k] + g2 * sph;
-      nph = a - floor(a / twopi) * twopi;
-      if (nxi > p.max_xi) nxi = 2.0 * p.max_xi - nxi;
-      if (nxi < 1.0) nxi = 2.0 - nxi;
-      inside = !(nxi < 1.0 || nxi > p.max_xi);
+      nxi = cs.px[k]; nph = cs.py[k]; inside = cs.prop_ok[k];
+      X = cs.pxx[k]; Y = cs.pyy[k]; Z = cs.pzz[k];
+    } else {
+      tip_xyz(p, 1.5, p.eta_1, 0.0, &X, &Y, &Z);
     }
-    double X, Y, Z;
-    tip_xyz(p, inside ? nxi : 1.5, p.eta_1, nph, &X, &Y, &Z);
     // field at the proposal (general form, all three components)
     double fx = 0, fy = 0, fz = 0;
     const int off = p.off;
@@ -655,6 +635,59 @@ k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool
   }
 }
 
+// ---- MH proposals: one thread per chain -------------------------------------------------
+// Planar: Gaussian step (box_muller) reflected at the emitter edges
+// (check_limits_metro_rec, src/mod_field_emission_v2.F90:1380-1393,
+// :1466-1516).  Tip: Gaussian step in (xi, phi), phi wrapped, xi reflected
+// once (Metro_algo_tip_v3, src/mod_emission_tip.f90:1334-1350).  The step
+// uses the fixed warm-up size for the first quarter of the jumps and MH_std
+// afterwards; MH_std was updated at the end of the previous iteration.
+__global__ void k_mh_propose(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy,
+                             const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                             ChainState cs, const int* __restrict__ ch_off,
+                             const int* __restrict__ step_ptr, int it_idx) {
+  const int nd = ph->n_diodes;
+  const int total = nd > 0 ? plan[nd - 1].pad0 + plan[nd - 1].n_i : 0;
+  const double twopi = 2.0 * c_k.pi;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    int lo = 0, hi = nd - 1;
+    while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (plan[mid].pad0 <= g) lo = mid; else hi = mid - 1; }
+    const int d = lo, c = g - plan[d].pad0;
+    const DiodeParams& p = P[d];
+    if (it_idx > p.mh_jumps) continue;
+    const int k = ch_off[d] + c;
+    if (!cs.ok[k]) continue;
+    const DiodeDyn& y = Dy[d];
+    const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
+    const int ndim_first = (int)nint_d(p.mh_jumps * 0.25);
+    double g1, g2;
+    gauss2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, &g1, &g2);
+    if (p.geometry == RD_G_TIP) {
+      double sxi = (it_idx > ndim_first) ? (p.max_xi - 1.0) * y.MH_std : (p.max_xi - 1.0) * 0.10;
+      double sph = (it_idx > ndim_first) ? twopi * y.MH_std : twopi * 0.10;
+      double nxi = cs.x[k] + g1 * sxi;
+      double a = cs.y[k] + g2 * sph;
+      double nph = a - floor(a / twopi) * twopi;   // Fortran MODULO
+      if (nxi > p.max_xi) nxi = 2.0 * p.max_xi - nxi;
+      if (nxi < 1.0) nxi = 2.0 - nxi;
+      int inside = !(nxi < 1.0 || nxi > p.max_xi);
+      double X, Y, Z;
+      tip_xyz(p, inside ? nxi : 1.5, p.eta_1, nph, &X, &Y, &Z);
+      cs.px[k] = nxi; cs.py[k] = nph; cs.prop_ok[k] = inside;
+      cs.pxx[k] = X; cs.pyy[k] = Y; cs.pzz[k] = Z;
+    } else {
+      double sx = (it_idx > ndim_first) ? p.em_Lx * y.MH_std : p.em_Lx * 0.10;
+      double sy = (it_idx > ndim_first) ? p.em_Ly * y.MH_std : p.em_Ly * 0.10;
+      double wx = g1 * sx + cs.x[k];
+      double wy = g2 * sy + cs.y[k];
+      double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+      if (wx > hx) wx = hx - (wx - hx); else if (wx < p.em_x0) wx = (p.em_x0 - wx) + p.em_x0;
+      if (wy > hy) wy = hy - (wy - hy); else if (wy < p.em_y0) wy = (p.em_y0 - wy) + p.em_y0;
+      cs.px[k] = wx; cs.py[k] = wy;
+    }
+  }
+}
+
 // ---- emission decisions and stable append ----------------------------------------------------
 // One CTA per emitting diode.  Candidates are tested in chain order
 // (Do_Field_Emission_Planar_rectangle :345-381; Do_Field_Emission_Tip_OLDCODE
@@ -671,7 +704,7 @@ k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, 
   const DiodeParams& p = P[d];
   if (!p.active || !p.emission) return;
   DiodeDyn& y = Dy[d];
-  const int step = *step_ptr;
+  const int step = *step_ptr - y.step_offset;
   const int M = y.chains;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   if (tid == 0) s_base = 0;
@@ -804,6 +837,7 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
                               const int* ch_off, const double* work, const int* step_ptr,
                               int it_idx, double* partial, int* tickets, double kscale) {
+  k_mh_propose<<<grid, 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx);
   if (geometry_mask & 1) {
     if (prec == 1) k_mh_jump_planar<1><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, work, step_ptr, it_idx, partial, tickets, kscale);
     else k_mh_jump_planar<0><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, work, step_ptr, it_idx, partial, tickets, kscale);

@@ -70,7 +70,7 @@ struct DiodeDyn {
   int mh_acc, mh_rej, mh_done;   // per-jump counters (reset by the last arriver)
   int sup_done;
   int absorbed_top_step, absorbed_bot_step;
-  int pad;
+  int step_offset;       // this diode's step = engine step - step_offset
   long long emitted_total, absorbed_top_total, absorbed_bot_total, dropped_total;
   long long electron_steps;      // sum over steps of particles in flight
   long long steps_done;

@@ -61,78 +61,90 @@ __device__ __forceinline__ void pack_one(const DiodeParams& p, const Pool& pool,
 }
 
 // ---- planner --------------------------------------------------------------------
+__device__ __forceinline__ int plan_ni(const DiodeParams& p, const DiodeDyn& y, int mode,
+                                       const int* npts, int d) {
+  const int nj = y.n;
+  switch (mode) {
+    case PM_FORCE_PLANAR: return p.geometry == RD_G_PLANAR ? nj : 0;
+    case PM_FORCE_TIP: return p.geometry == RD_G_TIP ? nj : 0;
+    case PM_FIELD: return npts[d];
+    case PM_SUPPLY_PLANAR: return (p.emission && p.geometry == RD_G_PLANAR) ? p.quad_n * p.quad_n : 0;
+    case PM_SUPPLY_TIP: return (p.emission && p.geometry == RD_G_TIP) ? 10000 : 0;
+    case PM_MH: return p.emission ? y.chains : 0;
+    default: return nj;
+  }
+}
+
+// Tiles and j-chunking of one diode.  The chunk length depends only on the
+// diode's own counts (at least RD_CLEN_MIN particles, at most RD_NCH_MAX
+// chunks per tile), so the summation order -- and therefore every result --
+// is the same whether a diode runs alone or among other diodes.
+#define RD_CLEN_MIN 1024
+#define RD_NCH_MAX 8
+__device__ __forceinline__ void plan_split(int ni, int nj, int tsize, bool pair, int grow,
+                                           int* tiles, int* nch, int* clen) {
+  *tiles = (ni + tsize - 1) / tsize;
+  *nch = 1;
+  *clen = RD_TILE;
+  if (pair && *tiles > 0) {
+    int c = (nj + RD_NCH_MAX - 1) / RD_NCH_MAX;
+    if (c < RD_CLEN_MIN) c = RD_CLEN_MIN;
+    c = ((c + RD_TILE - 1) / RD_TILE) * RD_TILE;
+    c <<= grow;   // only if the scratch bound is ever hit (never by construction)
+    *clen = c;
+    *nch = nj > 0 ? (nj + c - 1) / c : 1;
+  }
+}
+
 __global__ void __launch_bounds__(1024)
 k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int nslots, int mode,
        int target_items, int max_items, const int* __restrict__ npts, PlanEntry* __restrict__ plan,
        PlanHeader* __restrict__ ph) {
   __shared__ double red[1024];
   __shared__ int s_items[32], s_chains[32];
+  __shared__ int s_run_items, s_run_chains;
   const int tid = threadIdx.x;
   const int tsize = (mode == PM_PART1024) ? 1024 : RD_ITILE;
   const bool pair = (mode <= PM_MH);
-  // pass 1: total pair work
-  double work = 0.0;
-  for (int d = tid; d < nslots; d += blockDim.x) {
-    const DiodeParams& p = P[d];
-    if (!p.active) continue;
-    int ni = 0, nj = Dy[d].n;
-    switch (mode) {
-      case PM_FORCE_PLANAR: ni = p.geometry == RD_G_PLANAR ? nj : 0; break;
-      case PM_FORCE_TIP: ni = p.geometry == RD_G_TIP ? nj : 0; break;
-      case PM_FIELD: ni = npts[d]; break;
-      case PM_SUPPLY_PLANAR: ni = (p.emission && p.geometry == RD_G_PLANAR) ? p.quad_n * p.quad_n : 0; break;
-      case PM_SUPPLY_TIP: ni = (p.emission && p.geometry == RD_G_TIP) ? 10000 : 0; break;
-      case PM_MH: ni = p.emission ? Dy[d].chains : 0; break;
-      default: ni = nj; break;
-    }
-    work += (double)ni * (double)(nj > RD_TILE ? nj : RD_TILE);
-  }
-  red[tid] = work;
+  // grow the chunk length only if the items would not fit the scratch
+  __shared__ int s_grow;
+  if (tid == 0) s_grow = 0;
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (tid < s) red[tid] += red[tid + s];
+  for (int round = 0; round < 24; ++round) {
+    const int grow = s_grow;
+    double cnt = 0.0;
+    for (int d = tid; d < nslots; d += blockDim.x) {
+      if (!P[d].active) continue;
+      int tiles, nch, clen;
+      plan_split(plan_ni(P[d], Dy[d], mode, npts, d), Dy[d].n, tsize, pair, grow, &tiles, &nch, &clen);
+      cnt += (double)tiles * nch;
+    }
+    red[tid] = cnt;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (tid < s) red[tid] += red[tid + s];
+      __syncthreads();
+    }
+    const bool fits = red[0] <= (double)max_items;
+    __syncthreads();
+    if (fits) break;
+    if (tid == 0) s_grow = grow + 1;
     __syncthreads();
   }
-  const double total_work = red[0];
-  double per_item = total_work / (double)(target_items > 0 ? target_items : 1);
-  // pass 2: entries, serial prefix in chunks of blockDim
-  __shared__ int s_run_items, s_run_chains;
+  const int grow = s_grow;
+  // pass 3: entries with a running block scan
   if (tid == 0) { s_run_items = 0; s_run_chains = 0; }
   __syncthreads();
   for (int base = 0; base < nslots; base += blockDim.x) {
     int d = base + tid;
     int items = 0, ni = 0, nj = 0, tiles = 0, nch = 1, clen = RD_TILE, chains = 0;
-    if (d < nslots) {
-      const DiodeParams& p = P[d];
-      if (p.active) {
-        nj = Dy[d].n;
-        switch (mode) {
-          case PM_FORCE_PLANAR: ni = p.geometry == RD_G_PLANAR ? nj : 0; break;
-          case PM_FORCE_TIP: ni = p.geometry == RD_G_TIP ? nj : 0; break;
-          case PM_FIELD: ni = npts[d]; break;
-          case PM_SUPPLY_PLANAR: ni = (p.emission && p.geometry == RD_G_PLANAR) ? p.quad_n * p.quad_n : 0; break;
-          case PM_SUPPLY_TIP: ni = (p.emission && p.geometry == RD_G_TIP) ? 10000 : 0; break;
-          case PM_MH: ni = p.emission ? Dy[d].chains : 0; chains = ni; break;
-          default: ni = nj; break;
-        }
-        tiles = (ni + tsize - 1) / tsize;
-        if (pair && tiles > 0) {
-          int njr = ((nj + RD_TILE - 1) / RD_TILE) * RD_TILE;
-          if (njr < RD_TILE) njr = RD_TILE;
-          double want = per_item / (double)RD_ITILE;            // j per item
-          int c = (int)fmin((double)njr, fmax((double)RD_TILE, want));
-          c = ((c + RD_TILE - 1) / RD_TILE) * RD_TILE;
-          // keep the item count within the scratch budget
-          long long maxc = (long long)max_items / (tiles > 0 ? tiles : 1);
-          if (maxc < 1) maxc = 1;
-          while ((long long)((nj + c - 1) / c) > maxc) c *= 2;
-          clen = c;
-          nch = nj > 0 ? (nj + c - 1) / c : 1;
-        }
-        items = tiles * nch;
-      }
+    if (d < nslots && P[d].active) {
+      nj = Dy[d].n;
+      ni = plan_ni(P[d], Dy[d], mode, npts, d);
+      if (mode == PM_MH) chains = ni;
+      plan_split(ni, nj, tsize, pair, grow, &tiles, &nch, &clen);
+      items = tiles * nch;
     }
-    // block scan of items and chains
     int lane = tid & 31, w = tid >> 5;
     int vi = items, vc = chains;
     for (int o = 1; o < 32; o <<= 1) {
@@ -157,7 +169,7 @@ k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int n
     __syncthreads();
   }
   if (tid == 0) {
-    ph->total_items = s_run_items;
+    ph->total_items = s_run_items < max_items ? s_run_items : max_items;
     ph->n_diodes = nslots;
   }
 }
@@ -304,12 +316,12 @@ k_compact_scatter(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict_
                   Pool tmp, const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
                   const int* __restrict__ kept, int* __restrict__ life, const int* __restrict__ step_ptr) {
   __shared__ int wsum[32];
-  const int step = *step_ptr;
   for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
     ItemRef it = decode_item(plan, ph->n_diodes, g);
     const DiodeParams& p = P[it.d];
     const DiodeDyn& y = Dy[it.d];
     if (y.n_remove == 0) continue;
+    const int step = *step_ptr - y.step_offset;
     const int n = plan[it.d].n_i;
     const int b = it.tile, i0 = it.i0;
     if (i0 + 1024 <= y.first_dead) continue;   // nothing moves in this block
