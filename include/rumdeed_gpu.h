@@ -154,6 +154,23 @@ int rd_life_time(rd_engine* e, int diode, int* hist1000);
  * stream) and launches of library kernels per step. */
 int rd_last_run_stats(rd_engine* e, double* ms, int* kernels_per_step);
 
+/* ---- field at points without allocation -----------------------------------
+ * No counterpart in the reference.  The same field evaluation as rd_field_at,
+ * for callers that cannot allocate device memory at the time of the call:
+ * host codes whose device memory belongs to another runtime (an OpenACC
+ * driver passing acc_deviceptr of its own buffers), processes with a fixed
+ * device-memory budget, latency-critical loops.  The points and the result
+ * are caller-owned DEVICE buffers, (3, M) doubles each; all working memory
+ * of the call is a static 16 MiB device array inside the library, held by
+ * every GPU that loads it until the process exits.  M may be at most 65536
+ * (RD_ERR_INVALID otherwise).  The first call on a device resolves the array's
+ * device address and should come before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race, so issue them one after
+ * another.  Returns after the result is written (synchronises the engine
+ * stream). */
+int rd_field_at_noalloc(rd_engine* e, int diode, int M, const double* pos3m_dev,
+                        double* field3m_dev);
+
 /* ---- tracing: per-phase device times of one step --------------------------
  * The reference has only wall-clock stamps at start and end of the run
  * (src/main.F90:51,267).  rd_profile_step runs one main-loop iteration

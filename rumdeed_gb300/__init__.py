@@ -150,6 +150,7 @@ SIGNATURES = {
     "rd_cancel": (C.c_int, [C.c_void_p, C.c_longlong]),
     "rd_serve": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(ServeStats)]),
     "rd_clock": (C.c_int, [C.c_void_p, _dp]),
+    "rd_field_at_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
 }
 
 
@@ -400,6 +401,12 @@ class Diode:
         out = np.zeros_like(pts)
         _check(self.L.rd_field_at(self.e.h, self.index, pts.shape[0], _p(pts), _p(out)))
         return out
+
+    def calc_field_at_batch_noalloc(self, pos_dev_ptr, field_dev_ptr, M):
+        """rd_field_at_noalloc: points and result are caller-owned device
+        buffers ((3, M) doubles); the call allocates nothing."""
+        _check(self.L.rd_field_at_noalloc(self.e.h, self.index, M, C.c_void_p(pos_dev_ptr),
+                                          C.c_void_p(field_dev_ptr)))
 
     def mark_particles_remove(self, i, why):
         _check(self.L.rd_mark_remove(self.e.h, self.index, i, why))

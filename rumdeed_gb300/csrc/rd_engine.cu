@@ -434,6 +434,27 @@ static bool valid_diode(rd_engine* e, int d) {
   return e && d >= 0 && d < (int)e->slots.size() && e->slots[d].used;
 }
 
+// ---- helpers for rd_noalloc.cu (C++ linkage, not part of the C ABI) -----------------
+int rd_set_error(int code, const char* msg) { return fail(code, msg); }
+
+int rd_engine_view(rd_engine* e, int diode, const DiodeParams** P, const DiodeDyn** Dy, Pool* pool,
+                   int* geometry, int* precision, int* grid, double* kscale, cudaStream_t* st,
+                   int* device) {
+  if (!valid_diode(e, diode)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  *P = e->dP + diode;
+  *Dy = e->dD + diode;
+  *pool = e->pool;
+  *geometry = e->slots[diode].p.geometry;
+  *precision = e->cfg.precision;
+  *grid = e->grid;
+  *kscale = e->kscale;
+  *st = e->st;
+  *device = e->cfg.device;
+  return RD_OK;
+}
+
+int rd_engine_repack(rd_engine* e) { return repack(e); }
+
 // ---- C ABI ----------------------------------------------------------------------------
 extern "C" {
 
