@@ -18,7 +18,7 @@ LIB = os.path.join(OUT_DIR, "librumdeed_gb300.so")
 SOURCES = ["rd_force.cu", "rd_field.cu", "rd_step.cu", "rd_engine.cu", "rd_noalloc.cu"]
 HEADERS = ["rd_internal.h", "rd_device.cuh", "rd_pair.cuh", "rd_tiles.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-ftz=true", "-Xcompiler", "-fPIC,-ffp-contract=off",
          "-I", os.path.join(HERE, "..", "include")]
 
 

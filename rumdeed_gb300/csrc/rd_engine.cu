@@ -38,8 +38,8 @@ cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st
                                    int* tickets, double kscale);
 cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const DiodeParams* P,
                                 const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
-                                const double* qx, const double* qy, double* qF, double* partial,
-                                int* tickets, double kscale);
+                                const double* qx, const double* qy, const float4* qpp, double* qF,
+                                double* partial, int* tickets, double kscale);
 cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                     const double* qx, const double* qy, const double* qw,
                                     const double* qF, const double* qfx, const double* qfy,
@@ -47,11 +47,11 @@ cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodePara
 cudaError_t rd_launch_mh_init(int prec, int grid, cudaStream_t st, const DiodeParams* P,
                               DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
                               const PlanHeader* ph, const ChainState& cs, const int* ch_off,
-                              const double* work, const int* step_ptr, double kscale);
+                              const double* wtab, const int* step_ptr, double kscale);
 cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_t st,
                               const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
-                              const int* ch_off, const double* work, const int* step_ptr,
+                              const int* ch_off, const double* wtab, const int* step_ptr,
                               int it_idx, double* partial, int* tickets, double kscale);
 cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                            const Pool& pool, const ChainState& cs, const int* ch_off,
@@ -200,7 +200,9 @@ struct rd_engine {
   Pool pool{}, tmp{};
   std::vector<void*> allocs;
   double* work = nullptr;
+  double* wtab = nullptr;   // per work cell: log phi, log(l_const/phi^2), l_const/phi^2
   double *qx = nullptr, *qy = nullptr, *qz = nullptr, *qw = nullptr, *qF = nullptr, *qfx = nullptr, *qfy = nullptr;
+  float4* qpp = nullptr;   // planar quadrature points in the FP32 frame
   ChainState cs{};
   int *d_choff = nullptr, *d_qoff = nullptr, *d_npts = nullptr, *d_zero_off = nullptr;
   PlanEntry* plan[PM_COUNT] = {};
@@ -260,14 +262,14 @@ static int alloc_pool(rd_engine* e, Pool& P, long long cap) {
   for (auto p : dbl) CK(e->dalloc(p, cap));
   int** in[] = {&P.species, &P.id, &P.step0, &P.section, &P.mask};
   for (auto p : in) CK(e->dalloc(p, cap));
-  float4** f4[] = {&P.pk_hi, &P.pk_lo, &P.ip_hi, &P.ip_lo};
+  float4** f4[] = {&P.pk_hi, &P.pk_lo, &P.ip_hi, &P.ip_lo, &P.zk_hi, &P.zk_lo};
   for (auto p : f4) CK(e->dalloc(p, cap));
   return RD_OK;
 }
 
 // ---- pipeline pieces ----------------------------------------------------------------
 static int target_items(const rd_engine* e) {
-  return e->cfg.target_items > 0 ? e->cfg.target_items : 8 * e->grid;
+  return e->cfg.target_items > 0 ? e->cfg.target_items : 8 * 4 * e->sms;
 }
 
 static cudaError_t plan(rd_engine* e, int mode, const int* npts = nullptr) {
@@ -303,7 +305,7 @@ static int launch_emission(rd_engine* e) {
   if (s.emit_planar) {
     CK(plan(e, PM_SUPPLY_PLANAR));
     CK(rd_launch_z0_points(prec, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_PLANAR],
-                           e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qF, e->partial, e->tickets,
+                           e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qpp, e->qF, e->partial, e->tickets,
                            e->kscale));
     e->kernels_in_step++;
   }
@@ -318,15 +320,15 @@ static int launch_emission(rd_engine* e) {
                              e->work));
   e->kernels_in_step++;
   CK(plan(e, PM_MH));
-  CK(rd_launch_mh_init(prec, e->grid * 4, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                       e->cs, e->d_choff, e->work, e->d_step, e->kscale));
+  CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                       e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
   e->kernels_in_step++;
   const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
   for (int it = 1; it <= s.jumps; ++it) {
     CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH],
-                         e->ph[PM_MH], e->cs, e->d_choff, e->work, e->d_step, it, e->partial,
+                         e->ph[PM_MH], e->cs, e->d_choff, e->wtab, e->d_step, it, e->partial,
                          e->tickets, e->kscale));
-    e->kernels_in_step += (gmask == 3) ? 3 : 2;   // propose + jump kernel(s)
+    e->kernels_in_step += ((gmask & 1) ? 1 : 0) + ((gmask & 2) ? 2 : 0);   // planar jump, tip propose + jump
   }
   CK(rd_launch_emit(ns, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step));
   e->kernels_in_step++;
@@ -477,7 +479,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   ce = cudaGetDeviceProperties(&prop, cfg->device);
   if (ce != cudaSuccess) return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
   e->sms = prop.multiProcessorCount;
-  e->grid = cfg->grid_blocks > 0 ? cfg->grid_blocks : 4 * e->sms;
+  e->grid = cfg->grid_blocks > 0 ? cfg->grid_blocks : 0;   // 0: occupancy-based per kernel
   if ((ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess)
     return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
   cudaEventCreate(&e->ev0);
@@ -498,10 +500,11 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   e->max_items = (int)std::min<long long>(
       1 << 26, 8LL * (std::max(cap, std::max(chcap, qcap)) / RD_ITILE + 4LL * S) + 65536);
   if ((rc = alloc_pool(e, e->pool, cap)) || (rc = alloc_pool(e, e->tmp, cap))) return bail(rc);
-  if (e->dalloc(&e->dP, S) || e->dalloc(&e->dD, S) || e->dalloc(&e->work, (size_t)S * 4 + 4096) ||
+  if (e->dalloc(&e->dP, S) || e->dalloc(&e->dD, S) || e->dalloc(&e->work, (size_t)S * 4 + 4096) || e->dalloc(&e->wtab, 3 * ((size_t)S * 4 + 4096)) ||
       e->dalloc(&e->qx, qcap) || e->dalloc(&e->qy, qcap) || e->dalloc(&e->qz, qcap) ||
       e->dalloc(&e->qw, qcap) || e->dalloc(&e->qF, qcap) || e->dalloc(&e->qfx, qcap) ||
-      e->dalloc(&e->qfy, qcap) || e->dalloc(&e->d_choff, S) || e->dalloc(&e->d_qoff, S) ||
+      e->dalloc(&e->qfy, qcap) || e->dalloc(&e->qpp, qcap) || e->dalloc(&e->cs.gx, chcap) || e->dalloc(&e->cs.gy, chcap) ||
+      e->dalloc(&e->d_choff, S) || e->dalloc(&e->d_qoff, S) ||
       e->dalloc(&e->d_npts, S) || e->dalloc(&e->d_zero_off, S) ||
       e->dalloc(&e->partial, (size_t)e->max_items * 3 * RD_ITILE) ||
       e->dalloc(&e->tickets, e->max_items) || e->dalloc(&e->kept, e->max_items) ||
@@ -681,6 +684,13 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
           hw[k2] = (((0.5 * (p.a_foci * p.a_foci)) * std::sqrt(1.0 - e2)) * (ph2 - ph1)) * (fac(xi2) - fac(xi1));
         }
     }
+    std::vector<float4> hpp(npt);
+    for (int k2 = 0; k2 < npt; ++k2) {   // the FP32-frame split of rd_device.cuh split_nm
+      double vx = (hx[k2] - p.org_x) * 1.0e9, vy = (hy[k2] - p.org_y) * 1.0e9;
+      float ax = (float)vx, ay = (float)vy;
+      hpp[k2] = make_float4(ax, (float)(vx - (double)ax), ay, (float)(vy - (double)ay));
+    }
+    CK(cudaMemcpyAsync(e->qpp + sl.q_off, hpp.data(), npt * sizeof(float4), cudaMemcpyHostToDevice, e->st));
     CK(cudaMemcpyAsync(e->qx + sl.q_off, hx.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
     CK(cudaMemcpyAsync(e->qy + sl.q_off, hy.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
     CK(cudaMemcpyAsync(e->qz + sl.q_off, hz.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
@@ -688,6 +698,14 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
     CK(cudaStreamSynchronize(e->st));
   }
   CK(cudaMemcpyAsync(e->work + sl.w_off, wv.data(), sl.w_len * sizeof(double), cudaMemcpyHostToDevice, e->st));
+  std::vector<double> wt(3 * sl.w_len);
+  for (long long k2 = 0; k2 < sl.w_len; ++k2) {
+    const double phi = wv[k2];
+    wt[3 * k2] = std::log(phi);
+    wt[3 * k2 + 1] = std::log(e->k.l_const / (phi * phi));
+    wt[3 * k2 + 2] = e->k.l_const / (phi * phi);
+  }
+  CK(cudaMemcpyAsync(e->wtab + 3 * sl.w_off, wt.data(), wt.size() * sizeof(double), cudaMemcpyHostToDevice, e->st));
   DiodeDyn y{};
   y.MH_std = (c->geometry == RD_GEOM_TIP) ? 0.125 : 0.0125;   // fe_v2:58; tip 1.0 clamped to 0.125
   y.a_rate = (c->geometry == RD_GEOM_TIP) ? 0.5 : 1.0;
@@ -982,7 +1000,7 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
     if (s.emit_planar) {
       CK(plan(e, PM_SUPPLY_PLANAR));
       CK(rd_launch_z0_points(prec, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_PLANAR],
-                             e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qF, e->partial, e->tickets, e->kscale));
+                             e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qpp, e->qF, e->partial, e->tickets, e->kscale));
     }
     if (s.emit_tip) {
       CK(plan(e, PM_SUPPLY_TIP));
@@ -1002,14 +1020,14 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
       out->mh_pair_evals += (long long)dyn[d].chains * dyn[d].n * sl.p.mh_jumps;
     }
     CK(plan(e, PM_MH));
-    CK(rd_launch_mh_init(prec, e->grid * 4, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                         e->cs, e->d_choff, e->work, e->d_step, e->kscale));
+    CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                         e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
     CK(cudaEventRecord(ev[2], e->st));
     const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
     for (int it = 1; it <= s.jumps; ++it)
       CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                           e->cs, e->d_choff, e->work, e->d_step, it, e->partial, e->tickets, e->kscale));
-    out->mh_jump_launches = s.jumps * ((gmask == 3) ? 2 : 1);
+                           e->cs, e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale));
+    out->mh_jump_launches = s.jumps;
     CK(cudaEventRecord(ev[3], e->st));
     CK(rd_launch_emit(S, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step));
   } else {

@@ -124,29 +124,122 @@ k_field_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __
   }
 }
 
+// ---- work-function cell and the tabulated supply logarithm ------------------------------
+// Cell of the checkerboard (as work_at) without the section number.
+__device__ __forceinline__ int work_cell(const DiodeParams& p, double x, double y) {
+  if (p.work_nx == 1 && p.work_ny == 1) return 0;
+  double xs = (x - p.em_x0) / p.em_Lx, ys = (y - p.em_y0) / p.em_Ly;
+  int nx = p.work_nx, ny = p.work_ny;
+  int xi = (int)floor(xs / (1.0 / nx)) + 1, yi = (int)floor(ys / (1.0 / ny)) + 1;
+  xi = xi > nx ? nx : (xi < 1 ? 1 : xi);
+  yi = yi > ny ? ny : (yi < 1 ? 1 : yi);
+  yi = ny - yi + 1;
+  return (yi - 1) * nx + (xi - 1);
+}
+
+// Elec_Supply_log (src/mod_field_emission_v2.F90:589-595) with t_y (:532-553)
+// from a per-cell table (log phi, log(l_const/phi^2), l_const/phi^2):
+// log l = log(l_const/phi^2) + log(-F), so one log of -F and one of t_y.
+__device__ __forceinline__ double supply_log_tab(const DiodeParams& p, const double* __restrict__ wtab,
+                                                 int cell, double F) {
+  const double* t = wtab + 3 * (p.work_off + cell);
+  const double LF = log(-1.0 * F);
+  if (!p.image_charge) return 2.0 * LF - t[0];
+  double l = t[2] * (-1.0 * F), ll = t[1] + LF;
+  if (l > 1.0) { l = 1.0; ll = 0.0; }
+  const double ty = 1.0 + l * ((1.0 / 9.0) - (1.0 / 18.0) * ll);
+  return (2.0 * LF - 2.0 * log(ty)) - t[0];
+}
+
 // ---- cathode z = 0 field, planar ----------------------------------------------------
-// Sum over one j-tile of q_j sum_h h / r_h^3 (nm units), point at z = 0.
+// Sum over one j-tile of q_j sum_h h / r_h^3 (nm units) for a point at z = 0
+// given as (x_hi, x_lo, y_hi, y_lo).  Uses the cathode pack: zk_hi =
+// (x_hi, y_hi, z^2, q z), zk_lo = (x_lo, y_lo, z, q); z^2 >= 1e-20 so r^2 > 0.
+template <bool NIC0>
 __device__ __forceinline__ float z0_tile_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
-                                             int kmax, float pxh, float pxl, float pyh, float pyl,
-                                             int nic, float dnm) {
-  float s = 0.f;
+                                             int kmax, float4 pp, int nic, float dnm) {
+  float s0 = 0.f, s1 = 0.f;
+  int k = 0;
+  if (NIC0) {
 #pragma unroll 4
-  for (int k = 0; k < kmax; ++k) {
-    float4 h = sh[k], l = sl[k];
-    float dx = (pxh - h.x) + (pxl - l.x);
-    float dy = (pyh - h.y) + (pyl - l.y);
-    float dxy2 = fmaf(dx, dx, dy * dy);
-    float zj = h.z + l.z;
-    float inv = rsqrtf(fmaxf(fmaf(zj, zj, dxy2), 1e-20f));
-    s = fmaf(h.w * zj, (inv * inv) * inv, s);
-    for (int n = 1; n <= nic; ++n) {
-      float h1 = zj + 2.0f * n * dnm, h2 = zj - 2.0f * n * dnm;
-      float i1 = rsqrtf(fmaf(h1, h1, dxy2)), i2 = rsqrtf(fmaxf(fmaf(h2, h2, dxy2), 1e-20f));
-      s = fmaf(h.w * h1, (i1 * i1) * i1, s);
-      s = fmaf(h.w * h2, (i2 * i2) * i2, s);
+    for (; k + 1 < kmax; k += 2) {   // two independent accumulators
+      float4 h0 = sh[k], h1 = sh[k + 1];
+      float2 l0 = *reinterpret_cast<const float2*>(&sl[k]);
+      float2 l1 = *reinterpret_cast<const float2*>(&sl[k + 1]);
+      float dx0 = (pp.x - h0.x) + (pp.y - l0.x), dy0 = (pp.z - h0.y) + (pp.w - l0.y);
+      float dx1 = (pp.x - h1.x) + (pp.y - l1.x), dy1 = (pp.z - h1.y) + (pp.w - l1.y);
+      float i0 = rsqrtf(fmaf(dx0, dx0, fmaf(dy0, dy0, h0.z)));
+      float i1 = rsqrtf(fmaf(dx1, dx1, fmaf(dy1, dy1, h1.z)));
+      s0 = fmaf(h0.w, (i0 * i0) * i0, s0);
+      s1 = fmaf(h1.w, (i1 * i1) * i1, s1);
     }
   }
-  return s;
+  for (; k < kmax; ++k) {
+    float4 h = sh[k], l = sl[k];
+    float dx = (pp.x - h.x) + (pp.y - l.x), dy = (pp.z - h.y) + (pp.w - l.y);
+    float dxy2 = fmaf(dx, dx, dy * dy);
+    float inv = rsqrtf(dxy2 + h.z);
+    s0 = fmaf(h.w, (inv * inv) * inv, s0);
+    if (!NIC0) {
+      for (int n = 1; n <= nic; ++n) {
+        float ha = l.z + 2.0f * n * dnm, hb = l.z - 2.0f * n * dnm;
+        float ia = rsqrtf(fmaf(ha, ha, dxy2)), ib = rsqrtf(fmaxf(fmaf(hb, hb, dxy2), 1e-20f));
+        s0 = fmaf(l.w * ha, (ia * ia) * ia, s0);
+        s0 = fmaf(l.w * hb, (ib * ib) * ib, s0);
+      }
+    }
+  }
+  return s0 + s1;
+}
+
+// Two cathode points per thread (N_ic_max = 0): one shared load feeds two pairs.
+__device__ __forceinline__ void z0_tile2_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
+                                             int kmax, float4 pa, float4 pb, float& ra, float& rb) {
+  float sa = 0.f, sb = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < kmax; ++k) {
+    const float4 h = sh[k];
+    const float2 l = *reinterpret_cast<const float2*>(&sl[k]);
+    const float dxa = (pa.x - h.x) + (pa.y - l.x), dya = (pa.z - h.y) + (pa.w - l.y);
+    const float dxb = (pb.x - h.x) + (pb.y - l.x), dyb = (pb.z - h.y) + (pb.w - l.y);
+    const float ia = rsqrtf(fmaf(dxa, dxa, fmaf(dya, dya, h.z)));
+    const float ib = rsqrtf(fmaf(dxb, dxb, fmaf(dyb, dyb, h.z)));
+    sa = fmaf(h.w, (ia * ia) * ia, sa);
+    sb = fmaf(h.w, (ib * ib) * ib, sb);
+  }
+  ra += sa;
+  rb += sb;
+}
+
+// Partial F_z sums of the item for two points at z = 0 (FP32 compensated),
+// blockDim threads loading the j-tiles.
+__device__ __forceinline__ void z0_item_sum2(const DiodeParams& p, const Pool& pool, const ItemRef& it,
+                                             float4 pa, float4 pb, float4* sh, float4* sl,
+                                             double* out_a, double* out_b) {
+  const int off = p.off, tid = threadIdx.x, nt = blockDim.x;
+  const int nic = p.image_charge ? p.N_ic_max : 0;
+  const float dnm = (float)(p.d * 1.0e9);
+  float ha = 0.f, la = 0.f, hb = 0.f, lb = 0.f;
+  for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+    __syncthreads();
+    for (int q = tid; q < RD_TILE; q += nt) {
+      const int j = jt + q;
+      if (j < it.j1) { sh[q] = pool.zk_hi[off + j]; sl[q] = pool.zk_lo[off + j]; }
+    }
+    __syncthreads();
+    const int kmax = min(RD_TILE, it.j1 - jt);
+    float ta = 0.f, tb = 0.f;
+    if (nic == 0) {
+      z0_tile2_f32(sh, sl, kmax, pa, pb, ta, tb);
+    } else {
+      ta = z0_tile_f32<false>(sh, sl, kmax, pa, nic, dnm);
+      tb = z0_tile_f32<false>(sh, sl, kmax, pb, nic, dnm);
+    }
+    two_sum_acc(ha, la, ta);
+    two_sum_acc(hb, lb, tb);
+  }
+  *out_a = (double)ha + (double)la;
+  *out_b = (double)hb + (double)lb;
 }
 
 __device__ __forceinline__ double z0_tile_f64(const rd_d4* __restrict__ sj, int kmax, double px,
@@ -167,30 +260,36 @@ __device__ __forceinline__ double z0_tile_f64(const rd_d4* __restrict__ sj, int 
   return s;
 }
 
-// Partial F_z sum of the item for a point (px, py) at z = 0, in the units
-// that z0_finish turns into V/m.  Loads the j-tiles into shared memory.
+// A point at z = 0 in the FP32 frame of the diode: (x_hi, x_lo, y_hi, y_lo).
+__device__ __forceinline__ float4 z0_point(const DiodeParams& p, double px, double py) {
+  float4 r;
+  split_nm(px, p.org_x, &r.x, &r.y);
+  split_nm(py, p.org_y, &r.z, &r.w);
+  return r;
+}
+
+// Partial F_z sum of the item for one point at z = 0, in the units that
+// z0_finish turns into V/m.  Loads the j-tiles into shared memory.
 template <int PREC>
 __device__ __forceinline__ double z0_item_sum(const DiodeParams& p, const Pool& pool, const ItemRef& it,
-                                              double px, double py, float4* sh, float4* sl,
-                                              rd_d4* sj) {
+                                              double px, double py, float4 pp, float4* sh,
+                                              float4* sl, rd_d4* sj) {
   const int off = p.off, tid = threadIdx.x;
+  const int nic = p.image_charge ? p.N_ic_max : 0;
   if (PREC == 1) {
-    float pxh, pxl, pyh, pyl;
-    split_nm(px, p.org_x, &pxh, &pxl);
-    split_nm(py, p.org_y, &pyh, &pyl);
     const float dnm = (float)(p.d * 1.0e9);
-    const int nic = p.image_charge ? p.N_ic_max : 0;
     float hi = 0.f, lo = 0.f;
     for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
       __syncthreads();
       int j = jt + tid;
-      if (j < it.j1) { sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j]; }
+      if (j < it.j1) { sh[tid] = pool.zk_hi[off + j]; sl[tid] = pool.zk_lo[off + j]; }
       __syncthreads();
-      two_sum_acc(hi, lo, z0_tile_f32(sh, sl, min(RD_TILE, it.j1 - jt), pxh, pxl, pyh, pyl, nic, dnm));
+      const int kmax = min(RD_TILE, it.j1 - jt);
+      two_sum_acc(hi, lo, nic == 0 ? z0_tile_f32<true>(sh, sl, kmax, pp, 0, dnm)
+                                   : z0_tile_f32<false>(sh, sl, kmax, pp, nic, dnm));
     }
     return (double)hi + (double)lo;
   } else {
-    const int nic = p.image_charge ? p.N_ic_max : 0;
     double s = 0.0;
     for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
       __syncthreads();
@@ -212,30 +311,47 @@ __device__ __forceinline__ double z0_finish(const DiodeParams& p, double s, doub
   return p.E_z + f * c_k.div_fac_c * s;
 }
 
+// F_z at the supply quadrature points (qpp holds their FP32-frame split).
+// FP32: 64 threads, two points each; FP64: 128 threads, one point each.
 template <int PREC>
 __global__ void __launch_bounds__(RD_ITILE)
 k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __restrict__ plan,
             const PlanHeader* __restrict__ ph, const double* __restrict__ qx,
-            const double* __restrict__ qy, double* __restrict__ qF, double* __restrict__ partial,
-            int* __restrict__ tickets, double kscale) {
+            const double* __restrict__ qy, const float4* __restrict__ qpp, double* __restrict__ qF,
+            double* __restrict__ partial, int* __restrict__ tickets, double kscale) {
   __shared__ float4 sh[RD_TILE], sl[RD_TILE];
   __shared__ rd_d4 sj[RD_TILE];
+  constexpr int CPT = PREC == 1 ? 2 : 1;
+  const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
-    const int m = plan[it.d].n_i, i = it.i0 + tid;
-    const bool valid = i < m;
-    const int qo = p.q_off;
-    double px = valid ? qx[qo + i] : p.em_x0, py = valid ? qy[qo + i] : p.em_y0;
-    double s = z0_item_sum<PREC>(p, pool, it, px, py, sh, sl, sj);
-    if (it.nch > 1) {
-      partial[(size_t)g * RD_ITILE + tid] = s;
-      if (!tile_ticket(tickets, it)) continue;
-      s = 0.0;
-      for (int c = 0; c < it.nch; ++c) s += __ldcg(partial + (size_t)(it.base + c) * RD_ITILE + tid);
+    const int m = plan[it.d].n_i, qo = p.q_off;
+    double s[CPT];
+    if (PREC == 1) {
+      const int i0 = it.i0 + tid, i1 = it.i0 + nt + tid;
+      const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      z0_item_sum2(p, pool, it, i0 < m ? qpp[qo + i0] : z4, i1 < m ? qpp[qo + i1] : z4, sh, sl,
+                   &s[0], &s[CPT - 1]);
+    } else {
+      const int i = it.i0 + tid;
+      const bool valid = i < m;
+      s[0] = z0_item_sum<PREC>(p, pool, it, valid ? qx[qo + i] : p.em_x0, valid ? qy[qo + i] : p.em_y0,
+                               make_float4(0.f, 0.f, 0.f, 0.f), sh, sl, sj);
     }
-    if (valid) qF[qo + i] = z0_finish<PREC>(p, s, kscale);
+    if (it.nch > 1) {
+      for (int q = 0; q < CPT; ++q) partial[(size_t)g * RD_ITILE + tid + q * nt] = s[q];
+      if (!tile_ticket(tickets, it)) continue;
+      for (int q = 0; q < CPT; ++q) {
+        s[q] = 0.0;
+        for (int c = 0; c < it.nch; ++c) s[q] += __ldcg(partial + (size_t)(it.base + c) * RD_ITILE + tid + q * nt);
+      }
+    }
+    for (int q = 0; q < CPT; ++q) {
+      const int i = it.i0 + tid + q * nt;
+      if (i < m) qF[qo + i] = z0_finish<PREC>(p, s[q], kscale);
+    }
   }
 }
 
@@ -317,14 +433,13 @@ __device__ double warp_field_planar_z0(const DiodeParams& p, const Pool& pool, i
   const int nic = p.image_charge ? p.N_ic_max : 0;
   double s;
   if (PREC == 1) {
-    float pxh, pxl, pyh, pyl;
-    split_nm(px, p.org_x, &pxh, &pxl);
-    split_nm(py, p.org_y, &pyh, &pyl);
+    const float4 pp = z0_point(p, px, py);
     const float dnm = (float)(p.d * 1.0e9);
     float hi = 0.f, lo = 0.f;
     for (int j = lane; j < n; j += 32) {
-      float4 h = pool.pk_hi[off + j], l = pool.pk_lo[off + j];
-      two_sum_acc(hi, lo, z0_tile_f32(&h, &l, 1, pxh, pxl, pyh, pyl, nic, dnm));
+      float4 h = pool.zk_hi[off + j], l = pool.zk_lo[off + j];
+      two_sum_acc(hi, lo, nic == 0 ? z0_tile_f32<true>(&h, &l, 1, pp, 0, dnm)
+                                   : z0_tile_f32<false>(&h, &l, 1, pp, nic, dnm));
     }
     s = (double)hi + (double)lo;
   } else {
@@ -394,7 +509,7 @@ __device__ __forceinline__ double tip_target_log(const DiodeParams& p, double F,
 template <int PREC>
 __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
                           const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
-                          ChainState cs, const int* __restrict__ ch_off, const double* __restrict__ work,
+                          ChainState cs, const int* __restrict__ ch_off, const double* __restrict__ wtab,
                           const int* __restrict__ step_ptr, double kscale) {
   const int nd = ph->n_diodes;
   const int warps_total = (gridDim.x * blockDim.x) >> 5;
@@ -426,7 +541,7 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
         double Fz = warp_field_planar_z0<PREC>(p, pool, n, x, y, kscale);
         if (Fz < 0.0) {
           ok = 1; F = Fz; X = x; Y = y;
-          sup = fn_supply_log(Fz, work_at(p, work, x, y, nullptr), p.image_charge);
+          sup = supply_log_tab(p, wtab, work_cell(p, x, y), Fz);
         }
       }
     }
@@ -439,7 +554,14 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
       }
       cs.ok[k] = ok; cs.F[k] = F; cs.sup[k] = sup;
       if (p.geometry == RD_G_TIP) { cs.x[k] = xi; cs.y[k] = ph_; cs.tx[k] = X; cs.ty[k] = Y; cs.tz[k] = Z; }
-      else { cs.x[k] = X; cs.y[k] = Y; }
+      else {
+        cs.x[k] = X; cs.y[k] = Y;
+        if (ok) {   // Gaussian pair of the first jump
+          double g1, g2;
+          gauss2(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
+          cs.gx[k] = g1; cs.gy[k] = g2;
+        }
+      }
     }
   }
 }
@@ -448,11 +570,11 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
 __device__ __forceinline__ void mh_counts_and_update(const DiodeParams& p, DiodeDyn& y, int tiles,
                                                      int it_idx, int ndim_first, int a, int r,
                                                      int* red_i) {
-  // block reduce (a, r)
-  const int tid = threadIdx.x;
+  // block reduce (a, r); blockDim is a power of two <= RD_ITILE
+  const int tid = threadIdx.x, nt = blockDim.x;
   red_i[tid] = a; red_i[RD_ITILE + tid] = r;
   __syncthreads();
-  for (int s = RD_ITILE / 2; s > 0; s >>= 1) {
+  for (int s = nt / 2; s > 0; s >>= 1) {
     if (tid < s) { red_i[tid] += red_i[tid + s]; red_i[RD_ITILE + tid] += red_i[RD_ITILE + tid + s]; }
     __syncthreads();
   }
@@ -477,54 +599,105 @@ __device__ __forceinline__ void mh_counts_and_update(const DiodeParams& p, Diode
   __syncthreads();
 }
 
+// Accept / reject of one planar proposal (:1400-1443) and the Gaussian pair
+// of the chain's next proposal.  Returns 1 for accepted, 0 for rejected.
+__device__ __forceinline__ int mh_accept_one(const DiodeParams& p, ChainState& cs, const double* wtab,
+                                             int c, int k, int it_idx, uint32_t step, double F,
+                                             double wx, double wy) {
+  int a = 0;
+  if (F < 0.0) {
+    const double sn = supply_log_tab(p, wtab, work_cell(p, wx, wy), F);
+    const double sc = cs.sup[k];
+    bool take = sn >= sc;
+    if (!take) {
+      double u1, u2;
+      rng2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, &u1, &u2);
+      take = log(u1) <= sn - sc;
+    }
+    if (take) { cs.x[k] = wx; cs.y[k] = wy; cs.sup[k] = sn; cs.F[k] = F; a = 1; }
+  }
+  if (it_idx < p.mh_jumps) {
+    double g1, g2;
+    gauss2(p.seed, (uint32_t)c, (uint32_t)(it_idx + 1), step, &g1, &g2);
+    cs.gx[k] = g1; cs.gy[k] = g2;
+  }
+  return a;
+}
+
+// One Metropolis-Hastings jump iteration of the planar chains.  The
+// proposal is the stored Gaussian pair (box_muller, src/mod_global.F90:
+// 578-595) times the step size of this iteration (fixed during the warm-up,
+// MH_std afterwards, :1373-1378) plus the current position, reflected at the
+// emitter edges (check_limits_metro_rec :1466-1516).  The CTA completing a
+// tile then runs the accept / reject test of its chains (:1400-1443), draws
+// their next Gaussian pairs and counts acceptances; the tile completing the
+// diode updates MH_std from the iteration's acceptance rate (:1438-1443).
+// FP32: 64 threads, two chains each; FP64: 128 threads, one chain each.
 template <int PREC>
 __global__ void __launch_bounds__(RD_ITILE)
 k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
-                 const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
-                 ChainState cs, const int* __restrict__ ch_off, const double* __restrict__ work,
+                 const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph, ChainState cs,
+                 const int* __restrict__ ch_off, const double* __restrict__ wtab,
                  const int* __restrict__ step_ptr, int it_idx, double* __restrict__ partial,
                  int* __restrict__ tickets, double kscale) {
   __shared__ float4 sh[RD_TILE], sl[RD_TILE];
   __shared__ rd_d4 sj[RD_TILE];
   __shared__ int red_i[2 * RD_ITILE];
+  constexpr int CPT = PREC == 1 ? 2 : 1;
+  const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     if (p.geometry != RD_G_PLANAR || it_idx > p.mh_jumps) continue;
     DiodeDyn& y = Dy[it.d];
-    const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
-    const int M = plan[it.d].n_i, c = it.i0 + tid, k = ch_off[it.d] + c;
-    const bool valid = c < M;
-    const int ok = valid ? cs.ok[k] : 0;
+    const double mhs = y.MH_std;
     const int ndim_first = (int)nint_d(p.mh_jumps * 0.25);
-    // proposal from k_mh_propose
-    const double wx = ok ? cs.px[k] : p.em_x0, wy = ok ? cs.py[k] : p.em_y0;
-    double s = z0_item_sum<PREC>(p, pool, it, wx, wy, sh, sl, sj);
-    if (it.nch > 1) {
-      partial[(size_t)g * RD_ITILE + tid] = s;
-      if (!tile_ticket(tickets, it)) continue;
-      s = 0.0;
-      for (int cc = 0; cc < it.nch; ++cc) s += __ldcg(partial + (size_t)(it.base + cc) * RD_ITILE + tid);
-    }
-    // accept / reject (:1400-1443)
-    int a = 0, r = 0;
-    if (ok) {
-      double F = z0_finish<PREC>(p, s, kscale);
-      if (F >= 0.0) {
-        r = 1;
-      } else {
-        double sn = fn_supply_log(F, work_at(p, work, wx, wy, nullptr), p.image_charge);
-        double sc = cs.sup[k];
-        bool take = sn >= sc;
-        if (!take) {
-          double u1, u2;
-          rng2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, &u1, &u2);
-          take = log(u1) <= sn - sc;
-        }
-        if (take) { cs.x[k] = wx; cs.y[k] = wy; cs.sup[k] = sn; cs.F[k] = F; a = 1; }
-        else r = 1;
+    const double sx = (it_idx > ndim_first) ? p.em_Lx * mhs : p.em_Lx * 0.10;
+    const double sy = (it_idx > ndim_first) ? p.em_Ly * mhs : p.em_Ly * 0.10;
+    const int M = plan[it.d].n_i;
+    int ok[CPT], kk[CPT];
+    double wx[CPT], wy[CPT];
+    for (int q = 0; q < CPT; ++q) {
+      const int c = it.i0 + tid + q * nt;
+      kk[q] = ch_off[it.d] + c;
+      ok[q] = (c < M) ? cs.ok[kk[q]] : 0;
+      wx[q] = p.em_x0; wy[q] = p.em_y0;
+      if (ok[q]) {
+        const int k = kk[q];
+        double x = cs.gx[k] * sx + cs.x[k], yv = cs.gy[k] * sy + cs.y[k];
+        const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+        if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
+        if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
+        wx[q] = x; wy[q] = yv;
       }
+    }
+    double s[CPT];
+    if (PREC == 1) {
+      z0_item_sum2(p, pool, it, z0_point(p, wx[0], wy[0]), z0_point(p, wx[CPT - 1], wy[CPT - 1]), sh, sl,
+                   &s[0], &s[CPT - 1]);
+    } else {
+      s[0] = z0_item_sum<PREC>(p, pool, it, wx[0], wy[0], make_float4(0.f, 0.f, 0.f, 0.f), sh, sl, sj);
+    }
+    if (it.nch > 1) {
+      for (int q = 0; q < CPT; ++q) partial[(size_t)g * RD_ITILE + tid + q * nt] = s[q];
+      if (!tile_ticket(tickets, it)) continue;
+      for (int q = 0; q < CPT; ++q) {
+        s[q] = 0.0;
+        for (int cc = 0; cc < it.nch; ++cc)
+          s[q] += __ldcg(partial + (size_t)(it.base + cc) * RD_ITILE + tid + q * nt);
+      }
+    }
+    // epilogue of the completed tile
+    const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
+    int a = 0, r = 0;
+    for (int q = 0; q < CPT; ++q) {
+      if (!ok[q]) continue;
+      const int c = it.i0 + tid + q * nt;
+      const double F = z0_finish<PREC>(p, s[q], kscale);
+      const int acc = mh_accept_one(p, cs, wtab, c, kk[q], it_idx, step, F, wx[q], wy[q]);
+      a += acc;
+      r += 1 - acc;
     }
     mh_counts_and_update(p, y, plan[it.d].tiles, it_idx, ndim_first, a, r, red_i);
   }
@@ -654,7 +827,7 @@ __global__ void k_mh_propose(const DiodeParams* __restrict__ P, const DiodeDyn* 
     while (lo < hi) { int mid = (lo + hi + 1) >> 1; if (plan[mid].pad0 <= g) lo = mid; else hi = mid - 1; }
     const int d = lo, c = g - plan[d].pad0;
     const DiodeParams& p = P[d];
-    if (it_idx > p.mh_jumps) continue;
+    if (p.geometry != RD_G_TIP || it_idx > p.mh_jumps) continue;
     const int k = ch_off[d] + c;
     if (!cs.ok[k]) continue;
     const DiodeDyn& y = Dy[d];
@@ -797,21 +970,21 @@ cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st
                                    const PlanHeader* ph, const PointSet& pts, double* partial,
                                    int* tickets, double kscale) {
   if (prec == 1) {
-    if (geom == RD_G_TIP) k_field_points<1, RD_G_TIP><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
-    else k_field_points<1, RD_G_PLANAR><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
+    if (geom == RD_G_TIP) k_field_points<1, RD_G_TIP><<<rd_grid(k_field_points<1, RD_G_TIP>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
+    else k_field_points<1, RD_G_PLANAR><<<rd_grid(k_field_points<1, RD_G_PLANAR>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
   } else {
-    if (geom == RD_G_TIP) k_field_points<0, RD_G_TIP><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
-    else k_field_points<0, RD_G_PLANAR><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
+    if (geom == RD_G_TIP) k_field_points<0, RD_G_TIP><<<rd_grid(k_field_points<0, RD_G_TIP>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
+    else k_field_points<0, RD_G_PLANAR><<<rd_grid(k_field_points<0, RD_G_PLANAR>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph, pts, partial, tickets, kscale);
   }
   return cudaGetLastError();
 }
 
 cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const DiodeParams* P,
                                 const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
-                                const double* qx, const double* qy, double* qF, double* partial,
-                                int* tickets, double kscale) {
-  if (prec == 1) k_z0_points<1><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, qx, qy, qF, partial, tickets, kscale);
-  else k_z0_points<0><<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, qx, qy, qF, partial, tickets, kscale);
+                                const double* qx, const double* qy, const float4* qpp, double* qF,
+                                double* partial, int* tickets, double kscale) {
+  if (prec == 1) k_z0_points<1><<<rd_grid(k_z0_points<1>, 64, grid), 64, 0, st>>>(P, pool, plan, ph, qx, qy, qpp, qF, partial, tickets, kscale);
+  else k_z0_points<0><<<rd_grid(k_z0_points<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph, qx, qy, qpp, qF, partial, tickets, kscale);
   return cudaGetLastError();
 }
 
@@ -826,25 +999,25 @@ cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodePara
 cudaError_t rd_launch_mh_init(int prec, int grid, cudaStream_t st, const DiodeParams* P,
                               DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
                               const PlanHeader* ph, const ChainState& cs, const int* ch_off,
-                              const double* work, const int* step_ptr, double kscale) {
-  if (prec == 1) k_mh_init<1><<<grid, 256, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, work, step_ptr, kscale);
-  else k_mh_init<0><<<grid, 256, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, work, step_ptr, kscale);
+                              const double* wtab, const int* step_ptr, double kscale) {
+  if (prec == 1) k_mh_init<1><<<rd_grid(k_mh_init<1>, 256, grid), 256, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, kscale);
+  else k_mh_init<0><<<rd_grid(k_mh_init<0>, 256, grid), 256, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, kscale);
   return cudaGetLastError();
 }
 
 cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_t st,
                               const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
-                              const int* ch_off, const double* work, const int* step_ptr,
+                              const int* ch_off, const double* wtab, const int* step_ptr,
                               int it_idx, double* partial, int* tickets, double kscale) {
-  k_mh_propose<<<grid, 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx);
   if (geometry_mask & 1) {
-    if (prec == 1) k_mh_jump_planar<1><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, work, step_ptr, it_idx, partial, tickets, kscale);
-    else k_mh_jump_planar<0><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, work, step_ptr, it_idx, partial, tickets, kscale);
+    if (prec == 1) k_mh_jump_planar<1><<<rd_grid(k_mh_jump_planar<1>, 64, grid), 64, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale);
+    else k_mh_jump_planar<0><<<rd_grid(k_mh_jump_planar<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale);
   }
   if (geometry_mask & 2) {
-    if (prec == 1) k_mh_jump_tip<1><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale);
-    else k_mh_jump_tip<0><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale);
+    k_mh_propose<<<rd_grid(k_mh_propose, 256, grid), 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx);
+    if (prec == 1) k_mh_jump_tip<1><<<rd_grid(k_mh_jump_tip<1>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale);
+    else k_mh_jump_tip<0><<<rd_grid(k_mh_jump_tip<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale);
   }
   return cudaGetLastError();
 }

@@ -23,6 +23,130 @@
 
 namespace {
 
+// ---- planar, FP32 compensated, one image partner (N_ic_max = 0) -----------------
+// Two i-particles per thread (64 threads per 128-particle tile), so one
+// shared-memory load of a j-particle feeds two pairs.  Per pair: the Coulomb
+// term and the n = 0 image partner at -z_j, whose height difference is
+// z_i + z_j = 2 z_i - dz (2 z_i as one float: relative error 6e-8).  The
+// 1e-20 nm^2 floor inside dxy^2 keeps the self pair and coincident pairs
+// finite (their q or d is zero).
+template <bool IC, bool DIAG>
+__device__ __forceinline__ void planar_tile2_nic0(const float4* __restrict__ sh, const float4* __restrict__ sl,
+                                                  int kmax, float4 ah, float4 al, float atz, float4 bh,
+                                                  float4 bl, float btz, int self_a, int self_b,
+                                                  float3& ta, float3& tb) {
+  float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
+#pragma unroll 2
+  for (int k = 0; k < kmax; ++k) {
+    const float4 h = sh[k], l = sl[k];
+    const float qa = (DIAG && k == self_a) ? 0.f : h.w;
+    const float qb = (DIAG && k == self_b) ? 0.f : h.w;
+    {
+      const float dx = (ah.x - h.x) + (al.x - l.x), dy = (ah.y - h.y) + (al.y - l.y);
+      const float dz = (ah.z - h.z) + (al.z - l.z);
+      const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, 1e-20f));
+      const float inv = rsqrtf(fmaf(dz, dz, dxy2));
+      const float s = qa * ((inv * inv) * inv);
+      if (IC) {
+        const float zs = atz - dz;
+        const float ri = rsqrtf(fmaf(zs, zs, dxy2));
+        const float si = qa * ((ri * ri) * ri);
+        const float t = s - si;
+        ax = fmaf(t, dx, ax); ay = fmaf(t, dy, ay);
+        az = fmaf(s, dz, fmaf(-si, zs, az));
+      } else {
+        ax = fmaf(s, dx, ax); ay = fmaf(s, dy, ay); az = fmaf(s, dz, az);
+      }
+    }
+    {
+      const float dx = (bh.x - h.x) + (bl.x - l.x), dy = (bh.y - h.y) + (bl.y - l.y);
+      const float dz = (bh.z - h.z) + (bl.z - l.z);
+      const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, 1e-20f));
+      const float inv = rsqrtf(fmaf(dz, dz, dxy2));
+      const float s = qb * ((inv * inv) * inv);
+      if (IC) {
+        const float zs = btz - dz;
+        const float ri = rsqrtf(fmaf(zs, zs, dxy2));
+        const float si = qb * ((ri * ri) * ri);
+        const float t = s - si;
+        bx = fmaf(t, dx, bx); by = fmaf(t, dy, by);
+        bz = fmaf(s, dz, fmaf(-si, zs, bz));
+      } else {
+        bx = fmaf(s, dx, bx); by = fmaf(s, dy, by); bz = fmaf(s, dz, bz);
+      }
+    }
+  }
+  ta.x += ax; ta.y += ay; ta.z += az;
+  tb.x += bx; tb.y += by; tb.z += bz;
+}
+
+__global__ void __launch_bounds__(64)
+k_force_planar_f32_nic0(const DiodeParams* __restrict__ P, Pool pool,
+                        const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                        double* __restrict__ partial, int* __restrict__ tickets, double kscale) {
+  __shared__ float4 sh[RD_TILE], sl[RD_TILE];
+  const int total = ph->total_items, nd = ph->n_diodes;
+  const int tid = threadIdx.x, nt = 64;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    ItemRef it = decode_item(plan, nd, g);
+    const DiodeParams& p = P[it.d];
+    const int off = p.off, n = plan[it.d].n_i;
+    const int ia = it.i0 + tid, ib = it.i0 + nt + tid;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 ah = ia < n ? pool.pk_hi[off + ia] : z4, al = ia < n ? pool.pk_lo[off + ia] : z4;
+    const float4 bh = ib < n ? pool.pk_hi[off + ib] : z4, bl = ib < n ? pool.pk_lo[off + ib] : z4;
+    const float atz = 2.f * (ah.z + al.z), btz = 2.f * (bh.z + bl.z);
+    const bool ic = p.image_charge != 0;
+    F32Acc A, B;
+    A.zero(); B.zero();
+    for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+      __syncthreads();
+      for (int q = tid; q < RD_TILE; q += nt) {
+        const int j = jt + q;
+        if (j < it.j1) { sh[q] = pool.pk_hi[off + j]; sl[q] = pool.pk_lo[off + j]; }
+      }
+      __syncthreads();
+      const int kmax = min(RD_TILE, it.j1 - jt);
+      float3 ta = make_float3(0.f, 0.f, 0.f), tb = ta;
+      const bool diag = (jt == it.i0);
+      if (ic) {
+        if (diag) planar_tile2_nic0<true, true>(sh, sl, kmax, ah, al, atz, bh, bl, btz, tid, nt + tid, ta, tb);
+        else planar_tile2_nic0<true, false>(sh, sl, kmax, ah, al, atz, bh, bl, btz, -1, -1, ta, tb);
+      } else {
+        if (diag) planar_tile2_nic0<false, true>(sh, sl, kmax, ah, al, atz, bh, bl, btz, tid, nt + tid, ta, tb);
+        else planar_tile2_nic0<false, false>(sh, sl, kmax, ah, al, atz, bh, bl, btz, -1, -1, ta, tb);
+      }
+      A.add(ta.x, ta.y, ta.z);
+      B.add(tb.x, tb.y, tb.z);
+    }
+    double f[2][3] = {{(double)A.hx + (double)A.lx, (double)A.hy + (double)A.ly, (double)A.hz + (double)A.lz},
+                      {(double)B.hx + (double)B.lx, (double)B.hy + (double)B.ly, (double)B.hz + (double)B.lz}};
+    if (it.nch > 1) {
+      double* pp = partial + (size_t)g * 3 * RD_ITILE;
+      for (int q = 0; q < 2; ++q)
+        for (int c = 0; c < 3; ++c) pp[c * RD_ITILE + tid + q * nt] = f[q][c];
+      if (!tile_ticket(tickets, it)) continue;
+      for (int q = 0; q < 2; ++q)
+        for (int c = 0; c < 3; ++c) {
+          double v = 0.0;
+          for (int cc = 0; cc < it.nch; ++cc)
+            v += __ldcg(partial + (size_t)(it.base + cc) * 3 * RD_ITILE + c * RD_ITILE + tid + q * nt);
+          f[q][c] = v;
+        }
+    }
+    for (int q = 0; q < 2; ++q) {
+      const int i = it.i0 + tid + q * nt;
+      if (i >= n) continue;
+      const int gi = off + i;
+      const double qi = pool.q[gi], im = 1.0 / pool.m[gi];
+      const double pre = (qi * kscale) * im;   // kscale = k q0 1e18 (nm -> m)
+      pool.ax[gi] = pre * f[q][0];
+      pool.ay[gi] = pre * f[q][1];
+      pool.az[gi] = pre * f[q][2] + qi * p.E_z * im;
+    }
+  }
+}
+
 template <bool NIC0>
 __global__ void __launch_bounds__(RD_ITILE)
 k_force_planar_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
@@ -262,17 +386,17 @@ cudaError_t rd_launch_force(int prec, int geometry_mask, int nic_general, int gr
   // plan (separate plans per geometry are built by the engine).
   if (prec == 0) {
     if (geometry_mask & 1)
-      k_force_planar_f64<<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets);
+      k_force_planar_f64<<<rd_grid(k_force_planar_f64, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets);
     else
-      k_force_tip_f64<<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets);
+      k_force_tip_f64<<<rd_grid(k_force_tip_f64, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets);
   } else {
     if (geometry_mask & 1) {
       if (nic_general)
-        k_force_planar_f32<false><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale);
+        k_force_planar_f32<false><<<rd_grid(k_force_planar_f32<false>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale);
       else
-        k_force_planar_f32<true><<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale);
+        k_force_planar_f32_nic0<<<rd_grid(k_force_planar_f32_nic0, 64, grid), 64, 0, st>>>(P, pool, plan, ph, partial, tickets, kscale);
     } else {
-      k_force_tip_f32<<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale);
+      k_force_tip_f32<<<rd_grid(k_force_tip_f32, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale);
     }
   }
   return cudaGetLastError();

@@ -86,6 +86,9 @@ struct Pool {
   double *q, *m;
   int *species, *id, *step0, *section, *mask;
   float4 *pk_hi, *pk_lo, *ip_hi, *ip_lo;
+  // cathode-field pack (planar): zk_hi = (x_hi, y_hi, max(z^2, tiny), q z),
+  // zk_lo = (x_lo, y_lo, z, q), nm, z as one float (relative precision 6e-8)
+  float4 *zk_hi, *zk_lo;
 };
 
 // One unit of a pair-sum: i-tile (or point block) x j-chunk of one diode.
@@ -108,4 +111,5 @@ struct ChainState {
   double *tx, *ty, *tz;  // tip: cartesian position of the current state
   double *pxx, *pyy, *pzz;  // tip: cartesian position of the proposal
   int *prop_ok;          // proposal inside the domain
+  double *gx, *gy;       // planar: Gaussian pair of the next proposal
 };

@@ -11,7 +11,29 @@
 // the last chunk to finish (an atomic ticket, no waiting) adds the partials
 // in chunk order, so results do not depend on scheduling.
 #pragma once
+#include <mutex>
+#include <unordered_map>
 #include "rd_device.cuh"
+
+// Persistent grid size: a positive request wins; otherwise every SM gets as
+// many CTAs as can be resident at once (occupancy API), cached per kernel.
+template <class F>
+inline int rd_grid(F kernel, int block, int requested) {
+  if (requested > 0) return requested;
+  static std::mutex mu;
+  static std::unordered_map<const void*, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find((const void*)kernel);
+  if (it != cache.end()) return it->second;
+  int dev = 0, sms = 1, per = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, 0) != cudaSuccess || per < 1)
+    per = 1;
+  const int g = sms * per;
+  cache[(const void*)kernel] = g;
+  return g;
+}
 
 struct PlanEntry {
   int item_off;   // first item of this diode

@@ -46,6 +46,11 @@ __device__ __forceinline__ void pack_one(const DiodeParams& p, const Pool& pool,
   l.w = (float)((p.d - z) * 1.0e9);
   pool.pk_hi[gi] = h;
   pool.pk_lo[gi] = l;
+  if (p.geometry == RD_G_PLANAR) {
+    const float zf = (float)(z * 1.0e9), qf = h.w;
+    pool.zk_hi[gi] = make_float4(h.x, h.y, fmaxf(zf * zf, 1e-20f), qf * zf);
+    pool.zk_lo[gi] = make_float4(l.x, l.y, zf, qf);
+  }
   if (p.geometry == RD_G_TIP) {
     double xi, yi, zi;
     double dis = tip_image_point(p, x, y, z, &xi, &yi, &zi);
@@ -398,18 +403,18 @@ cudaError_t rd_launch_plan(cudaStream_t st, const DiodeParams* P, const DiodeDyn
 }
 cudaError_t rd_launch_pack(int grid, cudaStream_t st, const DiodeParams* P, const Pool& pool,
                            const PlanEntry* plan, const PlanHeader* ph) {
-  k_pack<<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph);
+  k_pack<<<rd_grid(k_pack, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph);
   return cudaGetLastError();
 }
 cudaError_t rd_launch_position(int grid, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                const Pool& pool, const PlanEntry* plan, const PlanHeader* ph) {
-  k_position<<<grid, RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph);
+  k_position<<<rd_grid(k_position, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph);
   return cudaGetLastError();
 }
 cudaError_t rd_launch_velocity(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
                                DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
                                const PlanHeader* ph, double* ramo) {
-  k_velocity<<<grid, RD_ITILE, 0, st>>>(P, pool, plan, ph, ramo);
+  k_velocity<<<rd_grid(k_velocity, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph, ramo);
   k_ramo<<<nslots, 256, 0, st>>>(P, Dy, ramo);
   return cudaGetLastError();
 }
@@ -417,9 +422,9 @@ cudaError_t rd_launch_compact(int grid, int nslots, cudaStream_t st, const Diode
                               DiodeDyn* Dy, const Pool& pool, const Pool& tmp,
                               const PlanEntry* plan, const PlanHeader* ph, int* kept, int* life,
                               const int* step_ptr) {
-  k_compact_count<<<grid, 1024, 0, st>>>(P, Dy, pool, plan, ph, kept);
-  k_compact_scatter<<<grid, 1024, 0, st>>>(P, Dy, pool, tmp, plan, ph, kept, life, step_ptr);
-  k_compact_copy<<<grid, 1024, 0, st>>>(P, Dy, pool, tmp, plan, ph);
+  k_compact_count<<<rd_grid(k_compact_count, 1024, grid), 1024, 0, st>>>(P, Dy, pool, plan, ph, kept);
+  k_compact_scatter<<<rd_grid(k_compact_scatter, 1024, grid), 1024, 0, st>>>(P, Dy, pool, tmp, plan, ph, kept, life, step_ptr);
+  k_compact_copy<<<rd_grid(k_compact_copy, 1024, grid), 1024, 0, st>>>(P, Dy, pool, tmp, plan, ph);
   k_compact_finish<<<(nslots + 127) / 128, 128, 0, st>>>(P, Dy, nslots);
   return cudaGetLastError();
 }
