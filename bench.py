@@ -18,6 +18,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -28,6 +29,10 @@ sys.path.insert(0, ROOT)
 NM = 1e-9
 METRIC = "electron-steps/s"
 SEED = 20261203
+WORKLOAD = ("serve: Poisson 20/s requests, each a planar diode with peak electrons log-U[256, 32768], "
+            "V U[0.5, 5] kV, gap U[200, 2000] nm, work function U[2.5, 5.5] eV, emitter side "
+            "U[100, 2000] nm, dt 0.25 fs, 1 image term, steps log-U[500, 20000]; pre-filled to peak N, "
+            "MH 200 jumps, chains capped at capacity")
 
 
 # ---------------------------------------------------------------------------------
@@ -83,7 +88,7 @@ class ClockSampler:
     def __init__(self, device=0):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+        self.path = os.path.join(tempfile.gettempdir(), "rumdeed_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
@@ -232,6 +237,36 @@ def plain_fp64_sample(rg, requests, budget_s=25.0):
 
 
 # ---------------------------------------------------------------------------------
+def reduce_ranks(world, maxes, sums):
+    """Max over ranks of the times, sum over ranks of the work counts."""
+    if world <= 1:
+        return list(maxes) + list(sums)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    mx = torch.tensor(maxes, dtype=torch.float64, device=dev)
+    sm = torch.tensor(sums, dtype=torch.float64, device=dev)
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return [float(x) for x in mx] + [float(x) for x in sm]
+
+
+def profile_figure(name, key):
+    """A figure from a committed ncu summary under profiles/ (a 'key: value'
+    line), or None when the summary is absent."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        s = line.strip().lstrip("-* ").replace("`", "")
+        if s.startswith(key + ":"):
+            try:
+                return float(s.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
 def run_ours(args, rank, world):
     import rumdeed_gb300 as rg
     rg.build()
@@ -277,7 +312,6 @@ def run_ours(args, rank, world):
     for k in range(args.steps):
         flush()
         w0 = time.perf_counter()
-        h2d += 0  # submissions are host-side copies into the engine's request queue
         submit_arrived()
         st = eng.serve(1)
         wall_s += time.perf_counter() - w0
@@ -299,22 +333,37 @@ def run_ours(args, rank, world):
         if s["admit_s"] >= 0:
             qd.append(s["admit_s"] - s["submit_s"])
     # per-phase profile of one more step (dominant kernel: MH jump launches)
-    prof = eng.profile_step(eng_step := 10 ** 6)
+    prof = eng.profile_step(10 ** 6)
     resident = [submitted[r] for r in list(submitted) if eng.poll(r)["state"] == rg.REQ_RUNNING]
+
+    # End to end through the public API (rd_submit / rd_serve, host buffers): every
+    # request is cancelled, then the same resident requests are submitted again at
+    # once from host memory, as new simulations.  The wall clock covers the
+    # submissions, their admission (host -> device uploads through the engine's
+    # pinned stage) and K serving iterations, each reading the per-diode counters
+    # back to the host.
+    for rid in list(submitted):
+        if eng.poll(rid)["state"] in (rg.REQ_QUEUED, rg.REQ_RUNNING):
+            eng.cancel(rid)
+    burst = sorted(resident, key=lambda q: q["index"])
+    burst_pos = [prefill(r) for r in burst]
+    e2e_steps, e2e_h2d, e2e_d2h = 0, 0, 0
+    w0 = time.perf_counter()
+    for r, pos in zip(burst, burst_pos):
+        eng.submit(r["steps"], pos=pos, **diode_kwargs(r))
+    for k in range(args.steps):
+        st = eng.serve(1)
+        e2e_steps += st["electron_steps"]
+        e2e_h2d += st["h2d_bytes"]
+        e2e_d2h += st["d2h_bytes"]
+    e2e_wall = time.perf_counter() - w0
     eng.close()
 
     tot_dev = dev_ms / 1e3
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([tot_dev, wall_s, float(e_steps)], dtype=torch.float64, device="cuda")
-        mx = t.clone(); dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm = t.clone(); dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        tot_dev, wall_s, e_all = float(mx[0]), float(mx[1]), float(sm[2])
-    else:
-        e_all = float(e_steps)
+    tot_dev, wall_s, e2e_wall, e_all, e2e_all = reduce_ranks(
+        world, [tot_dev, wall_s, e2e_wall], [float(e_steps), float(e2e_steps)])
     value = e_all / tot_dev if tot_dev > 0 else 0.0
-    e2e = e_all / wall_s if wall_s > 0 else 0.0
+    e2e = e2e_all / e2e_wall if e2e_wall > 0 else 0.0
     if rank != 0:
         return
     # dominant kernel roofline (FP32 pipe; 20 flops per Coulomb-like term)
@@ -327,11 +376,7 @@ def run_ours(args, rank, world):
     if peak is None:
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
         peak_src = "nominal: 152 SMs x 128 lanes x 2 x 2.07 GHz"
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "mh_jump_traffic.json")
-    if os.path.exists(tpath):
-        tj = json.load(open(tpath))
-        traffic = tj["dram_bytes_per_pair_eval"] * prof["mh_pair_evals"] / launches
+    traffic = profile_figure("k_mh_jump_planar_serve128.md", "dram_bytes_per_launch")
     plain_v, plain_caps = plain_fp64_sample(rg, resident, budget_s=args.plain_budget)
     cpu_v, cpu_desc, cores, cpu_t = cpu_sample(SEED, rank=rank)
     line = {
@@ -339,9 +384,8 @@ def run_ours(args, rank, world):
         "warmup": args.warmup, "ms_per_step": dev_ms / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 pair sums (compensated) + f64 integration/FN",
-        "data": "synthetic request stream (seeded; configs[3] distributions)",
-        "config": {"workload": "serve: Poisson 20/s planar-diode requests, configs[2] distributions, "
-                               "pre-filled to peak N, MH 200 jumps, chains capped at capacity",
+        "data": "synthetic request stream (seeded PCG64; no dataset involved)",
+        "config": {"workload": WORKLOAD,
                    "slots": S, "precision": "fp32c", "parallelism": "replicas" if world > 1 else "1 GPU",
                    "l2": "256 MB buffer written between timed iterations",
                    "resident_diodes": running, "queued_requests": queued,
@@ -353,16 +397,25 @@ def run_ours(args, rank, world):
                     "queueing_delay_s_p99": float(np.percentile(qd, 99)) if qd else None,
                     "simulation_latency": "no simulation completes inside the window: "
                                           "projected = steps x step time (>= 500 steps)"},
-        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": h2d / max(args.steps, 1),
-                "d2h_bytes_per_step": d2h / max(args.steps, 1)},
+        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": e2e_h2d / max(args.steps, 1),
+                "d2h_bytes_per_step": e2e_d2h / max(args.steps, 1),
+                "window": "the %d resident requests submitted again from host memory at once, "
+                          "admitted (uploads through the pinned stage) and served %d iterations "
+                          "with counter read-back; wall clock; no L2 flush" % (len(burst), args.steps),
+                "steady_state": {"value": e_all / wall_s if wall_s > 0 else 0.0,
+                                 "h2d_bytes_per_step": h2d / max(args.steps, 1),
+                                 "d2h_bytes_per_step": d2h / max(args.steps, 1),
+                                 "window": "the timed serving iterations, wall clock"}},
         "plain_fp64_one_diode_at_a_time": {"value": plain_v, "unit": METRIC,
                                            "sample_capacities": plain_caps,
                                            "served_over_plain": value / plain_v if plain_v else None},
-        "gpu_launches": args.steps * (kps + 1) + 2 * admitted,
-        "roofline": {"bound": "fp32", "kernel": "k_mh_jump_planar<fp32c>",
+        "gpu_launches": 2 * args.steps * (kps + 1) + 2 * (admitted + len(burst)),
+        "roofline": {"bound": "fp32", "kernel": "k_mh_jump_planar<1>",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_source": peak_src,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch "
+                                       "on the burst case (the same 128 resident requests)",
                      "flops_convention": "20 flops per Coulomb-like term (Nyland et al.); "
                                          "1 term per (chain, particle) at the cathode"},
         "phase_ms": {k: prof[k] for k in ("supply_ms", "mh_init_ms", "mh_jumps_ms", "emit_ms",
@@ -389,14 +442,146 @@ def run_reference(args, rank, world):
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_all / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic request stream (seeded; configs[3] distributions)",
-            "config": {"workload": "serve: Poisson 20/s planar-diode requests (bounded CPU sample)"},
+            "dtype": "f64", "data": "synthetic request stream (seeded PCG64; no dataset involved)",
+            "config": {"workload": WORKLOAD + " (bounded CPU sample)"},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
                              "sample": desc + " (the Fortran reference cannot be built here: no "
                                               "Fortran compiler, Cuba 4.2.2 not vendored)"},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------
+# Secondary workloads (--case).  Each prints JSON lines of its own; none of them
+# is the headline line above.
+
+def micro_positions(n, seed):
+    """n electrons, x, y uniform in a 1000 x 1000 nm box centred on the
+    emitter centre, z uniform in [1, 999] nm (PCG64 seed per size)."""
+    rng = np.random.default_rng(seed)
+    return np.column_stack([rng.uniform(-500 * NM, 500 * NM, n), rng.uniform(-500 * NM, 500 * NM, n),
+                            rng.uniform(1 * NM, 999 * NM, n)])
+
+
+def cathode_grid(m=64):
+    """m x m cell midpoints of the 1000 x 1000 nm cathode at z = 0."""
+    c = (np.arange(m) + 0.5) / m * 1000 * NM - 500 * NM
+    gx, gy = np.meshgrid(c, c, indexing="ij")
+    return np.column_stack([gx.ravel(), gy.ravel(), np.zeros(m * m)])
+
+
+def rel_err(got, ref):
+    """Per-row norm-relative error |got - ref| / |ref|: (max, rms)."""
+    e = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+    return float(e.max()), float(np.sqrt(np.mean(e * e)))
+
+
+def case_micro(args):
+    """Force/field kernel microbench: N uniform electrons (gap 1000 nm, V 2 kV,
+    planar image series N_ic_max in {0, 7}, i.e. 1 or 29 image partners), the
+    all-pair force of the FP32-compensated form against the FP64 form (max and
+    RMS per-particle relative error) and the field at the 64 x 64 cathode
+    midpoints.  Pair-interactions/s from device time (CUDA events)."""
+    import rumdeed_gb300 as rg
+    rg.build()
+    peak = measure_fp32_peak()
+    sizes = [int(s) for s in args.sizes.split(",")]
+    nics = [int(s) for s in args.nics.split(",")]
+    grid = cathode_grid(64)
+    for N in sizes:
+        pos = micro_positions(N, {4096: 1, 65536: 2, 262144: 3}.get(N, 4))
+        for nic in nics:
+            terms = 1 + 1 + 4 * nic
+            pairs = float(N) * (N - 1)
+            out = {"case": "micro", "N": N, "N_ic_max": nic, "terms_per_pair": terms}
+            res = {}
+            for prec, tag in ((rg.PREC_FP32C, "fp32c"), (rg.PREC_FP64, "fp64")):
+                if prec == rg.PREC_FP64 and pairs * terms > args.fp64_budget:
+                    out["fp64"] = "not run: %.2g pair-terms exceeds --fp64-budget" % (pairs * terms)
+                    continue
+                eng = rg.Engine(precision=prec, max_diodes=1, particle_capacity=N + 1024,
+                                chain_capacity=4096, quad_capacity=4096)
+                d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, capacity=N, image_charge=True, N_ic_max=nic)
+                d.add_particles(pos)
+                acc = d.calculate_acceleration_particles()
+                reps = 1 if pairs * terms > 2e11 else (3 if pairs > 1e9 else 20)
+                ms = eng.time_accel(reps)
+                fld = d.calc_field_at_batch(grid)
+                fms = d.time_field_at(grid, reps=max(reps, 3))
+                res[tag] = (acc, fld)
+                out[tag] = {"force_ms": ms, "force_pairs_per_s": pairs / (ms / 1e3),
+                            "force_tflops": 20.0 * terms * pairs / (ms / 1e3) / 1e12,
+                            "field_ms": fms, "field_point_particle_per_s": grid.shape[0] * N / (fms / 1e3)}
+                if prec == rg.PREC_FP32C and peak:
+                    out[tag]["force_frac_of_measured_fp32"] = out[tag]["force_tflops"] / peak
+                eng.close()
+            if "fp64" in res:
+                out["force_rel_err_max"], out["force_rel_err_rms"] = rel_err(res["fp32c"][0], res["fp64"][0])
+                out["field_rel_err_max"], out["field_rel_err_rms"] = rel_err(res["fp32c"][1], res["fp64"][1])
+                # the cathode field is the vacuum field minus the space-charge sum; where they
+                # nearly cancel, |E| is small and its relative error large: also against |E_vac|
+                dv = np.linalg.norm(res["fp32c"][1] - res["fp64"][1], axis=1) / (2.0e3 / (1000 * NM))
+                out["field_err_max_over_vacuum"] = float(dv.max())
+                out["field_min_over_vacuum"] = float(np.linalg.norm(res["fp64"][1], axis=1).min()
+                                                     / (2.0e3 / (1000 * NM)))
+            out["fp32_peak_tflops"] = peak
+            print(json.dumps(out), flush=True)
+
+
+def case_burst(args):
+    """The first S requests of the serving stream admitted at once (no arrival
+    pacing), then W + K serving iterations: the serving workload with a fixed
+    resident set and a fixed launch order, for profiler captures."""
+    import rumdeed_gb300 as rg
+    rg.build()
+    S = args.slots
+    free0 = None
+    try:
+        import torch
+        free0 = torch.cuda.mem_get_info()[0]
+    except Exception:
+        pass
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=S, particle_capacity=S * 32768 + 4096,
+                    chain_capacity=S * 32768 + 4096, quad_capacity=S * 4096 + 4096)
+    stream = RequestStream(SEED)
+    reqs = [stream.next() for _ in range(S)]
+    for r in reqs:
+        eng.submit(r["steps"], pos=prefill(r), **diode_kwargs(r))
+    ms, es = [], 0
+    for k in range(args.warmup + args.steps):
+        st = eng.serve(1)
+        if k >= args.warmup:
+            ms.append(st["device_ms"])
+            es += st["electron_steps"]
+    used = None
+    if free0 is not None:
+        import torch
+        used = (free0 - torch.cuda.mem_get_info()[0]) / 2 ** 30
+    eng.close()
+    print(json.dumps({"case": "burst", "slots": S, "steps": args.steps, "warmup": args.warmup,
+                      "electron_steps_per_s": es / (sum(ms) / 1e3) if ms else 0.0,
+                      "step_ms": ms, "device_gib_used": used}), flush=True)
+
+
+def case_mh_small(args):
+    """Small emission case for full profiler captures: 4 planar diodes of 6000
+    electrons (1000 x 1000 nm emitter, 3 kV over 1000 nm, work function 3.5 eV,
+    chains capped at 6000), one profiled step."""
+    import rumdeed_gb300 as rg
+    rg.build()
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=4, particle_capacity=4 * 8192,
+                    chain_capacity=4 * 8192, quad_capacity=4 * 4096)
+    rng = np.random.default_rng(1)
+    n, side = 6000, 1000 * NM
+    for k in range(4):
+        d = eng.add_diode(V_s=3000.0, gap=1000 * NM, capacity=n, emitter_pos=(-side / 2, -side / 2),
+                          emitter_dim=(side, side), work=[[3.5]], emission=True, max_chains=n, seed=10 + k)
+        d.add_particles(np.column_stack([rng.uniform(-side / 2, side / 2, n), rng.uniform(-side / 2, side / 2, n),
+                                         rng.uniform(1 * NM, 999 * NM, n)]), step=0)
+    p = eng.profile_step(1)
+    eng.close()
+    print(json.dumps({"case": "mh-small", **p}), flush=True)
 
 
 def main():
@@ -408,6 +593,12 @@ def main():
     ap.add_argument("--slots", type=int, default=128)
     ap.add_argument("--plain-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=1.0e10)
+    ap.add_argument("--case", default="serve", choices=["serve", "micro", "burst", "mh-small"],
+                    help="serve: the headline serving benchmark; the others are secondary workloads")
+    ap.add_argument("--sizes", default="4096,65536,262144", help="micro: electron counts")
+    ap.add_argument("--nics", default="0,7", help="micro: N_ic_max values")
+    ap.add_argument("--fp64-budget", type=float, default=2.0e11,
+                    help="micro: largest N(N-1) x terms run in FP64 for the error check")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -417,7 +608,10 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    if args.impl == "reference":
+    if args.case != "serve":
+        if rank == 0:
+            {"micro": case_micro, "burst": case_burst, "mh-small": case_mh_small}[args.case](args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world)

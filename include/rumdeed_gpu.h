@@ -51,8 +51,9 @@ typedef struct {
   long long particle_capacity;  /* particle pool size (sum of diode capacities) */
   long long chain_capacity;     /* MH chain pool size (sum of per-diode chain caps) */
   long long quad_capacity;      /* supply quadrature points over all diodes */
-  int target_items;             /* work items per pair sum (0 = 8 x grid) */
-  int grid_blocks;              /* persistent grid size (0 = 4 x SM count) */
+  int target_items;             /* reserved, 0 (work items follow the per-diode chunk rule) */
+  int grid_blocks;              /* persistent grid size (0 = per kernel: resident blocks per
+                                   SM at its occupancy x SM count) */
 } rd_engine_config;
 
 /* One diode (the namelist /input/ of one run, src/mod_global.F90:426-439). */
@@ -185,6 +186,17 @@ typedef struct {
   long long supply_pair_evals;
 } rd_phase_times;
 int rd_profile_step(rd_engine* e, int step, rd_phase_times* out);
+
+/* ---- kernel timing (measurement only; no counterpart in the reference) ----
+ * rd_time_accel: device time of one all-pair force evaluation of every
+ * resident diode (work plan + pair kernel, as inside a step), averaged over
+ * `reps` back-to-back evaluations timed with CUDA events on the engine
+ * stream.  rd_time_field_at: the same for the field at M points of one diode
+ * (points uploaded once, before the timed region; plan + field kernel per
+ * evaluation).  Both leave the particle state unchanged. */
+int rd_time_accel(rd_engine* e, int reps, double* ms_per_eval);
+int rd_time_field_at(rd_engine* e, int diode, int M, const double* pos3m, int reps,
+                     double* ms_per_eval);
 
 /* ---- serving: continuous batching of diode simulations ---------------------
  * The reference runs one simulation per process.  Requests queue in FIFO

@@ -151,6 +151,8 @@ SIGNATURES = {
     "rd_serve": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(ServeStats)]),
     "rd_clock": (C.c_int, [C.c_void_p, _dp]),
     "rd_field_at_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    "rd_time_accel": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "rd_time_field_at": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_int, _dp]),
 }
 
 
@@ -274,6 +276,12 @@ class Engine:
         st = ServeStats()
         _check(self.L.rd_serve(self.h, iterations, C.byref(st)))
         return st.as_dict()
+
+    def time_accel(self, reps=3):
+        """Device milliseconds of one force evaluation of all resident diodes."""
+        ms = C.c_double()
+        _check(self.L.rd_time_accel(self.h, reps, C.byref(ms)))
+        return ms.value
 
     def clock(self):
         t = C.c_double()
@@ -401,6 +409,13 @@ class Diode:
         out = np.zeros_like(pts)
         _check(self.L.rd_field_at(self.e.h, self.index, pts.shape[0], _p(pts), _p(out)))
         return out
+
+    def time_field_at(self, pts, reps=3):
+        """Device milliseconds of one field evaluation at the points."""
+        pts = _vec3(pts)
+        ms = C.c_double()
+        _check(self.L.rd_time_field_at(self.e.h, self.index, pts.shape[0], _p(pts), reps, C.byref(ms)))
+        return ms.value
 
     def calc_field_at_batch_noalloc(self, pos_dev_ptr, field_dev_ptr, M):
         """rd_field_at_noalloc: points and result are caller-owned device

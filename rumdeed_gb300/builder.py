@@ -15,6 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "librumdeed_gb300.so")
+DRIVER_SRC = os.path.join(HERE, "driver", "rd_main.cpp")
+DRIVER = os.path.join(OUT_DIR, "rd_main")
 SOURCES = ["rd_force.cu", "rd_field.cu", "rd_step.cu", "rd_engine.cu", "rd_noalloc.cu"]
 HEADERS = ["rd_internal.h", "rd_device.cuh", "rd_pair.cuh", "rd_tiles.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -36,8 +38,23 @@ def _newest_input():
     return max(os.path.getmtime(p) for p in paths)
 
 
+def build_driver(force=False):
+    """The native main-loop driver rd_main (g++), linked against the library."""
+    if not force and os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(
+            os.path.getmtime(DRIVER_SRC), os.path.getmtime(LIB)):
+        return DRIVER
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-o", DRIVER, DRIVER_SRC, "-L" + OUT_DIR, "-lrumdeed_gb300",
+           "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    return DRIVER
+
+
 def build(force=False, verbose=False, extra=()):
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_input():
+        build_driver()
         return LIB
     os.makedirs(OBJ_DIR, exist_ok=True)
     cc = nvcc()
@@ -60,6 +77,7 @@ def build(force=False, verbose=False, extra=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
+    build_driver(force=True)
     return LIB
 
 

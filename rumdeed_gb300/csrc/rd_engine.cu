@@ -217,6 +217,8 @@ struct rd_engine {
   long long fcap = 0;
   double *stage_d = nullptr;
   int* stage_i = nullptr;
+  double* stage_hd = nullptr;   // pinned host mirrors of stage_d / stage_i: uploads are DMA
+  int* stage_hi = nullptr;      // copies from page-locked memory
   long long stage_cap = 0;
   // host
   std::vector<SlotHost> slots;
@@ -320,6 +322,11 @@ static int launch_emission(rd_engine* e) {
                              e->work));
   e->kernels_in_step++;
   CK(plan(e, PM_MH));
+  if (s.emit_planar) {   // round 0 of the planar chain start, tiled
+    CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                         e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale));
+    e->kernels_in_step++;
+  }
   CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                        e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
   e->kernels_in_step++;
@@ -422,12 +429,18 @@ static int repack(rd_engine* e) {
 static int stage(rd_engine* e, long long doubles, long long ints) {
   long long need = std::max(doubles, ints);
   if (need <= e->stage_cap) return RD_OK;
+  CK(cudaStreamSynchronize(e->st));
   if (e->stage_d) cudaFree(e->stage_d);
   if (e->stage_i) cudaFree(e->stage_i);
-  e->stage_d = nullptr; e->stage_i = nullptr;
+  if (e->stage_hd) cudaFreeHost(e->stage_hd);
+  if (e->stage_hi) cudaFreeHost(e->stage_hi);
+  e->stage_d = nullptr; e->stage_i = nullptr; e->stage_hd = nullptr; e->stage_hi = nullptr;
+  e->stage_cap = 0;
   long long cap = std::max<long long>(need, 1 << 16);
   CK(cudaMalloc(&e->stage_d, cap * sizeof(double)));
   CK(cudaMalloc(&e->stage_i, cap * sizeof(int)));
+  CK(cudaHostAlloc(&e->stage_hd, cap * sizeof(double), cudaHostAllocDefault));
+  CK(cudaHostAlloc(&e->stage_hi, cap * sizeof(int), cudaHostAllocDefault));
   e->stage_cap = cap;
   return RD_OK;
 }
@@ -544,6 +557,8 @@ int rd_engine_destroy(rd_engine* e) {
   for (void* p : e->allocs) cudaFree(p);
   if (e->stage_d) cudaFree(e->stage_d);
   if (e->stage_i) cudaFree(e->stage_i);
+  if (e->stage_hd) cudaFreeHost(e->stage_hd);
+  if (e->stage_hi) cudaFreeHost(e->stage_hi);
   if (e->fpx) { cudaFree(e->fpx); cudaFree(e->fpy); cudaFree(e->fpz); cudaFree(e->ffx); cudaFree(e->ffy); cudaFree(e->ffz); }
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
@@ -756,9 +771,15 @@ int rd_add_particles(rd_engine* e, int d, int n, const double* pos, const double
   int rc = stage(e, 6LL * n, n);
   if (rc) return rc;
   if (n > 0) {
-    CK(cudaMemcpyAsync(e->stage_d, pos, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, e->st));
-    if (vel) CK(cudaMemcpyAsync(e->stage_d + 3LL * n, vel, 3 * sizeof(double) * n, cudaMemcpyHostToDevice, e->st));
-    if (species) CK(cudaMemcpyAsync(e->stage_i, species, sizeof(int) * n, cudaMemcpyHostToDevice, e->st));
+    // the previous upload from the pinned stage has completed (every call ends with a
+    // stream synchronize), so the stage can be refilled
+    std::memcpy(e->stage_hd, pos, 3 * sizeof(double) * n);
+    if (vel) std::memcpy(e->stage_hd + 3LL * n, vel, 3 * sizeof(double) * n);
+    CK(cudaMemcpyAsync(e->stage_d, e->stage_hd, (vel ? 6 : 3) * sizeof(double) * n, cudaMemcpyHostToDevice, e->st));
+    if (species) {
+      std::memcpy(e->stage_hi, species, sizeof(int) * n);
+      CK(cudaMemcpyAsync(e->stage_i, e->stage_hi, sizeof(int) * n, cudaMemcpyHostToDevice, e->st));
+    }
   }
   CK(rd_launch_add_particles(e->st, e->dP, e->dD, e->pool, d, n, e->stage_d, vel ? e->stage_d + 3LL * n : nullptr,
                              species ? e->stage_i : nullptr, step, section));
@@ -883,6 +904,44 @@ static int field_at_batch(rd_engine* e, int d, int M, const double* pos, double*
     CK(cudaStreamSynchronize(e->st));
     for (int i = 0; i < M; ++i) field[3 * i + k2] = h[i];
   }
+  return RD_OK;
+}
+
+int rd_time_accel(rd_engine* e, int reps, double* ms_per_eval) {
+  if (!e || !ms_per_eval || reps <= 0) return fail(RD_ERR_INVALID, "bad argument");
+  int rc = repack(e);
+  if (rc) return rc;
+  if ((rc = launch_force(e))) return rc;   // warm-up
+  CK(cudaEventRecord(e->ev0, e->st));
+  for (int r = 0; r < reps; ++r)
+    if ((rc = launch_force(e))) return rc;
+  CK(cudaEventRecord(e->ev1, e->st));
+  CK(cudaEventSynchronize(e->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+  *ms_per_eval = ms / reps;
+  return RD_OK;
+}
+
+int rd_time_field_at(rd_engine* e, int d, int M, const double* pos, int reps, double* ms_per_eval) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  if (M <= 0 || !pos || !ms_per_eval || reps <= 0) return fail(RD_ERR_INVALID, "bad argument");
+  if (M > (e->max_items / 2) * RD_ITILE) return fail(RD_ERR_CAPACITY, "too many points for one evaluation");
+  std::vector<double> field(3LL * M);
+  int rc = field_at_batch(e, d, M, pos, field.data());   // uploads the points; warm-up
+  if (rc) return rc;
+  PointSet pts{e->fpx, e->fpy, e->fpz, e->ffx, e->ffy, e->ffz, e->d_zero_off};
+  CK(cudaEventRecord(e->ev0, e->st));
+  for (int r = 0; r < reps; ++r) {
+    CK(plan(e, PM_FIELD, e->d_npts));
+    CK(rd_launch_field_points(e->cfg.precision, e->slots[d].p.geometry, e->grid, e->st, e->dP, e->pool,
+                              e->plan[PM_FIELD], e->ph[PM_FIELD], pts, e->partial, e->tickets, e->kscale));
+  }
+  CK(cudaEventRecord(e->ev1, e->st));
+  CK(cudaEventSynchronize(e->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+  *ms_per_eval = ms / reps;
   return RD_OK;
 }
 
@@ -1020,6 +1079,9 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
       out->mh_pair_evals += (long long)dyn[d].chains * dyn[d].n * sl.p.mh_jumps;
     }
     CK(plan(e, PM_MH));
+    if (s.emit_planar)
+      CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                           e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale));
     CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                          e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
     CK(cudaEventRecord(ev[2], e->st));

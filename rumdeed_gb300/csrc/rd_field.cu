@@ -192,23 +192,32 @@ __device__ __forceinline__ float z0_tile_f32(const float4* __restrict__ sh, cons
   return s0 + s1;
 }
 
-// Two cathode points per thread (N_ic_max = 0): one shared load feeds two pairs.
-__device__ __forceinline__ void z0_tile2_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
-                                             int kmax, float4 pa, float4 pb, float& ra, float& rb) {
-  float sa = 0.f, sb = 0.f;
+// Tile sums for two points a, b at z = 0 (nic = 0), in packed FP32x2
+// arithmetic: point a in the .x lanes, b in the .y lanes.  The j data sit in
+// shared memory duplicated and negated, s0 = (-x_hi, -x_hi, -x_lo, -x_lo),
+// s1 = (-y_hi, ..), s2 = (z^2, z^2, q z, q z), so each step for the two
+// points is one packed instruction (rsqrt stays per lane).  The points are
+// taken at their FP32 nm offsets (PX, PY: their high words; MH chains live on
+// that grid, on_f32_grid), so dx = (p - x_hi) - x_lo: the first difference
+// is exact for nearby pairs (Sterbenz) and the particle's low word restores
+// its FP64 position.
+__device__ __forceinline__ void z0_tile2_x2(const float4* __restrict__ s0, const float4* __restrict__ s1,
+                                            const float4* __restrict__ s2, int kmax, float2 PX, float2 PY,
+                                            float& ra, float& rb) {
+  float2 s = make_float2(0.f, 0.f);
 #pragma unroll 4
   for (int k = 0; k < kmax; ++k) {
-    const float4 h = sh[k];
-    const float2 l = *reinterpret_cast<const float2*>(&sl[k]);
-    const float dxa = (pa.x - h.x) + (pa.y - l.x), dya = (pa.z - h.y) + (pa.w - l.y);
-    const float dxb = (pb.x - h.x) + (pb.y - l.x), dyb = (pb.z - h.y) + (pb.w - l.y);
-    const float ia = rsqrtf(fmaf(dxa, dxa, fmaf(dya, dya, h.z)));
-    const float ib = rsqrtf(fmaf(dxb, dxb, fmaf(dyb, dyb, h.z)));
-    sa = fmaf(h.w, (ia * ia) * ia, sa);
-    sb = fmaf(h.w, (ib * ib) * ib, sb);
+    const float4 a = s0[k], b = s1[k], c = s2[k];
+    const float2 dx = __fadd2_rn(__fadd2_rn(PX, make_float2(a.x, a.y)), make_float2(a.z, a.w));
+    const float2 dy = __fadd2_rn(__fadd2_rn(PY, make_float2(b.x, b.y)), make_float2(b.z, b.w));
+    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, make_float2(c.x, c.y)));
+    float2 inv;
+    inv.x = rsqrtf(r2.x);
+    inv.y = rsqrtf(r2.y);
+    s = __ffma2_rn(make_float2(c.z, c.w), __fmul2_rn(__fmul2_rn(inv, inv), inv), s);
   }
-  ra += sa;
-  rb += sb;
+  ra += s.x;
+  rb += s.y;
 }
 
 // Partial F_z sums of the item for two points at z = 0 (FP32 compensated),
@@ -216,21 +225,32 @@ __device__ __forceinline__ void z0_tile2_f32(const float4* __restrict__ sh, cons
 __device__ __forceinline__ void z0_item_sum2(const DiodeParams& p, const Pool& pool, const ItemRef& it,
                                              float4 pa, float4 pb, float4* sh, float4* sl,
                                              double* out_a, double* out_b) {
+  __shared__ float4 sp[3][RD_TILE];
   const int off = p.off, tid = threadIdx.x, nt = blockDim.x;
   const int nic = p.image_charge ? p.N_ic_max : 0;
   const float dnm = (float)(p.d * 1.0e9);
   float ha = 0.f, la = 0.f, hb = 0.f, lb = 0.f;
+  const float2 PX = make_float2(pa.x, pb.x), PY = make_float2(pa.z, pb.z);
   for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
     __syncthreads();
     for (int q = tid; q < RD_TILE; q += nt) {
       const int j = jt + q;
-      if (j < it.j1) { sh[q] = pool.zk_hi[off + j]; sl[q] = pool.zk_lo[off + j]; }
+      if (j < it.j1) {
+        const float4 h = pool.zk_hi[off + j], l = pool.zk_lo[off + j];
+        if (nic == 0) {
+          sp[0][q] = make_float4(-h.x, -h.x, -l.x, -l.x);
+          sp[1][q] = make_float4(-h.y, -h.y, -l.y, -l.y);
+          sp[2][q] = make_float4(h.z, h.z, h.w, h.w);
+        } else {
+          sh[q] = h; sl[q] = l;
+        }
+      }
     }
     __syncthreads();
     const int kmax = min(RD_TILE, it.j1 - jt);
     float ta = 0.f, tb = 0.f;
     if (nic == 0) {
-      z0_tile2_f32(sh, sl, kmax, pa, pb, ta, tb);
+      z0_tile2_x2(sp[0], sp[1], sp[2], kmax, PX, PY, ta, tb);
     } else {
       ta = z0_tile_f32<false>(sh, sl, kmax, pa, nic, dnm);
       tb = z0_tile_f32<false>(sh, sl, kmax, pb, nic, dnm);
@@ -523,9 +543,11 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
     const DiodeParams& p = P[d];
     const int n = plan[d].n_j, k = ch_off[d] + c;
     const uint32_t step = (uint32_t)(*step_ptr - Dy[d].step_offset);
+    const bool planar = p.geometry != RD_G_TIP;
+    if (planar && cs.ok[k]) continue;   // round 0 made it (k_mh_jump_planar, it_idx 0)
     int ok = 0;
     double F = 1.0, sup = -1.79769313486231570e308, X = 0, Y = 0, Z = 0, xi = 1.0, ph_ = 0.0;
-    for (int r = 0; r < p.init_rounds && !ok; ++r) {
+    for (int r = planar ? 1 : 0; r < p.init_rounds && !ok; ++r) {
       double u1, u2;
       rng2(p.seed, (uint32_t)c, (uint32_t)r, step, RNG_INIT, &u1, &u2);
       if (p.geometry == RD_G_TIP) {
@@ -538,6 +560,7 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
         if (Fn < 0.0) { ok = 1; F = Fn; X = x; Y = y; Z = z; xi = txi; ph_ = tph; sup = tip_target_log(p, Fn, txi); }
       } else {
         double x = u1 * p.em_Lx + p.em_x0, y = u2 * p.em_Ly + p.em_y0;
+        if (PREC == 1) { x = on_f32_grid(x, p.org_x); y = on_f32_grid(y, p.org_y); }
         double Fz = warp_field_planar_z0<PREC>(p, pool, n, x, y, kscale);
         if (Fz < 0.0) {
           ok = 1; F = Fz; X = x; Y = y;
@@ -624,7 +647,10 @@ __device__ __forceinline__ int mh_accept_one(const DiodeParams& p, ChainState& c
   return a;
 }
 
-// One Metropolis-Hastings jump iteration of the planar chains.  The
+// One Metropolis-Hastings jump iteration of the planar chains (it_idx >= 1),
+// or round 0 of their uniform start (it_idx == 0: every chain of the step
+// evaluates its first uniform draw here, tiled like a jump; the chains that
+// drew an unfavourable point continue in k_mh_init from round 1).  The
 // proposal is the stored Gaussian pair (box_muller, src/mod_global.F90:
 // 578-595) times the step size of this iteration (fixed during the warm-up,
 // MH_std afterwards, :1373-1378) plus the current position, reflected at the
@@ -646,6 +672,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
   constexpr int CPT = PREC == 1 ? 2 : 1;
   const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
+  const bool init = it_idx == 0;
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
@@ -656,19 +683,27 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
     const double sx = (it_idx > ndim_first) ? p.em_Lx * mhs : p.em_Lx * 0.10;
     const double sy = (it_idx > ndim_first) ? p.em_Ly * mhs : p.em_Ly * 0.10;
     const int M = plan[it.d].n_i;
+    const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
     int ok[CPT], kk[CPT];
     double wx[CPT], wy[CPT];
     for (int q = 0; q < CPT; ++q) {
       const int c = it.i0 + tid + q * nt;
       kk[q] = ch_off[it.d] + c;
-      ok[q] = (c < M) ? cs.ok[kk[q]] : 0;
+      ok[q] = (c < M) ? (init ? 1 : cs.ok[kk[q]]) : 0;
       wx[q] = p.em_x0; wy[q] = p.em_y0;
-      if (ok[q]) {
+      if (init && ok[q]) {   // round 0 of the uniform start (:1321-1364)
+        double u1, u2;
+        rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+        double x = u1 * p.em_Lx + p.em_x0, yv = u2 * p.em_Ly + p.em_y0;
+        if (PREC == 1) { x = on_f32_grid(x, p.org_x); yv = on_f32_grid(yv, p.org_y); }
+        wx[q] = x; wy[q] = yv;
+      } else if (ok[q]) {
         const int k = kk[q];
         double x = cs.gx[k] * sx + cs.x[k], yv = cs.gy[k] * sy + cs.y[k];
         const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
         if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
         if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
+        if (PREC == 1) { x = on_f32_grid(x, p.org_x); yv = on_f32_grid(yv, p.org_y); }
         wx[q] = x; wy[q] = yv;
       }
     }
@@ -689,7 +724,23 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
       }
     }
     // epilogue of the completed tile
-    const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
+    if (init) {   // a favourable start (F < 0) makes the chain; the others go to k_mh_init
+      for (int q = 0; q < CPT; ++q) {
+        if (!ok[q]) continue;
+        const int c = it.i0 + tid + q * nt, k = kk[q];
+        const double F = z0_finish<PREC>(p, s[q], kscale);
+        if (F < 0.0 && p.init_rounds > 0) {
+          cs.ok[k] = 1; cs.F[k] = F; cs.x[k] = wx[q]; cs.y[k] = wy[q];
+          cs.sup[k] = supply_log_tab(p, wtab, work_cell(p, wx[q], wy[q]), F);
+          double g1, g2;
+          gauss2(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
+          cs.gx[k] = g1; cs.gy[k] = g2;
+        } else {
+          cs.ok[k] = 0;
+        }
+      }
+      continue;
+    }
     int a = 0, r = 0;
     for (int q = 0; q < CPT; ++q) {
       if (!ok[q]) continue;

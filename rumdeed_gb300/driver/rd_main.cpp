@@ -1,0 +1,331 @@
+// rd_main -- native main-loop driver over the C ABI of librumdeed_gb300.
+//
+// It runs a RUMDEED input deck the way the reference's main program does
+// (src/main.F90:175-219): read the /input/ namelist from the file `input`
+// (src/mod_global.F90:426-439, src/main.F90:298-411) and, for planar field
+// emission, the checkerboard work function from `work`
+// (src/mod_work_function.F90:53-152); then for step = 1..STEPS do emission,
+// Update_Position and Remove_Particles (one rd_step call) and write the
+// per-step records to out/emitted.dt (src/mod_field_emission_v2.F90:202-204),
+// out/absorbed{,_top,_bot}.dt (src/mod_pair.F90:789-804) and
+// out/ramo_current.dt (src/mod_pair.F90:811-835) with the reference's Fortran
+// edit descriptors.
+//
+// Supported decks: EMISSION_MODE = 10 (planar field emission, one
+// rectangular emitter, EMITTERS_TYPE 2) and EMISSION_MODE = 3 (hyperboloid
+// tip).  Extra, optional namelist /gb300/ in the same file: MAX_PARTICLES
+// (default 20000), SEED, PRECISION (0 = FP64, 1 = FP32 compensated), MH_JUMPS,
+// TIP_WORK_FUNCTION (eV, default 4.7 as the reference hard-codes).
+//
+//   rd_main [run directory]
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <algorithm>
+#include <map>
+#include <string>
+#include <sys/stat.h>
+#include <unistd.h>
+#include <vector>
+
+#include "../../include/rumdeed_gpu.h"
+
+namespace {
+
+// ---- namelist reader ---------------------------------------------------------------------
+// Reads `&name key = v1, v2, ... /` groups: keys are upper-cased with their
+// subscripts removed, values are split on commas/whitespace, `!` starts a
+// comment, Fortran logicals and d-exponents are accepted.
+using Group = std::map<std::string, std::vector<std::string>>;
+
+std::map<std::string, Group> read_namelists(const char* path) {
+  std::map<std::string, Group> out;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return out;
+  std::string text;
+  char buf[4096];
+  while (std::fgets(buf, sizeof buf, f)) {
+    std::string l(buf);
+    bool in_str = false;
+    for (size_t i = 0; i < l.size(); ++i) {
+      if (l[i] == '\'' || l[i] == '"') in_str = !in_str;
+      if (l[i] == '!' && !in_str) { l.resize(i); break; }
+    }
+    text += l + " ";
+  }
+  std::fclose(f);
+  size_t pos = 0;
+  while ((pos = text.find('&', pos)) != std::string::npos) {
+    size_t e = text.find_first_of(" \t\r\n", pos);
+    if (e == std::string::npos) break;
+    std::string name = text.substr(pos + 1, e - pos - 1);
+    for (auto& c : name) c = (char)std::toupper((unsigned char)c);
+    size_t end = text.find('/', e);
+    if (end == std::string::npos) end = text.size();
+    // tokens: split on commas and blanks outside parentheses; '=' is a token
+    std::vector<std::string> tok;
+    std::string cur;
+    int depth = 0;
+    for (size_t i = e; i < end; ++i) {
+      const char c = text[i];
+      if (c == '(') ++depth;
+      if (c == ')') --depth;
+      if (depth == 0 && (c == ',' || std::isspace((unsigned char)c) || c == '=')) {
+        if (!cur.empty()) { tok.push_back(cur); cur.clear(); }
+        if (c == '=') tok.push_back("=");
+      } else {
+        cur += c;
+      }
+    }
+    if (!cur.empty()) tok.push_back(cur);
+    Group g;
+    std::string key;
+    for (size_t i = 0; i < tok.size(); ++i) {
+      if (i + 1 < tok.size() && tok[i + 1] == "=") {
+        key.clear();
+        for (char c : tok[i].substr(0, tok[i].find('('))) key += (char)std::toupper((unsigned char)c);
+        g[key].clear();
+        ++i;
+      } else if (!key.empty()) {
+        const size_t star = tok[i].find('*');   // repeat count r*v
+        if (star != std::string::npos && star > 0) {
+          const int r = std::atoi(tok[i].substr(0, star).c_str());
+          for (int k = 0; k < r; ++k) g[key].push_back(tok[i].substr(star + 1));
+        } else {
+          g[key].push_back(tok[i]);
+        }
+      }
+    }
+    out[name] = g;
+    pos = end;
+  }
+  return out;
+}
+
+double to_double(std::string s) {
+  for (auto& c : s) if (c == 'd' || c == 'D') c = 'e';
+  return std::strtod(s.c_str(), nullptr);
+}
+
+bool to_logical(std::string s) {
+  for (auto& c : s) c = (char)std::toupper((unsigned char)c);
+  return s.find('T') != std::string::npos;
+}
+
+double get(const Group& g, const char* k, size_t i, double dflt) {
+  auto it = g.find(k);
+  if (it == g.end() || it->second.size() <= i) return dflt;
+  return to_double(it->second[i]);
+}
+
+// ---- Fortran edit descriptors ----------------------------------------------------------
+// Ew.d: 0.ddddddE+ee right-justified in w characters.
+std::string fmt_E(double v, int w, int d) {
+  char m[64];
+  if (v == 0.0) {
+    std::snprintf(m, sizeof m, "0.%0*dE+00", d, 0);
+  } else {
+    int ex = (int)std::floor(std::log10(std::fabs(v))) + 1;
+    double mant = std::fabs(v) / std::pow(10.0, ex);
+    double scale = std::pow(10.0, d);
+    double r = std::nearbyint(mant * scale);
+    if (r >= scale) { r /= 10.0; ex += 1; }
+    if (r < scale / 10.0) { r *= 10.0; ex -= 1; }
+    std::snprintf(m, sizeof m, "%s0.%0*.0fE%c%02d", v < 0 ? "-" : "", d, r, ex < 0 ? '-' : '+', std::abs(ex));
+  }
+  std::string s(m);
+  return std::string(s.size() < (size_t)w ? w - s.size() : 0, ' ') + s;
+}
+
+// ESw.d: d.ddddE+ee right-justified in w characters.
+std::string fmt_ES(double v, int w, int d) {
+  char m[64];
+  std::snprintf(m, sizeof m, "%*.*E", w, d, v);
+  return std::string(m);
+}
+
+std::string fmt_I(long long v, int w) {
+  char m[64];
+  std::snprintf(m, sizeof m, "%*lld", w, v);
+  return std::string(m);
+}
+
+int check(int rc, const char* what) {
+  if (rc != RD_OK) {
+    std::fprintf(stderr, "rd_main: %s failed (%d): %s\n", what, rc, rd_last_error());
+    std::exit(2);
+  }
+  return rc;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  bool print_only = false;
+  const char* dir = nullptr;
+  for (int a = 1; a < argc; ++a) {
+    if (!std::strcmp(argv[a], "--print-config")) print_only = true;
+    else dir = argv[a];
+  }
+  if (dir && chdir(dir) != 0) {
+    std::fprintf(stderr, "rd_main: cannot enter %s\n", dir);
+    return 2;
+  }
+  auto nl = read_namelists("input");
+  if (!nl.count("INPUT")) {
+    std::fprintf(stderr, "rd_main: ERROR UNABLE TO OPEN file input (or no &input group)\n");
+    return 2;
+  }
+  const Group& in = nl["INPUT"];
+  const Group gb = nl.count("GB300") ? nl["GB300"] : Group();
+  const double length_scale = 1.0e-9, time_scale = 1.0e-12;
+  const double V_s = get(in, "V_S", 0, 0.0);
+  const double d = get(in, "BOX_DIM", 2, 0.0) * length_scale;
+  const double dt = get(in, "TIME_STEP", 0, 0.0) * time_scale;
+  const int steps = (int)get(in, "STEPS", 0, 0.0);
+  const int mode = (int)get(in, "EMISSION_MODE", 0, 10.0);
+  const int n_ic = (int)get(in, "N_IC_MAX", 0, 0.0);
+  const bool image = in.count("IMAGE_CHARGE") ? to_logical(in.at("IMAGE_CHARGE")[0]) : true;
+  if (steps <= 0) { std::fprintf(stderr, "ERROR: steps <= 0\n"); return 2; }
+  if (mode != 10 && mode != 3) {
+    std::fprintf(stderr, "rd_main: EMISSION_MODE %d is not on this path (10: planar FE, 3: tip)\n", mode);
+    return 2;
+  }
+  if ((int)get(in, "NREMIT", 0, 1.0) != 1) {
+    std::fprintf(stderr, "rd_main: one emitter per run on this path (NREMIT = 1)\n");
+    return 2;
+  }
+
+  rd_diode_config dc;
+  std::memset(&dc, 0, sizeof dc);
+  dc.V_s = V_s;
+  dc.time_step = dt;
+  dc.image_charge = image ? 1 : 0;
+  dc.N_ic_max = n_ic;
+  dc.capacity = (int)get(gb, "MAX_PARTICLES", 0, 20000.0);
+  dc.emission = 1;
+  dc.mh_jumps = (int)get(gb, "MH_JUMPS", 0, 0.0);
+  dc.seed = (unsigned long long)get(gb, "SEED", 0, 20261203.0);
+  std::vector<double> work;
+  if (mode == 10) {
+    dc.geometry = RD_GEOM_PLANAR;
+    dc.gap = d;
+    dc.emitter_dim[0] = get(in, "EMITTERS_DIM", 0, 0.0) * length_scale;
+    dc.emitter_dim[1] = get(in, "EMITTERS_DIM", 1, 0.0) * length_scale;
+    dc.emitter_pos[0] = get(in, "EMITTERS_POS", 0, 0.0) * length_scale;
+    dc.emitter_pos[1] = get(in, "EMITTERS_POS", 1, 0.0) * length_scale;
+    FILE* wf = std::fopen("work", "r");
+    if (!wf) { std::fprintf(stderr, "RUMDEED: Failed to open file work. ABORTING\n"); return 2; }
+    int type = 0, ny = 0, nx = 0;
+    if (std::fscanf(wf, "%d %d %d", &type, &ny, &nx) != 3 || type != 1 || nx < 1 || ny < 1) {
+      std::fprintf(stderr, "rd_main: only the checkerboard work function (type 1) is on this path\n");
+      return 2;
+    }
+    work.resize((size_t)nx * ny);
+    for (auto& v : work) {
+      char tok[64];
+      if (std::fscanf(wf, "%63s", tok) != 1) { std::fprintf(stderr, "rd_main: short work file\n"); return 2; }
+      v = to_double(tok);
+    }
+    std::fclose(wf);
+    dc.work_nx = nx; dc.work_ny = ny; dc.work = work.data();   // row 0 = first row of the file
+  } else {
+    dc.geometry = RD_GEOM_TIP;
+    dc.tip_dim[0] = get(in, "EMITTERS_DIM", 0, 0.0) * length_scale;
+    dc.tip_dim[1] = get(in, "EMITTERS_DIM", 1, 0.0) * length_scale;
+    dc.tip_dim[2] = get(in, "EMITTERS_DIM", 2, 0.0) * length_scale;
+    dc.gap = dc.tip_dim[0] + dc.tip_dim[2];
+    dc.tip_work_function = get(gb, "TIP_WORK_FUNCTION", 0, 4.7);
+  }
+
+  if (print_only) {   // the deck as read, one "key value" line each, then stop
+    std::printf("geometry %d\nV_s %.17g\ngap %.17g\ntime_step %.17g\nsteps %d\nimage_charge %d\n"
+                "N_ic_max %d\ncapacity %d\nseed %llu\nemitter_pos %.17g %.17g\nemitter_dim %.17g %.17g\n"
+                "work %d x %d\ntip_dim %.17g %.17g %.17g\nE14.6 %s\nES12.4 %s\n",
+                dc.geometry, dc.V_s, dc.gap, dc.time_step, steps, dc.image_charge, dc.N_ic_max,
+                dc.capacity, dc.seed, dc.emitter_pos[0], dc.emitter_pos[1], dc.emitter_dim[0],
+                dc.emitter_dim[1], dc.work_ny, dc.work_nx, dc.tip_dim[0], dc.tip_dim[1], dc.tip_dim[2],
+                fmt_E(dt / time_scale, 14, 6).c_str(), fmt_ES(dt / time_scale, 12, 4).c_str());
+    for (double w : work) std::printf("work_value %.17g\n", w);
+    return 0;
+  }
+
+  rd_engine_config ec;
+  std::memset(&ec, 0, sizeof ec);
+  ec.precision = (int)get(gb, "PRECISION", 0, 0.0);
+  ec.max_diodes = 1;
+  ec.particle_capacity = dc.capacity + 64;
+  ec.chain_capacity = dc.capacity + 64;
+  ec.quad_capacity = 16384;
+  rd_engine* e = nullptr;
+  check(rd_engine_create(&ec, &e), "rd_engine_create");
+  int diode = -1;
+  check(rd_diode_add(e, &dc, &diode), "rd_diode_add");
+
+  mkdir("out", 0755);
+  FILE* f_emit = std::fopen("out/emitted.dt", "w");
+  FILE* f_abs = std::fopen("out/absorbed.dt", "w");
+  FILE* f_top = std::fopen("out/absorbed_top.dt", "w");
+  FILE* f_bot = std::fopen("out/absorbed_bot.dt", "w");
+  FILE* f_ramo = std::fopen("out/ramo_current.dt", "w");
+  if (!f_emit || !f_abs || !f_top || !f_bot || !f_ramo) {
+    std::fprintf(stderr, "rd_main: cannot write under out/\n");
+    return 2;
+  }
+  std::printf("RUMDEED: Starting main loop\n Doing %d time steps of size %12.4E ps\n", steps, dt / time_scale);
+  const double E_z = -V_s / (mode == 10 ? d : dc.gap);
+  std::vector<double> vel;
+  int progress = 1;
+  for (int step = 1; step <= steps; ++step) {
+    check(rd_step(e, step), "rd_step");
+    rd_counters c;
+    check(rd_counters_get(e, diode, &c), "rd_counters_get");
+    const double cur_time = dt * step / time_scale;
+    // emitted.dt: "(E14.6, *(tr8, i6))" time, step, emitted, electrons in flight, per emitter
+    std::string s = fmt_E(cur_time, 14, 6);
+    for (long long v : {(long long)step, (long long)c.emitted_step, (long long)c.n + c.absorbed_top_step +
+                        c.absorbed_bot_step, (long long)c.emitted_step})
+      s += std::string(8, ' ') + fmt_I(v, 6);
+    std::fprintf(f_emit, "%s\n", s.c_str());
+    // absorbed*.dt: "(ES12.4, *(tr2, i8))" time, step, particles, electrons, ions (+ per emitter)
+    auto absorbed = [&](FILE* f, long long n, bool per_emitter) {
+      std::string t = fmt_ES(cur_time, 12, 4);
+      std::vector<long long> cols = {step, n, n, 0};
+      if (per_emitter) cols.push_back(n);
+      for (long long v : cols) t += "  " + fmt_I(v, 8);
+      std::fprintf(f, "%s\n", t.c_str());
+    };
+    absorbed(f_abs, c.absorbed_top_step + c.absorbed_bot_step, false);
+    absorbed(f_top, c.absorbed_top_step, true);
+    absorbed(f_bot, c.absorbed_bot_step, false);
+    // ramo_current.dt: time, step, current, V, particles, electrons, ions, mobility, mean speeds,
+    // current per species (the speeds are those of the electrons left after the step)
+    vel.resize(3 * (size_t)std::max(c.n, 1));
+    int n = 0;
+    check(rd_get_particles(e, diode, c.n, nullptr, vel.data(), nullptr, nullptr, nullptr, nullptr, &n),
+          "rd_get_particles");
+    double av[3] = {0, 0, 0};
+    for (int i = 0; i < n; ++i) for (int k = 0; k < 3; ++k) av[k] += vel[3 * i + k];
+    if (n > 0) for (double& a : av) a /= n;
+    const double speed = std::sqrt(av[0] * av[0] + av[1] * av[1] + av[2] * av[2]);
+    const double mob = E_z != 0.0 ? speed / (-E_z) : 0.0;
+    std::string r = fmt_ES(cur_time, 12, 4) + "  " + fmt_I(step, 8) + "  " + fmt_ES(c.ramo_current, 12, 4) +
+                    "  " + fmt_ES(V_s, 12, 4) + "  " + fmt_I(n, 6) + "  " + fmt_I(n, 6) + "  " + fmt_I(0, 6) +
+                    "  " + fmt_ES(mob, 12, 4) + "  " + fmt_ES(speed, 12, 4) + "  " + fmt_ES(speed, 12, 4) +
+                    "  " + fmt_ES(0.0, 12, 4) + "  " + fmt_ES(c.ramo_current, 12, 4) + "  " +
+                    fmt_ES(0.0, 12, 4) + "  " + fmt_ES(0.0, 12, 4);
+    std::fprintf(f_ramo, "%s\n", r.c_str());
+    if (step * 10 >= progress * steps) {
+      std::printf("RUMDEED: %3d %%  electrons %d, emitted %lld, absorbed %lld\n", progress * 10, c.n,
+                  c.emitted_total, c.absorbed_top_total + c.absorbed_bot_total);
+      std::fflush(stdout);
+      ++progress;
+    }
+  }
+  for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo}) std::fclose(f);
+  rd_engine_destroy(e);
+  std::printf("RUMDEED: Main loop finished\n");
+  return 0;
+}

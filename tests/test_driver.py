@@ -1,0 +1,104 @@
+"""rd_main, the native main-loop driver (src/main.F90:175-219) over the C ABI:
+it reads a RUMDEED input deck (namelist /input/ plus the `work` file) and
+writes the reference's per-step text records.  On CPU: the deck is read as the
+reference reads it; on the GPU: the records agree, step for step, with the
+same run driven through the Python binding."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DRIVER = os.path.join(ROOT, "rumdeed_gb300", "_lib", "rd_main")
+
+DECK = """&INPUT
+  V_S = 2.0d3,                        ! volts over the gap
+  BOX_DIM = 0.0d0, 0.0d0, 1000.0d0,   ! nm; the last is the gap
+  TIME_STEP = 2.5d-4,                 ! ps
+  STEPS = 12,
+  EMISSION_MODE = 10,
+  NREMIT = 1,
+  IMAGE_CHARGE = .True.,
+  N_IC_MAX = 0,
+  COLLISION_MODE = 0, T_temp = 293.15d0,
+  EMITTERS_DIM(1:3, 1) = 1000.0d0, 1000.0d0, 0.0d0,
+  EMITTERS_POS(1:3, 1) = -500.0d0, -500.0d0, 0.0d0,
+  EMITTERS_TYPE(1) = 2,
+  EMITTERS_DELAY(1) = 0,
+/
+&GB300
+  MAX_PARTICLES = 3000, SEED = 11, MH_JUMPS = 40
+/
+"""
+WORK = "1\n2 2\n2.0 2.2\n2.4 2.6\n"
+
+
+@pytest.fixture(scope="module")
+def driver():
+    import rumdeed_gb300 as rg
+    rg.build()
+    from rumdeed_gb300 import builder
+    return builder.build_driver()
+
+
+def _deck(tmp_path):
+    (tmp_path / "input").write_text(DECK)
+    (tmp_path / "work").write_text(WORK)
+    return tmp_path
+
+
+def test_deck_is_read_like_the_reference(driver, tmp_path):
+    out = subprocess.run([driver, "--print-config", str(_deck(tmp_path))], capture_output=True, text=True,
+                         check=True).stdout
+    kv = {}
+    for line in out.splitlines():
+        k, _, v = line.partition(" ")
+        kv.setdefault(k, []).append(v)
+    assert kv["geometry"] == ["1"]
+    assert float(kv["V_s"][0]) == 2000.0
+    assert float(kv["gap"][0]) == 1000.0 * 1.0e-9           # box_dim * length_scale
+    assert float(kv["time_step"][0]) == 2.5e-4 * 1.0e-12     # time_step * time_scale
+    assert kv["steps"] == ["12"] and kv["image_charge"] == ["1"] and kv["N_ic_max"] == ["0"]
+    assert kv["capacity"] == ["3000"] and kv["seed"] == ["11"]
+    assert [float(x) for x in kv["emitter_pos"][0].split()] == [-500.0 * 1.0e-9] * 2
+    assert [float(x) for x in kv["emitter_dim"][0].split()] == [1000.0 * 1.0e-9] * 2
+    assert kv["work"] == ["2 x 2"]
+    assert [float(x) for x in kv["work_value"]] == [2.0, 2.2, 2.4, 2.6]
+    # Fortran edit descriptors: E14.6 and ES12.4
+    assert kv["E14.6"] == ["  0.250000E-03"]
+    assert kv["ES12.4"] == ["  2.5000E-04"]
+
+
+def test_deck_outside_the_path_is_refused(driver, tmp_path):
+    (tmp_path / "input").write_text(DECK.replace("EMISSION_MODE = 10", "EMISSION_MODE = 1"))
+    (tmp_path / "work").write_text(WORK)
+    r = subprocess.run([driver, "--print-config", str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode != 0 and "EMISSION_MODE" in r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_run_matches_python_binding(driver, tmp_path, rg):
+    deck = _deck(tmp_path)
+    r = subprocess.run([driver, str(deck)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    emitted = np.loadtxt(deck / "out" / "emitted.dt")
+    top = np.loadtxt(deck / "out" / "absorbed_top.dt")
+    bot = np.loadtxt(deck / "out" / "absorbed_bot.dt")
+    assert emitted.shape == (12, 5) and top.shape == (12, 6) and bot.shape == (12, 5)
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=3000 + 64,
+                    chain_capacity=3000 + 64, quad_capacity=16384)
+    d = eng.add_diode(V_s=2.0e3, gap=1000 * 1.0e-9, time_step=2.5e-4 * 1.0e-12, image_charge=True,
+                      N_ic_max=0, capacity=3000, emitter_pos=(-500.0 * 1.0e-9, -500.0 * 1.0e-9),
+                      emitter_dim=(1000.0 * 1.0e-9, 1000.0 * 1.0e-9), work=[[2.0, 2.2], [2.4, 2.6]], emission=True,
+                      mh_jumps=40, seed=11)
+    for step in range(1, 13):
+        eng.step(step)
+        c = d.counters()
+        row = emitted[step - 1]
+        assert row[1] == step
+        assert row[2] == c["emitted_step"]
+        assert row[3] == c["n"] + c["absorbed_top_step"] + c["absorbed_bot_step"]
+        assert top[step - 1][2] == c["absorbed_top_step"] and bot[step - 1][2] == c["absorbed_bot_step"]
+    assert emitted[:, 2].sum() > 0          # the deck emits
+    eng.close()
