@@ -584,6 +584,88 @@ def case_mh_small(args):
     print(json.dumps({"case": "mh-small", **p}), flush=True)
 
 
+def case_plain(args):
+    """The plain single-diode deck (CPU-runnable size): gap 1000 nm, 2 kV, a
+    1000 x 1000 nm emitter centred on the axis, work function 4.7 eV (and a
+    populated 2.0 eV variant), dt 0.25 fs, one image partner, MH with 100 and
+    with the reference's 200 jumps, FP64, Philox seed 20261203.  Steps/s of
+    the GPU engine (device time, rd_run) beside the CPU restatement."""
+    import rumdeed_gb300 as rg
+    rg.build()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import orc
+    orc.build()
+    side = 1000 * NM
+    kw = dict(V_s=2.0e3, gap=1000 * NM, time_step=0.25e-15, image_charge=True, N_ic_max=0, capacity=20000,
+              emitter_pos=(-side / 2, -side / 2), emitter_dim=(side, side), emission=True, seed=SEED)
+    for phi in (4.7, 2.0):
+        for jumps in (100, 200):
+            eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=20064,
+                            chain_capacity=20064, quad_capacity=4096)
+            d = eng.add_diode(work=[[phi]], mh_jumps=jumps, **kw)
+            eng.run(1, args.warmup)
+            eng.run(args.warmup + 1, args.steps)
+            ms, kps = eng.last_run_stats()
+            c = d.counters()
+            eng.close()
+            o = orc.OracleDiode(cap=20000, V_s=2.0e3, d=1000 * NM, time_step=0.25e-15, image_charge=True,
+                                N_ic_max=0)
+            o.set_planar_emitter(-side / 2, -side / 2, side, side, [[phi]])
+            o.set_emission(True, seed=SEED, mh_jumps=jumps, max_chains=20000, quad_panels=16, quad_order=4)
+            cpu_steps, t0 = 0, time.perf_counter()
+            while cpu_steps < 3 and time.perf_counter() - t0 < 20.0:
+                o.step(cpu_steps + 1)
+                cpu_steps += 1
+            cpu_t = time.perf_counter() - t0
+            print(json.dumps({"case": "plain", "work_function_eV": phi, "mh_jumps": jumps,
+                              "gpu_fp64_steps_per_s": args.steps / (ms / 1e3), "gpu_ms_per_step": ms / args.steps,
+                              "kernels_per_step": kps, "after_steps": args.warmup + args.steps,
+                              "in_flight": c["n"], "emitted_total": c["emitted_total"], "N_sup": c["N_sup"],
+                              "cpu_steps_per_s": cpu_steps / cpu_t, "cpu_steps": cpu_steps,
+                              "cpu_cores": orc.lib().orc_omp_threads()}), flush=True)
+
+
+def case_tips(args):
+    """16 hyperboloid tips in one engine: apex radius r U[10, 50] nm (base
+    radius R = sqrt(r (h^2 + 2 d h) / d)), tip height h 500 nm, tip-anode gap
+    d 1000 nm, V U[1, 5] kV, work function 4.5 eV, sphere image charge; each
+    tip pre-filled with --tip-electrons electrons (x, y uniform over the base
+    square, z uniform from 1 nm above the apex to 1 nm below the anode).
+    FP32-compensated; electron-steps/s from device time."""
+    import rumdeed_gb300 as rg
+    rg.build()
+    rng = np.random.default_rng([SEED, 4])
+    ntip, n = 16, args.tip_electrons
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=ntip, particle_capacity=ntip * (n + 64),
+                    chain_capacity=ntip * (n + 64), quad_capacity=ntip * 10000 + 4096)
+    h, dd = 500 * NM, 1000 * NM
+    tips = []
+    for t in range(ntip):
+        r = rng.uniform(10.0, 50.0) * NM
+        R = math.sqrt(r * (h * h + 2.0 * dd * h) / dd)
+        V = rng.uniform(1.0e3, 5.0e3)
+        d = eng.add_diode(geometry=rg.GEOM_TIP, V_s=V, time_step=0.25e-15, image_charge=True, capacity=n,
+                          tip_dim=(dd, R, h), tip_work_function=4.5, emission=True, max_chains=n,
+                          seed=int(rng.integers(1, 2 ** 62)))
+        pos = np.column_stack([rng.uniform(-R, R, n), rng.uniform(-R, R, n),
+                               rng.uniform(h + 1 * NM, h + dd - 1 * NM, n)])
+        d.add_particles(pos, step=0)
+        tips.append((r, R, V))
+    eng.run(1, args.warmup)
+    e0 = sum(dio.counters()["electron_steps"] for dio in eng.diodes.values())
+    eng.run(args.warmup + 1, args.steps)
+    ms, kps = eng.last_run_stats()
+    e1 = sum(dio.counters()["electron_steps"] for dio in eng.diodes.values())
+    prof = eng.profile_step(args.warmup + args.steps + 1)
+    cs = [dio.counters() for dio in eng.diodes.values()]
+    eng.close()
+    print(json.dumps({"case": "tips", "tips": ntip, "electrons_per_tip": n,
+                      "electron_steps_per_s": (e1 - e0) / (ms / 1e3), "ms_per_step": ms / args.steps,
+                      "kernels_per_step": kps, "phase_ms": prof,
+                      "chains": [c["chains"] for c in cs], "emitted_step": [c["emitted_step"] for c in cs],
+                      "in_flight": [c["n"] for c in cs]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -593,10 +675,11 @@ def main():
     ap.add_argument("--slots", type=int, default=128)
     ap.add_argument("--plain-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=1.0e10)
-    ap.add_argument("--case", default="serve", choices=["serve", "micro", "burst", "mh-small"],
+    ap.add_argument("--case", default="serve", choices=["serve", "micro", "burst", "mh-small", "plain", "tips"],
                     help="serve: the headline serving benchmark; the others are secondary workloads")
     ap.add_argument("--sizes", default="4096,65536,262144", help="micro: electron counts")
     ap.add_argument("--nics", default="0,7", help="micro: N_ic_max values")
+    ap.add_argument("--tip-electrons", type=int, default=100000, help="tips: electrons per tip")
     ap.add_argument("--fp64-budget", type=float, default=2.0e11,
                     help="micro: largest N(N-1) x terms run in FP64 for the error check")
     args = ap.parse_args()
@@ -610,7 +693,8 @@ def main():
         dist.init_process_group("nccl")
     if args.case != "serve":
         if rank == 0:
-            {"micro": case_micro, "burst": case_burst, "mh-small": case_mh_small}[args.case](args)
+            {"micro": case_micro, "burst": case_burst, "mh-small": case_mh_small, "plain": case_plain,
+             "tips": case_tips}[args.case](args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
