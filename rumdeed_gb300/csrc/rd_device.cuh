@@ -192,16 +192,6 @@ __device__ __forceinline__ void split_nm(double v_m, double origin_m, float* hi,
   *lo = (float)(v - (double)h);
 }
 
-// The point of the FP32 grid of nm offsets from `origin_m` next to v_m,
-// rounded toward the origin (so a point inside an emitter centred on the
-// origin stays inside).  The FP32-compensated form keeps its cathode sample
-// points (MH chains) on this grid: the field is then evaluated at the point
-// itself with no low word for it (split_nm's low part is ~1e-16 relative).
-__device__ __forceinline__ double on_f32_grid(double v_m, double origin_m) {
-  const float h = __double2float_rz((v_m - origin_m) * 1.0e9);
-  return origin_m + (double)h * 1.0e-9;
-}
-
 // Knuth two-sum accumulation of a float into a (hi, lo) pair.
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
   float s = hi + v;

@@ -24,6 +24,13 @@
 #include "../../include/rumdeed_gpu.h"
 #include "rd_pair.cuh"
 
+// The float next to v on the side of zero.
+static float f32_toward_zero(double v) {
+  float f = (float)v;
+  if (std::fabs((double)f) > std::fabs(v)) f = std::nextafter(f, 0.0f);
+  return f;
+}
+
 // ---- kernels (other translation units) ------------------------------------------
 cudaError_t rd_upload_constants_force(const RdConst&);
 cudaError_t rd_upload_constants_field(const RdConst&);
@@ -52,7 +59,7 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
                               const int* ch_off, const double* wtab, const int* step_ptr,
-                              int it_idx, double* partial, int* tickets, double kscale);
+                              int it_idx, double* partial, int* tickets, double kscale, int* queue);
 cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                            const Pool& pool, const ChainState& cs, const int* ch_off,
                            const double* work, const int* step_ptr);
@@ -209,6 +216,7 @@ struct rd_engine {
   PlanHeader* ph[PM_COUNT] = {};
   double* partial = nullptr;
   int* tickets = nullptr;
+  int* item_queue = nullptr;   // dynamic item counters (queue_next / queue_leave)
   int* kept = nullptr;
   double* ramo = nullptr;
   int* life = nullptr;
@@ -324,7 +332,7 @@ static int launch_emission(rd_engine* e) {
   CK(plan(e, PM_MH));
   if (s.emit_planar) {   // round 0 of the planar chain start, tiled
     CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                         e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale));
+                         e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue));
     e->kernels_in_step++;
   }
   CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
@@ -334,7 +342,7 @@ static int launch_emission(rd_engine* e) {
   for (int it = 1; it <= s.jumps; ++it) {
     CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH],
                          e->ph[PM_MH], e->cs, e->d_choff, e->wtab, e->d_step, it, e->partial,
-                         e->tickets, e->kscale));
+                         e->tickets, e->kscale, e->item_queue));
     e->kernels_in_step += ((gmask & 1) ? 1 : 0) + ((gmask & 2) ? 2 : 0);   // planar jump, tip propose + jump
   }
   CK(rd_launch_emit(ns, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step));
@@ -517,10 +525,13 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
       e->dalloc(&e->qx, qcap) || e->dalloc(&e->qy, qcap) || e->dalloc(&e->qz, qcap) ||
       e->dalloc(&e->qw, qcap) || e->dalloc(&e->qF, qcap) || e->dalloc(&e->qfx, qcap) ||
       e->dalloc(&e->qfy, qcap) || e->dalloc(&e->qpp, qcap) || e->dalloc(&e->cs.gx, chcap) || e->dalloc(&e->cs.gy, chcap) ||
+      e->dalloc(&e->cs.fx, chcap) || e->dalloc(&e->cs.fy, chcap) || e->dalloc(&e->cs.fsup, chcap) ||
+      e->dalloc(&e->cs.fgx, chcap) || e->dalloc(&e->cs.fgy, chcap) ||
       e->dalloc(&e->d_choff, S) || e->dalloc(&e->d_qoff, S) ||
       e->dalloc(&e->d_npts, S) || e->dalloc(&e->d_zero_off, S) ||
       e->dalloc(&e->partial, (size_t)e->max_items * 3 * RD_ITILE) ||
       e->dalloc(&e->tickets, e->max_items) || e->dalloc(&e->kept, e->max_items) ||
+      e->dalloc(&e->item_queue, 8) ||
       e->dalloc(&e->ramo, cap) || e->dalloc(&e->life, (size_t)S * RD_MAX_LIFE) ||
       e->dalloc(&e->d_step, 1))
     return bail(fail(RD_ERR_NOMEM, "device allocation failed"));
@@ -535,6 +546,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   cudaMemsetAsync(e->dP, 0, sizeof(DiodeParams) * S, e->st);
   cudaMemsetAsync(e->dD, 0, sizeof(DiodeDyn) * S, e->st);
   cudaMemsetAsync(e->tickets, 0, sizeof(int) * e->max_items, e->st);
+  cudaMemsetAsync(e->item_queue, 0, sizeof(int) * 8, e->st);
   cudaMemsetAsync(e->life, 0, sizeof(int) * (size_t)S * RD_MAX_LIFE, e->st);
   cudaMemsetAsync(e->d_npts, 0, sizeof(int) * S, e->st);
   cudaMemsetAsync(e->d_zero_off, 0, sizeof(int) * S, e->st);
@@ -603,6 +615,10 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
     if (p.emission && (p.em_Lx <= 0.0 || p.em_Ly <= 0.0)) return fail(RD_ERR_INVALID, "emitter_dim must be positive");
     p.org_x = p.em_x0 + 0.5 * p.em_Lx;
     p.org_y = p.em_y0 + 0.5 * p.em_Ly;
+    p.em_hx = f32_toward_zero(0.5 * p.em_Lx * 1.0e9);
+    p.em_hy = f32_toward_zero(0.5 * p.em_Ly * 1.0e9);
+    p.em_wx = (float)(p.em_Lx * 1.0e9);
+    p.em_wy = (float)(p.em_Ly * 1.0e9);
     p.mh_jumps = c->mh_jumps > 0 ? c->mh_jumps : 200;   // MH_ndim, fe_v2:70
     p.mh_lo = 0.00005; p.mh_hi = 0.1250;                 // fe_v2:75-76
     if (c->work_nx > 0 && c->work_ny > 0 && c->work) { p.work_nx = c->work_nx; p.work_ny = c->work_ny; }
@@ -1081,14 +1097,15 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
     CK(plan(e, PM_MH));
     if (s.emit_planar)
       CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                           e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale));
+                           e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue));
     CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                          e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
     CK(cudaEventRecord(ev[2], e->st));
     const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
     for (int it = 1; it <= s.jumps; ++it)
       CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                           e->cs, e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale));
+                           e->cs, e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale,
+                           e->item_queue));
     out->mh_jump_launches = s.jumps;
     CK(cudaEventRecord(ev[3], e->st));
     CK(rd_launch_emit(S, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step));

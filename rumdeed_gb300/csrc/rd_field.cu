@@ -151,6 +151,71 @@ __device__ __forceinline__ double supply_log_tab(const DiodeParams& p, const dou
   return (2.0 * LF - 2.0 * log(ty)) - t[0];
 }
 
+// ---- FP32 forms of the MH arithmetic (FP32-compensated planar chains) -----------------
+// The FP32 form keeps each chain as FP32 nm offsets from the emitter centre
+// and draws, proposes and tests in FP32; only the field finish and the state
+// handed to the emission test (x, y, F of accepted points) are FP64.  FP64 is
+// a small fraction of the FP32 rate on this part, and this arithmetic runs
+// once per chain per work item.
+
+// A uniform float in (0, 1) from 24 bits of a Philox word.
+__device__ __forceinline__ float u01f(uint32_t w) {
+  return ((float)(w >> 8) + 0.5f) * (1.0f / 16777216.0f);
+}
+
+__device__ __forceinline__ void rng2f(unsigned long long seed, uint32_t a, uint32_t b, uint32_t step,
+                                      uint32_t tag, float* u1, float* u2) {
+  uint32_t o[4];
+  philox4x32(a, b, step, tag, (uint32_t)seed, (uint32_t)(seed >> 32), o);
+  *u1 = u01f(o[0]);
+  *u2 = u01f(o[2]);
+}
+
+// box_muller, Marsaglia polar form (src/mod_global.F90:578-595) in FP32, on
+// the counters of gauss2.
+__device__ __forceinline__ void gauss2f(unsigned long long seed, uint32_t chain, uint32_t it,
+                                        uint32_t step, float* g1, float* g2) {
+  for (uint32_t k = 0; k < 64; ++k) {
+    float u1, u2;
+    rng2f(seed, chain, it, step, RNG_GAUSS | (k << 8), &u1, &u2);
+    const float x1 = 2.0f * u1 - 1.0f, x2 = 2.0f * u2 - 1.0f;
+    const float w = x1 * x1 + x2 * x2;
+    if (w < 1.0f && w > 0.0f) {
+      const float m = sqrtf((-2.0f * logf(w)) / w);
+      *g1 = x1 * m;
+      *g2 = x2 * m;
+      return;
+    }
+  }
+  *g1 = 0.0f;
+  *g2 = 0.0f;
+}
+
+// work_cell for a point given as FP32 nm offsets from the emitter centre.
+__device__ __forceinline__ int work_cell_f(const DiodeParams& p, float x, float y) {
+  if (p.work_nx == 1 && p.work_ny == 1) return 0;
+  const float xs = (x + 0.5f * p.em_wx) / p.em_wx, ys = (y + 0.5f * p.em_wy) / p.em_wy;
+  const int nx = p.work_nx, ny = p.work_ny;
+  int xi = (int)floorf(xs * (float)nx) + 1, yi = (int)floorf(ys * (float)ny) + 1;
+  xi = xi > nx ? nx : (xi < 1 ? 1 : xi);
+  yi = yi > ny ? ny : (yi < 1 ? 1 : yi);
+  yi = ny - yi + 1;
+  return (yi - 1) * nx + (xi - 1);
+}
+
+// supply_log_tab in FP32 (F < 0 as a float).
+__device__ __forceinline__ float supply_log_f(const DiodeParams& p, const double* __restrict__ wtab,
+                                              int cell, float F) {
+  const double* t = wtab + 3 * (p.work_off + cell);
+  const float t0 = (float)t[0];
+  const float LF = logf(-F);
+  if (!p.image_charge) return 2.0f * LF - t0;
+  float l = (float)t[2] * (-F), ll = (float)t[1] + LF;
+  if (l > 1.0f) { l = 1.0f; ll = 0.0f; }
+  const float ty = 1.0f + l * ((1.0f / 9.0f) - (1.0f / 18.0f) * ll);
+  return (2.0f * LF - 2.0f * logf(ty)) - t0;
+}
+
 // ---- cathode z = 0 field, planar ----------------------------------------------------
 // Sum over one j-tile of q_j sum_h h / r_h^3 (nm units) for a point at z = 0
 // given as (x_hi, x_lo, y_hi, y_lo).  Uses the cathode pack: zk_hi =
@@ -197,8 +262,8 @@ __device__ __forceinline__ float z0_tile_f32(const float4* __restrict__ sh, cons
 // shared memory duplicated and negated, s0 = (-x_hi, -x_hi, -x_lo, -x_lo),
 // s1 = (-y_hi, ..), s2 = (z^2, z^2, q z, q z), so each step for the two
 // points is one packed instruction (rsqrt stays per lane).  The points are
-// taken at their FP32 nm offsets (PX, PY: their high words; MH chains live on
-// that grid, on_f32_grid), so dx = (p - x_hi) - x_lo: the first difference
+// taken at their FP32 nm offsets (PX, PY: their high words; the FP32 MH
+// chains are kept as such offsets), so dx = (p - x_hi) - x_lo: the first difference
 // is exact for nearby pairs (Sterbenz) and the particle's low word restores
 // its FP64 position.
 __device__ __forceinline__ void z0_tile2_x2(const float4* __restrict__ s0, const float4* __restrict__ s1,
@@ -558,10 +623,23 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
         tip_normal(p, x, y, &nx, &ny, &nz);
         double Fn = (nx * ex + ny * ey) + nz * ez;
         if (Fn < 0.0) { ok = 1; F = Fn; X = x; Y = y; Z = z; xi = txi; ph_ = tph; sup = tip_target_log(p, Fn, txi); }
+      } else if constexpr (PREC == 1) {   // FP32 chains: the draw of k_mh_jump_planar's round 0
+        float v1, v2;
+        rng2f(p.seed, (uint32_t)c, (uint32_t)r, step, RNG_INIT, &v1, &v2);
+        const float fx = fminf(fmaf(v1, p.em_wx, -p.em_hx), p.em_hx);
+        const float fy = fminf(fmaf(v2, p.em_wy, -p.em_hy), p.em_hy);
+        const double x = p.org_x + (double)fx * 1.0e-9, y = p.org_y + (double)fy * 1.0e-9;
+        const double Fz = warp_field_planar_z0<PREC>(p, pool, n, x, y, kscale);
+        if (Fz < 0.0 && (float)Fz < 0.0f) {
+          ok = 1; F = Fz; X = x; Y = y;
+          if (lane == 0) {
+            cs.fx[k] = fx; cs.fy[k] = fy;
+            cs.fsup[k] = supply_log_f(p, wtab, work_cell_f(p, fx, fy), (float)Fz);
+          }
+        }
       } else {
-        double x = u1 * p.em_Lx + p.em_x0, y = u2 * p.em_Ly + p.em_y0;
-        if (PREC == 1) { x = on_f32_grid(x, p.org_x); y = on_f32_grid(y, p.org_y); }
-        double Fz = warp_field_planar_z0<PREC>(p, pool, n, x, y, kscale);
+        const double x = u1 * p.em_Lx + p.em_x0, y = u2 * p.em_Ly + p.em_y0;
+        const double Fz = warp_field_planar_z0<PREC>(p, pool, n, x, y, kscale);
         if (Fz < 0.0) {
           ok = 1; F = Fz; X = x; Y = y;
           sup = supply_log_tab(p, wtab, work_cell(p, x, y), Fz);
@@ -580,9 +658,15 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
       else {
         cs.x[k] = X; cs.y[k] = Y;
         if (ok) {   // Gaussian pair of the first jump
-          double g1, g2;
-          gauss2(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
-          cs.gx[k] = g1; cs.gy[k] = g2;
+          if constexpr (PREC == 1) {
+            float g1, g2;
+            gauss2f(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
+            cs.fgx[k] = g1; cs.fgy[k] = g2;
+          } else {
+            double g1, g2;
+            gauss2(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
+            cs.gx[k] = g1; cs.gy[k] = g2;
+          }
         }
       }
     }
@@ -647,6 +731,36 @@ __device__ __forceinline__ int mh_accept_one(const DiodeParams& p, ChainState& c
   return a;
 }
 
+// mh_accept_one for the FP32 chains (proposal wx, wy in FP32 nm offsets).
+__device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState& cs, const double* wtab,
+                                               int c, int k, int it_idx, uint32_t step, double F,
+                                               float wx, float wy) {
+  int a = 0;
+  const float Ff = (float)F;
+  if (F < 0.0 && Ff < 0.0f) {
+    const float sn = supply_log_f(p, wtab, work_cell_f(p, wx, wy), Ff);
+    const float sc = cs.fsup[k];
+    bool take = sn >= sc;
+    if (!take) {
+      float u1, u2;
+      rng2f(p.seed, (uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, &u1, &u2);
+      take = logf(u1) <= sn - sc;
+    }
+    if (take) {
+      cs.fx[k] = wx; cs.fy[k] = wy; cs.fsup[k] = sn; cs.F[k] = F;
+      cs.x[k] = p.org_x + (double)wx * 1.0e-9;
+      cs.y[k] = p.org_y + (double)wy * 1.0e-9;
+      a = 1;
+    }
+  }
+  if (it_idx < p.mh_jumps) {
+    float g1, g2;
+    gauss2f(p.seed, (uint32_t)c, (uint32_t)(it_idx + 1), step, &g1, &g2);
+    cs.fgx[k] = g1; cs.fgy[k] = g2;
+  }
+  return a;
+}
+
 // One Metropolis-Hastings jump iteration of the planar chains (it_idx >= 1),
 // or round 0 of their uniform start (it_idx == 0: every chain of the step
 // evaluates its first uniform draw here, tiled like a jump; the chains that
@@ -665,52 +779,78 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
                  const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph, ChainState cs,
                  const int* __restrict__ ch_off, const double* __restrict__ wtab,
                  const int* __restrict__ step_ptr, int it_idx, double* __restrict__ partial,
-                 int* __restrict__ tickets, double kscale) {
+                 int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
   __shared__ float4 sh[RD_TILE], sl[RD_TILE];
   __shared__ rd_d4 sj[RD_TILE];
   __shared__ int red_i[2 * RD_ITILE];
+  __shared__ int s_item;
   constexpr int CPT = PREC == 1 ? 2 : 1;
   const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   const bool init = it_idx == 0;
-  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     if (p.geometry != RD_G_PLANAR || it_idx > p.mh_jumps) continue;
     DiodeDyn& y = Dy[it.d];
-    const double mhs = y.MH_std;
-    const int ndim_first = (int)nint_d(p.mh_jumps * 0.25);
-    const double sx = (it_idx > ndim_first) ? p.em_Lx * mhs : p.em_Lx * 0.10;
-    const double sy = (it_idx > ndim_first) ? p.em_Ly * mhs : p.em_Ly * 0.10;
+    const int ndim_first = (p.mh_jumps + 2) / 4;   // nint(0.25 mh_jumps), :1141
     const int M = plan[it.d].n_i;
     const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
     int ok[CPT], kk[CPT];
-    double wx[CPT], wy[CPT];
-    for (int q = 0; q < CPT; ++q) {
-      const int c = it.i0 + tid + q * nt;
-      kk[q] = ch_off[it.d] + c;
-      ok[q] = (c < M) ? (init ? 1 : cs.ok[kk[q]]) : 0;
-      wx[q] = p.em_x0; wy[q] = p.em_y0;
-      if (init && ok[q]) {   // round 0 of the uniform start (:1321-1364)
-        double u1, u2;
-        rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
-        double x = u1 * p.em_Lx + p.em_x0, yv = u2 * p.em_Ly + p.em_y0;
-        if (PREC == 1) { x = on_f32_grid(x, p.org_x); yv = on_f32_grid(yv, p.org_y); }
-        wx[q] = x; wy[q] = yv;
-      } else if (ok[q]) {
-        const int k = kk[q];
-        double x = cs.gx[k] * sx + cs.x[k], yv = cs.gy[k] * sy + cs.y[k];
-        const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
-        if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
-        if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
-        if (PREC == 1) { x = on_f32_grid(x, p.org_x); yv = on_f32_grid(yv, p.org_y); }
-        wx[q] = x; wy[q] = yv;
+    double wx[CPT], wy[CPT];   // FP64 chains: proposal (m)
+    float fwx[CPT], fwy[CPT];  // FP32 chains: proposal (nm from the emitter centre)
+    if constexpr (PREC == 1) {
+      const float mhs = (float)y.MH_std;
+      const float sx = (it_idx > ndim_first) ? p.em_wx * mhs : p.em_wx * 0.10f;
+      const float sy = (it_idx > ndim_first) ? p.em_wy * mhs : p.em_wy * 0.10f;
+      const float hx = p.em_hx, hy = p.em_hy;
+      for (int q = 0; q < CPT; ++q) {
+        const int c = it.i0 + tid + q * nt;
+        kk[q] = ch_off[it.d] + c;
+        ok[q] = (c < M) ? (init ? 1 : cs.ok[kk[q]]) : 0;
+        float x = 0.0f, yv = 0.0f;
+        if (init && ok[q]) {   // round 0 of the uniform start (:1321-1364)
+          float u1, u2;
+          rng2f(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+          x = fminf(fmaf(u1, p.em_wx, -hx), hx);
+          yv = fminf(fmaf(u2, p.em_wy, -hy), hy);
+        } else if (ok[q]) {    // Gaussian step, reflected at the edges (:1466-1516)
+          const int k = kk[q];
+          x = fmaf(cs.fgx[k], sx, cs.fx[k]);
+          yv = fmaf(cs.fgy[k], sy, cs.fy[k]);
+          if (x > hx) x = hx - (x - hx); else if (x < -hx) x = -hx - (x + hx);
+          if (yv > hy) yv = hy - (yv - hy); else if (yv < -hy) yv = -hy - (yv + hy);
+        }
+        fwx[q] = x; fwy[q] = yv;
+      }
+    } else {
+      const double mhs = y.MH_std;
+      const double sx = (it_idx > ndim_first) ? p.em_Lx * mhs : p.em_Lx * 0.10;
+      const double sy = (it_idx > ndim_first) ? p.em_Ly * mhs : p.em_Ly * 0.10;
+      for (int q = 0; q < CPT; ++q) {
+        const int c = it.i0 + tid + q * nt;
+        kk[q] = ch_off[it.d] + c;
+        ok[q] = (c < M) ? (init ? 1 : cs.ok[kk[q]]) : 0;
+        wx[q] = p.em_x0; wy[q] = p.em_y0;
+        if (init && ok[q]) {   // round 0 of the uniform start (:1321-1364)
+          double u1, u2;
+          rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+          wx[q] = u1 * p.em_Lx + p.em_x0;
+          wy[q] = u2 * p.em_Ly + p.em_y0;
+        } else if (ok[q]) {
+          const int k = kk[q];
+          double x = cs.gx[k] * sx + cs.x[k], yv = cs.gy[k] * sy + cs.y[k];
+          const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+          if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
+          if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
+          wx[q] = x; wy[q] = yv;
+        }
       }
     }
     double s[CPT];
-    if (PREC == 1) {
-      z0_item_sum2(p, pool, it, z0_point(p, wx[0], wy[0]), z0_point(p, wx[CPT - 1], wy[CPT - 1]), sh, sl,
-                   &s[0], &s[CPT - 1]);
+    if constexpr (PREC == 1) {
+      z0_item_sum2(p, pool, it, make_float4(fwx[0], 0.f, fwy[0], 0.f),
+                   make_float4(fwx[CPT - 1], 0.f, fwy[CPT - 1], 0.f), sh, sl, &s[0], &s[CPT - 1]);
     } else {
       s[0] = z0_item_sum<PREC>(p, pool, it, wx[0], wy[0], make_float4(0.f, 0.f, 0.f, 0.f), sh, sl, sj);
     }
@@ -729,14 +869,29 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
         if (!ok[q]) continue;
         const int c = it.i0 + tid + q * nt, k = kk[q];
         const double F = z0_finish<PREC>(p, s[q], kscale);
-        if (F < 0.0 && p.init_rounds > 0) {
-          cs.ok[k] = 1; cs.F[k] = F; cs.x[k] = wx[q]; cs.y[k] = wy[q];
-          cs.sup[k] = supply_log_tab(p, wtab, work_cell(p, wx[q], wy[q]), F);
-          double g1, g2;
-          gauss2(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
-          cs.gx[k] = g1; cs.gy[k] = g2;
+        if constexpr (PREC == 1) {
+          if (F < 0.0 && (float)F < 0.0f && p.init_rounds > 0) {
+            cs.ok[k] = 1; cs.F[k] = F;
+            cs.fx[k] = fwx[q]; cs.fy[k] = fwy[q];
+            cs.x[k] = p.org_x + (double)fwx[q] * 1.0e-9;
+            cs.y[k] = p.org_y + (double)fwy[q] * 1.0e-9;
+            cs.fsup[k] = supply_log_f(p, wtab, work_cell_f(p, fwx[q], fwy[q]), (float)F);
+            float g1, g2;
+            gauss2f(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
+            cs.fgx[k] = g1; cs.fgy[k] = g2;
+          } else {
+            cs.ok[k] = 0;
+          }
         } else {
-          cs.ok[k] = 0;
+          if (F < 0.0 && p.init_rounds > 0) {
+            cs.ok[k] = 1; cs.F[k] = F; cs.x[k] = wx[q]; cs.y[k] = wy[q];
+            cs.sup[k] = supply_log_tab(p, wtab, work_cell(p, wx[q], wy[q]), F);
+            double g1, g2;
+            gauss2(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
+            cs.gx[k] = g1; cs.gy[k] = g2;
+          } else {
+            cs.ok[k] = 0;
+          }
         }
       }
       continue;
@@ -746,12 +901,15 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
       if (!ok[q]) continue;
       const int c = it.i0 + tid + q * nt;
       const double F = z0_finish<PREC>(p, s[q], kscale);
-      const int acc = mh_accept_one(p, cs, wtab, c, kk[q], it_idx, step, F, wx[q], wy[q]);
+      int acc;
+      if constexpr (PREC == 1) acc = mh_accept_one_f(p, cs, wtab, c, kk[q], it_idx, step, F, fwx[q], fwy[q]);
+      else acc = mh_accept_one(p, cs, wtab, c, kk[q], it_idx, step, F, wx[q], wy[q]);
       a += acc;
       r += 1 - acc;
     }
     mh_counts_and_update(p, y, plan[it.d].tiles, it_idx, ndim_first, a, r, red_i);
   }
+  queue_leave(queue, total);
 }
 
 template <int PREC>
@@ -1060,10 +1218,10 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
                               const int* ch_off, const double* wtab, const int* step_ptr,
-                              int it_idx, double* partial, int* tickets, double kscale) {
+                              int it_idx, double* partial, int* tickets, double kscale, int* queue) {
   if (geometry_mask & 1) {
-    if (prec == 1) k_mh_jump_planar<1><<<rd_grid(k_mh_jump_planar<1>, 64, grid), 64, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale);
-    else k_mh_jump_planar<0><<<rd_grid(k_mh_jump_planar<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale);
+    if (prec == 1) k_mh_jump_planar<1><<<rd_grid(k_mh_jump_planar<1>, 64, grid), 64, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue);
+    else k_mh_jump_planar<0><<<rd_grid(k_mh_jump_planar<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue);
   }
   if (geometry_mask & 2) {
     k_mh_propose<<<rd_grid(k_mh_propose, 256, grid), 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx);

@@ -57,6 +57,9 @@ struct DiodeParams {
   // hyperboloid tip (mod_hyperboloid_tip)
   double a_foci, eta_1, max_xi, shift_z, r_tip, h_tip, pre_E, pre_E_unit, tip_phi;
   double mh_lo, mh_hi;   // MH_std clamps
+  // FP32 frame of the planar emitter (nm, relative to its centre): half widths
+  // rounded toward zero (chains stay inside) and full widths
+  float em_hx, em_hy, em_wx, em_wy;
 };
 
 // Dynamic per-diode state (device resident, updated by kernels).
@@ -112,4 +115,7 @@ struct ChainState {
   double *pxx, *pyy, *pzz;  // tip: cartesian position of the proposal
   int *prop_ok;          // proposal inside the domain
   double *gx, *gy;       // planar: Gaussian pair of the next proposal
+  // FP32-compensated planar chains: position as FP32 nm offsets from the
+  // emitter centre (the chain lives on that grid), log target, Gaussian pair
+  float *fx, *fy, *fsup, *fgx, *fgy;
 };

@@ -6,7 +6,9 @@
 // times a j-chunk of consecutive particles.  A plan (one entry per diode,
 // built on the device from the particle counts) says how many tiles and
 // chunks each diode has; persistent CTAs walk the item index space
-// round-robin and decode (diode, tile, chunk) by binary search.  When a tile
+// (round-robin, or drawing items from a counter: queue_first / queue_next)
+// and decode
+// (diode, tile, chunk) by binary search.  When a tile
 // has more than one chunk, each chunk stores its partial sums in scratch and
 // the last chunk to finish (an atomic ticket, no waiting) adds the partials
 // in chunk order, so results do not depend on scheduling.
@@ -94,6 +96,40 @@ __device__ __forceinline__ bool tile_ticket(int* tickets, const ItemRef& it) {
   __syncthreads();
   if (s_last) __threadfence();
   return s_last != 0;
+}
+
+// Dynamic item scheduling.  The P = min(grid, total) first blocks take items
+// 0..P-1 (the others exit at once); after that a block draws its next item
+// from a counter (P + q[0]++) instead of walking a fixed stride, so blocks
+// that drew cheap items (small diodes) take more and the launch ends with the
+// work, not with the unluckiest block.  The last of the P blocks to leave
+// (q[1]) resets both counters for the next launch on the stream; its fence
+// orders each block's last draw before its leave.  No block waits on
+// another; results do not depend on the order (partials are added in chunk
+// order by tile_ticket).
+__device__ __forceinline__ int queue_first(int total) {
+  return (int)blockIdx.x < total ? (int)blockIdx.x : total;
+}
+
+__device__ __forceinline__ int queue_next(int* q, int* s_slot, int total) {
+  const int P = min((int)gridDim.x, total);
+  __syncthreads();
+  if (threadIdx.x == 0) *s_slot = P + atomicAdd(&q[0], 1);
+  __syncthreads();
+  return *s_slot;
+}
+
+__device__ __forceinline__ void queue_leave(int* q, int total) {
+  const int P = min((int)gridDim.x, total);
+  if ((int)blockIdx.x >= P) return;   // took no item
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&q[1], 1) == P - 1) {
+      q[0] = 0;
+      q[1] = 0;
+      __threadfence();
+    }
+  }
 }
 
 // Points of a field evaluation: per-diode lists at [off[d], off[d] + n_d).
