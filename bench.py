@@ -588,8 +588,9 @@ def case_plain(args):
     """The plain single-diode deck (CPU-runnable size): gap 1000 nm, 2 kV, a
     1000 x 1000 nm emitter centred on the axis, work function 4.7 eV (and a
     populated 2.0 eV variant), dt 0.25 fs, one image partner, MH with 100 and
-    with the reference's 200 jumps, FP64, Philox seed 20261203.  Steps/s of
-    the GPU engine (device time, rd_run) beside the CPU restatement."""
+    with the reference's 200 jumps, Philox seed 20261203.  Steps/s of the GPU
+    engine in FP64 and FP32-compensated form (device time, rd_run) beside the
+    CPU restatement (FP64)."""
     import rumdeed_gb300 as rg
     rg.build()
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -600,14 +601,18 @@ def case_plain(args):
               emitter_pos=(-side / 2, -side / 2), emitter_dim=(side, side), emission=True, seed=SEED)
     for phi in (4.7, 2.0):
         for jumps in (100, 200):
-            eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=20064,
-                            chain_capacity=20064, quad_capacity=4096)
-            d = eng.add_diode(work=[[phi]], mh_jumps=jumps, **kw)
-            eng.run(1, args.warmup)
-            eng.run(args.warmup + 1, args.steps)
-            ms, kps = eng.last_run_stats()
-            c = d.counters()
-            eng.close()
+            gpu = {}
+            for prec, tag in ((rg.PREC_FP64, "fp64"), (rg.PREC_FP32C, "fp32c")):
+                eng = rg.Engine(precision=prec, max_diodes=1, particle_capacity=20064,
+                                chain_capacity=20064, quad_capacity=4096)
+                d = eng.add_diode(work=[[phi]], mh_jumps=jumps, **kw)
+                eng.run(1, args.warmup)
+                eng.run(args.warmup + 1, args.steps)
+                ms, kps = eng.last_run_stats()
+                c = d.counters()
+                eng.close()
+                gpu[tag] = {"steps_per_s": args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                            "in_flight": c["n"], "emitted_total": c["emitted_total"], "N_sup": c["N_sup"]}
             o = orc.OracleDiode(cap=20000, V_s=2.0e3, d=1000 * NM, time_step=0.25e-15, image_charge=True,
                                 N_ic_max=0)
             o.set_planar_emitter(-side / 2, -side / 2, side, side, [[phi]])
@@ -618,10 +623,8 @@ def case_plain(args):
                 cpu_steps += 1
             cpu_t = time.perf_counter() - t0
             print(json.dumps({"case": "plain", "work_function_eV": phi, "mh_jumps": jumps,
-                              "gpu_fp64_steps_per_s": args.steps / (ms / 1e3), "gpu_ms_per_step": ms / args.steps,
-                              "kernels_per_step": kps, "after_steps": args.warmup + args.steps,
-                              "in_flight": c["n"], "emitted_total": c["emitted_total"], "N_sup": c["N_sup"],
-                              "cpu_steps_per_s": cpu_steps / cpu_t, "cpu_steps": cpu_steps,
+                              "after_steps": args.warmup + args.steps, "kernels_per_step": kps,
+                              "gpu": gpu, "cpu_steps_per_s": cpu_steps / cpu_t, "cpu_steps": cpu_steps,
                               "cpu_cores": orc.lib().orc_omp_threads()}), flush=True)
 
 

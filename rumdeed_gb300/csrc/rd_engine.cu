@@ -38,7 +38,7 @@ cudaError_t rd_upload_constants_step(const RdConst&);
 cudaError_t rd_launch_force(int prec, int geometry_mask, int nic_general, int grid, cudaStream_t st,
                             const DiodeParams* P, const DiodeDyn* Dy, const Pool& pool,
                             const PlanEntry* plan, const PlanHeader* ph, double* partial,
-                            int* tickets, double kscale);
+                            int* tickets, double kscale, int* queue);
 cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st,
                                    const DiodeParams* P, const Pool& pool, const PlanEntry* plan,
                                    const PlanHeader* ph, const PointSet& pts, double* partial,
@@ -46,7 +46,7 @@ cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st
 cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const DiodeParams* P,
                                 const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
                                 const double* qx, const double* qy, const float4* qpp, double* qF,
-                                double* partial, int* tickets, double kscale);
+                                double* partial, int* tickets, double kscale, int* queue);
 cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                     const double* qx, const double* qy, const double* qw,
                                     const double* qF, const double* qfx, const double* qfy,
@@ -316,7 +316,7 @@ static int launch_emission(rd_engine* e) {
     CK(plan(e, PM_SUPPLY_PLANAR));
     CK(rd_launch_z0_points(prec, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_PLANAR],
                            e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qpp, e->qF, e->partial, e->tickets,
-                           e->kscale));
+                           e->kscale, e->item_queue + 6));
     e->kernels_in_step++;
   }
   if (s.emit_tip) {
@@ -356,14 +356,14 @@ static int launch_force(rd_engine* e) {
     CK(plan(e, PM_FORCE_PLANAR));
     CK(rd_launch_force(e->cfg.precision, 1, s.nic ? 1 : 0, e->grid, e->st, e->dP, e->dD, e->pool,
                        e->plan[PM_FORCE_PLANAR], e->ph[PM_FORCE_PLANAR], e->partial, e->tickets,
-                       e->kscale));
+                       e->kscale, e->item_queue + 4));
     e->kernels_in_step++;
   }
   if (s.tip) {
     CK(plan(e, PM_FORCE_TIP));
     CK(rd_launch_force(e->cfg.precision, 2, 0, e->grid, e->st, e->dP, e->dD, e->pool,
                        e->plan[PM_FORCE_TIP], e->ph[PM_FORCE_TIP], e->partial, e->tickets,
-                       e->kscale));
+                       e->kscale, e->item_queue + 4));
     e->kernels_in_step++;
   }
   return RD_OK;
@@ -516,10 +516,10 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   const long long qcap = std::max<long long>(cfg->quad_capacity, 1);
   // scratch bound: the planner grows the chunk length until the items fit,
   // and with one chunk per tile every mode has at most capacity/128 + slots tiles
-  // scratch bound: at most 8 chunks per tile (RD_NCH_MAX) and at most
+  // scratch bound: at most RD_NCH_MAX chunks per tile and at most
   // capacity/128 + slots tiles in any pair sum
   e->max_items = (int)std::min<long long>(
-      1 << 26, 8LL * (std::max(cap, std::max(chcap, qcap)) / RD_ITILE + 4LL * S) + 65536);
+      1 << 26, (long long)RD_NCH_MAX * (std::max(cap, std::max(chcap, qcap)) / RD_ITILE + 4LL * S) + 65536);
   if ((rc = alloc_pool(e, e->pool, cap)) || (rc = alloc_pool(e, e->tmp, cap))) return bail(rc);
   if (e->dalloc(&e->dP, S) || e->dalloc(&e->dD, S) || e->dalloc(&e->work, (size_t)S * 4 + 4096) || e->dalloc(&e->wtab, 3 * ((size_t)S * 4 + 4096)) ||
       e->dalloc(&e->qx, qcap) || e->dalloc(&e->qy, qcap) || e->dalloc(&e->qz, qcap) ||
@@ -1075,7 +1075,7 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
     if (s.emit_planar) {
       CK(plan(e, PM_SUPPLY_PLANAR));
       CK(rd_launch_z0_points(prec, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_PLANAR],
-                             e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qpp, e->qF, e->partial, e->tickets, e->kscale));
+                             e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qpp, e->qF, e->partial, e->tickets, e->kscale, e->item_queue + 6));
     }
     if (s.emit_tip) {
       CK(plan(e, PM_SUPPLY_TIP));

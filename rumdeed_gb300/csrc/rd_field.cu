@@ -257,45 +257,64 @@ __device__ __forceinline__ float z0_tile_f32(const float4* __restrict__ sh, cons
   return s0 + s1;
 }
 
-// Tile sums for two points a, b at z = 0 (nic = 0), in packed FP32x2
-// arithmetic: point a in the .x lanes, b in the .y lanes.  The j data sit in
+// Tile sums for 2 NP points at z = 0 (nic = 0) in packed FP32x2 arithmetic:
+// points 2i and 2i+1 in the .x and .y lanes of pair i.  The j data sit in
 // shared memory duplicated and negated, s0 = (-x_hi, -x_hi, -x_lo, -x_lo),
-// s1 = (-y_hi, ..), s2 = (z^2, z^2, q z, q z), so each step for the two
-// points is one packed instruction (rsqrt stays per lane).  The points are
-// taken at their FP32 nm offsets (PX, PY: their high words; the FP32 MH
-// chains are kept as such offsets), so dx = (p - x_hi) - x_lo: the first difference
-// is exact for nearby pairs (Sterbenz) and the particle's low word restores
-// its FP64 position.
-__device__ __forceinline__ void z0_tile2_x2(const float4* __restrict__ s0, const float4* __restrict__ s1,
-                                            const float4* __restrict__ s2, int kmax, float2 PX, float2 PY,
-                                            float& ra, float& rb) {
-  float2 s = make_float2(0.f, 0.f);
+// s1 = (-y_hi, ..), s2 = (z^2, z^2, q z, q z), so each step for a pair of
+// points is one packed instruction (rsqrt stays per lane), and one set of
+// shared loads feeds all 2 NP points.  The points are taken at their FP32 nm
+// offsets (PX, PY: their high words; the FP32 MH chains are kept as such
+// offsets), so dx = (p - x_hi) - x_lo: the first difference is exact for
+// nearby pairs (Sterbenz) and the particle's low word restores its FP64
+// position.
+template <int NP>
+__device__ __forceinline__ void z0_tile_x2(const float4* __restrict__ s0, const float4* __restrict__ s1,
+                                           const float4* __restrict__ s2, int kmax, const float2* PX,
+                                           const float2* PY, float* r) {
+  float2 s[NP];
+#pragma unroll
+  for (int i = 0; i < NP; ++i) s[i] = make_float2(0.f, 0.f);
 #pragma unroll 4
   for (int k = 0; k < kmax; ++k) {
     const float4 a = s0[k], b = s1[k], c = s2[k];
-    const float2 dx = __fadd2_rn(__fadd2_rn(PX, make_float2(a.x, a.y)), make_float2(a.z, a.w));
-    const float2 dy = __fadd2_rn(__fadd2_rn(PY, make_float2(b.x, b.y)), make_float2(b.z, b.w));
-    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, make_float2(c.x, c.y)));
-    float2 inv;
-    inv.x = rsqrtf(r2.x);
-    inv.y = rsqrtf(r2.y);
-    s = __ffma2_rn(make_float2(c.z, c.w), __fmul2_rn(__fmul2_rn(inv, inv), inv), s);
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+      const float2 dx = __fadd2_rn(__fadd2_rn(PX[i], make_float2(a.x, a.y)), make_float2(a.z, a.w));
+      const float2 dy = __fadd2_rn(__fadd2_rn(PY[i], make_float2(b.x, b.y)), make_float2(b.z, b.w));
+      const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, make_float2(c.x, c.y)));
+      float2 inv;
+      inv.x = rsqrtf(r2.x);
+      inv.y = rsqrtf(r2.y);
+      s[i] = __ffma2_rn(make_float2(c.z, c.w), __fmul2_rn(__fmul2_rn(inv, inv), inv), s[i]);
+    }
   }
-  ra += s.x;
-  rb += s.y;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) { r[2 * i] += s[i].x; r[2 * i + 1] += s[i].y; }
 }
 
-// Partial F_z sums of the item for two points at z = 0 (FP32 compensated),
-// blockDim threads loading the j-tiles.
-__device__ __forceinline__ void z0_item_sum2(const DiodeParams& p, const Pool& pool, const ItemRef& it,
-                                             float4 pa, float4 pb, float4* sh, float4* sl,
-                                             double* out_a, double* out_b) {
+// Partial F_z sums of the item for CPT points at z = 0 (FP32 compensated),
+// given as (x_hi, x_lo, y_hi, y_lo) nm; blockDim threads load the j-tiles.
+// The raw sums (nm units) are folded into (hi, lo) pairs across j-tiles with
+// two-sum and returned as doubles; z0_finish turns them into V/m.
+template <int CPT>
+__device__ __forceinline__ void z0_item_sumN(const DiodeParams& p, const Pool& pool, const ItemRef& it,
+                                             const float4* pts, double* out) {
+  constexpr int NP = CPT / 2;
   __shared__ float4 sp[3][RD_TILE];
+  float4* sh = sp[0];   // nic > 0: raw packs
+  float4* sl = sp[1];
   const int off = p.off, tid = threadIdx.x, nt = blockDim.x;
   const int nic = p.image_charge ? p.N_ic_max : 0;
   const float dnm = (float)(p.d * 1.0e9);
-  float ha = 0.f, la = 0.f, hb = 0.f, lb = 0.f;
-  const float2 PX = make_float2(pa.x, pb.x), PY = make_float2(pa.z, pb.z);
+  float hi[CPT], lo[CPT];
+  float2 PX[NP], PY[NP];
+#pragma unroll
+  for (int i = 0; i < CPT; ++i) { hi[i] = 0.f; lo[i] = 0.f; }
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    PX[i] = make_float2(pts[2 * i].x, pts[2 * i + 1].x);
+    PY[i] = make_float2(pts[2 * i].z, pts[2 * i + 1].z);
+  }
   for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
     __syncthreads();
     for (int q = tid; q < RD_TILE; q += nt) {
@@ -313,18 +332,20 @@ __device__ __forceinline__ void z0_item_sum2(const DiodeParams& p, const Pool& p
     }
     __syncthreads();
     const int kmax = min(RD_TILE, it.j1 - jt);
-    float ta = 0.f, tb = 0.f;
+    float t[CPT];
+#pragma unroll
+    for (int i = 0; i < CPT; ++i) t[i] = 0.f;
     if (nic == 0) {
-      z0_tile2_x2(sp[0], sp[1], sp[2], kmax, PX, PY, ta, tb);
+      z0_tile_x2<NP>(sp[0], sp[1], sp[2], kmax, PX, PY, t);
     } else {
-      ta = z0_tile_f32<false>(sh, sl, kmax, pa, nic, dnm);
-      tb = z0_tile_f32<false>(sh, sl, kmax, pb, nic, dnm);
+#pragma unroll
+      for (int i = 0; i < CPT; ++i) t[i] = z0_tile_f32<false>(sh, sl, kmax, pts[i], nic, dnm);
     }
-    two_sum_acc(ha, la, ta);
-    two_sum_acc(hb, lb, tb);
+#pragma unroll
+    for (int i = 0; i < CPT; ++i) two_sum_acc(hi[i], lo[i], t[i]);
   }
-  *out_a = (double)ha + (double)la;
-  *out_b = (double)hb + (double)lb;
+#pragma unroll
+  for (int i = 0; i < CPT; ++i) out[i] = (double)hi[i] + (double)lo[i];
 }
 
 __device__ __forceinline__ double z0_tile_f64(const rd_d4* __restrict__ sj, int kmax, double px,
@@ -403,13 +424,14 @@ __global__ void __launch_bounds__(RD_ITILE)
 k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __restrict__ plan,
             const PlanHeader* __restrict__ ph, const double* __restrict__ qx,
             const double* __restrict__ qy, const float4* __restrict__ qpp, double* __restrict__ qF,
-            double* __restrict__ partial, int* __restrict__ tickets, double kscale) {
+            double* __restrict__ partial, int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
+  __shared__ int s_item;
   __shared__ float4 sh[RD_TILE], sl[RD_TILE];
   __shared__ rd_d4 sj[RD_TILE];
   constexpr int CPT = PREC == 1 ? 2 : 1;
   const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
-  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int m = plan[it.d].n_i, qo = p.q_off;
@@ -417,8 +439,8 @@ k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __res
     if (PREC == 1) {
       const int i0 = it.i0 + tid, i1 = it.i0 + nt + tid;
       const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-      z0_item_sum2(p, pool, it, i0 < m ? qpp[qo + i0] : z4, i1 < m ? qpp[qo + i1] : z4, sh, sl,
-                   &s[0], &s[CPT - 1]);
+      const float4 pts[2] = {i0 < m ? qpp[qo + i0] : z4, i1 < m ? qpp[qo + i1] : z4};
+      z0_item_sumN<2>(p, pool, it, pts, s);
     } else {
       const int i = it.i0 + tid;
       const bool valid = i < m;
@@ -438,6 +460,7 @@ k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __res
       if (i < m) qF[qo + i] = z0_finish<PREC>(p, s[q], kscale);
     }
   }
+  queue_leave(queue, total);
 }
 
 // ---- supply integrals ------------------------------------------------------------------
@@ -772,7 +795,7 @@ __device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState&
 // tile then runs the accept / reject test of its chains (:1400-1443), draws
 // their next Gaussian pairs and counts acceptances; the tile completing the
 // diode updates MH_std from the iteration's acceptance rate (:1438-1443).
-// FP32: 64 threads, two chains each; FP64: 128 threads, one chain each.
+// FP32: 32 threads, four chains each; FP64: 128 threads, one chain each.
 template <int PREC>
 __global__ void __launch_bounds__(RD_ITILE)
 k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
@@ -780,11 +803,9 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
                  const int* __restrict__ ch_off, const double* __restrict__ wtab,
                  const int* __restrict__ step_ptr, int it_idx, double* __restrict__ partial,
                  int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
-  __shared__ float4 sh[RD_TILE], sl[RD_TILE];
-  __shared__ rd_d4 sj[RD_TILE];
   __shared__ int red_i[2 * RD_ITILE];
   __shared__ int s_item;
-  constexpr int CPT = PREC == 1 ? 2 : 1;
+  constexpr int CPT = PREC == 1 ? 4 : 1;
   const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   const bool init = it_idx == 0;
@@ -849,9 +870,13 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
     }
     double s[CPT];
     if constexpr (PREC == 1) {
-      z0_item_sum2(p, pool, it, make_float4(fwx[0], 0.f, fwy[0], 0.f),
-                   make_float4(fwx[CPT - 1], 0.f, fwy[CPT - 1], 0.f), sh, sl, &s[0], &s[CPT - 1]);
+      float4 pts[CPT];
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) pts[q] = make_float4(fwx[q], 0.f, fwy[q], 0.f);
+      z0_item_sumN<CPT>(p, pool, it, pts, s);
     } else {
+      __shared__ float4 sh[RD_TILE], sl[RD_TILE];
+      __shared__ rd_d4 sj[RD_TILE];
       s[0] = z0_item_sum<PREC>(p, pool, it, wx[0], wy[0], make_float4(0.f, 0.f, 0.f, 0.f), sh, sl, sj);
     }
     if (it.nch > 1) {
@@ -917,12 +942,13 @@ __global__ void __launch_bounds__(RD_ITILE)
 k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
               const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
               ChainState cs, const int* __restrict__ ch_off, const int* __restrict__ step_ptr,
-              int it_idx, double* __restrict__ partial, int* __restrict__ tickets, double kscale) {
+              int it_idx, double* __restrict__ partial, int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
+  __shared__ int s_item;
   __shared__ float4 sh[RD_TILE], sl[RD_TILE], sih[RD_TILE], sil[RD_TILE];
   __shared__ rd_d4 sj[RD_TILE];
   __shared__ int red_i[2 * RD_ITILE];
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
-  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     if (p.geometry != RD_G_TIP || it_idx > p.mh_jumps) continue;
@@ -1015,6 +1041,7 @@ k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool
     }
     mh_counts_and_update(p, y, plan[it.d].tiles, it_idx, ndim_first, a, r, red_i);
   }
+  queue_leave(queue, total);
 }
 
 // ---- MH proposals: one thread per chain -------------------------------------------------
@@ -1191,9 +1218,9 @@ cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st
 cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const DiodeParams* P,
                                 const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
                                 const double* qx, const double* qy, const float4* qpp, double* qF,
-                                double* partial, int* tickets, double kscale) {
-  if (prec == 1) k_z0_points<1><<<rd_grid(k_z0_points<1>, 64, grid), 64, 0, st>>>(P, pool, plan, ph, qx, qy, qpp, qF, partial, tickets, kscale);
-  else k_z0_points<0><<<rd_grid(k_z0_points<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph, qx, qy, qpp, qF, partial, tickets, kscale);
+                                double* partial, int* tickets, double kscale, int* queue) {
+  if (prec == 1) k_z0_points<1><<<rd_grid(k_z0_points<1>, 64, grid), 64, 0, st>>>(P, pool, plan, ph, qx, qy, qpp, qF, partial, tickets, kscale, queue);
+  else k_z0_points<0><<<rd_grid(k_z0_points<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph, qx, qy, qpp, qF, partial, tickets, kscale, queue);
   return cudaGetLastError();
 }
 
@@ -1220,13 +1247,13 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               const int* ch_off, const double* wtab, const int* step_ptr,
                               int it_idx, double* partial, int* tickets, double kscale, int* queue) {
   if (geometry_mask & 1) {
-    if (prec == 1) k_mh_jump_planar<1><<<rd_grid(k_mh_jump_planar<1>, 64, grid), 64, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue);
+    if (prec == 1) k_mh_jump_planar<1><<<rd_grid(k_mh_jump_planar<1>, 32, grid), 32, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue);
     else k_mh_jump_planar<0><<<rd_grid(k_mh_jump_planar<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue);
   }
   if (geometry_mask & 2) {
     k_mh_propose<<<rd_grid(k_mh_propose, 256, grid), 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx);
-    if (prec == 1) k_mh_jump_tip<1><<<rd_grid(k_mh_jump_tip<1>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale);
-    else k_mh_jump_tip<0><<<rd_grid(k_mh_jump_tip<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale);
+    if (prec == 1) k_mh_jump_tip<1><<<rd_grid(k_mh_jump_tip<1>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale, queue + 2);
+    else k_mh_jump_tip<0><<<rd_grid(k_mh_jump_tip<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale, queue + 2);
   }
   return cudaGetLastError();
 }

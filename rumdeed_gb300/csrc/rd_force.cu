@@ -83,11 +83,12 @@ __device__ __forceinline__ void planar_tile2_nic0(const float4* __restrict__ sh,
 __global__ void __launch_bounds__(64)
 k_force_planar_f32_nic0(const DiodeParams* __restrict__ P, Pool pool,
                         const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
-                        double* __restrict__ partial, int* __restrict__ tickets, double kscale) {
+                        double* __restrict__ partial, int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
+  __shared__ int s_item;
   __shared__ float4 sh[RD_TILE], sl[RD_TILE];
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x, nt = 64;
-  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -145,17 +146,19 @@ k_force_planar_f32_nic0(const DiodeParams* __restrict__ P, Pool pool,
       pool.az[gi] = pre * f[q][2] + qi * p.E_z * im;
     }
   }
+  queue_leave(queue, total);
 }
 
 template <bool NIC0>
 __global__ void __launch_bounds__(RD_ITILE)
 k_force_planar_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
                    const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
-                   double* __restrict__ partial, int* __restrict__ tickets, double kscale) {
+                   double* __restrict__ partial, int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
+  __shared__ int s_item;
   __shared__ float4 sh[RD_TILE], sl[RD_TILE];
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x;
-  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -205,17 +208,19 @@ k_force_planar_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict
       pool.az[gi] = pre * fz + qi * p.E_z * im;
     }
   }
+  queue_leave(queue, total);
 }
 
 __global__ void __launch_bounds__(RD_ITILE)
 k_force_planar_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
                    const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
-                   double* __restrict__ partial, int* __restrict__ tickets) {
+                   double* __restrict__ partial, int* __restrict__ tickets, int* __restrict__ queue) {
+  __shared__ int s_item;
   __shared__ rd_d4 sj[RD_TILE];
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x;
   const double L2 = c_k.L2, dfc = c_k.div_fac_c;
-  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -256,17 +261,19 @@ k_force_planar_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict
       pool.az[gi] = (az + q1 * p.E_z) * im;
     }
   }
+  queue_leave(queue, total);
 }
 
 __global__ void __launch_bounds__(RD_ITILE)
 k_force_tip_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
                 const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
-                double* __restrict__ partial, int* __restrict__ tickets, double kscale) {
+                double* __restrict__ partial, int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
+  __shared__ int s_item;
   __shared__ float4 sh[RD_TILE], sl[RD_TILE], sih[RD_TILE], sil[RD_TILE];
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x;
   const float K = (float)c_k.tip_K;
-  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -319,17 +326,19 @@ k_force_tip_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
       pool.az[gi] = pre * fz + qi * ez * im;
     }
   }
+  queue_leave(queue, total);
 }
 
 __global__ void __launch_bounds__(RD_ITILE)
 k_force_tip_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
                 const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
-                double* __restrict__ partial, int* __restrict__ tickets) {
+                double* __restrict__ partial, int* __restrict__ tickets, int* __restrict__ queue) {
+  __shared__ int s_item;
   __shared__ rd_d4 sj[RD_TILE];
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x;
   const double L2 = c_k.L2, dfc = c_k.div_fac_c, K = c_k.tip_K;
-  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -372,6 +381,7 @@ k_force_tip_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
       pool.az[gi] = (az + q1 * ez) * im;
     }
   }
+  queue_leave(queue, total);
 }
 
 }  // namespace
@@ -380,23 +390,23 @@ k_force_tip_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
 cudaError_t rd_launch_force(int prec, int geometry_mask, int nic_general, int grid,
                             cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy,
                             const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
-                            double* partial, int* tickets, double kscale) {
+                            double* partial, int* tickets, double kscale, int* queue) {
   // geometry_mask: bit0 planar diodes present, bit1 tip diodes present.  The
   // planar and tip kernels each skip items of the other geometry through the
   // plan (separate plans per geometry are built by the engine).
   if (prec == 0) {
     if (geometry_mask & 1)
-      k_force_planar_f64<<<rd_grid(k_force_planar_f64, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets);
+      k_force_planar_f64<<<rd_grid(k_force_planar_f64, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, queue);
     else
-      k_force_tip_f64<<<rd_grid(k_force_tip_f64, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets);
+      k_force_tip_f64<<<rd_grid(k_force_tip_f64, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, queue);
   } else {
     if (geometry_mask & 1) {
       if (nic_general)
-        k_force_planar_f32<false><<<rd_grid(k_force_planar_f32<false>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale);
+        k_force_planar_f32<false><<<rd_grid(k_force_planar_f32<false>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale, queue);
       else
-        k_force_planar_f32_nic0<<<rd_grid(k_force_planar_f32_nic0, 64, grid), 64, 0, st>>>(P, pool, plan, ph, partial, tickets, kscale);
+        k_force_planar_f32_nic0<<<rd_grid(k_force_planar_f32_nic0, 64, grid), 64, 0, st>>>(P, pool, plan, ph, partial, tickets, kscale, queue);
     } else {
-      k_force_tip_f32<<<rd_grid(k_force_tip_f32, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale);
+      k_force_tip_f32<<<rd_grid(k_force_tip_f32, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale, queue);
     }
   }
   return cudaGetLastError();

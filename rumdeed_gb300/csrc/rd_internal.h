@@ -20,6 +20,10 @@
 
 #define RD_TILE 128           // particles per shared-memory j-tile
 #define RD_ITILE 128          // i-particles (or points) per work item
+// j-chunking of pair sums: at least RD_CLEN_MIN particles per chunk, at most
+// RD_NCH_MAX chunks per i-tile
+#define RD_CLEN_MIN 1024
+#define RD_NCH_MAX 32
 #define RD_MAX_LIFE 1000
 #define RD_MAX_WORK 4096      // max checkerboard cells per diode (64x64)
 

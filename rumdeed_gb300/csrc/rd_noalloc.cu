@@ -47,7 +47,7 @@
 #define NA_OFF_PTS 1024                                 // 3 x MAX doubles (x, y, z)
 #define NA_OFF_FLD (NA_OFF_PTS + 3 * 8 * RD_NOALLOC_MAX_POINTS)   // 3 x MAX doubles
 #define NA_OFF_PART (NA_OFF_FLD + 3 * 8 * RD_NOALLOC_MAX_POINTS)  // partials
-#define NA_MAX_ITEMS 4096                               // 512 tiles x 8 chunks
+#define NA_MAX_ITEMS 4096   // the planner lengthens the j-chunks of a call that would need more
 #define NA_OFF_TICK (NA_OFF_PART + NA_MAX_ITEMS * 3 * RD_ITILE * 8)
 #define NA_END (NA_OFF_TICK + NA_MAX_ITEMS * 4)
 static_assert(NA_END <= RD_NOALLOC_SCRATCH_BYTES, "no-alloc scratch layout exceeds the array");

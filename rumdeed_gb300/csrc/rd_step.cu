@@ -83,9 +83,9 @@ __device__ __forceinline__ int plan_ni(const DiodeParams& p, const DiodeDyn& y, 
 // Tiles and j-chunking of one diode.  The chunk length depends only on the
 // diode's own counts (at least RD_CLEN_MIN particles, at most RD_NCH_MAX
 // chunks per tile), so the summation order -- and therefore every result --
-// is the same whether a diode runs alone or among other diodes.
-#define RD_CLEN_MIN 1024
-#define RD_NCH_MAX 8
+// is the same whether a diode runs alone or among other diodes.  Chunks of
+// at most ~1024 particles also bound the cost of one work item, so the last
+// items of a launch end soon after the others.
 __device__ __forceinline__ void plan_split(int ni, int nj, int tsize, bool pair, int grow,
                                            int* tiles, int* nch, int* clen) {
   *tiles = (ni + tsize - 1) / tsize;
