@@ -301,6 +301,11 @@ def run_ours(args, rank, world):
             break
         if it > 100000:
             break
+    # the autotuner picks the pair-sum chunking for the resident mix; one more
+    # untimed iteration rebuilds the step graph under it
+    tune = eng.autotune()
+    submit_arrived()
+    eng.serve(1)
     # timed region
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     if world > 1:
@@ -387,6 +392,8 @@ def run_ours(args, rank, world):
         "data": "synthetic request stream (seeded PCG64; no dataset involved)",
         "config": {"workload": WORKLOAD,
                    "slots": S, "precision": "fp32c", "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "chunking": {"chunk_min": tune["chunk_min"], "chunk_count_max": tune["chunk_count_max"],
+                                "tuned_ms": tune["ms_chosen"], "default_ms": tune["ms_default"]},
                    "l2": "256 MB buffer written between timed iterations",
                    "resident_diodes": running, "queued_requests": queued,
                    "admitted_in_timed": admitted, "retired_in_timed": retired},

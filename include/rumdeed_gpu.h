@@ -51,9 +51,13 @@ typedef struct {
   long long particle_capacity;  /* particle pool size (sum of diode capacities) */
   long long chain_capacity;     /* MH chain pool size (sum of per-diode chain caps) */
   long long quad_capacity;      /* supply quadrature points over all diodes */
-  int target_items;             /* reserved, 0 (work items follow the per-diode chunk rule) */
+  int chunk_min;                /* j-chunk length floor of the pair sums, particles, a
+                                   multiple of 128 (0 = 1024); see rd_autotune */
   int grid_blocks;              /* persistent grid size (0 = per kernel: resident blocks per
                                    SM at its occupancy x SM count) */
+  int chunk_count_max;          /* at most this many j-chunks per i-tile, 1..32 (0 = 32) */
+  int event_capacity;           /* records the event log holds between two rd_events_take
+                                   calls (0 = no event log); see rd_events_take */
 } rd_engine_config;
 
 /* One diode (the namelist /input/ of one run, src/mod_global.F90:426-439). */
@@ -197,6 +201,47 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out);
 int rd_time_accel(rd_engine* e, int reps, double* ms_per_eval);
 int rd_time_field_at(rd_engine* e, int diode, int M, const double* pos3m, int reps,
                      double* ms_per_eval);
+
+/* ---- event log: emission and absorption records ------------------------------
+ * The reference writes one record per emitted particle (density_emit.bin and
+ * density_emit_elec.bin, src/mod_pair.F90:89-123, at Add_Particle) and one per
+ * electron absorbed at the anode or the cathode (density_absorb_top.bin /
+ * density_absorb_bot.bin, :241-257, at Mark_Particles_Remove) as the events
+ * happen.  With rd_engine_config.event_capacity > 0 the step kernels append
+ * the same data to a device log: position (m) and velocity (m/s) at the event
+ * (emission: the placement point, velocity 0; absorption: after the position
+ * update that crossed the electrode), diode, kind, section, particle id,
+ * species and the diode's step.  rd_events_take copies the records logged
+ * since the last take into `out` (at most `cap`), ordered by diode, kind and
+ * id, empties the log and reports records that did not fit (the log's or the
+ * caller's capacity) in n_lost. */
+enum { RD_EVENT_EMIT = 1, RD_EVENT_ABSORB_TOP = 2, RD_EVENT_ABSORB_BOT = 3 };
+typedef struct {
+  double pos[3], vel[3];
+  int diode, kind, section, id, species, step;
+} rd_event;
+int rd_events_take(rd_engine* e, int cap, rd_event* out, int* n_out, long long* n_lost);
+
+/* ---- autotuner (no counterpart in the reference) ----------------------------
+ * Every pair sum (forces, cathode fields, MH jumps) cuts an i-tile's j range
+ * into chunks of max(chunk_min, ceil(n / chunk_count_max)) particles (rounded
+ * up to 128): longer chunks mean fewer partial sums, shorter ones a shorter
+ * tail at the end of a launch.  The chunking depends only on a diode's own
+ * counts and these two numbers, so a diode's results are the same alone and
+ * in any mix under the same chunking; different chunkings differ in the last
+ * FP32 bits.  rd_autotune times every candidate chunking on the diodes
+ * resident now -- the force pass and a dry MH pass (the field at every
+ * chain's current point, nothing written) weighted by the jump count --
+ * keeps the fastest, rebuilds the step graph and leaves the particle state
+ * as it was.  rd_set_chunking sets one directly (0 = default). */
+typedef struct {
+  int chunk_min, chunk_count_max;   /* the chosen chunking */
+  double ms_default, ms_chosen;     /* estimated step pair-sum time under the default / chosen */
+  int candidates;
+} rd_tune_result;
+int rd_autotune(rd_engine* e, rd_tune_result* out);
+int rd_set_chunking(rd_engine* e, int chunk_min, int chunk_count_max);
+int rd_get_chunking(rd_engine* e, int* chunk_min, int* chunk_count_max);
 
 /* ---- serving: continuous batching of diode simulations ---------------------
  * The reference runs one simulation per process.  Requests queue in FIFO

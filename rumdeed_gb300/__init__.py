@@ -45,8 +45,16 @@ class RumdeedError(RuntimeError):
 class EngineConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("precision", C.c_int), ("max_diodes", C.c_int),
                 ("particle_capacity", C.c_longlong), ("chain_capacity", C.c_longlong),
-                ("quad_capacity", C.c_longlong), ("target_items", C.c_int),
-                ("grid_blocks", C.c_int)]
+                ("quad_capacity", C.c_longlong), ("chunk_min", C.c_int),
+                ("grid_blocks", C.c_int), ("chunk_count_max", C.c_int), ("event_capacity", C.c_int)]
+
+
+class Event(C.Structure):
+    _fields_ = [("pos", C.c_double * 3), ("vel", C.c_double * 3), ("diode", C.c_int), ("kind", C.c_int),
+                ("section", C.c_int), ("id", C.c_int), ("species", C.c_int), ("step", C.c_int)]
+
+
+EVENT_EMIT, EVENT_ABSORB_TOP, EVENT_ABSORB_BOT = 1, 2, 3
 
 
 class DiodeConfig(C.Structure):
@@ -113,6 +121,14 @@ class ServeStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("chunk_min", C.c_int), ("chunk_count_max", C.c_int), ("ms_default", C.c_double),
+                ("ms_chosen", C.c_double), ("candidates", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED = 0, 1, 2, 3
 
 
@@ -153,6 +169,10 @@ SIGNATURES = {
     "rd_field_at_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "rd_time_accel": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "rd_time_field_at": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_int, _dp]),
+    "rd_autotune": (C.c_int, [C.c_void_p, C.POINTER(TuneResult)]),
+    "rd_events_take": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Event), _ip, C.POINTER(C.c_longlong)]),
+    "rd_set_chunking": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "rd_get_chunking": (C.c_int, [C.c_void_p, _ip, _ip]),
 }
 
 
@@ -198,11 +218,11 @@ class Engine:
     """One GPU, a pool of diode slots advanced together (segment table)."""
 
     def __init__(self, precision=PREC_FP32C, max_diodes=16, particle_capacity=1 << 20,
-                 chain_capacity=1 << 16, quad_capacity=1 << 16, device=0, target_items=0,
-                 grid_blocks=0):
+                 chain_capacity=1 << 16, quad_capacity=1 << 16, device=0, chunk_min=0,
+                 grid_blocks=0, chunk_count_max=0, event_capacity=0):
         self.L = lib()
         cfg = EngineConfig(device, precision, max_diodes, particle_capacity, chain_capacity,
-                           quad_capacity, target_items, grid_blocks)
+                           quad_capacity, chunk_min, grid_blocks, chunk_count_max, event_capacity)
         h = C.c_void_p()
         _check(self.L.rd_engine_create(C.byref(cfg), C.byref(h)))
         self.h = h
@@ -276,6 +296,34 @@ class Engine:
         st = ServeStats()
         _check(self.L.rd_serve(self.h, iterations, C.byref(st)))
         return st.as_dict()
+
+    # event log -----------------------------------------------------------------
+    def events_take(self, cap=1 << 20):
+        """Emission / absorption records logged since the last take
+        (rd_events_take): a list of dicts and the number of lost records."""
+        buf = (Event * max(cap, 1))()
+        n = C.c_int()
+        lost = C.c_longlong()
+        _check(self.L.rd_events_take(self.h, cap, buf, C.byref(n), C.byref(lost)))
+        out = [{"pos": tuple(r.pos), "vel": tuple(r.vel), "diode": r.diode, "kind": r.kind,
+                "section": r.section, "id": r.id, "species": r.species, "step": r.step}
+               for r in buf[:n.value]]
+        return out, lost.value
+
+    # autotuner -----------------------------------------------------------------
+    def autotune(self):
+        """Pick the pair-sum chunking for the resident diodes (rd_autotune)."""
+        t = TuneResult()
+        _check(self.L.rd_autotune(self.h, C.byref(t)))
+        return t.as_dict()
+
+    def set_chunking(self, chunk_min=0, chunk_count_max=0):
+        _check(self.L.rd_set_chunking(self.h, chunk_min, chunk_count_max))
+
+    def get_chunking(self):
+        a, b = C.c_int(), C.c_int()
+        _check(self.L.rd_get_chunking(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def time_accel(self, reps=3):
         """Device milliseconds of one force evaluation of all resident diodes."""

@@ -192,6 +192,19 @@ __device__ __forceinline__ void split_nm(double v_m, double origin_m, float* hi,
   *lo = (float)(v - (double)h);
 }
 
+// Append one record to the event log (no-op without a log).
+__device__ __forceinline__ void log_event(const EventLog& L, double x, double y, double z, double vx,
+                                          double vy, double vz, int diode, int kind, int section,
+                                          int id, int species, int step) {
+  if (!L.buf) return;
+  const int k = atomicAdd(L.count, 1);
+  if (k >= L.cap) return;
+  rd_event& r = L.buf[k];
+  r.pos[0] = x; r.pos[1] = y; r.pos[2] = z;
+  r.vel[0] = vx; r.vel[1] = vy; r.vel[2] = vz;
+  r.diode = diode; r.kind = kind; r.section = section; r.id = id; r.species = species; r.step = step;
+}
+
 // Knuth two-sum accumulation of a float into a (hi, lo) pair.
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
   float s = hi + v;

@@ -62,14 +62,14 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               int it_idx, double* partial, int* tickets, double kscale, int* queue);
 cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                            const Pool& pool, const ChainState& cs, const int* ch_off,
-                           const double* work, const int* step_ptr);
+                           const double* work, const int* step_ptr, const EventLog& ev);
 cudaError_t rd_launch_plan(cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy, int nslots,
-                           int mode, int target_items, int max_items, const int* npts,
+                           int mode, int chunk_rule, int max_items, const int* npts,
                            PlanEntry* plan, PlanHeader* ph);
 cudaError_t rd_launch_pack(int grid, cudaStream_t st, const DiodeParams* P, const Pool& pool,
                            const PlanEntry* plan, const PlanHeader* ph);
 cudaError_t rd_launch_position(int grid, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
-                               const Pool& pool, const PlanEntry* plan, const PlanHeader* ph);
+                               const Pool& pool, const PlanEntry* plan, const PlanHeader* ph, const EventLog& ev, const int* step_ptr);
 cudaError_t rd_launch_velocity(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
                                DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
                                const PlanHeader* ph, double* ramo);
@@ -201,6 +201,7 @@ struct rd_engine {
   RdConst k{};
   double kscale = 0.0;
   int max_items = 0;
+  int clen_min = RD_CLEN_MIN, nch_max = RD_NCH_MAX;   // chunk rule of the pair sums
   // device memory
   DiodeParams* dP = nullptr;
   DiodeDyn* dD = nullptr;
@@ -217,6 +218,7 @@ struct rd_engine {
   double* partial = nullptr;
   int* tickets = nullptr;
   int* item_queue = nullptr;   // dynamic item counters (queue_next / queue_leave)
+  EventLog evlog{nullptr, nullptr, 0};   // emission / absorption records (rd_events_take)
   int* kept = nullptr;
   double* ramo = nullptr;
   int* life = nullptr;
@@ -278,14 +280,15 @@ static int alloc_pool(rd_engine* e, Pool& P, long long cap) {
 }
 
 // ---- pipeline pieces ----------------------------------------------------------------
-static int target_items(const rd_engine* e) {
-  return e->cfg.target_items > 0 ? e->cfg.target_items : 8 * 4 * e->sms;
-}
-
 static cudaError_t plan(rd_engine* e, int mode, const int* npts = nullptr) {
   e->kernels_in_step++;
-  return rd_launch_plan(e->st, e->dP, e->dD, e->nslots_hw(), mode, target_items(e), e->max_items,
-                        npts, e->plan[mode], e->ph[mode]);
+  return rd_launch_plan(e->st, e->dP, e->dD, e->nslots_hw(), mode, rd_chunk_rule(e->clen_min, e->nch_max),
+                        e->max_items, npts, e->plan[mode], e->ph[mode]);
+}
+
+static bool valid_chunking(int clen_min, int nch_max) {
+  return clen_min >= RD_TILE && clen_min <= 65536 && clen_min % RD_TILE == 0 && nch_max >= 1 &&
+         nch_max <= RD_NCH_MAX;
 }
 
 struct Sig {
@@ -330,22 +333,21 @@ static int launch_emission(rd_engine* e) {
                              e->work));
   e->kernels_in_step++;
   CK(plan(e, PM_MH));
-  if (s.emit_planar) {   // round 0 of the planar chain start, tiled
-    CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                         e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue));
-    e->kernels_in_step++;
-  }
+  const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
+  // round 0 of the chain start, tiled like a jump; k_mh_init continues the rest
+  CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                       e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue));
+  e->kernels_in_step += ((gmask & 1) ? 1 : 0) + ((gmask & 2) ? 2 : 0);
   CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                        e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
   e->kernels_in_step++;
-  const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
   for (int it = 1; it <= s.jumps; ++it) {
     CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH],
                          e->ph[PM_MH], e->cs, e->d_choff, e->wtab, e->d_step, it, e->partial,
                          e->tickets, e->kscale, e->item_queue));
     e->kernels_in_step += ((gmask & 1) ? 1 : 0) + ((gmask & 2) ? 2 : 0);   // planar jump, tip propose + jump
   }
-  CK(rd_launch_emit(ns, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step));
+  CK(rd_launch_emit(ns, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step, e->evlog));
   e->kernels_in_step++;
   return RD_OK;
 }
@@ -372,7 +374,8 @@ static int launch_force(rd_engine* e) {
 static int launch_update_position(rd_engine* e) {
   const int ns = e->nslots_hw();
   CK(plan(e, PM_PART));
-  CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART]));
+  CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->evlog,
+                        e->d_step));
   e->kernels_in_step++;
   int rc = launch_force(e);
   if (rc) return rc;
@@ -406,7 +409,8 @@ static int launch_step_body(rd_engine* e) {
 static std::string sig_string(rd_engine* e) {
   Sig s = signature(e);
   char b[128];
-  snprintf(b, sizeof b, "%d%d%d%d%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic, s.jumps);
+  snprintf(b, sizeof b, "%d%d%d%d%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic, s.jumps,
+           e->clen_min, e->nch_max);
   return b;
 }
 
@@ -477,6 +481,7 @@ int rd_engine_view(rd_engine* e, int diode, const DiodeParams** P, const DiodeDy
 }
 
 int rd_engine_repack(rd_engine* e) { return repack(e); }
+int rd_engine_chunk_rule(rd_engine* e) { return rd_chunk_rule(e->clen_min, e->nch_max); }
 
 // ---- C ABI ----------------------------------------------------------------------------
 extern "C" {
@@ -490,6 +495,9 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
     return fail(RD_ERR_INVALID, "max_diodes and particle_capacity must be positive");
   if (cfg->precision != RD_PREC_FP64 && cfg->precision != RD_PREC_FP32C)
     return fail(RD_ERR_INVALID, "unknown precision");
+  if (!valid_chunking(cfg->chunk_min > 0 ? cfg->chunk_min : RD_CLEN_MIN,
+                      cfg->chunk_count_max > 0 ? cfg->chunk_count_max : RD_NCH_MAX))
+    return fail(RD_ERR_INVALID, "chunk_min must be a multiple of 128 in [128, 65536], chunk_count_max in [1, 32]");
   rd_engine* e = new rd_engine();
   e->cfg = *cfg;
   int rc = RD_OK;
@@ -501,6 +509,8 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   if (ce != cudaSuccess) return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
   e->sms = prop.multiProcessorCount;
   e->grid = cfg->grid_blocks > 0 ? cfg->grid_blocks : 0;   // 0: occupancy-based per kernel
+  e->clen_min = cfg->chunk_min > 0 ? cfg->chunk_min : RD_CLEN_MIN;
+  e->nch_max = cfg->chunk_count_max > 0 ? cfg->chunk_count_max : RD_NCH_MAX;
   if ((ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess)
     return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
   cudaEventCreate(&e->ev0);
@@ -527,11 +537,14 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
       e->dalloc(&e->qfy, qcap) || e->dalloc(&e->qpp, qcap) || e->dalloc(&e->cs.gx, chcap) || e->dalloc(&e->cs.gy, chcap) ||
       e->dalloc(&e->cs.fx, chcap) || e->dalloc(&e->cs.fy, chcap) || e->dalloc(&e->cs.fsup, chcap) ||
       e->dalloc(&e->cs.fgx, chcap) || e->dalloc(&e->cs.fgy, chcap) ||
+      e->dalloc(&e->cs.pph, chcap) || e->dalloc(&e->cs.pih, chcap) ||
       e->dalloc(&e->d_choff, S) || e->dalloc(&e->d_qoff, S) ||
       e->dalloc(&e->d_npts, S) || e->dalloc(&e->d_zero_off, S) ||
       e->dalloc(&e->partial, (size_t)e->max_items * 3 * RD_ITILE) ||
       e->dalloc(&e->tickets, e->max_items) || e->dalloc(&e->kept, e->max_items) ||
       e->dalloc(&e->item_queue, 8) ||
+      (cfg->event_capacity > 0 && (e->dalloc(&e->evlog.buf, (size_t)cfg->event_capacity) ||
+                                   e->dalloc(&e->evlog.count, 1))) ||
       e->dalloc(&e->ramo, cap) || e->dalloc(&e->life, (size_t)S * RD_MAX_LIFE) ||
       e->dalloc(&e->d_step, 1))
     return bail(fail(RD_ERR_NOMEM, "device allocation failed"));
@@ -547,6 +560,8 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   cudaMemsetAsync(e->dD, 0, sizeof(DiodeDyn) * S, e->st);
   cudaMemsetAsync(e->tickets, 0, sizeof(int) * e->max_items, e->st);
   cudaMemsetAsync(e->item_queue, 0, sizeof(int) * 8, e->st);
+  if (e->evlog.count) cudaMemsetAsync(e->evlog.count, 0, sizeof(int), e->st);
+  e->evlog.cap = cfg->event_capacity > 0 ? cfg->event_capacity : 0;
   cudaMemsetAsync(e->life, 0, sizeof(int) * (size_t)S * RD_MAX_LIFE, e->st);
   cudaMemsetAsync(e->d_npts, 0, sizeof(int) * S, e->st);
   cudaMemsetAsync(e->d_zero_off, 0, sizeof(int) * S, e->st);
@@ -961,6 +976,127 @@ int rd_time_field_at(rd_engine* e, int d, int M, const double* pos, int reps, do
   return RD_OK;
 }
 
+// ---- event log -------------------------------------------------------------------------
+int rd_events_take(rd_engine* e, int cap, rd_event* out, int* n_out, long long* n_lost) {
+  if (!e || !n_out || !n_lost || cap < 0 || (cap > 0 && !out)) return fail(RD_ERR_INVALID, "bad argument");
+  *n_out = 0;
+  *n_lost = 0;
+  if (!e->evlog.buf) return fail(RD_ERR_STATE, "the engine has no event log (event_capacity = 0)");
+  int count = 0;
+  CK(cudaMemcpyAsync(&count, e->evlog.count, sizeof(int), cudaMemcpyDeviceToHost, e->st));
+  CK(cudaStreamSynchronize(e->st));
+  const int n = std::min(count, e->evlog.cap);
+  std::vector<rd_event> recs((size_t)n);
+  if (n > 0) CK(cudaMemcpyAsync(recs.data(), e->evlog.buf, sizeof(rd_event) * n, cudaMemcpyDeviceToHost, e->st));
+  CK(cudaMemsetAsync(e->evlog.count, 0, sizeof(int), e->st));
+  CK(cudaStreamSynchronize(e->st));
+  std::sort(recs.begin(), recs.end(), [](const rd_event& a, const rd_event& b) {
+    if (a.diode != b.diode) return a.diode < b.diode;
+    if (a.kind != b.kind) return a.kind < b.kind;
+    return a.id < b.id;
+  });
+  const int m = std::min(n, cap);
+  std::copy(recs.begin(), recs.begin() + m, out);
+  *n_out = m;
+  *n_lost = (long long)(count - n) + (n - m);
+  return RD_OK;
+}
+
+// ---- autotuner ------------------------------------------------------------------------
+// Device time of the pair-sum passes of one step under the current chunking:
+// the force pass and, if planar diodes emit, a dry MH jump pass (field at
+// every chain's current point; nothing written but scratch), each averaged
+// over `reps` launches after one warm-up.
+static int time_pair_passes(rd_engine* e, int reps, double* force_ms, double* mh_ms) {
+  Sig s = signature(e);
+  float ms = 0.f;
+  int rc = launch_force(e);
+  if (rc) return rc;
+  CK(cudaEventRecord(e->ev0, e->st));
+  for (int r = 0; r < reps; ++r)
+    if ((rc = launch_force(e))) return rc;
+  CK(cudaEventRecord(e->ev1, e->st));
+  CK(cudaEventSynchronize(e->ev1));
+  CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+  *force_ms = ms / reps;
+  *mh_ms = 0.0;
+  if (s.emit_planar) {
+    const int prec = e->cfg.precision;
+    for (int r = -1; r < reps; ++r) {
+      if (r == 0) CK(cudaEventRecord(e->ev0, e->st));
+      CK(plan(e, PM_MH));
+      CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                           e->cs, e->d_choff, e->wtab, e->d_step, -1, e->partial, e->tickets, e->kscale,
+                           e->item_queue));
+    }
+    CK(cudaEventRecord(e->ev1, e->st));
+    CK(cudaEventSynchronize(e->ev1));
+    CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+    *mh_ms = ms / reps;
+  }
+  return RD_OK;
+}
+
+int rd_autotune(rd_engine* e, rd_tune_result* out) {
+  if (!e || !out) return fail(RD_ERR_INVALID, "null argument");
+  *out = rd_tune_result{};
+  out->chunk_min = e->clen_min;
+  out->chunk_count_max = e->nch_max;
+  if (e->nslots_hw() == 0) return RD_OK;
+  int rc = repack(e);
+  if (rc) return rc;
+  // the force passes overwrite the current accelerations: keep them in the compaction pool
+  const size_t bytes = sizeof(double) * (size_t)e->cfg.particle_capacity;
+  CK(cudaMemcpyAsync(e->tmp.ax, e->pool.ax, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaMemcpyAsync(e->tmp.ay, e->pool.ay, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaMemcpyAsync(e->tmp.az, e->pool.az, bytes, cudaMemcpyDeviceToDevice, e->st));
+  const int jumps = std::max(signature(e).jumps, 1);
+  const int saved_min = e->clen_min, saved_max = e->nch_max;
+  double best = 1e300, at_default = 0.0;
+  int best_min = saved_min, best_max = saved_max;
+  const int mins[] = {512, 1024, 2048};
+  const int maxs[] = {8, 16, 32};
+  for (int a : mins)
+    for (int b : maxs) {
+      e->clen_min = a;
+      e->nch_max = b;
+      double fms = 0.0, mms = 0.0;
+      if ((rc = time_pair_passes(e, 2, &fms, &mms))) { e->clen_min = saved_min; e->nch_max = saved_max; return rc; }
+      const double est = fms + jumps * mms;
+      if (a == RD_CLEN_MIN && b == RD_NCH_MAX) at_default = est;
+      if (est < best) { best = est; best_min = a; best_max = b; }
+      out->candidates++;
+    }
+  e->clen_min = best_min;
+  e->nch_max = best_max;
+  CK(cudaMemcpyAsync(e->pool.ax, e->tmp.ax, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaMemcpyAsync(e->pool.ay, e->tmp.ay, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaMemcpyAsync(e->pool.az, e->tmp.az, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaStreamSynchronize(e->st));
+  out->chunk_min = best_min;
+  out->chunk_count_max = best_max;
+  out->ms_default = at_default;
+  out->ms_chosen = best;
+  return RD_OK;   // the step graph is rebuilt at the next step (its signature holds the chunking)
+}
+
+int rd_set_chunking(rd_engine* e, int chunk_min, int chunk_count_max) {
+  if (!e) return fail(RD_ERR_INVALID, "null engine");
+  const int a = chunk_min > 0 ? chunk_min : RD_CLEN_MIN, b = chunk_count_max > 0 ? chunk_count_max : RD_NCH_MAX;
+  if (!valid_chunking(a, b))
+    return fail(RD_ERR_INVALID, "chunk_min must be a multiple of 128 in [128, 65536], chunk_count_max in [1, 32]");
+  e->clen_min = a;
+  e->nch_max = b;
+  return RD_OK;
+}
+
+int rd_get_chunking(rd_engine* e, int* chunk_min, int* chunk_count_max) {
+  if (!e || !chunk_min || !chunk_count_max) return fail(RD_ERR_INVALID, "null argument");
+  *chunk_min = e->clen_min;
+  *chunk_count_max = e->nch_max;
+  return RD_OK;
+}
+
 int rd_mark_remove(rd_engine* e, int d, int i, int why) {
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (why != RD_REMOVE_TOP && why != RD_REMOVE_BOT) return fail(RD_ERR_INVALID, "unknown removal flag");
@@ -1095,20 +1231,19 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
       out->mh_pair_evals += (long long)dyn[d].chains * dyn[d].n * sl.p.mh_jumps;
     }
     CK(plan(e, PM_MH));
-    if (s.emit_planar)
-      CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                           e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue));
+    const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
+    CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                         e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue));
     CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                          e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
     CK(cudaEventRecord(ev[2], e->st));
-    const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
     for (int it = 1; it <= s.jumps; ++it)
       CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                            e->cs, e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale,
                            e->item_queue));
     out->mh_jump_launches = s.jumps;
     CK(cudaEventRecord(ev[3], e->st));
-    CK(rd_launch_emit(S, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step));
+    CK(rd_launch_emit(S, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step, e->evlog));
   } else {
     CK(cudaEventRecord(ev[1], e->st));
     CK(cudaEventRecord(ev[2], e->st));
@@ -1116,7 +1251,8 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
   }
   CK(cudaEventRecord(ev[4], e->st));
   CK(plan(e, PM_PART));
-  CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART]));
+  CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->evlog,
+                        e->d_step));
   CK(cudaEventRecord(ev[5], e->st));
   int rc = launch_force(e);
   if (rc) return rc;

@@ -533,7 +533,9 @@ __global__ void k_supply_reduce(const DiodeParams* __restrict__ P, DiodeDyn* __r
 // ---- MH chain initialisation: one warp per chain --------------------------------------
 // Uniform proposals until the field is favourable (F < 0), at most
 // init_rounds rounds (10000 in the reference, :1321-1364 and
-// mod_emission_tip.f90:1292-1318).
+// mod_emission_tip.f90:1292-1318).  Round 0 of every chain runs tiled in the
+// jump kernels (it_idx 0); this kernel continues from round 1 for the chains
+// whose first point was unfavourable.
 template <int PREC>
 __device__ double warp_field_planar_z0(const DiodeParams& p, const Pool& pool, int n, double px,
                                        double py, double kscale) {
@@ -631,11 +633,10 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
     const DiodeParams& p = P[d];
     const int n = plan[d].n_j, k = ch_off[d] + c;
     const uint32_t step = (uint32_t)(*step_ptr - Dy[d].step_offset);
-    const bool planar = p.geometry != RD_G_TIP;
-    if (planar && cs.ok[k]) continue;   // round 0 made it (k_mh_jump_planar, it_idx 0)
+    if (cs.ok[k]) continue;   // round 0 made it (k_mh_jump_planar / k_mh_jump_tip, it_idx 0)
     int ok = 0;
     double F = 1.0, sup = -1.79769313486231570e308, X = 0, Y = 0, Z = 0, xi = 1.0, ph_ = 0.0;
-    for (int r = planar ? 1 : 0; r < p.init_rounds && !ok; ++r) {
+    for (int r = 1; r < p.init_rounds && !ok; ++r) {
       double u1, u2;
       rng2(p.seed, (uint32_t)c, (uint32_t)r, step, RNG_INIT, &u1, &u2);
       if (p.geometry == RD_G_TIP) {
@@ -787,7 +788,9 @@ __device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState&
 // One Metropolis-Hastings jump iteration of the planar chains (it_idx >= 1),
 // or round 0 of their uniform start (it_idx == 0: every chain of the step
 // evaluates its first uniform draw here, tiled like a jump; the chains that
-// drew an unfavourable point continue in k_mh_init from round 1).  The
+// drew an unfavourable point continue in k_mh_init from round 1), or a dry
+// pass for the autotuner (it_idx < 0: the field at every chain's current
+// point, nothing written but the scratch).  The
 // proposal is the stored Gaussian pair (box_muller, src/mod_global.F90:
 // 578-595) times the step size of this iteration (fixed during the warm-up,
 // MH_std afterwards, :1373-1378) plus the current position, reflected at the
@@ -809,6 +812,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
   const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   const bool init = it_idx == 0;
+  const bool dry = it_idx < 0;   // timing pass: field at the current points, nothing written
   for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
@@ -835,6 +839,8 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
           rng2f(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
           x = fminf(fmaf(u1, p.em_wx, -hx), hx);
           yv = fminf(fmaf(u2, p.em_wy, -hy), hy);
+        } else if (dry && ok[q]) {
+          x = cs.fx[kk[q]]; yv = cs.fy[kk[q]];
         } else if (ok[q]) {    // Gaussian step, reflected at the edges (:1466-1516)
           const int k = kk[q];
           x = fmaf(cs.fgx[k], sx, cs.fx[k]);
@@ -858,6 +864,8 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
           rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
           wx[q] = u1 * p.em_Lx + p.em_x0;
           wy[q] = u2 * p.em_Ly + p.em_y0;
+        } else if (dry && ok[q]) {
+          wx[q] = cs.x[kk[q]]; wy[q] = cs.y[kk[q]];
         } else if (ok[q]) {
           const int k = kk[q];
           double x = cs.gx[k] * sx + cs.x[k], yv = cs.gy[k] * sy + cs.y[k];
@@ -889,6 +897,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
       }
     }
     // epilogue of the completed tile
+    if (dry) continue;
     if (init) {   // a favourable start (F < 0) makes the chain; the others go to k_mh_init
       for (int q = 0; q < CPT; ++q) {
         if (!ok[q]) continue;
@@ -937,61 +946,142 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
   queue_leave(queue, total);
 }
 
+// Field sums of one j-tile at CPT tip proposals (upper role: the point's own
+// apex-sphere image, tip_tile_f32<T_UPPER>); one shared load feeds all of the
+// thread's points.  The tip image term of the reference carries an extra
+// factor K = q0 / (4 pi eps0) (acc_tip_ic_force.inc:17-22):
+//   E = sum_j q_j [ d/|d|^3 + K (d/|d|^3 - c e/|e|^3) ] = (1 + K) D - K S,
+// D = sum q d/|d|^3, S = sum q c e/|e|^3; the two sums are kept apart here
+// (td, te) and combined in FP64 by the caller, so the K-scaled image part is
+// not lost below the FP32 resolution of the direct part.  The proposals sit
+// on the FP32 nm grid (k_mh_propose), so d = (p - x_hi) - x_lo.  S is formed
+// from high words only (e = image_hi - x_hi): its relative error, ~1e-5 for
+// the nearest charges, is ~1e-14 of the field once scaled by K.
+template <int CPT>
+__device__ __forceinline__ void tip_point_tiles_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
+                                                    int kmax, const float4* ih, const float4* iih, int ic,
+                                                    float (*td)[3], float (*te)[3]) {
+  float dx_[CPT], dy_[CPT], dz_[CPT], ex_[CPT], ey_[CPT], ez_[CPT];
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) dx_[q] = dy_[q] = dz_[q] = ex_[q] = ey_[q] = ez_[q] = 0.f;
+  for (int k = 0; k < kmax; ++k) {
+    const float4 h = sh[k], l = sl[k];
+    const float qj = h.w;
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) {
+      const float dx = (ih[q].x - h.x) - l.x;
+      const float dy = (ih[q].y - h.y) - l.y;
+      const float dz = (ih[q].z - h.z) - l.z;
+      const float inv = rsqrtf(fmaf(dz, dz, fmaf(dx, dx, fmaf(dy, dy, 1e-20f))));
+      const float s = qj * ((inv * inv) * inv);
+      dx_[q] = fmaf(s, dx, dx_[q]);
+      dy_[q] = fmaf(s, dy, dy_[q]);
+      dz_[q] = fmaf(s, dz, dz_[q]);
+      if (ic) {   // high words only: this sum enters scaled by K ~ 1e-9 (see above)
+        const float ex = iih[q].x - h.x;
+        const float ey = iih[q].y - h.y;
+        const float ez = iih[q].z - h.z;
+        const float re = rsqrtf(fmaf(ez, ez, fmaf(ex, ex, fmaf(ey, ey, 1e-20f))));
+        const float se = (qj * iih[q].w) * ((re * re) * re);
+        ex_[q] = fmaf(se, ex, ex_[q]);
+        ey_[q] = fmaf(se, ey, ey_[q]);
+        ez_[q] = fmaf(se, ez, ez_[q]);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    td[q][0] += dx_[q]; td[q][1] += dy_[q]; td[q][2] += dz_[q];
+    te[q][0] += ex_[q]; te[q][1] += ey_[q]; te[q][2] += ez_[q];
+  }
+}
+
+// One Metropolis-Hastings jump iteration of the tip chains (it_idx >= 1), or
+// round 0 of their uniform start (it_idx == 0; the chains whose first point
+// sees F >= 0 continue in k_mh_init).  The proposals come from k_mh_propose,
+// already packed into the FP32 frame.  The field at the proposal (all three
+// components: direct and sphere-image terms) is summed over the item's
+// j-chunk; the CTA completing a tile projects the total field (plus the
+// hyperboloid vacuum field) on the surface normal and runs the accept /
+// reject test (Metro_algo_tip_v3, src/mod_emission_tip.f90:1351-1389).
+// FP32: 64 threads, two chains each; FP64: 128 threads, one chain each.
 template <int PREC>
 __global__ void __launch_bounds__(RD_ITILE)
 k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
               const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
               ChainState cs, const int* __restrict__ ch_off, const int* __restrict__ step_ptr,
-              int it_idx, double* __restrict__ partial, int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
+              int it_idx, double* __restrict__ partial, int* __restrict__ tickets, double kscale,
+              int* __restrict__ queue) {
   __shared__ int s_item;
-  __shared__ float4 sh[RD_TILE], sl[RD_TILE], sih[RD_TILE], sil[RD_TILE];
-  __shared__ rd_d4 sj[RD_TILE];
   __shared__ int red_i[2 * RD_ITILE];
+  constexpr int CPT = PREC == 1 ? 2 : 1;
+  const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
+  const bool init = it_idx == 0;
   for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     if (p.geometry != RD_G_TIP || it_idx > p.mh_jumps) continue;
     DiodeDyn& y = Dy[it.d];
     const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
-    const int M = plan[it.d].n_i, c = it.i0 + tid, k = ch_off[it.d] + c;
-    const bool valid = c < M;
-    const int ok = valid ? cs.ok[k] : 0;
+    const int M = plan[it.d].n_i;
     const int ndim_first = (int)nint_d(p.mh_jumps * 0.25);
-    // proposal from k_mh_propose
-    double nxi = 1.5, nph = 0.0, X, Y, Z;
-    int inside = 0;
-    if (ok) {
-      nxi = cs.px[k]; nph = cs.py[k]; inside = cs.prop_ok[k];
-      X = cs.pxx[k]; Y = cs.pyy[k]; Z = cs.pzz[k];
-    } else {
-      tip_xyz(p, 1.5, p.eta_1, 0.0, &X, &Y, &Z);
-    }
-    // field at the proposal (general form, all three components)
-    double fx = 0, fy = 0, fz = 0;
     const int off = p.off;
-    if (PREC == 1) {
-      float4 ih, il, iih, iil;
-      point_pack(p, X, Y, Z, ih, il, iih, iil);
-      F32Acc acc;
-      acc.zero();
+    int ok[CPT], kk[CPT];
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) {
+      const int c = it.i0 + tid + q * nt;
+      kk[q] = ch_off[it.d] + c;
+      ok[q] = (c < M) ? (init ? 1 : cs.ok[kk[q]]) : 0;
+    }
+    double f3[CPT][3];
+    if constexpr (PREC == 1) {
+      __shared__ float4 sh[RD_TILE], sl[RD_TILE];
+      float4 ih[CPT], iih[CPT];
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) {
+        if (ok[q]) {
+          const int k = kk[q];
+          ih[q] = cs.pph[k]; iih[q] = cs.pih[k];
+        } else {   // idle lane: a point far above the tip, no image
+          ih[q] = make_float4(0.f, 0.f, 1.0e4f, 1.f);
+          iih[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      }
+      F32Acc accd[CPT];        // direct part: two-sum across tiles
+      float acce[CPT][3];      // image part (scaled by K ~ 1e-9 at the end): plain float sums
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) { accd[q].zero(); acce[q][0] = acce[q][1] = acce[q][2] = 0.f; }
       for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
         __syncthreads();
-        int j = jt + tid;
-        if (j < it.j1) {
-          sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j];
-          sih[tid] = pool.ip_hi[off + j]; sil[tid] = pool.ip_lo[off + j];
+        for (int q = tid; q < RD_TILE; q += nt) {
+          const int j = jt + q;
+          if (j < it.j1) { sh[q] = pool.pk_hi[off + j]; sl[q] = pool.pk_lo[off + j]; }
         }
         __syncthreads();
-        float tx = 0.f, ty = 0.f, tz = 0.f;
-        tip_tile_f32<T_UPPER>(sh, sl, sih, sil, min(RD_TILE, it.j1 - jt), ih, il, iih, iil, -1,
-                              p.image_charge, (float)c_k.tip_K, tx, ty, tz);
-        acc.add(tx, ty, tz);
+        float td[CPT][3], te[CPT][3];
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) td[q][0] = td[q][1] = td[q][2] = te[q][0] = te[q][1] = te[q][2] = 0.f;
+        tip_point_tiles_f32<CPT>(sh, sl, min(RD_TILE, it.j1 - jt), ih, iih, p.image_charge, td, te);
+#pragma unroll
+        for (int q = 0; q < CPT; ++q) {
+          accd[q].add(td[q][0], td[q][1], td[q][2]);
+          acce[q][0] += te[q][0]; acce[q][1] += te[q][1]; acce[q][2] += te[q][2];
+        }
       }
-      fx = ((double)acc.hx + (double)acc.lx) * kscale;
-      fy = ((double)acc.hy + (double)acc.ly) * kscale;
-      fz = ((double)acc.hz + (double)acc.lz) * kscale;
+      const double K = c_k.tip_K, cd = p.image_charge ? (1.0 + K) * kscale : kscale, ce = K * kscale;
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) {
+        f3[q][0] = ((double)accd[q].hx + (double)accd[q].lx) * cd - (double)acce[q][0] * ce;
+        f3[q][1] = ((double)accd[q].hy + (double)accd[q].ly) * cd - (double)acce[q][1] * ce;
+        f3[q][2] = ((double)accd[q].hz + (double)accd[q].lz) * cd - (double)acce[q][2] * ce;
+      }
     } else {
+      __shared__ rd_d4 sj[RD_TILE];
+      double X, Y, Z;
+      if (ok[0]) { X = cs.pxx[kk[0]]; Y = cs.pyy[kk[0]]; Z = cs.pzz[kk[0]]; }
+      else tip_xyz(p, 1.5, p.eta_1, 0.0, &X, &Y, &Z);
+      double fx = 0, fy = 0, fz = 0;
       for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
         __syncthreads();
         int j = jt + tid;
@@ -1000,61 +1090,83 @@ k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool
         tip_tile_f64<T_UPPER>(sj, min(RD_TILE, it.j1 - jt), X, Y, Z, c_k.div_fac_c, -1,
                               p.image_charge, p, c_k.L2, c_k.tip_K, fx, fy, fz);
       }
+      f3[0][0] = fx; f3[0][1] = fy; f3[0][2] = fz;
     }
     if (it.nch > 1) {
       double* pp = partial + (size_t)g * 3 * RD_ITILE;
-      pp[tid] = fx; pp[RD_ITILE + tid] = fy; pp[2 * RD_ITILE + tid] = fz;
+#pragma unroll
+      for (int q = 0; q < CPT; ++q)
+        for (int i = 0; i < 3; ++i) pp[i * RD_ITILE + tid + q * nt] = f3[q][i];
       if (!tile_ticket(tickets, it)) continue;
-      fx = fy = fz = 0.0;
-      for (int cc = 0; cc < it.nch; ++cc) {
-        const double* q = partial + (size_t)(it.base + cc) * 3 * RD_ITILE;
-        fx += __ldcg(q + tid); fy += __ldcg(q + RD_ITILE + tid); fz += __ldcg(q + 2 * RD_ITILE + tid);
-      }
+#pragma unroll
+      for (int q = 0; q < CPT; ++q)
+        for (int i = 0; i < 3; ++i) {
+          double s = 0.0;
+          for (int cc = 0; cc < it.nch; ++cc)
+            s += __ldcg(partial + (size_t)(it.base + cc) * 3 * RD_ITILE + i * RD_ITILE + tid + q * nt);
+          f3[q][i] = s;
+        }
     }
+    // epilogue of the completed tile: F = n . (E_vac + E_particles) at the proposal
     int a = 0, r = 0;
-    if (ok) {
-      if (!inside) {
-        r = 1;
-      } else {
+#pragma unroll
+    for (int q = 0; q < CPT; ++q) {
+      if (!ok[q]) continue;
+      const int c = it.i0 + tid + q * nt, k = kk[q];
+      const double X = cs.pxx[k], Y = cs.pyy[k], Z = cs.pzz[k], nxi = cs.px[k], nph = cs.py[k];
+      if (init) {   // a favourable start makes the chain; the others go to k_mh_init
         double ex, ey, ez, nx, ny, nz;
         tip_field_E(p, X, Y, Z, &ex, &ey, &ez);
-        ex += fx; ey += fy; ez += fz;
+        ex += f3[q][0]; ey += f3[q][1]; ez += f3[q][2];
         tip_normal(p, X, Y, &nx, &ny, &nz);
-        double F = (nx * ex + ny * ey) + nz * ez;
-        if (F >= 0.0) {
-          r = 1;
+        const double F = (nx * ex + ny * ey) + nz * ez;
+        if (F < 0.0 && p.init_rounds > 0) {
+          cs.ok[k] = 1; cs.x[k] = nxi; cs.y[k] = nph; cs.F[k] = F; cs.sup[k] = tip_target_log(p, F, nxi);
+          cs.tx[k] = X; cs.ty[k] = Y; cs.tz[k] = Z;
         } else {
-          double sn = tip_target_log(p, F, nxi), sc = cs.sup[k];
-          bool take = sn >= sc;
-          if (!take) {
-            double u1, u2;
-            rng2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, &u1, &u2);
-            take = log(u1) <= sn - sc;
-          }
-          if (take) {
-            cs.x[k] = nxi; cs.y[k] = nph; cs.F[k] = F; cs.sup[k] = sn;
-            cs.tx[k] = X; cs.ty[k] = Y; cs.tz[k] = Z;
-            a = 1;
-          } else r = 1;
+          cs.ok[k] = 0;
         }
+        continue;
+      }
+      if (!cs.prop_ok[k]) { r += 1; continue; }
+      double ex, ey, ez, nx, ny, nz;
+      tip_field_E(p, X, Y, Z, &ex, &ey, &ez);
+      ex += f3[q][0]; ey += f3[q][1]; ez += f3[q][2];
+      tip_normal(p, X, Y, &nx, &ny, &nz);
+      const double F = (nx * ex + ny * ey) + nz * ez;
+      if (F >= 0.0) { r += 1; continue; }
+      const double sn = tip_target_log(p, F, nxi), sc = cs.sup[k];
+      bool take = sn >= sc;
+      if (!take) {
+        double u1, u2;
+        rng2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, &u1, &u2);
+        take = log(u1) <= sn - sc;
+      }
+      if (take) {
+        cs.x[k] = nxi; cs.y[k] = nph; cs.F[k] = F; cs.sup[k] = sn;
+        cs.tx[k] = X; cs.ty[k] = Y; cs.tz[k] = Z;
+        a += 1;
+      } else {
+        r += 1;
       }
     }
+    if (init) continue;
     mh_counts_and_update(p, y, plan[it.d].tiles, it_idx, ndim_first, a, r, red_i);
   }
   queue_leave(queue, total);
 }
 
-// ---- MH proposals: one thread per chain -------------------------------------------------
-// Planar: Gaussian step (box_muller) reflected at the emitter edges
-// (check_limits_metro_rec, src/mod_field_emission_v2.F90:1380-1393,
-// :1466-1516).  Tip: Gaussian step in (xi, phi), phi wrapped, xi reflected
-// once (Metro_algo_tip_v3, src/mod_emission_tip.f90:1334-1350).  The step
-// uses the fixed warm-up size for the first quarter of the jumps and MH_std
-// afterwards; MH_std was updated at the end of the previous iteration.
+// ---- tip MH proposals: one thread per chain ---------------------------------------------
+// Jump it >= 1: Gaussian step in (xi, phi), phi wrapped, xi reflected once
+// (Metro_algo_tip_v3, src/mod_emission_tip.f90:1334-1350); the step uses the
+// fixed warm-up size for the first quarter of the jumps and MH_std
+// afterwards (MH_std was updated at the end of the previous iteration).
+// it = 0: round 0 of the uniform start of every chain.  The proposal is also
+// packed into the FP32 frame here, once, for the field tiles of the jump.
 __global__ void k_mh_propose(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy,
                              const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
                              ChainState cs, const int* __restrict__ ch_off,
-                             const int* __restrict__ step_ptr, int it_idx) {
+                             const int* __restrict__ step_ptr, int it_idx, int f32_grid) {
   const int nd = ph->n_diodes;
   const int total = nd > 0 ? plan[nd - 1].pad0 + plan[nd - 1].n_i : 0;
   const double twopi = 2.0 * c_k.pi;
@@ -1065,35 +1177,41 @@ __global__ void k_mh_propose(const DiodeParams* __restrict__ P, const DiodeDyn* 
     const DiodeParams& p = P[d];
     if (p.geometry != RD_G_TIP || it_idx > p.mh_jumps) continue;
     const int k = ch_off[d] + c;
-    if (!cs.ok[k]) continue;
     const DiodeDyn& y = Dy[d];
     const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
-    const int ndim_first = (int)nint_d(p.mh_jumps * 0.25);
-    double g1, g2;
-    gauss2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, &g1, &g2);
-    if (p.geometry == RD_G_TIP) {
-      double sxi = (it_idx > ndim_first) ? (p.max_xi - 1.0) * y.MH_std : (p.max_xi - 1.0) * 0.10;
-      double sph = (it_idx > ndim_first) ? twopi * y.MH_std : twopi * 0.10;
-      double nxi = cs.x[k] + g1 * sxi;
-      double a = cs.y[k] + g2 * sph;
-      double nph = a - floor(a / twopi) * twopi;   // Fortran MODULO
+    double nxi, nph;
+    int inside = 1;
+    if (it_idx == 0) {   // round 0 of the uniform start (mod_emission_tip.f90:1292-1318)
+      double u1, u2;
+      rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+      nxi = 1.0 + (p.max_xi - 1.0) * u1;
+      nph = twopi * u2;
+    } else {             // Gaussian step in (xi, phi), xi reflected, phi wrapped (:1337-1365)
+      if (!cs.ok[k]) continue;
+      const int ndim_first = (int)nint_d(p.mh_jumps * 0.25);
+      double g1, g2;
+      gauss2(p.seed, (uint32_t)c, (uint32_t)it_idx, step, &g1, &g2);
+      const double sxi = (it_idx > ndim_first) ? (p.max_xi - 1.0) * y.MH_std : (p.max_xi - 1.0) * 0.10;
+      const double sph = (it_idx > ndim_first) ? twopi * y.MH_std : twopi * 0.10;
+      nxi = cs.x[k] + g1 * sxi;
+      const double a = cs.y[k] + g2 * sph;
+      nph = a - floor(a / twopi) * twopi;   // Fortran MODULO
       if (nxi > p.max_xi) nxi = 2.0 * p.max_xi - nxi;
       if (nxi < 1.0) nxi = 2.0 - nxi;
-      int inside = !(nxi < 1.0 || nxi > p.max_xi);
-      double X, Y, Z;
-      tip_xyz(p, inside ? nxi : 1.5, p.eta_1, nph, &X, &Y, &Z);
-      cs.px[k] = nxi; cs.py[k] = nph; cs.prop_ok[k] = inside;
-      cs.pxx[k] = X; cs.pyy[k] = Y; cs.pzz[k] = Z;
-    } else {
-      double sx = (it_idx > ndim_first) ? p.em_Lx * y.MH_std : p.em_Lx * 0.10;
-      double sy = (it_idx > ndim_first) ? p.em_Ly * y.MH_std : p.em_Ly * 0.10;
-      double wx = g1 * sx + cs.x[k];
-      double wy = g2 * sy + cs.y[k];
-      double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
-      if (wx > hx) wx = hx - (wx - hx); else if (wx < p.em_x0) wx = (p.em_x0 - wx) + p.em_x0;
-      if (wy > hy) wy = hy - (wy - hy); else if (wy < p.em_y0) wy = (p.em_y0 - wy) + p.em_y0;
-      cs.px[k] = wx; cs.py[k] = wy;
+      inside = !(nxi < 1.0 || nxi > p.max_xi);
     }
+    double X, Y, Z;
+    tip_xyz(p, inside ? nxi : 1.5, p.eta_1, nph, &X, &Y, &Z);
+    if (f32_grid) {   // FP32 form: the point at its FP32 nm coordinates (at most 6e-5 nm off the surface)
+      X = (double)(float)(X * 1.0e9) * 1.0e-9;
+      Y = (double)(float)(Y * 1.0e9) * 1.0e-9;
+      Z = (double)(float)(Z * 1.0e9) * 1.0e-9;
+    }
+    cs.px[k] = nxi; cs.py[k] = nph; cs.prop_ok[k] = inside;
+    cs.pxx[k] = X; cs.pyy[k] = Y; cs.pzz[k] = Z;
+    float4 ih, il, iih, iil;   // FP32 frame of the proposal, once per jump
+    point_pack(p, X, Y, Z, ih, il, iih, iil);
+    cs.pph[k] = ih; cs.pih[k] = iih;
   }
 }
 
@@ -1106,7 +1224,7 @@ __global__ void k_mh_propose(const DiodeParams* __restrict__ P, const DiodeDyn* 
 __global__ void __launch_bounds__(1024)
 k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, ChainState cs,
        const int* __restrict__ ch_off, const double* __restrict__ work,
-       const int* __restrict__ step_ptr) {
+       const int* __restrict__ step_ptr, EventLog ev) {
   __shared__ int warp_tot[32];
   __shared__ int s_base;
   const int d = blockIdx.x;
@@ -1178,6 +1296,7 @@ k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, 
         pool.step0[gi] = step;
         pool.section[gi] = sec;
         pool.mask[gi] = 1;
+        log_event(ev, X, Y, Z, 0.0, 0.0, 0.0, d, RD_EVENT_EMIT, sec, id0 + slot, 1, step);   // density_emit*.bin
       }
     }
     __syncthreads();
@@ -1251,8 +1370,9 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
     else k_mh_jump_planar<0><<<rd_grid(k_mh_jump_planar<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue);
   }
   if (geometry_mask & 2) {
-    k_mh_propose<<<rd_grid(k_mh_propose, 256, grid), 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx);
-    if (prec == 1) k_mh_jump_tip<1><<<rd_grid(k_mh_jump_tip<1>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale, queue + 2);
+    k_mh_propose<<<rd_grid(k_mh_propose, 256, grid), 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx,
+                                                                   prec == 1);
+    if (prec == 1) k_mh_jump_tip<1><<<rd_grid(k_mh_jump_tip<1>, 64, grid), 64, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale, queue + 2);
     else k_mh_jump_tip<0><<<rd_grid(k_mh_jump_tip<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale, queue + 2);
   }
   return cudaGetLastError();
@@ -1260,8 +1380,8 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
 
 cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                            const Pool& pool, const ChainState& cs, const int* ch_off,
-                           const double* work, const int* step_ptr) {
-  k_emit<<<nslots, 1024, 0, st>>>(P, Dy, pool, cs, ch_off, work, step_ptr);
+                           const double* work, const int* step_ptr, const EventLog& ev) {
+  k_emit<<<nslots, 1024, 0, st>>>(P, Dy, pool, cs, ch_off, work, step_ptr, ev);
   return cudaGetLastError();
 }
 

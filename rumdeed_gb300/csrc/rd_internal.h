@@ -16,6 +16,7 @@
 // counters) lives in device memory, so a captured step graph stays valid
 // while requests are admitted and retired.
 #pragma once
+#include "../../include/rumdeed_gpu.h"
 #include <stdint.h>
 
 #define RD_TILE 128           // particles per shared-memory j-tile
@@ -24,6 +25,8 @@
 // RD_NCH_MAX chunks per i-tile
 #define RD_CLEN_MIN 1024
 #define RD_NCH_MAX 32
+// the planner's chunk rule argument: clen_min | nch_max << 16
+inline int rd_chunk_rule(int clen_min, int nch_max) { return clen_min | (nch_max << 16); }
 #define RD_MAX_LIFE 1000
 #define RD_MAX_WORK 4096      // max checkerboard cells per diode (64x64)
 
@@ -98,6 +101,14 @@ struct Pool {
   float4 *zk_hi, *zk_lo;
 };
 
+// Device event log (rd_events_take): rd_event records appended by atomic
+// index; records past `cap` are only counted.
+struct EventLog {
+  rd_event* buf;   // null: no log
+  int* count;
+  int cap;
+};
+
 // One unit of a pair-sum: i-tile (or point block) x j-chunk of one diode.
 struct WorkItem {
   int diode;
@@ -122,4 +133,8 @@ struct ChainState {
   // FP32-compensated planar chains: position as FP32 nm offsets from the
   // emitter centre (the chain lives on that grid), log target, Gaussian pair
   float *fx, *fy, *fsup, *fgx, *fgy;
+  // FP32-compensated tip chains: the proposal packed once per jump for the
+  // field tiles (the point on the FP32 nm grid and the high words of its
+  // apex-sphere image)
+  float4 *pph, *pih;
 };

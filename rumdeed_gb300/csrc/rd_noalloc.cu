@@ -56,7 +56,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[RD_NOALLOC_SCRA
 
 // kernels from the other translation units
 cudaError_t rd_launch_plan(cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy, int nslots,
-                           int mode, int target_items, int max_items, const int* npts,
+                           int mode, int chunk_rule, int max_items, const int* npts,
                            PlanEntry* plan, PlanHeader* ph);
 cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st,
                                    const DiodeParams* P, const Pool& pool, const PlanEntry* plan,
@@ -67,6 +67,7 @@ int rd_engine_view(rd_engine* e, int diode, const DiodeParams** P, const DiodeDy
                    int* geometry, int* precision, int* grid, double* kscale, cudaStream_t* st,
                    int* device);
 int rd_engine_repack(rd_engine* e);
+int rd_engine_chunk_rule(rd_engine* e);
 int rd_set_error(int code, const char* msg);
 
 namespace {
@@ -144,7 +145,7 @@ extern "C" int rd_field_at_noalloc(rd_engine* e, int diode, int M, const double*
                                  px + RD_NOALLOC_MAX_POINTS, px + 2 * RD_NOALLOC_MAX_POINTS);
   cudaError_t ce = cudaGetLastError();
   if (ce == cudaSuccess)
-    ce = rd_launch_plan(st, P, Dy, 1, /*PM_FIELD*/ 2, 1, NA_MAX_ITEMS, ints, plan, ph);
+    ce = rd_launch_plan(st, P, Dy, 1, /*PM_FIELD*/ 2, rd_engine_chunk_rule(e), NA_MAX_ITEMS, ints, plan, ph);
   PointSet pts{px, px + RD_NOALLOC_MAX_POINTS, px + 2 * RD_NOALLOC_MAX_POINTS,
                fx, fx + RD_NOALLOC_MAX_POINTS, fx + 2 * RD_NOALLOC_MAX_POINTS, ints + 1};
   if (ce == cudaSuccess)

@@ -24,7 +24,7 @@ enum { PM_FORCE_PLANAR = 0, PM_FORCE_TIP = 1, PM_FIELD = 2, PM_SUPPLY_PLANAR = 3
 namespace {
 
 __device__ __forceinline__ void mark_remove(const DiodeParams& p, DiodeDyn& y, Pool& pool, int i,
-                                            int gi, int why) {
+                                            int gi, int why, const EventLog& ev, int d, int step) {
   if (!pool.mask[gi]) return;
   pool.mask[gi] = 0;
   pool.q[gi] = 0.0;   // a marked particle no longer acts on others (:206-207)
@@ -33,6 +33,9 @@ __device__ __forceinline__ void mark_remove(const DiodeParams& p, DiodeDyn& y, P
   if (pool.species[gi] == 1) {
     if (why == 1) atomicAdd(&y.n_remove_top, 1);
     else atomicAdd(&y.n_remove_bot, 1);
+    // density_absorb_{top,bot}.bin record (:241-257)
+    log_event(ev, pool.x[gi], pool.y[gi], pool.z[gi], pool.vx[gi], pool.vy[gi], pool.vz[gi], d,
+              why == 1 ? RD_EVENT_ABSORB_TOP : RD_EVENT_ABSORB_BOT, pool.section[gi], pool.id[gi], 1, step);
   }
 }
 
@@ -81,19 +84,20 @@ __device__ __forceinline__ int plan_ni(const DiodeParams& p, const DiodeDyn& y, 
 }
 
 // Tiles and j-chunking of one diode.  The chunk length depends only on the
-// diode's own counts (at least RD_CLEN_MIN particles, at most RD_NCH_MAX
-// chunks per tile), so the summation order -- and therefore every result --
+// diode's own counts and the engine's chunk rule (at least clen_min
+// particles, at most nch_max chunks per tile; RD_CLEN_MIN / RD_NCH_MAX by
+// default), so the summation order -- and therefore every result --
 // is the same whether a diode runs alone or among other diodes.  Chunks of
 // at most ~1024 particles also bound the cost of one work item, so the last
 // items of a launch end soon after the others.
-__device__ __forceinline__ void plan_split(int ni, int nj, int tsize, bool pair, int grow,
-                                           int* tiles, int* nch, int* clen) {
+__device__ __forceinline__ void plan_split(int ni, int nj, int tsize, bool pair, int grow, int clen_min,
+                                           int nch_max, int* tiles, int* nch, int* clen) {
   *tiles = (ni + tsize - 1) / tsize;
   *nch = 1;
   *clen = RD_TILE;
   if (pair && *tiles > 0) {
-    int c = (nj + RD_NCH_MAX - 1) / RD_NCH_MAX;
-    if (c < RD_CLEN_MIN) c = RD_CLEN_MIN;
+    int c = (nj + nch_max - 1) / nch_max;
+    if (c < clen_min) c = clen_min;
     c = ((c + RD_TILE - 1) / RD_TILE) * RD_TILE;
     c <<= grow;   // only if the scratch bound is ever hit (never by construction)
     *clen = c;
@@ -103,7 +107,7 @@ __device__ __forceinline__ void plan_split(int ni, int nj, int tsize, bool pair,
 
 __global__ void __launch_bounds__(1024)
 k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int nslots, int mode,
-       int target_items, int max_items, const int* __restrict__ npts, PlanEntry* __restrict__ plan,
+       int chunk_rule, int max_items, const int* __restrict__ npts, PlanEntry* __restrict__ plan,
        PlanHeader* __restrict__ ph) {
   __shared__ double red[1024];
   __shared__ int s_items[32], s_chains[32];
@@ -111,6 +115,7 @@ k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int n
   const int tid = threadIdx.x;
   const int tsize = (mode == PM_PART1024) ? 1024 : RD_ITILE;
   const bool pair = (mode <= PM_MH);
+  const int clen_min = chunk_rule & 0xffff, nch_max = chunk_rule >> 16;   // see rd_chunk_rule
   // grow the chunk length only if the items would not fit the scratch
   __shared__ int s_grow;
   if (tid == 0) s_grow = 0;
@@ -121,7 +126,8 @@ k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int n
     for (int d = tid; d < nslots; d += blockDim.x) {
       if (!P[d].active) continue;
       int tiles, nch, clen;
-      plan_split(plan_ni(P[d], Dy[d], mode, npts, d), Dy[d].n, tsize, pair, grow, &tiles, &nch, &clen);
+      plan_split(plan_ni(P[d], Dy[d], mode, npts, d), Dy[d].n, tsize, pair, grow, clen_min, nch_max, &tiles,
+                 &nch, &clen);
       cnt += (double)tiles * nch;
     }
     red[tid] = cnt;
@@ -147,7 +153,7 @@ k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int n
       nj = Dy[d].n;
       ni = plan_ni(P[d], Dy[d], mode, npts, d);
       if (mode == PM_MH) chains = ni;
-      plan_split(ni, nj, tsize, pair, grow, &tiles, &nch, &clen);
+      plan_split(ni, nj, tsize, pair, grow, clen_min, nch_max, &tiles, &nch, &clen);
       items = tiles * nch;
     }
     int lane = tid & 31, w = tid >> 5;
@@ -200,7 +206,8 @@ k_pack(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __restrict
 
 __global__ void __launch_bounds__(RD_ITILE)
 k_position(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
-           const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph) {
+           const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph, EventLog ev,
+           const int* __restrict__ step_ptr) {
   for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
     int d, i;
     if (!part_index(plan, ph, g, &d, &i)) continue;
@@ -218,9 +225,10 @@ k_position(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool po
       pool.bx[gi] = ax; pool.by[gi] = ay; pool.bz[gi] = az;
       pool.ax[gi] = 0.0; pool.ay[gi] = 0.0; pool.az[gi] = 0.0;
       DiodeDyn& yy = Dy[d];
-      if (z < 0.0) mark_remove(p, yy, pool, i, gi, 2);
-      else if (z > p.d) mark_remove(p, yy, pool, i, gi, 1);
-      if (p.geometry == RD_G_TIP && tip_eta(p, x, y, z) < p.eta_1) mark_remove(p, yy, pool, i, gi, 2);
+      const int step = *step_ptr - yy.step_offset;
+      if (z < 0.0) mark_remove(p, yy, pool, i, gi, 2, ev, d, step);
+      else if (z > p.d) mark_remove(p, yy, pool, i, gi, 1, ev, d, step);
+      if (p.geometry == RD_G_TIP && tip_eta(p, x, y, z) < p.eta_1) mark_remove(p, yy, pool, i, gi, 2, ev, d, step);
     }
     pack_one(p, pool, gi);
   }
@@ -396,9 +404,9 @@ __global__ void k_step_inc(int* step_ptr) { *step_ptr += 1; }
 
 // ---- launch wrappers ------------------------------------------------------------------
 cudaError_t rd_launch_plan(cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy, int nslots,
-                           int mode, int target_items, int max_items, const int* npts,
+                           int mode, int chunk_rule, int max_items, const int* npts,
                            PlanEntry* plan, PlanHeader* ph) {
-  k_plan<<<1, 1024, 0, st>>>(P, Dy, nslots, mode, target_items, max_items, npts, plan, ph);
+  k_plan<<<1, 1024, 0, st>>>(P, Dy, nslots, mode, chunk_rule, max_items, npts, plan, ph);
   return cudaGetLastError();
 }
 cudaError_t rd_launch_pack(int grid, cudaStream_t st, const DiodeParams* P, const Pool& pool,
@@ -407,8 +415,9 @@ cudaError_t rd_launch_pack(int grid, cudaStream_t st, const DiodeParams* P, cons
   return cudaGetLastError();
 }
 cudaError_t rd_launch_position(int grid, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
-                               const Pool& pool, const PlanEntry* plan, const PlanHeader* ph) {
-  k_position<<<rd_grid(k_position, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph);
+                               const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
+                               const EventLog& ev, const int* step_ptr) {
+  k_position<<<rd_grid(k_position, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, ev, step_ptr);
   return cudaGetLastError();
 }
 cudaError_t rd_launch_velocity(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
@@ -482,7 +491,7 @@ __global__ void k_add_finish(const DiodeParams* __restrict__ P, DiodeDyn* __rest
 __global__ void k_mark(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, int d,
                        int i, int why) {
   if (i < Dy[d].n) {
-    mark_remove(P[d], Dy[d], pool, i, P[d].off + i, why);
+    mark_remove(P[d], Dy[d], pool, i, P[d].off + i, why, EventLog{nullptr, nullptr, 0}, d, 0);
     pack_one(P[d], pool, P[d].off + i);
   }
 }

@@ -9,7 +9,9 @@
 // per-step records to out/emitted.dt (src/mod_field_emission_v2.F90:202-204),
 // out/absorbed{,_top,_bot}.dt (src/mod_pair.F90:789-804) and
 // out/ramo_current.dt (src/mod_pair.F90:811-835) with the reference's Fortran
-// edit descriptors.
+// edit descriptors, and the per-event binary files out/density_emit.bin,
+// out/density_emit_elec.bin (src/mod_pair.F90:89-123) and
+// out/density_absorb_{top,bot}.bin (:241-257) from the engine's event log.
 //
 // Supported decks: EMISSION_MODE = 10 (planar field emission, one
 // rectangular emitter, EMITTERS_TYPE 2) and EMISSION_MODE = 3 (hyperboloid
@@ -259,6 +261,7 @@ int main(int argc, char** argv) {
   ec.particle_capacity = dc.capacity + 64;
   ec.chain_capacity = dc.capacity + 64;
   ec.quad_capacity = 16384;
+  ec.event_capacity = 4 * dc.capacity + 1024;   // emission and absorption records of one step
   rd_engine* e = nullptr;
   check(rd_engine_create(&ec, &e), "rd_engine_create");
   int diode = -1;
@@ -270,16 +273,51 @@ int main(int argc, char** argv) {
   FILE* f_top = std::fopen("out/absorbed_top.dt", "w");
   FILE* f_bot = std::fopen("out/absorbed_bot.dt", "w");
   FILE* f_ramo = std::fopen("out/ramo_current.dt", "w");
-  if (!f_emit || !f_abs || !f_top || !f_bot || !f_ramo) {
+  // binary event files (Fortran stream access: raw values, no record markers)
+  FILE* b_emit = std::fopen("out/density_emit.bin", "wb");
+  FILE* b_emit_elec = std::fopen("out/density_emit_elec.bin", "wb");
+  FILE* b_abs_top = std::fopen("out/density_absorb_top.bin", "wb");
+  FILE* b_abs_bot = std::fopen("out/density_absorb_bot.bin", "wb");
+  if (!f_emit || !f_abs || !f_top || !f_bot || !f_ramo || !b_emit || !b_emit_elec || !b_abs_top || !b_abs_bot) {
     std::fprintf(stderr, "rd_main: cannot write under out/\n");
     return 2;
   }
   std::printf("RUMDEED: Starting main loop\n Doing %d time steps of size %12.4E ps\n", steps, dt / time_scale);
   const double E_z = -V_s / (mode == 10 ? d : dc.gap);
   std::vector<double> vel;
+  std::vector<rd_event> events((size_t)ec.event_capacity);
+  long long lost_total = 0;
   int progress = 1;
   for (int step = 1; step <= steps; ++step) {
     check(rd_step(e, step), "rd_step");
+    // event records of the step, in the reference's binary layouts:
+    //   density_emit.bin       pos/length_scale (3 f64), emitter, section, id, species (4 i32)
+    //   density_emit_elec.bin  pos/length_scale (3 f64), emitter, id (2 i32)
+    //   density_absorb_top.bin x, y /length_scale (2 f64), v (3 f64, m/s), emitter, section, id (3 i32)
+    //   density_absorb_bot.bin x, y /length_scale (2 f64), emitter, section, id (3 i32)
+    int nev = 0;
+    long long lost = 0;
+    check(rd_events_take(e, (int)events.size(), events.data(), &nev, &lost), "rd_events_take");
+    lost_total += lost;
+    for (int k = 0; k < nev; ++k) {
+      const rd_event& r = events[k];
+      const double p3[3] = {r.pos[0] / length_scale, r.pos[1] / length_scale, r.pos[2] / length_scale};
+      const int emitter = 1;
+      if (r.kind == RD_EVENT_EMIT) {
+        const int i4[4] = {emitter, r.section, r.id, r.species};
+        std::fwrite(p3, sizeof(double), 3, b_emit);
+        std::fwrite(i4, sizeof(int), 4, b_emit);
+        const int i2[2] = {emitter, r.id};
+        std::fwrite(p3, sizeof(double), 3, b_emit_elec);
+        std::fwrite(i2, sizeof(int), 2, b_emit_elec);
+      } else {
+        const int i3[3] = {emitter, r.section, r.id};
+        FILE* bf = r.kind == RD_EVENT_ABSORB_TOP ? b_abs_top : b_abs_bot;
+        std::fwrite(p3, sizeof(double), 2, bf);
+        if (r.kind == RD_EVENT_ABSORB_TOP) std::fwrite(r.vel, sizeof(double), 3, bf);
+        std::fwrite(i3, sizeof(int), 3, bf);
+      }
+    }
     rd_counters c;
     check(rd_counters_get(e, diode, &c), "rd_counters_get");
     const double cur_time = dt * step / time_scale;
@@ -324,8 +362,9 @@ int main(int argc, char** argv) {
       ++progress;
     }
   }
-  for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo}) std::fclose(f);
+  for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo, b_emit, b_emit_elec, b_abs_top, b_abs_bot}) std::fclose(f);
   rd_engine_destroy(e);
+  if (lost_total) std::printf("RUMDEED: %lld event records did not fit the event log\n", lost_total);
   std::printf("RUMDEED: Main loop finished\n");
   return 0;
 }

@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -45,3 +47,10 @@ def test_no_oracle_in_product_path():
             if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
                 txt = open(os.path.join(dp, f)).read()
                 assert "orc" + "_" not in txt and "import orc" not in txt, f
+
+
+def test_invalid_chunking_is_refused_before_touching_the_gpu(rg):
+    with pytest.raises(rg.RumdeedError, match="chunk_min"):
+        rg.Engine(chunk_min=100)
+    with pytest.raises(rg.RumdeedError, match="chunk_count_max"):
+        rg.Engine(chunk_count_max=64)

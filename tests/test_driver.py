@@ -102,3 +102,41 @@ def test_driver_run_matches_python_binding(driver, tmp_path, rg):
         assert top[step - 1][2] == c["absorbed_top_step"] and bot[step - 1][2] == c["absorbed_bot_step"]
     assert emitted[:, 2].sum() > 0          # the deck emits
     eng.close()
+    # binary event files (Fortran stream layouts)
+    out = deck / "out"
+    rec_emit = np.dtype([("pos", "<f8", 3), ("emit", "<i4"), ("sec", "<i4"), ("id", "<i4"), ("species", "<i4")])
+    rec_elec = np.dtype([("pos", "<f8", 3), ("emit", "<i4"), ("id", "<i4")])
+    rec_top = np.dtype([("xy", "<f8", 2), ("vel", "<f8", 3), ("emit", "<i4"), ("sec", "<i4"), ("id", "<i4")])
+    rec_bot = np.dtype([("xy", "<f8", 2), ("emit", "<i4"), ("sec", "<i4"), ("id", "<i4")])
+    assert rec_emit.itemsize == 40 and rec_elec.itemsize == 32 and rec_top.itemsize == 52 and rec_bot.itemsize == 28
+    de = np.fromfile(out / "density_emit.bin", dtype=rec_emit)
+    dl = np.fromfile(out / "density_emit_elec.bin", dtype=rec_elec)
+    dt = np.fromfile(out / "density_absorb_top.bin", dtype=rec_top)
+    db = np.fromfile(out / "density_absorb_bot.bin", dtype=rec_bot)
+    assert len(de) == len(dl) == emitted[:, 2].sum()
+    assert len(dt) == top[:, 2].sum() and len(db) == bot[:, 2].sum()
+    np.testing.assert_allclose(de["pos"][:, 2], 1.0, rtol=1e-12)          # placed 1 nm above the cathode
+    assert np.all(np.abs(de["pos"][:, :2]) <= 500.0 + 1e-9)                # on the emitter
+    assert np.all(de["species"] == 1) and np.all(de["emit"] == 1) and np.all(np.diff(de["id"]) > 0)
+    np.testing.assert_array_equal(de["pos"], dl["pos"])
+    assert np.all(dt["vel"][:, 2] > 0.0) if len(dt) else True              # anode hits move up
+
+
+@pytest.mark.gpu
+def test_event_log_counts_and_loss(rg):
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=3000 + 64,
+                    chain_capacity=3000 + 64, quad_capacity=16384, event_capacity=8)
+    d = eng.add_diode(V_s=2.0e3, gap=1000 * 1.0e-9, time_step=2.5e-4 * 1.0e-12, image_charge=True,
+                      N_ic_max=0, capacity=3000, emitter_pos=(-500.0 * 1.0e-9, -500.0 * 1.0e-9),
+                      emitter_dim=(1000.0 * 1.0e-9, 1000.0 * 1.0e-9), work=[[2.0, 2.2], [2.4, 2.6]],
+                      emission=True, mh_jumps=40, seed=11)
+    eng.step(1)
+    ev, lost = eng.events_take()
+    c = d.counters()
+    assert c["emitted_step"] > 8
+    assert len(ev) == 8 and lost == c["emitted_step"] - 8                 # the log holds 8
+    assert all(r["kind"] == rg.EVENT_EMIT and r["step"] == 1 for r in ev)
+    assert [r["id"] for r in ev] == sorted(r["id"] for r in ev)
+    ev2, lost2 = eng.events_take()                                           # emptied by the take
+    assert ev2 == [] and lost2 == 0
+    eng.close()
