@@ -71,8 +71,8 @@ typedef struct {
   int capacity;            /* MAX_PARTICLES of this diode */
   double emitter_pos[2];   /* planar emitter lower-left corner (m) */
   double emitter_dim[2];   /* planar emitter size (m) */
-  int work_nx, work_ny;    /* checkerboard work function grid (1 x 1 = uniform) */
-  const double* work;      /* work_ny x work_nx values in eV, row 0 = top row */
+  int work_nx, work_ny;    /* checkerboard work function grid (1 x 1 = uniform); see work_model */
+  const double* work;      /* work_ny x work_nx values in eV, row 0 = top row; see work_model */
   double tip_dim[3];       /* tip (d_tip, R_base, h_tip) in m */
   double tip_work_function;/* eV (the reference hard-codes 4.7) */
   int emission;            /* 0: no emission; 1: Fowler-Nordheim field emission */
@@ -82,6 +82,22 @@ typedef struct {
   int quad_order;          /* planar supply rule: Gauss-Legendre order (0: 4) */
   int init_rounds;         /* MH start-position rounds (0: 10000 as the reference) */
   unsigned long long seed; /* Philox key of this diode */
+  int work_model;          /* planar work-function model (Read_work_function's types,
+                              src/mod_work_function.F90:53-152): 0 or 1 checkerboard
+                              (work = work_ny x work_nx values, eV); 2 Gaussian (work =
+                              base eV, then A eV, x_c, y_c, std_x, std_y nm per Gaussian;
+                              work_nx = the number of Gaussians); 4 Voronoi (work = x, y
+                              as fractions of the emitter, phi eV, section per site;
+                              work_nx = the number of sites) */
+  int emitter_delay;       /* the emitter emits from step emitter_delay + 1 on
+                              (EMITTERS_DELAY, src/mod_field_emission_v2.F90:181) */
+  int planes_N;            /* measurement planes, at most 10 (planes_N, planes_z of the
+                              namelist); particles crossing one upwards are logged */
+  double planes_z[10];     /* plane heights (m); <= 0: plane unused */
+  int mh_serial;           /* planar MH sampler: 0 batched (chains in lockstep, mh_batch =
+                              .true.), 1 serial (mh_batch = .false., the reference's default:
+                              each chain runs to completion, sees the electrons earlier
+                              chains of the step emitted and updates MH_std once) */
 } rd_diode_config;
 
 typedef struct {
@@ -92,6 +108,9 @@ typedef struct {
   long long electron_steps, steps_done;
   double ramo_current;     /* ramo_current(species_elec) of the last step (A) */
   double N_sup, MH_std, a_rate, residual;
+  double F_avg[3];         /* mean cathode field over the supply evaluation points
+                              (field.dt, src/mod_field_emission_v2.F90:644-651) */
+  double df_avg;           /* sum of the candidates' escape probabilities / N_sup (:354,385) */
 } rd_counters;
 
 const char* rd_last_error(void);
@@ -215,7 +234,9 @@ int rd_time_field_at(rd_engine* e, int diode, int M, const double* pos3m, int re
  * since the last take into `out` (at most `cap`), ordered by diode, kind and
  * id, empties the log and reports records that did not fit (the log's or the
  * caller's capacity) in n_lost. */
-enum { RD_EVENT_EMIT = 1, RD_EVENT_ABSORB_TOP = 2, RD_EVENT_ABSORB_BOT = 3 };
+enum { RD_EVENT_EMIT = 1, RD_EVENT_ABSORB_TOP = 2, RD_EVENT_ABSORB_BOT = 3,
+       RD_EVENT_PLANE = 16 /* + plane index k: crossed plane k upwards (planes-(k+1).bin,
+                              Check_Planes, src/mod_verlet.F90:343-367) */ };
 typedef struct {
   double pos[3], vel[3];
   int diode, kind, section, id, species, step;

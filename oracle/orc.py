@@ -62,6 +62,9 @@ class Diode(C.Structure):
         ("quad_order", C.c_int),
         ("init_rounds_max", C.c_int),
         ("last_chains", C.c_int), ("last_failed_chains", C.c_int),
+        ("work_model", C.c_int),
+        ("emit_delay", C.c_int), ("mh_serial", C.c_int),
+        ("F_avg_z", C.c_double), ("df_avg", C.c_double),
     ]
 
 
@@ -99,6 +102,9 @@ def lib():
             "orc_set_planar_emitter": (None, [D, C.c_double, C.c_double, C.c_double, C.c_double,
                                               C.c_int, C.c_int, _dp]),
             "orc_set_tip": (None, [D, C.c_double, C.c_double, C.c_double, C.c_double]),
+            "orc_set_work_model": (None, [D, C.c_int, C.c_int, _dp]),
+            "orc_work_gaussian": (C.c_double, [_dp, C.c_int, C.c_double, C.c_double]),
+            "orc_work_voronoi": (C.c_double, [_dp, C.c_int, _dp, _dp, C.c_double, C.c_double, _ip]),
             "orc_set_emission": (None, [D, C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_int,
                                         C.c_int]),
             "orc_reset": (None, [D]),
@@ -180,6 +186,12 @@ class OracleDiode:
         w = np.array([[4.7]] if work is None else work, dtype=np.float64)
         ny, nx = w.shape
         self.L.orc_set_planar_emitter(self.p, x0, y0, Lx, Ly, nx, ny, ptr(np.ascontiguousarray(w)))
+
+    def set_work_model(self, model, params):
+        """Gaussian (2) or Voronoi (4) work function (flat parameter list)."""
+        w = np.ascontiguousarray(params, dtype=np.float64).ravel()
+        n = (w.size - 1) // 5 if model == 2 else w.size // 4
+        self.L.orc_set_work_model(self.p, model, n, ptr(w))
 
     def set_tip(self, d_tip, R_base, h_tip, phi=4.7):
         self.L.orc_set_tip(self.p, d_tip, R_base, h_tip, phi)

@@ -120,8 +120,43 @@ double orc_work_checkerboard(const double* w, int x_num, int y_num, const double
   y_i = y_num - y_i + 1;                     /* reversed y in the matrix */
   return w[(y_i - 1) * x_num + (x_i - 1)];
 }
+/* w_theta_gaussian, src/mod_work_function.F90:214-254 (centres and widths in nm) */
+double orc_work_gaussian(const double* w, int n, double x, double y) {
+  double v = w[0];
+  for (int i = 0; i < n; ++i) {
+    const double* g = w + 1 + 5 * i;
+    double A = g[0];
+    double x_c = g[1] * LENGTH_SCALE, y_c = g[2] * LENGTH_SCALE;
+    double std_x = g[3] * LENGTH_SCALE, std_y = g[4] * LENGTH_SCALE;
+    v = v + A * exp(-1.0 * (((x - x_c) * (x - x_c)) / (2.0 * (std_x * std_x)) +
+                            ((y - y_c) * (y - y_c)) / (2.0 * (std_y * std_y))));
+  }
+  return v;
+}
+
+/* w_theta_voronoi, :533-571: the closest site; d starts at the single-precision 9.9E10 */
+double orc_work_voronoi(const double* w, int n, const double em_pos[2], const double em_dim[2],
+                        double x, double y, int* sec) {
+  int k = -1;
+  double d = (double)9.9e10f;
+  for (int i = 0; i < n; ++i) {
+    double sx = em_pos[0] + w[4 * i] * em_dim[0];   /* Read_work_function :130-131 */
+    double sy = em_pos[1] + w[4 * i + 1] * em_dim[1];
+    double d_p = (x - sx) * (x - sx) + (y - sy) * (y - sy);
+    if (d_p < d) { k = i; d = d_p; }
+  }
+  if (k < 0) k = 0;
+  if (sec) *sec = (int)w[4 * k + 3];
+  return w[4 * k + 2];
+}
+
 static double work_at(const orc_diode* s, double x, double y, int* sec) {
   double pos[2] = {s->em_pos[0], s->em_pos[1]}, dim[2] = {s->em_dim[0], s->em_dim[1]};
+  if (s->work_model == 2) {
+    if (sec) *sec = 1;
+    return orc_work_gaussian(s->work, s->work_nx, x, y);
+  }
+  if (s->work_model == 4) return orc_work_voronoi(s->work, s->work_nx, pos, dim, x, y, sec);
   return orc_work_checkerboard(s->work, s->work_nx, s->work_ny, pos, dim, x, y, sec);
 }
 
@@ -203,6 +238,7 @@ orc_diode* orc_diode_new(int geometry, int cap, double V_s, double d, double tim
   s->N_ic_max = N_ic_max;
   s->work_nx = s->work_ny = 1;
   s->work[0] = 4.7;
+  s->work_model = 1;
   s->tip_phi = 4.7;
   s->MH_std = 0.0125;                          /* fe_v2:58 */
   s->a_rate = 1.0;
@@ -226,8 +262,17 @@ void orc_diode_free(orc_diode* s) {
 void orc_set_planar_emitter(orc_diode* s, double x0, double y0, double Lx, double Ly,
                             int nx, int ny, const double* work) {
   s->em_pos[0] = x0; s->em_pos[1] = y0; s->em_dim[0] = Lx; s->em_dim[1] = Ly;
+  s->work_model = 1;
   s->work_nx = nx; s->work_ny = ny;
   for (int i = 0; i < nx * ny && i < 64 * 64; ++i) s->work[i] = work[i];
+}
+
+void orc_set_work_model(orc_diode* s, int model, int n, const double* params) {
+  int len = model == 2 ? 1 + 5 * n : 4 * n;
+  s->work_model = model;
+  s->work_nx = n;
+  s->work_ny = 1;
+  for (int i = 0; i < len && i < 64 * 64; ++i) s->work[i] = params[i];
 }
 
 /* Init_Emission_Tip, src/mod_emission_tip.f90:81-127 */
@@ -736,6 +781,7 @@ double orc_supply_integral_planar(orc_diode* s) {
   double A = s->em_dim[0] * s->em_dim[1];
   int npt = P * Q;
   double* val = (double*)calloc((size_t)npt * npt, sizeof(double));
+  double* fz = (double*)calloc((size_t)npt * npt, sizeof(double));
 #pragma omp parallel for schedule(dynamic, 8)
   for (int k = 0; k < npt * npt; ++k) {
     int iy = k / npt, ix = k % npt;
@@ -746,14 +792,19 @@ double orc_supply_integral_planar(orc_diode* s) {
     double p[3] = {s->em_pos[0] + ux * s->em_dim[0], s->em_pos[1] + uy * s->em_dim[1], 0.0};
     double f[3];
     orc_field_at(s, p, f, 1);
+    fz[k] = f[2];
     if (f[2] < 0.0) {
       double phi = work_at(s, p[0], p[1], NULL);
       val[k] = (wx * wy) * (A * orc_elec_supply_v2(f[2], phi, s->image_charge, s->time_step));
     }
   }
-  nsum tot = {0, 0};
-  for (int k = 0; k < npt * npt; ++k) if (val[k] != 0.0) nadd(&tot, val[k]);
-  free(val);
+  nsum tot = {0, 0}, ftot = {0, 0};
+  for (int k = 0; k < npt * npt; ++k) {
+    if (val[k] != 0.0) nadd(&tot, val[k]);
+    nadd(&ftot, fz[k]);
+  }
+  s->F_avg_z = nval(&ftot) / (double)(npt * npt);   /* F_avg, fe_v2:644-651 */
+  free(val); free(fz);
   return nval(&tot);
 }
 
@@ -839,6 +890,92 @@ void orc_mh_batch_planar(orc_diode* s, int step, int M, double* df_out, double* 
   free(sup);
 }
 
+/* Metropolis_Hastings_rectangle_J, src/mod_field_emission_v2.F90:1122-1265: one
+ * chain run to completion against the current particles (including the ones
+ * earlier chains of the step emitted); MH_std is fixed within the chain and
+ * updated once from the chain's acceptance rate over the jumps after the
+ * warm-up.  Same Philox counters as the batched sampler. */
+static void mh_serial_chain(orc_diode* s, int step, int c, double* df_out, double* F_out, double pos[3]) {
+  int ndim = s->mh_jumps, ndim_first = (int)nint_f(ndim * 0.25);
+  double std[2] = {s->em_dim[0] * 0.10, s->em_dim[1] * 0.10};
+  double cur[3] = {0, 0, 0}, f[3];
+  int found = 0;
+  for (int r = 0; r < s->init_rounds_max; ++r) {
+    double u1, u2;
+    rng2(s->seed, c, r, step, TAG_INIT, &u1, &u2);
+    cur[0] = u1 * s->em_dim[0] + s->em_pos[0];
+    cur[1] = u2 * s->em_dim[1] + s->em_pos[1];
+    orc_field_at(s, cur, f, 1);
+    if (f[2] < 0.0) { found = 1; break; }
+  }
+  if (!found) {   /* :1161-1170 */
+    *F_out = 1.0; *df_out = -DBL_MAX;
+    pos[0] = s->em_pos[0]; pos[1] = s->em_pos[1]; pos[2] = 0.0;
+    return;
+  }
+  *F_out = f[2];
+  double sup_cur = orc_elec_supply_log(f[2], work_at(s, cur[0], cur[1], NULL), s->image_charge);
+  int ja = 0, jr = 0;
+  for (int i = 1; i <= ndim; ++i) {
+    if (i > ndim_first) { std[0] = s->em_dim[0] * s->MH_std; std[1] = s->em_dim[1] * s->MH_std; }
+    double g1, g2;
+    gauss2(s->seed, c, i, step, &g1, &g2);
+    double w[3] = {g1 * std[0] + cur[0], g2 * std[1] + cur[1], 0.0};
+    for (int k = 0; k < 2; ++k) {     /* check_limits_metro_rec */
+      double lo = s->em_pos[k], hi = s->em_pos[k] + s->em_dim[k];
+      if (w[k] > hi) w[k] = hi - (w[k] - hi);
+      else if (w[k] < lo) w[k] = (lo - w[k]) + lo;
+    }
+    orc_field_at(s, w, f, 1);
+    if (f[2] >= 0.0) { if (i > ndim_first) jr++; continue; }
+    double sn = orc_elec_supply_log(f[2], work_at(s, w[0], w[1], NULL), s->image_charge);
+    double alpha = sn - sup_cur;
+    int take = 0;
+    if (sn >= sup_cur) take = 1;
+    else {
+      double u1, u2;
+      rng2(s->seed, c, i, step, TAG_ACCEPT, &u1, &u2);
+      take = (log(u1) <= alpha);
+    }
+    if (take) {
+      cur[0] = w[0]; cur[1] = w[1]; sup_cur = sn; *F_out = f[2];
+      if (i > ndim_first) ja++;
+    } else if (i > ndim_first) jr++;
+  }
+  if (ja + jr > 0) {   /* :1251-1254 */
+    s->a_rate = (double)ja / (double)(jr + ja);
+    mh_std_update(&s->MH_std, s->a_rate, 0.00005, 0.1250);
+  }
+  pos[0] = cur[0]; pos[1] = cur[1]; pos[2] = 0.0;
+  *df_out = orc_escape_prob_log(*F_out, work_at(s, cur[0], cur[1], NULL), s->image_charge);
+}
+
+/* The serial branch of Do_Field_Emission_Planar_rectangle (:322-333, 338-383):
+ * each candidate's chain, its emission test and its Add_Particle before the
+ * next candidate's chain. */
+static int emission_planar_serial(orc_diode* s, int step, int M) {
+  int emitted = 0;
+  double df_sum = 0.0;
+  for (int c = 0; c < M; ++c) {
+    double D, F, p[3];
+    mh_serial_chain(s, step, c, &D, &F, p);
+    if (F >= 0.0) D = -DBL_MAX;
+    df_sum += exp(D);
+    double u1, u2;
+    rng2(s->seed, c, 0, step, TAG_EMIT, &u1, &u2);
+    if (log(u1) <= D) {
+      double q[3] = {p[0], p[1], 1.0 * LENGTH_SCALE}, v[3] = {0, 0, 0};
+      int sec = 1;
+      work_at(s, q[0], q[1], &sec);
+      if (orc_add_particle(s, q, v, ORC_ELEC, step, sec) >= 0) emitted++;
+    }
+  }
+  s->df_avg = s->N_sup > 0.0 ? df_sum / s->N_sup : 0.0;
+  s->emitted_step = emitted;
+  s->emitted_total += emitted;
+  return emitted;
+}
+
 /* Do_Field_Emission_Planar_rectangle, src/mod_field_emission_v2.F90:261-395 */
 int orc_do_emission_planar(orc_diode* s, int step) {
   double N_sup = orc_supply_integral_planar(s);
@@ -849,17 +986,21 @@ int orc_do_emission_planar(orc_diode* s, int step) {
   if (M > s->max_chains) M = s->max_chains;
   s->last_chains = M;
   s->emitted_step = 0;
+  s->df_avg = 0.0;
   if (M == 0) return 0;
+  if (s->mh_serial) return emission_planar_serial(s, step, M);
   double* df = (double*)malloc(sizeof(double) * M);
   double* F = (double*)malloc(sizeof(double) * M);
   double* P = (double*)malloc(sizeof(double) * 3 * M);
   int* ok = (int*)malloc(sizeof(int) * M);
   orc_mh_batch_planar(s, step, M, df, F, P, ok);
   int emitted = 0, failed = 0;
+  double df_sum = 0.0;
   for (int c = 0; c < M; ++c) {
     double D = df[c];
     if (!ok[c]) failed++;
     if (F[c] >= 0.0) D = -DBL_MAX;
+    df_sum += exp(D);   /* df_avg, :354 */
     double u1, u2;
     rng2(s->seed, c, 0, step, TAG_EMIT, &u1, &u2);
     if (log(u1) <= D) {
@@ -870,6 +1011,7 @@ int orc_do_emission_planar(orc_diode* s, int step) {
     }
   }
   s->last_failed_chains = failed;
+  s->df_avg = N_sup > 0.0 ? df_sum / N_sup : 0.0;   /* :385 */
   free(df); free(F); free(P); free(ok);
   s->emitted_step = emitted;
   s->emitted_total += emitted;
@@ -1023,6 +1165,10 @@ int orc_do_emission_tip(orc_diode* s, int step) {
 
 int orc_do_emission(orc_diode* s, int step) {
   if (!s->emission) { s->emitted_step = 0; return 0; }
+  if (step <= s->emit_delay) {   /* emitters_delay(i) < step, fe_v2:181 */
+    s->emitted_step = 0; s->N_sup = 0.0; s->last_chains = 0; s->F_avg_z = 0.0; s->df_avg = 0.0;
+    return 0;
+  }
   return s->geometry == ORC_TIP ? orc_do_emission_tip(s, step) : orc_do_emission_planar(s, step);
 }
 

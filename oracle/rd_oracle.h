@@ -92,6 +92,14 @@ typedef struct {
   int mh_jumps, max_chains, quad_panels, quad_order;
   int init_rounds_max;      /* 10000 in the reference */
   int last_chains, last_failed_chains;
+  /* work-function model (Read_work_function types): 1 checkerboard (work =
+   * matrix), 2 Gaussian (work = base, then A, x_c, y_c, std_x, std_y per
+   * Gaussian, work_nx of them), 4 Voronoi (work = x, y fractions of the
+   * emitter, phi, section per site, work_nx of them) */
+  int work_model;
+  int emit_delay;           /* emitters_delay: emission from step emit_delay + 1 on */
+  int mh_serial;            /* 1: mh_batch = .false. (chains one after another) */
+  double F_avg_z, df_avg;   /* field.dt: mean cathode F_z of the supply points, sum exp(D) / N_sup */
 } orc_diode;
 
 /* Create / destroy.  Geometry parameters follow Init_Field_Emission_v2
@@ -103,6 +111,15 @@ void orc_diode_free(orc_diode* s);
 void orc_set_planar_emitter(orc_diode* s, double x0, double y0, double Lx, double Ly,
                             int work_nx, int work_ny, const double* work);
 void orc_set_tip(orc_diode* s, double d_tip, double R_base, double h_tip, double phi);
+/* A Gaussian (model 2) or Voronoi (model 4) work function on the planar emitter;
+ * n Gaussians / sites, parameters laid out as in orc_diode.work. */
+void orc_set_work_model(orc_diode* s, int model, int n, const double* params);
+/* w_theta_gaussian (src/mod_work_function.F90:214-254) and w_theta_voronoi
+ * (:533-571; sites as fractions of the emitter, converted as in
+ * Read_work_function :124-134). */
+double orc_work_gaussian(const double* w, int n, double x, double y);
+double orc_work_voronoi(const double* w, int n, const double em_pos[2], const double em_dim[2],
+                        double x, double y, int* sec);
 void orc_set_emission(orc_diode* s, int on, uint64_t seed, int mh_jumps, int max_chains,
                       int quad_panels, int quad_order);
 void orc_reset(orc_diode* s);  /* Setup_Test_System, src/mod_tests.F90:324-403 */

@@ -54,7 +54,7 @@ class Event(C.Structure):
                 ("section", C.c_int), ("id", C.c_int), ("species", C.c_int), ("step", C.c_int)]
 
 
-EVENT_EMIT, EVENT_ABSORB_TOP, EVENT_ABSORB_BOT = 1, 2, 3
+EVENT_EMIT, EVENT_ABSORB_TOP, EVENT_ABSORB_BOT, EVENT_PLANE = 1, 2, 3, 16
 
 
 class DiodeConfig(C.Structure):
@@ -65,7 +65,9 @@ class DiodeConfig(C.Structure):
                 ("work", C.POINTER(C.c_double)), ("tip_dim", C.c_double * 3),
                 ("tip_work_function", C.c_double), ("emission", C.c_int), ("mh_jumps", C.c_int),
                 ("max_chains", C.c_int), ("quad_panels", C.c_int), ("quad_order", C.c_int),
-                ("init_rounds", C.c_int), ("seed", C.c_ulonglong)]
+                ("init_rounds", C.c_int), ("seed", C.c_ulonglong), ("work_model", C.c_int),
+                ("emitter_delay", C.c_int), ("planes_N", C.c_int), ("planes_z", C.c_double * 10),
+                ("mh_serial", C.c_int)]
 
 
 class Counters(C.Structure):
@@ -76,10 +78,13 @@ class Counters(C.Structure):
                 ("absorbed_top_total", C.c_longlong), ("absorbed_bot_total", C.c_longlong),
                 ("electron_steps", C.c_longlong), ("steps_done", C.c_longlong),
                 ("ramo_current", C.c_double), ("N_sup", C.c_double), ("MH_std", C.c_double),
-                ("a_rate", C.c_double), ("residual", C.c_double)]
+                ("a_rate", C.c_double), ("residual", C.c_double), ("F_avg", C.c_double * 3),
+                ("df_avg", C.c_double)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["F_avg"] = tuple(self.F_avg)
+        return d
 
 
 class PhaseTimes(C.Structure):
@@ -370,8 +375,13 @@ def diode_config(geometry=GEOM_PLANAR, V_s=2.0e3, gap=1000e-9, time_step=0.25e-1
              image_charge=True, N_ic_max=0, capacity=4096, emitter_pos=(0.0, 0.0),
              emitter_dim=(0.0, 0.0), work=None, tip_dim=(0.0, 0.0, 0.0),
              tip_work_function=4.7, emission=False, mh_jumps=0, max_chains=0,
-             quad_panels=0, quad_order=0, init_rounds=0, seed=1):
-    """rd_diode_config from keyword arguments (the /input/ namelist of one run)."""
+             quad_panels=0, quad_order=0, init_rounds=0, seed=1, work_model=0, emitter_delay=0,
+             planes_z=(), mh_serial=False):
+    """rd_diode_config from keyword arguments (the /input/ namelist of one run).
+    `work`: the checkerboard matrix (work_model 0/1); for work_model 2
+    (Gaussian) the flat list base, then (A, x_c, y_c, std_x, std_y) per
+    Gaussian; for work_model 4 (Voronoi) the flat list (x, y, phi, section)
+    per site, x, y as fractions of the emitter."""
     cfg = DiodeConfig()
     cfg.geometry = geometry
     cfg.V_s = V_s
@@ -383,9 +393,20 @@ def diode_config(geometry=GEOM_PLANAR, V_s=2.0e3, gap=1000e-9, time_step=0.25e-1
     cfg.emitter_pos[:] = list(emitter_pos)
     cfg.emitter_dim[:] = list(emitter_dim)
     keep = None
+    cfg.work_model = work_model
+    cfg.emitter_delay = emitter_delay
+    cfg.mh_serial = int(bool(mh_serial))
+    cfg.planes_N = len(planes_z)
+    for k, z in enumerate(planes_z):
+        cfg.planes_z[k] = z
     if work is not None:
-        keep = np.ascontiguousarray(work, dtype=np.float64)
-        cfg.work_ny, cfg.work_nx = keep.shape
+        if work_model in (2, 4):
+            keep = np.ascontiguousarray(work, dtype=np.float64).ravel()
+            cfg.work_nx = (keep.size - 1) // 5 if work_model == 2 else keep.size // 4
+            cfg.work_ny = 1
+        else:
+            keep = np.ascontiguousarray(work, dtype=np.float64)
+            cfg.work_ny, cfg.work_nx = keep.shape
         cfg.work = keep.ctypes.data_as(_dp)
     cfg.tip_dim[:] = list(tip_dim)
     cfg.tip_work_function = tip_work_function

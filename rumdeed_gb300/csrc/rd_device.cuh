@@ -97,9 +97,49 @@ __device__ __forceinline__ double fn_supply_v2(double F, double phi, int ic, dou
   return (((dt / c_k.q0) * c_k.a_FN) / ((t * t) * phi)) * (F * F);
 }
 
-// ---- checkerboard work function (src/mod_work_function.F90:389-487) --------
+// ---- work-function models (src/mod_work_function.F90) ----------------------
+// Voronoi site closest to (x, y) (w_theta_voronoi :533-571): sites stored as
+// (x, y) fractions of the emitter, phi, section; converted like
+// Read_work_function (:124-134).  The start distance is the reference's
+// single-precision literal 9.9E10.
+__device__ __forceinline__ int voronoi_site(const DiodeParams& P, const double* w, double x, double y) {
+  int k = 0;
+  double d = (double)9.9e10f;
+  for (int i = 0; i < P.work_nx; ++i) {
+    const double sx = P.em_x0 + w[4 * i] * P.em_Lx, sy = P.em_y0 + w[4 * i + 1] * P.em_Ly;
+    const double dp = (x - sx) * (x - sx) + (y - sy) * (y - sy);
+    if (dp < d) { k = i; d = dp; }
+  }
+  return k;
+}
+
+// w_theta_gaussian (:214-254): base + sum A exp(-((x-xc)^2/(2 sx^2) + (y-yc)^2/(2 sy^2))),
+// centres and widths in nm.
+__device__ __forceinline__ double gaussian_work(const DiodeParams& P, const double* w, double x, double y) {
+  double v = w[0];
+  for (int i = 0; i < P.work_nx; ++i) {
+    const double* g = w + 1 + 5 * i;
+    const double xc = g[1] * c_k.length_scale, yc = g[2] * c_k.length_scale;
+    const double sx = g[3] * c_k.length_scale, sy = g[4] * c_k.length_scale;
+    v = v + g[0] * exp(-1.0 * (((x - xc) * (x - xc)) / (2.0 * (sx * sx)) + ((y - yc) * (y - yc)) / (2.0 * (sy * sy))));
+  }
+  return v;
+}
+
+// The work function at (x, y) and its section (ptr_Work_fun): checkerboard
+// (w_theta_checkerboard :389-487), Gaussian (section 1) or Voronoi.
 __device__ __forceinline__ double work_at(const DiodeParams& P, const double* work, double x,
                                           double y, int* sec) {
+  const double* w = work + P.work_off;
+  if (P.work_model == 2) {
+    if (sec) *sec = 1;
+    return gaussian_work(P, w, x, y);
+  }
+  if (P.work_model == 4) {
+    const int k = voronoi_site(P, w, x, y);
+    if (sec) *sec = (int)w[4 * k + 3];
+    return w[4 * k + 2];
+  }
   double xs = (x - P.em_x0) / P.em_Lx, ys = (y - P.em_y0) / P.em_Ly;
   int nx = P.work_nx, ny = P.work_ny;
   int xi = (int)floor(xs / (1.0 / nx)) + 1, yi = (int)floor(ys / (1.0 / ny)) + 1;
@@ -107,7 +147,7 @@ __device__ __forceinline__ double work_at(const DiodeParams& P, const double* wo
   yi = yi > ny ? ny : (yi < 1 ? 1 : yi);
   if (sec) *sec = nx * (yi - 1) + xi;
   yi = ny - yi + 1;
-  return work[P.work_off + (yi - 1) * nx + (xi - 1)];
+  return w[(yi - 1) * nx + (xi - 1)];
 }
 
 // ---- hyperboloid tip (src/mod_hyperboloid_tip.f90) ---------------------------

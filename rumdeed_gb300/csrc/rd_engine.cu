@@ -50,7 +50,10 @@ cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const Diode
 cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                     const double* qx, const double* qy, const double* qw,
                                     const double* qF, const double* qfx, const double* qfy,
-                                    const double* work);
+                                    const double* work, const int* step_ptr);
+cudaError_t rd_launch_mh_serial(int prec, int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                                const Pool& pool, const double* work, const double* wtab,
+                                const int* step_ptr, double kscale, const EventLog& ev);
 cudaError_t rd_launch_mh_init(int prec, int grid, cudaStream_t st, const DiodeParams* P,
                               DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
                               const PlanHeader* ph, const ChainState& cs, const int* ch_off,
@@ -293,6 +296,7 @@ static bool valid_chunking(int clen_min, int nch_max) {
 
 struct Sig {
   bool planar = false, tip = false, emit_planar = false, emit_tip = false, nic = false;
+  bool emit_serial = false;   // some planar diode uses the serial MH sampler
   int jumps = 0;
 };
 static Sig signature(const rd_engine* e) {
@@ -304,6 +308,7 @@ static Sig signature(const rd_engine* e) {
     if (p.geometry == RD_G_PLANAR && p.image_charge && p.N_ic_max > 0) s.nic = true;
     if (p.emission) {
       if (p.geometry == RD_G_TIP) s.emit_tip = true; else s.emit_planar = true;
+      if (p.geometry != RD_G_TIP && p.mh_serial) s.emit_serial = true;
       s.jumps = std::max(s.jumps, p.mh_jumps);
     }
   }
@@ -330,7 +335,7 @@ static int launch_emission(rd_engine* e) {
     e->kernels_in_step++;
   }
   CK(rd_launch_supply_reduce(ns, e->st, e->dP, e->dD, e->qx, e->qy, e->qw, e->qF, e->qfx, e->qfy,
-                             e->work));
+                             e->work, e->d_step));
   e->kernels_in_step++;
   CK(plan(e, PM_MH));
   const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
@@ -349,6 +354,11 @@ static int launch_emission(rd_engine* e) {
   }
   CK(rd_launch_emit(ns, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step, e->evlog));
   e->kernels_in_step++;
+  if (s.emit_serial) {   // serial MH diodes: chains one after another, one block per diode
+    CK(rd_launch_mh_serial(prec, ns, e->st, e->dP, e->dD, e->pool, e->work, e->wtab, e->d_step, e->kscale,
+                           e->evlog));
+    e->kernels_in_step++;
+  }
   return RD_OK;
 }
 
@@ -409,8 +419,8 @@ static int launch_step_body(rd_engine* e) {
 static std::string sig_string(rd_engine* e) {
   Sig s = signature(e);
   char b[128];
-  snprintf(b, sizeof b, "%d%d%d%d%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic, s.jumps,
-           e->clen_min, e->nch_max);
+  snprintf(b, sizeof b, "%d%d%d%d%d%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
+           s.emit_serial, s.jumps, e->clen_min, e->nch_max);
   return b;
 }
 
@@ -619,8 +629,14 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
   p.dt = c->time_step;
   p.dt2 = c->time_step * c->time_step;
   p.seed = c->seed;
+  p.emit_delay = c->emitter_delay > 0 ? c->emitter_delay : 0;
+  p.mh_serial = c->mh_serial ? 1 : 0;
+  if (c->planes_N < 0 || c->planes_N > 10) return fail(RD_ERR_INVALID, "planes_N must be in [0, 10]");
+  p.planes_n = c->planes_N;
+  for (int k = 0; k < p.planes_n; ++k) p.planes_z[k] = c->planes_z[k];
   p.init_rounds = c->init_rounds > 0 ? c->init_rounds : 10000;
   p.work_nx = p.work_ny = 1;
+  p.work_model = 1;
   if (c->geometry == RD_GEOM_PLANAR) {
     if (c->gap <= 0.0) return fail(RD_ERR_INVALID, "gap must be positive");
     p.d = c->gap;
@@ -636,7 +652,17 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
     p.em_wy = (float)(p.em_Ly * 1.0e9);
     p.mh_jumps = c->mh_jumps > 0 ? c->mh_jumps : 200;   // MH_ndim, fe_v2:70
     p.mh_lo = 0.00005; p.mh_hi = 0.1250;                 // fe_v2:75-76
-    if (c->work_nx > 0 && c->work_ny > 0 && c->work) { p.work_nx = c->work_nx; p.work_ny = c->work_ny; }
+    p.work_model = c->work_model > 0 ? c->work_model : 1;
+    if (p.work_model != 1 && p.work_model != 2 && p.work_model != 4)
+      return fail(RD_ERR_INVALID, "work_model must be 1 (checkerboard), 2 (Gaussian) or 4 (Voronoi)");
+    if (p.work_model == 1) {
+      if (c->work_nx > 0 && c->work_ny > 0 && c->work) { p.work_nx = c->work_nx; p.work_ny = c->work_ny; }
+    } else {
+      if (!c->work || c->work_nx < (p.work_model == 4 ? 1 : 0))
+        return fail(RD_ERR_INVALID, "the Gaussian / Voronoi work function needs its parameters (work, work_nx)");
+      p.work_nx = c->work_nx;
+      p.work_ny = 1;
+    }
   } else {
     // Init_Emission_Tip, src/mod_emission_tip.f90:81-127
     double dt_ = c->tip_dim[0], Rb = c->tip_dim[1], ht = c->tip_dim[2];
@@ -668,13 +694,16 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
     if (sl.q_len) e->q_alloc.release(sl.q_off, sl.q_len);
     if (sl.w_len) e->w_alloc.release(sl.w_off, sl.w_len);
   };
-  // work function table
+  // work function table: checkerboard values, Gaussian parameters or Voronoi sites
   sl.w_len = (long long)p.work_nx * p.work_ny;
+  if (p.work_model == 2) sl.w_len = 1 + 5LL * p.work_nx;
+  if (p.work_model == 4) sl.w_len = 4LL * p.work_nx;
   sl.w_off = e->w_alloc.alloc(sl.w_len, 1);
   if (sl.w_off < 0) { sl.w_len = 0; undo(); return fail(RD_ERR_CAPACITY, "work-function table full"); }
   p.work_off = (int)sl.w_off;
+  p.work_data = e->work + sl.w_off;
   std::vector<double> wv(sl.w_len, 4.7);
-  if (c->geometry == RD_GEOM_PLANAR && c->work && c->work_nx > 0 && c->work_ny > 0)
+  if (c->geometry == RD_GEOM_PLANAR && c->work && (p.work_model != 1 || (c->work_nx > 0 && c->work_ny > 0)))
     for (long long k2 = 0; k2 < sl.w_len; ++k2) wv[k2] = c->work[k2];
   if (p.emission) {
     p.max_chains = c->max_chains > 0 ? c->max_chains : p.cap;
@@ -744,9 +773,11 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
     CK(cudaStreamSynchronize(e->st));
   }
   CK(cudaMemcpyAsync(e->work + sl.w_off, wv.data(), sl.w_len * sizeof(double), cudaMemcpyHostToDevice, e->st));
-  std::vector<double> wt(3 * sl.w_len);
-  for (long long k2 = 0; k2 < sl.w_len; ++k2) {
-    const double phi = wv[k2];
+  // supply-target table per checkerboard cell or Voronoi site (the Gaussian model has none)
+  std::vector<double> wt(3 * sl.w_len, 0.0);
+  const long long cells = p.work_model == 1 ? sl.w_len : (p.work_model == 4 ? p.work_nx : 0);
+  for (long long k2 = 0; k2 < cells; ++k2) {
+    const double phi = p.work_model == 4 ? wv[4 * k2 + 2] : wv[k2];
     wt[3 * k2] = std::log(phi);
     wt[3 * k2 + 1] = std::log(e->k.l_const / (phi * phi));
     wt[3 * k2 + 2] = e->k.l_const / (phi * phi);
@@ -1150,12 +1181,7 @@ int rd_run(rd_engine* e, int first_step, int nsteps) {
 
 int rd_step(rd_engine* e, int step) { return rd_run(e, step, 1); }
 
-int rd_counters_get(rd_engine* e, int d, rd_counters* o) {
-  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
-  if (!o) return fail(RD_ERR_INVALID, "null argument");
-  DiodeDyn y;
-  int rc = read_dyn(e, d, &y);
-  if (rc) return rc;
+static void fill_counters(const DiodeDyn& y, rd_counters* o) {
   o->n = y.n;
   o->emitted_step = y.emitted_step; o->dropped_step = y.dropped_step;
   o->absorbed_top_step = y.absorbed_top_step; o->absorbed_bot_step = y.absorbed_bot_step;
@@ -1165,6 +1191,17 @@ int rd_counters_get(rd_engine* e, int d, rd_counters* o) {
   o->electron_steps = y.electron_steps; o->steps_done = y.steps_done;
   o->ramo_current = y.ramo_current; o->N_sup = y.N_sup; o->MH_std = y.MH_std;
   o->a_rate = y.a_rate; o->residual = y.residual;
+  o->F_avg[0] = 0.0; o->F_avg[1] = 0.0; o->F_avg[2] = y.F_avg_z;   // x, y cancel at the cathode
+  o->df_avg = y.df_avg;
+}
+
+int rd_counters_get(rd_engine* e, int d, rd_counters* o) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  if (!o) return fail(RD_ERR_INVALID, "null argument");
+  DiodeDyn y;
+  int rc = read_dyn(e, d, &y);
+  if (rc) return rc;
+  fill_counters(y, o);
   return RD_OK;
 }
 
@@ -1182,17 +1219,6 @@ int rd_last_run_stats(rd_engine* e, double* ms, int* kps) {
   return RD_OK;
 }
 
-static void fill_counters(const DiodeDyn& y, rd_counters* o) {
-  o->n = y.n;
-  o->emitted_step = y.emitted_step; o->dropped_step = y.dropped_step;
-  o->absorbed_top_step = y.absorbed_top_step; o->absorbed_bot_step = y.absorbed_bot_step;
-  o->chains = y.chains; o->chains_failed = y.chains_failed; o->chains_capped = y.chains_capped;
-  o->emitted_total = y.emitted_total; o->dropped_total = y.dropped_total;
-  o->absorbed_top_total = y.absorbed_top_total; o->absorbed_bot_total = y.absorbed_bot_total;
-  o->electron_steps = y.electron_steps; o->steps_done = y.steps_done;
-  o->ramo_current = y.ramo_current; o->N_sup = y.N_sup; o->MH_std = y.MH_std;
-  o->a_rate = y.a_rate; o->residual = y.residual;
-}
 
 int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
   if (!e || !out) return fail(RD_ERR_INVALID, "null argument");
@@ -1219,7 +1245,8 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
       CK(rd_launch_field_points(prec, RD_G_TIP, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_TIP],
                                 e->ph[PM_SUPPLY_TIP], pts, e->partial, e->tickets, e->kscale));
     }
-    CK(rd_launch_supply_reduce(S, e->st, e->dP, e->dD, e->qx, e->qy, e->qw, e->qF, e->qfx, e->qfy, e->work));
+    CK(rd_launch_supply_reduce(S, e->st, e->dP, e->dD, e->qx, e->qy, e->qw, e->qF, e->qfx, e->qfy, e->work,
+                               e->d_step));
     CK(cudaEventRecord(ev[1], e->st));
     CK(cudaMemcpyAsync(dyn.data(), e->dD, sizeof(DiodeDyn) * S, cudaMemcpyDeviceToHost, e->st));
     CK(cudaStreamSynchronize(e->st));
@@ -1244,6 +1271,9 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
     out->mh_jump_launches = s.jumps;
     CK(cudaEventRecord(ev[3], e->st));
     CK(rd_launch_emit(S, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step, e->evlog));
+    if (s.emit_serial)
+      CK(rd_launch_mh_serial(prec, S, e->st, e->dP, e->dD, e->pool, e->work, e->wtab, e->d_step, e->kscale,
+                             e->evlog));
   } else {
     CK(cudaEventRecord(ev[1], e->st));
     CK(cudaEventRecord(ev[2], e->st));

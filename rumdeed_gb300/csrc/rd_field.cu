@@ -126,7 +126,11 @@ k_field_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __
 
 // ---- work-function cell and the tabulated supply logarithm ------------------------------
 // Cell of the checkerboard (as work_at) without the section number.
+// The supply-table entry of (x, y): the checkerboard cell or the Voronoi
+// site; -1 for the Gaussian model, whose work function has no cells.
 __device__ __forceinline__ int work_cell(const DiodeParams& p, double x, double y) {
+  if (p.work_model == 2) return -1;
+  if (p.work_model == 4) return voronoi_site(p, p.work_data, x, y);
   if (p.work_nx == 1 && p.work_ny == 1) return 0;
   double xs = (x - p.em_x0) / p.em_Lx, ys = (y - p.em_y0) / p.em_Ly;
   int nx = p.work_nx, ny = p.work_ny;
@@ -149,6 +153,15 @@ __device__ __forceinline__ double supply_log_tab(const DiodeParams& p, const dou
   if (l > 1.0) { l = 1.0; ll = 0.0; }
   const double ty = 1.0 + l * ((1.0 / 9.0) - (1.0 / 18.0) * ll);
   return (2.0 * LF - 2.0 * log(ty)) - t[0];
+}
+
+// Elec_Supply_log at (x, y) for any work-function model: tabulated per cell
+// or site, computed from phi(x, y) for the Gaussian model.
+__device__ __forceinline__ double supply_log_xy(const DiodeParams& p, const double* __restrict__ wtab,
+                                                double x, double y, double F) {
+  const int cell = work_cell(p, x, y);
+  if (cell < 0) return fn_supply_log(F, gaussian_work(p, p.work_data, x, y), p.image_charge);
+  return supply_log_tab(p, wtab, cell, F);
 }
 
 // ---- FP32 forms of the MH arithmetic (FP32-compensated planar chains) -----------------
@@ -203,17 +216,34 @@ __device__ __forceinline__ int work_cell_f(const DiodeParams& p, float x, float 
   return (yi - 1) * nx + (xi - 1);
 }
 
+// supply_log_tab in FP32 from the table entry (log phi, log(l_const/phi^2),
+// l_const/phi^2) (F < 0 as a float).
+__device__ __forceinline__ float supply_log_entry_f(const DiodeParams& p, float t0, float t1, float t2, float F) {
+  const float LF = logf(-F);
+  if (!p.image_charge) return 2.0f * LF - t0;
+  float l = t2 * (-F), ll = t1 + LF;
+  if (l > 1.0f) { l = 1.0f; ll = 0.0f; }
+  const float ty = 1.0f + l * ((1.0f / 9.0f) - (1.0f / 18.0f) * ll);
+  return (2.0f * LF - 2.0f * logf(ty)) - t0;
+}
+
 // supply_log_tab in FP32 (F < 0 as a float).
 __device__ __forceinline__ float supply_log_f(const DiodeParams& p, const double* __restrict__ wtab,
                                               int cell, float F) {
   const double* t = wtab + 3 * (p.work_off + cell);
-  const float t0 = (float)t[0];
-  const float LF = logf(-F);
-  if (!p.image_charge) return 2.0f * LF - t0;
-  float l = (float)t[2] * (-F), ll = (float)t[1] + LF;
-  if (l > 1.0f) { l = 1.0f; ll = 0.0f; }
-  const float ty = 1.0f + l * ((1.0f / 9.0f) - (1.0f / 18.0f) * ll);
-  return (2.0f * LF - 2.0f * logf(ty)) - t0;
+  return supply_log_entry_f(p, (float)t[0], (float)t[1], (float)t[2], F);
+}
+
+// The FP32 chains' target at (x, y) given as FP32 nm offsets, any model.
+__device__ __forceinline__ float supply_log_xy_f(const DiodeParams& p, const double* __restrict__ wtab,
+                                                 float x, float y, float F) {
+  if (p.work_model == 1) return supply_log_f(p, wtab, work_cell_f(p, x, y), F);
+  const double X = p.org_x + (double)x * 1.0e-9, Y = p.org_y + (double)y * 1.0e-9;
+  const int cell = work_cell(p, X, Y);
+  if (cell >= 0) return supply_log_f(p, wtab, cell, F);
+  const double phi = gaussian_work(p, p.work_data, X, Y);
+  const double l2 = c_k.l_const / (phi * phi);
+  return supply_log_entry_f(p, (float)log(phi), (float)log(l2), (float)l2, F);
 }
 
 // ---- cathode z = 0 field, planar ----------------------------------------------------
@@ -487,16 +517,25 @@ __global__ void k_supply_reduce(const DiodeParams* __restrict__ P, DiodeDyn* __r
                                 const double* __restrict__ qx, const double* __restrict__ qy,
                                 const double* __restrict__ qw, const double* __restrict__ qF,
                                 const double* __restrict__ qfx, const double* __restrict__ qfy,
-                                const double* __restrict__ work) {
+                                const double* __restrict__ work, const int* __restrict__ step_ptr) {
   __shared__ double red[256];
   const int d = blockIdx.x;
   const DiodeParams& p = P[d];
   if (!p.active || !p.emission) return;
   DiodeDyn& y = Dy[d];
+  if (*step_ptr - y.step_offset <= p.emit_delay) {   // the emitter is not on yet (:181)
+    if (threadIdx.x == 0) {
+      y.N_sup = 0.0; y.chains = y.chains_capped = y.chains_failed = 0;
+      y.mh_acc = y.mh_rej = y.mh_done = 0;
+      y.F_avg_z = 0.0; y.df_avg = 0.0;
+    }
+    return;
+  }
   const int npt = (p.geometry == RD_G_TIP) ? 10000 : p.quad_n * p.quad_n;
-  double acc = 0.0;
+  double acc = 0.0, fsum = 0.0;
   for (int k = threadIdx.x; k < npt; k += blockDim.x) {
     double F = qF[p.q_off + k];
+    fsum += F;
     if (p.geometry == RD_G_TIP) {   // Field_normal :105-112
       double nx, ny, nz;
       tip_normal(p, qx[p.q_off + k], qy[p.q_off + k], &nx, &ny, &nz);
@@ -513,8 +552,11 @@ __global__ void k_supply_reduce(const DiodeParams* __restrict__ P, DiodeDyn* __r
     }
   }
   double N_sup = block_sum(acc, red);
+  __syncthreads();
+  const double F_sum = block_sum(fsum, red);
   if (threadIdx.x == 0) {
     y.N_sup = N_sup;
+    y.F_avg_z = p.geometry == RD_G_TIP ? 0.0 : F_sum / npt;   // F_avg, :644-651 (planar)
     long nr;
     if (p.geometry == RD_G_TIP) {
       nr = nint_d(N_sup);
@@ -658,7 +700,7 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
           ok = 1; F = Fz; X = x; Y = y;
           if (lane == 0) {
             cs.fx[k] = fx; cs.fy[k] = fy;
-            cs.fsup[k] = supply_log_f(p, wtab, work_cell_f(p, fx, fy), (float)Fz);
+            cs.fsup[k] = supply_log_xy_f(p, wtab, fx, fy, (float)Fz);
           }
         }
       } else {
@@ -666,7 +708,7 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
         const double Fz = warp_field_planar_z0<PREC>(p, pool, n, x, y, kscale);
         if (Fz < 0.0) {
           ok = 1; F = Fz; X = x; Y = y;
-          sup = supply_log_tab(p, wtab, work_cell(p, x, y), Fz);
+          sup = supply_log_xy(p, wtab, x, y, Fz);
         }
       }
     }
@@ -737,7 +779,7 @@ __device__ __forceinline__ int mh_accept_one(const DiodeParams& p, ChainState& c
                                              double wx, double wy) {
   int a = 0;
   if (F < 0.0) {
-    const double sn = supply_log_tab(p, wtab, work_cell(p, wx, wy), F);
+    const double sn = supply_log_xy(p, wtab, wx, wy, F);
     const double sc = cs.sup[k];
     bool take = sn >= sc;
     if (!take) {
@@ -762,7 +804,7 @@ __device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState&
   int a = 0;
   const float Ff = (float)F;
   if (F < 0.0 && Ff < 0.0f) {
-    const float sn = supply_log_f(p, wtab, work_cell_f(p, wx, wy), Ff);
+    const float sn = supply_log_xy_f(p, wtab, wx, wy, Ff);
     const float sc = cs.fsup[k];
     bool take = sn >= sc;
     if (!take) {
@@ -909,7 +951,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
             cs.fx[k] = fwx[q]; cs.fy[k] = fwy[q];
             cs.x[k] = p.org_x + (double)fwx[q] * 1.0e-9;
             cs.y[k] = p.org_y + (double)fwy[q] * 1.0e-9;
-            cs.fsup[k] = supply_log_f(p, wtab, work_cell_f(p, fwx[q], fwy[q]), (float)F);
+            cs.fsup[k] = supply_log_xy_f(p, wtab, fwx[q], fwy[q], (float)F);
             float g1, g2;
             gauss2f(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
             cs.fgx[k] = g1; cs.fgy[k] = g2;
@@ -919,7 +961,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
         } else {
           if (F < 0.0 && p.init_rounds > 0) {
             cs.ok[k] = 1; cs.F[k] = F; cs.x[k] = wx[q]; cs.y[k] = wy[q];
-            cs.sup[k] = supply_log_tab(p, wtab, work_cell(p, wx[q], wy[q]), F);
+            cs.sup[k] = supply_log_xy(p, wtab, wx[q], wy[q], F);
             double g1, g2;
             gauss2(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
             cs.gx[k] = g1; cs.gy[k] = g2;
@@ -1227,10 +1269,12 @@ k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, 
        const int* __restrict__ step_ptr, EventLog ev) {
   __shared__ int warp_tot[32];
   __shared__ int s_base;
+  __shared__ double warp_df[32];
   const int d = blockIdx.x;
   const DiodeParams& p = P[d];
-  if (!p.active || !p.emission) return;
+  if (!p.active || !p.emission || p.mh_serial) return;   // serial diodes emit in k_mh_serial
   DiodeDyn& y = Dy[d];
+  double df_sum = 0.0;   // sum of the candidates' escape probabilities (df_avg, :354)
   const int step = *step_ptr - y.step_offset;
   const int M = y.chains;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
@@ -1254,6 +1298,7 @@ k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, 
           double sq = sqrt(p.tip_phi);   // Escape_Prob_Tip :1734-1758
           Df = exp(((c_k.b_FN * ((sq * sq) * sq)) * fn_v_y(F, p.tip_phi, p.image_charge)) / fabs(F));
         }
+        df_sum += Df;
         if (F < 0.0 && u1 <= Df) {
           e = 1;
           double nx, ny, nz;
@@ -1267,6 +1312,7 @@ k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, 
         double phi = work_at(p, work, X, Y, &sec);
         double D = ok ? fn_escape_log(F, phi, p.image_charge) : -1.79769313486231570e308;
         if (F >= 0.0) D = -1.79769313486231570e308;
+        df_sum += exp(D);
         if (log(u1) <= D) { e = 1; Z = 1.0 * c_k.length_scale; }
       }
     }
@@ -1303,7 +1349,13 @@ k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, 
     if (tid == 0) s_base += tot;
     __syncthreads();
   }
+  for (int o = 16; o > 0; o >>= 1) df_sum += __shfl_xor_sync(0xffffffffu, df_sum, o);
+  if (lane == 0) warp_df[w] = df_sum;
+  __syncthreads();
   if (tid == 0) {
+    double s = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += warp_df[q];
+    y.df_avg = y.N_sup > 0.0 ? s / y.N_sup : 0.0;
     int tot = s_base;
     int room = p.cap - n0;
     emitted = tot < room ? tot : (room > 0 ? room : 0);
@@ -1318,6 +1370,167 @@ k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, 
 }
 
 }  // namespace
+
+// ---- serial MH sampler (mh_batch = .false.) ---------------------------------------------
+// F_z at one cathode point from the diode's first n particles, summed by the
+// whole block (every thread gets the total).
+template <int PREC>
+__device__ double block_field_z0(const DiodeParams& p, const Pool& pool, int n, double px, double py,
+                                 double kscale, double* red) {
+  const int tid = threadIdx.x, nt = blockDim.x, off = p.off;
+  const int nic = p.image_charge ? p.N_ic_max : 0;
+  double s;
+  if (PREC == 1) {
+    const float4 pp = z0_point(p, px, py);
+    const float dnm = (float)(p.d * 1.0e9);
+    float hi = 0.f, lo = 0.f;
+    for (int j = tid; j < n; j += nt) {
+      float4 h = pool.zk_hi[off + j], l = pool.zk_lo[off + j];
+      two_sum_acc(hi, lo, nic == 0 ? z0_tile_f32<true>(&h, &l, 1, pp, 0, dnm)
+                                   : z0_tile_f32<false>(&h, &l, 1, pp, nic, dnm));
+    }
+    s = (double)hi + (double)lo;
+  } else {
+    s = 0.0;
+    for (int j = tid; j < n; j += nt) {
+      rd_d4 pj = make_d4(pool.x[off + j], pool.y[off + j], pool.z[off + j], pool.q[off + j]);
+      s += z0_tile_f64(&pj, 1, px, py, nic, p.d, c_k.L2);
+    }
+  }
+  return z0_finish<PREC>(p, block_sum(s, red), kscale);
+}
+
+// The serial branch of Do_Field_Emission_Planar_rectangle (:322-333, 338-383)
+// with Metropolis_Hastings_rectangle_J (:1122-1265): one block per serial
+// diode runs its candidates' chains one after another.  Each chain starts
+// from uniform draws until F_z < 0, makes mh_jumps jumps (the warm-up quarter
+// with 10 % of the emitter as the step, then MH_std), updates MH_std once from
+// its own acceptance rate after the warm-up, and its electron, if the escape
+// test passes, is added before the next chain starts, so later chains see it.
+// Same Philox counters as the batched sampler; every thread follows the same
+// control flow (the field sum is block-reduced and broadcast).
+template <int PREC>
+__global__ void __launch_bounds__(256)
+k_mh_serial(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
+            const double* __restrict__ work, const double* __restrict__ wtab,
+            const int* __restrict__ step_ptr, double kscale, EventLog ev) {
+  __shared__ double red[256];
+  const int d = blockIdx.x;
+  const DiodeParams& p = P[d];
+  if (!p.active || !p.emission || !p.mh_serial || p.geometry != RD_G_PLANAR) return;
+  DiodeDyn& y = Dy[d];
+  const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
+  const int M = y.chains, n0 = y.n, id0 = y.nrID;
+  const int ndim = p.mh_jumps, ndim_first = (ndim + 2) / 4;
+  int n = n0, emitted = 0, dropped = 0, failed = 0;
+  double mhs = y.MH_std, a_rate = y.a_rate, df_sum = 0.0;
+  for (int c = 0; c < M; ++c) {
+    double cx = p.em_x0, cy = p.em_y0, F = 1.0;
+    bool found = false;
+    for (int r = 0; r < p.init_rounds && !found; ++r) {
+      double u1, u2;
+      rng2(p.seed, (uint32_t)c, (uint32_t)r, step, RNG_INIT, &u1, &u2);
+      cx = u1 * p.em_Lx + p.em_x0;
+      cy = u2 * p.em_Ly + p.em_y0;
+      F = block_field_z0<PREC>(p, pool, n, cx, cy, kscale, red);
+      found = F < 0.0;
+    }
+    double D = -1.79769313486231570e308, Fout = 1.0;
+    if (!found) {
+      cx = p.em_x0; cy = p.em_y0;
+      ++failed;
+    } else {
+      Fout = F;
+      double sup_cur = supply_log_xy(p, wtab, cx, cy, F);
+      int ja = 0, jr = 0;
+      double sx = p.em_Lx * 0.10, sy = p.em_Ly * 0.10;
+      for (int i = 1; i <= ndim; ++i) {
+        if (i > ndim_first) { sx = p.em_Lx * mhs; sy = p.em_Ly * mhs; }
+        double g1, g2;
+        gauss2(p.seed, (uint32_t)c, (uint32_t)i, step, &g1, &g2);
+        double wx = g1 * sx + cx, wy = g2 * sy + cy;
+        const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+        if (wx > hx) wx = hx - (wx - hx); else if (wx < p.em_x0) wx = (p.em_x0 - wx) + p.em_x0;
+        if (wy > hy) wy = hy - (wy - hy); else if (wy < p.em_y0) wy = (p.em_y0 - wy) + p.em_y0;
+        const double Fw = block_field_z0<PREC>(p, pool, n, wx, wy, kscale, red);
+        if (Fw >= 0.0) { if (i > ndim_first) ++jr; continue; }
+        const double sn = supply_log_xy(p, wtab, wx, wy, Fw);
+        bool take = sn >= sup_cur;
+        if (!take) {
+          double u1, u2;
+          rng2(p.seed, (uint32_t)c, (uint32_t)i, step, RNG_ACCEPT, &u1, &u2);
+          take = log(u1) <= sn - sup_cur;
+        }
+        if (take) {
+          cx = wx; cy = wy; sup_cur = sn; Fout = Fw;
+          if (i > ndim_first) ++ja;
+        } else if (i > ndim_first) {
+          ++jr;
+        }
+      }
+      if (ja + jr > 0) {   // MH_std_update once per chain (:1251-1254, :603-612)
+        a_rate = (double)ja / (double)(jr + ja);
+        mhs = mhs * exp(0.025 * (a_rate - 0.35));
+        if (mhs > p.mh_hi) mhs = p.mh_hi; else if (mhs < p.mh_lo) mhs = p.mh_lo;
+      }
+      D = fn_escape_log(Fout, work_at(p, work, cx, cy, nullptr), p.image_charge);
+    }
+    if (Fout >= 0.0) D = -1.79769313486231570e308;
+    df_sum += exp(D);
+    double u1, u2;
+    rng2(p.seed, (uint32_t)c, 0u, step, RNG_EMIT, &u1, &u2);
+    if (log(u1) <= D) {
+      if (n < p.cap) {   // Add_Particle (src/mod_pair.F90:29-159), visible to the next chains
+        if (threadIdx.x == 0) {
+          const int gi = p.off + n;
+          const double X = cx, Y = cy, Z = 1.0 * c_k.length_scale;
+          int sec = 1;
+          work_at(p, work, X, Y, &sec);
+          double ex, ey, ez;
+          vacuum_field(p, X, Y, Z, &ex, &ey, &ez);
+          const double qm = (-1.0 * c_k.q0) / (1.0 * c_k.m0);
+          pool.x[gi] = X; pool.y[gi] = Y; pool.z[gi] = Z;
+          pool.vx[gi] = 0.0; pool.vy[gi] = 0.0; pool.vz[gi] = 0.0;
+          pool.ax[gi] = pool.bx[gi] = pool.cx[gi] = qm * ex;
+          pool.ay[gi] = pool.by[gi] = pool.cy[gi] = qm * ey;
+          pool.az[gi] = pool.bz[gi] = pool.cz[gi] = qm * ez;
+          pool.q[gi] = -1.0 * c_k.q0;
+          pool.m[gi] = 1.0 * c_k.m0;
+          pool.species[gi] = 1;
+          pool.id[gi] = id0 + emitted;
+          pool.step0[gi] = (int)step;
+          pool.section[gi] = sec;
+          pool.mask[gi] = 1;
+          float4 h, l;   // its cathode pack, for the FP32 field sums of the next chains
+          split_nm(X, p.org_x, &h.x, &l.x);
+          split_nm(Y, p.org_y, &h.y, &l.y);
+          const float zf = (float)(Z * 1.0e9), qf = -1.0f;
+          pool.zk_hi[gi] = make_float4(h.x, h.y, fmaxf(zf * zf, 1e-20f), qf * zf);
+          pool.zk_lo[gi] = make_float4(l.x, l.y, zf, qf);
+          log_event(ev, X, Y, Z, 0.0, 0.0, 0.0, d, RD_EVENT_EMIT, sec, id0 + emitted, 1, (int)step);
+        }
+        __threadfence_block();
+        __syncthreads();
+        ++n;
+        ++emitted;
+      } else {
+        ++dropped;
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    y.n = n;
+    y.nrID = id0 + emitted;
+    y.emitted_step = emitted;
+    y.dropped_step = dropped;
+    y.emitted_total += emitted;
+    y.dropped_total += dropped;
+    y.chains_failed = failed;
+    y.MH_std = mhs;
+    y.a_rate = a_rate;
+    y.df_avg = y.N_sup > 0.0 ? df_sum / y.N_sup : 0.0;
+  }
+}
 
 // ---- launch wrappers --------------------------------------------------------------------------
 cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st,
@@ -1346,8 +1559,8 @@ cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const Diode
 cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                     const double* qx, const double* qy, const double* qw,
                                     const double* qF, const double* qfx, const double* qfy,
-                                    const double* work) {
-  k_supply_reduce<<<nslots, 256, 0, st>>>(P, Dy, qx, qy, qw, qF, qfx, qfy, work);
+                                    const double* work, const int* step_ptr) {
+  k_supply_reduce<<<nslots, 256, 0, st>>>(P, Dy, qx, qy, qw, qF, qfx, qfy, work, step_ptr);
   return cudaGetLastError();
 }
 
@@ -1382,6 +1595,14 @@ cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, Di
                            const Pool& pool, const ChainState& cs, const int* ch_off,
                            const double* work, const int* step_ptr, const EventLog& ev) {
   k_emit<<<nslots, 1024, 0, st>>>(P, Dy, pool, cs, ch_off, work, step_ptr, ev);
+  return cudaGetLastError();
+}
+
+cudaError_t rd_launch_mh_serial(int prec, int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                                const Pool& pool, const double* work, const double* wtab,
+                                const int* step_ptr, double kscale, const EventLog& ev) {
+  if (prec == 1) k_mh_serial<1><<<nslots, 256, 0, st>>>(P, Dy, pool, work, wtab, step_ptr, kscale, ev);
+  else k_mh_serial<0><<<nslots, 256, 0, st>>>(P, Dy, pool, work, wtab, step_ptr, kscale, ev);
   return cudaGetLastError();
 }
 

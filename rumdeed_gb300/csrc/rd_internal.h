@@ -56,7 +56,8 @@ struct DiodeParams {
   int quad_n;            // supply quadrature points per dimension (planar)
   int q_off;             // offset of this diode's quadrature points in the quad table
   int work_nx, work_ny, work_off;
-  int pad0;
+  int work_model;        // 1 checkerboard, 2 Gaussian, 4 Voronoi (Read_work_function types)
+  const double* work_data;   // this diode's work-function parameters (device)
   unsigned long long seed;
   double V, d, E_z, dt, dt2;
   double em_x0, em_y0, em_Lx, em_Ly;
@@ -67,6 +68,10 @@ struct DiodeParams {
   // FP32 frame of the planar emitter (nm, relative to its centre): half widths
   // rounded toward zero (chains stay inside) and full widths
   float em_hx, em_hy, em_wx, em_wy;
+  int emit_delay;        // the emitter emits from step emit_delay + 1 on
+  int mh_serial;         // 1: serial MH sampler (k_mh_serial)
+  int planes_n;          // measurement planes (Check_Planes)
+  double planes_z[10];
 };
 
 // Dynamic per-diode state (device resident, updated by kernels).
@@ -86,6 +91,7 @@ struct DiodeDyn {
   long long steps_done;
   double ramo_current;
   double MH_std, a_rate, residual, N_sup;
+  double F_avg_z, df_avg;   // field.dt quantities of the last emission
   double avg_vel[3];
 };
 

@@ -78,7 +78,7 @@ __device__ __forceinline__ int plan_ni(const DiodeParams& p, const DiodeDyn& y, 
     case PM_FIELD: return npts[d];
     case PM_SUPPLY_PLANAR: return (p.emission && p.geometry == RD_G_PLANAR) ? p.quad_n * p.quad_n : 0;
     case PM_SUPPLY_TIP: return (p.emission && p.geometry == RD_G_TIP) ? 10000 : 0;
-    case PM_MH: return p.emission ? y.chains : 0;
+    case PM_MH: return (p.emission && !p.mh_serial) ? y.chains : 0;   // serial diodes: k_mh_serial
     default: return nj;
   }
 }
@@ -217,15 +217,22 @@ k_position(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool po
       const double dt = p.dt, dt2 = p.dt2;
       double ax = pool.ax[gi], ay = pool.ay[gi], az = pool.az[gi];
       double bx = pool.bx[gi], by = pool.by[gi], bz = pool.bz[gi];
+      const double z_prev = pool.z[gi];
       double x = (pool.x[gi] + pool.vx[gi] * dt) + ((1.0 / 6.0) * (4.0 * ax - bx)) * dt2;
       double y = (pool.y[gi] + pool.vy[gi] * dt) + ((1.0 / 6.0) * (4.0 * ay - by)) * dt2;
-      double z = (pool.z[gi] + pool.vz[gi] * dt) + ((1.0 / 6.0) * (4.0 * az - bz)) * dt2;
+      double z = (z_prev + pool.vz[gi] * dt) + ((1.0 / 6.0) * (4.0 * az - bz)) * dt2;
       pool.x[gi] = x; pool.y[gi] = y; pool.z[gi] = z;
       pool.cx[gi] = bx; pool.cy[gi] = by; pool.cz[gi] = bz;
       pool.bx[gi] = ax; pool.by[gi] = ay; pool.bz[gi] = az;
       pool.ax[gi] = 0.0; pool.ay[gi] = 0.0; pool.az[gi] = 0.0;
       DiodeDyn& yy = Dy[d];
       const int step = *step_ptr - yy.step_offset;
+      for (int k = 0; k < p.planes_n; ++k) {   // Check_Planes (src/mod_verlet.F90:343-367)
+        const double zp = p.planes_z[k];
+        if (zp > 0.0 && z > zp && z_prev < zp)
+          log_event(ev, x, y, z, pool.vx[gi], pool.vy[gi], pool.vz[gi], d, RD_EVENT_PLANE + k,
+                    pool.section[gi], pool.id[gi], pool.species[gi], step);
+      }
       if (z < 0.0) mark_remove(p, yy, pool, i, gi, 2, ev, d, step);
       else if (z > p.d) mark_remove(p, yy, pool, i, gi, 1, ev, d, step);
       if (p.geometry == RD_G_TIP && tip_eta(p, x, y, z) < p.eta_1) mark_remove(p, yy, pool, i, gi, 2, ev, d, step);

@@ -10,8 +10,10 @@
 // out/absorbed{,_top,_bot}.dt (src/mod_pair.F90:789-804) and
 // out/ramo_current.dt (src/mod_pair.F90:811-835) with the reference's Fortran
 // edit descriptors, and the per-event binary files out/density_emit.bin,
-// out/density_emit_elec.bin (src/mod_pair.F90:89-123) and
-// out/density_absorb_{top,bot}.bin (:241-257) from the engine's event log.
+// out/density_emit_elec.bin (src/mod_pair.F90:89-123),
+// out/density_absorb_{top,bot}.bin (:241-257) and out/planes-<k>.bin
+// (Check_Planes, src/mod_verlet.F90:343-367) from the engine's event log, and
+// out/field.dt (src/mod_field_emission_v2.F90:389-390).
 //
 // Supported decks: EMISSION_MODE = 10 (planar field emission, one
 // rectangular emitter, EMITTERS_TYPE 2) and EMISSION_MODE = 3 (hyperboloid
@@ -210,6 +212,10 @@ int main(int argc, char** argv) {
   dc.emission = 1;
   dc.mh_jumps = (int)get(gb, "MH_JUMPS", 0, 0.0);
   dc.seed = (unsigned long long)get(gb, "SEED", 0, 20261203.0);
+  dc.emitter_delay = (int)get(in, "EMITTERS_DELAY", 0, 0.0);
+  dc.planes_N = (int)get(in, "PLANES_N", 0, 0.0);
+  if (dc.planes_N < 0 || dc.planes_N > 10) { std::fprintf(stderr, "rd_main: planes_N must be in [0, 10]\n"); return 2; }
+  for (int k = 0; k < dc.planes_N; ++k) dc.planes_z[k] = get(in, "PLANES_Z", k, -1.0) * length_scale;
   std::vector<double> work;
   if (mode == 10) {
     dc.geometry = RD_GEOM_PLANAR;
@@ -218,21 +224,44 @@ int main(int argc, char** argv) {
     dc.emitter_dim[1] = get(in, "EMITTERS_DIM", 1, 0.0) * length_scale;
     dc.emitter_pos[0] = get(in, "EMITTERS_POS", 0, 0.0) * length_scale;
     dc.emitter_pos[1] = get(in, "EMITTERS_POS", 1, 0.0) * length_scale;
+    // Read_work_function (src/mod_work_function.F90:53-152): 1 checkerboard
+    // (y_num x_num, then the matrix), 2 Gaussian (base, count, then A x y sx sy
+    // per line), 4 Voronoi (count, then x y phi section per line)
     FILE* wf = std::fopen("work", "r");
     if (!wf) { std::fprintf(stderr, "RUMDEED: Failed to open file work. ABORTING\n"); return 2; }
-    int type = 0, ny = 0, nx = 0;
-    if (std::fscanf(wf, "%d %d %d", &type, &ny, &nx) != 3 || type != 1 || nx < 1 || ny < 1) {
-      std::fprintf(stderr, "rd_main: only the checkerboard work function (type 1) is on this path\n");
+    auto next = [&](double* v) {
+      char tok[64];
+      if (std::fscanf(wf, "%63s", tok) != 1) return false;
+      *v = to_double(tok);
+      return true;
+    };
+    double t = 0.0, a = 0.0, b = 0.0;
+    if (!next(&t)) { std::fprintf(stderr, "rd_main: empty work file\n"); return 2; }
+    const int type = (int)t;
+    int nx = 1, ny = 1, nvals = 0;
+    if (type == 1) {
+      if (!next(&a) || !next(&b)) { std::fprintf(stderr, "rd_main: short work file\n"); return 2; }
+      ny = (int)a; nx = (int)b; nvals = nx * ny;
+    } else if (type == 2) {
+      if (!next(&a) || !next(&b)) { std::fprintf(stderr, "rd_main: short work file\n"); return 2; }
+      work.push_back(a);   // base
+      nx = (int)b; nvals = 5 * nx;
+    } else if (type == 4) {
+      if (!next(&a)) { std::fprintf(stderr, "rd_main: short work file\n"); return 2; }
+      nx = (int)a; nvals = 4 * nx;
+    } else {
+      std::fprintf(stderr, "rd_main: work function type %d is not on this path (1, 2 or 4)\n", type);
       return 2;
     }
-    work.resize((size_t)nx * ny);
-    for (auto& v : work) {
-      char tok[64];
-      if (std::fscanf(wf, "%63s", tok) != 1) { std::fprintf(stderr, "rd_main: short work file\n"); return 2; }
-      v = to_double(tok);
+    if (nx < 1 || ny < 1) { std::fprintf(stderr, "rd_main: bad work file sizes\n"); return 2; }
+    for (int k = 0; k < nvals; ++k) {
+      double v;
+      if (!next(&v)) { std::fprintf(stderr, "rd_main: short work file\n"); return 2; }
+      work.push_back(v);
     }
     std::fclose(wf);
-    dc.work_nx = nx; dc.work_ny = ny; dc.work = work.data();   // row 0 = first row of the file
+    dc.work_model = type;
+    dc.work_nx = nx; dc.work_ny = ny; dc.work = work.data();   // checkerboard row 0 = first row of the file
   } else {
     dc.geometry = RD_GEOM_TIP;
     dc.tip_dim[0] = get(in, "EMITTERS_DIM", 0, 0.0) * length_scale;
@@ -245,11 +274,14 @@ int main(int argc, char** argv) {
   if (print_only) {   // the deck as read, one "key value" line each, then stop
     std::printf("geometry %d\nV_s %.17g\ngap %.17g\ntime_step %.17g\nsteps %d\nimage_charge %d\n"
                 "N_ic_max %d\ncapacity %d\nseed %llu\nemitter_pos %.17g %.17g\nemitter_dim %.17g %.17g\n"
-                "work %d x %d\ntip_dim %.17g %.17g %.17g\nE14.6 %s\nES12.4 %s\n",
+                "work %d x %d\nwork_model %d\ntip_dim %.17g %.17g %.17g\nE14.6 %s\nES12.4 %s\n"
+                "emitter_delay %d\nplanes %d\n",
                 dc.geometry, dc.V_s, dc.gap, dc.time_step, steps, dc.image_charge, dc.N_ic_max,
                 dc.capacity, dc.seed, dc.emitter_pos[0], dc.emitter_pos[1], dc.emitter_dim[0],
-                dc.emitter_dim[1], dc.work_ny, dc.work_nx, dc.tip_dim[0], dc.tip_dim[1], dc.tip_dim[2],
-                fmt_E(dt / time_scale, 14, 6).c_str(), fmt_ES(dt / time_scale, 12, 4).c_str());
+                dc.emitter_dim[1], dc.work_ny, dc.work_nx, dc.work_model, dc.tip_dim[0], dc.tip_dim[1], dc.tip_dim[2],
+                fmt_E(dt / time_scale, 14, 6).c_str(), fmt_ES(dt / time_scale, 12, 4).c_str(), dc.emitter_delay,
+                dc.planes_N);
+    for (int k = 0; k < dc.planes_N; ++k) std::printf("plane_z %.17g\n", dc.planes_z[k]);
     for (double w : work) std::printf("work_value %.17g\n", w);
     return 0;
   }
@@ -278,7 +310,17 @@ int main(int argc, char** argv) {
   FILE* b_emit_elec = std::fopen("out/density_emit_elec.bin", "wb");
   FILE* b_abs_top = std::fopen("out/density_absorb_top.bin", "wb");
   FILE* b_abs_bot = std::fopen("out/density_absorb_bot.bin", "wb");
-  if (!f_emit || !f_abs || !f_top || !f_bot || !f_ramo || !b_emit || !b_emit_elec || !b_abs_top || !b_abs_bot) {
+  FILE* f_field = std::fopen("out/field.dt", "w");
+  FILE* b_planes[10] = {};
+  for (int k = 0; k < dc.planes_N; ++k)
+    if (dc.planes_z[k] > 0.0) {   // out/planes-<k>.bin, src/main.F90:727-738
+      char name[64];
+      std::snprintf(name, sizeof name, "out/planes-%d.bin", k + 1);
+      b_planes[k] = std::fopen(name, "wb");
+      if (!b_planes[k]) { std::fprintf(stderr, "rd_main: cannot write %s\n", name); return 2; }
+    }
+  if (!f_emit || !f_abs || !f_top || !f_bot || !f_ramo || !b_emit || !b_emit_elec || !b_abs_top || !b_abs_bot ||
+      !f_field) {
     std::fprintf(stderr, "rd_main: cannot write under out/\n");
     return 2;
   }
@@ -311,10 +353,15 @@ int main(int argc, char** argv) {
         std::fwrite(p3, sizeof(double), 3, b_emit_elec);
         std::fwrite(i2, sizeof(int), 2, b_emit_elec);
       } else {
+        // absorb_top and planes: x, y, v, emitter, section, id; absorb_bot: x, y, emitter, section, id
         const int i3[3] = {emitter, r.section, r.id};
-        FILE* bf = r.kind == RD_EVENT_ABSORB_TOP ? b_abs_top : b_abs_bot;
+        FILE* bf = nullptr;
+        if (r.kind == RD_EVENT_ABSORB_TOP) bf = b_abs_top;
+        else if (r.kind == RD_EVENT_ABSORB_BOT) bf = b_abs_bot;
+        else if (r.kind >= RD_EVENT_PLANE && r.kind < RD_EVENT_PLANE + 10) bf = b_planes[r.kind - RD_EVENT_PLANE];
+        if (!bf) continue;
         std::fwrite(p3, sizeof(double), 2, bf);
-        if (r.kind == RD_EVENT_ABSORB_TOP) std::fwrite(r.vel, sizeof(double), 3, bf);
+        if (r.kind != RD_EVENT_ABSORB_BOT) std::fwrite(r.vel, sizeof(double), 3, bf);
         std::fwrite(i3, sizeof(int), 3, bf);
       }
     }
@@ -335,6 +382,14 @@ int main(int argc, char** argv) {
       for (long long v : cols) t += "  " + fmt_I(v, 8);
       std::fprintf(f, "%s\n", t.c_str());
     };
+    // field.dt: "(i8, tr2, E16.8, tr2, ...)" step, F_avg(1:3), N_sup, df_avg, a_rate, MH_std
+    // (written by the emission, src/mod_field_emission_v2.F90:389-390)
+    if (mode == 10 && step > dc.emitter_delay) {
+      std::string fl = fmt_I(step, 8);
+      for (double v : {c.F_avg[0], c.F_avg[1], c.F_avg[2], c.N_sup, c.df_avg, c.a_rate, c.MH_std})
+        fl += "  " + fmt_E(v, 16, 8);
+      std::fprintf(f_field, "%s\n", fl.c_str());
+    }
     absorbed(f_abs, c.absorbed_top_step + c.absorbed_bot_step, false);
     absorbed(f_top, c.absorbed_top_step, true);
     absorbed(f_bot, c.absorbed_bot_step, false);
@@ -362,7 +417,9 @@ int main(int argc, char** argv) {
       ++progress;
     }
   }
-  for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo, b_emit, b_emit_elec, b_abs_top, b_abs_bot}) std::fclose(f);
+  for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo, b_emit, b_emit_elec, b_abs_top, b_abs_bot, f_field})
+    std::fclose(f);
+  for (FILE* f : b_planes) if (f) std::fclose(f);
   rd_engine_destroy(e);
   if (lost_total) std::printf("RUMDEED: %lld event records did not fit the event log\n", lost_total);
   std::printf("RUMDEED: Main loop finished\n");

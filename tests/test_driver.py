@@ -25,7 +25,9 @@ DECK = """&INPUT
   EMITTERS_DIM(1:3, 1) = 1000.0d0, 1000.0d0, 0.0d0,
   EMITTERS_POS(1:3, 1) = -500.0d0, -500.0d0, 0.0d0,
   EMITTERS_TYPE(1) = 2,
-  EMITTERS_DELAY(1) = 0,
+  EMITTERS_DELAY(1) = 2,
+  PLANES_N = 2,
+  PLANES_Z = 200.0d0, 600.0d0,
 /
 &GB300
   MAX_PARTICLES = 3000, SEED = 11, MH_JUMPS = 40
@@ -64,10 +66,27 @@ def test_deck_is_read_like_the_reference(driver, tmp_path):
     assert [float(x) for x in kv["emitter_pos"][0].split()] == [-500.0 * 1.0e-9] * 2
     assert [float(x) for x in kv["emitter_dim"][0].split()] == [1000.0 * 1.0e-9] * 2
     assert kv["work"] == ["2 x 2"]
+    assert kv["emitter_delay"] == ["2"] and kv["planes"] == ["2"]
+    assert [float(z) for z in kv["plane_z"]] == [200.0 * 1.0e-9, 600.0 * 1.0e-9]
     assert [float(x) for x in kv["work_value"]] == [2.0, 2.2, 2.4, 2.6]
     # Fortran edit descriptors: E14.6 and ES12.4
     assert kv["E14.6"] == ["  0.250000E-03"]
     assert kv["ES12.4"] == ["  2.5000E-04"]
+
+
+def test_gaussian_and_voronoi_work_files_are_read(driver, tmp_path):
+    (tmp_path / "input").write_text(DECK)
+    (tmp_path / "work").write_text("2\n4.5\n2\n-0.5 10 -20 30 40\n0.25 0 0 5 5\n")
+    out = subprocess.run([driver, "--print-config", str(tmp_path)], capture_output=True, text=True,
+                         check=True).stdout
+    vals = [float(l.split()[1]) for l in out.splitlines() if l.startswith("work_value")]
+    assert "work_model 2" in out and "work 1 x 2" in out
+    assert vals == [4.5, -0.5, 10, -20, 30, 40, 0.25, 0, 0, 5, 5]
+    (tmp_path / "work").write_text("4\n2\n0.25 0.5 2.0 1\n0.75 0.5 3.0 2\n")
+    out = subprocess.run([driver, "--print-config", str(tmp_path)], capture_output=True, text=True,
+                         check=True).stdout
+    vals = [float(l.split()[1]) for l in out.splitlines() if l.startswith("work_value")]
+    assert "work_model 4" in out and vals == [0.25, 0.5, 2.0, 1, 0.75, 0.5, 3.0, 2]
 
 
 def test_deck_outside_the_path_is_refused(driver, tmp_path):
@@ -91,7 +110,7 @@ def test_driver_run_matches_python_binding(driver, tmp_path, rg):
     d = eng.add_diode(V_s=2.0e3, gap=1000 * 1.0e-9, time_step=2.5e-4 * 1.0e-12, image_charge=True,
                       N_ic_max=0, capacity=3000, emitter_pos=(-500.0 * 1.0e-9, -500.0 * 1.0e-9),
                       emitter_dim=(1000.0 * 1.0e-9, 1000.0 * 1.0e-9), work=[[2.0, 2.2], [2.4, 2.6]], emission=True,
-                      mh_jumps=40, seed=11)
+                      mh_jumps=40, seed=11, emitter_delay=2, planes_z=(200.0 * 1.0e-9, 600.0 * 1.0e-9))
     for step in range(1, 13):
         eng.step(step)
         c = d.counters()
@@ -120,6 +139,14 @@ def test_driver_run_matches_python_binding(driver, tmp_path, rg):
     assert np.all(de["species"] == 1) and np.all(de["emit"] == 1) and np.all(np.diff(de["id"]) > 0)
     np.testing.assert_array_equal(de["pos"], dl["pos"])
     assert np.all(dt["vel"][:, 2] > 0.0) if len(dt) else True              # anode hits move up
+    # field.dt: one line per step the emitter is on, F_avg_z < 0, N_sup as in the counters
+    fd = np.loadtxt(out / "field.dt")
+    assert fd.shape == (12 - 2, 8) and np.all(fd[:, 0] == np.arange(3, 13)) and np.all(fd[:, 3] < 0)
+    assert emitted[0, 2] == emitted[1, 2] == 0 and emitted[2:, 2].sum() > 0  # EMITTERS_DELAY = 2
+    # planes-1.bin / planes-2.bin: 52-byte records of upward crossings of 200 nm / 600 nm
+    p1 = np.fromfile(out / "planes-1.bin", dtype=rec_top)
+    p2 = np.fromfile(out / "planes-2.bin", dtype=rec_top)
+    assert len(p1) >= len(p2) and np.all(p1["vel"][:, 2] > 0) if len(p1) else True
 
 
 @pytest.mark.gpu

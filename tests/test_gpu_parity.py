@@ -213,6 +213,8 @@ def test_emission_fp64_matches_oracle_chain_for_chain(rg, orc):
     assert c["chains"] == o.s.last_chains
     assert c["MH_std"] == pytest.approx(o.s.MH_std, rel=1e-12)
     assert c["emitted_step"] == o.s.emitted_step > 0
+    assert c["F_avg"][2] == pytest.approx(o.s.F_avg_z, rel=1e-12) and c["F_avg"][2] < 0   # field.dt
+    assert c["df_avg"] == pytest.approx(o.s.df_avg, rel=1e-10)
     p = dio.particles()
     assert dio.n == o.n
     new = slice(n_before, dio.n)
@@ -292,3 +294,153 @@ def test_batch_equals_alone(rg, orc):
         np.testing.assert_array_equal(pa["pos"], pb["pos"])
         np.testing.assert_array_equal(pa["vel"], pb["vel"])
         solo.close(); mix.close()
+
+
+WORK_MODELS = {
+    # Gaussian: base 2.3 eV, a 0.6 eV dip and a 0.3 eV bump (nm)
+    2: [2.2, -0.6, -20.0, 10.0, 25.0, 15.0, 0.3, 30.0, -25.0, 10.0, 20.0],
+    # Voronoi: four sites (fractions of the emitter), phi, section
+    4: [0.2, 0.2, 1.6, 1.0, 0.8, 0.3, 1.7, 2.0, 0.4, 0.8, 1.65, 3.0, 0.7, 0.7, 2.4, 4.0],
+}
+
+
+@pytest.mark.parametrize("model", [2, 4])
+def test_emission_work_models_fp64_match_oracle(rg, orc, model):
+    """Gaussian and Voronoi work functions (mod_work_function.F90:214-254,
+    :533-571): supply integral, MH chains and emission of the FP64 GPU form
+    match the oracle electron for electron, sections included."""
+    rng = np.random.default_rng(21)
+    d, V, n0 = 500 * NM, 1.0e3, 120
+    pos = np.column_stack([rng.uniform(-60 * NM, 60 * NM, n0), rng.uniform(-60 * NM, 60 * NM, n0),
+                           rng.uniform(2 * NM, 490 * NM, n0)])
+    kw = dict(V_s=V, gap=d, capacity=4096, emitter_pos=(-50 * NM, -50 * NM), emitter_dim=(100 * NM, 100 * NM),
+              work=WORK_MODELS[model], work_model=model, emission=True, mh_jumps=40, max_chains=300,
+              quad_panels=8, quad_order=4, seed=5)
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=2, particle_capacity=8192, chain_capacity=4096)
+    dio = eng.add_diode(**kw)
+    dio.add_particles(pos)
+    o = orc.OracleDiode(cap=4096, V_s=V, d=d)
+    o.set_planar_emitter(-50 * NM, -50 * NM, 100 * NM, 100 * NM)
+    o.set_work_model(model, WORK_MODELS[model])
+    o.set_emission(True, seed=5, mh_jumps=40, max_chains=300, quad_panels=8, quad_order=4)
+    for p in pos:
+        o.add(p)
+    n_before = dio.n
+    eng.do_emission(1)
+    o.emission(1)
+    c = dio.counters()
+    assert c["N_sup"] == pytest.approx(o.s.N_sup, rel=1e-12)
+    assert c["emitted_step"] == o.s.emitted_step > 0
+    p = dio.particles()
+    new = slice(n_before, dio.n)
+    assert np.max(np.abs(p["pos"][new] - o.arr("pos")[new])) < 1e-12 * 100 * NM
+    np.testing.assert_array_equal(p["section"], o.iarr("section"))
+    if model == 4:
+        assert len(set(p["section"][new])) > 1      # several Voronoi cells emit
+    eng.close()
+    # the FP32-compensated form on the same deck: same supply, statistically the same emission
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=2, particle_capacity=8192, chain_capacity=4096)
+    dio = eng.add_diode(**kw)
+    dio.add_particles(pos)
+    eng.do_emission(1)
+    c32 = dio.counters()
+    assert c32["N_sup"] == pytest.approx(o.s.N_sup, rel=1e-5)
+    assert abs(c32["emitted_step"] - o.s.emitted_step) <= 4 * np.sqrt(o.s.emitted_step) + 2
+    eng.close()
+
+
+def test_emitter_delay_matches_oracle(rg, orc):
+    """EMITTERS_DELAY: the emitter emits from step delay + 1 on (fe_v2:181)."""
+    o = orc.OracleDiode(cap=4096, V_s=1.0e3, d=500 * NM)
+    o.set_planar_emitter(-50 * NM, -50 * NM, 100 * NM, 100 * NM, [[2.0]])
+    o.set_emission(True, seed=77, mh_jumps=40, max_chains=300, quad_panels=8, quad_order=4)
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=2, particle_capacity=8192, chain_capacity=4096)
+    dio = eng.add_diode(V_s=1.0e3, gap=500 * NM, capacity=4096, emitter_pos=(-50 * NM, -50 * NM),
+                        emitter_dim=(100 * NM, 100 * NM), work=[[2.0]], emission=True, mh_jumps=40,
+                        max_chains=300, quad_panels=8, quad_order=4, seed=77, emitter_delay=2)
+    o.s.emit_delay = 2
+    emitted = []
+    for step in range(1, 5):
+        eng.step(step)
+        o.step(step)
+        c = dio.counters()
+        assert c["emitted_step"] == o.s.emitted_step
+        emitted.append(c["emitted_step"])
+    assert emitted[0] == emitted[1] == 0 and emitted[2] > 0
+    eng.close()
+
+
+def test_planes_log_upward_crossings(rg):
+    """Check_Planes (src/mod_verlet.F90:343-367): a particle whose z passes a
+    plane upwards during the position update is logged once for that plane."""
+    rng = np.random.default_rng(8)
+    n = 400
+    pos = np.column_stack([rng.uniform(-50 * NM, 50 * NM, n), rng.uniform(-50 * NM, 50 * NM, n),
+                           rng.uniform(5 * NM, 480 * NM, n)])
+    vel = np.column_stack([np.zeros(n), np.zeros(n), rng.uniform(-2e5, 6e6, n)])
+    planes = (100 * NM, 250 * NM, 0.0)
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=1024, chain_capacity=256,
+                    event_capacity=4096)
+    d = eng.add_diode(V_s=1.0e3, gap=500 * NM, capacity=1000, time_step=2e-15, planes_z=planes)
+    d.add_particles(pos, vel=vel)
+    for step in range(1, 4):
+        before = d.particles()
+        zb = dict(zip(before["id"], before["pos"][:, 2]))
+        eng.update_position(step)
+        after = d.particles()        # marked particles are still present until removal
+        za = dict(zip(after["id"], after["pos"][:, 2]))
+        eng.remove_particles(step)
+        ev, lost = eng.events_take()
+        assert lost == 0
+        for k, zp in enumerate(planes):
+            got = sorted(r["id"] for r in ev if r["kind"] == rg.EVENT_PLANE + k)
+            want = sorted(i for i in za if zp > 0 and zb[i] < zp < za[i])
+            assert got == want
+        assert any(r["kind"] >= rg.EVENT_PLANE for r in ev) or step > 1
+    eng.close()
+
+
+def test_serial_mh_fp64_matches_oracle(rg, orc):
+    """mh_batch = .false. (the reference's default): each chain runs to
+    completion, sees the electrons earlier chains emitted in the same step and
+    updates MH_std once (src/mod_field_emission_v2.F90:322-333, 1122-1265).
+    The FP64 GPU form reproduces the oracle's serial sampler electron for
+    electron over two steps."""
+    rng = np.random.default_rng(31)
+    d, V, n0 = 500 * NM, 1.0e3, 150
+    pos = np.column_stack([rng.uniform(-60 * NM, 60 * NM, n0), rng.uniform(-60 * NM, 60 * NM, n0),
+                           rng.uniform(2 * NM, 490 * NM, n0)])
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=2, particle_capacity=8192, chain_capacity=4096)
+    dio = eng.add_diode(V_s=V, gap=d, capacity=4096, emitter_pos=(-50 * NM, -50 * NM),
+                        emitter_dim=(100 * NM, 100 * NM), work=[[2.0]], emission=True, mh_jumps=40,
+                        max_chains=300, quad_panels=8, quad_order=4, seed=31, mh_serial=True)
+    dio.add_particles(pos)
+    o = orc.OracleDiode(cap=4096, V_s=V, d=d)
+    o.set_planar_emitter(-50 * NM, -50 * NM, 100 * NM, 100 * NM, [[2.0]])
+    o.set_emission(True, seed=31, mh_jumps=40, max_chains=300, quad_panels=8, quad_order=4)
+    o.s.mh_serial = 1
+    for p in pos:
+        o.add(p)
+    for step in (1, 2):
+        eng.do_emission(step)
+        o.emission(step)
+        c = dio.counters()
+        assert c["N_sup"] == pytest.approx(o.s.N_sup, rel=1e-12)
+        assert c["emitted_step"] == o.s.emitted_step > 0
+        assert c["MH_std"] == pytest.approx(o.s.MH_std, rel=1e-12)
+        assert c["df_avg"] == pytest.approx(o.s.df_avg, rel=1e-10)
+        assert dio.n == o.n
+        p = dio.particles()
+        assert np.max(np.abs(p["pos"] - o.arr("pos")[:dio.n])) < 1e-12 * 100 * NM
+        np.testing.assert_array_equal(p["id"], o.iarr("id"))
+    eng.close()
+    # the FP32-compensated serial form: same supply, statistically the same emission
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=2, particle_capacity=8192, chain_capacity=4096)
+    dio = eng.add_diode(V_s=V, gap=d, capacity=4096, emitter_pos=(-50 * NM, -50 * NM),
+                        emitter_dim=(100 * NM, 100 * NM), work=[[2.0]], emission=True, mh_jumps=40,
+                        max_chains=300, quad_panels=8, quad_order=4, seed=31, mh_serial=True)
+    dio.add_particles(pos)
+    eng.do_emission(1)
+    c32 = dio.counters()
+    assert c32["emitted_step"] > 0 and c32["MH_std"] != 0.0125
+    eng.close()

@@ -339,3 +339,35 @@ def test_planar_system(orc):
     assert bounds_ok and finite_ok
     assert abs(Q - Q_exp) < 0.10 * abs(Q_exp)
     assert 0.5e-3 < I_ss < 4.0e-3, I_ss
+
+
+# ---- work-function models (src/mod_work_function.F90) --------------------------------
+def test_voronoi_work_function_unit_test(orc):
+    """unit_test_voronoi (src/mod_work_function.F90:582-626): nine sites, the
+    points (1.5, 1.0) and (1/3, 5/3) fall to sites 8 and 3.  The sites are
+    given there in absolute coordinates; with a unit emitter at the origin
+    the fraction-of-emitter convention of Read_work_function gives the same."""
+    import ctypes as C
+    xs = [0.5, 0.0, 0.0, 1.1, 0.8, 1.4, 2.33, 2.0, 2.1]
+    ys = [0.0, 1.0, 2.3, 0.0, 1.0, 2.0, 0.0, 1.25, 2.7]
+    w = np.array([v for i in range(9) for v in (xs[i], ys[i], float(i + 1), float(i + 1))])
+    pos, dim = np.zeros(2), np.ones(2)
+    sec = C.c_int(-1)
+    L = orc.lib()
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    assert L.orc_work_voronoi(dp(w), 9, dp(pos), dp(dim), 1.5, 1.0, C.byref(sec)) == pytest.approx(8.0, abs=1e-3)
+    assert sec.value == 8
+    assert L.orc_work_voronoi(dp(w), 9, dp(pos), dp(dim), 1.0 / 3.0, 5.0 / 3.0, C.byref(sec)) == pytest.approx(3.0, abs=1e-3)
+    assert sec.value == 3
+
+
+def test_gaussian_work_function_formula(orc):
+    """w_theta_gaussian (:214-254): base + sum A exp(-(dx^2/(2 sx^2) + dy^2/(2 sy^2)))
+    with centres and widths in nm."""
+    import ctypes as C
+    w = np.array([4.5, -0.5, 10.0, -20.0, 30.0, 40.0, 0.25, 0.0, 0.0, 5.0, 5.0])
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    for x, y in ((10e-9, -20e-9), (0.0, 0.0), (35e-9, 12e-9)):
+        expect = 4.5 - 0.5 * np.exp(-(((x - 10e-9) ** 2) / (2 * (30e-9) ** 2) + ((y + 20e-9) ** 2) / (2 * (40e-9) ** 2))) \
+            + 0.25 * np.exp(-((x ** 2) / (2 * (5e-9) ** 2) + (y ** 2) / (2 * (5e-9) ** 2)))
+        assert orc.lib().orc_work_gaussian(dp(w), 2, x, y) == pytest.approx(expect, rel=1e-14)
