@@ -98,6 +98,13 @@ typedef struct {
                               .true.), 1 serial (mh_batch = .false., the reference's default:
                               each chain runs to completion, sees the electrons earlier
                               chains of the step emitted and updates MH_std once) */
+  int emitter_type;        /* planar emitter shape (EMITTERS_TYPE, src/mod_global.F90:265-268):
+                              0 or 2 rectangle, 1 circle (sampled over its bounding box, as the
+                              reference does), 4 ring centred on the axis: outer radius
+                              emitter_dim[0], radial width emitter_thickness; a ring always
+                              uses the serial sampler (Metropolis_Hastings_ring_J) */
+  double emitter_thickness;/* ring width (m); 0: sqrt(q0 d / (pi eps0 V)) as the reference
+                              (src/main.F90:363-371) */
 } rd_diode_config;
 
 typedef struct {

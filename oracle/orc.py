@@ -64,6 +64,7 @@ class Diode(C.Structure):
         ("last_chains", C.c_int), ("last_failed_chains", C.c_int),
         ("work_model", C.c_int),
         ("emit_delay", C.c_int), ("mh_serial", C.c_int),
+        ("emitter_type", C.c_int), ("ring_rmin", C.c_double), ("ring_thick", C.c_double),
         ("F_avg_z", C.c_double), ("df_avg", C.c_double),
     ]
 
@@ -103,6 +104,7 @@ def lib():
                                               C.c_int, C.c_int, _dp]),
             "orc_set_tip": (None, [D, C.c_double, C.c_double, C.c_double, C.c_double]),
             "orc_set_work_model": (None, [D, C.c_int, C.c_int, _dp]),
+            "orc_set_ring": (None, [D, C.c_double, C.c_double]),
             "orc_work_gaussian": (C.c_double, [_dp, C.c_int, C.c_double, C.c_double]),
             "orc_work_voronoi": (C.c_double, [_dp, C.c_int, _dp, _dp, C.c_double, C.c_double, _ip]),
             "orc_set_emission": (None, [D, C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_int,
@@ -192,6 +194,9 @@ class OracleDiode:
         w = np.ascontiguousarray(params, dtype=np.float64).ravel()
         n = (w.size - 1) // 5 if model == 2 else w.size // 4
         self.L.orc_set_work_model(self.p, model, n, ptr(w))
+
+    def set_ring(self, r_out, thickness):
+        self.L.orc_set_ring(self.p, r_out, thickness)
 
     def set_tip(self, d_tip, R_base, h_tip, phi=4.7):
         self.L.orc_set_tip(self.p, d_tip, R_base, h_tip, phi)

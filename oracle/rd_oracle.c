@@ -239,6 +239,7 @@ orc_diode* orc_diode_new(int geometry, int cap, double V_s, double d, double tim
   s->work_nx = s->work_ny = 1;
   s->work[0] = 4.7;
   s->work_model = 1;
+  s->emitter_type = 2;
   s->tip_phi = 4.7;
   s->MH_std = 0.0125;                          /* fe_v2:58 */
   s->a_rate = 1.0;
@@ -263,8 +264,16 @@ void orc_set_planar_emitter(orc_diode* s, double x0, double y0, double Lx, doubl
                             int nx, int ny, const double* work) {
   s->em_pos[0] = x0; s->em_pos[1] = y0; s->em_dim[0] = Lx; s->em_dim[1] = Ly;
   s->work_model = 1;
+  s->emitter_type = 2;
   s->work_nx = nx; s->work_ny = ny;
   for (int i = 0; i < nx * ny && i < 64 * 64; ++i) s->work[i] = work[i];
+}
+
+void orc_set_ring(orc_diode* s, double r_out, double thickness) {
+  s->emitter_type = 4;
+  s->ring_thick = thickness;
+  s->ring_rmin = r_out - thickness;
+  s->mh_serial = 1;
 }
 
 void orc_set_work_model(orc_diode* s, int model, int n, const double* params) {
@@ -790,12 +799,19 @@ double orc_supply_integral_planar(orc_diode* s) {
     double ux = ((ix / Q) + 0.5 * (gx[ix % Q] + 1.0)) / P;
     double wx = 0.5 * gw[ix % Q] / P;
     double p[3] = {s->em_pos[0] + ux * s->em_dim[0], s->em_pos[1] + uy * s->em_dim[1], 0.0};
+    double Ak = A;
+    if (s->emitter_type == 4) {   /* integrand_cuba_fe_v EMIT_RING, :701-707 */
+      double angle = ux * 2.0 * PI, radius = s->ring_rmin + uy * s->ring_thick;
+      p[0] = radius * cos(angle);
+      p[1] = radius * sin(angle);
+      Ak = 2.0 * PI * s->ring_thick * radius;
+    }
     double f[3];
     orc_field_at(s, p, f, 1);
     fz[k] = f[2];
     if (f[2] < 0.0) {
       double phi = work_at(s, p[0], p[1], NULL);
-      val[k] = (wx * wy) * (A * orc_elec_supply_v2(f[2], phi, s->image_charge, s->time_step));
+      val[k] = (wx * wy) * (Ak * orc_elec_supply_v2(f[2], phi, s->image_charge, s->time_step));
     }
   }
   nsum tot = {0, 0}, ftot = {0, 0};
@@ -950,16 +966,79 @@ static void mh_serial_chain(orc_diode* s, int step, int c, double* df_out, doubl
   *df_out = orc_escape_prob_log(*F_out, work_at(s, cur[0], cur[1], NULL), s->image_charge);
 }
 
-/* The serial branch of Do_Field_Emission_Planar_rectangle (:322-333, 338-383):
- * each candidate's chain, its emission test and its Add_Particle before the
- * next candidate's chain. */
+/* Metropolis_Hastings_ring_J, :1521-1685: the chain moves in (angle, radius)
+ * of the ring; proposals off the ring are rejected; log(radius) is added to
+ * the target (the Jacobian).  MH_std updated once per chain. */
+static void mh_ring_chain(orc_diode* s, int step, int c, double* df_out, double* F_out, double pos[3]) {
+  int ndim = s->mh_jumps, ndim_first = (int)nint_f(ndim * 0.25);
+  double r_min = s->ring_rmin, r_max = s->ring_rmin + s->ring_thick;
+  double std[2] = {2.0 * PI * 0.10, s->ring_thick * 0.10};
+  double cur[3] = {0, 0, 0}, f[3], ca = 0.0, cr = r_min;
+  int found = 0;
+  for (int r = 0; r < s->init_rounds_max; ++r) {
+    double u1, u2;
+    rng2(s->seed, c, r, step, TAG_INIT, &u1, &u2);
+    ca = u1 * 2.0 * PI;
+    cr = r_min + u2 * s->ring_thick;
+    cur[0] = cr * cos(ca);
+    cur[1] = cr * sin(ca);
+    orc_field_at(s, cur, f, 1);
+    if (f[2] < 0.0) { found = 1; break; }
+  }
+  if (!found) {
+    *F_out = 1.0; *df_out = -DBL_MAX;
+    pos[0] = r_min; pos[1] = 0.0; pos[2] = 0.0;
+    return;
+  }
+  *F_out = f[2];
+  double sup_cur = orc_elec_supply_log(f[2], work_at(s, cur[0], cur[1], NULL), s->image_charge) + log(cr);
+  int ja = 0, jr = 0;
+  for (int i = 1; i <= ndim; ++i) {
+    if (i > ndim_first) { std[0] = 2.0 * PI * s->MH_std; std[1] = s->ring_thick * s->MH_std; }
+    double g1, g2;
+    gauss2(s->seed, c, i, step, &g1, &g2);
+    double a = g1 * std[0] + ca;
+    double na = a - floor(a / (2.0 * PI)) * (2.0 * PI), nr = g2 * std[1] + cr;
+    if (nr < r_min || nr > r_max) { if (i > ndim_first) jr++; continue; }
+    double w[3] = {nr * cos(na), nr * sin(na), 0.0};
+    orc_field_at(s, w, f, 1);
+    if (f[2] >= 0.0) { if (i > ndim_first) jr++; continue; }
+    double sn = orc_elec_supply_log(f[2], work_at(s, w[0], w[1], NULL), s->image_charge) + log(nr);
+    double alpha = sn - sup_cur;
+    int take = 0;
+    if (sn >= sup_cur) take = 1;
+    else {
+      double u1, u2;
+      rng2(s->seed, c, i, step, TAG_ACCEPT, &u1, &u2);
+      take = (log(u1) <= alpha);
+    }
+    if (take) {
+      cur[0] = w[0]; cur[1] = w[1]; ca = na; cr = nr; sup_cur = sn; *F_out = f[2];
+      if (i > ndim_first) ja++;
+    } else if (i > ndim_first) jr++;
+  }
+  if (ja + jr > 0) {
+    s->a_rate = (double)ja / (double)(jr + ja);
+    mh_std_update(&s->MH_std, s->a_rate, 0.00005, 0.1250);
+  }
+  pos[0] = cur[0]; pos[1] = cur[1]; pos[2] = 0.0;
+  *df_out = orc_escape_prob_log(*F_out, work_at(s, cur[0], cur[1], NULL), s->image_charge);
+}
+
+/* The serial branch of Do_Field_Emission_Planar_rectangle (:322-333, 338-383)
+ * and Do_Field_Emission_Planar_ring (:399-505): each candidate's chain, its
+ * emission test and its Add_Particle before the next candidate's chain. */
 static int emission_planar_serial(orc_diode* s, int step, int M) {
   int emitted = 0;
   double df_sum = 0.0;
   for (int c = 0; c < M; ++c) {
     double D, F, p[3];
-    mh_serial_chain(s, step, c, &D, &F, p);
-    if (F >= 0.0) D = -DBL_MAX;
+    if (s->emitter_type == 4) mh_ring_chain(s, step, c, &D, &F, p);
+    else mh_serial_chain(s, step, c, &D, &F, p);
+    if (F >= 0.0) {
+      D = -DBL_MAX;
+      if (s->emitter_type == 4) break;   /* Do_Field_Emission_Planar_ring exits here, :447-455 */
+    }
     df_sum += exp(D);
     double u1, u2;
     rng2(s->seed, c, 0, step, TAG_EMIT, &u1, &u2);

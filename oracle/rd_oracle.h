@@ -99,6 +99,8 @@ typedef struct {
   int work_model;
   int emit_delay;           /* emitters_delay: emission from step emit_delay + 1 on */
   int mh_serial;            /* 1: mh_batch = .false. (chains one after another) */
+  int emitter_type;         /* 2 rectangle, 4 ring (centred on the axis) */
+  double ring_rmin, ring_thick;
   double F_avg_z, df_avg;   /* field.dt: mean cathode F_z of the supply points, sum exp(D) / N_sup */
 } orc_diode;
 
@@ -114,6 +116,10 @@ void orc_set_tip(orc_diode* s, double d_tip, double R_base, double h_tip, double
 /* A Gaussian (model 2) or Voronoi (model 4) work function on the planar emitter;
  * n Gaussians / sites, parameters laid out as in orc_diode.work. */
 void orc_set_work_model(orc_diode* s, int model, int n, const double* params);
+/* A ring emitter (EMIT_RING): outer radius r_out, radial width thickness
+ * (emitters_ring, src/main.F90:363-371); sampled serially
+ * (Metropolis_Hastings_ring_J).  Call after orc_set_planar_emitter. */
+void orc_set_ring(orc_diode* s, double r_out, double thickness);
 /* w_theta_gaussian (src/mod_work_function.F90:214-254) and w_theta_voronoi
  * (:533-571; sites as fractions of the emitter, converted as in
  * Read_work_function :124-134). */

@@ -67,7 +67,7 @@ class DiodeConfig(C.Structure):
                 ("max_chains", C.c_int), ("quad_panels", C.c_int), ("quad_order", C.c_int),
                 ("init_rounds", C.c_int), ("seed", C.c_ulonglong), ("work_model", C.c_int),
                 ("emitter_delay", C.c_int), ("planes_N", C.c_int), ("planes_z", C.c_double * 10),
-                ("mh_serial", C.c_int)]
+                ("mh_serial", C.c_int), ("emitter_type", C.c_int), ("emitter_thickness", C.c_double)]
 
 
 class Counters(C.Structure):
@@ -376,7 +376,7 @@ def diode_config(geometry=GEOM_PLANAR, V_s=2.0e3, gap=1000e-9, time_step=0.25e-1
              emitter_dim=(0.0, 0.0), work=None, tip_dim=(0.0, 0.0, 0.0),
              tip_work_function=4.7, emission=False, mh_jumps=0, max_chains=0,
              quad_panels=0, quad_order=0, init_rounds=0, seed=1, work_model=0, emitter_delay=0,
-             planes_z=(), mh_serial=False):
+             planes_z=(), mh_serial=False, emitter_type=0, emitter_thickness=0.0):
     """rd_diode_config from keyword arguments (the /input/ namelist of one run).
     `work`: the checkerboard matrix (work_model 0/1); for work_model 2
     (Gaussian) the flat list base, then (A, x_c, y_c, std_x, std_y) per
@@ -396,6 +396,8 @@ def diode_config(geometry=GEOM_PLANAR, V_s=2.0e3, gap=1000e-9, time_step=0.25e-1
     cfg.work_model = work_model
     cfg.emitter_delay = emitter_delay
     cfg.mh_serial = int(bool(mh_serial))
+    cfg.emitter_type = emitter_type
+    cfg.emitter_thickness = emitter_thickness
     cfg.planes_N = len(planes_z)
     for k, z in enumerate(planes_z):
         cfg.planes_z[k] = z

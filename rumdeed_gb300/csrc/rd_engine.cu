@@ -631,6 +631,7 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
   p.seed = c->seed;
   p.emit_delay = c->emitter_delay > 0 ? c->emitter_delay : 0;
   p.mh_serial = c->mh_serial ? 1 : 0;
+  p.emitter_type = 2;
   if (c->planes_N < 0 || c->planes_N > 10) return fail(RD_ERR_INVALID, "planes_N must be in [0, 10]");
   p.planes_n = c->planes_N;
   for (int k = 0; k < p.planes_n; ++k) p.planes_z[k] = c->planes_z[k];
@@ -646,6 +647,20 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
     if (p.emission && (p.em_Lx <= 0.0 || p.em_Ly <= 0.0)) return fail(RD_ERR_INVALID, "emitter_dim must be positive");
     p.org_x = p.em_x0 + 0.5 * p.em_Lx;
     p.org_y = p.em_y0 + 0.5 * p.em_Ly;
+    p.emitter_type = c->emitter_type > 0 ? c->emitter_type : 2;
+    if (p.emitter_type != 1 && p.emitter_type != 2 && p.emitter_type != 4)
+      return fail(RD_ERR_INVALID, "emitter_type must be 1 (circle), 2 (rectangle) or 4 (ring)");
+    if (p.emitter_type == 4) {   // emitters_ring (src/main.F90:363-371), centred on the axis
+      p.ring_thick = c->emitter_thickness > 0.0
+                         ? c->emitter_thickness
+                         : std::sqrt((e->k.q0 * p.d) / (e->k.pi * e->k.eps0 * c->V_s));
+      p.ring_rmin = p.em_Lx - p.ring_thick;
+      if (p.ring_thick <= 0.0 || p.ring_rmin < 0.0)
+        return fail(RD_ERR_INVALID, "ring emitter: emitter_dim[0] (outer radius) must exceed its thickness");
+      p.org_x = 0.0;
+      p.org_y = 0.0;
+      p.mh_serial = 1;
+    }
     p.em_hx = f32_toward_zero(0.5 * p.em_Lx * 1.0e9);
     p.em_hy = f32_toward_zero(0.5 * p.em_Ly * 1.0e9);
     p.em_wx = (float)(p.em_Lx * 1.0e9);
@@ -734,9 +749,16 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
         for (int ix = 0; ix < p.quad_n; ++ix) {
           double ux = ((ix / Q) + 0.5 * (gx[ix % Q] + 1.0)) / P_, wx = 0.5 * gw[ix % Q] / P_;
           int k2 = iy * p.quad_n + ix;
-          hx[k2] = p.em_x0 + ux * p.em_Lx;
-          hy[k2] = p.em_y0 + uy * p.em_Ly;
-          hw[k2] = (wx * wy) * A;
+          if (p.emitter_type == 4) {   // (angle, radius) of the ring, area factor 2 pi w r (fe_v2:701-707)
+            const double angle = ux * 2.0 * e->k.pi, radius = p.ring_rmin + uy * p.ring_thick;
+            hx[k2] = radius * std::cos(angle);
+            hy[k2] = radius * std::sin(angle);
+            hw[k2] = (wx * wy) * (2.0 * e->k.pi * p.ring_thick * radius);
+          } else {
+            hx[k2] = p.em_x0 + ux * p.em_Lx;
+            hy[k2] = p.em_y0 + uy * p.em_Ly;
+            hw[k2] = (wx * wy) * A;
+          }
         }
       }
     } else {

@@ -1401,7 +1401,9 @@ __device__ double block_field_z0(const DiodeParams& p, const Pool& pool, int n, 
 }
 
 // The serial branch of Do_Field_Emission_Planar_rectangle (:322-333, 338-383)
-// with Metropolis_Hastings_rectangle_J (:1122-1265): one block per serial
+// with Metropolis_Hastings_rectangle_J (:1122-1265), and the ring emitter
+// (Do_Field_Emission_Planar_ring :399-505 with Metropolis_Hastings_ring_J
+// :1521-1685, chains in (angle, radius)): one block per serial
 // diode runs its candidates' chains one after another.  Each chain starts
 // from uniform draws until F_z < 0, makes mh_jumps jumps (the warm-up quarter
 // with 10 % of the emitter as the step, then MH_std), updates MH_std once from
@@ -1424,37 +1426,60 @@ k_mh_serial(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool p
   const int ndim = p.mh_jumps, ndim_first = (ndim + 2) / 4;
   int n = n0, emitted = 0, dropped = 0, failed = 0;
   double mhs = y.MH_std, a_rate = y.a_rate, df_sum = 0.0;
+  const bool ring = p.emitter_type == 4;
+  const double twopi = 2.0 * c_k.pi, rmin = p.ring_rmin, rmax = p.ring_rmin + p.ring_thick;
   for (int c = 0; c < M; ++c) {
     double cx = p.em_x0, cy = p.em_y0, F = 1.0;
+    double ca = 0.0, cr = rmin;   // ring: (angle, radius) of the chain (Metropolis_Hastings_ring_J)
     bool found = false;
     for (int r = 0; r < p.init_rounds && !found; ++r) {
       double u1, u2;
       rng2(p.seed, (uint32_t)c, (uint32_t)r, step, RNG_INIT, &u1, &u2);
-      cx = u1 * p.em_Lx + p.em_x0;
-      cy = u2 * p.em_Ly + p.em_y0;
+      if (ring) {
+        ca = u1 * twopi;
+        cr = rmin + u2 * p.ring_thick;
+        cx = cr * cos(ca);
+        cy = cr * sin(ca);
+      } else {
+        cx = u1 * p.em_Lx + p.em_x0;
+        cy = u2 * p.em_Ly + p.em_y0;
+      }
       F = block_field_z0<PREC>(p, pool, n, cx, cy, kscale, red);
       found = F < 0.0;
     }
     double D = -1.79769313486231570e308, Fout = 1.0;
     if (!found) {
-      cx = p.em_x0; cy = p.em_y0;
+      cx = ring ? rmin : p.em_x0;
+      cy = ring ? 0.0 : p.em_y0;
       ++failed;
     } else {
       Fout = F;
-      double sup_cur = supply_log_xy(p, wtab, cx, cy, F);
+      // ring: log(radius) is the Jacobian of the (angle, radius) parametrisation (:1592-1596)
+      double sup_cur = supply_log_xy(p, wtab, cx, cy, F) + (ring ? log(cr) : 0.0);
       int ja = 0, jr = 0;
-      double sx = p.em_Lx * 0.10, sy = p.em_Ly * 0.10;
+      double sx = (ring ? twopi : p.em_Lx) * 0.10, sy = (ring ? p.ring_thick : p.em_Ly) * 0.10;
       for (int i = 1; i <= ndim; ++i) {
-        if (i > ndim_first) { sx = p.em_Lx * mhs; sy = p.em_Ly * mhs; }
+        if (i > ndim_first) { sx = (ring ? twopi : p.em_Lx) * mhs; sy = (ring ? p.ring_thick : p.em_Ly) * mhs; }
         double g1, g2;
         gauss2(p.seed, (uint32_t)c, (uint32_t)i, step, &g1, &g2);
-        double wx = g1 * sx + cx, wy = g2 * sy + cy;
-        const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
-        if (wx > hx) wx = hx - (wx - hx); else if (wx < p.em_x0) wx = (p.em_x0 - wx) + p.em_x0;
-        if (wy > hy) wy = hy - (wy - hy); else if (wy < p.em_y0) wy = (p.em_y0 - wy) + p.em_y0;
+        double wx, wy, na = 0.0, nr = 0.0;
+        if (ring) {   // angle wrapped (Fortran MODULO), radius outside the ring rejected
+          const double a = g1 * sx + ca;
+          na = a - floor(a / twopi) * twopi;
+          nr = g2 * sy + cr;
+          if (nr < rmin || nr > rmax) { if (i > ndim_first) ++jr; continue; }
+          wx = nr * cos(na);
+          wy = nr * sin(na);
+        } else {
+          wx = g1 * sx + cx;
+          wy = g2 * sy + cy;
+          const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+          if (wx > hx) wx = hx - (wx - hx); else if (wx < p.em_x0) wx = (p.em_x0 - wx) + p.em_x0;
+          if (wy > hy) wy = hy - (wy - hy); else if (wy < p.em_y0) wy = (p.em_y0 - wy) + p.em_y0;
+        }
         const double Fw = block_field_z0<PREC>(p, pool, n, wx, wy, kscale, red);
         if (Fw >= 0.0) { if (i > ndim_first) ++jr; continue; }
-        const double sn = supply_log_xy(p, wtab, wx, wy, Fw);
+        const double sn = supply_log_xy(p, wtab, wx, wy, Fw) + (ring ? log(nr) : 0.0);
         bool take = sn >= sup_cur;
         if (!take) {
           double u1, u2;
@@ -1462,7 +1487,7 @@ k_mh_serial(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool p
           take = log(u1) <= sn - sup_cur;
         }
         if (take) {
-          cx = wx; cy = wy; sup_cur = sn; Fout = Fw;
+          cx = wx; cy = wy; sup_cur = sn; Fout = Fw; ca = na; cr = nr;
           if (i > ndim_first) ++ja;
         } else if (i > ndim_first) {
           ++jr;
@@ -1475,7 +1500,10 @@ k_mh_serial(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool p
       }
       D = fn_escape_log(Fout, work_at(p, work, cx, cy, nullptr), p.image_charge);
     }
-    if (Fout >= 0.0) D = -1.79769313486231570e308;
+    if (Fout >= 0.0) {
+      D = -1.79769313486231570e308;
+      if (ring) break;   // the ring emitter's loop stops at an unfavourable chain (:447-455)
+    }
     df_sum += exp(D);
     double u1, u2;
     rng2(p.seed, (uint32_t)c, 0u, step, RNG_EMIT, &u1, &u2);

@@ -70,6 +70,8 @@ struct DiodeParams {
   float em_hx, em_hy, em_wx, em_wy;
   int emit_delay;        // the emitter emits from step emit_delay + 1 on
   int mh_serial;         // 1: serial MH sampler (k_mh_serial)
+  int emitter_type;      // 2 rectangle (1 circle is sampled as its box), 4 ring
+  double ring_rmin, ring_thick;   // ring emitter: inner radius and width (m)
   int planes_n;          // measurement planes (Check_Planes)
   double planes_z[10];
 };

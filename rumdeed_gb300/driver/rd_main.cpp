@@ -19,7 +19,10 @@
 // rectangular emitter, EMITTERS_TYPE 2) and EMISSION_MODE = 3 (hyperboloid
 // tip).  Extra, optional namelist /gb300/ in the same file: MAX_PARTICLES
 // (default 20000), SEED, PRECISION (0 = FP64, 1 = FP32 compensated), MH_JUMPS,
-// TIP_WORK_FUNCTION (eV, default 4.7 as the reference hard-codes).
+// TIP_WORK_FUNCTION (eV, default 4.7 as the reference hard-codes), MH_SERIAL.
+// The MH sampler is serial with MH_SERIAL = 1 or /input/'s MH_BATCH = .False.,
+// batched otherwise (the reference's default, absent MH_BATCH, is serial;
+// this driver's is batched); a ring emitter (EMITTERS_TYPE 4) is always serial.
 //
 //   rd_main [run directory]
 #include <cctype>
@@ -224,6 +227,10 @@ int main(int argc, char** argv) {
     dc.emitter_dim[1] = get(in, "EMITTERS_DIM", 1, 0.0) * length_scale;
     dc.emitter_pos[0] = get(in, "EMITTERS_POS", 0, 0.0) * length_scale;
     dc.emitter_pos[1] = get(in, "EMITTERS_POS", 1, 0.0) * length_scale;
+    dc.emitter_type = (int)get(in, "EMITTERS_TYPE", 0, 2.0);
+    dc.emitter_thickness = get(in, "EMITTERS_DIM", 2, 0.0) * length_scale;   // ring width (0: from V, d)
+    dc.mh_serial = get(gb, "MH_SERIAL", 0, 0.0) != 0.0 ||
+                   (in.count("MH_BATCH") && !to_logical(in.at("MH_BATCH")[0]));
     // Read_work_function (src/mod_work_function.F90:53-152): 1 checkerboard
     // (y_num x_num, then the matrix), 2 Gaussian (base, count, then A x y sx sy
     // per line), 4 Voronoi (count, then x y phi section per line)
@@ -275,12 +282,12 @@ int main(int argc, char** argv) {
     std::printf("geometry %d\nV_s %.17g\ngap %.17g\ntime_step %.17g\nsteps %d\nimage_charge %d\n"
                 "N_ic_max %d\ncapacity %d\nseed %llu\nemitter_pos %.17g %.17g\nemitter_dim %.17g %.17g\n"
                 "work %d x %d\nwork_model %d\ntip_dim %.17g %.17g %.17g\nE14.6 %s\nES12.4 %s\n"
-                "emitter_delay %d\nplanes %d\n",
+                "emitter_delay %d\nplanes %d\nemitter_type %d\nmh_serial %d\n",
                 dc.geometry, dc.V_s, dc.gap, dc.time_step, steps, dc.image_charge, dc.N_ic_max,
                 dc.capacity, dc.seed, dc.emitter_pos[0], dc.emitter_pos[1], dc.emitter_dim[0],
                 dc.emitter_dim[1], dc.work_ny, dc.work_nx, dc.work_model, dc.tip_dim[0], dc.tip_dim[1], dc.tip_dim[2],
                 fmt_E(dt / time_scale, 14, 6).c_str(), fmt_ES(dt / time_scale, 12, 4).c_str(), dc.emitter_delay,
-                dc.planes_N);
+                dc.planes_N, dc.emitter_type, dc.mh_serial);
     for (int k = 0; k < dc.planes_N; ++k) std::printf("plane_z %.17g\n", dc.planes_z[k]);
     for (double w : work) std::printf("work_value %.17g\n", w);
     return 0;

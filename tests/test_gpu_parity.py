@@ -444,3 +444,43 @@ def test_serial_mh_fp64_matches_oracle(rg, orc):
     c32 = dio.counters()
     assert c32["emitted_step"] > 0 and c32["MH_std"] != 0.0125
     eng.close()
+
+
+def test_ring_emitter_fp64_matches_oracle(rg, orc):
+    """Ring emitter (EMIT_RING): supply integral over (angle, radius) with the
+    2 pi w r area factor (fe_v2:701-707) and the serial ring sampler
+    (Metropolis_Hastings_ring_J :1521-1685, log r Jacobian, off-ring
+    proposals rejected): the FP64 GPU form matches the oracle electron for
+    electron."""
+    rng = np.random.default_rng(41)
+    d, V, n0 = 500 * NM, 1.0e3, 100
+    r_out, w = 60 * NM, 20 * NM
+    pos = np.column_stack([rng.uniform(-70 * NM, 70 * NM, n0), rng.uniform(-70 * NM, 70 * NM, n0),
+                           rng.uniform(2 * NM, 490 * NM, n0)])
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=2, particle_capacity=8192, chain_capacity=4096)
+    dio = eng.add_diode(V_s=V, gap=d, capacity=4096, emitter_pos=(-r_out, -r_out),
+                        emitter_dim=(r_out, r_out), work=[[1.8]], emission=True, mh_jumps=40,
+                        max_chains=300, quad_panels=8, quad_order=4, seed=41, emitter_type=4,
+                        emitter_thickness=w)
+    dio.add_particles(pos)
+    o = orc.OracleDiode(cap=4096, V_s=V, d=d)
+    o.set_planar_emitter(-r_out, -r_out, r_out, r_out, [[1.8]])
+    o.set_ring(r_out, w)
+    o.set_emission(True, seed=41, mh_jumps=40, max_chains=300, quad_panels=8, quad_order=4)
+    for p in pos:
+        o.add(p)
+    for step in (1, 2):
+        eng.do_emission(step)
+        o.emission(step)
+        c = dio.counters()
+        assert c["N_sup"] == pytest.approx(o.s.N_sup, rel=1e-12)
+        assert c["emitted_step"] == o.s.emitted_step
+        assert c["MH_std"] == pytest.approx(o.s.MH_std, rel=1e-12)
+        p = dio.particles()
+        assert dio.n == o.n
+        np.testing.assert_allclose(p["pos"], o.arr("pos")[:dio.n], rtol=0, atol=1e-12 * 100 * NM)
+    new = dio.particles()["pos"][n0:]
+    assert len(new) > 0
+    r = np.hypot(new[:, 0], new[:, 1])
+    assert np.all(r >= r_out - w - 1e-15) and np.all(r <= r_out + 1e-15)   # emitted on the ring
+    eng.close()
