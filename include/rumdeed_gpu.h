@@ -105,6 +105,12 @@ typedef struct {
                               uses the serial sampler (Metropolis_Hastings_ring_J) */
   double emitter_thickness;/* ring width (m); 0: sqrt(q0 d / (pi eps0 V)) as the reference
                               (src/main.F90:363-371) */
+  int atom_time_interval;  /* two-time-step integrator (atom_time_interval of the namelist,
+                              src/main.F90:391-395): 0 off; T > 0: electrons move every step,
+                              ions only on steps divisible by T with the step T*time_step, and
+                              the ions' acceleration gathers the electron forces of every step
+                              in between (src/mod_verlet.F90:183-194,234-290,403-416,511-590,
+                              886-1151) */
 } rd_diode_config;
 
 typedef struct {
@@ -118,6 +124,7 @@ typedef struct {
   double F_avg[3];         /* mean cathode field over the supply evaluation points
                               (field.dt, src/mod_field_emission_v2.F90:644-651) */
   double df_avg;           /* sum of the candidates' escape probabilities / N_sup (:354,385) */
+  double ramo_current_ion; /* ramo_current(species_ion) of the last step (A) */
 } rd_counters;
 
 const char* rd_last_error(void);

@@ -66,6 +66,7 @@ class Diode(C.Structure):
         ("emit_delay", C.c_int), ("mh_serial", C.c_int),
         ("emitter_type", C.c_int), ("ring_rmin", C.c_double), ("ring_thick", C.c_double),
         ("F_avg_z", C.c_double), ("df_avg", C.c_double),
+        ("atom_time_interval", C.c_int), ("ramo_current_ion", C.c_double),
     ]
 
 
@@ -125,6 +126,9 @@ def lib():
             "orc_update_position": (None, [D]),
             "orc_update_velocity": (None, [D]),
             "orc_velocity_verlet": (None, [D, C.c_int]),
+            "orc_update_position_tts": (None, [D, C.c_int]),
+            "orc_accel_tts": (None, [D, C.c_int, C.c_int]),
+            "orc_update_velocity_tts": (None, [D, C.c_int]),
             "orc_supply_integral_planar": (C.c_double, [D]),
             "orc_mh_batch_planar": (None, [D, C.c_int, C.c_int, _dp, _dp, _dp, _ip]),
             "orc_do_emission_planar": (C.c_int, [D, C.c_int]),
@@ -255,6 +259,10 @@ class OracleDiode:
 
     def update_velocity(self):
         self.L.orc_update_velocity(self.p)
+
+    def set_tts(self, interval):
+        """Two-time-step integrator with atom_time_interval = interval (0 = off)."""
+        self.s.atom_time_interval = int(interval)
 
     def verlet(self, step):
         self.L.orc_velocity_verlet(self.p, step)

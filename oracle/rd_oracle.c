@@ -686,10 +686,135 @@ void orc_update_position(orc_diode* s) {
   }
 }
 
+/* ---- two-time-step integrator (two_time_step, atom_time_interval = T > 0) ----
+ * Update_Species_Position :234-290: electrons every step; ions on steps
+ * divisible by T with nrStep = T; atoms never (Update_Particle_Position
+ * :181-194).  Electrons are taken in their pointer order, then the ions. */
+static void species_position(orc_diode* s, int species, double nr) {
+  double dt = s->time_step, dt2 = s->time_step2, nr2 = nr * nr;
+  for (int i = 0; i < s->n; ++i) {
+    if (s->species[i] != species) continue;
+    for (int k = 0; k < 3; ++k) {
+      int q = 3 * i + k;
+      s->pos[q] = (s->pos[q] + (s->vel[q] * dt) * nr) +
+                  (((1.0 / 6.0) * (4.0 * s->acc[q] - s->acc_prev[q])) * dt2) * nr2;
+      s->acc_prev2[q] = s->acc_prev[q];
+      s->acc_prev[q] = s->acc[q];
+      s->acc[q] = 0.0;
+    }
+    check_boundary(s, i);
+  }
+}
+
+void orc_update_position_tts(orc_diode* s, int step) {
+  species_position(s, ORC_ELEC, 1.0);
+  if (step % s->atom_time_interval == 0) species_position(s, ORC_ION, (double)s->atom_time_interval);
+}
+
+/* One pair of Update_Elec_Acceleration / Update_Ion_Acceleration
+ * (:899-1151): particle i in the (a) role, particle j mirrored in x, y. */
+static void tts_pair(const orc_diode* s, int i, int j, nsum* a, int comp) {
+  const double* p1 = s->pos + 3 * i;
+  const double* p2 = s->pos + 3 * j;
+  double im1 = 1.0 / s->mass[i], im2 = 1.0 / s->mass[j];
+  double pre = (s->charge[i] * DIV_FAC_C) * s->charge[j];
+  double diff[3] = {p1[0] - p2[0], p1[1] - p2[1], p1[2] - p2[2]};
+  double r = sqrt((diff[0] * diff[0] + diff[1] * diff[1]) + diff[2] * diff[2]) + L2;
+  double inv = 1.0 / ((r * r) * r);
+  double fc[3], ic[3] = {0, 0, 0}, icN[3];
+  for (int k = 0; k < 3; ++k) fc[k] = (pre * inv) * diff[k];
+  if (s->image_charge) image_effect(s, p1, p2, ic);
+  for (int k = 0; k < 3; ++k) ic[k] = pre * ic[k];
+  icN[0] = -1.0 * ic[0]; icN[1] = -1.0 * ic[1]; icN[2] = 1.0 * ic[2];
+  for (int k = 0; k < 3; ++k) {
+    double vj = icN[k] * im2 - fc[k] * im2, vi = fc[k] * im1 + ic[k] * im1;
+    if (comp) { nadd(&a[3 * j + k], vj); nadd(&a[3 * i + k], vi); }
+    else { a[3 * j + k].s += vj; a[3 * i + k].s += vi; }
+  }
+}
+
+static void tts_field(const orc_diode* s, int i, nsum* a, int comp) {
+  double e[3], im1 = 1.0 / s->mass[i];
+  orc_field_E(s, s->pos + 3 * i, e);
+  for (int k = 0; k < 3; ++k) {
+    double v = (s->charge[i] * e[k]) * im1;
+    if (comp) nadd(&a[3 * i + k], v); else a[3 * i + k].s += v;
+  }
+}
+
+/* Update_Particle_Acceleration :886-897 in two-time-step mode: the electron
+ * pass (every electron against the later electrons and all ions, the
+ * electron in the (a) role of every electron-ion pair) on every step, the
+ * ion pass (ions against later ions, plus the field) on steps divisible by
+ * T; both add their sums to particles_cur_accel, which the position update
+ * cleared only for the particles it moved. */
+void orc_accel_tts(orc_diode* s, int step, int comp) {
+  init_constants();
+  int n = s->n;
+  nsum* a = (nsum*)calloc((size_t)3 * (n > 0 ? n : 1), sizeof(nsum));
+  for (int i = 0; i < n; ++i) {           /* Update_Elec_Acceleration */
+    if (s->species[i] != ORC_ELEC) continue;
+    for (int j = i + 1; j < n; ++j)
+      if (s->species[j] == ORC_ELEC) tts_pair(s, i, j, a, comp);
+    for (int j = 0; j < n; ++j)
+      if (s->species[j] == ORC_ION) tts_pair(s, i, j, a, comp);
+    tts_field(s, i, a, comp);
+  }
+  for (int k = 0; k < 3 * n; ++k) s->acc[k] += nval(&a[k]);
+  if (step % s->atom_time_interval == 0) {  /* Update_Ion_Acceleration */
+    memset(a, 0, sizeof(nsum) * 3 * (size_t)n);
+    for (int i = 0; i < n; ++i) {
+      if (s->species[i] != ORC_ION) continue;
+      for (int j = i + 1; j < n; ++j)
+        if (s->species[j] == ORC_ION) tts_pair(s, i, j, a, comp);
+      tts_field(s, i, a, comp);
+    }
+    for (int k = 0; k < 3 * n; ++k) s->acc[k] += nval(&a[k]);
+  }
+  free(a);
+}
+
+/* Beeman velocity and Ramo current of one particle (the loop bodies of
+ * Update_ElecIon_Velocity :449-509 and Update_Species_Velocity :511-590). */
+static void velocity_one(orc_diode* s, int i, double nr, nsum* ramo, nsum* ramo_ion, double* sum,
+                         int* n_elec) {
+  double dt = s->time_step;
+  for (int k = 0; k < 3; ++k) {
+    int q = 3 * i + k;
+    s->vel[q] = s->vel[q] + (((1.0 / 6.0) * ((2.0 * s->acc[q] + 5.0 * s->acc_prev[q]) -
+                                              s->acc_prev2[q])) * dt) * nr;
+  }
+  double ez[3];
+  orc_E_zunit(s, s->pos + 3 * i, ez);
+  double ezv = (s->vel[3 * i] * ez[0] + s->vel[3 * i + 1] * ez[1]) + s->vel[3 * i + 2] * ez[2];
+  if (s->species[i] == ORC_ELEC) {
+    nadd(ramo, s->charge[i] * ezv);
+    for (int k = 0; k < 3; ++k) sum[k] += s->vel[3 * i + k];
+    (*n_elec)++;
+  } else if (s->species[i] == ORC_ION) {
+    nadd(ramo_ion, s->charge[i] * ezv);
+  }
+}
+
+void orc_update_velocity_tts(orc_diode* s, int step) {
+  nsum ramo = {0, 0}, ramo_ion = {0, 0};
+  double sum[3] = {0, 0, 0};
+  int n_elec = 0;
+  for (int i = 0; i < s->n; ++i)
+    if (s->species[i] == ORC_ELEC) velocity_one(s, i, 1.0, &ramo, &ramo_ion, sum, &n_elec);
+  if (step % s->atom_time_interval == 0)
+    for (int i = 0; i < s->n; ++i)
+      if (s->species[i] == ORC_ION)
+        velocity_one(s, i, (double)s->atom_time_interval, &ramo, &ramo_ion, sum, &n_elec);
+  s->ramo_current = nval(&ramo);
+  s->ramo_current_ion = nval(&ramo_ion);
+  for (int k = 0; k < 3; ++k) s->avg_elec_vel[k] = n_elec ? sum[k] / n_elec : 0.0;
+}
+
 /* Update_ElecIon_Velocity :449-509 + Average_Velocities :428-447 */
 void orc_update_velocity(orc_diode* s) {
   double dt = s->time_step;
-  nsum ramo = {0, 0};
+  nsum ramo = {0, 0}, ramo_ion = {0, 0};
   double sum[3] = {0, 0, 0};
   int n_elec = 0;
   for (int i = 0; i < s->n; ++i) {
@@ -706,15 +831,24 @@ void orc_update_velocity(orc_diode* s) {
       nadd(&ramo, s->charge[i] * ezv);
       for (int k = 0; k < 3; ++k) sum[k] += s->vel[3 * i + k];
       n_elec++;
+    } else if (s->species[i] == ORC_ION) {
+      nadd(&ramo_ion, s->charge[i] * ezv);
     }
   }
   s->ramo_current = nval(&ramo);
+  s->ramo_current_ion = nval(&ramo_ion);
   for (int k = 0; k < 3; ++k) s->avg_elec_vel[k] = n_elec ? sum[k] / n_elec : 0.0;
 }
 
-/* Velocity_Verlet :123-162 with the gather acceleration (the GPU semantics) */
+/* Velocity_Verlet :123-162 with the gather acceleration (the GPU semantics),
+ * or the two-time-step routines when atom_time_interval > 0 */
 void orc_velocity_verlet(orc_diode* s, int step) {
-  (void)step;
+  if (s->atom_time_interval > 0) {
+    orc_update_position_tts(s, step);
+    orc_accel_tts(s, step, 1);
+    orc_update_velocity_tts(s, step);
+    return;
+  }
   orc_update_position(s);
   orc_accel_gather(s, s->acc, 1);
   orc_update_velocity(s);

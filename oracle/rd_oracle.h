@@ -102,6 +102,9 @@ typedef struct {
   int emitter_type;         /* 2 rectangle, 4 ring (centred on the axis) */
   double ring_rmin, ring_thick;
   double F_avg_z, df_avg;   /* field.dt: mean cathode F_z of the supply points, sum exp(D) / N_sup */
+  /* two-time-step integrator (atom_time_interval, src/main.F90:391-395): 0 off */
+  int atom_time_interval;
+  double ramo_current_ion;  /* ramo_current(species_ion) of the last step */
 } orc_diode;
 
 /* Create / destroy.  Geometry parameters follow Init_Field_Emission_v2
@@ -165,6 +168,12 @@ void orc_field_at_batch(const orc_diode* s, int M, const double* pts, double* ou
 void orc_update_position(orc_diode* s);  /* Update_ElecIon_Position :197-232 */
 void orc_update_velocity(orc_diode* s);  /* Update_ElecIon_Velocity :449-509 + :428-447 */
 void orc_velocity_verlet(orc_diode* s, int step);  /* :123-162 (accel via gather) */
+/* Two-time-step routines (atom_time_interval > 0): Update_Species_Position
+ * :234-290, Update_Elec_Acceleration + Update_Ion_Acceleration :886-1151 (adds
+ * to acc), Update_Species_Velocity :511-590. */
+void orc_update_position_tts(orc_diode* s, int step);
+void orc_accel_tts(orc_diode* s, int step, int compensated);
+void orc_update_velocity_tts(orc_diode* s, int step);
 
 /* Emission (device algorithm restated with the shared Philox streams) */
 double orc_supply_integral_planar(orc_diode* s);

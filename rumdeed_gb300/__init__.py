@@ -67,7 +67,8 @@ class DiodeConfig(C.Structure):
                 ("max_chains", C.c_int), ("quad_panels", C.c_int), ("quad_order", C.c_int),
                 ("init_rounds", C.c_int), ("seed", C.c_ulonglong), ("work_model", C.c_int),
                 ("emitter_delay", C.c_int), ("planes_N", C.c_int), ("planes_z", C.c_double * 10),
-                ("mh_serial", C.c_int), ("emitter_type", C.c_int), ("emitter_thickness", C.c_double)]
+                ("mh_serial", C.c_int), ("emitter_type", C.c_int), ("emitter_thickness", C.c_double),
+                ("atom_time_interval", C.c_int)]
 
 
 class Counters(C.Structure):
@@ -79,7 +80,7 @@ class Counters(C.Structure):
                 ("electron_steps", C.c_longlong), ("steps_done", C.c_longlong),
                 ("ramo_current", C.c_double), ("N_sup", C.c_double), ("MH_std", C.c_double),
                 ("a_rate", C.c_double), ("residual", C.c_double), ("F_avg", C.c_double * 3),
-                ("df_avg", C.c_double)]
+                ("df_avg", C.c_double), ("ramo_current_ion", C.c_double)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -376,12 +377,14 @@ def diode_config(geometry=GEOM_PLANAR, V_s=2.0e3, gap=1000e-9, time_step=0.25e-1
              emitter_dim=(0.0, 0.0), work=None, tip_dim=(0.0, 0.0, 0.0),
              tip_work_function=4.7, emission=False, mh_jumps=0, max_chains=0,
              quad_panels=0, quad_order=0, init_rounds=0, seed=1, work_model=0, emitter_delay=0,
-             planes_z=(), mh_serial=False, emitter_type=0, emitter_thickness=0.0):
+             planes_z=(), mh_serial=False, emitter_type=0, emitter_thickness=0.0,
+             atom_time_interval=0):
     """rd_diode_config from keyword arguments (the /input/ namelist of one run).
     `work`: the checkerboard matrix (work_model 0/1); for work_model 2
     (Gaussian) the flat list base, then (A, x_c, y_c, std_x, std_y) per
     Gaussian; for work_model 4 (Voronoi) the flat list (x, y, phi, section)
-    per site, x, y as fractions of the emitter."""
+    per site, x, y as fractions of the emitter.  `atom_time_interval` > 0
+    selects the two-time-step integrator (ions move every that many steps)."""
     cfg = DiodeConfig()
     cfg.geometry = geometry
     cfg.V_s = V_s
@@ -398,6 +401,7 @@ def diode_config(geometry=GEOM_PLANAR, V_s=2.0e3, gap=1000e-9, time_step=0.25e-1
     cfg.mh_serial = int(bool(mh_serial))
     cfg.emitter_type = emitter_type
     cfg.emitter_thickness = emitter_thickness
+    cfg.atom_time_interval = int(atom_time_interval)
     cfg.planes_N = len(planes_z)
     for k, z in enumerate(planes_z):
         cfg.planes_z[k] = z

@@ -75,7 +75,10 @@ cudaError_t rd_launch_position(int grid, cudaStream_t st, const DiodeParams* P, 
                                const Pool& pool, const PlanEntry* plan, const PlanHeader* ph, const EventLog& ev, const int* step_ptr);
 cudaError_t rd_launch_velocity(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
                                DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
-                               const PlanHeader* ph, double* ramo);
+                               const PlanHeader* ph, double* ramo, const int* step_ptr);
+cudaError_t rd_launch_force_tts(int grid, cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy,
+                                const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
+                                double* partial, int* tickets, int* queue, const int* step_ptr);
 cudaError_t rd_launch_compact(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
                               DiodeDyn* Dy, const Pool& pool, const Pool& tmp,
                               const PlanEntry* plan, const PlanHeader* ph, int* kept, int* life,
@@ -88,8 +91,6 @@ cudaError_t rd_launch_add_particles(cudaStream_t st, const DiodeParams* P, Diode
 cudaError_t rd_launch_mark(cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
                            int d, int i, int why);
 
-enum { PM_FORCE_PLANAR = 0, PM_FORCE_TIP = 1, PM_FIELD = 2, PM_SUPPLY_PLANAR = 3,
-       PM_SUPPLY_TIP = 4, PM_MH = 5, PM_PART = 6, PM_PART1024 = 7, PM_COUNT = 8 };
 
 // ---- errors -------------------------------------------------------------------------
 static thread_local std::string g_err;
@@ -285,8 +286,9 @@ static int alloc_pool(rd_engine* e, Pool& P, long long cap) {
 // ---- pipeline pieces ----------------------------------------------------------------
 static cudaError_t plan(rd_engine* e, int mode, const int* npts = nullptr) {
   e->kernels_in_step++;
+  const int slot = mode & 0xff;
   return rd_launch_plan(e->st, e->dP, e->dD, e->nslots_hw(), mode, rd_chunk_rule(e->clen_min, e->nch_max),
-                        e->max_items, npts, e->plan[mode], e->ph[mode]);
+                        e->max_items, npts, e->plan[slot], e->ph[slot]);
 }
 
 static bool valid_chunking(int clen_min, int nch_max) {
@@ -297,6 +299,7 @@ static bool valid_chunking(int clen_min, int nch_max) {
 struct Sig {
   bool planar = false, tip = false, emit_planar = false, emit_tip = false, nic = false;
   bool emit_serial = false;   // some planar diode uses the serial MH sampler
+  bool tts = false;           // some diode uses the two-time-step integrator
   int jumps = 0;
 };
 static Sig signature(const rd_engine* e) {
@@ -306,6 +309,7 @@ static Sig signature(const rd_engine* e) {
     const DiodeParams& p = sl.p;
     if (p.geometry == RD_G_TIP) s.tip = true; else s.planar = true;
     if (p.geometry == RD_G_PLANAR && p.image_charge && p.N_ic_max > 0) s.nic = true;
+    if (p.tts > 0) s.tts = true;
     if (p.emission) {
       if (p.geometry == RD_G_TIP) s.emit_tip = true; else s.emit_planar = true;
       if (p.geometry != RD_G_TIP && p.mh_serial) s.emit_serial = true;
@@ -362,20 +366,31 @@ static int launch_emission(rd_engine* e) {
   return RD_OK;
 }
 
-static int launch_force(rd_engine* e) {
+// The acceleration pass.  In a time step (step_pass) two-time-step diodes
+// take k_force_tts (Update_Particle_Acceleration, src/mod_verlet.F90:886-897);
+// otherwise every diode takes the plain pass (Calculate_Acceleration_Particles,
+// which does not look at two_time_step), which is also idempotent for timing.
+static int launch_force(rd_engine* e, bool step_pass = false) {
   Sig s = signature(e);
+  const int all = step_pass ? 0 : PM_ALL_DIODES;
   if (s.planar) {
-    CK(plan(e, PM_FORCE_PLANAR));
+    CK(plan(e, PM_FORCE_PLANAR | all));
     CK(rd_launch_force(e->cfg.precision, 1, s.nic ? 1 : 0, e->grid, e->st, e->dP, e->dD, e->pool,
                        e->plan[PM_FORCE_PLANAR], e->ph[PM_FORCE_PLANAR], e->partial, e->tickets,
                        e->kscale, e->item_queue + 4));
     e->kernels_in_step++;
   }
   if (s.tip) {
-    CK(plan(e, PM_FORCE_TIP));
+    CK(plan(e, PM_FORCE_TIP | all));
     CK(rd_launch_force(e->cfg.precision, 2, 0, e->grid, e->st, e->dP, e->dD, e->pool,
                        e->plan[PM_FORCE_TIP], e->ph[PM_FORCE_TIP], e->partial, e->tickets,
                        e->kscale, e->item_queue + 4));
+    e->kernels_in_step++;
+  }
+  if (step_pass && s.tts) {
+    CK(plan(e, PM_FORCE_TTS));
+    CK(rd_launch_force_tts(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_FORCE_TTS], e->ph[PM_FORCE_TTS],
+                           e->partial, e->tickets, e->item_queue + 4, e->d_step));
     e->kernels_in_step++;
   }
   return RD_OK;
@@ -387,10 +402,10 @@ static int launch_update_position(rd_engine* e) {
   CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->evlog,
                         e->d_step));
   e->kernels_in_step++;
-  int rc = launch_force(e);
+  int rc = launch_force(e, true);
   if (rc) return rc;
   CK(rd_launch_velocity(e->grid, ns, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART],
-                        e->ramo));
+                        e->ramo, e->d_step));
   e->kernels_in_step += 2;
   return RD_OK;
 }
@@ -419,8 +434,8 @@ static int launch_step_body(rd_engine* e) {
 static std::string sig_string(rd_engine* e) {
   Sig s = signature(e);
   char b[128];
-  snprintf(b, sizeof b, "%d%d%d%d%d%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
-           s.emit_serial, s.jumps, e->clen_min, e->nch_max);
+  snprintf(b, sizeof b, "%d%d%d%d%d%d%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
+           s.emit_serial, s.tts, s.jumps, e->clen_min, e->nch_max);
   return b;
 }
 
@@ -635,6 +650,8 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
   if (c->planes_N < 0 || c->planes_N > 10) return fail(RD_ERR_INVALID, "planes_N must be in [0, 10]");
   p.planes_n = c->planes_N;
   for (int k = 0; k < p.planes_n; ++k) p.planes_z[k] = c->planes_z[k];
+  if (c->atom_time_interval < 0) return fail(RD_ERR_INVALID, "atom_time_interval must be >= 0");
+  p.tts = c->atom_time_interval;
   p.init_rounds = c->init_rounds > 0 ? c->init_rounds : 10000;
   p.work_nx = p.work_ny = 1;
   p.work_model = 1;
@@ -1215,6 +1232,7 @@ static void fill_counters(const DiodeDyn& y, rd_counters* o) {
   o->a_rate = y.a_rate; o->residual = y.residual;
   o->F_avg[0] = 0.0; o->F_avg[1] = 0.0; o->F_avg[2] = y.F_avg_z;   // x, y cancel at the cathode
   o->df_avg = y.df_avg;
+  o->ramo_current_ion = y.ramo_ion;
 }
 
 int rd_counters_get(rd_engine* e, int d, rd_counters* o) {
@@ -1306,10 +1324,11 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
   CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->evlog,
                         e->d_step));
   CK(cudaEventRecord(ev[5], e->st));
-  int rc = launch_force(e);
+  int rc = launch_force(e, true);
   if (rc) return rc;
   CK(cudaEventRecord(ev[6], e->st));
-  CK(rd_launch_velocity(e->grid, S, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->ramo));
+  CK(rd_launch_velocity(e->grid, S, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->ramo,
+                        e->d_step));
   CK(cudaEventRecord(ev[7], e->st));
   CK(cudaMemcpyAsync(dyn.data(), e->dD, sizeof(DiodeDyn) * S, cudaMemcpyDeviceToHost, e->st));
   rc = launch_remove(e);

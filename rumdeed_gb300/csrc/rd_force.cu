@@ -384,6 +384,95 @@ k_force_tip_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
   queue_leave(queue, total);
 }
 
+// ---- two-time-step diodes (FP64, both geometries) ----------------------------------
+// Update_Elec_Acceleration and Update_Ion_Acceleration
+// (src/mod_verlet.F90:899-1151) as a gather.  Pairs run over the electron and
+// ion lists only (atoms take no part); the image term of an electron-ion
+// pair has the electron in the "a" role whatever the indices, a pair of the
+// same species the lower index.  Electrons gather from electrons and ions on
+// every step.  Ions gather the electron forces on every step and, on steps
+// divisible by T, the ion-ion forces and the vacuum field: on those steps the
+// position update has just cleared their acceleration, on the others the
+// electron forces add to what is there, as the reference's accumulation into
+// particles_cur_accel does.
+__global__ void __launch_bounds__(RD_ITILE)
+k_force_tts_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
+                const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+                double* __restrict__ partial, int* __restrict__ tickets, int* __restrict__ queue,
+                const int* __restrict__ step_ptr) {
+  __shared__ int s_item;
+  __shared__ rd_d4 sj[RD_TILE];
+  __shared__ int ssp[RD_TILE];
+  const int total = ph->total_items, nd = ph->n_diodes;
+  const int tid = threadIdx.x;
+  const double L2 = c_k.L2, dfc = c_k.div_fac_c, K = c_k.tip_K;
+  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
+    ItemRef it = decode_item(plan, nd, g);
+    const DiodeParams& p = P[it.d];
+    const int off = p.off, n = plan[it.d].n_i;
+    const int i = it.i0 + tid;
+    const bool valid = i < n;
+    const bool ion_step = (*step_ptr - Dy[it.d].step_offset) % p.tts == 0;
+    const bool tip = p.geometry == RD_G_TIP;
+    double x1 = 0, y1 = 0, z1 = 0, q1 = 0;
+    int si = 3;
+    if (valid) {
+      x1 = pool.x[off + i]; y1 = pool.y[off + i]; z1 = pool.z[off + i]; q1 = pool.q[off + i];
+      si = pool.species[off + i];
+    }
+    const double qd1 = q1 * dfc;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
+      __syncthreads();
+      int j = jt + tid;
+      if (j < it.j1) {
+        sj[tid] = make_d4(pool.x[off + j], pool.y[off + j], pool.z[off + j], pool.q[off + j]);
+        ssp[tid] = pool.species[off + j];
+      }
+      __syncthreads();
+      const int kmax = min(RD_TILE, it.j1 - jt);
+      for (int k = 0; k < kmax; ++k) {
+        const int jj = jt + k, sjk = ssp[k];
+        if (jj == i) continue;
+        const bool take = (si == 1 && (sjk == 1 || sjk == 2)) ||
+                          (si == 2 && (sjk == 1 || (sjk == 2 && ion_step)));
+        if (!take) continue;
+        const bool upper = (si != sjk) ? (si == 1) : (jj > i);
+        if (tip)
+          tip_pair_f64(sj[k], x1, y1, z1, qd1, upper, p.image_charge, p, L2, K, ax, ay, az);
+        else
+          planar_pair_f64(sj[k], x1, y1, z1, qd1, upper, p.N_ic_max, p.d, p.image_charge, L2, ax, ay, az);
+      }
+    }
+    if (it.nch > 1) {
+      double* pp = partial + (size_t)g * 3 * RD_ITILE;
+      pp[tid] = ax; pp[RD_ITILE + tid] = ay; pp[2 * RD_ITILE + tid] = az;
+      if (!tile_ticket(tickets, it)) continue;
+      ax = ay = az = 0.0;
+      for (int c = 0; c < it.nch; ++c) {
+        const double* q = partial + (size_t)(it.base + c) * 3 * RD_ITILE;
+        ax += __ldcg(q + tid); ay += __ldcg(q + RD_ITILE + tid); az += __ldcg(q + 2 * RD_ITILE + tid);
+      }
+    }
+    if (valid && (si == 1 || si == 2)) {
+      const int gi = off + i;
+      const double im = 1.0 / pool.m[gi];
+      if (si == 1 || ion_step) {
+        double ex = 0.0, ey = 0.0, ez = p.E_z;
+        if (tip) tip_field_E(p, x1, y1, z1, &ex, &ey, &ez);
+        pool.ax[gi] = (ax + q1 * ex) * im;
+        pool.ay[gi] = (ay + q1 * ey) * im;
+        pool.az[gi] = (az + q1 * ez) * im;
+      } else {
+        pool.ax[gi] += ax * im;
+        pool.ay[gi] += ay * im;
+        pool.az[gi] += az * im;
+      }
+    }
+  }
+  queue_leave(queue, total);
+}
+
 }  // namespace
 
 // Launch wrappers (called by the engine).
@@ -409,6 +498,15 @@ cudaError_t rd_launch_force(int prec, int geometry_mask, int nic_general, int gr
       k_force_tip_f32<<<rd_grid(k_force_tip_f32, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial, tickets, kscale, queue);
     }
   }
+  return cudaGetLastError();
+}
+
+// Two-time-step diodes of both geometries; the plan (PM_FORCE_TTS) holds only them.
+cudaError_t rd_launch_force_tts(int grid, cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy,
+                                const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
+                                double* partial, int* tickets, int* queue, const int* step_ptr) {
+  k_force_tts_f64<<<rd_grid(k_force_tts_f64, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, partial,
+                                                                                 tickets, queue, step_ptr);
   return cudaGetLastError();
 }
 

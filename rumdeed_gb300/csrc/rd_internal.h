@@ -74,7 +74,17 @@ struct DiodeParams {
   double ring_rmin, ring_thick;   // ring emitter: inner radius and width (m)
   int planes_n;          // measurement planes (Check_Planes)
   double planes_z[10];
+  int tts;               // two-time-step interval T (atom_time_interval); 0 off
 };
+
+// Planner modes (k_plan): which i-set of each diode a pair-sum plan covers.
+// Modes up to PM_FORCE_TTS are pair sums (tiles x j-chunks), the two PM_PART
+// modes per-particle index spaces.  PM_ALL_DIODES added to PM_FORCE_PLANAR or
+// PM_FORCE_TIP also covers the two-time-step diodes (the plain
+// Calculate_Acceleration_Particles pass, which ignores two_time_step).
+enum { PM_FORCE_PLANAR = 0, PM_FORCE_TIP = 1, PM_FIELD = 2, PM_SUPPLY_PLANAR = 3,
+       PM_SUPPLY_TIP = 4, PM_MH = 5, PM_FORCE_TTS = 6, PM_PART = 7, PM_PART1024 = 8, PM_COUNT = 9,
+       PM_ALL_DIODES = 0x100 };
 
 // Dynamic per-diode state (device resident, updated by kernels).
 struct DiodeDyn {
@@ -91,7 +101,7 @@ struct DiodeDyn {
   long long emitted_total, absorbed_top_total, absorbed_bot_total, dropped_total;
   long long electron_steps;      // sum over steps of particles in flight
   long long steps_done;
-  double ramo_current;
+  double ramo_current, ramo_ion;   // ramo_current(species_elec), ramo_current(species_ion)
   double MH_std, a_rate, residual, N_sup;
   double F_avg_z, df_avg;   // field.dt quantities of the last emission
   double avg_vel[3];

@@ -145,7 +145,7 @@ extern "C" int rd_field_at_noalloc(rd_engine* e, int diode, int M, const double*
                                  px + RD_NOALLOC_MAX_POINTS, px + 2 * RD_NOALLOC_MAX_POINTS);
   cudaError_t ce = cudaGetLastError();
   if (ce == cudaSuccess)
-    ce = rd_launch_plan(st, P, Dy, 1, /*PM_FIELD*/ 2, rd_engine_chunk_rule(e), NA_MAX_ITEMS, ints, plan, ph);
+    ce = rd_launch_plan(st, P, Dy, 1, PM_FIELD, rd_engine_chunk_rule(e), NA_MAX_ITEMS, ints, plan, ph);
   PointSet pts{px, px + RD_NOALLOC_MAX_POINTS, px + 2 * RD_NOALLOC_MAX_POINTS,
                fx, fx + RD_NOALLOC_MAX_POINTS, fx + 2 * RD_NOALLOC_MAX_POINTS, ints + 1};
   if (ce == cudaSuccess)

@@ -18,9 +18,6 @@
 //    life-time histogram (record_lifetime :1135-1160).
 #include "rd_pair.cuh"
 
-enum { PM_FORCE_PLANAR = 0, PM_FORCE_TIP = 1, PM_FIELD = 2, PM_SUPPLY_PLANAR = 3,
-       PM_SUPPLY_TIP = 4, PM_MH = 5, PM_PART = 6, PM_PART1024 = 7 };
-
 namespace {
 
 __device__ __forceinline__ void mark_remove(const DiodeParams& p, DiodeDyn& y, Pool& pool, int i,
@@ -72,9 +69,11 @@ __device__ __forceinline__ void pack_one(const DiodeParams& p, const Pool& pool,
 __device__ __forceinline__ int plan_ni(const DiodeParams& p, const DiodeDyn& y, int mode,
                                        const int* npts, int d) {
   const int nj = y.n;
-  switch (mode) {
-    case PM_FORCE_PLANAR: return p.geometry == RD_G_PLANAR ? nj : 0;
-    case PM_FORCE_TIP: return p.geometry == RD_G_TIP ? nj : 0;
+  const bool std_force = p.tts == 0 || (mode & PM_ALL_DIODES);   // else k_force_tts
+  switch (mode & 0xff) {
+    case PM_FORCE_PLANAR: return (p.geometry == RD_G_PLANAR && std_force) ? nj : 0;
+    case PM_FORCE_TIP: return (p.geometry == RD_G_TIP && std_force) ? nj : 0;
+    case PM_FORCE_TTS: return p.tts > 0 ? nj : 0;
     case PM_FIELD: return npts[d];
     case PM_SUPPLY_PLANAR: return (p.emission && p.geometry == RD_G_PLANAR) ? p.quad_n * p.quad_n : 0;
     case PM_SUPPLY_TIP: return (p.emission && p.geometry == RD_G_TIP) ? 10000 : 0;
@@ -114,7 +113,7 @@ k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int n
   __shared__ int s_run_items, s_run_chains;
   const int tid = threadIdx.x;
   const int tsize = (mode == PM_PART1024) ? 1024 : RD_ITILE;
-  const bool pair = (mode <= PM_MH);
+  const bool pair = ((mode & 0xff) <= PM_FORCE_TTS);
   const int clen_min = chunk_rule & 0xffff, nch_max = chunk_rule >> 16;   // see rd_chunk_rule
   // grow the chunk length only if the items would not fit the scratch
   __shared__ int s_grow;
@@ -213,20 +212,34 @@ k_position(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool po
     if (!part_index(plan, ph, g, &d, &i)) continue;
     const DiodeParams& p = P[d];
     const int gi = p.off + i;
-    if (pool.species[gi] != 3) {
+    const int sp = pool.species[gi];
+    DiodeDyn& yy = Dy[d];
+    const int step = *step_ptr - yy.step_offset;
+    // two-time-step diodes: ions move only on steps divisible by T, with the
+    // step T*dt (Update_Species_Position, src/mod_verlet.F90:234-290); T = 1
+    // takes the plain formula (the factor 1 is exact), so it stays bit-equal
+    // to the standard integrator whatever the compiler contracts
+    const bool slow = p.tts > 1 && sp == 2;
+    if (sp != 3 && !(slow && step % p.tts != 0)) {
       const double dt = p.dt, dt2 = p.dt2;
       double ax = pool.ax[gi], ay = pool.ay[gi], az = pool.az[gi];
       double bx = pool.bx[gi], by = pool.by[gi], bz = pool.bz[gi];
       const double z_prev = pool.z[gi];
-      double x = (pool.x[gi] + pool.vx[gi] * dt) + ((1.0 / 6.0) * (4.0 * ax - bx)) * dt2;
-      double y = (pool.y[gi] + pool.vy[gi] * dt) + ((1.0 / 6.0) * (4.0 * ay - by)) * dt2;
-      double z = (z_prev + pool.vz[gi] * dt) + ((1.0 / 6.0) * (4.0 * az - bz)) * dt2;
+      double x, y, z;
+      if (!slow) {
+        x = (pool.x[gi] + pool.vx[gi] * dt) + ((1.0 / 6.0) * (4.0 * ax - bx)) * dt2;
+        y = (pool.y[gi] + pool.vy[gi] * dt) + ((1.0 / 6.0) * (4.0 * ay - by)) * dt2;
+        z = (z_prev + pool.vz[gi] * dt) + ((1.0 / 6.0) * (4.0 * az - bz)) * dt2;
+      } else {
+        const double T = (double)p.tts, T2 = T * T;
+        x = (pool.x[gi] + (pool.vx[gi] * dt) * T) + (((1.0 / 6.0) * (4.0 * ax - bx)) * dt2) * T2;
+        y = (pool.y[gi] + (pool.vy[gi] * dt) * T) + (((1.0 / 6.0) * (4.0 * ay - by)) * dt2) * T2;
+        z = (z_prev + (pool.vz[gi] * dt) * T) + (((1.0 / 6.0) * (4.0 * az - bz)) * dt2) * T2;
+      }
       pool.x[gi] = x; pool.y[gi] = y; pool.z[gi] = z;
       pool.cx[gi] = bx; pool.cy[gi] = by; pool.cz[gi] = bz;
       pool.bx[gi] = ax; pool.by[gi] = ay; pool.bz[gi] = az;
       pool.ax[gi] = 0.0; pool.ay[gi] = 0.0; pool.az[gi] = 0.0;
-      DiodeDyn& yy = Dy[d];
-      const int step = *step_ptr - yy.step_offset;
       for (int k = 0; k < p.planes_n; ++k) {   // Check_Planes (src/mod_verlet.F90:343-367)
         const double zp = p.planes_z[k];
         if (zp > 0.0 && z > zp && z_prev < zp)
@@ -242,21 +255,35 @@ k_position(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool po
 }
 
 __global__ void __launch_bounds__(RD_ITILE)
-k_velocity(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __restrict__ plan,
-           const PlanHeader* __restrict__ ph, double* __restrict__ ramo) {
+k_velocity(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
+           const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+           double* __restrict__ ramo, const int* __restrict__ step_ptr) {
   for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
     int d, i;
     if (!part_index(plan, ph, g, &d, &i)) continue;
     const DiodeParams& p = P[d];
     const int gi = p.off + i;
+    const int sp = pool.species[gi];
     double r = 0.0;
-    if (pool.species[gi] != 3) {
+    // two-time-step diodes: ions only on steps divisible by T, with the step
+    // T*dt (Update_Species_Velocity, src/mod_verlet.F90:511-590); T = 1 as in
+    // k_position
+    const bool slow = p.tts > 1 && sp == 2;
+    if (sp != 3 && !(slow && (*step_ptr - Dy[d].step_offset) % p.tts != 0)) {
       const double dt = p.dt;
-      double vx = pool.vx[gi] + ((1.0 / 6.0) * ((2.0 * pool.ax[gi] + 5.0 * pool.bx[gi]) - pool.cx[gi])) * dt;
-      double vy = pool.vy[gi] + ((1.0 / 6.0) * ((2.0 * pool.ay[gi] + 5.0 * pool.by[gi]) - pool.cy[gi])) * dt;
-      double vz = pool.vz[gi] + ((1.0 / 6.0) * ((2.0 * pool.az[gi] + 5.0 * pool.bz[gi]) - pool.cz[gi])) * dt;
+      double vx, vy, vz;
+      if (!slow) {
+        vx = pool.vx[gi] + ((1.0 / 6.0) * ((2.0 * pool.ax[gi] + 5.0 * pool.bx[gi]) - pool.cx[gi])) * dt;
+        vy = pool.vy[gi] + ((1.0 / 6.0) * ((2.0 * pool.ay[gi] + 5.0 * pool.by[gi]) - pool.cy[gi])) * dt;
+        vz = pool.vz[gi] + ((1.0 / 6.0) * ((2.0 * pool.az[gi] + 5.0 * pool.bz[gi]) - pool.cz[gi])) * dt;
+      } else {
+        const double T = (double)p.tts;
+        vx = pool.vx[gi] + (((1.0 / 6.0) * ((2.0 * pool.ax[gi] + 5.0 * pool.bx[gi]) - pool.cx[gi])) * dt) * T;
+        vy = pool.vy[gi] + (((1.0 / 6.0) * ((2.0 * pool.ay[gi] + 5.0 * pool.by[gi]) - pool.cy[gi])) * dt) * T;
+        vz = pool.vz[gi] + (((1.0 / 6.0) * ((2.0 * pool.az[gi] + 5.0 * pool.bz[gi]) - pool.cz[gi])) * dt) * T;
+      }
       pool.vx[gi] = vx; pool.vy[gi] = vy; pool.vz[gi] = vz;
-      if (pool.species[gi] == 1) {
+      {   // ramo_current(species): electrons and ions
         double ux, uy, uz;
         if (p.geometry == RD_G_TIP) {   // E_zunit_tip
           double ex, ey, ez;
@@ -272,24 +299,34 @@ k_velocity(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __rest
   }
 }
 
-// Ramo current and electron-step count per diode (fixed-order reduction).
+// Ramo current per species and electron-step count per diode (fixed-order
+// reduction).
 __global__ void __launch_bounds__(256)
-k_ramo(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, const double* __restrict__ ramo) {
-  __shared__ double red[256];
+k_ramo(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, const double* __restrict__ ramo,
+       const int* __restrict__ species) {
+  __shared__ double red[256], red_ion[256];
   const int d = blockIdx.x;
   const DiodeParams& p = P[d];
   if (!p.active) return;
   const int n = Dy[d].n;
-  double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += ramo[p.off + i];
+  double s = 0.0, si = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double r = ramo[p.off + i];
+    if (species[p.off + i] == 2) si += r; else s += r;
+  }
   red[threadIdx.x] = s;
+  red_ion[threadIdx.x] = si;
   __syncthreads();
   for (int k = blockDim.x / 2; k > 0; k >>= 1) {
-    if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    if (threadIdx.x < k) {
+      red[threadIdx.x] += red[threadIdx.x + k];
+      red_ion[threadIdx.x] += red_ion[threadIdx.x + k];
+    }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     Dy[d].ramo_current = red[0];
+    Dy[d].ramo_ion = red_ion[0];
     Dy[d].electron_steps += n;
     Dy[d].steps_done += 1;
   }
@@ -429,9 +466,9 @@ cudaError_t rd_launch_position(int grid, cudaStream_t st, const DiodeParams* P, 
 }
 cudaError_t rd_launch_velocity(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
                                DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
-                               const PlanHeader* ph, double* ramo) {
-  k_velocity<<<rd_grid(k_velocity, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph, ramo);
-  k_ramo<<<nslots, 256, 0, st>>>(P, Dy, ramo);
+                               const PlanHeader* ph, double* ramo, const int* step_ptr) {
+  k_velocity<<<rd_grid(k_velocity, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, ramo, step_ptr);
+  k_ramo<<<nslots, 256, 0, st>>>(P, Dy, ramo, pool.species);
   return cudaGetLastError();
 }
 cudaError_t rd_launch_compact(int grid, int nslots, cudaStream_t st, const DiodeParams* P,

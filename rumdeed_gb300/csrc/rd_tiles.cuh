@@ -85,6 +85,45 @@ __device__ __forceinline__ void planar_tile_f32(const float4* __restrict__ sh, c
 }
 
 // ---- planar, FP64 (reference arithmetic) ---------------------------------------
+// One pair (i, j): Coulomb term plus, with image charges on, the planar
+// series of acc_ic_planar_series.inc with i in the "a" role when upper and j
+// in it otherwise (the x, y parts then change sign: force_ic_N).
+__device__ __forceinline__ void planar_pair_f64(const rd_d4& pj, double x1, double y1, double z1,
+                                                double qd1, bool upper, int nic, double d, int ic,
+                                                double L2, double& ax, double& ay, double& az) {
+  double pre = qd1 * pj.w;
+  double dx = x1 - pj.x, dy = y1 - pj.y, dz = z1 - pj.z;
+  double dxy2 = dx * dx + dy * dy;
+  double r = sqrt(dxy2 + dz * dz) + L2;
+  double inv = 1.0 / ((r * r) * r);
+  ax = ax + (pre * inv) * dx;
+  ay = ay + (pre * inv) * dy;
+  az = az + (pre * inv) * dz;
+  if (ic) {
+    double za = upper ? z1 : pj.z, zb = upper ? pj.z : z1;
+    // acc_ic_planar_series.inc
+    double zic = -1.0 * zb, dzi = za - zic;
+    r = sqrt(dxy2 + dzi * dzi) + L2;
+    inv = 1.0 / ((r * r) * r);
+    double icx = -dx * inv, icy = -dy * inv, icz = -dzi * inv;
+    for (int n = 1; n <= nic; ++n) {
+      double zz0 = (2.0 * n) * d - zb, zz1 = (-2.0 * n) * d - zb;
+      double zz2 = (2.0 * n) * d + zb, zz3 = (-2.0 * n) * d + zb;
+      dzi = za - zz0; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
+      icx = icx - dx * inv; icy = icy - dy * inv; icz = icz - dzi * inv;
+      dzi = za - zz1; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
+      icx = icx - dx * inv; icy = icy - dy * inv; icz = icz - dzi * inv;
+      dzi = za - zz2; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
+      icx = icx + dx * inv; icy = icy + dy * inv; icz = icz + dzi * inv;
+      dzi = za - zz3; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
+      icx = icx + dx * inv; icy = icy + dy * inv; icz = icz + dzi * inv;
+    }
+    ax = ax + pre * icx;
+    ay = ay + pre * icy;
+    az = az + pre * icz;
+  }
+}
+
 template <int MODE>
 __device__ __forceinline__ void planar_tile_f64(const rd_d4* __restrict__ sj, int kmax, double x1,
                                                 double y1, double z1, double qd1, int self_k,
@@ -92,39 +131,8 @@ __device__ __forceinline__ void planar_tile_f64(const rd_d4* __restrict__ sj, in
                                                 double& ax, double& ay, double& az) {
   for (int k = 0; k < kmax; ++k) {
     if (MODE == T_DIAG && k == self_k) continue;
-    rd_d4 pj = sj[k];
-    double pre = qd1 * pj.w;
-    double dx = x1 - pj.x, dy = y1 - pj.y, dz = z1 - pj.z;
-    double dxy2 = dx * dx + dy * dy;
-    double r = sqrt(dxy2 + dz * dz) + L2;
-    double inv = 1.0 / ((r * r) * r);
-    ax = ax + (pre * inv) * dx;
-    ay = ay + (pre * inv) * dy;
-    az = az + (pre * inv) * dz;
-    if (ic) {
-      bool upper = (MODE == T_UPPER) || (MODE == T_DIAG && k > self_k);
-      double za = upper ? z1 : pj.z, zb = upper ? pj.z : z1;
-      // acc_ic_planar_series.inc
-      double zic = -1.0 * zb, dzi = za - zic;
-      r = sqrt(dxy2 + dzi * dzi) + L2;
-      inv = 1.0 / ((r * r) * r);
-      double icx = -dx * inv, icy = -dy * inv, icz = -dzi * inv;
-      for (int n = 1; n <= nic; ++n) {
-        double zz0 = (2.0 * n) * d - zb, zz1 = (-2.0 * n) * d - zb;
-        double zz2 = (2.0 * n) * d + zb, zz3 = (-2.0 * n) * d + zb;
-        dzi = za - zz0; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
-        icx = icx - dx * inv; icy = icy - dy * inv; icz = icz - dzi * inv;
-        dzi = za - zz1; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
-        icx = icx - dx * inv; icy = icy - dy * inv; icz = icz - dzi * inv;
-        dzi = za - zz2; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
-        icx = icx + dx * inv; icy = icy + dy * inv; icz = icz + dzi * inv;
-        dzi = za - zz3; r = sqrt(dxy2 + dzi * dzi) + L2; inv = 1.0 / ((r * r) * r);
-        icx = icx + dx * inv; icy = icy + dy * inv; icz = icz + dzi * inv;
-      }
-      ax = ax + pre * icx;
-      ay = ay + pre * icy;
-      az = az + pre * icz;
-    }
+    const bool upper = (MODE == T_UPPER) || (MODE == T_DIAG && k > self_k);
+    planar_pair_f64(sj[k], x1, y1, z1, qd1, upper, nic, d, ic, L2, ax, ay, az);
   }
 }
 
@@ -187,40 +195,46 @@ __device__ __forceinline__ void tip_tile_f32(const float4* __restrict__ sh, cons
 }
 
 // FP64 tip gather: Calculate_Acceleration_Particles_ACC tip branch (:1344-1426).
+// One pair (i, j); upper: i is the lower-indexed ("a") particle.
+__device__ __forceinline__ void tip_pair_f64(const rd_d4& pj, double x1, double y1, double z1,
+                                             double qd1, bool upper, int ic, const DiodeParams& p,
+                                             double L2, double K, double& ax, double& ay,
+                                             double& az) {
+  const double z0 = p.h_tip - p.r_tip, R = p.r_tip;
+  double pre = qd1 * pj.w;
+  double dx = x1 - pj.x, dy = y1 - pj.y, dz = z1 - pj.z;
+  double r = sqrt(dx * dx + dy * dy + dz * dz) + L2;
+  double inv = 1.0 / ((r * r) * r);
+  ax = ax + (pre * inv) * dx;
+  ay = ay + (pre * inv) * dy;
+  az = az + (pre * inv) * dz;
+  if (ic) {
+    double xa = upper ? x1 : pj.x, ya = upper ? y1 : pj.y, za = upper ? z1 : pj.z;
+    double xb = upper ? pj.x : x1, yb = upper ? pj.y : y1, zb = upper ? pj.z : z1;
+    double sgn = upper ? 1.0 : -1.0;
+    double dza = za - z0;
+    double dis = sqrt(xa * xa + ya * ya + dza * dza);
+    double zim = z0 + (R * R) / (sqrt((1.0 + (xa * xa) / (dza * dza)) + (ya * ya) / (dza * dza)) * dis);
+    double xim = ((zim - z0) * xa) / dza, yim = ((zim - z0) * ya) / dza;
+    double tda = pow((xb - xa) * (xb - xa) + (yb - ya) * (yb - ya) + (zb - za) * (zb - za), 1.5);
+    double tdb = pow((xb - xim) * (xb - xim) + (yb - yim) * (yb - yim) + (zb - zim) * (zb - zim), 1.5);
+    double icx = K * ((xa - xb) / tda - (R * (xim - xb)) / (dis * tdb));
+    double icy = K * ((ya - yb) / tda - (R * (yim - yb)) / (dis * tdb));
+    double icz = K * ((za - zb) / tda - (R * (zim - zb)) / (dis * tdb));
+    ax = ax + pre * sgn * icx;
+    ay = ay + pre * sgn * icy;
+    az = az + pre * icz;
+  }
+}
+
 template <int MODE>
 __device__ __forceinline__ void tip_tile_f64(const rd_d4* __restrict__ sj, int kmax, double x1,
                                              double y1, double z1, double qd1, int self_k, int ic,
                                              const DiodeParams& p, double L2, double K,
                                              double& ax, double& ay, double& az) {
-  const double z0 = p.h_tip - p.r_tip, R = p.r_tip;
   for (int k = 0; k < kmax; ++k) {
     if (MODE == T_DIAG && k == self_k) continue;
-    rd_d4 pj = sj[k];
-    double pre = qd1 * pj.w;
-    double dx = x1 - pj.x, dy = y1 - pj.y, dz = z1 - pj.z;
-    double r = sqrt(dx * dx + dy * dy + dz * dz) + L2;
-    double inv = 1.0 / ((r * r) * r);
-    ax = ax + (pre * inv) * dx;
-    ay = ay + (pre * inv) * dy;
-    az = az + (pre * inv) * dz;
-    if (ic) {
-      bool upper = (MODE == T_UPPER) || (MODE == T_DIAG && k > self_k);
-      double xa = upper ? x1 : pj.x, ya = upper ? y1 : pj.y, za = upper ? z1 : pj.z;
-      double xb = upper ? pj.x : x1, yb = upper ? pj.y : y1, zb = upper ? pj.z : z1;
-      double sgn = upper ? 1.0 : -1.0;
-      double dza = za - z0;
-      double dis = sqrt(xa * xa + ya * ya + dza * dza);
-      double zim = z0 + (R * R) / (sqrt((1.0 + (xa * xa) / (dza * dza)) + (ya * ya) / (dza * dza)) * dis);
-      double xim = ((zim - z0) * xa) / dza, yim = ((zim - z0) * ya) / dza;
-      double tda = pow((xb - xa) * (xb - xa) + (yb - ya) * (yb - ya) + (zb - za) * (zb - za), 1.5);
-      double tdb = pow((xb - xim) * (xb - xim) + (yb - yim) * (yb - yim) + (zb - zim) * (zb - zim), 1.5);
-      double icx = K * ((xa - xb) / tda - (R * (xim - xb)) / (dis * tdb));
-      double icy = K * ((ya - yb) / tda - (R * (yim - yb)) / (dis * tdb));
-      double icz = K * ((za - zb) / tda - (R * (zim - zb)) / (dis * tdb));
-      ax = ax + pre * sgn * icx;
-      ay = ay + pre * sgn * icy;
-      az = az + pre * icz;
-    }
+    const bool upper = (MODE == T_UPPER) || (MODE == T_DIAG && k > self_k);
+    tip_pair_f64(sj[k], x1, y1, z1, qd1, upper, ic, p, L2, K, ax, ay, az);
   }
 }
-

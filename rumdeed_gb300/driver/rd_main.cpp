@@ -216,6 +216,8 @@ int main(int argc, char** argv) {
   dc.mh_jumps = (int)get(gb, "MH_JUMPS", 0, 0.0);
   dc.seed = (unsigned long long)get(gb, "SEED", 0, 20261203.0);
   dc.emitter_delay = (int)get(in, "EMITTERS_DELAY", 0, 0.0);
+  dc.atom_time_interval = (int)get(in, "ATOM_TIME_INTERVAL", 0, 0.0);   // two_time_step when > 0
+  if (dc.atom_time_interval < 0) { std::fprintf(stderr, "rd_main: atom_time_interval must be >= 0\n"); return 2; }
   dc.planes_N = (int)get(in, "PLANES_N", 0, 0.0);
   if (dc.planes_N < 0 || dc.planes_N > 10) { std::fprintf(stderr, "rd_main: planes_N must be in [0, 10]\n"); return 2; }
   for (int k = 0; k < dc.planes_N; ++k) dc.planes_z[k] = get(in, "PLANES_Z", k, -1.0) * length_scale;
@@ -282,12 +284,12 @@ int main(int argc, char** argv) {
     std::printf("geometry %d\nV_s %.17g\ngap %.17g\ntime_step %.17g\nsteps %d\nimage_charge %d\n"
                 "N_ic_max %d\ncapacity %d\nseed %llu\nemitter_pos %.17g %.17g\nemitter_dim %.17g %.17g\n"
                 "work %d x %d\nwork_model %d\ntip_dim %.17g %.17g %.17g\nE14.6 %s\nES12.4 %s\n"
-                "emitter_delay %d\nplanes %d\nemitter_type %d\nmh_serial %d\n",
+                "emitter_delay %d\nplanes %d\nemitter_type %d\nmh_serial %d\natom_time_interval %d\n",
                 dc.geometry, dc.V_s, dc.gap, dc.time_step, steps, dc.image_charge, dc.N_ic_max,
                 dc.capacity, dc.seed, dc.emitter_pos[0], dc.emitter_pos[1], dc.emitter_dim[0],
                 dc.emitter_dim[1], dc.work_ny, dc.work_nx, dc.work_model, dc.tip_dim[0], dc.tip_dim[1], dc.tip_dim[2],
                 fmt_E(dt / time_scale, 14, 6).c_str(), fmt_ES(dt / time_scale, 12, 4).c_str(), dc.emitter_delay,
-                dc.planes_N, dc.emitter_type, dc.mh_serial);
+                dc.planes_N, dc.emitter_type, dc.mh_serial, dc.atom_time_interval);
     for (int k = 0; k < dc.planes_N; ++k) std::printf("plane_z %.17g\n", dc.planes_z[k]);
     for (double w : work) std::printf("work_value %.17g\n", w);
     return 0;

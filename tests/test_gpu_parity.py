@@ -484,3 +484,86 @@ def test_ring_emitter_fp64_matches_oracle(rg, orc):
     r = np.hypot(new[:, 0], new[:, 1])
     assert np.all(r >= r_out - w - 1e-15) and np.all(r <= r_out + 1e-15)   # emitted on the ring
     eng.close()
+
+
+def _tts_pair(rg, orc, geometry, T, n=300, nic=1, seed=21):
+    """A diode under the two-time-step integrator on the GPU and in the
+    oracle: electrons with every fourth particle an ion (the first one too,
+    so electron-ion pairs take both index orders)."""
+    rng = np.random.default_rng(seed)
+    tip = (900 * NM, 100 * NM, 100 * NM)
+    if geometry == "tip":
+        pos = np.column_stack([rng.uniform(-300 * NM, 300 * NM, n), rng.uniform(-300 * NM, 300 * NM, n),
+                               rng.uniform(105 * NM, 990 * NM, n)])
+    else:
+        pos = uniform_particles(rng, n)
+    vel = rng.normal(0.0, 2e4, (n, 3))
+    sp = np.where(np.arange(n) % 4 == 0, 2, 1)
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=2, particle_capacity=4096)
+    kw = dict(V_s=2e3, capacity=1024, image_charge=True, atom_time_interval=T)
+    if geometry == "tip":
+        dio = eng.add_diode(geometry=rg.GEOM_TIP, tip_dim=tip, **kw)
+        o = orc.OracleDiode(orc.TIP, cap=1024, V_s=2e3, d=1000 * NM, image_charge=True)
+        o.set_tip(*tip, 4.7)
+    else:
+        dio = eng.add_diode(gap=1000 * NM, N_ic_max=nic, **kw)
+        o = orc.OracleDiode(cap=1024, V_s=2e3, d=1000 * NM, image_charge=True, N_ic_max=nic)
+    dio.add_particles(pos, vel=vel, species=sp)
+    for p, v, s in zip(pos, vel, sp):
+        o.add(p, vel=v, species=int(s))
+    o.set_tts(T)
+    return eng, dio, o, sp
+
+
+@pytest.mark.parametrize("geometry", ["planar", "tip"])
+def test_two_time_step_fp64_matches_oracle(rg, orc, geometry):
+    """atom_time_interval = 3 (Update_Species_Position / _Velocity,
+    Update_Elec_Acceleration / Update_Ion_Acceleration): electrons every
+    step, ions on steps 3 and 6 with the step 3 dt, ion accelerations
+    gathering electron forces in between; trajectories, accelerations and
+    both Ramo currents agree with the oracle at every step."""
+    eng, dio, o, sp = _tts_pair(rg, orc, geometry, 3)
+    ion = sp == 2
+    for step in range(1, 8):
+        eng.update_position(step)
+        o.verlet(step)
+        p = dio.particles()
+        assert np.max(np.abs(p["pos"] - o.arr("pos"))) < 1e-9 * NM, step
+        assert nrel(p["vel"], o.arr("vel")) < 1e-11, step
+        assert nrel(p["acc"], o.arr("acc")) < 1e-11, step
+        c = dio.counters()
+        assert c["ramo_current"] == pytest.approx(o.s.ramo_current, rel=1e-11)
+        assert c["ramo_current_ion"] == pytest.approx(o.s.ramo_current_ion, rel=1e-11, abs=1e-30)
+        assert (c["ramo_current_ion"] != 0.0) == (step % 3 == 0), step
+    # the ions moved on steps 3 and 6 only
+    eng.close()
+
+
+def test_two_time_step_interval_one_equals_standard(rg, orc):
+    """Test_TTS_Equivalence (src/mod_tests.F90:1455-1545) on the GPU: with
+    atom_time_interval = 1 and the ions after the electrons, a two-time-step
+    diode and a standard diode of the same engine step bit for bit alike; the
+    plain acceleration pass (rd_accel) ignores the interval."""
+    rng = np.random.default_rng(8)
+    n = 257
+    pos = uniform_particles(rng, n)
+    vel = rng.normal(0.0, 2e4, (n, 3))
+    sp = np.where(np.arange(n) >= n - 40, 2, 1)
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=4, particle_capacity=4096)
+    a = eng.add_diode(V_s=2e3, gap=1000 * NM, capacity=1024, N_ic_max=2)
+    b = eng.add_diode(V_s=2e3, gap=1000 * NM, capacity=1024, N_ic_max=2, atom_time_interval=1)
+    for dio in (a, b):
+        dio.add_particles(pos, vel=vel, species=sp)
+    o = orc.OracleDiode(cap=1024, V_s=2e3, d=1000 * NM, image_charge=True, N_ic_max=2)
+    for p, v, s in zip(pos, vel, sp):
+        o.add(p, vel=v, species=int(s))
+    assert nrel(b.calculate_acceleration_particles(), o.accel("gather", True)) <= TOL64
+    for step in range(1, 4):
+        eng.update_position(step)
+    pa, pb = a.particles(), b.particles()
+    for k in ("pos", "vel", "acc"):
+        assert np.array_equal(pa[k], pb[k]), k
+    ca, cb = a.counters(), b.counters()
+    assert ca["ramo_current"] == cb["ramo_current"]
+    assert ca["ramo_current_ion"] == cb["ramo_current_ion"] != 0.0
+    eng.close()

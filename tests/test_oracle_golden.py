@@ -371,3 +371,66 @@ def test_gaussian_work_function_formula(orc):
         expect = 4.5 - 0.5 * np.exp(-(((x - 10e-9) ** 2) / (2 * (30e-9) ** 2) + ((y + 20e-9) ** 2) / (2 * (40e-9) ** 2))) \
             + 0.25 * np.exp(-((x ** 2) / (2 * (5e-9) ** 2) + (y ** 2) / (2 * (5e-9) ** 2)))
         assert orc.lib().orc_work_gaussian(dp(w), 2, x, y) == pytest.approx(expect, rel=1e-14)
+
+
+def _tts_system(orc, tts, ion_first=False, nic=0):
+    """Two electrons and one ion a few nm apart (Test_TTS_Equivalence,
+    src/mod_tests.F90:1460-1488), optionally with the ion added first."""
+    o = orc.OracleDiode(cap=8, V_s=2.0e3, d=1000 * NM, time_step=0.25e-15, image_charge=True,
+                        N_ic_max=nic)
+    R0 = np.array([[1.0, -2.0, 500.0], [3.0, 4.0, 503.0], [-2.0, 1.0, 505.0]]) * NM
+    V0 = np.array([[1.0e3, 0.0, 0.0], [0.0, -1.0e3, 0.0], [0.0, 0.0, 0.0]])
+    spc = [orc.ELEC, orc.ELEC, orc.ION]
+    order = [2, 0, 1] if ion_first else [0, 1, 2]
+    for i in order:
+        o.add(R0[i], vel=V0[i], species=spc[i])
+    o.set_tts(tts)
+    return o
+
+
+def test_tts_equivalence(orc):
+    """Test_TTS_Equivalence, src/mod_tests.F90:1455-1545: with
+    atom_time_interval = 1 the two-time-step integrator reproduces the
+    standard one (trajectories, velocities, both Ramo currents) over 3 steps,
+    and the field summed over the species lists equals the plain field."""
+    ref = _tts_system(orc, 0)
+    tts = _tts_system(orc, 1)
+    probe = np.array([[0.0, 1.0, 502.0]]) * NM
+    close(tts.field_at(probe)[0], ref.field_at(probe)[0])
+    for i in range(1, 4):
+        ref.verlet(i)
+        tts.verlet(i)
+    for k in range(3):
+        close(tts.arr("pos")[k] / NM, ref.arr("pos")[k] / NM)
+        close(tts.arr("vel")[k], ref.arr("vel")[k])
+    close(tts.s.ramo_current * 1e9, ref.s.ramo_current * 1e9)
+    close(tts.s.ramo_current_ion * 1e9, ref.s.ramo_current_ion * 1e9)
+    # beyond the reference's 2 %: the same arithmetic up to summation order
+    np.testing.assert_allclose(tts.arr("pos"), ref.arr("pos"), rtol=1e-14, atol=0)
+    np.testing.assert_allclose(tts.arr("vel"), ref.arr("vel"), rtol=1e-12, atol=1e-12)
+    assert ref.s.ramo_current_ion != 0.0
+
+
+def test_tts_ion_moves_every_T_steps(orc):
+    """A lone ion in the vacuum field under atom_time_interval = 3: it stays
+    put between its steps and, Beeman being exact for a constant
+    acceleration, sits at z0 + a (3 k dt)^2 / 2 after k of them
+    (Update_Species_Position / Update_Species_Velocity with nrStep = 3)."""
+    k = orc.constants()
+    d, V, dt, T = 1000 * NM, 2.0e3, 0.25e-15, 3
+    o = orc.OracleDiode(cap=4, V_s=V, d=d, time_step=dt, image_charge=False)
+    z0 = 500 * NM
+    o.add([0.0, 0.0, z0], species=orc.ION)
+    o.set_tts(T)
+    a = k["q_0"] * (-V / d) / k["m_N2p"] * -1.0   # E_z = -V/d, charge +q0
+    for step in range(1, 10):
+        before = o.arr("pos")[0].copy()
+        o.verlet(step)
+        z = o.arr("pos")[0][2]
+        if step % T:
+            assert z == before[2]
+        else:
+            t = step * dt
+            assert z == pytest.approx(z0 - 0.5 * a * t * t, rel=1e-12)
+            assert o.arr("vel")[0][2] == pytest.approx(-a * t, rel=1e-12)
+            assert o.s.ramo_current_ion != 0.0
