@@ -511,6 +511,7 @@ def case_micro(args):
                                 chain_capacity=4096, quad_capacity=4096)
                 d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, capacity=N, image_charge=True, N_ic_max=nic)
                 d.add_particles(pos)
+                tune = eng.autotune()   # chunking for this system size (the project's tuner)
                 acc = d.calculate_acceleration_particles()
                 reps = 1 if pairs * terms > 2e11 else (3 if pairs > 1e9 else 20)
                 ms = eng.time_accel(reps)
@@ -519,7 +520,9 @@ def case_micro(args):
                 res[tag] = (acc, fld)
                 out[tag] = {"force_ms": ms, "force_pairs_per_s": pairs / (ms / 1e3),
                             "force_tflops": 20.0 * terms * pairs / (ms / 1e3) / 1e12,
-                            "field_ms": fms, "field_point_particle_per_s": grid.shape[0] * N / (fms / 1e3)}
+                            "field_ms": fms, "field_point_particle_per_s": grid.shape[0] * N / (fms / 1e3),
+                            "chunking": {"chunk_min": tune["chunk_min"],
+                                         "chunk_count_max": tune["chunk_count_max"]}}
                 if prec == rg.PREC_FP32C and peak:
                     out[tag]["force_frac_of_measured_fp32"] = out[tag]["force_tflops"] / peak
                 eng.close()

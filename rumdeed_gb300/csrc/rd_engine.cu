@@ -1124,7 +1124,7 @@ int rd_autotune(rd_engine* e, rd_tune_result* out) {
   const int saved_min = e->clen_min, saved_max = e->nch_max;
   double best = 1e300, at_default = 0.0;
   int best_min = saved_min, best_max = saved_max;
-  const int mins[] = {512, 1024, 2048};
+  const int mins[] = {128, 256, 512, 1024, 2048};   // short chunks: more items for small systems
   const int maxs[] = {8, 16, 32};
   for (int a : mins)
     for (int b : maxs) {

@@ -992,10 +992,12 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
 // apex-sphere image, tip_tile_f32<T_UPPER>); one shared load feeds all of the
 // thread's points.  The tip image term of the reference carries an extra
 // factor K = q0 / (4 pi eps0) (acc_tip_ic_force.inc:17-22):
-//   E = sum_j q_j [ d/|d|^3 + K (d/|d|^3 - c e/|e|^3) ] = (1 + K) D - K S,
-// D = sum q d/|d|^3, S = sum q c e/|e|^3; the two sums are kept apart here
-// (td, te) and combined in FP64 by the caller, so the K-scaled image part is
-// not lost below the FP32 resolution of the direct part.  The proposals sit
+//   E = sum_j q_j [ d/|d|^3 + K (d/|d|^3 - c e/|e|^3) ] = (1 + K) D - K c S,
+// D = sum q d/|d|^3, S = sum q e/|e|^3, c = R / dis of the point (applied by
+// the caller); the two sums are kept apart here (td, te) and combined in
+// FP64 by the caller, so the K-scaled image part is not lost below the FP32
+// resolution of the direct part.  (A packed FP32x2 form of this tile ran no
+// faster: the FMA pipe, 75 % busy, is the limit either way.)  The proposals sit
 // on the FP32 nm grid (k_mh_propose), so d = (p - x_hi) - x_lo.  S is formed
 // from high words only (e = image_hi - x_hi): its relative error, ~1e-5 for
 // the nearest charges, is ~1e-14 of the field once scaled by K.
@@ -1024,7 +1026,7 @@ __device__ __forceinline__ void tip_point_tiles_f32(const float4* __restrict__ s
         const float ey = iih[q].y - h.y;
         const float ez = iih[q].z - h.z;
         const float re = rsqrtf(fmaf(ez, ez, fmaf(ex, ex, fmaf(ey, ey, 1e-20f))));
-        const float se = (qj * iih[q].w) * ((re * re) * re);
+        const float se = qj * ((re * re) * re);
         ex_[q] = fmaf(se, ex, ex_[q]);
         ey_[q] = fmaf(se, ey, ey_[q]);
         ez_[q] = fmaf(se, ez, ez_[q]);
@@ -1046,7 +1048,8 @@ __device__ __forceinline__ void tip_point_tiles_f32(const float4* __restrict__ s
 // j-chunk; the CTA completing a tile projects the total field (plus the
 // hyperboloid vacuum field) on the surface normal and runs the accept /
 // reject test (Metro_algo_tip_v3, src/mod_emission_tip.f90:1351-1389).
-// FP32: 64 threads, two chains each; FP64: 128 threads, one chain each.
+// FP32: RD_TIP_CPT chains per thread (RD_ITILE / RD_TIP_CPT threads); FP64:
+// 128 threads, one chain each.
 template <int PREC>
 __global__ void __launch_bounds__(RD_ITILE)
 k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
@@ -1056,7 +1059,7 @@ k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool
               int* __restrict__ queue) {
   __shared__ int s_item;
   __shared__ int red_i[2 * RD_ITILE];
-  constexpr int CPT = PREC == 1 ? 2 : 1;
+  constexpr int CPT = PREC == 1 ? RD_TIP_CPT : 1;
   const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   const bool init = it_idx == 0;
@@ -1114,9 +1117,10 @@ k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool
       const double K = c_k.tip_K, cd = p.image_charge ? (1.0 + K) * kscale : kscale, ce = K * kscale;
 #pragma unroll
       for (int q = 0; q < CPT; ++q) {
-        f3[q][0] = ((double)accd[q].hx + (double)accd[q].lx) * cd - (double)acce[q][0] * ce;
-        f3[q][1] = ((double)accd[q].hy + (double)accd[q].ly) * cd - (double)acce[q][1] * ce;
-        f3[q][2] = ((double)accd[q].hz + (double)accd[q].lz) * cd - (double)acce[q][2] * ce;
+        const double cq = ce * (double)iih[q].w;
+        f3[q][0] = ((double)accd[q].hx + (double)accd[q].lx) * cd - (double)acce[q][0] * cq;
+        f3[q][1] = ((double)accd[q].hy + (double)accd[q].ly) * cd - (double)acce[q][1] * cq;
+        f3[q][2] = ((double)accd[q].hz + (double)accd[q].lz) * cd - (double)acce[q][2] * cq;
       }
     } else {
       __shared__ rd_d4 sj[RD_TILE];
@@ -1613,7 +1617,7 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
   if (geometry_mask & 2) {
     k_mh_propose<<<rd_grid(k_mh_propose, 256, grid), 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx,
                                                                    prec == 1);
-    if (prec == 1) k_mh_jump_tip<1><<<rd_grid(k_mh_jump_tip<1>, 64, grid), 64, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale, queue + 2);
+    if (prec == 1) k_mh_jump_tip<1><<<rd_grid(k_mh_jump_tip<1>, RD_ITILE / RD_TIP_CPT, grid), RD_ITILE / RD_TIP_CPT, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale, queue + 2);
     else k_mh_jump_tip<0><<<rd_grid(k_mh_jump_tip<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, step_ptr, it_idx, partial, tickets, kscale, queue + 2);
   }
   return cudaGetLastError();

@@ -251,6 +251,36 @@ def test_emission_fp32c_statistics(rg, orc):
     eng.close()
 
 
+def test_tip_emission_fp32c_statistics(rg, orc):
+    """Tip emission in the FP32 compensated form (packed FP32x2 field tiles of
+    the tip MH jump) against the FP64 oracle: the same supply integral and
+    chain count, and emitted counts that differ only where an accept or
+    escape decision sits within the FP32 field error of its threshold."""
+    tip = (900 * NM, 100 * NM, 100 * NM)
+    rng = np.random.default_rng(17)
+    n = 3000
+    pos = np.column_stack([rng.uniform(-300 * NM, 300 * NM, n), rng.uniform(-300 * NM, 300 * NM, n),
+                           rng.uniform(110 * NM, 990 * NM, n)])
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=2, particle_capacity=16384, chain_capacity=16384,
+                    quad_capacity=20000)
+    d = eng.add_diode(geometry=rg.GEOM_TIP, V_s=800.0, time_step=0.25e-15, capacity=8192, tip_dim=tip,
+                      tip_work_function=3.0, emission=True, mh_jumps=40, max_chains=2000, seed=5)
+    d.add_particles(pos, step=0)
+    o = orc.OracleDiode(orc.TIP, cap=8192, V_s=800.0, d=1000 * NM)
+    o.set_tip(*tip, 3.0)
+    o.set_emission(True, seed=5, mh_jumps=40, max_chains=2000)
+    for p in pos:
+        o.add(p, step=0)
+    eng.do_emission(1)
+    o.emission(1)
+    c = d.counters()
+    assert c["N_sup"] == pytest.approx(o.s.N_sup, rel=1e-5)
+    assert c["chains"] == o.s.last_chains
+    assert o.s.emitted_step > 100   # 280 of 744 chains with these numbers
+    assert abs(c["emitted_step"] - o.s.emitted_step) <= max(2, 0.05 * o.s.emitted_step)
+    eng.close()
+
+
 def test_tip_emission_fp64(rg, orc):
     tip = (900 * NM, 100 * NM, 100 * NM)
     eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=2, particle_capacity=8192, chain_capacity=8192,

@@ -41,8 +41,8 @@ def test_autotune_keeps_state_and_matches_chosen_chunking(rg):
     e1.run(1, 3)
     before = _state(d1)
     t = e1.autotune()
-    assert t["candidates"] == 9
-    assert t["chunk_min"] in (512, 1024, 2048) and t["chunk_count_max"] in (8, 16, 32)
+    assert t["candidates"] == 15
+    assert t["chunk_min"] in (128, 256, 512, 1024, 2048) and t["chunk_count_max"] in (8, 16, 32)
     assert 0 < t["ms_chosen"] <= t["ms_default"]
     assert e1.get_chunking() == (t["chunk_min"], t["chunk_count_max"])
     _same(before, _state(d1))                           # nothing moved
