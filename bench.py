@@ -371,17 +371,19 @@ def run_ours(args, rank, world):
     e2e = e2e_all / e2e_wall if e2e_wall > 0 else 0.0
     if rank != 0:
         return
-    # dominant kernel roofline (FP32 pipe; 20 flops per Coulomb-like term)
-    launches = max(prof["mh_jump_launches"], 1)
-    avg_ms = prof["mh_jumps_ms"] / launches
-    flops_per_launch = 20.0 * prof["mh_pair_evals"] / launches
-    achieved = flops_per_launch / (avg_ms / 1e3) / 1e12 if avg_ms > 0 else 0.0
+    # dominant kernel roofline (FP32 pipe; 20 flops per Coulomb-like term).  The unit is one
+    # MH jump: the two concurrent launches of k_mh_jump_planar<1> (one per half of the plan,
+    # on two streams), timed together by CUDA events that bracket the fork and the join.
+    jumps = max(prof["mh_jump_launches"], 1)
+    avg_ms = prof["mh_jumps_ms"] / jumps
+    flops_per_jump = 20.0 * prof["mh_pair_evals"] / jumps
+    achieved = flops_per_jump / (avg_ms / 1e3) / 1e12 if avg_ms > 0 else 0.0
     peak = measure_fp32_peak()
     peak_src = "measured: cuBLAS SGEMM 8192^3, TF32 off"
     if peak is None:
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
         peak_src = "nominal: 152 SMs x 128 lanes x 2 x 2.07 GHz"
-    traffic = profile_figure("k_mh_jump_planar_serve128.md", "dram_bytes_per_launch")
+    traffic = profile_figure("k_mh_jump_planar_serve128.md", "dram_bytes_per_jump")
     plain_v, plain_caps = plain_fp64_sample(rg, resident, budget_s=args.plain_budget)
     cpu_v, cpu_desc, cores, cpu_t = cpu_sample(SEED, rank=rank)
     line = {
@@ -421,8 +423,11 @@ def run_ours(args, rank, world):
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_source": peak_src,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch "
-                                       "on the burst case (the same 128 resident requests)",
+                     "unit_of_work": "one MH jump of every chain: the two concurrent launches "
+                                     "(halves of the plan) of k_mh_jump_planar<1>",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the two "
+                                       "launches of a jump on the burst case (the same 128 resident "
+                                       "requests)",
                      "flops_convention": "20 flops per Coulomb-like term (Nyland et al.); "
                                          "1 term per (chain, particle) at the cathode"},
         "phase_ms": {k: prof[k] for k in ("supply_ms", "mh_init_ms", "mh_jumps_ms", "emit_ms",

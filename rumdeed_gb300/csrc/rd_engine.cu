@@ -62,7 +62,8 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
                               const int* ch_off, const double* wtab, const int* step_ptr,
-                              int it_idx, double* partial, int* tickets, double kscale, int* queue);
+                              int it_idx, double* partial, int* tickets, double kscale, int* queue,
+                              int part = 0);
 cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                            const Pool& pool, const ChainState& cs, const int* ch_off,
                            const double* work, const int* step_ptr, const EventLog& ev);
@@ -202,6 +203,8 @@ struct rd_engine {
   rd_engine_config cfg{};
   int sms = 0, grid = 0;
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;                                // second half of the planar MH jumps
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;          // st -> st2 and back
   RdConst k{};
   double kscale = 0.0;
   int max_items = 0;
@@ -221,7 +224,9 @@ struct rd_engine {
   PlanHeader* ph[PM_COUNT] = {};
   double* partial = nullptr;
   int* tickets = nullptr;
-  int* item_queue = nullptr;   // dynamic item counters (queue_next / queue_leave)
+  int* item_queue = nullptr;   // dynamic item counters (queue_next / queue_leave): [0..1] planar
+                               // MH (part 0 / 1), [2..3] tip MH, [4..5] force, [6..7] supply,
+                               // [8..9] planar MH part 2
   EventLog evlog{nullptr, nullptr, 0};   // emission / absorption records (rd_events_take)
   int* kept = nullptr;
   double* ramo = nullptr;
@@ -319,6 +324,40 @@ static Sig signature(const rd_engine* e) {
   return s;
 }
 
+// Jumps 1..jumps of the batched MH chains.  The planar jumps run as two
+// launches per jump, one per half of the plan (part_range), on two streams:
+// the halves are independent (each diode's chains and counters sit in one),
+// so the second stream's launch fills the SMs that the first one's last items
+// leave idle, and vice versa.  Results do not depend on it.
+static int launch_mh_jumps(rd_engine* e, const Sig& s) {
+  const int prec = e->cfg.precision;
+  const bool split = s.emit_planar;
+  if (split) {
+    CK(cudaEventRecord(e->ev_fork, e->st));
+    CK(cudaStreamWaitEvent(e->st2, e->ev_fork, 0));
+  }
+  for (int it = 1; it <= s.jumps; ++it) {
+    if (s.emit_planar) {
+      CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
+                           e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, e->item_queue, 1));
+      CK(rd_launch_mh_jump(prec, 1, e->grid, e->st2, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
+                           e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, e->item_queue + 8,
+                           2));
+      e->kernels_in_step += 2;
+    }
+    if (s.emit_tip) {   // tip propose + jump
+      CK(rd_launch_mh_jump(prec, 2, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
+                           e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, e->item_queue));
+      e->kernels_in_step += 2;
+    }
+  }
+  if (split) {
+    CK(cudaEventRecord(e->ev_join, e->st2));
+    CK(cudaStreamWaitEvent(e->st, e->ev_join, 0));
+  }
+  return RD_OK;
+}
+
 static int launch_emission(rd_engine* e) {
   Sig s = signature(e);
   if (!s.emit_planar && !s.emit_tip) return RD_OK;
@@ -350,12 +389,8 @@ static int launch_emission(rd_engine* e) {
   CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                        e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
   e->kernels_in_step++;
-  for (int it = 1; it <= s.jumps; ++it) {
-    CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH],
-                         e->ph[PM_MH], e->cs, e->d_choff, e->wtab, e->d_step, it, e->partial,
-                         e->tickets, e->kscale, e->item_queue));
-    e->kernels_in_step += ((gmask & 1) ? 1 : 0) + ((gmask & 2) ? 2 : 0);   // planar jump, tip propose + jump
-  }
+  int rc = launch_mh_jumps(e, s);
+  if (rc) return rc;
   CK(rd_launch_emit(ns, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step, e->evlog));
   e->kernels_in_step++;
   if (s.emit_serial) {   // serial MH diodes: chains one after another, one block per diode
@@ -536,7 +571,10 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   e->grid = cfg->grid_blocks > 0 ? cfg->grid_blocks : 0;   // 0: occupancy-based per kernel
   e->clen_min = cfg->chunk_min > 0 ? cfg->chunk_min : RD_CLEN_MIN;
   e->nch_max = cfg->chunk_count_max > 0 ? cfg->chunk_count_max : RD_NCH_MAX;
-  if ((ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess)
+  if ((ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess ||
+      (ce = cudaStreamCreateWithFlags(&e->st2, cudaStreamNonBlocking)) != cudaSuccess ||
+      (ce = cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
+      (ce = cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming)) != cudaSuccess)
     return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
   cudaEventCreate(&e->ev0);
   cudaEventCreate(&e->ev1);
@@ -567,7 +605,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
       e->dalloc(&e->d_npts, S) || e->dalloc(&e->d_zero_off, S) ||
       e->dalloc(&e->partial, (size_t)e->max_items * 3 * RD_ITILE) ||
       e->dalloc(&e->tickets, e->max_items) || e->dalloc(&e->kept, e->max_items) ||
-      e->dalloc(&e->item_queue, 8) ||
+      e->dalloc(&e->item_queue, 16) ||
       (cfg->event_capacity > 0 && (e->dalloc(&e->evlog.buf, (size_t)cfg->event_capacity) ||
                                    e->dalloc(&e->evlog.count, 1))) ||
       e->dalloc(&e->ramo, cap) || e->dalloc(&e->life, (size_t)S * RD_MAX_LIFE) ||
@@ -584,7 +622,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   cudaMemsetAsync(e->dP, 0, sizeof(DiodeParams) * S, e->st);
   cudaMemsetAsync(e->dD, 0, sizeof(DiodeDyn) * S, e->st);
   cudaMemsetAsync(e->tickets, 0, sizeof(int) * e->max_items, e->st);
-  cudaMemsetAsync(e->item_queue, 0, sizeof(int) * 8, e->st);
+  cudaMemsetAsync(e->item_queue, 0, sizeof(int) * 16, e->st);
   if (e->evlog.count) cudaMemsetAsync(e->evlog.count, 0, sizeof(int), e->st);
   e->evlog.cap = cfg->event_capacity > 0 ? cfg->event_capacity : 0;
   cudaMemsetAsync(e->life, 0, sizeof(int) * (size_t)S * RD_MAX_LIFE, e->st);
@@ -614,6 +652,9 @@ int rd_engine_destroy(rd_engine* e) {
   if (e->fpx) { cudaFree(e->fpx); cudaFree(e->fpy); cudaFree(e->fpz); cudaFree(e->ffx); cudaFree(e->ffy); cudaFree(e->ffz); }
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+  if (e->ev_join) cudaEventDestroy(e->ev_join);
+  if (e->st2) cudaStreamDestroy(e->st2);
   if (e->st) cudaStreamDestroy(e->st);
   delete e;
   return RD_OK;
@@ -1304,10 +1345,8 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
     CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                          e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
     CK(cudaEventRecord(ev[2], e->st));
-    for (int it = 1; it <= s.jumps; ++it)
-      CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                           e->cs, e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale,
-                           e->item_queue));
+    int rcj = launch_mh_jumps(e, s);
+    if (rcj) return rcj;
     out->mh_jump_launches = s.jumps;
     CK(cudaEventRecord(ev[3], e->st));
     CK(rd_launch_emit(S, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step, e->evlog));

@@ -461,7 +461,7 @@ k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __res
   constexpr int CPT = PREC == 1 ? 2 : 1;
   const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
-  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
+  for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int m = plan[it.d].n_i, qo = p.q_off;
@@ -490,7 +490,7 @@ k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __res
       if (i < m) qF[qo + i] = z0_finish<PREC>(p, s[q], kscale);
     }
   }
-  queue_leave(queue, total);
+  queue_leave(queue, 0, total);
 }
 
 // ---- supply integrals ------------------------------------------------------------------
@@ -847,7 +847,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
                  const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph, ChainState cs,
                  const int* __restrict__ ch_off, const double* __restrict__ wtab,
                  const int* __restrict__ step_ptr, int it_idx, double* __restrict__ partial,
-                 int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
+                 int* __restrict__ tickets, double kscale, int* __restrict__ queue, int part) {
   __shared__ int red_i[2 * RD_ITILE];
   __shared__ int s_item;
   constexpr int CPT = PREC == 1 ? 4 : 1;
@@ -855,7 +855,9 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   const bool init = it_idx == 0;
   const bool dry = it_idx < 0;   // timing pass: field at the current points, nothing written
-  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
+  int lo, hi;   // this launch's part of the plan (part_range)
+  part_range(plan, nd, total, part, &lo, &hi);
+  for (int g = queue_first(lo, hi); g < hi; g = queue_next(queue, &s_item, lo, hi)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     if (p.geometry != RD_G_PLANAR || it_idx > p.mh_jumps) continue;
@@ -985,7 +987,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
     }
     mh_counts_and_update(p, y, plan[it.d].tiles, it_idx, ndim_first, a, r, red_i);
   }
-  queue_leave(queue, total);
+  queue_leave(queue, lo, hi);
 }
 
 // Field sums of one j-tile at CPT tip proposals (upper role: the point's own
@@ -1063,7 +1065,7 @@ k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool
   const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   const bool init = it_idx == 0;
-  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
+  for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     if (p.geometry != RD_G_TIP || it_idx > p.mh_jumps) continue;
@@ -1199,7 +1201,7 @@ k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool
     if (init) continue;
     mh_counts_and_update(p, y, plan[it.d].tiles, it_idx, ndim_first, a, r, red_i);
   }
-  queue_leave(queue, total);
+  queue_leave(queue, 0, total);
 }
 
 // ---- tip MH proposals: one thread per chain ---------------------------------------------
@@ -1609,10 +1611,12 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
                               const int* ch_off, const double* wtab, const int* step_ptr,
-                              int it_idx, double* partial, int* tickets, double kscale, int* queue) {
+                              int it_idx, double* partial, int* tickets, double kscale, int* queue,
+                              int part) {
+  // part (planar jumps): 0 all items, 1 / 2 the two halves of the plan (part_range)
   if (geometry_mask & 1) {
-    if (prec == 1) k_mh_jump_planar<1><<<rd_grid(k_mh_jump_planar<1>, 32, grid), 32, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue);
-    else k_mh_jump_planar<0><<<rd_grid(k_mh_jump_planar<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue);
+    if (prec == 1) k_mh_jump_planar<1><<<rd_grid(k_mh_jump_planar<1>, 32, grid), 32, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part);
+    else k_mh_jump_planar<0><<<rd_grid(k_mh_jump_planar<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part);
   }
   if (geometry_mask & 2) {
     k_mh_propose<<<rd_grid(k_mh_propose, 256, grid), 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx,

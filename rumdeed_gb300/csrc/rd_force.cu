@@ -88,7 +88,7 @@ k_force_planar_f32_nic0(const DiodeParams* __restrict__ P, Pool pool,
   __shared__ float4 sh[RD_TILE], sl[RD_TILE];
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x, nt = 64;
-  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
+  for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -146,7 +146,7 @@ k_force_planar_f32_nic0(const DiodeParams* __restrict__ P, Pool pool,
       pool.az[gi] = pre * f[q][2] + qi * p.E_z * im;
     }
   }
-  queue_leave(queue, total);
+  queue_leave(queue, 0, total);
 }
 
 template <bool NIC0>
@@ -158,7 +158,7 @@ k_force_planar_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict
   __shared__ float4 sh[RD_TILE], sl[RD_TILE];
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x;
-  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
+  for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -208,7 +208,7 @@ k_force_planar_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict
       pool.az[gi] = pre * fz + qi * p.E_z * im;
     }
   }
-  queue_leave(queue, total);
+  queue_leave(queue, 0, total);
 }
 
 __global__ void __launch_bounds__(RD_ITILE)
@@ -220,7 +220,7 @@ k_force_planar_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x;
   const double L2 = c_k.L2, dfc = c_k.div_fac_c;
-  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
+  for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -261,7 +261,7 @@ k_force_planar_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict
       pool.az[gi] = (az + q1 * p.E_z) * im;
     }
   }
-  queue_leave(queue, total);
+  queue_leave(queue, 0, total);
 }
 
 __global__ void __launch_bounds__(RD_ITILE)
@@ -273,7 +273,7 @@ k_force_tip_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x;
   const float K = (float)c_k.tip_K;
-  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
+  for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -326,7 +326,7 @@ k_force_tip_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
       pool.az[gi] = pre * fz + qi * ez * im;
     }
   }
-  queue_leave(queue, total);
+  queue_leave(queue, 0, total);
 }
 
 __global__ void __launch_bounds__(RD_ITILE)
@@ -338,7 +338,7 @@ k_force_tip_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x;
   const double L2 = c_k.L2, dfc = c_k.div_fac_c, K = c_k.tip_K;
-  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
+  for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -381,7 +381,7 @@ k_force_tip_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
       pool.az[gi] = (az + q1 * ez) * im;
     }
   }
-  queue_leave(queue, total);
+  queue_leave(queue, 0, total);
 }
 
 // ---- two-time-step diodes (FP64, both geometries) ----------------------------------
@@ -406,7 +406,7 @@ k_force_tts_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x;
   const double L2 = c_k.L2, dfc = c_k.div_fac_c, K = c_k.tip_K;
-  for (int g = queue_first(total); g < total; g = queue_next(queue, &s_item, total)) {
+  for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
     const int off = p.off, n = plan[it.d].n_i;
@@ -470,7 +470,7 @@ k_force_tts_f64(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
       }
     }
   }
-  queue_leave(queue, total);
+  queue_leave(queue, 0, total);
 }
 
 }  // namespace

@@ -98,29 +98,29 @@ __device__ __forceinline__ bool tile_ticket(int* tickets, const ItemRef& it) {
   return s_last != 0;
 }
 
-// Dynamic item scheduling.  The P = min(grid, total) first blocks take items
-// 0..P-1 (the others exit at once); after that a block draws its next item
-// from a counter (P + q[0]++) instead of walking a fixed stride, so blocks
-// that drew cheap items (small diodes) take more and the launch ends with the
-// work, not with the unluckiest block.  The last of the P blocks to leave
-// (q[1]) resets both counters for the next launch on the stream; its fence
-// orders each block's last draw before its leave.  No block waits on
-// another; results do not depend on the order (partials are added in chunk
-// order by tile_ticket).
-__device__ __forceinline__ int queue_first(int total) {
-  return (int)blockIdx.x < total ? (int)blockIdx.x : total;
+// Dynamic item scheduling over the item range [lo, hi) of a launch.  The
+// P = min(grid, hi - lo) first blocks take items lo..lo+P-1 (the others exit
+// at once); after that a block draws its next item from a counter
+// (lo + P + q[0]++) instead of walking a fixed stride, so blocks that drew
+// cheap items (small diodes) take more and the launch ends with the work, not
+// with the unluckiest block.  The last of the P blocks to leave (q[1]) resets
+// both counters for the next launch on the stream; its fence orders each
+// block's last draw before its leave.  No block waits on another; results do
+// not depend on the order (partials are added in chunk order by tile_ticket).
+__device__ __forceinline__ int queue_first(int lo, int hi) {
+  return lo + (int)blockIdx.x < hi ? lo + (int)blockIdx.x : hi;
 }
 
-__device__ __forceinline__ int queue_next(int* q, int* s_slot, int total) {
-  const int P = min((int)gridDim.x, total);
+__device__ __forceinline__ int queue_next(int* q, int* s_slot, int lo, int hi) {
+  const int P = min((int)gridDim.x, hi - lo);
   __syncthreads();
-  if (threadIdx.x == 0) *s_slot = P + atomicAdd(&q[0], 1);
+  if (threadIdx.x == 0) *s_slot = lo + P + atomicAdd(&q[0], 1);
   __syncthreads();
   return *s_slot;
 }
 
-__device__ __forceinline__ void queue_leave(int* q, int total) {
-  const int P = min((int)gridDim.x, total);
+__device__ __forceinline__ void queue_leave(int* q, int lo, int hi) {
+  const int P = min((int)gridDim.x, hi - lo);
   if ((int)blockIdx.x >= P) return;   // took no item
   if (threadIdx.x == 0) {
     __threadfence();
@@ -130,6 +130,27 @@ __device__ __forceinline__ void queue_leave(int* q, int total) {
       __threadfence();
     }
   }
+}
+
+// Item range of one part of a plan: part 0 is the whole plan, parts 1 and 2
+// its two halves split at the diode boundary nearest to half the items, so
+// that two launches on two streams (each with its own item counters) share
+// the GPU and one fills the SMs the other's last items leave idle.  Every
+// diode's items stay in one part; both parts compute the same split.
+__device__ __forceinline__ void part_range(const PlanEntry* plan, int nd, int total, int part, int* lo,
+                                           int* hi) {
+  if (part == 0 || nd == 0) { *lo = 0; *hi = part == 2 ? 0 : total; return; }
+  const int half = total / 2;
+  int a = 0, b = nd - 1;   // last entry with item_off <= half
+  while (a < b) {
+    const int mid = (a + b + 1) >> 1;
+    if (plan[mid].item_off <= half) a = mid; else b = mid - 1;
+  }
+  const int below = min(plan[a].item_off, total);
+  const int above = a + 1 < nd ? min(plan[a + 1].item_off, total) : total;
+  const int split = (half - below <= above - half) ? below : above;
+  *lo = part == 1 ? 0 : split;
+  *hi = part == 1 ? split : total;
 }
 
 // Points of a field evaluation: per-diode lists at [off[d], off[d] + n_d).
