@@ -203,8 +203,9 @@ struct rd_engine {
   rd_engine_config cfg{};
   int sms = 0, grid = 0;
   cudaStream_t st = nullptr;
-  cudaStream_t st2 = nullptr;                                // second half of the planar MH jumps
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;          // st -> st2 and back
+  cudaStream_t stp[RD_MH_PARTS] = {};    // planar MH jump parts 2.. (part 1 runs on st)
+  cudaEvent_t ev_fork = nullptr;         // st -> the part streams
+  cudaEvent_t ev_join[RD_MH_PARTS] = {}; // each part stream -> st
   RdConst k{};
   double kscale = 0.0;
   int max_items = 0;
@@ -226,7 +227,7 @@ struct rd_engine {
   int* tickets = nullptr;
   int* item_queue = nullptr;   // dynamic item counters (queue_next / queue_leave): [0..1] planar
                                // MH (part 0 / 1), [2..3] tip MH, [4..5] force, [6..7] supply,
-                               // [8..9] planar MH part 2
+                               // [6 + 2p .. 7 + 2p] planar MH part p >= 2
   EventLog evlog{nullptr, nullptr, 0};   // emission / absorption records (rd_events_take)
   int* kept = nullptr;
   double* ramo = nullptr;
@@ -324,26 +325,28 @@ static Sig signature(const rd_engine* e) {
   return s;
 }
 
-// Jumps 1..jumps of the batched MH chains.  The planar jumps run as two
-// launches per jump, one per half of the plan (part_range), on two streams:
-// the halves are independent (each diode's chains and counters sit in one),
-// so the second stream's launch fills the SMs that the first one's last items
-// leave idle, and vice versa.  Results do not depend on it.
+// Jumps 1..jumps of the batched MH chains.  The planar jumps run as
+// RD_MH_PARTS launches per jump, one per part of the plan (part_range), each
+// on its own stream: the parts are independent (each diode's chains and
+// counters sit in one), so while one stream's launch runs its last items the
+// others' launches fill the idle SMs.  Results do not depend on it.
 static int launch_mh_jumps(rd_engine* e, const Sig& s) {
   const int prec = e->cfg.precision;
-  const bool split = s.emit_planar;
-  if (split) {
+  const int parts = s.emit_planar ? RD_MH_PARTS : 1;
+  if (parts > 1) {
     CK(cudaEventRecord(e->ev_fork, e->st));
-    CK(cudaStreamWaitEvent(e->st2, e->ev_fork, 0));
+    for (int q = 1; q < parts; ++q) CK(cudaStreamWaitEvent(e->stp[q], e->ev_fork, 0));
   }
   for (int it = 1; it <= s.jumps; ++it) {
     if (s.emit_planar) {
-      CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
-                           e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, e->item_queue, 1));
-      CK(rd_launch_mh_jump(prec, 1, e->grid, e->st2, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
-                           e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, e->item_queue + 8,
-                           2));
-      e->kernels_in_step += 2;
+      for (int q = 0; q < parts; ++q) {
+        cudaStream_t sq = q == 0 ? e->st : e->stp[q];
+        int* queue = q == 0 ? e->item_queue : e->item_queue + 6 + 2 * (q + 1);
+        CK(rd_launch_mh_jump(prec, 1, e->grid, sq, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
+                             e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, queue,
+                             q + 1));
+      }
+      e->kernels_in_step += parts;
     }
     if (s.emit_tip) {   // tip propose + jump
       CK(rd_launch_mh_jump(prec, 2, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
@@ -351,9 +354,9 @@ static int launch_mh_jumps(rd_engine* e, const Sig& s) {
       e->kernels_in_step += 2;
     }
   }
-  if (split) {
-    CK(cudaEventRecord(e->ev_join, e->st2));
-    CK(cudaStreamWaitEvent(e->st, e->ev_join, 0));
+  for (int q = 1; q < parts; ++q) {
+    CK(cudaEventRecord(e->ev_join[q], e->stp[q]));
+    CK(cudaStreamWaitEvent(e->st, e->ev_join[q], 0));
   }
   return RD_OK;
 }
@@ -572,10 +575,12 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   e->clen_min = cfg->chunk_min > 0 ? cfg->chunk_min : RD_CLEN_MIN;
   e->nch_max = cfg->chunk_count_max > 0 ? cfg->chunk_count_max : RD_NCH_MAX;
   if ((ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess ||
-      (ce = cudaStreamCreateWithFlags(&e->st2, cudaStreamNonBlocking)) != cudaSuccess ||
-      (ce = cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
-      (ce = cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming)) != cudaSuccess)
+      (ce = cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming)) != cudaSuccess)
     return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
+  for (int q = 1; q < RD_MH_PARTS; ++q)
+    if ((ce = cudaStreamCreateWithFlags(&e->stp[q], cudaStreamNonBlocking)) != cudaSuccess ||
+        (ce = cudaEventCreateWithFlags(&e->ev_join[q], cudaEventDisableTiming)) != cudaSuccess)
+      return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
   cudaEventCreate(&e->ev0);
   cudaEventCreate(&e->ev1);
   e->k = make_constants();
@@ -605,7 +610,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
       e->dalloc(&e->d_npts, S) || e->dalloc(&e->d_zero_off, S) ||
       e->dalloc(&e->partial, (size_t)e->max_items * 3 * RD_ITILE) ||
       e->dalloc(&e->tickets, e->max_items) || e->dalloc(&e->kept, e->max_items) ||
-      e->dalloc(&e->item_queue, 16) ||
+      e->dalloc(&e->item_queue, 8 + 2 * RD_MH_PARTS) ||
       (cfg->event_capacity > 0 && (e->dalloc(&e->evlog.buf, (size_t)cfg->event_capacity) ||
                                    e->dalloc(&e->evlog.count, 1))) ||
       e->dalloc(&e->ramo, cap) || e->dalloc(&e->life, (size_t)S * RD_MAX_LIFE) ||
@@ -622,7 +627,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   cudaMemsetAsync(e->dP, 0, sizeof(DiodeParams) * S, e->st);
   cudaMemsetAsync(e->dD, 0, sizeof(DiodeDyn) * S, e->st);
   cudaMemsetAsync(e->tickets, 0, sizeof(int) * e->max_items, e->st);
-  cudaMemsetAsync(e->item_queue, 0, sizeof(int) * 16, e->st);
+  cudaMemsetAsync(e->item_queue, 0, sizeof(int) * (8 + 2 * RD_MH_PARTS), e->st);
   if (e->evlog.count) cudaMemsetAsync(e->evlog.count, 0, sizeof(int), e->st);
   e->evlog.cap = cfg->event_capacity > 0 ? cfg->event_capacity : 0;
   cudaMemsetAsync(e->life, 0, sizeof(int) * (size_t)S * RD_MAX_LIFE, e->st);
@@ -653,8 +658,10 @@ int rd_engine_destroy(rd_engine* e) {
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
   if (e->ev_fork) cudaEventDestroy(e->ev_fork);
-  if (e->ev_join) cudaEventDestroy(e->ev_join);
-  if (e->st2) cudaStreamDestroy(e->st2);
+  for (int q = 1; q < RD_MH_PARTS; ++q) {
+    if (e->ev_join[q]) cudaEventDestroy(e->ev_join[q]);
+    if (e->stp[q]) cudaStreamDestroy(e->stp[q]);
+  }
   if (e->st) cudaStreamDestroy(e->st);
   delete e;
   return RD_OK;

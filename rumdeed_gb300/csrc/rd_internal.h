@@ -22,6 +22,7 @@
 #define RD_TILE 128           // particles per shared-memory j-tile
 #define RD_ITILE 128          // i-particles (or points) per work item
 #define RD_TIP_CPT 2          // tip MH chains per thread (FP32 form; even)
+#define RD_MH_PARTS 2         // planar MH jump launches per jump, one stream each (1..4)
 // j-chunking of pair sums: at least RD_CLEN_MIN particles per chunk, at most
 // RD_NCH_MAX chunks per i-tile
 #define RD_CLEN_MIN 1024

@@ -132,25 +132,30 @@ __device__ __forceinline__ void queue_leave(int* q, int lo, int hi) {
   }
 }
 
-// Item range of one part of a plan: part 0 is the whole plan, parts 1 and 2
-// its two halves split at the diode boundary nearest to half the items, so
-// that two launches on two streams (each with its own item counters) share
-// the GPU and one fills the SMs the other's last items leave idle.  Every
-// diode's items stay in one part; both parts compute the same split.
-__device__ __forceinline__ void part_range(const PlanEntry* plan, int nd, int total, int part, int* lo,
-                                           int* hi) {
-  if (part == 0 || nd == 0) { *lo = 0; *hi = part == 2 ? 0 : total; return; }
-  const int half = total / 2;
-  int a = 0, b = nd - 1;   // last entry with item_off <= half
+// Item range of one part of a plan: part 0 is the whole plan; parts
+// 1..nparts cut it at the diode boundaries nearest to k/nparts of the items,
+// so that nparts launches on as many streams (each with its own item
+// counters) share the GPU and fill the SMs that the others' last items leave
+// idle.  Every diode's items stay in one part; all parts compute the same cuts.
+__device__ __forceinline__ int part_cut(const PlanEntry* plan, int nd, int total, int k, int nparts) {
+  if (k <= 0) return 0;
+  if (k >= nparts) return total;
+  const int target = (int)(((long long)total * k) / nparts);
+  int a = 0, b = nd - 1;   // last entry with item_off <= target
   while (a < b) {
     const int mid = (a + b + 1) >> 1;
-    if (plan[mid].item_off <= half) a = mid; else b = mid - 1;
+    if (plan[mid].item_off <= target) a = mid; else b = mid - 1;
   }
   const int below = min(plan[a].item_off, total);
   const int above = a + 1 < nd ? min(plan[a + 1].item_off, total) : total;
-  const int split = (half - below <= above - half) ? below : above;
-  *lo = part == 1 ? 0 : split;
-  *hi = part == 1 ? split : total;
+  return (target - below <= above - target) ? below : above;
+}
+
+__device__ __forceinline__ void part_range(const PlanEntry* plan, int nd, int total, int part, int nparts,
+                                           int* lo, int* hi) {
+  if (part == 0 || nd == 0) { *lo = 0; *hi = part == 0 ? total : 0; return; }
+  *lo = part_cut(plan, nd, total, part - 1, nparts);
+  *hi = part_cut(plan, nd, total, part, nparts);
 }
 
 // Points of a field evaluation: per-diode lists at [off[d], off[d] + n_d).
