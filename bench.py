@@ -696,7 +696,8 @@ def main():
     ap.add_argument("--case", default="serve", choices=["serve", "micro", "burst", "mh-small", "plain", "tips"],
                     help="serve: the headline serving benchmark; the others are secondary workloads")
     ap.add_argument("--sizes", default="4096,65536,262144", help="micro: electron counts")
-    ap.add_argument("--nics", default="0,7", help="micro: N_ic_max values")
+    ap.add_argument("--nics", default="0,7,8", help="micro: N_ic_max values (K = 8 mirror terms read "
+                    "as N_ic_max = 7, the series through n = 7, or as N_ic_max = 8)")
     ap.add_argument("--tip-electrons", type=int, default=100000, help="tips: electrons per tip")
     ap.add_argument("--fp64-budget", type=float, default=2.0e11,
                     help="micro: largest N(N-1) x terms run in FP64 for the error check")
