@@ -516,7 +516,10 @@ def case_micro(args):
                                 chain_capacity=4096, quad_capacity=4096)
                 d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, capacity=N, image_charge=True, N_ic_max=nic)
                 d.add_particles(pos)
-                tune = eng.autotune()   # chunking for this system size (the project's tuner)
+                # chunking for this system size (the project's tuner); the FP64 form only where
+                # its 45 timing passes stay short
+                tune = eng.autotune() if (prec == rg.PREC_FP32C or pairs * terms < 2e9) else \
+                    dict(zip(("chunk_min", "chunk_count_max"), eng.get_chunking()))
                 acc = d.calculate_acceleration_particles()
                 reps = 1 if pairs * terms > 2e11 else (3 if pairs > 1e9 else 20)
                 ms = eng.time_accel(reps)
