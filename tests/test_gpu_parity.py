@@ -597,3 +597,37 @@ def test_two_time_step_interval_one_equals_standard(rg, orc):
     assert ca["ramo_current"] == cb["ramo_current"]
     assert ca["ramo_current_ion"] == cb["ramo_current_ion"] != 0.0
     eng.close()
+
+
+def test_two_time_step_full_steps_with_emission_fp64(rg, orc):
+    """Main-loop iterations (emission, Beeman, forces, removal and
+    compaction) of a two-time-step diode with ions among the electrons
+    (atom_time_interval = 2): the FP64 GPU form follows the oracle step for
+    step, including the electrons emitted into the mix."""
+    eng0, _, o = _emission_pair(rg, orc, rg.PREC_FP64, seed=31, n0=0)   # the oracle side only
+    eng0.close()
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=2, particle_capacity=8192, chain_capacity=4096)
+    dio = eng.add_diode(V_s=1.0e3, gap=500 * NM, capacity=4096, emitter_pos=(-50 * NM, -50 * NM),
+                        emitter_dim=(100 * NM, 100 * NM), work=[[2.0]], emission=True, mh_jumps=40,
+                        max_chains=300, quad_panels=8, quad_order=4, seed=31, atom_time_interval=2)
+    rng = np.random.default_rng(31)
+    n0 = 120
+    pos = np.column_stack([rng.uniform(-60 * NM, 60 * NM, n0), rng.uniform(-60 * NM, 60 * NM, n0),
+                           rng.uniform(2 * NM, 490 * NM, n0)])
+    sp = np.where(np.arange(n0) % 3 == 0, 2, 1)
+    dio.add_particles(pos, species=sp)
+    for p, s in zip(pos, sp):
+        o.add(p, species=int(s))
+    o.set_tts(2)
+    for step in range(1, 6):
+        eng.step(step)
+        o.step(step)
+        c = dio.counters()
+        assert dio.n == o.n, step
+        assert c["emitted_step"] == o.s.emitted_step, step
+        assert c["ramo_current_ion"] == pytest.approx(o.s.ramo_current_ion, rel=1e-9, abs=1e-30)
+    p = dio.particles()
+    assert np.max(np.abs(p["pos"] - o.arr("pos"))) < 1e-9 * NM
+    assert nrel(p["vel"] + 1e-3, o.arr("vel") + 1e-3) < 1e-8
+    assert c["emitted_total"] == o.s.emitted_total > 0
+    eng.close()
