@@ -12,12 +12,13 @@
 // edit descriptors, and the per-event binary files out/density_emit.bin,
 // out/density_emit_elec.bin (src/mod_pair.F90:89-123),
 // out/density_absorb_{top,bot}.bin (:241-257) and out/planes-<k>.bin
-// (Check_Planes, src/mod_verlet.F90:343-367) from the engine's event log, and
-// out/field.dt (src/mod_field_emission_v2.F90:389-390).
+// (Check_Planes, src/mod_verlet.F90:343-367) from the engine's event log,
+// out/field.dt (src/mod_field_emission_v2.F90:389-390) and out/volt.dt
+// (Set_Voltage, src/mod_verlet.F90:2050-2057).
 //
-// Supported decks: EMISSION_MODE = 10 (planar field emission, one
-// rectangular emitter, EMITTERS_TYPE 2) and EMISSION_MODE = 3 (hyperboloid
-// tip).  Extra, optional namelist /gb300/ in the same file: MAX_PARTICLES
+// Supported decks: EMISSION_MODE = 10 (planar field emission, one emitter,
+// EMITTERS_TYPE 1, 2 or 4) and EMISSION_MODE = 3 (hyperboloid tip);
+// ATOM_TIME_INTERVAL > 0 selects the two-time-step integrator.  Extra, optional namelist /gb300/ in the same file: MAX_PARTICLES
 // (default 20000), SEED, PRECISION (0 = FP64, 1 = FP32 compensated), MH_JUMPS,
 // TIP_WORK_FUNCTION (eV, default 4.7 as the reference hard-codes), MH_SERIAL.
 // The MH sampler is serial with MH_SERIAL = 1 or /input/'s MH_BATCH = .False.,
@@ -320,6 +321,7 @@ int main(int argc, char** argv) {
   FILE* b_abs_top = std::fopen("out/density_absorb_top.bin", "wb");
   FILE* b_abs_bot = std::fopen("out/density_absorb_bot.bin", "wb");
   FILE* f_field = std::fopen("out/field.dt", "w");
+  FILE* f_volt = std::fopen("out/volt.dt", "w");
   FILE* b_planes[10] = {};
   for (int k = 0; k < dc.planes_N; ++k)
     if (dc.planes_z[k] > 0.0) {   // out/planes-<k>.bin, src/main.F90:727-738
@@ -329,7 +331,7 @@ int main(int argc, char** argv) {
       if (!b_planes[k]) { std::fprintf(stderr, "rd_main: cannot write %s\n", name); return 2; }
     }
   if (!f_emit || !f_abs || !f_top || !f_bot || !f_ramo || !b_emit || !b_emit_elec || !b_abs_top || !b_abs_bot ||
-      !f_field) {
+      !f_field || !f_volt) {
     std::fprintf(stderr, "rd_main: cannot write under out/\n");
     return 2;
   }
@@ -341,6 +343,13 @@ int main(int argc, char** argv) {
   int progress = 1;
   for (int step = 1; step <= steps; ++step) {
     check(rd_step(e, step), "rd_step");
+    // volt.dt (Set_Voltage, src/mod_verlet.F90:2050-2057): "(ES12.4, tr2, i8, tr2, ES18.8)" with
+    // four items, so format reversion puts V_rf (0) on a record of its own
+    {
+      const double t = dt * step / time_scale;
+      std::fprintf(f_volt, "%s  %s  %s\n%s\n", fmt_ES(t, 12, 4).c_str(), fmt_I(step, 8).c_str(),
+                   fmt_ES(V_s, 18, 8).c_str(), fmt_ES(0.0, 12, 4).c_str());
+    }
     // event records of the step, in the reference's binary layouts:
     //   density_emit.bin       pos/length_scale (3 f64), emitter, section, id, species (4 i32)
     //   density_emit_elec.bin  pos/length_scale (3 f64), emitter, id (2 i32)
@@ -413,11 +422,15 @@ int main(int argc, char** argv) {
     if (n > 0) for (double& a : av) a /= n;
     const double speed = std::sqrt(av[0] * av[0] + av[1] * av[1] + av[2] * av[2]);
     const double mob = E_z != 0.0 ? speed / (-E_z) : 0.0;
-    std::string r = fmt_ES(cur_time, 12, 4) + "  " + fmt_I(step, 8) + "  " + fmt_ES(c.ramo_current, 12, 4) +
+    // (Write_Ramo_Current, src/mod_pair.F90:812-835: total = sum over species, then one column
+    // per species; this driver adds electrons only, so the ion and atom columns stay 0 unless
+    // the library holds ions)
+    const double ramo_total = c.ramo_current + c.ramo_current_ion;
+    std::string r = fmt_ES(cur_time, 12, 4) + "  " + fmt_I(step, 8) + "  " + fmt_ES(ramo_total, 12, 4) +
                     "  " + fmt_ES(V_s, 12, 4) + "  " + fmt_I(n, 6) + "  " + fmt_I(n, 6) + "  " + fmt_I(0, 6) +
                     "  " + fmt_ES(mob, 12, 4) + "  " + fmt_ES(speed, 12, 4) + "  " + fmt_ES(speed, 12, 4) +
                     "  " + fmt_ES(0.0, 12, 4) + "  " + fmt_ES(c.ramo_current, 12, 4) + "  " +
-                    fmt_ES(0.0, 12, 4) + "  " + fmt_ES(0.0, 12, 4);
+                    fmt_ES(c.ramo_current_ion, 12, 4) + "  " + fmt_ES(0.0, 12, 4);
     std::fprintf(f_ramo, "%s\n", r.c_str());
     if (step * 10 >= progress * steps) {
       std::printf("RUMDEED: %3d %%  electrons %d, emitted %lld, absorbed %lld\n", progress * 10, c.n,
@@ -426,7 +439,7 @@ int main(int argc, char** argv) {
       ++progress;
     }
   }
-  for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo, b_emit, b_emit_elec, b_abs_top, b_abs_bot, f_field})
+  for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo, b_emit, b_emit_elec, b_abs_top, b_abs_bot, f_field, f_volt})
     std::fclose(f);
   for (FILE* f : b_planes) if (f) std::fclose(f);
   rd_engine_destroy(e);

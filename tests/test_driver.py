@@ -147,6 +147,12 @@ def test_driver_run_matches_python_binding(driver, tmp_path, rg):
     p1 = np.fromfile(out / "planes-1.bin", dtype=rec_top)
     p2 = np.fromfile(out / "planes-2.bin", dtype=rec_top)
     assert len(p1) >= len(p2) and np.all(p1["vel"][:, 2] > 0) if len(p1) else True
+    # volt.dt: "(ES12.4, tr2, i8, tr2, ES18.8)" with 4 items: time, step, V_d, then V_rf alone on
+    # the next record by format reversion (Set_Voltage, src/mod_verlet.F90:2050-2057)
+    vl = (out / "volt.dt").read_text().splitlines()
+    assert len(vl) == 2 * 12
+    assert vl[0] == "  2.5000E-04         1      2.00000000E+03" and vl[1] == "  0.0000E+00"
+    assert vl[22].split()[1] == "12"
 
 
 @pytest.mark.gpu
