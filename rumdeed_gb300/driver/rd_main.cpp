@@ -322,6 +322,27 @@ int main(int argc, char** argv) {
   FILE* b_abs_bot = std::fopen("out/density_absorb_bot.bin", "wb");
   FILE* f_field = std::fopen("out/field.dt", "w");
   FILE* f_volt = std::fopen("out/volt.dt", "w");
+  // optional files of the namelist's WRITE_POSITION_FILE / WRITE_RAMO_SEC (default off)
+  const bool write_pos = in.count("WRITE_POSITION_FILE") && to_logical(in.at("WRITE_POSITION_FILE")[0]);
+  const bool write_ramo_sec = in.count("WRITE_RAMO_SEC") && to_logical(in.at("WRITE_RAMO_SEC")[0]);
+  if (write_ramo_sec && mode != 10) {
+    std::fprintf(stderr, "rd_main: WRITE_RAMO_SEC is supported for planar decks only\n");
+    return 2;
+  }
+  FILE* b_pos = write_pos ? std::fopen("out/position.bin", "wb") : nullptr;
+  FILE* b_ramo_sec = write_ramo_sec ? std::fopen("out/ramo_current.bin", "wb") : nullptr;
+  if ((write_pos && !b_pos) || (write_ramo_sec && !b_ramo_sec)) {
+    std::fprintf(stderr, "rd_main: cannot write under out/\n");
+    return 2;
+  }
+  const int max_sections = 96 * 96;   // MAX_SECTIONS x MAX_EMITTERS (= 1), src/mod_global.F90:99-100
+  std::vector<double> ramo_sec(write_ramo_sec ? max_sections : 0);
+  std::vector<double> pbuf, qbuf;
+  std::vector<int> idbuf, secbuf;
+  if (b_pos) {   // Write_Position, src/mod_pair.F90:841-867: header steps, N_steps (= 1)
+    const int hdr[2] = {steps, 1};
+    std::fwrite(hdr, sizeof(int), 2, b_pos);
+  }
   FILE* b_planes[10] = {};
   for (int k = 0; k < dc.planes_N; ++k)
     if (dc.planes_z[k] > 0.0) {   // out/planes-<k>.bin, src/main.F90:727-738
@@ -342,7 +363,31 @@ int main(int argc, char** argv) {
   long long lost_total = 0;
   int progress = 1;
   for (int step = 1; step <= steps; ++step) {
-    check(rd_step(e, step), "rd_step");
+    if (!b_pos) {
+      check(rd_step(e, step), "rd_step");
+    } else {
+      // the main loop's order (src/main.F90:186-198): emission, Update_Position, Write_Position
+      // (particles marked for removal still in the arrays), Remove_Particles
+      check(rd_do_emission(e, step), "rd_do_emission");
+      check(rd_update_position(e, step), "rd_update_position");
+      rd_counters c0;
+      check(rd_counters_get(e, diode, &c0), "rd_counters_get");
+      const int np = c0.n;
+      pbuf.resize(3 * (size_t)std::max(np, 1));
+      idbuf.resize((size_t)std::max(np, 1));
+      secbuf.resize((size_t)std::max(np, 1));
+      int got = 0;
+      check(rd_get_particles(e, diode, np, pbuf.data(), nullptr, nullptr, nullptr, idbuf.data(), secbuf.data(),
+                             &got), "rd_get_particles");
+      const int rec[2] = {step, got};
+      std::fwrite(rec, sizeof(int), 2, b_pos);
+      for (int i = 0; i < got; ++i) {   // x, y, z (m), emitter, section, id
+        const int i3[3] = {1, secbuf[i], idbuf[i]};
+        std::fwrite(&pbuf[3 * (size_t)i], sizeof(double), 3, b_pos);
+        std::fwrite(i3, sizeof(int), 3, b_pos);
+      }
+      check(rd_remove_particles(e, step), "rd_remove_particles");
+    }
     // volt.dt (Set_Voltage, src/mod_verlet.F90:2050-2057): "(ES12.4, tr2, i8, tr2, ES18.8)" with
     // four items, so format reversion puts V_rf (0) on a record of its own
     {
@@ -432,6 +477,23 @@ int main(int argc, char** argv) {
                     "  " + fmt_ES(0.0, 12, 4) + "  " + fmt_ES(c.ramo_current, 12, 4) + "  " +
                     fmt_ES(c.ramo_current_ion, 12, 4) + "  " + fmt_ES(0.0, 12, 4);
     std::fprintf(f_ramo, "%s\n", r.c_str());
+    if (b_ramo_sec) {
+      // ramo_current.bin (Write_Ramo_Current, src/mod_pair.F90:822-826): ramo_current_emit(section,
+      // emitter) of the step, MAX_SECTIONS x MAX_EMITTERS doubles.  Per particle q v . E_zunit with
+      // the velocities of the step; the particles removed in the step carry q = 0 there
+      // (Mark_Particles_Remove), so the survivors give the whole sum.
+      std::fill(ramo_sec.begin(), ramo_sec.end(), 0.0);
+      qbuf.resize((size_t)std::max(n, 1));
+      secbuf.resize((size_t)std::max(n, 1));
+      int got = 0;
+      check(rd_get_particles(e, diode, n, nullptr, vel.data(), nullptr, qbuf.data(), nullptr, secbuf.data(), &got),
+            "rd_get_particles");
+      for (int i = 0; i < got; ++i) {
+        const int sec = secbuf[i];
+        if (sec >= 1 && sec <= max_sections) ramo_sec[sec - 1] += qbuf[i] * (vel[3 * (size_t)i + 2] * (-1.0 / d));
+      }
+      std::fwrite(ramo_sec.data(), sizeof(double), ramo_sec.size(), b_ramo_sec);
+    }
     if (step * 10 >= progress * steps) {
       std::printf("RUMDEED: %3d %%  electrons %d, emitted %lld, absorbed %lld\n", progress * 10, c.n,
                   c.emitted_total, c.absorbed_top_total + c.absorbed_bot_total);
@@ -442,6 +504,8 @@ int main(int argc, char** argv) {
   for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo, b_emit, b_emit_elec, b_abs_top, b_abs_bot, f_field, f_volt})
     std::fclose(f);
   for (FILE* f : b_planes) if (f) std::fclose(f);
+  if (b_pos) std::fclose(b_pos);
+  if (b_ramo_sec) std::fclose(b_ramo_sec);
   rd_engine_destroy(e);
   if (lost_total) std::printf("RUMDEED: %lld event records did not fit the event log\n", lost_total);
   std::printf("RUMDEED: Main loop finished\n");

@@ -156,6 +156,53 @@ def test_driver_run_matches_python_binding(driver, tmp_path, rg):
 
 
 @pytest.mark.gpu
+def test_optional_position_and_section_current_files(driver, tmp_path, rg):
+    """WRITE_POSITION_FILE and WRITE_RAMO_SEC: out/position.bin (Write_Position,
+    src/mod_pair.F90:841-867, positions after Update_Position with the removed
+    particles still in place) and out/ramo_current.bin (ramo_current_emit per
+    section, 96 x 96 x 1 doubles a step).  The phase-by-phase stepping these
+    files need gives the same records as the graph-captured step."""
+    plain = tmp_path / "plain"
+    plain.mkdir()
+    _deck(plain)
+    r = subprocess.run([driver, str(plain)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    opt = tmp_path / "opt"
+    opt.mkdir()
+    (opt / "input").write_text(DECK.replace("  PLANES_N = 2,", "  WRITE_POSITION_FILE = .True.,\n"
+                                            "  WRITE_RAMO_SEC = .True.,\n  PLANES_N = 2,"))
+    (opt / "work").write_text(WORK)
+    r = subprocess.run([driver, str(opt)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    for name in ("emitted.dt", "absorbed_top.dt", "absorbed_bot.dt", "field.dt"):
+        assert (opt / "out" / name).read_text() == (plain / "out" / name).read_text(), name
+    emitted = np.loadtxt(opt / "out" / "emitted.dt")
+    top = np.loadtxt(opt / "out" / "absorbed_top.dt")
+    bot = np.loadtxt(opt / "out" / "absorbed_bot.dt")
+    raw = (opt / "out" / "position.bin").read_bytes()
+    head = np.frombuffer(raw[:8], dtype="<i4")
+    assert list(head) == [12, 1]
+    rec = np.dtype([("pos", "<f8", 3), ("emit", "<i4"), ("sec", "<i4"), ("id", "<i4")])
+    off = 8
+    for step in range(1, 13):
+        st, n = np.frombuffer(raw[off:off + 8], dtype="<i4")
+        off += 8
+        assert st == step
+        # in flight after the position update = emitted so far - absorbed in earlier steps
+        absorbed_before = top[:step - 1, 2].sum() + bot[:step - 1, 2].sum()
+        assert n == emitted[:step, 2].sum() - absorbed_before
+        parts = np.frombuffer(raw[off:off + n * rec.itemsize], dtype=rec)
+        off += n * rec.itemsize
+        assert np.all(parts["emit"] == 1) and np.all(np.diff(parts["id"]) > 0)
+        assert np.all(parts["sec"] >= 1) and np.all(parts["sec"] <= 4)   # the 2 x 2 work grid
+    assert off == len(raw)
+    rs = np.fromfile(opt / "out" / "ramo_current.bin", dtype="<f8").reshape(12, 96 * 96)
+    ramo = np.loadtxt(opt / "out" / "ramo_current.dt")
+    np.testing.assert_allclose(rs.sum(axis=1), ramo[:, 11], rtol=1e-4, atol=1e-30)   # ES12.4 text
+    assert np.all(rs[:, 4:] == 0.0) and np.abs(rs).sum() > 0
+
+
+@pytest.mark.gpu
 def test_event_log_counts_and_loss(rg):
     eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=3000 + 64,
                     chain_capacity=3000 + 64, quad_capacity=16384, event_capacity=8)
