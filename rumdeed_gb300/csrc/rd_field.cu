@@ -67,28 +67,34 @@ k_field_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __
       const float dnm = (float)(p.d * 1.0e9);
       F32Acc acc;
       acc.zero();
+      TipSums ts;   // tip: the K-scaled image sums, kept apart (tip_tile_split_f32)
+      ts.zero();
       for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
         __syncthreads();
         int j = jt + tid;
         if (j < it.j1) {
           sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j];
-          if (GEOM == RD_G_TIP) { sih[tid] = pool.ip_hi[off + j]; sil[tid] = pool.ip_lo[off + j]; }
+          if (GEOM == RD_G_TIP) sih[tid] = pool.ip_hi[off + j];
         }
         __syncthreads();
         int kmax = min(RD_TILE, it.j1 - jt);
         float tx = 0.f, ty = 0.f, tz = 0.f;
-        if (GEOM == RD_G_TIP)
-          tip_tile_f32<T_UPPER>(sh, sl, sih, sil, kmax, ih, il, iih, iil, -1, p.image_charge,
-                                (float)c_k.tip_K, tx, ty, tz);
-        else if (p.N_ic_max == 0)
+        if (GEOM == RD_G_TIP) {   // D per tile (folded into acc), U across the tiles
+          ts.dx = ts.dy = ts.dz = 0.f;
+          tip_tile_split_f32<T_UPPER>(sh, sl, sih, kmax, ih, il, iih, -1, p.image_charge, ts);
+          tx = ts.dx; ty = ts.dy; tz = ts.dz;
+        } else if (p.N_ic_max == 0) {
           planar_tile_f32<T_UPPER, true>(sh, sl, kmax, ih, il, -1, 0, dnm, p.image_charge, tx, ty, tz);
-        else
+        } else {
           planar_tile_f32<T_UPPER, false>(sh, sl, kmax, ih, il, -1, p.N_ic_max, dnm, p.image_charge, tx, ty, tz);
+        }
         acc.add(tx, ty, tz);
       }
-      fx = ((double)acc.hx + (double)acc.lx) * kscale;
-      fy = ((double)acc.hy + (double)acc.ly) * kscale;
-      fz = ((double)acc.hz + (double)acc.lz) * kscale;
+      fx = ((double)acc.hx + (double)acc.lx);
+      fy = ((double)acc.hy + (double)acc.ly);
+      fz = ((double)acc.hz + (double)acc.lz);
+      if (GEOM == RD_G_TIP) tip_split_finish(fx, fy, fz, ts, iih.w, p.image_charge, c_k.tip_K, &fx, &fy, &fz);
+      fx *= kscale; fy *= kscale; fz *= kscale;
     } else {
       const double L2 = c_k.L2, dfc = c_k.div_fac_c;
       fx = fy = fz = 0.0;
@@ -617,21 +623,26 @@ __device__ void warp_field_general(const DiodeParams& p, const Pool& pool, int n
     const float dnm = (float)(p.d * 1.0e9);
     F32Acc acc;
     acc.zero();
+    TipSums ts;   // tip: the K-scaled image sums, kept apart (tip_tile_split_f32)
+    ts.zero();
     for (int j = lane; j < n; j += 32) {
       float4 h = pool.pk_hi[off + j], l = pool.pk_lo[off + j];
       float tx = 0.f, ty = 0.f, tz = 0.f;
       if (p.geometry == RD_G_TIP) {
-        float4 jh = pool.ip_hi[off + j], jl = pool.ip_lo[off + j];
-        tip_tile_f32<T_UPPER>(&h, &l, &jh, &jl, 1, ih, il, iih, iil, -1, p.image_charge,
-                              (float)c_k.tip_K, tx, ty, tz);
+        float4 jh = pool.ip_hi[off + j];
+        ts.dx = ts.dy = ts.dz = 0.f;
+        tip_tile_split_f32<T_UPPER>(&h, &l, &jh, 1, ih, il, iih, -1, p.image_charge, ts);
+        tx = ts.dx; ty = ts.dy; tz = ts.dz;
       } else {
         planar_tile_f32<T_UPPER, false>(&h, &l, 1, ih, il, -1, p.N_ic_max, dnm, p.image_charge, tx, ty, tz);
       }
       acc.add(tx, ty, tz);
     }
-    fx = ((double)acc.hx + (double)acc.lx) * kscale;
-    fy = ((double)acc.hy + (double)acc.ly) * kscale;
-    fz = ((double)acc.hz + (double)acc.lz) * kscale;
+    fx = ((double)acc.hx + (double)acc.lx);
+    fy = ((double)acc.hy + (double)acc.ly);
+    fz = ((double)acc.hz + (double)acc.lz);
+    if (p.geometry == RD_G_TIP) tip_split_finish(fx, fy, fz, ts, iih.w, p.image_charge, c_k.tip_K, &fx, &fy, &fz);
+    fx *= kscale; fy *= kscale; fz *= kscale;
   } else {
     for (int j = lane; j < n; j += 32) {
       rd_d4 pj = make_d4(pool.x[off + j], pool.y[off + j], pool.z[off + j], pool.q[off + j]);
@@ -994,7 +1005,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
 }
 
 // Field sums of one j-tile at CPT tip proposals (upper role: the point's own
-// apex-sphere image, tip_tile_f32<T_UPPER>); one shared load feeds all of the
+// apex-sphere image, as tip_tile_split_f32<T_UPPER>); one shared load feeds all of the
 // thread's points.  The tip image term of the reference carries an extra
 // factor K = q0 / (4 pi eps0) (acc_tip_ic_force.inc:17-22):
 //   E = sum_j q_j [ d/|d|^3 + K (d/|d|^3 - c e/|e|^3) ] = (1 + K) D - K c S,

@@ -269,10 +269,9 @@ k_force_tip_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
                 const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
                 double* __restrict__ partial, int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
   __shared__ int s_item;
-  __shared__ float4 sh[RD_TILE], sl[RD_TILE], sih[RD_TILE], sil[RD_TILE];
+  __shared__ float4 sh[RD_TILE], sl[RD_TILE], sih[RD_TILE];
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x;
-  const float K = (float)c_k.tip_K;
   for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
@@ -281,30 +280,32 @@ k_force_tip_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
     const bool valid = i < n;
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     float4 ih = valid ? pool.pk_hi[off + i] : z4, il = valid ? pool.pk_lo[off + i] : z4;
-    float4 iih = valid ? pool.ip_hi[off + i] : z4, iil = valid ? pool.ip_lo[off + i] : z4;
-    F32Acc acc;
+    float4 iih = valid ? pool.ip_hi[off + i] : z4;
+    F32Acc acc;          // the direct sum D, compensated across tiles
     acc.zero();
+    TipSums ts;          // the K-scaled image sums U, W, Lz (tip_tile_split_f32)
+    ts.zero();
     for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
       __syncthreads();
       int j = jt + tid;
       if (j < it.j1) {
         sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j];
-        sih[tid] = pool.ip_hi[off + j]; sil[tid] = pool.ip_lo[off + j];
+        sih[tid] = pool.ip_hi[off + j];
       }
       __syncthreads();
       int kmax = min(RD_TILE, it.j1 - jt);
-      float tx = 0.f, ty = 0.f, tz = 0.f;
+      ts.dx = ts.dy = ts.dz = 0.f;
       if (jt == it.i0)
-        tip_tile_f32<T_DIAG>(sh, sl, sih, sil, kmax, ih, il, iih, iil, tid, p.image_charge, K, tx, ty, tz);
+        tip_tile_split_f32<T_DIAG>(sh, sl, sih, kmax, ih, il, iih, tid, p.image_charge, ts);
       else if (jt > it.i0)
-        tip_tile_f32<T_UPPER>(sh, sl, sih, sil, kmax, ih, il, iih, iil, -1, p.image_charge, K, tx, ty, tz);
+        tip_tile_split_f32<T_UPPER>(sh, sl, sih, kmax, ih, il, iih, -1, p.image_charge, ts);
       else
-        tip_tile_f32<T_LOWER>(sh, sl, sih, sil, kmax, ih, il, iih, iil, -1, p.image_charge, K, tx, ty, tz);
-      acc.add(tx, ty, tz);
+        tip_tile_split_f32<T_LOWER>(sh, sl, sih, kmax, ih, il, iih, -1, p.image_charge, ts);
+      acc.add(ts.dx, ts.dy, ts.dz);
     }
-    double fx = (double)acc.hx + (double)acc.lx;
-    double fy = (double)acc.hy + (double)acc.ly;
-    double fz = (double)acc.hz + (double)acc.lz;
+    double fx, fy, fz;
+    tip_split_finish((double)acc.hx + (double)acc.lx, (double)acc.hy + (double)acc.ly,
+                     (double)acc.hz + (double)acc.lz, ts, iih.w, p.image_charge, c_k.tip_K, &fx, &fy, &fz);
     if (it.nch > 1) {
       double* pp = partial + (size_t)g * 3 * RD_ITILE;
       pp[tid] = fx; pp[RD_ITILE + tid] = fy; pp[2 * RD_ITILE + tid] = fz;

@@ -139,59 +139,72 @@ __device__ __forceinline__ void planar_tile_f64(const rd_d4* __restrict__ sj, in
 // ---- hyperboloid tip -------------------------------------------------------------
 // Sphere image term (acc_tip_image_point.inc + acc_tip_ic_force.inc):
 // a = lower-indexed particle, b = higher-indexed,
-//   IC = K [ (a - b)/|b - a|^3 - (R/dis_a) (im_a - b)/|b - im_a|^3 ]
+//   IC = K [ (a - b)/|b - a|^3 - c_a (im_a - b)/|b - im_a|^3 ],  c_a = R / dis_a,
 // applied to the lower particle as is and to the higher one mirrored in x, y.
+// With K = q0 / (4 pi eps0) ~ 1.4e-9 this part sits far below the FP32
+// resolution of the direct sum, so the FP32 tiles keep it in separate sums
+// that the caller scales by K in FP64.  For particle i against the j of one
+// tile (d = x_i - x_j, e = image point - position):
+//   D  = sum q d / |d|^3                          (all j; compensated d)
+//   U  = sum_{j > i} q e_i / |e_i|^3,   e_i = im_i - x_j   (i in the a role)
+//   W  = sum_{j < i} q c_j (ex, ey, -ez)_j / |e_j|^3,  e_j = im_j - x_i
+//   Lz = sum_{j < i} q dz / |d|^3
+// and the field is (1 + K) D + K (W - c_i U - 2 Lz z^).  U and W use the high
+// words only: their relative error (~1e-5 for the nearest charges) is ~1e-14
+// of the field once scaled by K.  MODE T_UPPER: every j in the a... b role of
+// a point (fields), T_LOWER: every j lower, T_DIAG: by index against self_k.
+struct TipSums {
+  float dx, dy, dz, ux, uy, uz, wx, wy, wz, lz;
+  __device__ void zero() { dx = dy = dz = ux = uy = uz = wx = wy = wz = lz = 0.f; }
+};
+
 template <int MODE>
-__device__ __forceinline__ void tip_tile_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
-                                             const float4* __restrict__ sih, const float4* __restrict__ sil,
-                                             int kmax, float4 ih, float4 il, float4 iih, float4 iil,
-                                             int self_k, int ic, float K, float& tx, float& ty,
-                                             float& tz) {
-  float sx = 0.f, sy = 0.f, sz = 0.f;
+__device__ __forceinline__ void tip_tile_split_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
+                                                   const float4* __restrict__ sih, int kmax, float4 ih,
+                                                   float4 il, float4 iih, int self_k, int ic, TipSums& t) {
   for (int k = 0; k < kmax; ++k) {
-    float4 h = sh[k], l = sl[k];
-    float q = h.w;
-    if (MODE == T_DIAG) q = (k == self_k) ? 0.f : q;
-    float dx = (ih.x - h.x) + (il.x - l.x);
-    float dy = (ih.y - h.y) + (il.y - l.y);
-    float dz = (ih.z - h.z) + (il.z - l.z);
-    float r2 = fmaf(dz, dz, fmaf(dx, dx, dy * dy));
-    float inv = rsqrtf(fmaxf(r2, 1e-20f));
-    float inv3 = (inv * inv) * inv;
-    float s = q * inv3;
-    sx = fmaf(s, dx, sx);
-    sy = fmaf(s, dy, sy);
-    sz = fmaf(s, dz, sz);
+    const float4 h = sh[k], l = sl[k];
+    const float q = (MODE == T_DIAG && k == self_k) ? 0.f : h.w;
+    const float dx = (ih.x - h.x) + (il.x - l.x);
+    const float dy = (ih.y - h.y) + (il.y - l.y);
+    const float dz = (ih.z - h.z) + (il.z - l.z);
+    const float inv = rsqrtf(fmaf(dz, dz, fmaf(dx, dx, fmaf(dy, dy, 1e-20f))));
+    const float s = q * ((inv * inv) * inv);
+    t.dx = fmaf(s, dx, t.dx);
+    t.dy = fmaf(s, dy, t.dy);
+    t.dz = fmaf(s, dz, t.dz);
     if (ic) {
-      bool upper = (MODE == T_UPPER) || (MODE == T_DIAG && k > self_k);
-      // e = im_a - b: upper (a = i, b = j) uses the thread's image point,
-      // lower (a = j, b = i) the tile's.
-      float ex, ey, ez, c;
+      const bool upper = (MODE == T_UPPER) || (MODE == T_DIAG && k > self_k);
       if (upper) {
-        ex = (iih.x - h.x) + (iil.x - l.x);
-        ey = (iih.y - h.y) + (iil.y - l.y);
-        ez = (iih.z - h.z) + (iil.z - l.z);
-        c = iih.w;
+        const float ex = iih.x - h.x, ey = iih.y - h.y, ez = iih.z - h.z;
+        const float re = rsqrtf(fmaf(ez, ez, fmaf(ex, ex, fmaf(ey, ey, 1e-20f))));
+        const float se = q * ((re * re) * re);
+        t.ux = fmaf(se, ex, t.ux);
+        t.uy = fmaf(se, ey, t.uy);
+        t.uz = fmaf(se, ez, t.uz);
       } else {
-        float4 jh = sih[k], jl = sil[k];
-        ex = (jh.x - ih.x) + (jl.x - il.x);
-        ey = (jh.y - ih.y) + (jl.y - il.y);
-        ez = (jh.z - ih.z) + (jl.z - il.z);
-        c = jh.w;
+        const float4 jh = sih[k];
+        const float ex = jh.x - ih.x, ey = jh.y - ih.y, ez = jh.z - ih.z;
+        const float re = rsqrtf(fmaf(ez, ez, fmaf(ex, ex, fmaf(ey, ey, 1e-20f))));
+        const float se = (q * jh.w) * ((re * re) * re);
+        t.wx = fmaf(se, ex, t.wx);
+        t.wy = fmaf(se, ey, t.wy);
+        t.wz = fmaf(-se, ez, t.wz);
+        t.lz = fmaf(s, dz, t.lz);
       }
-      float re = rsqrtf(fmaxf(fmaf(ez, ez, fmaf(ex, ex, ey * ey)), 1e-20f));
-      float se = c * (re * re) * re;
-      // upper: K[ d inv3 - c e/|e|^3 ];  lower (mirrored x, y):
-      //        K[ (dx, dy, -dz) inv3 + c (ex, ey, -ez)/|e|^3 ]
-      //   x, y: K [ d inv3 - sgn c e/|e|^3 ],  z: K [ sgn d inv3 - c e/|e|^3 ]
-      float sgn = upper ? 1.f : -1.f;
-      float kq = K * q;
-      sx = fmaf(kq, fmaf(inv3, dx, -sgn * se * ex), sx);
-      sy = fmaf(kq, fmaf(inv3, dy, -sgn * se * ey), sy);
-      sz = fmaf(kq, fmaf(sgn * inv3, dz, -se * ez), sz);
     }
   }
-  tx += sx; ty += sy; tz += sz;
+}
+
+// The FP64 finish of the split sums: (1 + K) D + K (W - c_i U - 2 Lz z^), D
+// given in FP64 (compensated across tiles), c_i = R / dis_i of the point.
+__device__ __forceinline__ void tip_split_finish(double Dx, double Dy, double Dz, const TipSums& t, float ci,
+                                                 int ic, double K, double* fx, double* fy, double* fz) {
+  if (!ic) { *fx = Dx; *fy = Dy; *fz = Dz; return; }
+  const double c = (double)ci;
+  *fx = (1.0 + K) * Dx + K * ((double)t.wx - c * (double)t.ux);
+  *fy = (1.0 + K) * Dy + K * ((double)t.wy - c * (double)t.uy);
+  *fz = (1.0 + K) * Dz + K * (((double)t.wz - c * (double)t.uz) - 2.0 * (double)t.lz);
 }
 
 // FP64 tip gather: Calculate_Acceleration_Particles_ACC tip branch (:1344-1426).

@@ -631,3 +631,37 @@ def test_two_time_step_full_steps_with_emission_fp64(rg, orc):
     assert nrel(p["vel"] + 1e-3, o.arr("vel") + 1e-3) < 1e-8
     assert c["emitted_total"] == o.s.emitted_total > 0
     eng.close()
+
+
+def test_tip_image_term_survives_fp32(rg):
+    """The tip sphere-image term carries the reference's extra factor
+    K = q0 / (4 pi eps0) ~ 1.4e-9 (acc_tip_ic_force.inc), far below the FP32
+    resolution of the direct sum.  The FP32 tiles keep it in separate sums
+    scaled in FP64, so the image part of the acceleration and of the field
+    (image charge on minus off) matches the FP64 form's."""
+    rng = np.random.default_rng(5)
+    tip = (900 * NM, 100 * NM, 100 * NM)
+    n = 257
+    pos = np.column_stack([rng.uniform(-300 * NM, 300 * NM, n), rng.uniform(-300 * NM, 300 * NM, n),
+                           rng.uniform(105 * NM, 990 * NM, n)])
+    pts = np.array([[0.0, 0.0, 102.0], [30.0, -10.0, 130.0], [-50.0, 40.0, 300.0]]) * NM
+    diff = {}
+    for prec in (rg.PREC_FP64, rg.PREC_FP32C):
+        eng = rg.Engine(precision=prec, max_diodes=2, particle_capacity=4096)
+        on = eng.add_diode(geometry=rg.GEOM_TIP, V_s=2e3, capacity=1024, tip_dim=tip, image_charge=True)
+        off = eng.add_diode(geometry=rg.GEOM_TIP, V_s=2e3, capacity=1024, tip_dim=tip, image_charge=False)
+        on.add_particles(pos)
+        off.add_particles(pos)
+        a_on = on.calculate_acceleration_particles()
+        a_off = off.particles()["acc"]   # the same pass filled both diodes
+        f_on = on.calc_field_at_batch(pts)
+        diff[prec] = (a_on - a_off, f_on - off.calc_field_at_batch(pts), f_on)
+        eng.close()
+    da64, df64, f64 = diff[rg.PREC_FP64]
+    da32, df32, _ = diff[rg.PREC_FP32C]
+    assert np.all(np.linalg.norm(da64, axis=1) > 0)
+    assert nrel(da32, da64) < 1e-3
+    # the fields include the GV/m vacuum field: both forms round the total at its ulp, which is
+    # ~1e-3 of the image part here, and the FP64 form adds each image term into the running sum
+    tol = 1e-3 * np.abs(df64) + 16 * np.finfo(float).eps * np.linalg.norm(f64, axis=1)[:, None]
+    assert np.all(np.abs(df32 - df64) <= tol), (df32, df64)
