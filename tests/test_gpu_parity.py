@@ -2,7 +2,7 @@
 
 Tolerances (per particle / point, norm-relative, as src/mod_tests.F90:1665-1669):
   FP64 plain form          <= 1e-12
-  FP32 compensated form    <= 1e-5  (the spec force tolerance)
+  FP32 compensated form    <= 1e-5  (the stated force tolerance of the FP32 form)
 Integer and index results (counts, ids, order, emitted sets) must be equal.
 """
 import numpy as np
