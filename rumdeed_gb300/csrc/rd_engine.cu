@@ -307,6 +307,7 @@ struct Sig {
   bool emit_serial = false;   // some planar diode uses the serial MH sampler
   bool tts = false;           // some diode uses the two-time-step integrator
   int jumps = 0;
+  int mh_planar = 0;          // planar diodes with batched MH chains
 };
 static Sig signature(const rd_engine* e) {
   Sig s;
@@ -319,6 +320,7 @@ static Sig signature(const rd_engine* e) {
     if (p.emission) {
       if (p.geometry == RD_G_TIP) s.emit_tip = true; else s.emit_planar = true;
       if (p.geometry != RD_G_TIP && p.mh_serial) s.emit_serial = true;
+      if (p.geometry != RD_G_TIP && !p.mh_serial) s.mh_planar++;
       s.jumps = std::max(s.jumps, p.mh_jumps);
     }
   }
@@ -332,7 +334,8 @@ static Sig signature(const rd_engine* e) {
 // others' launches fill the idle SMs.  Results do not depend on it.
 static int launch_mh_jumps(rd_engine* e, const Sig& s) {
   const int prec = e->cfg.precision;
-  const int parts = s.emit_planar ? RD_MH_PARTS : 1;
+  // one diode cannot be split: it runs as one launch per jump (part 0)
+  const int parts = s.mh_planar > 1 ? RD_MH_PARTS : 1;
   if (parts > 1) {
     CK(cudaEventRecord(e->ev_fork, e->st));
     for (int q = 1; q < parts; ++q) CK(cudaStreamWaitEvent(e->stp[q], e->ev_fork, 0));
@@ -344,7 +347,7 @@ static int launch_mh_jumps(rd_engine* e, const Sig& s) {
         int* queue = q == 0 ? e->item_queue : e->item_queue + 6 + 2 * (q + 1);
         CK(rd_launch_mh_jump(prec, 1, e->grid, sq, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
                              e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, queue,
-                             q + 1));
+                             parts > 1 ? q + 1 : 0));
       }
       e->kernels_in_step += parts;
     }
@@ -472,8 +475,8 @@ static int launch_step_body(rd_engine* e) {
 static std::string sig_string(rd_engine* e) {
   Sig s = signature(e);
   char b[128];
-  snprintf(b, sizeof b, "%d%d%d%d%d%d%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
-           s.emit_serial, s.tts, s.jumps, e->clen_min, e->nch_max);
+  snprintf(b, sizeof b, "%d%d%d%d%d%d%d%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
+           s.emit_serial, s.tts, s.mh_planar > 1, s.jumps, e->clen_min, e->nch_max);
   return b;
 }
 
