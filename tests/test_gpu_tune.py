@@ -7,7 +7,7 @@ mix under any one chunking."""
 import numpy as np
 import pytest
 
-from test_gpu_serve import alone, make_requests
+from test_gpu_serve import make_requests
 
 pytestmark = pytest.mark.gpu
 
