@@ -1,15 +1,29 @@
 """Pins the CPU oracle (oracle/rd_oracle.c) to the reference's own tests.
 
 Every test here ports a known-answer test of src/mod_tests.F90 (or
-src/mod_field_emission_v2.F90:1742-1778) with its golden values and its
+src/mod_field_emission_v2.F90:1742-1778) with its golden values (read from the
+fixture tests/golden/reference_golden.json, extracted from those sources) and its
 tolerances (2 % relative or 1e-6 absolute per component, src/mod_global.F90:
 419-420, unless the reference test states a tighter one).  Runs on CPU only.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
 NM = 1e-9
 TOL_REL, TOL_ABS = 0.02, 1e-6
+
+# The literals the reference's own tests compare against, extracted from its
+# sources by tests/golden/extract_reference_golden.py (committed fixture).
+with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_golden.json")) as _f:
+    GOLDEN = json.load(_f)
+
+
+def golden(label):
+    """Expected value of the reference test assertion with this label."""
+    return GOLDEN["assert_close"][label]["value"]
 
 
 def close(actual, expected):
@@ -42,19 +56,20 @@ def test_constants(orc):
 def test_fn_functions(orc):
     """Test_FN_Functions, src/mod_tests.F90:1688-1736 (phi = 4.7 eV)."""
     L = orc.lib()
-    assert L.orc_v_y(-2e9, 4.7, 0) == 1.0 and L.orc_t_y(-2e9, 4.7, 0) == 1.0
-    close(L.orc_v_y(-2e9, 4.7, 1), 0.8253581935658024)
-    close(L.orc_t_y(-2e9, 4.7, 1), 1.0292422630703880)
-    close(L.orc_escape_prob_log(-2e9, 4.7, 1), -28.723444978828507)
-    close(L.orc_v_y(-4e9, 4.7, 1), 0.6808388366998485)
-    close(L.orc_t_y(-4e9, 4.7, 1), 1.0484437096180323)
-    close(L.orc_escape_prob_log(-4e9, 4.7, 1), -11.846999895226958)
-    close(L.orc_v_y(-1e12, 4.7, 1), 0.0)
+    assert L.orc_v_y(-2e9, 4.7, 0) == golden("FN: v_y = 1 without image charge")
+    assert L.orc_t_y(-2e9, 4.7, 0) == golden("FN: t_y = 1 without image charge")
+    close(L.orc_v_y(-2e9, 4.7, 1), golden("FN: v_y at F = -2 GV/m"))
+    close(L.orc_t_y(-2e9, 4.7, 1), golden("FN: t_y at F = -2 GV/m"))
+    close(L.orc_escape_prob_log(-2e9, 4.7, 1), golden("FN: log escape probability at F = -2 GV/m"))
+    close(L.orc_v_y(-4e9, 4.7, 1), golden("FN: v_y at F = -4 GV/m"))
+    close(L.orc_t_y(-4e9, 4.7, 1), golden("FN: t_y at F = -4 GV/m"))
+    close(L.orc_escape_prob_log(-4e9, 4.7, 1), golden("FN: log escape probability at F = -4 GV/m"))
+    close(L.orc_v_y(-1e12, 4.7, 1), golden("FN: v_y clamps to 0 above the barrier maximum"))
     # the restatement reproduces the golden values far below the 2 % band
-    assert abs(L.orc_escape_prob_log(-2e9, 4.7, 1) + 28.723444978828507) < 1e-12
-    assert abs(L.orc_v_y(-4e9, 4.7, 1) - 0.6808388366998485) < 1e-14
+    assert abs(L.orc_escape_prob_log(-2e9, 4.7, 1) - golden("FN: log escape probability at F = -2 GV/m")) < 1e-12
+    assert abs(L.orc_v_y(-4e9, 4.7, 1) - golden("FN: v_y at F = -4 GV/m")) < 1e-14
     # Test_Field_Emission_Module (mod_field_emission_v2.F90:1758-1765): |dv| < 1e-6
-    assert abs(L.orc_v_y(-2.0e3 / 1000.0e-9, 4.7, 1) - 0.8253581935658024) < 1e-6
+    assert abs(L.orc_v_y(-2.0e3 / 1000.0e-9, 4.7, 1) - golden("FN: v_y at F = -2 GV/m")) < 1e-6
 
 
 def _three_particles(orc, ic=False, nic=0, d=100 * NM, V=2.0):
@@ -93,7 +108,7 @@ def test_field_probe_golden(orc):
     # the probe literals are default (single precision) REALs in the reference
     probe = np.array([np.float32(-4.55), np.float32(-2.34), np.float32(96.44)], dtype=np.float64) * NM
     E = o.field_at(probe[None, :])[0]
-    close(E, [-314559.29097098, 1423979.07058996, -20246038.87978313])
+    close(E, GOLDEN["E_python"]["values"])
     # empty-system field (Test_Planar_Field :1128-1148)
     empty = orc.OracleDiode(cap=4, V_s=2.0, d=100 * NM, image_charge=False)
     close(empty.field_at(np.array([[-4.55, -2.34, 96.44]]) * NM)[0], [0.0, 0.0, -2.0 / (100 * NM)])
@@ -270,12 +285,12 @@ def test_work_function_checkerboard(orc):
                                     C.byref(sec))
         return v, sec.value
 
-    assert at(25, 25) == (4.30, 1)
-    assert at(75, 25) == (4.40, 2)
-    assert at(25, 75) == (4.10, 3)
-    assert at(75, 75) == (4.20, 4)
-    assert at(150, 25) == (4.40, 2)
-    assert at(-10, 130) == (4.10, 3)
+    assert at(25, 25) == (golden("Work function: bottom left value"), 1)
+    assert at(75, 25) == (golden("Work function: bottom right value"), 2)
+    assert at(25, 75) == (golden("Work function: top left value"), 3)
+    assert at(75, 75) == (golden("Work function: top right value"), 4)
+    assert at(150, 25) == (golden("Work function: clamped in x"), 2)
+    assert at(-10, 130) == (golden("Work function: clamped in x and y"), 3)
 
 
 def test_tip_acceleration(orc):
@@ -348,17 +363,17 @@ def test_voronoi_work_function_unit_test(orc):
     given there in absolute coordinates; with a unit emitter at the origin
     the fraction-of-emitter convention of Read_work_function gives the same."""
     import ctypes as C
-    xs = [0.5, 0.0, 0.0, 1.1, 0.8, 1.4, 2.33, 2.0, 2.1]
-    ys = [0.0, 1.0, 2.3, 0.0, 1.0, 2.0, 0.0, 1.25, 2.7]
-    w = np.array([v for i in range(9) for v in (xs[i], ys[i], float(i + 1), float(i + 1))])
+    v = GOLDEN["voronoi"]
+    n = len(v["sites_x"])
+    w = np.array([x for i in range(n) for x in (v["sites_x"][i], v["sites_y"][i], v["w_theta"][i], v["sec"][i])])
     pos, dim = np.zeros(2), np.ones(2)
     sec = C.c_int(-1)
     L = orc.lib()
     dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
-    assert L.orc_work_voronoi(dp(w), 9, dp(pos), dp(dim), 1.5, 1.0, C.byref(sec)) == pytest.approx(8.0, abs=1e-3)
-    assert sec.value == 8
-    assert L.orc_work_voronoi(dp(w), 9, dp(pos), dp(dim), 1.0 / 3.0, 5.0 / 3.0, C.byref(sec)) == pytest.approx(3.0, abs=1e-3)
-    assert sec.value == 3
+    assert len(v["points"]) == len(v["expect"]) == 2
+    for (x, y), e in zip(v["points"], v["expect"]):
+        assert L.orc_work_voronoi(dp(w), n, dp(pos), dp(dim), x, y, C.byref(sec)) == pytest.approx(e["w_theta"], abs=e["tol"])
+        assert sec.value == e["sec"]
 
 
 def test_gaussian_work_function_formula(orc):
