@@ -30,7 +30,9 @@ namespace {
 // z_i + z_j = 2 z_i - dz (2 z_i as one float: relative error 6e-8).  The
 // 1e-20 nm^2 floor inside dxy^2 keeps the self pair and coincident pairs
 // finite (their q or d is zero).
-template <bool IC, bool DIAG>
+// ELEC (off-diagonal tiles whose charges are all -1, the electrons' q/q0):
+// the charge multiplies are dropped and the sign folded into the sums.
+template <bool IC, bool DIAG, bool ELEC = false>
 __device__ __forceinline__ void planar_tile2_nic0(const float4* __restrict__ sh, const float4* __restrict__ sl,
                                                   int kmax, float4 ah, float4 al, float atz, float4 bh,
                                                   float4 bl, float btz, int self_a, int self_b,
@@ -39,8 +41,8 @@ __device__ __forceinline__ void planar_tile2_nic0(const float4* __restrict__ sh,
 #pragma unroll 2
   for (int k = 0; k < kmax; ++k) {
     const float4 h = sh[k], l = sl[k];
-    const float qa = (DIAG && k == self_a) ? 0.f : h.w;
-    const float qb = (DIAG && k == self_b) ? 0.f : h.w;
+    const float qa = ELEC ? 1.f : ((DIAG && k == self_a) ? 0.f : h.w);
+    const float qb = ELEC ? 1.f : ((DIAG && k == self_b) ? 0.f : h.w);
     {
       const float dx = (ah.x - h.x) + (al.x - l.x), dy = (ah.y - h.y) + (al.y - l.y);
       const float dz = (ah.z - h.z) + (al.z - l.z);
@@ -76,6 +78,7 @@ __device__ __forceinline__ void planar_tile2_nic0(const float4* __restrict__ sh,
       }
     }
   }
+  if (ELEC) { ax = -ax; ay = -ay; az = -az; bx = -bx; by = -by; bz = -bz; }
   ta.x += ax; ta.y += ay; ta.z += az;
   tb.x += bx; tb.y += by; tb.z += bz;
 }
@@ -102,16 +105,22 @@ k_force_planar_f32_nic0(const DiodeParams* __restrict__ P, Pool pool,
     A.zero(); B.zero();
     for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
       __syncthreads();
+      int elec = 1;   // every charge of the tile is an electron's
       for (int q = tid; q < RD_TILE; q += nt) {
         const int j = jt + q;
-        if (j < it.j1) { sh[q] = pool.pk_hi[off + j]; sl[q] = pool.pk_lo[off + j]; }
+        if (j < it.j1) {
+          const float4 hj = pool.pk_hi[off + j];
+          sh[q] = hj; sl[q] = pool.pk_lo[off + j];
+          elec &= (hj.w == -1.0f);
+        }
       }
-      __syncthreads();
+      elec = __syncthreads_and(elec);
       const int kmax = min(RD_TILE, it.j1 - jt);
       float3 ta = make_float3(0.f, 0.f, 0.f), tb = ta;
       const bool diag = (jt == it.i0);
       if (ic) {
         if (diag) planar_tile2_nic0<true, true>(sh, sl, kmax, ah, al, atz, bh, bl, btz, tid, nt + tid, ta, tb);
+        else if (elec) planar_tile2_nic0<true, false, true>(sh, sl, kmax, ah, al, atz, bh, bl, btz, -1, -1, ta, tb);
         else planar_tile2_nic0<true, false>(sh, sl, kmax, ah, al, atz, bh, bl, btz, -1, -1, ta, tb);
       } else {
         if (diag) planar_tile2_nic0<false, true>(sh, sl, kmax, ah, al, atz, bh, bl, btz, tid, nt + tid, ta, tb);
@@ -173,16 +182,23 @@ k_force_planar_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict
     for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
       __syncthreads();
       int j = jt + tid;
-      if (j < it.j1) { sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j]; }
-      __syncthreads();
+      int elec = 1;   // every charge of the tile is an electron's
+      if (j < it.j1) {
+        const float4 hj = pool.pk_hi[off + j];
+        sh[tid] = hj; sl[tid] = pool.pk_lo[off + j];
+        elec = (hj.w == -1.0f);
+      }
+      elec = __syncthreads_and(elec);
       int kmax = min(RD_TILE, it.j1 - jt);
       float tx = 0.f, ty = 0.f, tz = 0.f;
       if (jt == it.i0)
         planar_tile_f32<T_DIAG, NIC0>(sh, sl, kmax, ih, il, tid, nic, dnm, ic, tx, ty, tz);
       else if (jt > it.i0)
-        planar_tile_f32<T_UPPER, NIC0>(sh, sl, kmax, ih, il, -1, nic, dnm, ic, tx, ty, tz);
+        elec ? planar_tile_f32<T_UPPER, NIC0, true>(sh, sl, kmax, ih, il, -1, nic, dnm, ic, tx, ty, tz)
+             : planar_tile_f32<T_UPPER, NIC0>(sh, sl, kmax, ih, il, -1, nic, dnm, ic, tx, ty, tz);
       else
-        planar_tile_f32<T_LOWER, NIC0>(sh, sl, kmax, ih, il, -1, nic, dnm, ic, tx, ty, tz);
+        elec ? planar_tile_f32<T_LOWER, NIC0, true>(sh, sl, kmax, ih, il, -1, nic, dnm, ic, tx, ty, tz)
+             : planar_tile_f32<T_LOWER, NIC0>(sh, sl, kmax, ih, il, -1, nic, dnm, ic, tx, ty, tz);
       acc.add(tx, ty, tz);
     }
     double fx = (double)acc.hx + (double)acc.lx;
@@ -288,19 +304,24 @@ k_force_tip_f32(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
     for (int jt = it.j0; jt < it.j1; jt += RD_TILE) {
       __syncthreads();
       int j = jt + tid;
+      int elec = 1;   // every charge of the tile is an electron's
       if (j < it.j1) {
-        sh[tid] = pool.pk_hi[off + j]; sl[tid] = pool.pk_lo[off + j];
+        const float4 hj = pool.pk_hi[off + j];
+        sh[tid] = hj; sl[tid] = pool.pk_lo[off + j];
         sih[tid] = pool.ip_hi[off + j];
+        elec = (hj.w == -1.0f);
       }
-      __syncthreads();
+      elec = __syncthreads_and(elec);
       int kmax = min(RD_TILE, it.j1 - jt);
       ts.dx = ts.dy = ts.dz = 0.f;
       if (jt == it.i0)
         tip_tile_split_f32<T_DIAG>(sh, sl, sih, kmax, ih, il, iih, tid, p.image_charge, ts);
       else if (jt > it.i0)
-        tip_tile_split_f32<T_UPPER>(sh, sl, sih, kmax, ih, il, iih, -1, p.image_charge, ts);
+        elec ? tip_tile_split_f32<T_UPPER, true>(sh, sl, sih, kmax, ih, il, iih, -1, p.image_charge, ts)
+             : tip_tile_split_f32<T_UPPER>(sh, sl, sih, kmax, ih, il, iih, -1, p.image_charge, ts);
       else
-        tip_tile_split_f32<T_LOWER>(sh, sl, sih, kmax, ih, il, iih, -1, p.image_charge, ts);
+        elec ? tip_tile_split_f32<T_LOWER, true>(sh, sl, sih, kmax, ih, il, iih, -1, p.image_charge, ts)
+             : tip_tile_split_f32<T_LOWER>(sh, sl, sih, kmax, ih, il, iih, -1, p.image_charge, ts);
       acc.add(ts.dx, ts.dy, ts.dz);
     }
     double fx, fy, fz;

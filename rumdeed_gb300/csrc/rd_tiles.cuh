@@ -19,7 +19,9 @@ struct F32Acc {
 
 // ---- planar, FP32 compensated ------------------------------------------------
 // One j-tile against the thread's particle i.  NIC0: N_ic_max == 0 fast path.
-template <int MODE, bool NIC0>
+// ELEC (tiles whose charges are all -1, the electrons' q/q0; not the
+// diagonal tile): the charge is a constant, so its multiplies fold into signs.
+template <int MODE, bool NIC0, bool ELEC = false>
 __device__ __forceinline__ void planar_tile_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
                                                 int kmax, float4 ih, float4 il, int self_k,
                                                 int nic, float dnm, int ic, float& tx,
@@ -28,7 +30,7 @@ __device__ __forceinline__ void planar_tile_f32(const float4* __restrict__ sh, c
 #pragma unroll 4
   for (int k = 0; k < kmax; ++k) {
     float4 h = sh[k], l = sl[k];
-    float q = h.w;
+    float q = ELEC ? -1.f : h.w;
     if (MODE == T_DIAG) q = (k == self_k) ? 0.f : q;
     float dx = (ih.x - h.x) + (il.x - l.x);
     float dy = (ih.y - h.y) + (il.y - l.y);
@@ -158,13 +160,15 @@ struct TipSums {
   __device__ void zero() { dx = dy = dz = ux = uy = uz = wx = wy = wz = lz = 0.f; }
 };
 
-template <int MODE>
+// ELEC (off-diagonal tiles whose charges are all -1, the electrons' q/q0):
+// the charge is a constant and its multiplies fold into the sums' signs.
+template <int MODE, bool ELEC = false>
 __device__ __forceinline__ void tip_tile_split_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
                                                    const float4* __restrict__ sih, int kmax, float4 ih,
                                                    float4 il, float4 iih, int self_k, int ic, TipSums& t) {
   for (int k = 0; k < kmax; ++k) {
     const float4 h = sh[k], l = sl[k];
-    const float q = (MODE == T_DIAG && k == self_k) ? 0.f : h.w;
+    const float q = ELEC ? -1.f : ((MODE == T_DIAG && k == self_k) ? 0.f : h.w);
     const float dx = (ih.x - h.x) + (il.x - l.x);
     const float dy = (ih.y - h.y) + (il.y - l.y);
     const float dz = (ih.z - h.z) + (il.z - l.z);
