@@ -665,3 +665,26 @@ def test_tip_image_term_survives_fp32(rg):
     # ~1e-3 of the image part here, and the FP64 form adds each image term into the running sum
     tol = 1e-3 * np.abs(df64) + 16 * np.finfo(float).eps * np.linalg.norm(f64, axis=1)[:, None]
     assert np.all(np.abs(df32 - df64) <= tol), (df32, df64)
+
+
+@pytest.mark.parametrize("nic", [0, 3])
+def test_fp32c_mixed_electron_and_ion_tiles(rg, orc, nic):
+    """Ions only among the first 64 particles: their j-tile takes the general
+    FP32 tile, the all-electron tiles the variant without charge multiplies;
+    accelerations and fields stay within the FP32 tolerance of the FP64 oracle."""
+    rng = np.random.default_rng(12)
+    n = 700
+    pos = uniform_particles(rng, n)
+    sp = np.where((np.arange(n) < 64) & (np.arange(n) % 4 == 1), 2, 1)
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=2, particle_capacity=4096)
+    dio = eng.add_diode(V_s=2e3, gap=1000 * NM, capacity=1024, image_charge=True, N_ic_max=nic)
+    dio.add_particles(pos, species=sp)
+    o = orc.OracleDiode(cap=1024, V_s=2e3, d=1000 * NM, image_charge=True, N_ic_max=nic)
+    for p, s in zip(pos, sp):
+        o.add(p, species=int(s))
+    assert nrel(dio.calculate_acceleration_particles(), o.accel("gather", True)) <= TOL32
+    pts = np.vstack([uniform_particles(rng, 50),
+                     np.column_stack([rng.uniform(-500 * NM, 500 * NM, 50), rng.uniform(-500 * NM, 500 * NM, 50),
+                                      np.zeros(50)])])
+    assert nrel(dio.calc_field_at_batch(pts), o.field_at(pts)) <= TOL32
+    eng.close()
