@@ -102,3 +102,31 @@ def test_profile_step_reports_phases(rg):
                                "force_ms", "velocity_ms", "compact_ms"))
     assert parts <= p["total_ms"] * 1.01 + 1e-3
     eng.close()
+
+
+def test_served_two_time_step_diode_equals_alone(rg):
+    """A two-time-step diode (atom_time_interval = 3, its force pass on the
+    k_force_tts plan) served among standard diodes ends bit-identical to the
+    same diode simulated alone, and so do its neighbours."""
+    reqs = make_requests(n=4, seed=9)
+    reqs[1][2]["atom_time_interval"] = 3
+    eng = rg.Engine(precision=1, max_diodes=4, particle_capacity=4 * 1024, chain_capacity=4 * 256,
+                    quad_capacity=4 * 1024)
+    ids = [eng.submit(steps, pos=pos, **kw) for steps, pos, kw in reqs]
+    finals = {}
+    for _ in range(100):
+        eng.serve(1)
+        for rid in ids:
+            s = eng.poll(rid)
+            if s["state"] == rg.REQ_DONE and rid not in finals:
+                finals[rid] = s
+        if len(finals) == len(ids):
+            break
+    assert len(finals) == len(ids)
+    for rid, (steps, pos, kw) in zip(ids, reqs):
+        c, _ = alone(rg, 1, steps, pos, kw)
+        got = finals[rid]["counters"]
+        for key in ("n", "emitted_total", "absorbed_top_total", "absorbed_bot_total", "electron_steps"):
+            assert got[key] == c[key], (rid, key)
+        assert got["ramo_current"] == c["ramo_current"]
+    eng.close()
