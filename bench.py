@@ -547,6 +547,58 @@ def case_micro(args):
             print(json.dumps(out), flush=True)
 
 
+def case_serve_latency(args):
+    """Per-simulation latency of the serving loop, measured: the serving
+    request stream (Poisson 20/s, the same diode distributions) with every
+    request's step count divided by --step-scale so that simulations finish
+    inside the window, served in real time for --window seconds.  Reports,
+    over the requests that completed, the latency from submission to the
+    last step (p50 / p99), its queueing part (submission to admission) and
+    its service part, with the electron-steps/s of the window.  The full step
+    counts (500-20000) make one simulation last minutes, so the headline run
+    projects that latency instead."""
+    import rumdeed_gb300 as rg
+    rg.build()
+    S = args.slots
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=S, particle_capacity=S * 32768 + 4096,
+                    chain_capacity=S * 32768 + 4096, quad_capacity=S * 4096 + 4096)
+    stream = RequestStream(SEED)
+    pending = stream.next()
+    ids = []
+    t0 = time.perf_counter()
+    e_steps, dev_ms = 0, 0.0
+    while time.perf_counter() - t0 < args.window:
+        now = time.perf_counter() - t0
+        while pending is not None and pending["arrival"] <= now:
+            steps = max(1, int(round(pending["steps"] / args.step_scale)))
+            ids.append(eng.submit(steps, pos=prefill(pending), **diode_kwargs(pending)))
+            pending = stream.next()
+        st = eng.serve(1)
+        e_steps += st["electron_steps"]
+        dev_ms += st["device_ms"]
+    wall = time.perf_counter() - t0
+    lat, queue, service = [], [], []
+    states = {}
+    for rid in ids:
+        s = eng.poll(rid)
+        states[s["state"]] = states.get(s["state"], 0) + 1
+        if s["state"] == rg.REQ_DONE:
+            lat.append(s["done_s"] - s["submit_s"])
+            queue.append(s["admit_s"] - s["submit_s"])
+            service.append(s["done_s"] - s["admit_s"])
+    eng.close()
+    pct = lambda v, q: float(np.percentile(v, q)) if v else None
+    print(json.dumps({"case": "serve-latency", "window_s": wall, "step_scale": args.step_scale,
+                      "submitted": len(ids), "completed": len(lat),
+                      "running_or_queued": len(ids) - len(lat),
+                      "latency_s_p50": pct(lat, 50), "latency_s_p99": pct(lat, 99),
+                      "queueing_s_p50": pct(queue, 50), "queueing_s_p99": pct(queue, 99),
+                      "service_s_p50": pct(service, 50), "service_s_p99": pct(service, 99),
+                      "electron_steps_per_s_wall": e_steps / wall,
+                      "electron_steps_per_s_device": e_steps / (dev_ms / 1e3) if dev_ms else None}),
+          flush=True)
+
+
 def case_burst(args):
     """The first S requests of the serving stream admitted at once (no arrival
     pacing), then W + K serving iterations: the serving workload with a fixed
@@ -696,12 +748,16 @@ def main():
     ap.add_argument("--slots", type=int, default=128)
     ap.add_argument("--plain-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=1.0e10)
-    ap.add_argument("--case", default="serve", choices=["serve", "micro", "burst", "mh-small", "plain", "tips"],
+    ap.add_argument("--case", default="serve",
+                    choices=["serve", "micro", "burst", "mh-small", "plain", "tips", "serve-latency"],
                     help="serve: the headline serving benchmark; the others are secondary workloads")
     ap.add_argument("--sizes", default="4096,65536,262144", help="micro: electron counts")
     ap.add_argument("--nics", default="0,7,8", help="micro: N_ic_max values (K = 8 mirror terms read "
                     "as N_ic_max = 7, the series through n = 7, or as N_ic_max = 8)")
     ap.add_argument("--tip-electrons", type=int, default=100000, help="tips: electrons per tip")
+    ap.add_argument("--step-scale", type=float, default=100.0,
+                    help="serve-latency: every request's step count is divided by this")
+    ap.add_argument("--window", type=float, default=60.0, help="serve-latency: seconds of real-time serving")
     ap.add_argument("--fp64-budget", type=float, default=2.0e11,
                     help="micro: largest N(N-1) x terms run in FP64 for the error check")
     args = ap.parse_args()
@@ -716,6 +772,7 @@ def main():
     if args.case != "serve":
         if rank == 0:
             {"micro": case_micro, "burst": case_burst, "mh-small": case_mh_small, "plain": case_plain,
+             "serve-latency": case_serve_latency,
              "tips": case_tips}[args.case](args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
