@@ -405,7 +405,8 @@ def run_ours(args, rank, world):
                     "queueing_delay_s_p50": float(np.percentile(qd, 50)) if qd else None,
                     "queueing_delay_s_p99": float(np.percentile(qd, 99)) if qd else None,
                     "simulation_latency": "no simulation completes inside the window: "
-                                          "projected = steps x step time (>= 500 steps)"},
+                                          "projected = steps x step time (>= 500 steps); measured "
+                                          "with step counts / 100 by --case serve-latency"},
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": e2e_h2d / max(args.steps, 1),
                 "d2h_bytes_per_step": e2e_d2h / max(args.steps, 1),
                 "window": "the %d resident requests submitted again from host memory at once, "
