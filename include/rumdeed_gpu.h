@@ -125,6 +125,12 @@ typedef struct {
                               (field.dt, src/mod_field_emission_v2.F90:644-651) */
   double df_avg;           /* sum of the candidates' escape probabilities / N_sup (:354,385) */
   double ramo_current_ion; /* ramo_current(species_ion) of the last step (A) */
+  double avg_part_vel[3], avg_elec_vel[3], avg_ion_vel[3];   /* Average_Velocities of the last
+                              step (src/mod_verlet.F90:428-447): velocity sums of the particles the
+                              step moved over the counts below (m/s) */
+  double avg_mob;          /* |avg_elec_vel| / (-E_z) (m^2/(V s)) */
+  int n_part_vel, n_elec_vel, n_ion_vel;   /* nrPart, nrElec, nrIon at the velocity update, before
+                              removal (the counts Write_Ramo_Current writes) */
 } rd_counters;
 
 const char* rd_last_error(void);

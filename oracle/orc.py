@@ -67,6 +67,8 @@ class Diode(C.Structure):
         ("emitter_type", C.c_int), ("ring_rmin", C.c_double), ("ring_thick", C.c_double),
         ("F_avg_z", C.c_double), ("df_avg", C.c_double),
         ("atom_time_interval", C.c_int), ("ramo_current_ion", C.c_double),
+        ("avg_part_vel", C.c_double * 3), ("avg_ion_vel", C.c_double * 3), ("avg_mob", C.c_double),
+        ("n_part_vel", C.c_int), ("n_elec_vel", C.c_int), ("n_ion_vel", C.c_int),
     ]
 
 

@@ -774,10 +774,30 @@ void orc_accel_tts(orc_diode* s, int step, int comp) {
   free(a);
 }
 
+/* Average_Velocities :428-447: the velocity sums of the particles the update
+ * moved, over nrPart / nrElec / nrIon before removal; the mobility from the
+ * electrons' mean velocity. */
+static void average_velocities(orc_diode* s, const double* se, const double* si) {
+  int ne = 0, ni = 0;
+  for (int i = 0; i < s->n; ++i) {
+    if (s->species[i] == ORC_ELEC) ne++;
+    else if (s->species[i] == ORC_ION) ni++;
+  }
+  for (int k = 0; k < 3; ++k) {
+    s->avg_part_vel[k] = s->n ? (se[k] + si[k]) / s->n : 0.0;
+    s->avg_elec_vel[k] = ne ? se[k] / ne : 0.0;
+    s->avg_ion_vel[k] = ni ? si[k] / ni : 0.0;
+  }
+  double a = sqrt(s->avg_elec_vel[0] * s->avg_elec_vel[0] + s->avg_elec_vel[1] * s->avg_elec_vel[1] +
+                  s->avg_elec_vel[2] * s->avg_elec_vel[2]);
+  s->avg_mob = s->E_z != 0.0 ? a / (-1.0 * s->E_z) : 0.0;
+  s->n_part_vel = s->n; s->n_elec_vel = ne; s->n_ion_vel = ni;
+}
+
 /* Beeman velocity and Ramo current of one particle (the loop bodies of
  * Update_ElecIon_Velocity :449-509 and Update_Species_Velocity :511-590). */
 static void velocity_one(orc_diode* s, int i, double nr, nsum* ramo, nsum* ramo_ion, double* sum,
-                         int* n_elec) {
+                         double* sum_ion) {
   double dt = s->time_step;
   for (int k = 0; k < 3; ++k) {
     int q = 3 * i + k;
@@ -790,33 +810,31 @@ static void velocity_one(orc_diode* s, int i, double nr, nsum* ramo, nsum* ramo_
   if (s->species[i] == ORC_ELEC) {
     nadd(ramo, s->charge[i] * ezv);
     for (int k = 0; k < 3; ++k) sum[k] += s->vel[3 * i + k];
-    (*n_elec)++;
   } else if (s->species[i] == ORC_ION) {
     nadd(ramo_ion, s->charge[i] * ezv);
+    for (int k = 0; k < 3; ++k) sum_ion[k] += s->vel[3 * i + k];
   }
 }
 
 void orc_update_velocity_tts(orc_diode* s, int step) {
   nsum ramo = {0, 0}, ramo_ion = {0, 0};
-  double sum[3] = {0, 0, 0};
-  int n_elec = 0;
+  double sum[3] = {0, 0, 0}, sum_ion[3] = {0, 0, 0};
   for (int i = 0; i < s->n; ++i)
-    if (s->species[i] == ORC_ELEC) velocity_one(s, i, 1.0, &ramo, &ramo_ion, sum, &n_elec);
+    if (s->species[i] == ORC_ELEC) velocity_one(s, i, 1.0, &ramo, &ramo_ion, sum, sum_ion);
   if (step % s->atom_time_interval == 0)
     for (int i = 0; i < s->n; ++i)
       if (s->species[i] == ORC_ION)
-        velocity_one(s, i, (double)s->atom_time_interval, &ramo, &ramo_ion, sum, &n_elec);
+        velocity_one(s, i, (double)s->atom_time_interval, &ramo, &ramo_ion, sum, sum_ion);
   s->ramo_current = nval(&ramo);
   s->ramo_current_ion = nval(&ramo_ion);
-  for (int k = 0; k < 3; ++k) s->avg_elec_vel[k] = n_elec ? sum[k] / n_elec : 0.0;
+  average_velocities(s, sum, sum_ion);
 }
 
 /* Update_ElecIon_Velocity :449-509 + Average_Velocities :428-447 */
 void orc_update_velocity(orc_diode* s) {
   double dt = s->time_step;
   nsum ramo = {0, 0}, ramo_ion = {0, 0};
-  double sum[3] = {0, 0, 0};
-  int n_elec = 0;
+  double sum[3] = {0, 0, 0}, sum_ion[3] = {0, 0, 0};
   for (int i = 0; i < s->n; ++i) {
     if (s->species[i] == ORC_ATOM) continue;
     for (int k = 0; k < 3; ++k) {
@@ -830,14 +848,14 @@ void orc_update_velocity(orc_diode* s) {
     if (s->species[i] == ORC_ELEC) {
       nadd(&ramo, s->charge[i] * ezv);
       for (int k = 0; k < 3; ++k) sum[k] += s->vel[3 * i + k];
-      n_elec++;
     } else if (s->species[i] == ORC_ION) {
       nadd(&ramo_ion, s->charge[i] * ezv);
+      for (int k = 0; k < 3; ++k) sum_ion[k] += s->vel[3 * i + k];
     }
   }
   s->ramo_current = nval(&ramo);
   s->ramo_current_ion = nval(&ramo_ion);
-  for (int k = 0; k < 3; ++k) s->avg_elec_vel[k] = n_elec ? sum[k] / n_elec : 0.0;
+  average_velocities(s, sum, sum_ion);
 }
 
 /* Velocity_Verlet :123-162 with the gather acceleration (the GPU semantics),

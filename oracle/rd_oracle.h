@@ -105,6 +105,10 @@ typedef struct {
   /* two-time-step integrator (atom_time_interval, src/main.F90:391-395): 0 off */
   int atom_time_interval;
   double ramo_current_ion;  /* ramo_current(species_ion) of the last step */
+  /* Average_Velocities (src/mod_verlet.F90:428-447) of the last velocity update and the
+   * particle counts it divides by (before removal); avg_elec_vel is above */
+  double avg_part_vel[3], avg_ion_vel[3], avg_mob;
+  int n_part_vel, n_elec_vel, n_ion_vel;
 } orc_diode;
 
 /* Create / destroy.  Geometry parameters follow Init_Field_Emission_v2

@@ -80,11 +80,15 @@ class Counters(C.Structure):
                 ("electron_steps", C.c_longlong), ("steps_done", C.c_longlong),
                 ("ramo_current", C.c_double), ("N_sup", C.c_double), ("MH_std", C.c_double),
                 ("a_rate", C.c_double), ("residual", C.c_double), ("F_avg", C.c_double * 3),
-                ("df_avg", C.c_double), ("ramo_current_ion", C.c_double)]
+                ("df_avg", C.c_double), ("ramo_current_ion", C.c_double),
+                ("avg_part_vel", C.c_double * 3), ("avg_elec_vel", C.c_double * 3),
+                ("avg_ion_vel", C.c_double * 3), ("avg_mob", C.c_double),
+                ("n_part_vel", C.c_int), ("n_elec_vel", C.c_int), ("n_ion_vel", C.c_int)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
-        d["F_avg"] = tuple(self.F_avg)
+        for k in ("F_avg", "avg_part_vel", "avg_elec_vel", "avg_ion_vel"):
+            d[k] = tuple(getattr(self, k))
         return d
 
 

@@ -1284,6 +1284,15 @@ static void fill_counters(const DiodeDyn& y, rd_counters* o) {
   o->F_avg[0] = 0.0; o->F_avg[1] = 0.0; o->F_avg[2] = y.F_avg_z;   // x, y cancel at the cathode
   o->df_avg = y.df_avg;
   o->ramo_current_ion = y.ramo_ion;
+  for (int c = 0; c < 3; ++c) {
+    o->avg_part_vel[c] = y.avg_part_vel[c];
+    o->avg_elec_vel[c] = y.avg_elec_vel[c];
+    o->avg_ion_vel[c] = y.avg_ion_vel[c];
+  }
+  o->avg_mob = y.avg_mob;
+  o->n_part_vel = y.n_vel;
+  o->n_elec_vel = y.n_elec_vel;
+  o->n_ion_vel = y.n_ion_vel;
 }
 
 int rd_counters_get(rd_engine* e, int d, rd_counters* o) {

@@ -106,7 +106,8 @@ struct DiodeDyn {
   double ramo_current, ramo_ion;   // ramo_current(species_elec), ramo_current(species_ion)
   double MH_std, a_rate, residual, N_sup;
   double F_avg_z, df_avg;   // field.dt quantities of the last emission
-  double avg_vel[3];
+  double avg_part_vel[3], avg_elec_vel[3], avg_ion_vel[3], avg_mob;   // Average_Velocities
+  int n_vel, n_elec_vel, n_ion_vel;   // particle counts at the velocity update (before removal)
 };
 
 // Particle pool (device pointers).

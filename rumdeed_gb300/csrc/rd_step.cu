@@ -299,36 +299,64 @@ k_velocity(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, P
   }
 }
 
-// Ramo current per species and electron-step count per diode (fixed-order
-// reduction).
+// Ramo current per species, the mean velocities of Average_Velocities
+// (src/mod_verlet.F90:428-447: sums over the particles the velocity update
+// moved, divided by the particle counts before removal) and the
+// electron-step count, per diode (fixed-order reduction).
 __global__ void __launch_bounds__(256)
 k_ramo(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, const double* __restrict__ ramo,
-       const int* __restrict__ species) {
-  __shared__ double red[256], red_ion[256];
+       Pool pool, const int* __restrict__ step_ptr) {
+  constexpr int NV = 10;   // ramo e, ramo ion, v elec (3), v ion (3), electrons, ions
+  __shared__ double red[NV][256];
   const int d = blockIdx.x;
   const DiodeParams& p = P[d];
   if (!p.active) return;
-  const int n = Dy[d].n;
-  double s = 0.0, si = 0.0;
+  DiodeDyn& y = Dy[d];
+  const int n = y.n;
+  const int step = *step_ptr - y.step_offset;
+  const bool ion_step = p.tts <= 1 || step % p.tts == 0;   // ions moved in this step (k_velocity)
+  double v[NV];
+  for (int k = 0; k < NV; ++k) v[k] = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double r = ramo[p.off + i];
-    if (species[p.off + i] == 2) si += r; else s += r;
-  }
-  red[threadIdx.x] = s;
-  red_ion[threadIdx.x] = si;
-  __syncthreads();
-  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
-    if (threadIdx.x < k) {
-      red[threadIdx.x] += red[threadIdx.x + k];
-      red_ion[threadIdx.x] += red_ion[threadIdx.x + k];
+    const int gi = p.off + i, sp = pool.species[gi];
+    const double r = ramo[gi];
+    if (sp == 2) {
+      v[1] += r;
+      v[9] += 1.0;
+      if (ion_step) { v[5] += pool.vx[gi]; v[6] += pool.vy[gi]; v[7] += pool.vz[gi]; }
+    } else {
+      v[0] += r;
+      if (sp == 1) {
+        v[8] += 1.0;
+        v[2] += pool.vx[gi]; v[3] += pool.vy[gi]; v[4] += pool.vz[gi];
+      }
     }
+  }
+  for (int k = 0; k < NV; ++k) red[k][threadIdx.x] = v[k];
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h)
+      for (int k = 0; k < NV; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    Dy[d].ramo_current = red[0];
-    Dy[d].ramo_ion = red_ion[0];
-    Dy[d].electron_steps += n;
-    Dy[d].steps_done += 1;
+    const double ne = red[8][0], ni = red[9][0];
+    y.ramo_current = red[0][0];
+    y.ramo_ion = red[1][0];
+    for (int c = 0; c < 3; ++c) {
+      const double se = red[2 + c][0], si = red[5 + c][0];
+      y.avg_part_vel[c] = n > 0 ? (se + si) / n : 0.0;
+      y.avg_elec_vel[c] = ne > 0.0 ? se / ne : 0.0;
+      y.avg_ion_vel[c] = ni > 0.0 ? si / ni : 0.0;
+    }
+    const double ae = sqrt((y.avg_elec_vel[0] * y.avg_elec_vel[0] + y.avg_elec_vel[1] * y.avg_elec_vel[1]) +
+                           y.avg_elec_vel[2] * y.avg_elec_vel[2]);
+    y.avg_mob = p.E_z != 0.0 ? ae / (-1.0 * p.E_z) : 0.0;
+    y.n_vel = n;
+    y.n_elec_vel = (int)ne;
+    y.n_ion_vel = (int)ni;
+    y.electron_steps += n;
+    y.steps_done += 1;
   }
 }
 
@@ -468,7 +496,7 @@ cudaError_t rd_launch_velocity(int grid, int nslots, cudaStream_t st, const Diod
                                DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
                                const PlanHeader* ph, double* ramo, const int* step_ptr) {
   k_velocity<<<rd_grid(k_velocity, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, ramo, step_ptr);
-  k_ramo<<<nslots, 256, 0, st>>>(P, Dy, ramo, pool.species);
+  k_ramo<<<nslots, 256, 0, st>>>(P, Dy, ramo, pool, step_ptr);
   return cudaGetLastError();
 }
 cudaError_t rd_launch_compact(int grid, int nslots, cudaStream_t st, const DiodeParams* P,

@@ -357,7 +357,6 @@ int main(int argc, char** argv) {
     return 2;
   }
   std::printf("RUMDEED: Starting main loop\n Doing %d time steps of size %12.4E ps\n", steps, dt / time_scale);
-  const double E_z = -V_s / (mode == 10 ? d : dc.gap);
   std::vector<double> vel;
   std::vector<rd_event> events((size_t)ec.event_capacity);
   long long lost_total = 0;
@@ -456,25 +455,17 @@ int main(int argc, char** argv) {
     absorbed(f_abs, c.absorbed_top_step + c.absorbed_bot_step, false);
     absorbed(f_top, c.absorbed_top_step, true);
     absorbed(f_bot, c.absorbed_bot_step, false);
-    // ramo_current.dt: time, step, current, V, particles, electrons, ions, mobility, mean speeds,
-    // current per species (the speeds are those of the electrons left after the step)
-    vel.resize(3 * (size_t)std::max(c.n, 1));
-    int n = 0;
-    check(rd_get_particles(e, diode, c.n, nullptr, vel.data(), nullptr, nullptr, nullptr, nullptr, &n),
-          "rd_get_particles");
-    double av[3] = {0, 0, 0};
-    for (int i = 0; i < n; ++i) for (int k = 0; k < 3; ++k) av[k] += vel[3 * i + k];
-    if (n > 0) for (double& a : av) a /= n;
-    const double speed = std::sqrt(av[0] * av[0] + av[1] * av[1] + av[2] * av[2]);
-    const double mob = E_z != 0.0 ? speed / (-E_z) : 0.0;
-    // (Write_Ramo_Current, src/mod_pair.F90:812-835: total = sum over species, then one column
-    // per species; this driver adds electrons only, so the ion and atom columns stay 0 unless
-    // the library holds ions)
+    // ramo_current.dt (Write_Ramo_Current, src/mod_pair.F90:812-835): time, step, total current
+    // (sum over species), V, nrPart, nrElec, nrIon and the mean speeds and mobility of
+    // Average_Velocities, all as the velocity update left them (before removal), then the
+    // current per species (electron, ion, atom)
+    auto norm3 = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
     const double ramo_total = c.ramo_current + c.ramo_current_ion;
     std::string r = fmt_ES(cur_time, 12, 4) + "  " + fmt_I(step, 8) + "  " + fmt_ES(ramo_total, 12, 4) +
-                    "  " + fmt_ES(V_s, 12, 4) + "  " + fmt_I(n, 6) + "  " + fmt_I(n, 6) + "  " + fmt_I(0, 6) +
-                    "  " + fmt_ES(mob, 12, 4) + "  " + fmt_ES(speed, 12, 4) + "  " + fmt_ES(speed, 12, 4) +
-                    "  " + fmt_ES(0.0, 12, 4) + "  " + fmt_ES(c.ramo_current, 12, 4) + "  " +
+                    "  " + fmt_ES(V_s, 12, 4) + "  " + fmt_I(c.n_part_vel, 6) + "  " + fmt_I(c.n_elec_vel, 6) +
+                    "  " + fmt_I(c.n_ion_vel, 6) + "  " + fmt_ES(c.avg_mob, 12, 4) + "  " +
+                    fmt_ES(norm3(c.avg_part_vel), 12, 4) + "  " + fmt_ES(norm3(c.avg_elec_vel), 12, 4) + "  " +
+                    fmt_ES(norm3(c.avg_ion_vel), 12, 4) + "  " + fmt_ES(c.ramo_current, 12, 4) + "  " +
                     fmt_ES(c.ramo_current_ion, 12, 4) + "  " + fmt_ES(0.0, 12, 4);
     std::fprintf(f_ramo, "%s\n", r.c_str());
     if (b_ramo_sec) {
@@ -483,6 +474,8 @@ int main(int argc, char** argv) {
       // the velocities of the step; the particles removed in the step carry q = 0 there
       // (Mark_Particles_Remove), so the survivors give the whole sum.
       std::fill(ramo_sec.begin(), ramo_sec.end(), 0.0);
+      const int n = c.n;
+      vel.resize(3 * (size_t)std::max(n, 1));
       qbuf.resize((size_t)std::max(n, 1));
       secbuf.resize((size_t)std::max(n, 1));
       int got = 0;

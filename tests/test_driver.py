@@ -147,6 +147,13 @@ def test_driver_run_matches_python_binding(driver, tmp_path, rg):
     p1 = np.fromfile(out / "planes-1.bin", dtype=rec_top)
     p2 = np.fromfile(out / "planes-2.bin", dtype=rec_top)
     assert len(p1) >= len(p2) and np.all(p1["vel"][:, 2] > 0) if len(p1) else True
+    # ramo_current.dt: nrPart / nrElec / nrIon at the velocity update (before removal) equal the
+    # electrons in flight that emitted.dt records after the emission of the step
+    ramo = np.loadtxt(out / "ramo_current.dt")
+    assert ramo.shape == (12, 14)
+    np.testing.assert_array_equal(ramo[:, 4], emitted[:, 3])
+    np.testing.assert_array_equal(ramo[:, 5], emitted[:, 3])
+    assert np.all(ramo[:, 6] == 0) and np.all(ramo[:, 7] >= 0)
     # volt.dt: "(ES12.4, tr2, i8, tr2, ES18.8)" with 4 items: time, step, V_d, then V_rf alone on
     # the next record by format reversion (Set_Voltage, src/mod_verlet.F90:2050-2057)
     vl = (out / "volt.dt").read_text().splitlines()

@@ -236,7 +236,16 @@ def test_full_steps_fp64_trajectory(rg, orc):
     c = dio.counters()
     assert c["emitted_total"] == o.s.emitted_total
     assert c["ramo_current"] == pytest.approx(o.s.ramo_current, rel=1e-9)
+    _check_average_velocities(c, o)
     eng.close()
+
+
+def _check_average_velocities(c, o):
+    """Average_Velocities (src/mod_verlet.F90:428-447) of the last step against the oracle."""
+    assert (c["n_part_vel"], c["n_elec_vel"], c["n_ion_vel"]) == (o.s.n_part_vel, o.s.n_elec_vel, o.s.n_ion_vel)
+    for key in ("avg_part_vel", "avg_elec_vel", "avg_ion_vel"):
+        np.testing.assert_allclose(c[key], list(getattr(o.s, key)), rtol=1e-8, atol=1e-6, err_msg=key)
+    assert c["avg_mob"] == pytest.approx(o.s.avg_mob, rel=1e-8, abs=1e-18)
 
 
 def test_emission_fp32c_statistics(rg, orc):
@@ -630,6 +639,8 @@ def test_two_time_step_full_steps_with_emission_fp64(rg, orc):
     assert np.max(np.abs(p["pos"] - o.arr("pos"))) < 1e-9 * NM
     assert nrel(p["vel"] + 1e-3, o.arr("vel") + 1e-3) < 1e-8
     assert c["emitted_total"] == o.s.emitted_total > 0
+    _check_average_velocities(c, o)   # step 5: the ions did not move, their mean is 0
+    assert c["n_ion_vel"] > 0 and c["avg_ion_vel"] == (0.0, 0.0, 0.0)
     eng.close()
 
 
