@@ -13,8 +13,9 @@
 // out/density_emit_elec.bin (src/mod_pair.F90:89-123),
 // out/density_absorb_{top,bot}.bin (:241-257) and out/planes-<k>.bin
 // (Check_Planes, src/mod_verlet.F90:343-367) from the engine's event log,
-// out/field.dt (src/mod_field_emission_v2.F90:389-390) and out/volt.dt
-// (Set_Voltage, src/mod_verlet.F90:2050-2057).
+// out/field.dt (src/mod_field_emission_v2.F90:389-390), out/volt.dt
+// (Set_Voltage, src/mod_verlet.F90:2050-2057) and, once, out/init.bin and
+// out/init.dt (Write_Initial_Variables, src/main.F90:852-932).
 //
 // Supported decks: EMISSION_MODE = 10 (planar field emission, one emitter,
 // EMITTERS_TYPE 1, 2 or 4) and EMISSION_MODE = 3 (hyperboloid tip);
@@ -310,6 +311,53 @@ int main(int argc, char** argv) {
   check(rd_diode_add(e, &dc, &diode), "rd_diode_add");
 
   mkdir("out", 0755);
+  {
+    // Write_Initial_Variables (src/main.F90:852-932): out/init.bin, 7 float64 then 4 int32, which
+    // the reference's readers use for the scales and the ramo_current.bin dimensions, and the
+    // text summary out/init.dt
+    const double scales[7] = {1.0, 1.0, 1.0, length_scale, time_scale, length_scale / time_scale, 1.0};
+    const int dims[4] = {dc.capacity, 1, 96 * 96, 1000};   // MAX_PARTICLES, _EMITTERS, _SECTIONS, _LIFE_TIME
+    FILE* fb = std::fopen("out/init.bin", "wb");
+    FILE* ft = std::fopen("out/init.dt", "w");
+    if (!fb || !ft) { std::fprintf(stderr, "rd_main: cannot write under out/\n"); return 2; }
+    std::fwrite(scales, sizeof(double), 7, fb);
+    std::fwrite(dims, sizeof(int), 4, fb);
+    std::fclose(fb);
+    auto rel = [&](const char* name, double v, const char* what) {
+      std::fprintf(ft, "%s  %s  %s\n", name, fmt_ES(v, 16, 6).c_str(), what);
+    };
+    auto integer = [&](const char* name, long long v, const char* what) {
+      std::fprintf(ft, "%s        %s      %s\n", name, fmt_I(v, 8).c_str(), what);
+    };
+    const char* rule = " ---------------------------------------------------------";
+    std::fprintf(ft, " Vacuum Electronics Molecular Dynamics\n Values used for constans and variables\n\n");
+    std::fprintf(ft, "%s\nVacuum\n", rule);
+    rel("epsilon_r  = ", 1.0, "Relative permittivity");
+    rel("m_eeff     = ", 1.0, "Effective mass for electrons");
+    rel("m_ieff     = ", 1.0, "Effective mass for ions");
+    std::fprintf(ft, "%s\n\n\n%s\n", rule, rule);
+    rel("length_scale    = ", length_scale, "The length scale used for output (m)");
+    rel("time_scale      = ", time_scale, "The time scale used for output (s)");
+    rel("vel_scale       = ", length_scale / time_scale, "The velocity scale used for output (m/s)");
+    rel("cur_scale       = ", 1.0, "The current scale used for output (A)");
+    rel("time_step       = ", dt, "Size of the time_step used in the Verlet integration (s)");
+    integer("steps           = ", steps, "Number of time steps in the Verlet integration");
+    std::fprintf(ft, "%s\n\n\n%s\n", rule, rule);
+    integer("MAX_PARTICLES       = ", dc.capacity, "Maximum number of electrons in the system");
+    std::fprintf(ft, "my_seed             =         %12llu\n", dc.seed);
+    std::fprintf(ft, "%s\n\n\n%s\n", rule, rule);
+    rel("V_s           = ", V_s, "The Voltage from the source");
+    rel("box_dim_x     = ", 0.0, "System x-length");
+    rel("box_dim_y     = ", 0.0, "System y-length");
+    rel("box_dim_z     = ", mode == 10 ? d : dc.gap, "System z-length");
+    rel("d             = ", mode == 10 ? d : dc.gap, "Gap spacing in the system");
+    rel("E_z           = ", -V_s / (mode == 10 ? d : dc.gap), "Y-component of the electric field in the system");
+    std::fprintf(ft, "%s\n%s\n", rule, rule);
+    integer("NrEmit        = ", 1, "Number of emitters");
+    integer("EMISSION_MODE = ", mode, "The emission mechanism");
+    std::fprintf(ft, "%s\n GIT VERSION\n", rule);
+    std::fclose(ft);
+  }
   FILE* f_emit = std::fopen("out/emitted.dt", "w");
   FILE* f_abs = std::fopen("out/absorbed.dt", "w");
   FILE* f_top = std::fopen("out/absorbed_top.dt", "w");

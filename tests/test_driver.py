@@ -203,6 +203,15 @@ def test_optional_position_and_section_current_files(driver, tmp_path, rg):
         assert np.all(parts["emit"] == 1) and np.all(np.diff(parts["id"]) > 0)
         assert np.all(parts["sec"] >= 1) and np.all(parts["sec"] <= 4)   # the 2 x 2 work grid
     assert off == len(raw)
+    # init.bin (Write_Initial_Variables): 7 float64 then 4 int32; the reference's readers take the
+    # ramo_current.bin dimensions from it
+    init = np.fromfile(opt / "out" / "init.bin", dtype=np.dtype(
+        [("scales", "<f8", 7), ("MAX_PARTICLES", "<i4"), ("MAX_EMITTERS", "<i4"), ("MAX_SECTIONS", "<i4"),
+         ("MAX_LIFE_TIME", "<i4")]))
+    assert len(init) == 1 and (opt / "out" / "init.bin").stat().st_size == 72
+    np.testing.assert_allclose(init["scales"][0], [1, 1, 1, 1e-9, 1e-12, 1e3, 1])
+    assert (init["MAX_PARTICLES"][0], init["MAX_EMITTERS"][0], init["MAX_SECTIONS"][0]) == (3000, 1, 96 * 96)
+    assert (opt / "out" / "ramo_current.bin").stat().st_size == 96 * 96 * 1 * 12 * 8
     rs = np.fromfile(opt / "out" / "ramo_current.bin", dtype="<f8").reshape(12, 96 * 96)
     ramo = np.loadtxt(opt / "out" / "ramo_current.dt")
     np.testing.assert_allclose(rs.sum(axis=1), ramo[:, 11], rtol=1e-4, atol=1e-30)   # ES12.4 text
