@@ -370,6 +370,14 @@ int main(int argc, char** argv) {
   FILE* b_abs_bot = std::fopen("out/density_absorb_bot.bin", "wb");
   FILE* f_field = std::fopen("out/field.dt", "w");
   FILE* f_volt = std::fopen("out/volt.dt", "w");
+  // per-species emission files (src/main.F90:681-700): ions and atoms only appear here when the
+  // library holds them; the collision files stay empty (collisions are outside this path)
+  FILE* b_emit_ion = std::fopen("out/density_emit_ion.bin", "wb");
+  FILE* b_emit_atom = std::fopen("out/density_emit_atom.bin", "wb");
+  for (const char* empty : {"out/density_ion.bin", "out/density_absorb_recom.bin", "out/absorbed_recom.dt"}) {
+    FILE* f = std::fopen(empty, "wb");
+    if (f) std::fclose(f);
+  }
   // optional files of the namelist's WRITE_POSITION_FILE / WRITE_RAMO_SEC (default off)
   const bool write_pos = in.count("WRITE_POSITION_FILE") && to_logical(in.at("WRITE_POSITION_FILE")[0]);
   const bool write_ramo_sec = in.count("WRITE_RAMO_SEC") && to_logical(in.at("WRITE_RAMO_SEC")[0]);
@@ -400,7 +408,7 @@ int main(int argc, char** argv) {
       if (!b_planes[k]) { std::fprintf(stderr, "rd_main: cannot write %s\n", name); return 2; }
     }
   if (!f_emit || !f_abs || !f_top || !f_bot || !f_ramo || !b_emit || !b_emit_elec || !b_abs_top || !b_abs_bot ||
-      !f_field || !f_volt) {
+      !f_field || !f_volt || !b_emit_ion || !b_emit_atom) {
     std::fprintf(stderr, "rd_main: cannot write under out/\n");
     return 2;
   }
@@ -460,8 +468,9 @@ int main(int argc, char** argv) {
         std::fwrite(p3, sizeof(double), 3, b_emit);
         std::fwrite(i4, sizeof(int), 4, b_emit);
         const int i2[2] = {emitter, r.id};
-        std::fwrite(p3, sizeof(double), 3, b_emit_elec);
-        std::fwrite(i2, sizeof(int), 2, b_emit_elec);
+        FILE* bs = r.species == RD_SPECIES_ION ? b_emit_ion : r.species == RD_SPECIES_ATOM ? b_emit_atom : b_emit_elec;
+        std::fwrite(p3, sizeof(double), 3, bs);
+        std::fwrite(i2, sizeof(int), 2, bs);
       } else {
         // absorb_top and planes: x, y, v, emitter, section, id; absorb_bot: x, y, emitter, section, id
         const int i3[3] = {emitter, r.section, r.id};
@@ -542,7 +551,8 @@ int main(int argc, char** argv) {
       ++progress;
     }
   }
-  for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo, b_emit, b_emit_elec, b_abs_top, b_abs_bot, f_field, f_volt})
+  for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo, b_emit, b_emit_elec, b_abs_top, b_abs_bot, f_field, f_volt,
+                  b_emit_ion, b_emit_atom})
     std::fclose(f);
   for (FILE* f : b_planes) if (f) std::fclose(f);
   if (b_pos) std::fclose(b_pos);
