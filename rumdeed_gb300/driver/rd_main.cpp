@@ -374,10 +374,20 @@ int main(int argc, char** argv) {
   // library holds them; the collision files stay empty (collisions are outside this path)
   FILE* b_emit_ion = std::fopen("out/density_emit_ion.bin", "wb");
   FILE* b_emit_atom = std::fopen("out/density_emit_atom.bin", "wb");
-  for (const char* empty : {"out/density_ion.bin", "out/density_absorb_recom.bin", "out/absorbed_recom.dt"}) {
+  // the files the reference opens on every run but writes only in modes outside this path
+  // (collisions, Laplace solvers, photo emission, MH tracing) are created empty, as there
+  for (const char* empty : {"out/density_ion.bin", "out/density_absorb_recom.bin", "out/absorbed_recom.dt",
+                            "out/ionization_data.bin", "out/recombination_data.bin", "out/collisions.dt",
+                            "out/laplace_average_field.dt", "out/laplace_grid.dt", "out/gauss.dt", "out/mh.bin"}) {
     FILE* f = std::fopen(empty, "wb");
     if (f) std::fclose(f);
   }
+  // integration.dt (Do_Surface_Integration_FE, src/mod_field_emission_v2.F90:653-655): the
+  // reference logs Cuba's regions, evaluations, fail flag, integral, error and probability;
+  // here the supply rule is a fixed composite Gauss-Legendre rule, so the line gives its panels,
+  // nodes, 0 and N_sup (no error estimate: 0)
+  FILE* f_integ = std::fopen("out/integration.dt", "w");
+  const int q_panels = dc.quad_panels > 0 ? dc.quad_panels : 16, q_order = dc.quad_order > 0 ? dc.quad_order : 4;
   // optional files of the namelist's WRITE_POSITION_FILE / WRITE_RAMO_SEC (default off)
   const bool write_pos = in.count("WRITE_POSITION_FILE") && to_logical(in.at("WRITE_POSITION_FILE")[0]);
   const bool write_ramo_sec = in.count("WRITE_RAMO_SEC") && to_logical(in.at("WRITE_RAMO_SEC")[0]);
@@ -385,8 +395,11 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "rd_main: WRITE_RAMO_SEC is supported for planar decks only\n");
     return 2;
   }
-  FILE* b_pos = write_pos ? std::fopen("out/position.bin", "wb") : nullptr;
-  FILE* b_ramo_sec = write_ramo_sec ? std::fopen("out/ramo_current.bin", "wb") : nullptr;
+  // both files are created on every run (empty unless asked for), as the reference does
+  FILE* b_pos = std::fopen("out/position.bin", "wb");
+  FILE* b_ramo_sec = std::fopen("out/ramo_current.bin", "wb");
+  if (b_pos && !write_pos) { std::fclose(b_pos); b_pos = nullptr; }
+  if (b_ramo_sec && !write_ramo_sec) { std::fclose(b_ramo_sec); b_ramo_sec = nullptr; }
   if ((write_pos && !b_pos) || (write_ramo_sec && !b_ramo_sec)) {
     std::fprintf(stderr, "rd_main: cannot write under out/\n");
     return 2;
@@ -408,7 +421,7 @@ int main(int argc, char** argv) {
       if (!b_planes[k]) { std::fprintf(stderr, "rd_main: cannot write %s\n", name); return 2; }
     }
   if (!f_emit || !f_abs || !f_top || !f_bot || !f_ramo || !b_emit || !b_emit_elec || !b_abs_top || !b_abs_bot ||
-      !f_field || !f_volt || !b_emit_ion || !b_emit_atom) {
+      !f_field || !f_volt || !b_emit_ion || !b_emit_atom || !f_integ) {
     std::fprintf(stderr, "rd_main: cannot write under out/\n");
     return 2;
   }
@@ -508,6 +521,11 @@ int main(int argc, char** argv) {
       for (double v : {c.F_avg[0], c.F_avg[1], c.F_avg[2], c.N_sup, c.df_avg, c.a_rate, c.MH_std})
         fl += "  " + fmt_E(v, 16, 8);
       std::fprintf(f_field, "%s\n", fl.c_str());
+      const long long nodes = (long long)q_panels * q_order;
+      std::fprintf(f_integ, "%s  %s  %s  %s  %s  %s  %s\n", fmt_I(1, 3).c_str(),
+                   fmt_I((long long)q_panels * q_panels, 8).c_str(), fmt_I(nodes * nodes, 8).c_str(),
+                   fmt_I(0, 4).c_str(), fmt_ES(c.N_sup, 12, 4).c_str(), fmt_ES(0.0, 12, 4).c_str(),
+                   fmt_ES(0.0, 12, 4).c_str());
     }
     absorbed(f_abs, c.absorbed_top_step + c.absorbed_bot_step, false);
     absorbed(f_top, c.absorbed_top_step, true);
@@ -552,7 +570,7 @@ int main(int argc, char** argv) {
     }
   }
   for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo, b_emit, b_emit_elec, b_abs_top, b_abs_bot, f_field, f_volt,
-                  b_emit_ion, b_emit_atom})
+                  b_emit_ion, b_emit_atom, f_integ})
     std::fclose(f);
   for (FILE* f : b_planes) if (f) std::fclose(f);
   if (b_pos) std::fclose(b_pos);

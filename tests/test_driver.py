@@ -142,6 +142,14 @@ def test_driver_run_matches_python_binding(driver, tmp_path, rg):
     # field.dt: one line per step the emitter is on, F_avg_z < 0, N_sup as in the counters
     fd = np.loadtxt(out / "field.dt")
     assert fd.shape == (12 - 2, 8) and np.all(fd[:, 0] == np.arange(3, 13)) and np.all(fd[:, 3] < 0)
+    # integration.dt: emitter, regions (16 x 16 panels), nodes (64 x 64), fail 0, N_sup, 0, 0
+    ig = np.loadtxt(out / "integration.dt")
+    assert ig.shape == (10, 7) and np.all(ig[:, :4] == [1, 256, 4096, 0])
+    np.testing.assert_allclose(ig[:, 4], fd[:, 4], rtol=1e-4)
+    # the files the reference creates on every run exist (empty outside their modes)
+    for name in ("density_emit_ion.bin", "density_emit_atom.bin", "density_ion.bin", "absorbed_recom.dt",
+                 "mh.bin", "position.bin", "ramo_current.bin", "init.bin", "init.dt", "volt.dt"):
+        assert (out / name).exists(), name
     assert emitted[0, 2] == emitted[1, 2] == 0 and emitted[2:, 2].sum() > 0  # EMITTERS_DELAY = 2
     # planes-1.bin / planes-2.bin: 52-byte records of upward crossings of 200 nm / 600 nm
     p1 = np.fromfile(out / "planes-1.bin", dtype=rec_top)
