@@ -10,6 +10,7 @@
 // compaction -- is a fixed sequence of kernels whose work lists are built on
 // the device, captured once as a CUDA graph and replayed every step.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <chrono>
@@ -99,6 +100,13 @@ static int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+// NVTX range over a host entry point (visible in Nsight Systems; a no-op
+// unless a profiler is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
 #define CK(call)                                                                     \
   do {                                                                               \
     cudaError_t e_ = (call);                                                         \
@@ -1003,6 +1011,7 @@ int rd_set_particles(rd_engine* e, int d, int n, const double* pos, const double
 }
 
 int rd_accel(rd_engine* e, int d, double* acc3n) {
+  NvtxRange nvtx_range("rd_accel");
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   int rc = repack(e);
   if (rc) return rc;
@@ -1015,6 +1024,7 @@ int rd_accel(rd_engine* e, int d, double* acc3n) {
 static int field_at_batch(rd_engine* e, int d, int M, const double* pos, double* field);
 
 int rd_field_at(rd_engine* e, int d, int M, const double* pos, double* field) {
+  NvtxRange nvtx_range("rd_field_at");
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (M < 0 || (M > 0 && (!pos || !field))) return fail(RD_ERR_INVALID, "bad point arrays");
   const int chunk = (e->max_items / 2) * RD_ITILE;
@@ -1159,6 +1169,7 @@ static int time_pair_passes(rd_engine* e, int reps, double* force_ms, double* mh
 }
 
 int rd_autotune(rd_engine* e, rd_tune_result* out) {
+  NvtxRange nvtx_range("rd_autotune");
   if (!e || !out) return fail(RD_ERR_INVALID, "null argument");
   *out = rd_tune_result{};
   out->chunk_min = e->clen_min;
@@ -1227,6 +1238,7 @@ int rd_mark_remove(rd_engine* e, int d, int i, int why) {
 }
 
 int rd_do_emission(rd_engine* e, int step) {
+  NvtxRange nvtx_range("rd_do_emission");
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   CK(rd_launch_step_set(e->st, e->d_step, step));
   int rc = launch_emission(e);
@@ -1236,6 +1248,7 @@ int rd_do_emission(rd_engine* e, int step) {
 }
 
 int rd_update_position(rd_engine* e, int step) {
+  NvtxRange nvtx_range("rd_update_position");
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   CK(rd_launch_step_set(e->st, e->d_step, step));
   int rc = launch_update_position(e);
@@ -1245,6 +1258,7 @@ int rd_update_position(rd_engine* e, int step) {
 }
 
 int rd_remove_particles(rd_engine* e, int step) {
+  NvtxRange nvtx_range("rd_remove_particles");
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   CK(rd_launch_step_set(e->st, e->d_step, step));
   int rc = launch_remove(e);
@@ -1254,6 +1268,7 @@ int rd_remove_particles(rd_engine* e, int step) {
 }
 
 int rd_run(rd_engine* e, int first_step, int nsteps) {
+  NvtxRange nvtx_range("rd_run");
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   if (nsteps < 0) return fail(RD_ERR_INVALID, "nsteps < 0");
   int rc = ensure_graph(e);
@@ -1321,6 +1336,7 @@ int rd_last_run_stats(rd_engine* e, double* ms, int* kps) {
 
 
 int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
+  NvtxRange nvtx_range("rd_profile_step");
   if (!e || !out) return fail(RD_ERR_INVALID, "null argument");
   *out = rd_phase_times{};
   const int S = e->cfg.max_diodes;
@@ -1505,6 +1521,7 @@ static int serve_admit(rd_engine* e, rd_serve_stats* st) {
 }
 
 int rd_serve(rd_engine* e, int iterations, rd_serve_stats* out) {
+  NvtxRange nvtx_range("rd_serve");
   if (!e || !out) return fail(RD_ERR_INVALID, "null argument");
   *out = rd_serve_stats{};
   const double w0 = e->clock();

@@ -29,6 +29,7 @@
 //   rd_main [run directory]
 #include <cctype>
 #include <cmath>
+#include <csignal>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -160,6 +161,12 @@ std::string fmt_I(long long v, int w) {
   std::snprintf(m, sizeof m, "%*lld", w, v);
   return std::string(m);
 }
+
+// SIGINT (ctrl+c) and SIGUSR1 (sent by Slurm before the time limit) stop the
+// main loop cleanly after the current step, as Signal_Handler does
+// (src/main.F90:214-217,289-294,531-535).
+volatile std::sig_atomic_t g_stop = 0;
+extern "C" void on_stop_signal(int) { g_stop = 1; }
 
 int check(int rc, const char* what) {
   if (rc != RD_OK) {
@@ -430,6 +437,8 @@ int main(int argc, char** argv) {
   std::vector<rd_event> events((size_t)ec.event_capacity);
   long long lost_total = 0;
   int progress = 1;
+  std::signal(SIGINT, on_stop_signal);
+  std::signal(SIGUSR1, on_stop_signal);
   for (int step = 1; step <= steps; ++step) {
     if (!b_pos) {
       check(rd_step(e, step), "rd_step");
@@ -567,6 +576,10 @@ int main(int argc, char** argv) {
                   c.emitted_total, c.absorbed_top_total + c.absorbed_bot_total);
       std::fflush(stdout);
       ++progress;
+    }
+    if (g_stop) {
+      std::printf("RUMDEED: Got signal SIGINT stopping main loop.\n");
+      break;
     }
   }
   for (FILE* f : {f_emit, f_abs, f_top, f_bot, f_ramo, b_emit, b_emit_elec, b_abs_top, b_abs_bot, f_field, f_volt,

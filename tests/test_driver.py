@@ -227,6 +227,29 @@ def test_optional_position_and_section_current_files(driver, tmp_path, rg):
 
 
 @pytest.mark.gpu
+def test_stop_signal_ends_the_run_cleanly(driver, tmp_path):
+    """SIGUSR1 (Slurm's warning) or SIGINT stops the main loop after the
+    current step, as the reference's Signal_Handler does: exit status 0, the
+    stop message, whole records for the steps that ran."""
+    import signal
+    import time
+    (tmp_path / "input").write_text(DECK.replace("STEPS = 12", "STEPS = 200000"))
+    (tmp_path / "work").write_text(WORK)
+    p = subprocess.Popen([driver, str(tmp_path)], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    emitted = tmp_path / "out" / "emitted.dt"
+    t0 = time.time()
+    while time.time() - t0 < 120 and not (emitted.exists() and emitted.stat().st_size > 0):
+        time.sleep(0.2)
+    p.send_signal(signal.SIGUSR1)
+    out, err = p.communicate(timeout=120)
+    assert p.returncode == 0, err
+    assert "Got signal SIGINT stopping main loop." in out
+    rows = np.loadtxt(emitted, ndmin=2)
+    assert 0 < len(rows) < 200000 and rows.shape[1] == 5
+    assert np.all(rows[:, 1] == np.arange(1, len(rows) + 1))
+
+
+@pytest.mark.gpu
 def test_event_log_counts_and_loss(rg):
     eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=3000 + 64,
                     chain_capacity=3000 + 64, quad_capacity=16384, event_capacity=8)
