@@ -194,6 +194,19 @@ int rd_counters_get(rd_engine* e, int diode, rd_counters* out);
  * k+1 steps (record_lifetime, src/mod_pair.F90:1135-1160), 1000 entries. */
 int rd_life_time(rd_engine* e, int diode, int* hist1000);
 
+/* Checkpoint of one diode between steps: its counters and emission state
+ * (MH_std, residual, ids), every particle (positions, velocities, the three
+ * acceleration histories, charge, mass, species, id, creation step, section)
+ * and its life-time histogram.  rd_diode_state_size gives the bytes;
+ * rd_diode_save writes them to a caller buffer; rd_diode_load puts them into a
+ * diode slot added with the same rd_diode_config (here or in another engine),
+ * after which stepping on from the saved step gives the same results as the
+ * run that was saved.  The reference has no restart file; this serves
+ * eviction and re-admission of long requests and resuming runs. */
+int rd_diode_state_size(rd_engine* e, int diode, long long* bytes);
+int rd_diode_save(rd_engine* e, int diode, void* buf, long long cap, long long* written);
+int rd_diode_load(rd_engine* e, int diode, const void* buf, long long size);
+
 /* Timing of the last rd_run: device milliseconds (CUDA events on the engine
  * stream) and launches of library kernels per step. */
 int rd_last_run_stats(rd_engine* e, double* ms, int* kernels_per_step);

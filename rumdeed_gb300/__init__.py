@@ -183,6 +183,9 @@ SIGNATURES = {
     "rd_events_take": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Event), _ip, C.POINTER(C.c_longlong)]),
     "rd_set_chunking": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "rd_get_chunking": (C.c_int, [C.c_void_p, _ip, _ip]),
+    "rd_diode_state_size": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_longlong)]),
+    "rd_diode_save": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]),
+    "rd_diode_load": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong]),
 }
 
 
@@ -504,6 +507,20 @@ class Diode:
 
     def mark_particles_remove(self, i, why):
         _check(self.L.rd_mark_remove(self.e.h, self.index, i, why))
+
+    def save_state(self):
+        """Checkpoint of the diode between steps (rd_diode_save), as bytes."""
+        size = C.c_longlong()
+        _check(self.L.rd_diode_state_size(self.e.h, self.index, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        written = C.c_longlong()
+        _check(self.L.rd_diode_save(self.e.h, self.index, buf, size.value, C.byref(written)))
+        return buf.raw[:written.value]
+
+    def load_state(self, state):
+        """Put a checkpoint into this diode (rd_diode_load); the diode must have
+        been added with the configuration of the saved one."""
+        _check(self.L.rd_diode_load(self.e.h, self.index, state, len(state)))
 
     def life_time(self):
         h = np.zeros(1000, dtype=np.int32)

@@ -1320,6 +1320,108 @@ int rd_counters_get(rd_engine* e, int d, rd_counters* o) {
   return RD_OK;
 }
 
+// ---- diode checkpoints ----------------------------------------------------------------
+namespace {
+struct StateHeader {
+  char magic[8];      // "RDSTATE1"
+  int version;        // 1
+  int n;              // particles saved
+  int dyn_bytes;      // sizeof(DiodeDyn) of the writer
+  int life_len;       // RD_MAX_LIFE
+  int capacity;       // the slot's capacity when saved
+  int pad;
+};
+constexpr int kStateDoubles = 17;   // x y z vx vy vz, a, a_prev, a_prev2 (9), q, m
+constexpr int kStateInts = 5;       // species id step0 section mask
+
+double* state_dbl(Pool& p, int k) {
+  double* a[kStateDoubles] = {p.x, p.y, p.z, p.vx, p.vy, p.vz, p.ax, p.ay, p.az,
+                              p.bx, p.by, p.bz, p.cx, p.cy, p.cz, p.q, p.m};
+  return a[k];
+}
+int* state_int(Pool& p, int k) {
+  int* a[kStateInts] = {p.species, p.id, p.step0, p.section, p.mask};
+  return a[k];
+}
+long long state_bytes(int n) {
+  return (long long)sizeof(StateHeader) + (long long)sizeof(DiodeDyn) +
+         (long long)n * (kStateDoubles * (long long)sizeof(double) + kStateInts * (long long)sizeof(int)) +
+         (long long)RD_MAX_LIFE * (long long)sizeof(int);
+}
+}  // namespace
+
+int rd_diode_state_size(rd_engine* e, int d, long long* bytes) {
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  if (!bytes) return fail(RD_ERR_INVALID, "null argument");
+  DiodeDyn y;
+  int rc = read_dyn(e, d, &y);
+  if (rc) return rc;
+  *bytes = state_bytes(y.n);
+  return RD_OK;
+}
+
+int rd_diode_save(rd_engine* e, int d, void* buf, long long cap, long long* written) {
+  NvtxRange nvtx_range("rd_diode_save");
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  if (!buf) return fail(RD_ERR_INVALID, "null buffer");
+  DiodeDyn y;
+  int rc = read_dyn(e, d, &y);
+  if (rc) return rc;
+  const long long need = state_bytes(y.n);
+  if (cap < need) return fail(RD_ERR_INVALID, "buffer smaller than rd_diode_state_size");
+  char* out = static_cast<char*>(buf);
+  StateHeader h{};
+  std::memcpy(h.magic, "RDSTATE1", 8);
+  h.version = 1;
+  h.n = y.n;
+  h.dyn_bytes = (int)sizeof(DiodeDyn);
+  h.life_len = RD_MAX_LIFE;
+  h.capacity = e->slots[d].p.cap;
+  std::memcpy(out, &h, sizeof h);
+  out += sizeof h;
+  std::memcpy(out, &y, sizeof y);
+  out += sizeof y;
+  const int off = e->slots[d].p.off;
+  for (int k = 0; k < kStateDoubles; ++k, out += sizeof(double) * (size_t)y.n)
+    if (y.n) CK(cudaMemcpy(out, state_dbl(e->pool, k) + off, sizeof(double) * (size_t)y.n, cudaMemcpyDeviceToHost));
+  for (int k = 0; k < kStateInts; ++k, out += sizeof(int) * (size_t)y.n)
+    if (y.n) CK(cudaMemcpy(out, state_int(e->pool, k) + off, sizeof(int) * (size_t)y.n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(out, e->life + (size_t)d * RD_MAX_LIFE, sizeof(int) * RD_MAX_LIFE, cudaMemcpyDeviceToHost));
+  if (written) *written = need;
+  return RD_OK;
+}
+
+int rd_diode_load(rd_engine* e, int d, const void* buf, long long size) {
+  NvtxRange nvtx_range("rd_diode_load");
+  if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
+  if (!buf || size < (long long)sizeof(StateHeader)) return fail(RD_ERR_INVALID, "not a diode state");
+  const char* in = static_cast<const char*>(buf);
+  StateHeader h;
+  std::memcpy(&h, in, sizeof h);
+  if (std::memcmp(h.magic, "RDSTATE1", 8) != 0 || h.version != 1 || h.dyn_bytes != (int)sizeof(DiodeDyn) ||
+      h.life_len != RD_MAX_LIFE || h.n < 0)
+    return fail(RD_ERR_INVALID, "not a diode state of this library version");
+  if (size < state_bytes(h.n)) return fail(RD_ERR_INVALID, "diode state truncated");
+  const DiodeParams& p = e->slots[d].p;
+  if (h.n > p.cap) return fail(RD_ERR_CAPACITY, "saved particles exceed the slot's capacity");
+  CK(cudaStreamSynchronize(e->st));
+  in += sizeof h;
+  DiodeDyn y;
+  std::memcpy(&y, in, sizeof y);
+  in += sizeof y;
+  const int off = p.off;
+  for (int k = 0; k < kStateDoubles; ++k, in += sizeof(double) * (size_t)h.n)
+    if (h.n) CK(cudaMemcpy(state_dbl(e->pool, k) + off, in, sizeof(double) * (size_t)h.n, cudaMemcpyHostToDevice));
+  for (int k = 0; k < kStateInts; ++k, in += sizeof(int) * (size_t)h.n)
+    if (h.n) CK(cudaMemcpy(state_int(e->pool, k) + off, in, sizeof(int) * (size_t)h.n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(e->life + (size_t)d * RD_MAX_LIFE, in, sizeof(int) * RD_MAX_LIFE, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(e->dD + d, &y, sizeof y, cudaMemcpyHostToDevice));
+  int rc = repack(e);   // the FP32 packs (and tip image points) of the loaded particles
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(e->st));
+  return RD_OK;
+}
+
 int rd_life_time(rd_engine* e, int d, int* hist) {
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (!hist) return fail(RD_ERR_INVALID, "null argument");

@@ -130,3 +130,35 @@ def test_served_two_time_step_diode_equals_alone(rg):
             assert got[key] == c[key], (rid, key)
         assert got["ramo_current"] == c["ramo_current"]
     eng.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_checkpoint_resume_equals_continuous_run(rg, prec):
+    """rd_diode_save after 4 steps, rd_diode_load into a fresh diode of another
+    engine (among other diodes), 4 more steps: the same particles, counters
+    and life-time histogram as the run that went on without stopping."""
+    (steps, pos, kw), (_, pos2, kw2) = make_requests(n=2, seed=21)
+    a = rg.Engine(precision=prec, max_diodes=2, particle_capacity=4096, chain_capacity=1024, quad_capacity=2048)
+    da = a.add_diode(**kw)
+    da.add_particles(pos, step=0)
+    a.run(1, 4)
+    state = da.save_state()
+    a.run(5, 4)
+    b = rg.Engine(precision=prec, max_diodes=3, particle_capacity=8192, chain_capacity=2048, quad_capacity=4096)
+    other = b.add_diode(**kw2)
+    other.add_particles(pos2, step=0)
+    db = b.add_diode(**kw)
+    db.load_state(state)
+    b.run(5, 4)
+    ca, cb = da.counters(), db.counters()
+    for key in ("n", "emitted_total", "absorbed_top_total", "absorbed_bot_total", "dropped_total",
+                "electron_steps", "steps_done", "chains", "ramo_current", "N_sup", "MH_std", "residual"):
+        assert ca[key] == cb[key], key
+    pa, pb = da.particles(), db.particles()
+    for key in ("pos", "vel", "acc", "charge", "id", "section"):
+        np.testing.assert_array_equal(pa[key], pb[key], err_msg=key)
+    np.testing.assert_array_equal(da.life_time(), db.life_time())
+    with pytest.raises(rg.RumdeedError):
+        db.load_state(state[:100])   # truncated
+    a.close()
+    b.close()
