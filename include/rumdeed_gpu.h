@@ -203,6 +203,16 @@ int rd_life_time(rd_engine* e, int diode, int* hist1000);
  * after which stepping on from the saved step gives the same results as the
  * run that was saved.  The reference has no restart file; this serves
  * eviction and re-admission of long requests and resuming runs. */
+/* State invariants of every resident diode, checked on the device between
+ * steps (a sanitizer-like self check; the counts do not stop anything):
+ * counts[k] = violations of kind k summed over the diodes, k = 0 particle count
+ * outside [0, capacity], 1 removal bookkeeping not cleared, 2 unknown
+ * species, 3 particle still marked for removal, 4 non-finite position /
+ * velocity / acceleration, 5 ids not strictly increasing within a diode,
+ * 6 charge or mass not those of the species.  *total = their sum. */
+enum { RD_VALIDATE_KINDS = 7 };
+int rd_validate(rd_engine* e, int counts[7], long long* total);
+
 int rd_diode_state_size(rd_engine* e, int diode, long long* bytes);
 int rd_diode_save(rd_engine* e, int diode, void* buf, long long cap, long long* written);
 int rd_diode_load(rd_engine* e, int diode, const void* buf, long long size);

@@ -183,6 +183,7 @@ SIGNATURES = {
     "rd_events_take": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Event), _ip, C.POINTER(C.c_longlong)]),
     "rd_set_chunking": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "rd_get_chunking": (C.c_int, [C.c_void_p, _ip, _ip]),
+    "rd_validate": (C.c_int, [C.c_void_p, _ip, C.POINTER(C.c_longlong)]),
     "rd_diode_state_size": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_longlong)]),
     "rd_diode_save": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]),
     "rd_diode_load": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong]),
@@ -371,6 +372,17 @@ class Engine:
 
     def sync(self):
         _check(self.L.rd_sync(self.h))
+
+    VALIDATE_KINDS = ("count_outside_capacity", "removal_not_cleared", "unknown_species", "still_marked",
+                      "non_finite_state", "ids_not_increasing", "charge_mass_mismatch")
+
+    def validate(self):
+        """Device-side state invariants of every resident diode (rd_validate):
+        violation counts by kind; all zero for a healthy engine."""
+        counts = (C.c_int * 7)()
+        total = C.c_longlong()
+        _check(self.L.rd_validate(self.h, counts, C.byref(total)))
+        return dict(zip(self.VALIDATE_KINDS, list(counts)))
 
     def last_run_stats(self):
         ms = C.c_double()

@@ -92,6 +92,8 @@ cudaError_t rd_launch_add_particles(cudaStream_t st, const DiodeParams* P, Diode
                                     const double* vel, const int* species, int step, int section);
 cudaError_t rd_launch_mark(cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
                            int d, int i, int why);
+cudaError_t rd_launch_validate(int nslots, cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy,
+                               const Pool& pool, int* bad);
 
 
 // ---- errors -------------------------------------------------------------------------
@@ -1317,6 +1319,28 @@ int rd_counters_get(rd_engine* e, int d, rd_counters* o) {
   int rc = read_dyn(e, d, &y);
   if (rc) return rc;
   fill_counters(y, o);
+  return RD_OK;
+}
+
+int rd_validate(rd_engine* e, int counts[RD_VALIDATE_KINDS], long long* total) {
+  NvtxRange nvtx_range("rd_validate");
+  if (!e || !counts) return fail(RD_ERR_INVALID, "null argument");
+  const int S = e->nslots_hw();
+  std::vector<int> bad((size_t)std::max(S, 1) * RD_VALIDATE_KINDS, 0);
+  int* dbad = nullptr;
+  CK(cudaMalloc(&dbad, sizeof(int) * bad.size()));
+  cudaError_t ce = rd_launch_validate(S, e->st, e->dP, e->dD, e->pool, dbad);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(bad.data(), dbad, sizeof(int) * bad.size(), cudaMemcpyDeviceToHost, e->st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->st);
+  cudaFree(dbad);
+  CK(ce);
+  long long sum = 0;
+  for (int k = 0; k < RD_VALIDATE_KINDS; ++k) {
+    counts[k] = 0;
+    for (int d = 0; d < S; ++d) counts[k] += bad[(size_t)d * RD_VALIDATE_KINDS + k];
+    sum += counts[k];
+  }
+  if (total) *total = sum;
   return RD_OK;
 }
 

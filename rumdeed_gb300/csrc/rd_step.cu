@@ -586,4 +586,49 @@ cudaError_t rd_launch_mark(cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy, 
   return cudaGetLastError();
 }
 
+namespace {
+// State invariants of every resident diode between steps, one block per
+// diode; bad[d * RD_VALIDATE_KINDS + k] counts the violations of kind k:
+//   0 particle count outside [0, capacity]      1 removal bookkeeping not cleared
+//   2 species outside {1, 2, 3}                  3 a particle still marked for removal
+//   4 non-finite position, velocity or acceleration
+//   5 ids not strictly increasing (the stable compaction keeps creation order)
+//   6 charge / mass not those of the species (Add_Particle)
+__global__ void __launch_bounds__(256)
+k_validate(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool, int* __restrict__ bad) {
+  const int d = blockIdx.x;
+  const DiodeParams& p = P[d];
+  if (!p.active) return;
+  const DiodeDyn& y = Dy[d];
+  int* b = bad + d * RD_VALIDATE_KINDS;
+  if (threadIdx.x == 0) {
+    if (y.n < 0 || y.n > p.cap) atomicAdd(&b[0], 1);
+    if (y.n_remove != 0 || y.n_remove_top != 0 || y.n_remove_bot != 0) atomicAdd(&b[1], 1);
+  }
+  const int n = min(max(y.n, 0), p.cap);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int gi = p.off + i, sp = pool.species[gi];
+    if (sp < 1 || sp > 3) atomicAdd(&b[2], 1);
+    if (pool.mask[gi] != 1) atomicAdd(&b[3], 1);
+    const double v[9] = {pool.x[gi], pool.y[gi], pool.z[gi], pool.vx[gi], pool.vy[gi], pool.vz[gi],
+                         pool.ax[gi], pool.ay[gi], pool.az[gi]};
+    bool finite = true;
+    for (int k = 0; k < 9; ++k) finite = finite && isfinite(v[k]);
+    if (!finite) atomicAdd(&b[4], 1);
+    if (i > 0 && pool.id[gi] <= pool.id[gi - 1]) atomicAdd(&b[5], 1);
+    const double q = pool.q[gi], m = pool.m[gi];
+    const bool ok = (sp == 1 && q == -1.0 * c_k.q0 && m == 1.0 * c_k.m0) ||
+                    (sp == 2 && q == 1.0 * c_k.q0 && m == c_k.m_N2p) || (sp == 3 && q == 0.0 && m == c_k.m_N2);
+    if (!ok) atomicAdd(&b[6], 1);
+  }
+}
+}  // namespace
+
+cudaError_t rd_launch_validate(int nslots, cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy,
+                               const Pool& pool, int* bad) {
+  cudaMemsetAsync(bad, 0, sizeof(int) * (size_t)nslots * RD_VALIDATE_KINDS, st);
+  if (nslots > 0) k_validate<<<nslots, 256, 0, st>>>(P, Dy, pool, bad);
+  return cudaGetLastError();
+}
+
 RD_DEFINE_CONSTANT_UPLOAD(step)

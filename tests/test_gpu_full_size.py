@@ -85,6 +85,7 @@ def test_largest_diode_alone_equals_128_mix(rg):
         ds.append(d)
     eng.run(1, 1)
     mixed = ds[big].particles()
+    assert all(v == 0 for v in eng.validate().values())   # 128 diodes, 0.79 M electrons
     eng.close()
     r = reqs[big]
     one = rg.Engine(precision=rg.PREC_FP32C, max_diodes=1, particle_capacity=r["capacity"] + 64,

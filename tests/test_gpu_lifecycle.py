@@ -39,3 +39,28 @@ def test_engines_release_device_memory(rg):
         assert again == first     # same inputs, same results, engine after engine
     leaked = base - _free_bytes()
     assert leaked < 64 * 1024 * 1024, "%.1f MiB not returned" % (leaked / 2 ** 20)
+
+
+def test_validate_reports_clean_and_corrupted_state(rg):
+    """rd_validate: zero violations after steps; a non-finite position put in
+    with rd_set_particles (no step runs on it) is counted, and the count
+    returns to zero once the position is repaired."""
+    rng = np.random.default_rng(3)
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=2, particle_capacity=8192, chain_capacity=2048,
+                    quad_capacity=4096)
+    d = eng.add_diode(V_s=2.0e3, gap=800 * NM, capacity=4096, emitter_pos=(-100 * NM, -100 * NM),
+                      emitter_dim=(200 * NM, 200 * NM), work=[[2.5]], emission=True, mh_jumps=20,
+                      max_chains=256, seed=7)
+    d.add_particles(np.column_stack([rng.uniform(-100 * NM, 100 * NM, 300), rng.uniform(-100 * NM, 100 * NM, 300),
+                                     rng.uniform(2 * NM, 790 * NM, 300)]), step=0)
+    eng.run(1, 5)
+    assert all(v == 0 for v in eng.validate().values())
+    pos = d.particles()["pos"]
+    bad = pos.copy()
+    bad[7, 2] = np.nan
+    d.set_particles(pos=bad)
+    v = eng.validate()
+    assert v["non_finite_state"] == 1 and sum(v.values()) == 1
+    d.set_particles(pos=pos)
+    assert all(v == 0 for v in eng.validate().values())
+    eng.close()

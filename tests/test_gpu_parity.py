@@ -641,6 +641,7 @@ def test_two_time_step_full_steps_with_emission_fp64(rg, orc):
     assert c["emitted_total"] == o.s.emitted_total > 0
     _check_average_velocities(c, o)   # step 5: the ions did not move, their mean is 0
     assert c["n_ion_vel"] > 0 and c["avg_ion_vel"] == (0.0, 0.0, 0.0)
+    assert all(v == 0 for v in eng.validate().values())
     eng.close()
 
 

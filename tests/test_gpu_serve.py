@@ -67,6 +67,7 @@ def test_served_equals_alone(rg, prec):
         for key in ("ramo_current", "N_sup", "MH_std", "residual"):
             assert c[key] == c_alone[key], key
         assert finals[rid]["done_s"] >= finals[rid]["admit_s"] >= finals[rid]["submit_s"]
+    assert all(v == 0 for v in eng.validate().values())
     eng.close()
 
 
