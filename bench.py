@@ -215,7 +215,8 @@ def cpu_sample(stream_seed, budget_pairs=2.0e10, rank=0):
 
 def plain_fp64_sample(rg, requests, budget_s=25.0):
     """The plain FP64 GPU form, one diode at a time (own engine, rd_run per
-    diode), on a sample of the served requests."""
+    diode, chunking tuned per diode like the served engine's), on a sample of
+    the served requests."""
     e_steps, dev_s, names = 0, 0.0, []
     t_start = time.perf_counter()
     for r in sorted(requests, key=lambda q: q["capacity"]):
@@ -226,8 +227,10 @@ def plain_fp64_sample(rg, requests, budget_s=25.0):
         d = eng.add_diode(**diode_kwargs(r))
         d.add_particles(prefill(r), step=0)
         eng.run(1, 1)                     # first step (graph capture) untimed
+        eng.autotune()                    # the same tuning the served engine gets
+        eng.run(2, 1)                     # graph rebuilt under the chosen chunking, untimed
         n0 = d.counters()["electron_steps"]
-        eng.run(2, 1)
+        eng.run(3, 1)
         ms, _ = eng.last_run_stats()
         e_steps += d.counters()["electron_steps"] - n0
         dev_s += ms / 1e3
@@ -678,12 +681,14 @@ def case_plain(args):
                                 chain_capacity=20064, quad_capacity=4096)
                 d = eng.add_diode(work=[[phi]], mh_jumps=jumps, **kw)
                 eng.run(1, args.warmup)
+                tune = eng.autotune()   # a lone diode needs short chunks to fill the GPU
                 eng.run(args.warmup + 1, args.steps)
                 ms, kps = eng.last_run_stats()
                 c = d.counters()
                 eng.close()
                 gpu[tag] = {"steps_per_s": args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
-                            "in_flight": c["n"], "emitted_total": c["emitted_total"], "N_sup": c["N_sup"]}
+                            "in_flight": c["n"], "emitted_total": c["emitted_total"], "N_sup": c["N_sup"],
+                            "chunking": [tune["chunk_min"], tune["chunk_count_max"]]}
             o = orc.OracleDiode(cap=20000, V_s=2.0e3, d=1000 * NM, time_step=0.25e-15, image_charge=True,
                                 N_ic_max=0)
             o.set_planar_emitter(-side / 2, -side / 2, side, side, [[phi]])
