@@ -570,7 +570,7 @@ def case_serve_latency(args):
     pending = stream.next()
     ids = []
     t0 = time.perf_counter()
-    e_steps, dev_ms = 0, 0.0
+    e_steps, dev_ms, iters, checks, violations = 0, 0.0, 0, 0, 0
     while time.perf_counter() - t0 < args.window:
         now = time.perf_counter() - t0
         while pending is not None and pending["arrival"] <= now:
@@ -580,6 +580,10 @@ def case_serve_latency(args):
         st = eng.serve(1)
         e_steps += st["electron_steps"]
         dev_ms += st["device_ms"]
+        iters += 1
+        if args.validate_every and iters % args.validate_every == 0:   # rd_validate self check
+            violations += sum(eng.validate().values())
+            checks += 1
     wall = time.perf_counter() - t0
     lat, queue, service = [], [], []
     states = {}
@@ -598,6 +602,7 @@ def case_serve_latency(args):
                       "latency_s_p50": pct(lat, 50), "latency_s_p99": pct(lat, 99),
                       "queueing_s_p50": pct(queue, 50), "queueing_s_p99": pct(queue, 99),
                       "service_s_p50": pct(service, 50), "service_s_p99": pct(service, 99),
+                      "iterations": iters, "validate_checks": checks, "violations": violations,
                       "electron_steps_per_s_wall": e_steps / wall,
                       "electron_steps_per_s_device": e_steps / (dev_ms / 1e3) if dev_ms else None}),
           flush=True)
@@ -764,6 +769,8 @@ def main():
     ap.add_argument("--step-scale", type=float, default=100.0,
                     help="serve-latency: every request's step count is divided by this")
     ap.add_argument("--window", type=float, default=60.0, help="serve-latency: seconds of real-time serving")
+    ap.add_argument("--validate-every", type=int, default=0,
+                    help="serve-latency: run rd_validate every this many iterations (0: never)")
     ap.add_argument("--fp64-budget", type=float, default=2.0e11,
                     help="micro: largest N(N-1) x terms run in FP64 for the error check")
     args = ap.parse_args()
