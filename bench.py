@@ -608,6 +608,50 @@ def case_serve_latency(args):
           flush=True)
 
 
+def hbm_peak_gbs():
+    """Measured copy bandwidth of this GPU pool (MEASURED_PEAKS.json), or None."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def case_verlet(args):
+    """The HBM-bound per-particle kernels at a size that fills the GPU: 64
+    planar diodes of --verlet-n / 64 electrons each (no emission), the Beeman
+    position pass (k_position: boundary checks and FP32 packs included) and
+    the velocity pass (k_velocity + the Ramo / mean-velocity reduction), timed
+    with CUDA events (rd_time_verlet).  Algorithmic bytes per electron:
+    position 268 B (reads species, x, v, a, a_prev, q = 108 B; writes x,
+    a_prev2, a_prev, the cleared a and the four FP32 packs = 160 B), velocity
+    176 B (reads species, v, a, a_prev, a_prev2, q = 108 B; writes v and the
+    Ramo term = 32 B; the reduction reads the Ramo term, species and v =
+    36 B)."""
+    import rumdeed_gb300 as rg
+    rg.build()
+    D, n = 64, max(1, args.verlet_n // 64)
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=D, particle_capacity=D * (n + 64),
+                    chain_capacity=4096, quad_capacity=4096)
+    rng = np.random.default_rng(7)
+    for k in range(D):
+        d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, capacity=n, image_charge=True, N_ic_max=0)
+        d.add_particles(np.column_stack([rng.uniform(-500 * NM, 500 * NM, n), rng.uniform(-500 * NM, 500 * NM, n),
+                                         rng.uniform(400 * NM, 600 * NM, n)]), step=0)
+    pos_ms, vel_ms = eng.time_verlet(reps=20)
+    eng.close()
+    N = D * n
+    peak = hbm_peak_gbs()
+    out = {"case": "verlet", "electrons": N}
+    for name, ms, b in (("position", pos_ms, 268), ("velocity", vel_ms, 176)):
+        gbs = b * N / (ms / 1e3) / 1e9
+        out[name] = {"ms": ms, "bytes_per_electron": b, "achieved_gbs": gbs,
+                     "frac_of_measured_hbm": gbs / peak if peak else None}
+    out["hbm_peak_gbs"] = peak
+    print(json.dumps(out), flush=True)
+
+
 def case_burst(args):
     """The first S requests of the serving stream admitted at once (no arrival
     pacing), then W + K serving iterations: the serving workload with a fixed
@@ -760,7 +804,7 @@ def main():
     ap.add_argument("--plain-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=1.0e10)
     ap.add_argument("--case", default="serve",
-                    choices=["serve", "micro", "burst", "mh-small", "plain", "tips", "serve-latency"],
+                    choices=["serve", "micro", "burst", "mh-small", "plain", "tips", "serve-latency", "verlet"],
                     help="serve: the headline serving benchmark; the others are secondary workloads")
     ap.add_argument("--sizes", default="4096,65536,262144", help="micro: electron counts")
     ap.add_argument("--nics", default="0,7,8", help="micro: N_ic_max values (K = 8 mirror terms read "
@@ -769,6 +813,7 @@ def main():
     ap.add_argument("--step-scale", type=float, default=100.0,
                     help="serve-latency: every request's step count is divided by this")
     ap.add_argument("--window", type=float, default=60.0, help="serve-latency: seconds of real-time serving")
+    ap.add_argument("--verlet-n", type=int, default=1 << 24, help="verlet: electrons in all (64 diodes)")
     ap.add_argument("--validate-every", type=int, default=0,
                     help="serve-latency: run rd_validate every this many iterations (0: never)")
     ap.add_argument("--fp64-budget", type=float, default=2.0e11,
@@ -785,7 +830,7 @@ def main():
     if args.case != "serve":
         if rank == 0:
             {"micro": case_micro, "burst": case_burst, "mh-small": case_mh_small, "plain": case_plain,
-             "serve-latency": case_serve_latency,
+             "serve-latency": case_serve_latency, "verlet": case_verlet,
              "tips": case_tips}[args.case](args)
     elif args.impl == "reference":
         run_reference(args, rank, world)

@@ -263,6 +263,13 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out);
 int rd_time_accel(rd_engine* e, int reps, double* ms_per_eval);
 int rd_time_field_at(rd_engine* e, int diode, int M, const double* pos3m, int reps,
                      double* ms_per_eval);
+/* rd_time_verlet: device time of one Beeman position pass (k_position, with
+ * the boundary checks and FP32 packs) and of one velocity pass (k_velocity +
+ * the Ramo reduction) over every resident particle, averaged over `reps`
+ * passes each.  Unlike the two timers above it advances the particle state
+ * (positions, velocities, histories): a measurement of the HBM-bound kernels
+ * on a snapshot that is thrown away. */
+int rd_time_verlet(rd_engine* e, int reps, double* position_ms, double* velocity_ms);
 
 /* ---- event log: emission and absorption records ------------------------------
  * The reference writes one record per emitted particle (density_emit.bin and

@@ -178,6 +178,7 @@ SIGNATURES = {
     "rd_clock": (C.c_int, [C.c_void_p, _dp]),
     "rd_field_at_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
     "rd_time_accel": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "rd_time_verlet": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "rd_time_field_at": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, C.c_int, _dp]),
     "rd_autotune": (C.c_int, [C.c_void_p, C.POINTER(TuneResult)]),
     "rd_events_take": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Event), _ip, C.POINTER(C.c_longlong)]),
@@ -337,6 +338,13 @@ class Engine:
     def get_chunking(self):
         a, b = C.c_int(), C.c_int()
         _check(self.L.rd_get_chunking(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def time_verlet(self, reps=5):
+        """Device ms of one position pass and of one velocity pass (rd_time_verlet;
+        advances the state)."""
+        a, b = C.c_double(), C.c_double()
+        _check(self.L.rd_time_verlet(self.h, reps, C.byref(a), C.byref(b)))
         return a.value, b.value
 
     def time_accel(self, reps=3):

@@ -1087,6 +1087,35 @@ int rd_time_accel(rd_engine* e, int reps, double* ms_per_eval) {
   return RD_OK;
 }
 
+int rd_time_verlet(rd_engine* e, int reps, double* position_ms, double* velocity_ms) {
+  NvtxRange nvtx_range("rd_time_verlet");
+  if (!e || !position_ms || !velocity_ms || reps <= 0) return fail(RD_ERR_INVALID, "bad argument");
+  const int ns = e->nslots_hw();
+  CK(plan(e, PM_PART));
+  CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->evlog,
+                        e->d_step));   // warm-up
+  CK(rd_launch_velocity(e->grid, ns, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->ramo,
+                        e->d_step));
+  float ms = 0.f;
+  CK(cudaEventRecord(e->ev0, e->st));
+  for (int r = 0; r < reps; ++r)
+    CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->evlog,
+                          e->d_step));
+  CK(cudaEventRecord(e->ev1, e->st));
+  CK(cudaEventSynchronize(e->ev1));
+  CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+  *position_ms = ms / reps;
+  CK(cudaEventRecord(e->ev0, e->st));
+  for (int r = 0; r < reps; ++r)
+    CK(rd_launch_velocity(e->grid, ns, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->ramo,
+                          e->d_step));
+  CK(cudaEventRecord(e->ev1, e->st));
+  CK(cudaEventSynchronize(e->ev1));
+  CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+  *velocity_ms = ms / reps;
+  return RD_OK;
+}
+
 int rd_time_field_at(rd_engine* e, int d, int M, const double* pos, int reps, double* ms_per_eval) {
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (M <= 0 || !pos || !ms_per_eval || reps <= 0) return fail(RD_ERR_INVALID, "bad argument");
