@@ -135,6 +135,7 @@ static RdConst make_constants() {
   k.tip_K = (1.0 * k.q0) / ((4.0 * k.pi) * k.eps0);
   k.m_N2 = 28.0134 * m_u;
   k.m_N2p = k.m_N2 - k.m0;
+  k.q0_inv = 1.0 / k.q0;
   return k;
 }
 
@@ -240,7 +241,7 @@ struct rd_engine {
                                // [6 + 2p .. 7 + 2p] planar MH part p >= 2
   EventLog evlog{nullptr, nullptr, 0};   // emission / absorption records (rd_events_take)
   int* kept = nullptr;
-  double* ramo = nullptr;
+  double* ramo = nullptr;   // velocity-pass item partials (10 per 128-particle item)
   int* life = nullptr;
   int* d_step = nullptr;
   double *fpx = nullptr, *fpy = nullptr, *fpz = nullptr, *ffx = nullptr, *ffy = nullptr, *ffz = nullptr;
@@ -626,7 +627,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
       e->dalloc(&e->item_queue, 8 + 2 * RD_MH_PARTS) ||
       (cfg->event_capacity > 0 && (e->dalloc(&e->evlog.buf, (size_t)cfg->event_capacity) ||
                                    e->dalloc(&e->evlog.count, 1))) ||
-      e->dalloc(&e->ramo, cap) || e->dalloc(&e->life, (size_t)S * RD_MAX_LIFE) ||
+      e->dalloc(&e->ramo, ((size_t)cap / RD_ITILE + S + 1) * 10) || e->dalloc(&e->life, (size_t)S * RD_MAX_LIFE) ||
       e->dalloc(&e->d_step, 1))
     return bail(fail(RD_ERR_NOMEM, "device allocation failed"));
   double** chd[] = {&e->cs.x, &e->cs.y, &e->cs.F, &e->cs.sup, &e->cs.df, &e->cs.px, &e->cs.py,
@@ -776,6 +777,7 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
     p.mh_jumps = c->mh_jumps > 0 ? c->mh_jumps : 80;     // ndim, emission_tip:506
     p.mh_lo = 0.0005; p.mh_hi = 0.125;                   // emission_tip:62-63
   }
+  p.ramo_uz = -1.0 / p.d;   // E_zunit_planar, once per diode
   SlotHost sl;
   sl.pool_len = p.cap;
   sl.pool_off = e->pool_alloc.alloc(sl.pool_len, 32);

@@ -45,6 +45,7 @@ __host__ __device__ inline rd_d4 make_d4(double x, double y, double z, double w)
 struct RdConst {
   double pi, q0, m0, eps0, hbar, div_fac_c, a_FN, b_FN, l_const, L2, tip_K, m_N2, m_N2p;
   double length_scale;
+  double q0_inv;   // 1 / q0, for the FP32 charge packs
 };
 
 // Static parameters of one diode slot.
@@ -77,6 +78,7 @@ struct DiodeParams {
   int planes_n;          // measurement planes (Check_Planes)
   double planes_z[10];
   int tts;               // two-time-step interval T (atom_time_interval); 0 off
+  double ramo_uz;        // -1 / d: z of the planar unit field E_zunit_planar
 };
 
 // Planner modes (k_plan): which i-set of each diode a pair-sum plan covers.

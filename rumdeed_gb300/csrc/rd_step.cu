@@ -42,7 +42,7 @@ __device__ __forceinline__ void pack_one(const DiodeParams& p, const Pool& pool,
   split_nm(x, p.org_x, &h.x, &l.x);
   split_nm(y, p.org_y, &h.y, &l.y);
   split_nm(z, 0.0, &h.z, &l.z);
-  h.w = (float)(pool.q[gi] / c_k.q0);
+  h.w = (float)(pool.q[gi] * c_k.q0_inv);   // exact for charges that are multiples of q0
   l.w = (float)((p.d - z) * 1.0e9);
   pool.pk_hi[gi] = h;
   pool.pk_lo[gi] = l;
@@ -254,22 +254,60 @@ k_position(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool po
   }
 }
 
+// Item partials of the velocity pass: 10 values per 128-particle item (ramo
+// e, ramo ion, electron v (3), ion v (3), electrons, ions).
+constexpr int RD_VEL_NV = 10;
+
+// Sum of 8 per-lane values over a warp by transpose reduction: three halving
+// exchanges (lanes 16, 8, 4 apart) leave each lane one value summed over 8
+// lanes, two butterfly steps finish it.  Lane l returns the total of value
+// (l >> 2) & 7.  9 FP64 additions per lane (a butterfly per value takes 40);
+// the order is fixed, so the result does not depend on scheduling.
+__device__ __forceinline__ double warp_sum8(double a[8], int lane) {
+  const bool u16 = lane & 16, u8 = lane & 8, u4 = lane & 4;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double send = u16 ? a[k] : a[k + 4], keep = u16 ? a[k + 4] : a[k];
+    a[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const double send = u8 ? a[k] : a[k + 2], keep = u8 ? a[k + 2] : a[k];
+    a[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+  double t;
+  {
+    const double send = u4 ? a[0] : a[1], keep = u4 ? a[1] : a[0];
+    t = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  t += __shfl_xor_sync(0xffffffffu, t, 2);
+  t += __shfl_xor_sync(0xffffffffu, t, 1);
+  return t;
+}
+
 __global__ void __launch_bounds__(RD_ITILE)
 k_velocity(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
            const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
-           double* __restrict__ ramo, const int* __restrict__ step_ptr) {
-  for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
+           double* __restrict__ part, const int* __restrict__ step_ptr) {
+  __shared__ double s_w[RD_ITILE / 32][8];
+  __shared__ int s_n[RD_ITILE / 32][2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {   // g is block-uniform
     int d, i;
-    if (!part_index(plan, ph, g, &d, &i)) continue;
+    const bool live = part_index(plan, ph, g, &d, &i);
     const DiodeParams& p = P[d];
     const int gi = p.off + i;
-    const int sp = pool.species[gi];
-    double r = 0.0;
+    const int sp = live ? pool.species[gi] : 0;
+    const bool ion_step = p.tts <= 1 || (*step_ptr - Dy[d].step_offset) % p.tts == 0;
+    // a: ramo e, ramo ion, electron v (3), ion v (3)
+    double a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = 0.0;
     // two-time-step diodes: ions only on steps divisible by T, with the step
     // T*dt (Update_Species_Velocity, src/mod_verlet.F90:511-590); T = 1 as in
     // k_position
     const bool slow = p.tts > 1 && sp == 2;
-    if (sp != 3 && !(slow && (*step_ptr - Dy[d].step_offset) % p.tts != 0)) {
+    if (live && sp != 3 && !(slow && !ion_step)) {
       const double dt = p.dt;
       double vx, vy, vz;
       if (!slow) {
@@ -283,60 +321,69 @@ k_velocity(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, P
         vz = pool.vz[gi] + (((1.0 / 6.0) * ((2.0 * pool.az[gi] + 5.0 * pool.bz[gi]) - pool.cz[gi])) * dt) * T;
       }
       pool.vx[gi] = vx; pool.vy[gi] = vy; pool.vz[gi] = vz;
-      {   // ramo_current(species): electrons and ions
-        double ux, uy, uz;
-        if (p.geometry == RD_G_TIP) {   // E_zunit_tip
-          double ex, ey, ez;
-          tip_field_E(p, pool.x[gi], pool.y[gi], pool.z[gi], &ex, &ey, &ez);
-          ux = (ex * p.pre_E_unit) / p.pre_E; uy = (ey * p.pre_E_unit) / p.pre_E; uz = (ez * p.pre_E_unit) / p.pre_E;
-        } else {                        // E_zunit_planar
-          ux = 0.0; uy = 0.0; uz = -1.0 / p.d;
-        }
+      double r;   // ramo_current(species): electrons and ions
+      if (p.geometry == RD_G_TIP) {   // E_zunit_tip
+        double ex, ey, ez;
+        tip_field_E(p, pool.x[gi], pool.y[gi], pool.z[gi], &ex, &ey, &ez);
+        const double ux = (ex * p.pre_E_unit) / p.pre_E, uy = (ey * p.pre_E_unit) / p.pre_E,
+                     uz = (ez * p.pre_E_unit) / p.pre_E;
         r = pool.q[gi] * ((vx * ux + vy * uy) + vz * uz);
+      } else {                        // E_zunit_planar: (0, 0, -1/d); the x, y terms are 0
+        r = pool.q[gi] * (vz * p.ramo_uz);
+      }
+      if (sp == 2) {
+        a[1] = r; a[5] = vx; a[6] = vy; a[7] = vz;
+      } else {
+        a[0] = r;
+        if (sp == 1) { a[2] = vx; a[3] = vy; a[4] = vz; }
       }
     }
-    ramo[gi] = r;
+    // Average_Velocities counts the particles before removal, moved or not
+    const int ne = __popc(__ballot_sync(0xffffffffu, live && sp == 1));
+    const int ni = __popc(__ballot_sync(0xffffffffu, live && sp == 2));
+    const double t = warp_sum8(a, lane);
+    if ((lane & 3) == 0) s_w[w][lane >> 2] = t;
+    if (lane == 0) { s_n[w][0] = ne; s_n[w][1] = ni; }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+      double u = s_w[0][threadIdx.x];
+#pragma unroll
+      for (int q = 1; q < RD_ITILE / 32; ++q) u += s_w[q][threadIdx.x];
+      part[(size_t)g * RD_VEL_NV + threadIdx.x] = u;
+    } else if (threadIdx.x < RD_VEL_NV) {
+      int c = 0;
+#pragma unroll
+      for (int q = 0; q < RD_ITILE / 32; ++q) c += s_n[q][threadIdx.x - 8];
+      part[(size_t)g * RD_VEL_NV + threadIdx.x] = (double)c;
+    }
+    __syncthreads();
   }
 }
 
 // Ramo current per species, the mean velocities of Average_Velocities
 // (src/mod_verlet.F90:428-447: sums over the particles the velocity update
 // moved, divided by the particle counts before removal) and the
-// electron-step count, per diode (fixed-order reduction).
+// electron-step count, per diode: the diode's item partials (k_velocity)
+// added in a fixed order.
 __global__ void __launch_bounds__(256)
-k_ramo(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, const double* __restrict__ ramo,
-       Pool pool, const int* __restrict__ step_ptr) {
-  constexpr int NV = 10;   // ramo e, ramo ion, v elec (3), v ion (3), electrons, ions
-  __shared__ double red[NV][256];
+k_ramo(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, const PlanEntry* __restrict__ plan,
+       const double* __restrict__ part) {
+  __shared__ double red[RD_VEL_NV][256];
   const int d = blockIdx.x;
   const DiodeParams& p = P[d];
   if (!p.active) return;
   DiodeDyn& y = Dy[d];
   const int n = y.n;
-  const int step = *step_ptr - y.step_offset;
-  const bool ion_step = p.tts <= 1 || step % p.tts == 0;   // ions moved in this step (k_velocity)
-  double v[NV];
-  for (int k = 0; k < NV; ++k) v[k] = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int gi = p.off + i, sp = pool.species[gi];
-    const double r = ramo[gi];
-    if (sp == 2) {
-      v[1] += r;
-      v[9] += 1.0;
-      if (ion_step) { v[5] += pool.vx[gi]; v[6] += pool.vy[gi]; v[7] += pool.vz[gi]; }
-    } else {
-      v[0] += r;
-      if (sp == 1) {
-        v[8] += 1.0;
-        v[2] += pool.vx[gi]; v[3] += pool.vy[gi]; v[4] += pool.vz[gi];
-      }
-    }
-  }
-  for (int k = 0; k < NV; ++k) red[k][threadIdx.x] = v[k];
+  const int g0 = plan[d].item_off, items = plan[d].tiles;
+  double v[RD_VEL_NV];
+  for (int k = 0; k < RD_VEL_NV; ++k) v[k] = 0.0;
+  for (int t = threadIdx.x; t < items; t += blockDim.x)
+    for (int k = 0; k < RD_VEL_NV; ++k) v[k] += part[(size_t)(g0 + t) * RD_VEL_NV + k];
+  for (int k = 0; k < RD_VEL_NV; ++k) red[k][threadIdx.x] = v[k];
   __syncthreads();
   for (int h = blockDim.x / 2; h > 0; h >>= 1) {
     if (threadIdx.x < h)
-      for (int k = 0; k < NV; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+      for (int k = 0; k < RD_VEL_NV; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
     __syncthreads();
   }
   if (threadIdx.x == 0) {
@@ -494,9 +541,9 @@ cudaError_t rd_launch_position(int grid, cudaStream_t st, const DiodeParams* P, 
 }
 cudaError_t rd_launch_velocity(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
                                DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
-                               const PlanHeader* ph, double* ramo, const int* step_ptr) {
-  k_velocity<<<rd_grid(k_velocity, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, ramo, step_ptr);
-  k_ramo<<<nslots, 256, 0, st>>>(P, Dy, ramo, pool, step_ptr);
+                               const PlanHeader* ph, double* part, const int* step_ptr) {
+  k_velocity<<<rd_grid(k_velocity, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, part, step_ptr);
+  k_ramo<<<nslots, 256, 0, st>>>(P, Dy, plan, part);
   return cudaGetLastError();
 }
 cudaError_t rd_launch_compact(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
