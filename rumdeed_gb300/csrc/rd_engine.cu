@@ -51,7 +51,7 @@ cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const Diode
 cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                     const double* qx, const double* qy, const double* qw,
                                     const double* qF, const double* qfx, const double* qfy,
-                                    const double* work, const int* step_ptr);
+                                    const double* work, const int* step_ptr, double* sup_part);
 cudaError_t rd_launch_mh_serial(int prec, int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                 const Pool& pool, const double* work, const double* wtab,
                                 const int* step_ptr, double kscale, const EventLog& ev);
@@ -235,6 +235,7 @@ struct rd_engine {
   PlanEntry* plan[PM_COUNT] = {};
   PlanHeader* ph[PM_COUNT] = {};
   double* partial = nullptr;
+  double* sup_part = nullptr;   // supply sums per (diode, block of its points)
   int* tickets = nullptr;
   int* item_queue = nullptr;   // dynamic item counters (queue_next / queue_leave): [0..1] planar
                                // MH (part 0 / 1), [2..3] tip MH, [4..5] force, [6..7] supply,
@@ -395,8 +396,8 @@ static int launch_emission(rd_engine* e) {
     e->kernels_in_step++;
   }
   CK(rd_launch_supply_reduce(ns, e->st, e->dP, e->dD, e->qx, e->qy, e->qw, e->qF, e->qfx, e->qfy,
-                             e->work, e->d_step));
-  e->kernels_in_step++;
+                             e->work, e->d_step, e->sup_part));
+  e->kernels_in_step += 2;
   CK(plan(e, PM_MH));
   const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
   // round 0 of the chain start, tiled like a jump; k_mh_init continues the rest
@@ -624,6 +625,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
       e->dalloc(&e->d_npts, S) || e->dalloc(&e->d_zero_off, S) ||
       e->dalloc(&e->partial, (size_t)e->max_items * 3 * RD_ITILE) ||
       e->dalloc(&e->tickets, e->max_items) || e->dalloc(&e->kept, e->max_items) ||
+      e->dalloc(&e->sup_part, (size_t)S * RD_SUP_SPLIT * 2) ||
       e->dalloc(&e->item_queue, 8 + 2 * RD_MH_PARTS) ||
       (cfg->event_capacity > 0 && (e->dalloc(&e->evlog.buf, (size_t)cfg->event_capacity) ||
                                    e->dalloc(&e->evlog.count, 1))) ||
@@ -1519,7 +1521,7 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
                                 e->ph[PM_SUPPLY_TIP], pts, e->partial, e->tickets, e->kscale));
     }
     CK(rd_launch_supply_reduce(S, e->st, e->dP, e->dD, e->qx, e->qy, e->qw, e->qF, e->qfx, e->qfy, e->work,
-                               e->d_step));
+                               e->d_step, e->sup_part));
     CK(cudaEventRecord(ev[1], e->st));
     CK(cudaMemcpyAsync(dyn.data(), e->dD, sizeof(DiodeDyn) * S, cudaMemcpyDeviceToHost, e->st));
     CK(cudaStreamSynchronize(e->st));

@@ -525,27 +525,30 @@ __device__ __forceinline__ long nint_d(double x) {
 
 // N_sup = sum_k w_k A S(F_k), N_round = nint(N_sup + residual) (planar,
 // Do_Field_Emission_Planar_rectangle :282-285) or nint(N_sup) (tip, :488).
-__global__ void k_supply_reduce(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy,
-                                const double* __restrict__ qx, const double* __restrict__ qy,
-                                const double* __restrict__ qw, const double* __restrict__ qF,
-                                const double* __restrict__ qfx, const double* __restrict__ qfy,
-                                const double* __restrict__ work, const int* __restrict__ step_ptr) {
+// The FN supply of a point is FP64 transcendental work, so a diode's points
+// are spread over RD_SUP_SPLIT blocks (contiguous ranges); each block writes
+// its (supply, field) sums and k_supply_finish adds a diode's block sums in
+// block order, so N_sup depends only on the diode's own points.
+__device__ __forceinline__ bool supply_live(const DiodeParams& p, const DiodeDyn& y, const int* step_ptr) {
+  return p.active && p.emission && *step_ptr - y.step_offset > p.emit_delay;   // emitter on (:181)
+}
+
+__global__ void __launch_bounds__(256)
+k_supply_reduce(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy,
+                const double* __restrict__ qx, const double* __restrict__ qy,
+                const double* __restrict__ qw, const double* __restrict__ qF,
+                const double* __restrict__ qfx, const double* __restrict__ qfy,
+                const double* __restrict__ work, const int* __restrict__ step_ptr,
+                double* __restrict__ sup_part) {
   __shared__ double red[256];
-  const int d = blockIdx.x;
+  const int d = blockIdx.x, b = blockIdx.y;
   const DiodeParams& p = P[d];
-  if (!p.active || !p.emission) return;
-  DiodeDyn& y = Dy[d];
-  if (*step_ptr - y.step_offset <= p.emit_delay) {   // the emitter is not on yet (:181)
-    if (threadIdx.x == 0) {
-      y.N_sup = 0.0; y.chains = y.chains_capped = y.chains_failed = 0;
-      y.mh_acc = y.mh_rej = y.mh_done = 0;
-      y.F_avg_z = 0.0; y.df_avg = 0.0;
-    }
-    return;
-  }
+  if (!supply_live(p, Dy[d], step_ptr)) return;
   const int npt = (p.geometry == RD_G_TIP) ? 10000 : p.quad_n * p.quad_n;
+  const int per = (npt + RD_SUP_SPLIT - 1) / RD_SUP_SPLIT;
+  const int k0 = b * per, k1 = min(npt, k0 + per);
   double acc = 0.0, fsum = 0.0;
-  for (int k = threadIdx.x; k < npt; k += blockDim.x) {
+  for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
     double F = qF[p.q_off + k];
     fsum += F;
     if (p.geometry == RD_G_TIP) {   // Field_normal :105-112
@@ -563,25 +566,47 @@ __global__ void k_supply_reduce(const DiodeParams* __restrict__ P, DiodeDyn* __r
       }
     }
   }
-  double N_sup = block_sum(acc, red);
-  __syncthreads();
+  const double N_sup = block_sum(acc, red);
   const double F_sum = block_sum(fsum, red);
   if (threadIdx.x == 0) {
-    y.N_sup = N_sup;
-    y.F_avg_z = p.geometry == RD_G_TIP ? 0.0 : F_sum / npt;   // F_avg, :644-651 (planar)
-    long nr;
-    if (p.geometry == RD_G_TIP) {
-      nr = nint_d(N_sup);
-    } else {
-      nr = nint_d(N_sup + y.residual);
-      y.residual = N_sup - (double)nr;
-    }
-    long M = nr > 0 ? nr : 0;
-    y.chains_capped = M > p.max_chains ? (int)(M - p.max_chains) : 0;
-    y.chains = (int)(M > p.max_chains ? p.max_chains : M);
-    y.chains_failed = 0;
-    y.mh_acc = y.mh_rej = y.mh_done = 0;
+    sup_part[((size_t)d * RD_SUP_SPLIT + b) * 2] = N_sup;
+    sup_part[((size_t)d * RD_SUP_SPLIT + b) * 2 + 1] = F_sum;
   }
+}
+
+__global__ void k_supply_finish(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, int nslots,
+                                const int* __restrict__ step_ptr, const double* __restrict__ sup_part) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nslots) return;
+  const DiodeParams& p = P[d];
+  if (!p.active || !p.emission) return;
+  DiodeDyn& y = Dy[d];
+  if (!supply_live(p, y, step_ptr)) {   // the emitter is not on yet (:181)
+    y.N_sup = 0.0; y.chains = y.chains_capped = y.chains_failed = 0;
+    y.mh_acc = y.mh_rej = y.mh_done = 0;
+    y.F_avg_z = 0.0; y.df_avg = 0.0;
+    return;
+  }
+  const int npt = (p.geometry == RD_G_TIP) ? 10000 : p.quad_n * p.quad_n;
+  double N_sup = 0.0, F_sum = 0.0;
+  for (int b = 0; b < RD_SUP_SPLIT; ++b) {
+    N_sup += sup_part[((size_t)d * RD_SUP_SPLIT + b) * 2];
+    F_sum += sup_part[((size_t)d * RD_SUP_SPLIT + b) * 2 + 1];
+  }
+  y.N_sup = N_sup;
+  y.F_avg_z = p.geometry == RD_G_TIP ? 0.0 : F_sum / npt;   // F_avg, :644-651 (planar)
+  long nr;
+  if (p.geometry == RD_G_TIP) {
+    nr = nint_d(N_sup);
+  } else {
+    nr = nint_d(N_sup + y.residual);
+    y.residual = N_sup - (double)nr;
+  }
+  long M = nr > 0 ? nr : 0;
+  y.chains_capped = M > p.max_chains ? (int)(M - p.max_chains) : 0;
+  y.chains = (int)(M > p.max_chains ? p.max_chains : M);
+  y.chains_failed = 0;
+  y.mh_acc = y.mh_rej = y.mh_done = 0;
 }
 
 // ---- MH chain initialisation: one warp per chain --------------------------------------
@@ -1625,8 +1650,10 @@ cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const Diode
 cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                     const double* qx, const double* qy, const double* qw,
                                     const double* qF, const double* qfx, const double* qfy,
-                                    const double* work, const int* step_ptr) {
-  k_supply_reduce<<<nslots, 256, 0, st>>>(P, Dy, qx, qy, qw, qF, qfx, qfy, work, step_ptr);
+                                    const double* work, const int* step_ptr, double* sup_part) {
+  k_supply_reduce<<<dim3(nslots, RD_SUP_SPLIT), 256, 0, st>>>(P, Dy, qx, qy, qw, qF, qfx, qfy, work, step_ptr,
+                                                              sup_part);
+  k_supply_finish<<<(nslots + 127) / 128, 128, 0, st>>>(P, Dy, nslots, step_ptr, sup_part);
   return cudaGetLastError();
 }
 

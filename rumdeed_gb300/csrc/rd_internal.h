@@ -23,6 +23,7 @@
 #define RD_ITILE 128          // i-particles (or points) per work item
 #define RD_TIP_CPT 2          // tip MH chains per thread (FP32 form; even)
 #define RD_MH_PARTS 2         // planar MH jump launches per jump, one stream each (1..4)
+#define RD_SUP_SPLIT 16       // blocks per diode in the supply reduction
 // j-chunking of pair sums: at least RD_CLEN_MIN particles per chunk, at most
 // RD_NCH_MAX chunks per i-tile
 #define RD_CLEN_MIN 1024

@@ -64,3 +64,28 @@ def test_validate_reports_clean_and_corrupted_state(rg):
     d.set_particles(pos=pos)
     assert all(v == 0 for v in eng.validate().values())
     eng.close()
+
+
+def test_time_verlet_times_both_passes_and_keeps_state_valid(rg):
+    """rd_time_verlet: positive device times for the position and the velocity
+    pass; the passes it runs leave a state that rd_validate finds clean, with
+    the Ramo / mean-velocity sums of the last velocity pass in the counters."""
+    rng = np.random.default_rng(5)
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=3, particle_capacity=3 * 4096, chain_capacity=1024,
+                    quad_capacity=1024)
+    ds = []
+    for k, n in enumerate((1000, 129, 4000)):   # ragged: partial 128-electron items
+        d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, capacity=4096, image_charge=True, N_ic_max=0)
+        d.add_particles(np.column_stack([rng.uniform(-500 * NM, 500 * NM, n), rng.uniform(-500 * NM, 500 * NM, n),
+                                         rng.uniform(450 * NM, 550 * NM, n)]), step=0)
+        d.set_particles(vel=rng.normal(0.0, 1.0e5, (n, 3)))
+        ds.append((d, n))
+    pos_ms, vel_ms = eng.time_verlet(reps=3)
+    assert pos_ms > 0.0 and vel_ms > 0.0
+    assert all(v == 0 for v in eng.validate().values())
+    for d, n in ds:
+        c = d.counters()
+        assert c["n_elec_vel"] == n and c["n_ion_vel"] == 0
+        v = d.particles()["vel"]
+        np.testing.assert_allclose(c["avg_elec_vel"], v.mean(axis=0), rtol=1e-12, atol=1e-9)
+    eng.close()
