@@ -410,7 +410,7 @@ static int launch_emission(rd_engine* e) {
   int rc = launch_mh_jumps(e, s);
   if (rc) return rc;
   CK(rd_launch_emit(ns, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step, e->evlog));
-  e->kernels_in_step++;
+  e->kernels_in_step += 2;
   if (s.emit_serial) {   // serial MH diodes: chains one after another, one block per diode
     CK(rd_launch_mh_serial(prec, ns, e->st, e->dP, e->dD, e->pool, e->work, e->wtab, e->d_step, e->kscale,
                            e->evlog));
@@ -635,7 +635,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   double** chd[] = {&e->cs.x, &e->cs.y, &e->cs.F, &e->cs.sup, &e->cs.df, &e->cs.px, &e->cs.py,
                     &e->cs.pF, &e->cs.tx, &e->cs.ty, &e->cs.tz, &e->cs.pxx, &e->cs.pyy, &e->cs.pzz};
   for (auto p : chd) if (e->dalloc(p, chcap)) return bail(fail(RD_ERR_NOMEM, "chain pool allocation failed"));
-  if (e->dalloc(&e->cs.ok, chcap) || e->dalloc(&e->cs.prop_ok, chcap))
+  if (e->dalloc(&e->cs.ok, chcap) || e->dalloc(&e->cs.prop_ok, chcap) || e->dalloc(&e->cs.em, chcap))
     return bail(fail(RD_ERR_NOMEM, "chain pool allocation failed"));
   for (int m = 0; m < PM_COUNT; ++m)
     if (e->dalloc(&e->plan[m], S) || e->dalloc(&e->ph[m], 1))

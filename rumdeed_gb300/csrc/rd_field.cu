@@ -1326,6 +1326,51 @@ __global__ void k_mh_propose(const DiodeParams* __restrict__ P, const DiodeDyn* 
 // :504-523) and the emitted electrons are appended in that order with
 // Add_Particle semantics (src/mod_pair.F90:29-159): capacity check with a
 // drop count, q = -q0, m = m0, the Beeman history seeded with (q/m) E_vac.
+// Accept test of every chain's final state (Escape_Prob_Planar / _Tip and the
+// uniform draw), spread over RD_EMIT_SPLIT blocks per diode: the FN escape
+// exponent is FP64 transcendental work.  Stores the chain's escape
+// probability (cs.df, the term of df_avg) and whether it emits (cs.em);
+// k_emit then appends in chain order.
+__global__ void __launch_bounds__(256)
+k_emit_test(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, ChainState cs,
+            const int* __restrict__ ch_off, const double* __restrict__ work, const int* __restrict__ step_ptr) {
+  const int d = blockIdx.x;
+  const DiodeParams& p = P[d];
+  if (!p.active || !p.emission || p.mh_serial) return;   // serial diodes emit in k_mh_serial
+  const DiodeDyn& y = Dy[d];
+  const int step = *step_ptr - y.step_offset;
+  const int M = y.chains;
+  for (int c = blockIdx.y * blockDim.x + threadIdx.x; c < M; c += gridDim.y * blockDim.x) {
+    const int k = ch_off[d] + c;
+    double u1, u2;
+    rng2(p.seed, (uint32_t)c, 0u, (uint32_t)step, RNG_EMIT, &u1, &u2);
+    const int ok = cs.ok[k];
+    const double F = cs.F[k];
+    int e = 0;
+    double df;
+    if (p.geometry == RD_G_TIP) {
+      double Df = 0.0;
+      if (ok) {
+        double sq = sqrt(p.tip_phi);   // Escape_Prob_Tip :1734-1758
+        Df = exp(((c_k.b_FN * ((sq * sq) * sq)) * fn_v_y(F, p.tip_phi, p.image_charge)) / fabs(F));
+      }
+      df = Df;
+      e = F < 0.0 && u1 <= Df;
+    } else {
+      const double phi = work_at(p, work, cs.x[k], cs.y[k], nullptr);
+      double D = ok ? fn_escape_log(F, phi, p.image_charge) : -1.79769313486231570e308;
+      if (F >= 0.0) D = -1.79769313486231570e308;
+      df = exp(D);
+      e = log(u1) <= D;
+    }
+    cs.df[k] = df;
+    cs.em[k] = e;
+  }
+}
+
+// Append the emitted electrons of each diode in chain order (one block per
+// diode: block-wide scan of k_emit_test's flags) and average the escape
+// probabilities (df_avg, :354; fixed summation order).
 __global__ void __launch_bounds__(1024)
 k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, ChainState cs,
        const int* __restrict__ ch_off, const double* __restrict__ work,
@@ -1348,36 +1393,9 @@ k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, 
   for (int c0 = 0; c0 < M; c0 += blockDim.x) {
     const int c = c0 + tid, k = ch_off[d] + c;
     int e = 0;
-    double X = 0, Y = 0, Z = 0;
-    int sec = 1;
     if (c < M) {
-      double u1, u2;
-      rng2(p.seed, (uint32_t)c, 0u, (uint32_t)step, RNG_EMIT, &u1, &u2);
-      const int ok = cs.ok[k];
-      const double F = cs.F[k];
-      if (p.geometry == RD_G_TIP) {
-        double Df = 0.0;
-        if (ok) {
-          double sq = sqrt(p.tip_phi);   // Escape_Prob_Tip :1734-1758
-          Df = exp(((c_k.b_FN * ((sq * sq) * sq)) * fn_v_y(F, p.tip_phi, p.image_charge)) / fabs(F));
-        }
-        df_sum += Df;
-        if (F < 0.0 && u1 <= Df) {
-          e = 1;
-          double nx, ny, nz;
-          tip_normal(p, cs.tx[k], cs.ty[k], &nx, &ny, &nz);
-          X = cs.tx[k] + nx * c_k.length_scale;
-          Y = cs.ty[k] + ny * c_k.length_scale;
-          Z = cs.tz[k] + nz * c_k.length_scale;
-        }
-      } else {
-        X = cs.x[k]; Y = cs.y[k];
-        double phi = work_at(p, work, X, Y, &sec);
-        double D = ok ? fn_escape_log(F, phi, p.image_charge) : -1.79769313486231570e308;
-        if (F >= 0.0) D = -1.79769313486231570e308;
-        df_sum += exp(D);
-        if (log(u1) <= D) { e = 1; Z = 1.0 * c_k.length_scale; }
-      }
+      df_sum += cs.df[k];
+      e = cs.em[k];
     }
     // block-wide exclusive scan of e
     unsigned bal = __ballot_sync(0xffffffffu, e);
@@ -1390,6 +1408,19 @@ k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, 
     if (e) {
       int i = n0 + slot;
       if (i < p.cap) {
+        double X, Y, Z;
+        int sec = 1;
+        if (p.geometry == RD_G_TIP) {   // one length scale out along the surface normal
+          double nx, ny, nz;
+          tip_normal(p, cs.tx[k], cs.ty[k], &nx, &ny, &nz);
+          X = cs.tx[k] + nx * c_k.length_scale;
+          Y = cs.ty[k] + ny * c_k.length_scale;
+          Z = cs.tz[k] + nz * c_k.length_scale;
+        } else {
+          X = cs.x[k]; Y = cs.y[k];
+          work_at(p, work, X, Y, &sec);
+          Z = 1.0 * c_k.length_scale;
+        }
         int gi = p.off + i;
         double qm = (-1.0 * c_k.q0) / (1.0 * c_k.m0), ex, ey, ez;
         vacuum_field(p, X, Y, Z, &ex, &ey, &ez);
@@ -1689,6 +1720,7 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
 cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                            const Pool& pool, const ChainState& cs, const int* ch_off,
                            const double* work, const int* step_ptr, const EventLog& ev) {
+  k_emit_test<<<dim3(nslots, RD_EMIT_SPLIT), 256, 0, st>>>(P, Dy, cs, ch_off, work, step_ptr);
   k_emit<<<nslots, 1024, 0, st>>>(P, Dy, pool, cs, ch_off, work, step_ptr, ev);
   return cudaGetLastError();
 }

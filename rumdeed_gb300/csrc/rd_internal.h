@@ -24,6 +24,7 @@
 #define RD_TIP_CPT 2          // tip MH chains per thread (FP32 form; even)
 #define RD_MH_PARTS 2         // planar MH jump launches per jump, one stream each (1..4)
 #define RD_SUP_SPLIT 16       // blocks per diode in the supply reduction
+#define RD_EMIT_SPLIT 8       // blocks per diode in the emission accept test
 // j-chunking of pair sums: at least RD_CLEN_MIN particles per chunk, at most
 // RD_NCH_MAX chunks per i-tile
 #define RD_CLEN_MIN 1024
@@ -153,6 +154,7 @@ struct ChainState {
   double *tx, *ty, *tz;  // tip: cartesian position of the current state
   double *pxx, *pyy, *pzz;  // tip: cartesian position of the proposal
   int *prop_ok;          // proposal inside the domain
+  int *em;               // emits this step (k_emit_test)
   double *gx, *gy;       // planar: Gaussian pair of the next proposal
   // FP32-compensated planar chains: position as FP32 nm offsets from the
   // emitter centre (the chain lives on that grid), log target, Gaussian pair
