@@ -64,7 +64,7 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
                               const int* ch_off, const double* wtab, const int* step_ptr,
                               int it_idx, double* partial, int* tickets, double kscale, int* queue,
-                              int part = 0);
+                              int part = 0, bool lone = false);
 cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                            const Pool& pool, const ChainState& cs, const int* ch_off,
                            const double* work, const int* step_ptr, const EventLog& ev);
@@ -359,7 +359,7 @@ static int launch_mh_jumps(rd_engine* e, const Sig& s) {
         int* queue = q == 0 ? e->item_queue : e->item_queue + 6 + 2 * (q + 1);
         CK(rd_launch_mh_jump(prec, 1, e->grid, sq, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
                              e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, queue,
-                             parts > 1 ? q + 1 : 0));
+                             parts > 1 ? q + 1 : 0, s.mh_planar == 1));
       }
       e->kernels_in_step += parts;
     }
@@ -402,7 +402,8 @@ static int launch_emission(rd_engine* e) {
   const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
   // round 0 of the chain start, tiled like a jump; k_mh_init continues the rest
   CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                       e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue));
+                       e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue,
+                       0, s.mh_planar == 1));
   e->kernels_in_step += ((gmask & 1) ? 1 : 0) + ((gmask & 2) ? 2 : 0);
   CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                        e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
@@ -488,7 +489,7 @@ static std::string sig_string(rd_engine* e) {
   Sig s = signature(e);
   char b[128];
   snprintf(b, sizeof b, "%d%d%d%d%d%d%d%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
-           s.emit_serial, s.tts, s.mh_planar > 1, s.jumps, e->clen_min, e->nch_max);
+           s.emit_serial, s.tts, s.mh_planar > 1 ? 2 : s.mh_planar, s.jumps, e->clen_min, e->nch_max);
   return b;
 }
 
@@ -1193,7 +1194,7 @@ static int time_pair_passes(rd_engine* e, int reps, double* force_ms, double* mh
       CK(plan(e, PM_MH));
       CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                            e->cs, e->d_choff, e->wtab, e->d_step, -1, e->partial, e->tickets, e->kscale,
-                           e->item_queue));
+                           e->item_queue, 0, s.mh_planar == 1));
     }
     CK(cudaEventRecord(e->ev1, e->st));
     CK(cudaEventSynchronize(e->ev1));
@@ -1535,7 +1536,8 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
     CK(plan(e, PM_MH));
     const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
     CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                         e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue));
+                         e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue,
+                         0, s.mh_planar == 1));
     CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                          e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
     CK(cudaEventRecord(ev[2], e->st));

@@ -885,9 +885,11 @@ __device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState&
 // FP32: 32 threads, four chains each, at most 64 registers so that 32 CTAs
 // (the per-SM block limit) are resident: 32 warps instead of the 28 that
 // 72 registers allowed, +1.6 % on the served step; FP64: 128 threads, one
-// chain each.
-template <int PREC>
-__global__ void __launch_bounds__(PREC == 1 ? 32 : RD_ITILE, PREC == 1 ? 32 : 1)
+// chain each.  LONE (FP32, a single emitting planar diode): 64 threads, two
+// chains each, so that a diode's few tiles spread over twice the warps; a
+// chain's sum is the same lane arithmetic in the same j order either way.
+template <int PREC, int LONE>
+__global__ void __launch_bounds__(PREC == 1 ? (LONE ? 64 : 32) : RD_ITILE, PREC == 1 ? (LONE ? 16 : 32) : 1)
 k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
                  const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph, ChainState cs,
                  const int* __restrict__ ch_off, const double* __restrict__ wtab,
@@ -895,7 +897,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
                  int* __restrict__ tickets, double kscale, int* __restrict__ queue, int part) {
   __shared__ int red_i[2 * RD_ITILE];
   __shared__ int s_item;
-  constexpr int CPT = PREC == 1 ? 4 : 1;
+  constexpr int CPT = PREC == 1 ? (LONE ? 2 : 4) : 1;
   const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   const bool init = it_idx == 0;
@@ -1702,11 +1704,13 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
                               const int* ch_off, const double* wtab, const int* step_ptr,
                               int it_idx, double* partial, int* tickets, double kscale, int* queue,
-                              int part) {
-  // part (planar jumps): 0 all items, 1..RD_MH_PARTS one part of the plan (part_range)
+                              int part, bool lone) {
+  // part (planar jumps): 0 all items, 1..RD_MH_PARTS one part of the plan (part_range);
+  // lone: the only emitting planar diode (FP32: the 64-thread form)
   if (geometry_mask & 1) {
-    if (prec == 1) k_mh_jump_planar<1><<<rd_grid(k_mh_jump_planar<1>, 32, grid), 32, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part);
-    else k_mh_jump_planar<0><<<rd_grid(k_mh_jump_planar<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part);
+    if (prec == 1 && lone) k_mh_jump_planar<1, 1><<<rd_grid(k_mh_jump_planar<1, 1>, 64, grid), 64, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part);
+    else if (prec == 1) k_mh_jump_planar<1, 0><<<rd_grid(k_mh_jump_planar<1, 0>, 32, grid), 32, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part);
+    else k_mh_jump_planar<0, 0><<<rd_grid(k_mh_jump_planar<0, 0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part);
   }
   if (geometry_mask & 2) {
     k_mh_propose<<<rd_grid(k_mh_propose, 256, grid), 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx,
