@@ -609,7 +609,7 @@ def case_serve_latency(args):
 
 
 def hbm_peak_gbs():
-    """Measured copy bandwidth of this GPU pool (MEASURED_PEAKS.json), or None."""
+    """Measured HBM copy bandwidth in GB/s (MEASURED_PEAKS.json), or None."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         with open(path) as f:
