@@ -709,6 +709,32 @@ def case_mh_small(args):
     print(json.dumps({"case": "mh-small", **p}), flush=True)
 
 
+def case_one_diode(args):
+    """One planar diode of the reference's one-diode configuration (1 um gap,
+    2 kV, 1000 x 1000 nm emitter, dt 0.25 fs, one image term) at work function
+    --phi and --jumps MH jumps per step, in --precision; no CPU leg and no
+    tuner, so that a profiler sees only the engine's own launches.  Prints
+    device ms per step and the kernels per step."""
+    import rumdeed_gb300 as rg
+    rg.build()
+    side = 1000 * NM
+    prec = rg.PREC_FP64 if args.precision == "fp64" else rg.PREC_FP32C
+    eng = rg.Engine(precision=prec, max_diodes=1, particle_capacity=20064, chain_capacity=20064,
+                    quad_capacity=4096)
+    d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, time_step=0.25e-15, image_charge=True, N_ic_max=0,
+                      capacity=20000, emitter_pos=(-side / 2, -side / 2), emitter_dim=(side, side),
+                      emission=True, seed=SEED, work=[[args.phi]], mh_jumps=args.jumps)
+    eng.run(1, args.warmup)
+    eng.run(args.warmup + 1, args.steps)
+    ms, kps = eng.last_run_stats()
+    c = d.counters()
+    eng.close()
+    print(json.dumps({"case": "one-diode", "precision": args.precision, "work_function_eV": args.phi,
+                      "mh_jumps": args.jumps, "steps": args.steps, "ms_per_step": ms / args.steps,
+                      "steps_per_s": args.steps / (ms / 1e3), "kernels_per_step": kps, "in_flight": c["n"]}),
+          flush=True)
+
+
 def case_plain(args):
     """The plain single-diode deck (CPU-runnable size): gap 1000 nm, 2 kV, a
     1000 x 1000 nm emitter centred on the axis, work function 4.7 eV (and a
@@ -806,7 +832,8 @@ def main():
     ap.add_argument("--plain-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=1.0e10)
     ap.add_argument("--case", default="serve",
-                    choices=["serve", "micro", "burst", "mh-small", "plain", "tips", "serve-latency", "verlet"],
+                    choices=["serve", "micro", "burst", "mh-small", "plain", "tips", "serve-latency", "verlet",
+                             "one-diode"],
                     help="serve: the headline serving benchmark; the others are secondary workloads")
     ap.add_argument("--sizes", default="4096,65536,262144", help="micro: electron counts")
     ap.add_argument("--nics", default="0,7,8", help="micro: N_ic_max values (K = 8 mirror terms read "
@@ -816,6 +843,9 @@ def main():
                     help="serve-latency: every request's step count is divided by this")
     ap.add_argument("--window", type=float, default=60.0, help="serve-latency: seconds of real-time serving")
     ap.add_argument("--verlet-n", type=int, default=1 << 24, help="verlet: electrons in all (64 diodes)")
+    ap.add_argument("--phi", type=float, default=4.7, help="one-diode: work function (eV)")
+    ap.add_argument("--jumps", type=int, default=100, help="one-diode: MH jumps per step")
+    ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"], help="one-diode: engine precision")
     ap.add_argument("--validate-every", type=int, default=0,
                     help="serve-latency: run rd_validate every this many iterations (0: never)")
     ap.add_argument("--fp64-budget", type=float, default=2.0e11,
@@ -832,7 +862,7 @@ def main():
     if args.case != "serve":
         if rank == 0:
             {"micro": case_micro, "burst": case_burst, "mh-small": case_mh_small, "plain": case_plain,
-             "serve-latency": case_serve_latency, "verlet": case_verlet,
+             "serve-latency": case_serve_latency, "verlet": case_verlet, "one-diode": case_one_diode,
              "tips": case_tips}[args.case](args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
