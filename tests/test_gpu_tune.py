@@ -58,6 +58,9 @@ def test_autotune_keeps_state_and_matches_chosen_chunking(rg):
 
 @pytest.mark.parametrize("chunking", [(512, 8), (2048, 32)])
 def test_alone_equals_mix_under_a_chunking(rg, chunking):
+    """A lone emitting diode runs the 64-thread, two-chains-per-thread MH jump
+    form and a mix the 32-thread, four-chain form: the states must still be
+    bit-equal."""
     reqs = make_requests(n=3, seed=5)
     eng, ds = _engine(rg, reqs, chunk_min=chunking[0], chunk_count_max=chunking[1])
     eng.run(1, 4)
