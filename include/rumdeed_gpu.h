@@ -4,8 +4,8 @@
  *
  * The reference (NanoPhysicsCenter/RUMDEED, Fortran 2008) exposes this path
  * as Fortran module procedures that share state through module globals.  Each
- * entry point below replaces one of them; a Fortran iso_c_binding interface
- * module that keeps the old procedure names is given in INTEGRATION.md.
+ * entry point below replaces one of them, and a Fortran iso_c_binding
+ * interface module binds them under the old procedure names.
  *
  * Conventions
  *  - Every function returns an int status: RD_OK (0) or a negative RD_ERR_*.
@@ -230,11 +230,15 @@ int rd_last_run_stats(rd_engine* e, double* ms, int* kernels_per_step);
  * are caller-owned DEVICE buffers, (3, M) doubles each; all working memory
  * of the call is a static 16 MiB device array inside the library, held by
  * every GPU that loads it until the process exits.  M may be at most 65536
- * (RD_ERR_INVALID otherwise).  The first call on a device resolves the array's
- * device address and should come before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race, so issue them one after
- * another.  Returns after the result is written (synchronises the engine
- * stream). */
+ * (RD_ERR_INVALID otherwise).  rd_engine_create does the set-up: it loads the
+ * module that holds the array and the kernels the call launches, and resolves
+ * the array's device address on the engine's device, so no call commits
+ * device memory, even under lazy module loading.  The call runs on the
+ * engine's own stream, which is not ordered after the caller's streams: the
+ * points must be completely written (device- or stream-synchronised) before
+ * the call.  All calls share the array: calls that overlap on the GPU race,
+ * so issue them one after another.  Returns after the result is written
+ * (synchronises the engine stream). */
 int rd_field_at_noalloc(rd_engine* e, int diode, int M, const double* pos3m_dev,
                         double* field3m_dev);
 

@@ -542,6 +542,7 @@ static bool valid_diode(rd_engine* e, int d) {
 
 // ---- helpers for rd_noalloc.cu (C++ linkage, not part of the C ABI) -----------------
 int rd_set_error(int code, const char* msg) { return fail(code, msg); }
+int rd_noalloc_prepare(int device, int prec);   // rd_noalloc.cu
 
 int rd_engine_view(rd_engine* e, int diode, const DiodeParams** P, const DiodeDyn** Dy, Pool* pool,
                    int* geometry, int* precision, int* grid, double* kscale, cudaStream_t* st,
@@ -658,6 +659,8 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   e->ch_alloc.init(chcap);
   e->q_alloc.init(qcap);
   e->w_alloc.init((long long)S * 4 + 4096);
+  // load rd_field_at_noalloc's module and kernels now, so that its calls commit no memory
+  if ((rc = rd_noalloc_prepare(cfg->device, cfg->precision))) return bail(rc);
   *out = e;
   return RD_OK;
 }

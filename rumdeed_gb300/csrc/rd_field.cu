@@ -1671,6 +1671,25 @@ cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st
   return cudaGetLastError();
 }
 
+// Loads the field-at-points kernels of one precision into the current context
+// now (under lazy module loading they would load at their first launch).
+cudaError_t rd_preload_field_points(int prec) {
+  cudaFuncAttributes a;
+  cudaError_t e;
+  if (prec == 1) {
+    if ((e = cudaFuncGetAttributes(&a, k_field_points<1, RD_G_TIP>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&a, k_field_points<1, RD_G_PLANAR>)) != cudaSuccess) return e;
+    rd_grid(k_field_points<1, RD_G_TIP>, RD_ITILE, 0);
+    rd_grid(k_field_points<1, RD_G_PLANAR>, RD_ITILE, 0);
+  } else {
+    if ((e = cudaFuncGetAttributes(&a, k_field_points<0, RD_G_TIP>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&a, k_field_points<0, RD_G_PLANAR>)) != cudaSuccess) return e;
+    rd_grid(k_field_points<0, RD_G_TIP>, RD_ITILE, 0);
+    rd_grid(k_field_points<0, RD_G_PLANAR>, RD_ITILE, 0);
+  }
+  return cudaSuccess;
+}
+
 cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const DiodeParams* P,
                                 const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
                                 const double* qx, const double* qy, const float4* qpp, double* qF,

@@ -21,9 +21,17 @@
 //
 // Limits and sharing:
 //  - at most RD_NOALLOC_MAX_POINTS points per call (larger M is rejected);
-//  - the first call on a device resolves the device address of the array
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture;
+//  - set-up happens when an engine is created (rd_noalloc_prepare, called by
+//    rd_engine_create with the engine's device current): it loads this file's
+//    module -- the array and its kernels -- and the field and planner kernels
+//    the call launches, and resolves the device address of the array
+//    (cudaGetSymbolAddress).  Under lazy module loading (the CUDA default) that
+//    load is where the array's device memory is committed, so it happens
+//    before the caller's time-critical loop, never inside a call;
+//  - the call runs on the engine's own stream, which is not ordered after the
+//    caller's streams: the caller's writes of the points must be complete
+//    (device- or stream-synchronised) before the call; the result is complete
+//    when the call returns;
 //  - all calls share the array and it keeps the last call's contents; the
 //    call clears the tickets it needs at zero itself.  Calls that overlap on
 //    the GPU (other streams, other engines, other host threads) race on the
@@ -62,6 +70,8 @@ cudaError_t rd_launch_field_points(int prec, int geom, int grid, cudaStream_t st
                                    const DiodeParams* P, const Pool& pool, const PlanEntry* plan,
                                    const PlanHeader* ph, const PointSet& pts, double* partial,
                                    int* tickets, double kscale);
+cudaError_t rd_preload_field_points(int prec);
+cudaError_t rd_preload_plan();
 // engine internals needed here (rd_engine.cu)
 int rd_engine_view(rd_engine* e, int diode, const DiodeParams** P, const DiodeDyn** Dy, Pool* pool,
                    int* geometry, int* precision, int* grid, double* kscale, cudaStream_t* st,
@@ -115,6 +125,38 @@ int scratch_for_device(int device, unsigned char** out) {
 
 }  // namespace
 
+// Set-up of the no-allocation path on `device` for an engine of precision
+// `prec` (called by rd_engine_create with that device current): loads the
+// module of this file (array and kernels) and the kernels the call launches,
+// and resolves the array's device address.
+int rd_noalloc_prepare(int device, int prec) {
+  unsigned char* s = nullptr;
+  int rc = scratch_for_device(device, &s);
+  if (rc) return rc;
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, k_na_begin);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_na_end);
+  if (e == cudaSuccess) e = rd_preload_field_points(prec);
+  if (e == cudaSuccess) e = rd_preload_plan();
+  if (e != cudaSuccess) return rd_set_error(RD_ERR_CUDA, cudaGetErrorString(e));
+  return RD_OK;
+}
+
+// Makes `device` current for the lifetime of the object and restores the
+// caller's device afterwards.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceScope(int device) {
+    err = cudaGetDevice(&prev);
+    if (err == cudaSuccess && prev != device) err = cudaSetDevice(device);
+    else if (err == cudaSuccess) prev = -1;   // nothing to restore
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
 extern "C" int rd_field_at_noalloc(rd_engine* e, int diode, int M, const double* pos3m_dev,
                                    double* field3m_dev) {
   if (!e) return rd_set_error(RD_ERR_INVALID, "null engine");
@@ -130,6 +172,8 @@ extern "C" int rd_field_at_noalloc(rd_engine* e, int diode, int M, const double*
   int rc = rd_engine_view(e, diode, &P, &Dy, &pool, &geom, &prec, &grid, &kscale, &st, &device);
   if (rc) return rc;
   if (M == 0) return RD_OK;
+  DeviceScope scope(device);   // the engine's stream and the scratch address belong to its device
+  if (scope.err != cudaSuccess) return rd_set_error(RD_ERR_CUDA, cudaGetErrorString(scope.err));
   unsigned char* s = nullptr;
   if ((rc = scratch_for_device(device, &s))) return rc;
   PlanEntry* plan = (PlanEntry*)(s + NA_OFF_PLAN);

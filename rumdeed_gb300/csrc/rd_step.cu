@@ -528,6 +528,15 @@ cudaError_t rd_launch_plan(cudaStream_t st, const DiodeParams* P, const DiodeDyn
   k_plan<<<1, 1024, 0, st>>>(P, Dy, nslots, mode, chunk_rule, max_items, npts, plan, ph);
   return cudaGetLastError();
 }
+// Loads the planner and the pack kernel into the current context now (they
+// would otherwise load at their first launch under lazy module loading).
+cudaError_t rd_preload_plan() {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, k_plan);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, k_pack);
+  if (e == cudaSuccess) rd_grid(k_pack, RD_ITILE, 0);
+  return e;
+}
 cudaError_t rd_launch_pack(int grid, cudaStream_t st, const DiodeParams* P, const Pool& pool,
                            const PlanEntry* plan, const PlanHeader* ph) {
   k_pack<<<rd_grid(k_pack, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph);
