@@ -123,6 +123,7 @@ def lib():
             "orc_accel_generic": (None, [D, _dp, C.c_int]),
             "orc_accel_planar": (None, [D, _dp, C.c_int]),
             "orc_accel_gather": (None, [D, _dp, C.c_int]),
+            "orc_accel_rows": (None, [D, C.c_int, _ip, _dp, C.c_int]),
             "orc_field_at": (None, [D, _dp, _dp, C.c_int]),
             "orc_field_at_batch": (None, [D, C.c_int, _dp, _dp, C.c_int]),
             "orc_update_position": (None, [D]),
@@ -243,6 +244,18 @@ class OracleDiode:
         out = np.zeros(3 * max(self.s.n, 1))
         getattr(self.L, "orc_accel_" + kind)(self.p, ptr(out), int(compensated))
         return out[:3 * self.s.n].reshape(-1, 3)
+
+    def accel_rows(self, rows, compensated=True):
+        """The gather acceleration of the particles `rows` only, (len(rows), 3)."""
+        rows = np.ascontiguousarray(rows, dtype=np.int32)
+        out = np.zeros(3 * max(len(rows), 1))
+        self.L.orc_accel_rows(self.p, len(rows), rows.ctypes.data_as(_ip), ptr(out), int(compensated))
+        return out[:3 * len(rows)].reshape(-1, 3)
+
+    def add_many(self, pos, species=ELEC, step=1, sec=1):
+        """Add_Particle for every row of pos (velocity 0), in order."""
+        for p in np.ascontiguousarray(pos, dtype=np.float64):
+            self.L.orc_add_particle(self.p, ptr(p), ptr(np.zeros(3)), species, step, sec)
 
     def field_at(self, pts, compensated=True):
         pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)

@@ -509,35 +509,47 @@ void orc_accel_planar(const orc_diode* s, double* acc, int comp) {
  * particle gathers over all others; the image term of the pair is always
  * evaluated with the lower-indexed particle in the (a) role and mirrored in
  * x, y for the higher-indexed one. */
+static void gather_row(const orc_diode* s, int i, double* out3, int comp) {
+  int n = s->n;
+  const double* p1 = s->pos + 3 * i;
+  double q1 = s->charge[i], qd1 = q1 * DIV_FAC_C;
+  nsum a[3] = {{0, 0}, {0, 0}, {0, 0}};
+  for (int j = 0; j < n; ++j) {
+    if (j == i) continue;
+    const double* p2 = s->pos + 3 * j;
+    double pre = qd1 * s->charge[j];
+    double diff[3] = {p1[0] - p2[0], p1[1] - p2[1], p1[2] - p2[2]};
+    double r = sqrt((diff[0] * diff[0] + diff[1] * diff[1]) + diff[2] * diff[2]) + L2;
+    double inv = 1.0 / ((r * r) * r);
+    double t[3];
+    for (int k = 0; k < 3; ++k) t[k] = (pre * inv) * diff[k];
+    if (s->image_charge) {
+      double ic[3], sgn = (j > i) ? 1.0 : -1.0;
+      if (j > i) image_effect(s, p1, p2, ic); else image_effect(s, p2, p1, ic);
+      t[0] += pre * (sgn * ic[0]); t[1] += pre * (sgn * ic[1]); t[2] += pre * ic[2];
+    }
+    for (int k = 0; k < 3; ++k) { if (comp) nadd(&a[k], t[k]); else a[k].s += t[k]; }
+  }
+  double e[3];
+  orc_field_E(s, p1, e);
+  double im1 = 1.0 / s->mass[i];
+  for (int k = 0; k < 3; ++k) out3[k] = (nval(&a[k]) + q1 * e[k]) * im1;
+}
+
 void orc_accel_gather(const orc_diode* s, double* acc, int comp) {
   init_constants();
   int n = s->n;
 #pragma omp parallel for schedule(dynamic, 16)
-  for (int i = 0; i < n; ++i) {
-    const double* p1 = s->pos + 3 * i;
-    double q1 = s->charge[i], qd1 = q1 * DIV_FAC_C;
-    nsum a[3] = {{0, 0}, {0, 0}, {0, 0}};
-    for (int j = 0; j < n; ++j) {
-      if (j == i) continue;
-      const double* p2 = s->pos + 3 * j;
-      double pre = qd1 * s->charge[j];
-      double diff[3] = {p1[0] - p2[0], p1[1] - p2[1], p1[2] - p2[2]};
-      double r = sqrt((diff[0] * diff[0] + diff[1] * diff[1]) + diff[2] * diff[2]) + L2;
-      double inv = 1.0 / ((r * r) * r);
-      double t[3];
-      for (int k = 0; k < 3; ++k) t[k] = (pre * inv) * diff[k];
-      if (s->image_charge) {
-        double ic[3], sgn = (j > i) ? 1.0 : -1.0;
-        if (j > i) image_effect(s, p1, p2, ic); else image_effect(s, p2, p1, ic);
-        t[0] += pre * (sgn * ic[0]); t[1] += pre * (sgn * ic[1]); t[2] += pre * ic[2];
-      }
-      for (int k = 0; k < 3; ++k) { if (comp) nadd(&a[k], t[k]); else a[k].s += t[k]; }
-    }
-    double e[3];
-    orc_field_E(s, p1, e);
-    double im1 = 1.0 / s->mass[i];
-    for (int k = 0; k < 3; ++k) acc[3 * i + k] = (nval(&a[k]) + q1 * e[k]) * im1;
-  }
+  for (int i = 0; i < n; ++i) gather_row(s, i, acc + 3 * i, comp);
+}
+
+/* orc_accel_gather for the listed particles only: acc3 gets (3, nrows), row k
+ * the acceleration of particle rows[k] against all others.  The rows of a
+ * gather are independent, so a sample of them checks a full-size system. */
+void orc_accel_rows(const orc_diode* s, int nrows, const int* rows, double* acc3, int comp) {
+  init_constants();
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int k = 0; k < nrows; ++k) gather_row(s, rows[k], acc3 + 3 * k, comp);
 }
 
 /* Calc_Field_at, src/mod_verlet.F90:1466-1529 */

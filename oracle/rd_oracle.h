@@ -162,6 +162,8 @@ void orc_sphere_ic_field(const orc_diode* s, const double p1[3], const double p2
 void orc_accel_generic(const orc_diode* s, double* acc, int compensated);
 void orc_accel_planar(const orc_diode* s, double* acc, int compensated);
 void orc_accel_gather(const orc_diode* s, double* acc, int compensated);
+/* The gather for the listed particles only: acc3 (3, nrows), row k = particle rows[k]. */
+void orc_accel_rows(const orc_diode* s, int nrows, const int* rows, double* acc3, int compensated);
 
 /* Field at points (Calc_Field_at, :1466-1529; batch semantics :1635-1911) */
 void orc_field_at(const orc_diode* s, const double p[3], double out[3], int compensated);
