@@ -254,20 +254,10 @@ def reduce_ranks(world, maxes, sums):
     return [float(x) for x in mx] + [float(x) for x in sm]
 
 
-def profile_figure(name, key):
-    """A figure from a committed ncu summary under profiles/ (a 'key: value'
-    line), or None when the summary is absent."""
-    path = os.path.join(ROOT, "profiles", name)
-    if not os.path.exists(path):
-        return None
-    for line in open(path):
-        s = line.strip().lstrip("-* ").replace("`", "")
-        if s.startswith(key + ":"):
-            try:
-                return float(s.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+# DRAM bytes (read + write) of one planar MH jump, both halves of the plan, on the 128
+# resident requests of the stream: the mean of jumps 2 and 3 of a one-pass ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum), profiles/k_mh_jump_planar_serve128.md.
+MH_JUMP_DRAM_BYTES = 35.05e6
 
 
 def run_ours(args, rank, world):
@@ -386,7 +376,7 @@ def run_ours(args, rank, world):
     if peak is None:
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
         peak_src = "nominal: 152 SMs x 128 lanes x 2 x 2.07 GHz"
-    traffic = profile_figure("k_mh_jump_planar_serve128.md", "dram_bytes_per_jump")
+    traffic = MH_JUMP_DRAM_BYTES
     plain_v, plain_caps = plain_fp64_sample(rg, resident, budget_s=args.plain_budget)
     cpu_v, cpu_desc, cores, cpu_t = cpu_sample(SEED, rank=rank)
     line = {

@@ -14,7 +14,7 @@ Nothing here runs the reference (it is Fortran and cannot be built here); the
 values are the literals its tests compare against.  The fixture is committed,
 so the tests need only it:
 
-    python tests/golden/extract_reference_golden.py [reference checkout]
+    python tests/golden/extract_reference_golden.py <reference checkout>
 """
 import json
 import os
@@ -22,7 +22,6 @@ import re
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = "/root/reference"
 NUM = r"[-+]?\d+(?:\.\d*)?(?:[dDeE][-+]?\d+)?"
 
 
@@ -88,7 +87,9 @@ def voronoi_unit_test(path):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF
+    if len(sys.argv) != 2:
+        sys.exit("usage: extract_reference_golden.py <path of a RUMDEED checkout>")
+    ref = sys.argv[1]
     tests = os.path.join(ref, "src", "mod_tests.F90")
     work = os.path.join(ref, "src", "mod_work_function.F90")
     out = {
