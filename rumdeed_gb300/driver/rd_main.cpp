@@ -21,10 +21,11 @@
 // EMITTERS_TYPE 1, 2 or 4) and EMISSION_MODE = 3 (hyperboloid tip);
 // ATOM_TIME_INTERVAL > 0 selects the two-time-step integrator.  Extra, optional namelist /gb300/ in the same file: MAX_PARTICLES
 // (default 20000), SEED, PRECISION (0 = FP64, 1 = FP32 compensated), MH_JUMPS,
-// TIP_WORK_FUNCTION (eV, default 4.7 as the reference hard-codes), MH_SERIAL.
-// The MH sampler is serial with MH_SERIAL = 1 or /input/'s MH_BATCH = .False.,
-// batched otherwise (the reference's default, absent MH_BATCH, is serial;
-// this driver's is batched); a ring emitter (EMITTERS_TYPE 4) is always serial.
+// TIP_WORK_FUNCTION (eV, default 4.7 as the reference hard-codes), MH_SERIAL,
+// MAX_CHAINS (MH chains per step at most, default 2^20: in effect every
+// candidate runs, as in the reference).  The MH sampler is the reference's:
+// serial unless /input/ sets MH_BATCH = .True.; MH_SERIAL = 0 or 1 overrides
+// it; a ring emitter (EMITTERS_TYPE 4) is always serial.
 //
 //   rd_main [run directory]
 #include <cctype>
@@ -221,6 +222,11 @@ int main(int argc, char** argv) {
   dc.image_charge = image ? 1 : 0;
   dc.N_ic_max = n_ic;
   dc.capacity = (int)get(gb, "MAX_PARTICLES", 0, 20000.0);
+  // every one of the step's N_round candidates runs a chain, and Add_Particle drops what does
+  // not fit (src/mod_field_emission_v2.F90:283-330, src/mod_pair.F90:37-44); /gb300/ MAX_CHAINS
+  // caps them (the chain pool is sized to it)
+  dc.max_chains = (int)get(gb, "MAX_CHAINS", 0, (double)(1 << 20));
+  if (dc.max_chains < 1) { std::fprintf(stderr, "rd_main: MAX_CHAINS must be positive\n"); return 2; }
   dc.emission = 1;
   dc.mh_jumps = (int)get(gb, "MH_JUMPS", 0, 0.0);
   dc.seed = (unsigned long long)get(gb, "SEED", 0, 20261203.0);
@@ -240,8 +246,10 @@ int main(int argc, char** argv) {
     dc.emitter_pos[1] = get(in, "EMITTERS_POS", 1, 0.0) * length_scale;
     dc.emitter_type = (int)get(in, "EMITTERS_TYPE", 0, 2.0);
     dc.emitter_thickness = get(in, "EMITTERS_DIM", 2, 0.0) * length_scale;   // ring width (0: from V, d)
-    dc.mh_serial = get(gb, "MH_SERIAL", 0, 0.0) != 0.0 ||
-                   (in.count("MH_BATCH") && !to_logical(in.at("MH_BATCH")[0]));
+    // the reference's default sampler is serial: mh_batch = .false. unless the deck sets
+    // MH_BATCH = .true. (src/mod_global.F90:316-328); /gb300/ MH_SERIAL overrides either way
+    dc.mh_serial = in.count("MH_BATCH") ? !to_logical(in.at("MH_BATCH")[0]) : 1;
+    if (gb.count("MH_SERIAL")) dc.mh_serial = get(gb, "MH_SERIAL", 0, 1.0) != 0.0;
     // Read_work_function (src/mod_work_function.F90:53-152): 1 checkerboard
     // (y_num x_num, then the matrix), 2 Gaussian (base, count, then A x y sx sy
     // per line), 4 Voronoi (count, then x y phi section per line)
@@ -293,12 +301,13 @@ int main(int argc, char** argv) {
     std::printf("geometry %d\nV_s %.17g\ngap %.17g\ntime_step %.17g\nsteps %d\nimage_charge %d\n"
                 "N_ic_max %d\ncapacity %d\nseed %llu\nemitter_pos %.17g %.17g\nemitter_dim %.17g %.17g\n"
                 "work %d x %d\nwork_model %d\ntip_dim %.17g %.17g %.17g\nE14.6 %s\nES12.4 %s\n"
-                "emitter_delay %d\nplanes %d\nemitter_type %d\nmh_serial %d\natom_time_interval %d\n",
+                "emitter_delay %d\nplanes %d\nemitter_type %d\nmh_serial %d\natom_time_interval %d\n"
+                "max_chains %d\n",
                 dc.geometry, dc.V_s, dc.gap, dc.time_step, steps, dc.image_charge, dc.N_ic_max,
                 dc.capacity, dc.seed, dc.emitter_pos[0], dc.emitter_pos[1], dc.emitter_dim[0],
                 dc.emitter_dim[1], dc.work_ny, dc.work_nx, dc.work_model, dc.tip_dim[0], dc.tip_dim[1], dc.tip_dim[2],
                 fmt_E(dt / time_scale, 14, 6).c_str(), fmt_ES(dt / time_scale, 12, 4).c_str(), dc.emitter_delay,
-                dc.planes_N, dc.emitter_type, dc.mh_serial, dc.atom_time_interval);
+                dc.planes_N, dc.emitter_type, dc.mh_serial, dc.atom_time_interval, dc.max_chains);
     for (int k = 0; k < dc.planes_N; ++k) std::printf("plane_z %.17g\n", dc.planes_z[k]);
     for (double w : work) std::printf("work_value %.17g\n", w);
     return 0;
@@ -309,8 +318,10 @@ int main(int argc, char** argv) {
   ec.precision = (int)get(gb, "PRECISION", 0, 0.0);
   ec.max_diodes = 1;
   ec.particle_capacity = dc.capacity + 64;
-  ec.chain_capacity = dc.capacity + 64;
-  ec.quad_capacity = 16384;
+  ec.chain_capacity = (long long)dc.max_chains + 64;
+  long long supply_pts = 0;
+  check(rd_supply_points(&dc, &supply_pts), "rd_supply_points");
+  ec.quad_capacity = supply_pts + 64;
   ec.event_capacity = 4 * dc.capacity + 1024;   // emission and absorption records of one step
   rd_engine* e = nullptr;
   check(rd_engine_create(&ec, &e), "rd_engine_create");
@@ -394,7 +405,8 @@ int main(int argc, char** argv) {
   // here the supply rule is a fixed composite Gauss-Legendre rule, so the line gives its panels,
   // nodes, 0 and N_sup (no error estimate: 0)
   FILE* f_integ = std::fopen("out/integration.dt", "w");
-  const int q_panels = dc.quad_panels > 0 ? dc.quad_panels : 16, q_order = dc.quad_order > 0 ? dc.quad_order : 4;
+  const int q_order = dc.quad_order > 0 ? dc.quad_order : 4;   // the rule of rd_supply_points
+  const int q_panels = (int)std::lround(std::sqrt((double)supply_pts)) / q_order;
   // optional files of the namelist's WRITE_POSITION_FILE / WRITE_RAMO_SEC (default off)
   const bool write_pos = in.count("WRITE_POSITION_FILE") && to_logical(in.at("WRITE_POSITION_FILE")[0]);
   const bool write_ramo_sec = in.count("WRITE_RAMO_SEC") && to_logical(in.at("WRITE_RAMO_SEC")[0]);

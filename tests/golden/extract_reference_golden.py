@@ -8,7 +8,10 @@ Reads, as text, the reference's known-answer tests for this path and writes
   Test_FN_Functions among them), keyed by its label, with the line number;
 * the ``E_python`` probe field of Test_Acceleration_Without_Image_Charge;
 * the sites, work functions, test points and expected answers of
-  unit_test_voronoi in src/mod_work_function.F90.
+  unit_test_voronoi in src/mod_work_function.F90;
+* the record layouts (numpy dtypes) and the ramo_current.dt column names of
+  the reference's output reader, scripts/python_package/rumdeed_io.py, which
+  cannot be imported here (it needs pandas).
 
 Nothing here runs the reference (it is Fortran and cannot be built here); the
 values are the literals its tests compare against.  The fixture is committed,
@@ -86,18 +89,42 @@ def voronoi_unit_test(path):
             "expect": [{"w_theta": fnum(a), "tol": fnum(t), "sec": int(s)} for a, t, s in checks]}
 
 
+def reader_layouts(path):
+    """The record layouts of the reference's output reader
+    (scripts/python_package/rumdeed_io.py), read as text: every
+    ``NAME = np.dtype([('field', np.type), ...])`` as a list of (field, numpy
+    type string) pairs, every ``NAME = OTHER`` alias of one, and the column
+    names of ramo_current.dt (RAMO_COLUMNS)."""
+    with open(path) as f:
+        text = f.read()
+    out = {}
+    for m in re.finditer(r"^(\w+)\s*=\s*np\.dtype\(\[(.*?)\]\)", text, re.S | re.M):
+        fields = re.findall(r"\('(\w+)',\s*np\.(\w+)\)", m.group(2))
+        out[m.group(1)] = [[name, "<" + {"float64": "f8", "int32": "i4", "int64": "i8",
+                                          "float32": "f4"}[t]] for name, t in fields]
+    for m in re.finditer(r"^(\w+)\s*=\s*(\w+_DTYPE)\s*$", text, re.M):
+        if m.group(2) in out:
+            out[m.group(1)] = out[m.group(2)]
+    cols = re.search(r"^RAMO_COLUMNS\s*=\s*\[(.*?)\]", text, re.S | re.M)
+    out["RAMO_COLUMNS"] = re.findall(r"'(\w+)'", cols.group(1))
+    return out
+
+
 def main():
     if len(sys.argv) != 2:
         sys.exit("usage: extract_reference_golden.py <path of a RUMDEED checkout>")
     ref = sys.argv[1]
     tests = os.path.join(ref, "src", "mod_tests.F90")
     work = os.path.join(ref, "src", "mod_work_function.F90")
+    reader = os.path.join(ref, "scripts", "python_package", "rumdeed_io.py")
     out = {
         "source": {"assert_close": "src/mod_tests.F90", "E_python": "src/mod_tests.F90",
-                   "voronoi": "src/mod_work_function.F90 (unit_test_voronoi)"},
+                   "voronoi": "src/mod_work_function.F90 (unit_test_voronoi)",
+                   "reader_layouts": "scripts/python_package/rumdeed_io.py"},
         "assert_close": assert_close_literals(tests),
         "E_python": array_literal(tests, "E_python"),
         "voronoi": voronoi_unit_test(work),
+        "reader_layouts": reader_layouts(reader),
     }
     path = os.path.join(HERE, "reference_golden.json")
     with open(path, "w") as f:

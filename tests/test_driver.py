@@ -3,6 +3,7 @@ it reads a RUMDEED input deck (namelist /input/ plus the `work` file) and
 writes the reference's per-step text records.  On CPU: the deck is read as the
 reference reads it; on the GPU: the records agree, step for step, with the
 same run driven through the Python binding."""
+import json
 import os
 import subprocess
 
@@ -11,6 +12,32 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DRIVER = os.path.join(ROOT, "rumdeed_gb300", "_lib", "rd_main")
+
+# The record layouts and ramo_current.dt columns of the reference's own output
+# reader (scripts/python_package/rumdeed_io.py), extracted into the golden
+# fixture: that module needs pandas, which is not installed, so its readers are
+# restated below on its own dtypes.
+with open(os.path.join(ROOT, "tests", "golden", "reference_golden.json")) as _f:
+    LAYOUT = json.load(_f)["reader_layouts"]
+
+
+def reader_dtype(name):
+    return np.dtype([(f, t) for f, t in LAYOUT[name]])
+
+
+def read_records(path, name):
+    """rumdeed_io._read_records: fixed-size records, an empty file gives none."""
+    dt = reader_dtype(name)
+    if os.path.getsize(path) == 0:
+        return np.empty(0, dtype=dt)
+    return np.array(np.memmap(path, dtype=dt, mode="r", order="F"))
+
+
+def read_ramo_current(path):
+    """rumdeed_io.read_ramo_current: whitespace-separated columns named RAMO_COLUMNS."""
+    a = np.loadtxt(path, ndmin=2)
+    assert a.shape[1] == len(LAYOUT["RAMO_COLUMNS"])
+    return {name: a[:, k] for k, name in enumerate(LAYOUT["RAMO_COLUMNS"])}
 
 DECK = """&INPUT
   V_S = 2.0d3,                        ! volts over the gap
@@ -72,6 +99,24 @@ def test_deck_is_read_like_the_reference(driver, tmp_path):
     # Fortran edit descriptors: E14.6 and ES12.4
     assert kv["E14.6"] == ["  0.250000E-03"]
     assert kv["ES12.4"] == ["  2.5000E-04"]
+    # no MH_BATCH in the deck: the reference's serial sampler (mh_batch = .false.,
+    # src/mod_global.F90:316-328), and no cap on the chains below the driver's 2^20 bound
+    assert kv["mh_serial"] == ["1"] and kv["max_chains"] == [str(1 << 20)]
+
+
+def test_sampler_keys(driver, tmp_path):
+    """MH_BATCH = .True. selects the batched sampler; /gb300/ MH_SERIAL and
+    MAX_CHAINS override the defaults."""
+    def cfg(deck):
+        (tmp_path / "input").write_text(deck)
+        (tmp_path / "work").write_text(WORK)
+        out = subprocess.run([driver, "--print-config", str(tmp_path)], capture_output=True, text=True,
+                             check=True).stdout
+        return dict(l.split(" ", 1) for l in out.splitlines())
+    assert cfg(DECK.replace("  PLANES_N = 2,", "  MH_BATCH = .True.,\n  PLANES_N = 2,"))["mh_serial"] == "0"
+    assert cfg(DECK.replace("  PLANES_N = 2,", "  MH_BATCH = .False.,\n  PLANES_N = 2,"))["mh_serial"] == "1"
+    c = cfg(DECK.replace("MH_JUMPS = 40", "MH_JUMPS = 40, MH_SERIAL = 0, MAX_CHAINS = 5000"))
+    assert c["mh_serial"] == "0" and c["max_chains"] == "5000"
 
 
 def test_gaussian_and_voronoi_work_files_are_read(driver, tmp_path):
@@ -105,12 +150,15 @@ def test_driver_run_matches_python_binding(driver, tmp_path, rg):
     top = np.loadtxt(deck / "out" / "absorbed_top.dt")
     bot = np.loadtxt(deck / "out" / "absorbed_bot.dt")
     assert emitted.shape == (12, 5) and top.shape == (12, 6) and bot.shape == (12, 5)
+    # the deck sets no MH_BATCH and no MAX_CHAINS: the reference's serial sampler, every
+    # candidate runs a chain (the driver's chain bound is 2^20)
     eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=3000 + 64,
-                    chain_capacity=3000 + 64, quad_capacity=16384)
+                    chain_capacity=(1 << 20) + 64, quad_capacity=65536)
     d = eng.add_diode(V_s=2.0e3, gap=1000 * 1.0e-9, time_step=2.5e-4 * 1.0e-12, image_charge=True,
                       N_ic_max=0, capacity=3000, emitter_pos=(-500.0 * 1.0e-9, -500.0 * 1.0e-9),
                       emitter_dim=(1000.0 * 1.0e-9, 1000.0 * 1.0e-9), work=[[2.0, 2.2], [2.4, 2.6]], emission=True,
-                      mh_jumps=40, seed=11, emitter_delay=2, planes_z=(200.0 * 1.0e-9, 600.0 * 1.0e-9))
+                      mh_jumps=40, seed=11, emitter_delay=2, planes_z=(200.0 * 1.0e-9, 600.0 * 1.0e-9),
+                      mh_serial=1, max_chains=1 << 20)
     for step in range(1, 13):
         eng.step(step)
         c = d.counters()
@@ -121,30 +169,30 @@ def test_driver_run_matches_python_binding(driver, tmp_path, rg):
         assert top[step - 1][2] == c["absorbed_top_step"] and bot[step - 1][2] == c["absorbed_bot_step"]
     assert emitted[:, 2].sum() > 0          # the deck emits
     eng.close()
-    # binary event files (Fortran stream layouts)
+    # binary event files (Fortran stream layouts), read with the reference reader's record layouts
     out = deck / "out"
-    rec_emit = np.dtype([("pos", "<f8", 3), ("emit", "<i4"), ("sec", "<i4"), ("id", "<i4"), ("species", "<i4")])
-    rec_elec = np.dtype([("pos", "<f8", 3), ("emit", "<i4"), ("id", "<i4")])
-    rec_top = np.dtype([("xy", "<f8", 2), ("vel", "<f8", 3), ("emit", "<i4"), ("sec", "<i4"), ("id", "<i4")])
-    rec_bot = np.dtype([("xy", "<f8", 2), ("emit", "<i4"), ("sec", "<i4"), ("id", "<i4")])
-    assert rec_emit.itemsize == 40 and rec_elec.itemsize == 32 and rec_top.itemsize == 52 and rec_bot.itemsize == 28
-    de = np.fromfile(out / "density_emit.bin", dtype=rec_emit)
-    dl = np.fromfile(out / "density_emit_elec.bin", dtype=rec_elec)
-    dt = np.fromfile(out / "density_absorb_top.bin", dtype=rec_top)
-    db = np.fromfile(out / "density_absorb_bot.bin", dtype=rec_bot)
+    sizes = {k: reader_dtype(k).itemsize for k in ("DENSITY_EMIT_DTYPE", "DENSITY_EMIT_SPECIES_DTYPE",
+                                                   "DENSITY_ABSORB_TOP_DTYPE", "DENSITY_ABSORB_BOT_DTYPE")}
+    assert list(sizes.values()) == [40, 32, 52, 28]
+    de = read_records(out / "density_emit.bin", "DENSITY_EMIT_DTYPE")
+    dl = read_records(out / "density_emit_elec.bin", "DENSITY_EMIT_SPECIES_DTYPE")
+    dt = read_records(out / "density_absorb_top.bin", "DENSITY_ABSORB_TOP_DTYPE")
+    db = read_records(out / "density_absorb_bot.bin", "DENSITY_ABSORB_BOT_DTYPE")
     assert len(de) == len(dl) == emitted[:, 2].sum()
     assert len(dt) == top[:, 2].sum() and len(db) == bot[:, 2].sum()
-    np.testing.assert_allclose(de["pos"][:, 2], 1.0, rtol=1e-12)          # placed 1 nm above the cathode
-    assert np.all(np.abs(de["pos"][:, :2]) <= 500.0 + 1e-9)                # on the emitter
+    np.testing.assert_allclose(de["z"], 1.0, rtol=1e-12)                     # placed 1 nm above the cathode
+    assert np.all(np.abs(de["x"]) <= 500.0 + 1e-9) and np.all(np.abs(de["y"]) <= 500.0 + 1e-9)   # on the emitter
     assert np.all(de["species"] == 1) and np.all(de["emit"] == 1) and np.all(np.diff(de["id"]) > 0)
-    np.testing.assert_array_equal(de["pos"], dl["pos"])
-    assert np.all(dt["vel"][:, 2] > 0.0) if len(dt) else True              # anode hits move up
+    for k in ("x", "y", "z", "emit", "id"):
+        np.testing.assert_array_equal(de[k], dl[k])
+    assert np.all(dt["vz"] > 0.0) if len(dt) else True                      # anode hits move up
     # field.dt: one line per step the emitter is on, F_avg_z < 0, N_sup as in the counters
     fd = np.loadtxt(out / "field.dt")
     assert fd.shape == (12 - 2, 8) and np.all(fd[:, 0] == np.arange(3, 13)) and np.all(fd[:, 3] < 0)
-    # integration.dt: emitter, regions (16 x 16 panels), nodes (64 x 64), fail 0, N_sup, 0, 0
+    # integration.dt: emitter, regions (50 x 50 panels: nodes 5 nm apart over 1000 nm), nodes
+    # (200 x 200), fail 0, N_sup, 0, 0
     ig = np.loadtxt(out / "integration.dt")
-    assert ig.shape == (10, 7) and np.all(ig[:, :4] == [1, 256, 4096, 0])
+    assert ig.shape == (10, 7) and np.all(ig[:, :4] == [1, 2500, 40000, 0])
     np.testing.assert_allclose(ig[:, 4], fd[:, 4], rtol=1e-4)
     # the files the reference creates on every run exist (empty outside their modes)
     for name in ("density_emit_ion.bin", "density_emit_atom.bin", "density_ion.bin", "absorbed_recom.dt",
@@ -152,16 +200,16 @@ def test_driver_run_matches_python_binding(driver, tmp_path, rg):
         assert (out / name).exists(), name
     assert emitted[0, 2] == emitted[1, 2] == 0 and emitted[2:, 2].sum() > 0  # EMITTERS_DELAY = 2
     # planes-1.bin / planes-2.bin: 52-byte records of upward crossings of 200 nm / 600 nm
-    p1 = np.fromfile(out / "planes-1.bin", dtype=rec_top)
-    p2 = np.fromfile(out / "planes-2.bin", dtype=rec_top)
-    assert len(p1) >= len(p2) and np.all(p1["vel"][:, 2] > 0) if len(p1) else True
+    p1 = read_records(out / "planes-1.bin", "PLANES_DTYPE")
+    p2 = read_records(out / "planes-2.bin", "PLANES_DTYPE")
+    assert len(p1) >= len(p2) and np.all(p1["vz"] > 0) if len(p1) else True
     # ramo_current.dt: nrPart / nrElec / nrIon at the velocity update (before removal) equal the
     # electrons in flight that emitted.dt records after the emission of the step
-    ramo = np.loadtxt(out / "ramo_current.dt")
-    assert ramo.shape == (12, 14)
-    np.testing.assert_array_equal(ramo[:, 4], emitted[:, 3])
-    np.testing.assert_array_equal(ramo[:, 5], emitted[:, 3])
-    assert np.all(ramo[:, 6] == 0) and np.all(ramo[:, 7] >= 0)
+    ramo = read_ramo_current(out / "ramo_current.dt")
+    assert len(ramo["step"]) == 12 and np.all(ramo["step"] == np.arange(1, 13))
+    np.testing.assert_array_equal(ramo["nrPart"], emitted[:, 3])
+    np.testing.assert_array_equal(ramo["nrElec"], emitted[:, 3])
+    assert np.all(ramo["nrIon"] == 0) and np.all(ramo["avg_mob"] >= 0)
     # volt.dt: "(ES12.4, tr2, i8, tr2, ES18.8)" with 4 items: time, step, V_d, then V_rf alone on
     # the next record by format reversion (Set_Voltage, src/mod_verlet.F90:2050-2057)
     vl = (out / "volt.dt").read_text().splitlines()
@@ -197,7 +245,7 @@ def test_optional_position_and_section_current_files(driver, tmp_path, rg):
     raw = (opt / "out" / "position.bin").read_bytes()
     head = np.frombuffer(raw[:8], dtype="<i4")
     assert list(head) == [12, 1]
-    rec = np.dtype([("pos", "<f8", 3), ("emit", "<i4"), ("sec", "<i4"), ("id", "<i4")])
+    rec = reader_dtype("POSITION_PARTICLE_DTYPE")   # rumdeed_io.read_position_step's records
     off = 8
     for step in range(1, 13):
         st, n = np.frombuffer(raw[off:off + 8], dtype="<i4")
@@ -213,16 +261,15 @@ def test_optional_position_and_section_current_files(driver, tmp_path, rg):
     assert off == len(raw)
     # init.bin (Write_Initial_Variables): 7 float64 then 4 int32; the reference's readers take the
     # ramo_current.bin dimensions from it
-    init = np.fromfile(opt / "out" / "init.bin", dtype=np.dtype(
-        [("scales", "<f8", 7), ("MAX_PARTICLES", "<i4"), ("MAX_EMITTERS", "<i4"), ("MAX_SECTIONS", "<i4"),
-         ("MAX_LIFE_TIME", "<i4")]))
+    init = np.fromfile(opt / "out" / "init.bin", dtype=reader_dtype("INIT_DTYPE"), count=1)   # read_init
     assert len(init) == 1 and (opt / "out" / "init.bin").stat().st_size == 72
-    np.testing.assert_allclose(init["scales"][0], [1, 1, 1, 1e-9, 1e-12, 1e3, 1])
+    np.testing.assert_allclose([init[k][0] for k in ("epsilon_r", "m_eeff", "m_ieff", "length_scale", "time_scale",
+                                                     "vel_scale", "cur_scale")], [1, 1, 1, 1e-9, 1e-12, 1e3, 1])
     assert (init["MAX_PARTICLES"][0], init["MAX_EMITTERS"][0], init["MAX_SECTIONS"][0]) == (3000, 1, 96 * 96)
     assert (opt / "out" / "ramo_current.bin").stat().st_size == 96 * 96 * 1 * 12 * 8
     rs = np.fromfile(opt / "out" / "ramo_current.bin", dtype="<f8").reshape(12, 96 * 96)
-    ramo = np.loadtxt(opt / "out" / "ramo_current.dt")
-    np.testing.assert_allclose(rs.sum(axis=1), ramo[:, 11], rtol=1e-4, atol=1e-30)   # ES12.4 text
+    ramo = read_ramo_current(opt / "out" / "ramo_current.dt")
+    np.testing.assert_allclose(rs.sum(axis=1), ramo["ramo_elec"], rtol=1e-4, atol=1e-30)   # ES12.4 text
     assert np.all(rs[:, 4:] == 0.0) and np.abs(rs).sum() > 0
 
 
@@ -252,7 +299,7 @@ def test_stop_signal_ends_the_run_cleanly(driver, tmp_path):
 @pytest.mark.gpu
 def test_event_log_counts_and_loss(rg):
     eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=3000 + 64,
-                    chain_capacity=3000 + 64, quad_capacity=16384, event_capacity=8)
+                    chain_capacity=3000 + 64, quad_capacity=65536, event_capacity=8)
     d = eng.add_diode(V_s=2.0e3, gap=1000 * 1.0e-9, time_step=2.5e-4 * 1.0e-12, image_charge=True,
                       N_ic_max=0, capacity=3000, emitter_pos=(-500.0 * 1.0e-9, -500.0 * 1.0e-9),
                       emitter_dim=(1000.0 * 1.0e-9, 1000.0 * 1.0e-9), work=[[2.0, 2.2], [2.4, 2.6]],
