@@ -133,6 +133,8 @@ def lib():
             "orc_accel_tts": (None, [D, C.c_int, C.c_int]),
             "orc_update_velocity_tts": (None, [D, C.c_int]),
             "orc_supply_integral_planar": (C.c_double, [D]),
+            "orc_supply_panels": (C.c_int, [D]),
+            "orc_supply_planar_converged": (C.c_double, [D, C.c_double, C.c_int, C.POINTER(C.c_longlong)]),
             "orc_mh_batch_planar": (None, [D, C.c_int, C.c_int, _dp, _dp, _dp, _ip]),
             "orc_do_emission_planar": (C.c_int, [D, C.c_int]),
             "orc_supply_tip": (C.c_double, [D]),
@@ -292,6 +294,13 @@ class OracleDiode:
         if self.s.geometry == TIP:
             return self.L.orc_supply_tip(self.p)
         return self.L.orc_supply_integral_planar(self.p)
+
+    def supply_converged(self, tol=0.01, max_depth=12):
+        """The planar supply integral integrated adaptively to convergence:
+        (N_sup, integrand evaluations)."""
+        ev = C.c_longlong()
+        v = self.L.orc_supply_planar_converged(self.p, tol, max_depth, C.byref(ev))
+        return v, ev.value
 
     def mh_batch(self, step, M):
         df = np.zeros(max(M, 1)); F = np.zeros(max(M, 1)); P = np.zeros(3 * max(M, 1))

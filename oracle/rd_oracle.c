@@ -245,7 +245,7 @@ orc_diode* orc_diode_new(int geometry, int cap, double V_s, double d, double tim
   s->a_rate = 1.0;
   s->mh_jumps = 200;
   s->max_chains = 1 << 30;
-  s->quad_panels = 16;
+  s->quad_panels = 0;   /* 0: orc_supply_panels, nodes at most 5 nm apart */
   s->quad_order = 4;
   s->init_rounds_max = 10000;
   for (int i = 0; i < cap; ++i) s->mask[i] = 1;
@@ -947,8 +947,25 @@ static void gauss_legendre(int n, double* x, double* w) {
  * Integration_FE, src/mod_field_emission_v2.F90:635-656 with the integrand
  * integrand_cuba_fe_v :668-745), by a composite Gauss-Legendre rule in place
  * of the third-party Cuba library. */
+/* Panels per side of the supply rule when none are set: Gauss-Legendre nodes at
+ * most 5 nm apart along the emitter's longer side (a ring: the longer of its
+ * outer circumference and its width), 16 to 256 panels -- the GPU library's
+ * default rule, stated identically. */
+int orc_supply_panels(const orc_diode* s) {
+  if (s->quad_panels > 0) return s->quad_panels;
+  int Q = s->quad_order > 0 ? s->quad_order : 4;
+  double L = s->em_dim[0] > s->em_dim[1] ? s->em_dim[0] : s->em_dim[1];
+  if (s->emitter_type == 4) {
+    double c = 2.0 * 3.14159265358979323846 * (s->ring_rmin + s->ring_thick);
+    L = c > s->ring_thick ? c : s->ring_thick;
+  }
+  double r = L / (Q * 5.0e-9);
+  int P = (int)ceil(r * (1.0 - 1e-12));
+  return P < 16 ? 16 : (P > 256 ? 256 : P);
+}
+
 double orc_supply_integral_planar(orc_diode* s) {
-  int P = s->quad_panels, Q = s->quad_order;
+  int P = orc_supply_panels(s), Q = s->quad_order;
   double gx[16], gw[16];
   gauss_legendre(Q, gx, gw);
   double A = s->em_dim[0] * s->em_dim[1];
@@ -986,6 +1003,104 @@ double orc_supply_integral_planar(orc_diode* s) {
   s->F_avg_z = nval(&ftot) / (double)(npt * npt);   /* F_avg, fe_v2:644-651 */
   free(val); free(fz);
   return nval(&tot);
+}
+
+/* ---- converged supply integral (checker of the quadrature rules) ---------------
+ * The same integrand as orc_supply_integral_planar, integrated adaptively to a
+ * converged value: every panel of the P x P rule is bisected into 2 x 2
+ * children while the Q x Q Gauss-Legendre sums of parent and children differ
+ * by more than the panel's share of `tol` (halved at each level), and also
+ * while an electron whose height h is below half the panel width lies within
+ * the panel widened by 4 h -- the field of such an electron varies on the
+ * scale h, below the node spacing, where no error estimate can see it.  At
+ * most max_depth levels.  This stands in for the adaptive integrator of the
+ * reference (Cuba Divonne, asked for max(0.5 electron, 1e-3 N_sup),
+ * src/mod_global.F90:84-92) as the value a rule must reproduce. */
+typedef struct {
+  const orc_diode* s;
+  const double* nx; const double* ny; const double* nh; int nn;   /* electrons below the cut */
+  double gx[16], gw[16];
+  int Q, max_depth;
+  long long evals;
+} adapt_ctx;
+
+static double supply_point(const orc_diode* s, double x, double y) {
+  double p[3] = {x, y, 0.0}, f[3];
+  orc_field_at(s, p, f, 1);
+  if (f[2] >= 0.0) return 0.0;
+  double phi = work_at(s, x, y, NULL);
+  return s->em_dim[0] * s->em_dim[1] * orc_elec_supply_v2(f[2], phi, s->image_charge, s->time_step);
+}
+
+/* Q x Q Gauss-Legendre sum over [x0, x0 + hx] x [y0, y0 + hy], in units of the
+ * emitter area (weights as the P x P rule's) */
+static double panel_sum(adapt_ctx* c, double x0, double y0, double hx, double hy) {
+  const orc_diode* s = c->s;
+  double t = 0.0;
+  for (int iy = 0; iy < c->Q; ++iy)
+    for (int ix = 0; ix < c->Q; ++ix) {
+      double x = x0 + 0.5 * (c->gx[ix] + 1.0) * hx, y = y0 + 0.5 * (c->gx[iy] + 1.0) * hy;
+      t += (0.25 * c->gw[ix] * c->gw[iy]) * (hx * hy) / (s->em_dim[0] * s->em_dim[1]) * supply_point(s, x, y);
+      c->evals++;
+    }
+  return t;
+}
+
+static int panel_has_low_electron(const adapt_ctx* c, double x0, double y0, double hx, double hy) {
+  double w = hx > hy ? hx : hy;
+  for (int j = 0; j < c->nn; ++j) {
+    double h = c->nh[j];
+    if (h >= 0.5 * w) continue;
+    double m = 4.0 * h;
+    if (c->nx[j] >= x0 - m && c->nx[j] <= x0 + hx + m && c->ny[j] >= y0 - m && c->ny[j] <= y0 + hy + m)
+      return 1;
+  }
+  return 0;
+}
+
+static double adapt_panel(adapt_ctx* c, double x0, double y0, double hx, double hy, double whole,
+                          double tol, int depth) {
+  double hx2 = 0.5 * hx, hy2 = 0.5 * hy, q[4];
+  q[0] = panel_sum(c, x0, y0, hx2, hy2);
+  q[1] = panel_sum(c, x0 + hx2, y0, hx2, hy2);
+  q[2] = panel_sum(c, x0, y0 + hy2, hx2, hy2);
+  q[3] = panel_sum(c, x0 + hx2, y0 + hy2, hx2, hy2);
+  double kids = (q[0] + q[1]) + (q[2] + q[3]);
+  if (depth >= c->max_depth) return kids;
+  int low = panel_has_low_electron(c, x0, y0, hx, hy);
+  if (!low && fabs(kids - whole) <= tol) return kids;
+  double x[4] = {x0, x0 + hx2, x0, x0 + hx2}, y[4] = {y0, y0, y0 + hy2, y0 + hy2}, t = 0.0;
+  for (int k = 0; k < 4; ++k) t += adapt_panel(c, x[k], y[k], hx2, hy2, q[k], 0.5 * tol, depth + 1);
+  return t;
+}
+
+double orc_supply_planar_converged(orc_diode* s, double tol, int max_depth, long long* evals) {
+  init_constants();
+  int P = orc_supply_panels(s), Q = s->quad_order > 0 ? s->quad_order : 4;
+  int n = s->n, nn = 0;
+  double* buf = (double*)malloc(sizeof(double) * 3 * (n > 0 ? n : 1));
+  double *nx = buf, *ny = buf + n, *nh = buf + 2 * n;
+  double wmax = (s->em_dim[0] > s->em_dim[1] ? s->em_dim[0] : s->em_dim[1]) / P;
+  for (int j = 0; j < n; ++j) {
+    if (s->species[j] == ORC_ATOM) continue;
+    double h = s->pos[3 * j + 2];
+    if (h > 0.0 && h < 0.5 * wmax) { nx[nn] = s->pos[3 * j]; ny[nn] = s->pos[3 * j + 1]; nh[nn] = h; nn++; }
+  }
+  double hx = s->em_dim[0] / P, hy = s->em_dim[1] / P, tot = 0.0;
+  long long ev = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : tot, ev)
+  for (int k = 0; k < P * P; ++k) {
+    adapt_ctx c;
+    c.s = s; c.nx = nx; c.ny = ny; c.nh = nh; c.nn = nn; c.Q = Q; c.max_depth = max_depth; c.evals = 0;
+    gauss_legendre(Q, c.gx, c.gw);
+    double x0 = s->em_pos[0] + (k % P) * hx, y0 = s->em_pos[1] + (k / P) * hy;
+    double whole = panel_sum(&c, x0, y0, hx, hy);
+    tot += adapt_panel(&c, x0, y0, hx, hy, whole, tol / (P * P), 0);
+    ev += c.evals;
+  }
+  free(buf);
+  if (evals) *evals = ev;
+  return tot;
 }
 
 static long nint_f(double x) { return (long)(x >= 0 ? floor(x + 0.5) : -floor(-x + 0.5)); }

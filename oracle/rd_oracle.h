@@ -183,6 +183,15 @@ void orc_update_velocity_tts(orc_diode* s, int step);
 
 /* Emission (device algorithm restated with the shared Philox streams) */
 double orc_supply_integral_planar(orc_diode* s);
+/* Panels per side of the planar supply rule: quad_panels, or when 0 the
+ * resolution rule (nodes at most 5 nm apart, 16 to 256 panels). */
+int orc_supply_panels(const orc_diode* s);
+/* The same supply integral integrated adaptively to convergence (rectangle
+ * emitter): panels of the quad_panels x quad_order rule bisected while their
+ * Gauss-Legendre sums change by more than their share of tol (electrons) or
+ * while an electron lower than half a panel width sits over them; at most
+ * max_depth levels.  evals gets the integrand evaluations. */
+double orc_supply_planar_converged(orc_diode* s, double tol, int max_depth, long long* evals);
 void orc_mh_batch_planar(orc_diode* s, int step, int M, double* df_out, double* F_out,
                          double* pos_out, int* ok_out);
 int orc_do_emission_planar(orc_diode* s, int step);
