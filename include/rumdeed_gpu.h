@@ -78,7 +78,9 @@ typedef struct {
   int emission;            /* 0: no emission; 1: Fowler-Nordheim field emission */
   int mh_jumps;            /* 0: reference default (200 planar, 80 tip) */
   int max_chains;          /* MH chains per step at most (0: capacity) */
-  int quad_panels;         /* planar supply rule: panels per side (0: 16) */
+  int quad_panels;         /* planar supply rule: panels per side (0: enough panels for nodes at
+                              most 5 nm apart along the longer emitter side, 16 to 256; see
+                              rd_supply_points) */
   int quad_order;          /* planar supply rule: Gauss-Legendre order (0: 4) */
   int init_rounds;         /* MH start-position rounds (0: 10000 as the reference) */
   unsigned long long seed; /* Philox key of this diode */
@@ -173,6 +175,14 @@ int rd_accel(rd_engine* e, int diode, double* acc3n);
 /* Calc_Field_at_Batch (src/mod_verlet.F90:1635-1911): field (V/m) at M
  * points of one diode. */
 int rd_field_at(rd_engine* e, int diode, int M, const double* pos3m, double* field3m);
+
+/* Supply quadrature points a diode of this configuration takes in the
+ * engine's quadrature table (rd_engine_config.quad_capacity): (panels x
+ * order)^2 for a planar emitter, 10000 for a tip, 0 without emission.  The
+ * supply integral (Do_Surface_Integration_FE, src/mod_field_emission_v2.F90:
+ * 635-656) is a composite Gauss-Legendre rule here in place of the reference's
+ * adaptive Cuba integrator. */
+int rd_supply_points(const rd_diode_config* c, long long* npts);
 
 /* Mark_Particles_Remove (src/mod_pair.F90:169-339), for tests and drivers. */
 int rd_mark_remove(rd_engine* e, int diode, int index, int why);
@@ -274,6 +284,15 @@ int rd_time_field_at(rd_engine* e, int diode, int M, const double* pos3m, int re
  * (positions, velocities, histories): a measurement of the HBM-bound kernels
  * on a snapshot that is thrown away. */
 int rd_time_verlet(rd_engine* e, int reps, double* position_ms, double* velocity_ms);
+/* rd_time_remove: device time of one Beeman position pass (which marks the
+ * particles that crossed an electrode, Check_Boundary_Planar ->
+ * Mark_Particles_Remove) and of the removal that follows it (the stable
+ * compaction of Remove_Particles, src/mod_pair.F90:352-562, with its life-time
+ * record), one launch each, CUDA events on the engine stream.  moved gets the
+ * survivors the compaction moved (those behind a diode's first removed
+ * particle), removed the particles removed.  Advances the state like the two
+ * phases of a step, without the force and velocity passes. */
+int rd_time_remove(rd_engine* e, double* position_ms, double* remove_ms, long long* moved, long long* removed);
 
 /* ---- event log: emission and absorption records ------------------------------
  * The reference writes one record per emitted particle (density_emit.bin and
@@ -307,16 +326,28 @@ int rd_events_take(rd_engine* e, int cap, rd_event* out, int* n_out, long long* 
  * FP32 bits.  rd_autotune times every candidate chunking on the diodes
  * resident now -- the force pass and a dry MH pass (the field at every
  * chain's current point, nothing written) weighted by the jump count --
- * keeps the fastest, rebuilds the step graph and leaves the particle state
- * as it was.  rd_set_chunking sets one directly (0 = default). */
+ * keeps the fastest, then times the MH launch shapes (rd_set_mh_launch) under
+ * it, rebuilds the step graph and leaves the particle state as it was.
+ * rd_set_chunking sets one directly (0 = default).  The i-tile width (128
+ * particles, points or chains per work item) is fixed. */
 typedef struct {
   int chunk_min, chunk_count_max;   /* the chosen chunking */
   double ms_default, ms_chosen;     /* estimated step pair-sum time under the default / chosen */
   int candidates;
+  int mh_parts, mh_form;            /* the chosen MH launch shape (rd_set_mh_launch) */
 } rd_tune_result;
 int rd_autotune(rd_engine* e, rd_tune_result* out);
 int rd_set_chunking(rd_engine* e, int chunk_min, int chunk_count_max);
 int rd_get_chunking(rd_engine* e, int* chunk_min, int* chunk_count_max);
+/* Launch shape of the planar MH jumps, which changes no result: `parts`
+ * launches per jump on as many streams, each over a part of the work plan cut
+ * at diode boundaries (1..4; 0 = 2, used only when two or more diodes run
+ * batched chains), and the FP32 thread form (0: 32 threads x 4 chains per
+ * 128-chain tile, 1: 64 threads x 2 chains; -1 = form 1 for a single emitting
+ * planar diode, else form 0).  rd_autotune searches both after the chunking;
+ * rd_get_mh_launch reports what the next step uses. */
+int rd_set_mh_launch(rd_engine* e, int parts, int form);
+int rd_get_mh_launch(rd_engine* e, int* parts, int* form);
 
 /* ---- serving: continuous batching of diode simulations ---------------------
  * The reference runs one simulation per process.  Requests queue in FIFO

@@ -133,7 +133,7 @@ class ServeStats(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("chunk_min", C.c_int), ("chunk_count_max", C.c_int), ("ms_default", C.c_double),
-                ("ms_chosen", C.c_double), ("candidates", C.c_int)]
+                ("ms_chosen", C.c_double), ("candidates", C.c_int), ("mh_parts", C.c_int), ("mh_form", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -184,6 +184,11 @@ SIGNATURES = {
     "rd_events_take": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Event), _ip, C.POINTER(C.c_longlong)]),
     "rd_set_chunking": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "rd_get_chunking": (C.c_int, [C.c_void_p, _ip, _ip]),
+    "rd_set_mh_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "rd_time_remove": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                 C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "rd_supply_points": (C.c_int, [C.POINTER(DiodeConfig), C.POINTER(C.c_longlong)]),
+    "rd_get_mh_launch": (C.c_int, [C.c_void_p, _ip, _ip]),
     "rd_validate": (C.c_int, [C.c_void_p, _ip, C.POINTER(C.c_longlong)]),
     "rd_diode_state_size": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_longlong)]),
     "rd_diode_save": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]),
@@ -340,12 +345,29 @@ class Engine:
         _check(self.L.rd_get_chunking(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def set_mh_launch(self, parts=0, form=-1):
+        """Planar MH launch shape (rd_set_mh_launch): plan parts and FP32 thread form."""
+        _check(self.L.rd_set_mh_launch(self.h, parts, form))
+
+    def get_mh_launch(self):
+        a, b = C.c_int(), C.c_int()
+        _check(self.L.rd_get_mh_launch(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def time_verlet(self, reps=5):
         """Device ms of one position pass and of one velocity pass (rd_time_verlet;
         advances the state)."""
         a, b = C.c_double(), C.c_double()
         _check(self.L.rd_time_verlet(self.h, reps, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def time_remove(self):
+        """One position pass and the removal after it (rd_time_remove): (position ms,
+        removal ms, survivors moved, particles removed)."""
+        a, b = C.c_double(), C.c_double()
+        m, r = C.c_longlong(), C.c_longlong()
+        _check(self.L.rd_time_remove(self.h, C.byref(a), C.byref(b), C.byref(m), C.byref(r)))
+        return a.value, b.value, m.value, r.value
 
     def time_accel(self, reps=3):
         """Device milliseconds of one force evaluation of all resident diodes."""
@@ -451,6 +473,15 @@ def diode_config(geometry=GEOM_PLANAR, V_s=2.0e3, gap=1000e-9, time_step=0.25e-1
     cfg.init_rounds = init_rounds
     cfg.seed = seed
     return cfg, keep
+
+
+def supply_points(**kw):
+    """rd_supply_points: quadrature points a diode of this configuration takes."""
+    cfg, keep = diode_config(**kw)
+    n = C.c_longlong()
+    _check(lib().rd_supply_points(C.byref(cfg), C.byref(n)))
+    del keep
+    return n.value
 
 
 class Diode:

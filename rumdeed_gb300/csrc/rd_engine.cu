@@ -55,6 +55,10 @@ cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodePara
 cudaError_t rd_launch_mh_serial(int prec, int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                 const Pool& pool, const double* work, const double* wtab,
                                 const int* step_ptr, double kscale, const EventLog& ev);
+cudaError_t rd_launch_mh_cond(cudaStream_t st, cudaGraphConditionalHandle h, const PlanHeader* ph);
+cudaError_t rd_launch_mh_vacuum(int prec, int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                                const ChainState& cs, const int* ch_off, const double* wtab, const int* step_ptr,
+                                double kscale);
 cudaError_t rd_launch_mh_init(int prec, int grid, cudaStream_t st, const DiodeParams* P,
                               DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
                               const PlanHeader* ph, const ChainState& cs, const int* ch_off,
@@ -64,7 +68,7 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
                               const int* ch_off, const double* wtab, const int* step_ptr,
                               int it_idx, double* partial, int* tickets, double kscale, int* queue,
-                              int part = 0, bool lone = false);
+                              int part = 0, int nparts = 1, int form = 0);
 cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                            const Pool& pool, const ChainState& cs, const int* ch_off,
                            const double* work, const int* step_ptr, const EventLog& ev);
@@ -90,6 +94,8 @@ cudaError_t rd_launch_step_inc(cudaStream_t st, int* step_ptr);
 cudaError_t rd_launch_add_particles(cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                     const Pool& pool, int d, int cnt, const double* pos,
                                     const double* vel, const int* species, int step, int section);
+cudaError_t rd_launch_quad_fill(cudaStream_t st, const QuadSpec& q, double* qx, double* qy, double* qz,
+                                double* qw, float4* qpp);
 cudaError_t rd_launch_mark(cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy, const Pool& pool,
                            int d, int i, int why);
 cudaError_t rd_launch_validate(int nslots, cudaStream_t st, const DiodeParams* P, const DiodeDyn* Dy,
@@ -214,9 +220,11 @@ struct rd_engine {
   rd_engine_config cfg{};
   int sms = 0, grid = 0;
   cudaStream_t st = nullptr;
-  cudaStream_t stp[RD_MH_PARTS] = {};    // planar MH jump parts 2.. (part 1 runs on st)
-  cudaEvent_t ev_fork = nullptr;         // st -> the part streams
-  cudaEvent_t ev_join[RD_MH_PARTS] = {}; // each part stream -> st
+  cudaStream_t stp[RD_MH_PARTS_MAX] = {};    // planar MH jump parts 2.. (part 1 runs on st)
+  cudaEvent_t ev_fork = nullptr;             // st -> the part streams
+  cudaEvent_t ev_join[RD_MH_PARTS_MAX] = {}; // each part stream -> st
+  int mh_parts = 0;   // planar MH launches per jump when two or more diodes run batched chains (0: RD_MH_PARTS)
+  int mh_form = -1;   // FP32 MH jump form: 0 32 threads x 4 chains, 1 64 x 2 (-1: 1 for a lone diode, else 0)
   RdConst k{};
   double kscale = 0.0;
   int max_items = 0;
@@ -239,7 +247,7 @@ struct rd_engine {
   int* tickets = nullptr;
   int* item_queue = nullptr;   // dynamic item counters (queue_next / queue_leave): [0..1] planar
                                // MH (part 0 / 1), [2..3] tip MH, [4..5] force, [6..7] supply,
-                               // [6 + 2p .. 7 + 2p] planar MH part p >= 2
+                               // [6 + 2p .. 7 + 2p] planar MH part p >= 2 (8 + 2 RD_MH_PARTS_MAX)
   EventLog evlog{nullptr, nullptr, 0};   // emission / absorption records (rd_events_take)
   int* kept = nullptr;
   double* ramo = nullptr;   // velocity-pass item partials (10 per 128-particle item)
@@ -252,6 +260,18 @@ struct rd_engine {
   double* stage_hd = nullptr;   // pinned host mirrors of stage_d / stage_i: uploads are DMA
   int* stage_hi = nullptr;      // copies from page-locked memory
   long long stage_cap = 0;
+  // overlapped admission (rd_serve): uploads on stream sa from a pinned arena into a device
+  // arena, slots activated on st before the next step (activate_pending)
+  cudaStream_t sa = nullptr;
+  cudaStream_t sbody = nullptr;     // captures the body of the step graph's conditional MH node
+  cudaEvent_t ev_adm = nullptr;
+  unsigned char* adm_h = nullptr;   // pinned
+  unsigned char* adm_d = nullptr;
+  size_t adm_cap = 0, adm_used = 0;
+  DiodeParams* act_P = nullptr;     // pinned, per slot: the parameters to activate
+  DiodeDyn* act_D = nullptr;        // pinned, per slot
+  int *act_choff = nullptr, *act_qoff = nullptr;   // pinned, per slot
+  std::vector<int> pending;         // slots written on sa, not yet active
   // host
   std::vector<SlotHost> slots;
   RangeAlloc pool_alloc, ch_alloc, q_alloc, w_alloc;
@@ -289,6 +309,29 @@ struct rd_engine {
   // captured step graph stays valid while requests come and go.
   int nslots_hw() const { return cfg.max_diodes; }
 };
+
+extern "C" {
+static int flush_admissions(rd_engine* e);   // defined in the C ABI block below
+}
+
+// Panels per side of the planar supply rule when the diode does not set them:
+// Gauss-Legendre nodes at most RD_SUPPLY_SPACING apart along the emitter's
+// longer side (for a ring, the longer of its outer circumference and its
+// width), between 16 and 256 panels.  The supply integrand varies on the scale
+// of the emission height (1 nm): an electron that sits there removes a disc of
+// a few nm^2 from the emitting area, and a coarser rule sees it only when a
+// node happens to fall inside.  Against the converged integral of
+// space-charge-limited states this spacing keeps N_sup within max(0.5,
+// 1e-3 N_sup) electrons, the tolerance the reference asks of its adaptive
+// integrator (src/mod_global.F90:84-92); 16 panels of 4 nodes over 1 um did not.
+#define RD_SUPPLY_SPACING 5.0e-9
+static int supply_panels(double Lx, double Ly, int emitter_type, double ring_rmin, double ring_thick, int Q) {
+  double L = std::max(Lx, Ly);
+  if (emitter_type == 4) L = std::max(2.0 * 3.14159265358979323846 * (ring_rmin + ring_thick), ring_thick);
+  const double r = L / (Q * RD_SUPPLY_SPACING);
+  int P = (int)std::ceil(r * (1.0 - 1e-12));
+  return std::min(256, std::max(16, P));
+}
 
 static int alloc_pool(rd_engine* e, Pool& P, long long cap) {
   double** dbl[] = {&P.x, &P.y, &P.z, &P.vx, &P.vy, &P.vz, &P.ax, &P.ay, &P.az,
@@ -339,40 +382,115 @@ static Sig signature(const rd_engine* e) {
   return s;
 }
 
-// Jumps 1..jumps of the batched MH chains.  The planar jumps run as
-// RD_MH_PARTS launches per jump, one per part of the plan (part_range), each
-// on its own stream: the parts are independent (each diode's chains and
-// counters sit in one), so while one stream's launch runs its last items the
-// others' launches fill the idle SMs.  Results do not depend on it.
-static int launch_mh_jumps(rd_engine* e, const Sig& s) {
-  const int prec = e->cfg.precision;
-  // one diode cannot be split: it runs as one launch per jump (part 0)
-  const int parts = s.mh_planar > 1 ? RD_MH_PARTS : 1;
-  if (parts > 1) {
-    CK(cudaEventRecord(e->ev_fork, e->st));
-    for (int q = 1; q < parts; ++q) CK(cudaStreamWaitEvent(e->stp[q], e->ev_fork, 0));
+// MH launch shape of the planar jumps for the resident mix: parts of the plan
+// (one launch and one stream each; one diode cannot be split) and the FP32
+// thread form.  Neither changes a result: each diode's chains and counters sit
+// in one part, and both forms do the same lane arithmetic in the same order.
+static int mh_parts_for(const rd_engine* e, const Sig& s) {
+  if (s.mh_planar <= 1) return 1;
+  return e->mh_parts > 0 ? e->mh_parts : RD_MH_PARTS;
+}
+static int mh_form_for(const rd_engine* e, const Sig& s) {
+  if (e->mh_form >= 0) return e->mh_form;
+  return s.mh_planar == 1 ? 1 : 0;
+}
+
+static int planar_mh_launch(rd_engine* e, const Sig& s, int it, int parts, int form, cudaStream_t main) {
+  for (int q = 0; q < parts; ++q) {
+    cudaStream_t sq = q == 0 ? main : e->stp[q];
+    int* queue = q == 0 ? e->item_queue : e->item_queue + 6 + 2 * (q + 1);
+    CK(rd_launch_mh_jump(e->cfg.precision, 1, e->grid, sq, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                         e->cs, e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, queue,
+                         parts > 1 ? q + 1 : 0, parts, form));
   }
+  return RD_OK;
+}
+
+static int mh_fork(rd_engine* e, int parts, cudaStream_t main) {
+  if (parts <= 1) return RD_OK;
+  CK(cudaEventRecord(e->ev_fork, main));
+  for (int q = 1; q < parts; ++q) CK(cudaStreamWaitEvent(e->stp[q], e->ev_fork, 0));
+  return RD_OK;
+}
+static int mh_join(rd_engine* e, int parts, cudaStream_t main) {
+  for (int q = 1; q < parts; ++q) {
+    CK(cudaEventRecord(e->ev_join[q], e->stp[q]));
+    CK(cudaStreamWaitEvent(main, e->ev_join[q], 0));
+  }
+  return RD_OK;
+}
+
+// Jumps 1..jumps of the batched MH chains.  The planar jumps run as `parts`
+// launches per jump, one per part of the plan (part_range), each on its own
+// stream: the parts are independent (each diode's chains and counters sit in
+// one), so while one stream's launch runs its last items the others' launches
+// fill the idle SMs.  Results do not depend on it.
+static int launch_mh_jumps(rd_engine* e, const Sig& s, cudaStream_t main) {
+  const int prec = e->cfg.precision;
+  const int parts = mh_parts_for(e, s), form = mh_form_for(e, s);
+  int rc = mh_fork(e, parts, main);
+  if (rc) return rc;
   for (int it = 1; it <= s.jumps; ++it) {
     if (s.emit_planar) {
-      for (int q = 0; q < parts; ++q) {
-        cudaStream_t sq = q == 0 ? e->st : e->stp[q];
-        int* queue = q == 0 ? e->item_queue : e->item_queue + 6 + 2 * (q + 1);
-        CK(rd_launch_mh_jump(prec, 1, e->grid, sq, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
-                             e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, queue,
-                             parts > 1 ? q + 1 : 0, s.mh_planar == 1));
-      }
+      if ((rc = planar_mh_launch(e, s, it, parts, form, main))) return rc;
       e->kernels_in_step += parts;
     }
     if (s.emit_tip) {   // tip propose + jump
-      CK(rd_launch_mh_jump(prec, 2, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
+      CK(rd_launch_mh_jump(prec, 2, e->grid, main, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH], e->cs,
                            e->d_choff, e->wtab, e->d_step, it, e->partial, e->tickets, e->kscale, e->item_queue));
       e->kernels_in_step += 2;
     }
   }
-  for (int q = 1; q < parts; ++q) {
-    CK(cudaEventRecord(e->ev_join[q], e->stp[q]));
-    CK(cudaStreamWaitEvent(e->st, e->ev_join[q], 0));
-  }
+  return mh_join(e, parts, main);
+}
+
+// The tiled MH chains of a step on stream `main`: round 0 of the start (tiled
+// like a jump), k_mh_init for the rest of the start, then the jumps.
+static int launch_mh_tiled(rd_engine* e, const Sig& s, cudaStream_t main) {
+  const int prec = e->cfg.precision;
+  const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
+  CK(rd_launch_mh_jump(prec, gmask, e->grid, main, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                       e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue,
+                       0, 1, mh_form_for(e, s)));
+  e->kernels_in_step += ((gmask & 1) ? 1 : 0) + ((gmask & 2) ? 2 : 0);
+  CK(rd_launch_mh_init(prec, e->grid, main, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
+                       e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
+  e->kernels_in_step++;
+  return launch_mh_jumps(e, s, main);
+}
+
+// Inside a stream capture: the tiled MH chains as the body of a conditional
+// (IF) graph node, which a one-thread kernel switches on only when the MH plan
+// has work items.  A step whose emitting diodes all sample the vacuum field
+// (k_mh_vacuum) -- or that has no chain at all -- then skips the start and
+// jump launches entirely.  The body is captured on stream e->sbody.
+static int launch_mh_tiled_if(rd_engine* e, const Sig& s) {
+  cudaStreamCaptureStatus cst;
+  cudaGraph_t cap = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  CK(cudaStreamGetCaptureInfo(e->st, &cst, nullptr, &cap, nullptr, nullptr, nullptr));
+  if (cst != cudaStreamCaptureStatusActive) return launch_mh_tiled(e, s, e->st);
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, cap, 0, cudaGraphCondAssignDefault));
+  CK(rd_launch_mh_cond(e->st, h, e->ph[PM_MH]));
+  e->kernels_in_step++;
+  CK(cudaStreamGetCaptureInfo(e->st, &cst, nullptr, &cap, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, cap, deps, nullptr, ndeps, &cp));
+  CK(cudaStreamUpdateCaptureDependencies(e->st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(e->sbody, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  int rc = launch_mh_tiled(e, s, e->sbody);
+  cudaGraph_t done = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(e->sbody, &done);
+  if (rc) return rc;
+  CK(ce);
   return RD_OK;
 }
 
@@ -399,16 +517,11 @@ static int launch_emission(rd_engine* e) {
                              e->work, e->d_step, e->sup_part));
   e->kernels_in_step += 2;
   CK(plan(e, PM_MH));
-  const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
-  // round 0 of the chain start, tiled like a jump; k_mh_init continues the rest
-  CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                       e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue,
-                       0, s.mh_planar == 1));
-  e->kernels_in_step += ((gmask & 1) ? 1 : 0) + ((gmask & 2) ? 2 : 0);
-  CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                       e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
-  e->kernels_in_step++;
-  int rc = launch_mh_jumps(e, s);
+  if (s.emit_planar) {   // diodes with no particle in flight: all their MH sampling in one launch
+    CK(rd_launch_mh_vacuum(prec, ns, e->st, e->dP, e->dD, e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
+    e->kernels_in_step++;
+  }
+  int rc = launch_mh_tiled_if(e, s);
   if (rc) return rc;
   CK(rd_launch_emit(ns, e->st, e->dP, e->dD, e->pool, e->cs, e->d_choff, e->work, e->d_step, e->evlog));
   e->kernels_in_step += 2;
@@ -488,8 +601,9 @@ static int launch_step_body(rd_engine* e) {
 static std::string sig_string(rd_engine* e) {
   Sig s = signature(e);
   char b[128];
-  snprintf(b, sizeof b, "%d%d%d%d%d%d%d%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
-           s.emit_serial, s.tts, s.mh_planar > 1 ? 2 : s.mh_planar, s.jumps, e->clen_min, e->nch_max);
+  snprintf(b, sizeof b, "%d%d%d%d%d%d%d%d:%d:%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
+           s.emit_serial, s.tts, s.mh_planar > 1 ? 2 : s.mh_planar, s.jumps, e->clen_min, e->nch_max,
+           mh_parts_for(e, s), mh_form_for(e, s));
   return b;
 }
 
@@ -547,6 +661,7 @@ int rd_noalloc_prepare(int device, int prec);   // rd_noalloc.cu
 int rd_engine_view(rd_engine* e, int diode, const DiodeParams** P, const DiodeDyn** Dy, Pool* pool,
                    int* geometry, int* precision, int* grid, double* kscale, cudaStream_t* st,
                    int* device) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!valid_diode(e, diode)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   *P = e->dP + diode;
   *Dy = e->dD + diode;
@@ -594,12 +709,20 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   if ((ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess ||
       (ce = cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming)) != cudaSuccess)
     return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
-  for (int q = 1; q < RD_MH_PARTS; ++q)
+  for (int q = 1; q < RD_MH_PARTS_MAX; ++q)
     if ((ce = cudaStreamCreateWithFlags(&e->stp[q], cudaStreamNonBlocking)) != cudaSuccess ||
         (ce = cudaEventCreateWithFlags(&e->ev_join[q], cudaEventDisableTiming)) != cudaSuccess)
       return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
   cudaEventCreate(&e->ev0);
   cudaEventCreate(&e->ev1);
+  if ((ce = cudaStreamCreateWithFlags(&e->sa, cudaStreamNonBlocking)) != cudaSuccess ||
+      (ce = cudaStreamCreateWithFlags(&e->sbody, cudaStreamNonBlocking)) != cudaSuccess ||
+      (ce = cudaEventCreateWithFlags(&e->ev_adm, cudaEventDisableTiming)) != cudaSuccess ||
+      (ce = cudaHostAlloc((void**)&e->act_P, sizeof(DiodeParams) * cfg->max_diodes, cudaHostAllocDefault)) != cudaSuccess ||
+      (ce = cudaHostAlloc((void**)&e->act_D, sizeof(DiodeDyn) * cfg->max_diodes, cudaHostAllocDefault)) != cudaSuccess ||
+      (ce = cudaHostAlloc((void**)&e->act_choff, sizeof(int) * cfg->max_diodes, cudaHostAllocDefault)) != cudaSuccess ||
+      (ce = cudaHostAlloc((void**)&e->act_qoff, sizeof(int) * cfg->max_diodes, cudaHostAllocDefault)) != cudaSuccess)
+    return bail(fail(RD_ERR_CUDA, cudaGetErrorString(ce)));
   e->k = make_constants();
   e->kscale = e->k.div_fac_c * e->k.q0 * 1.0e18;
   if (rd_upload_constants_force(e->k) != cudaSuccess || rd_upload_constants_field(e->k) != cudaSuccess ||
@@ -609,12 +732,11 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   const int S = cfg->max_diodes;
   const long long chcap = std::max<long long>(cfg->chain_capacity, 1);
   const long long qcap = std::max<long long>(cfg->quad_capacity, 1);
-  // scratch bound: the planner grows the chunk length until the items fit,
-  // and with one chunk per tile every mode has at most capacity/128 + slots tiles
-  // scratch bound: at most RD_NCH_MAX chunks per tile and at most
-  // capacity/128 + slots tiles in any pair sum
+  // scratch bound: at most RD_NCH_MAX chunks per tile (RD_SUP_NCH for the
+  // planar supply points) and at most capacity/128 + slots tiles in any pair sum
   e->max_items = (int)std::min<long long>(
-      1 << 26, (long long)RD_NCH_MAX * (std::max(cap, std::max(chcap, qcap)) / RD_ITILE + 4LL * S) + 65536);
+      1 << 26, std::max((long long)RD_NCH_MAX * (std::max(cap, chcap) / RD_ITILE + 4LL * S),
+                        (long long)RD_SUP_NCH * (qcap / RD_ITILE + 4LL * S)) + 65536);
   if ((rc = alloc_pool(e, e->pool, cap)) || (rc = alloc_pool(e, e->tmp, cap))) return bail(rc);
   if (e->dalloc(&e->dP, S) || e->dalloc(&e->dD, S) || e->dalloc(&e->work, (size_t)S * 4 + 4096) || e->dalloc(&e->wtab, 3 * ((size_t)S * 4 + 4096)) ||
       e->dalloc(&e->qx, qcap) || e->dalloc(&e->qy, qcap) || e->dalloc(&e->qz, qcap) ||
@@ -628,7 +750,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
       e->dalloc(&e->partial, (size_t)e->max_items * 3 * RD_ITILE) ||
       e->dalloc(&e->tickets, e->max_items) || e->dalloc(&e->kept, e->max_items) ||
       e->dalloc(&e->sup_part, (size_t)S * RD_SUP_SPLIT * 2) ||
-      e->dalloc(&e->item_queue, 8 + 2 * RD_MH_PARTS) ||
+      e->dalloc(&e->item_queue, 8 + 2 * RD_MH_PARTS_MAX) ||
       (cfg->event_capacity > 0 && (e->dalloc(&e->evlog.buf, (size_t)cfg->event_capacity) ||
                                    e->dalloc(&e->evlog.count, 1))) ||
       e->dalloc(&e->ramo, ((size_t)cap / RD_ITILE + S + 1) * 10) || e->dalloc(&e->life, (size_t)S * RD_MAX_LIFE) ||
@@ -645,7 +767,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   cudaMemsetAsync(e->dP, 0, sizeof(DiodeParams) * S, e->st);
   cudaMemsetAsync(e->dD, 0, sizeof(DiodeDyn) * S, e->st);
   cudaMemsetAsync(e->tickets, 0, sizeof(int) * e->max_items, e->st);
-  cudaMemsetAsync(e->item_queue, 0, sizeof(int) * (8 + 2 * RD_MH_PARTS), e->st);
+  cudaMemsetAsync(e->item_queue, 0, sizeof(int) * (8 + 2 * RD_MH_PARTS_MAX), e->st);
   if (e->evlog.count) cudaMemsetAsync(e->evlog.count, 0, sizeof(int), e->st);
   e->evlog.cap = cfg->event_capacity > 0 ? cfg->event_capacity : 0;
   cudaMemsetAsync(e->life, 0, sizeof(int) * (size_t)S * RD_MAX_LIFE, e->st);
@@ -666,6 +788,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
 }
 
 int rd_engine_destroy(rd_engine* e) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!e) return RD_OK;
   if (e->st) cudaStreamSynchronize(e->st);
   if (e->graph) cudaGraphExecDestroy(e->graph);
@@ -677,8 +800,17 @@ int rd_engine_destroy(rd_engine* e) {
   if (e->fpx) { cudaFree(e->fpx); cudaFree(e->fpy); cudaFree(e->fpz); cudaFree(e->ffx); cudaFree(e->ffy); cudaFree(e->ffz); }
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->sa) { cudaStreamSynchronize(e->sa); cudaStreamDestroy(e->sa); }
+  if (e->sbody) cudaStreamDestroy(e->sbody);
+  if (e->ev_adm) cudaEventDestroy(e->ev_adm);
+  if (e->adm_h) cudaFreeHost(e->adm_h);
+  if (e->adm_d) cudaFree(e->adm_d);
+  if (e->act_P) cudaFreeHost(e->act_P);
+  if (e->act_D) cudaFreeHost(e->act_D);
+  if (e->act_choff) cudaFreeHost(e->act_choff);
+  if (e->act_qoff) cudaFreeHost(e->act_qoff);
   if (e->ev_fork) cudaEventDestroy(e->ev_fork);
-  for (int q = 1; q < RD_MH_PARTS; ++q) {
+  for (int q = 1; q < RD_MH_PARTS_MAX; ++q) {
     if (e->ev_join[q]) cudaEventDestroy(e->ev_join[q]);
     if (e->stp[q]) cudaStreamDestroy(e->stp[q]);
   }
@@ -688,12 +820,83 @@ int rd_engine_destroy(rd_engine* e) {
 }
 
 int rd_sync(rd_engine* e) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   CK(cudaStreamSynchronize(e->st));
   return RD_OK;
 }
 
-int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
+// Admission arena: host bytes staged in pinned memory for an upload on sa.
+// The previous batch's copies are waited for before the arena is reused.
+static cudaError_t adm_grow(rd_engine* e, size_t need) {
+  cudaError_t ce = cudaStreamSynchronize(e->sa);
+  if (ce != cudaSuccess) return ce;
+  if (need <= e->adm_cap) return cudaSuccess;
+  if (e->adm_h) cudaFreeHost(e->adm_h);
+  if (e->adm_d) cudaFree(e->adm_d);
+  e->adm_h = nullptr; e->adm_d = nullptr; e->adm_cap = 0; e->adm_used = 0;
+  const size_t cap = std::max<size_t>(need, 2 * (size_t)(1 << 20));
+  if ((ce = cudaHostAlloc((void**)&e->adm_h, cap, cudaHostAllocDefault)) != cudaSuccess) return ce;
+  if ((ce = cudaMalloc((void**)&e->adm_d, cap)) != cudaSuccess) return ce;
+  e->adm_cap = cap;
+  return cudaSuccess;
+}
+
+// Room for `bytes` in the admission arena: offset of the region (host and device alike).
+static cudaError_t adm_take(rd_engine* e, size_t bytes, size_t* off) {
+  const size_t len = (bytes + 255) & ~(size_t)255;
+  if (e->adm_used + len > e->adm_cap) {
+    cudaError_t ce = adm_grow(e, std::max(e->adm_cap * 2, e->adm_used + len));
+    if (ce != cudaSuccess) return ce;
+    // adm_grow waited for every copy from the arena: what was taken is free again unless kept
+  }
+  *off = e->adm_used;
+  e->adm_used += len;
+  return cudaSuccess;
+}
+
+// Host -> device copy on stream us: staged through the pinned admission arena
+// when `deferred` (nothing waits, the source may go away at once), directly
+// from the (pageable) source otherwise (the caller synchronises us).
+static cudaError_t upload(rd_engine* e, void* dst, const void* src, size_t bytes, cudaStream_t us, bool deferred) {
+  if (bytes == 0) return cudaSuccess;
+  if (!deferred) return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, us);
+  size_t off = 0;
+  cudaError_t ce = adm_take(e, bytes, &off);
+  if (ce != cudaSuccess) return ce;
+  std::memcpy(e->adm_h + off, src, bytes);
+  return cudaMemcpyAsync(dst, e->adm_h + off, bytes, cudaMemcpyHostToDevice, us);
+}
+
+// Makes the slots admitted on sa active on the engine stream: the stream waits
+// for sa's uploads, then each slot's parameters (active) are copied in.  The
+// next step on the engine stream includes them.
+static int activate_pending(rd_engine* e) {
+  if (e->pending.empty()) return RD_OK;
+  CK(cudaEventRecord(e->ev_adm, e->sa));
+  CK(cudaStreamWaitEvent(e->st, e->ev_adm, 0));
+  for (int s : e->pending)
+    CK(cudaMemcpyAsync(e->dP + s, &e->act_P[s], sizeof(DiodeParams), cudaMemcpyHostToDevice, e->st));
+  e->pending.clear();
+  return RD_OK;
+}
+
+// Completes any admission still in flight (entry points that touch device state call it).
+static int flush_admissions(rd_engine* e) {
+  if (e->pending.empty()) return RD_OK;
+  int rc = activate_pending(e);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(e->st));
+  return RD_OK;
+}
+
+// rd_diode_add on stream `us`.  deferred: the slot is written inactive and
+// its parameters are kept for activate_pending(), which makes it active on the
+// engine stream before the next step; nothing here waits for the GPU, so the
+// uploads overlap a step running on the engine stream (which skips inactive
+// slots).  Otherwise the slot is active when the call returns.
+static int diode_add_impl(rd_engine* e, const rd_diode_config* c, int* diode, cudaStream_t us, bool deferred,
+                          int step_offset = 0) {
   if (!e || !c || !diode) return fail(RD_ERR_INVALID, "null argument");
   if (c->geometry != RD_GEOM_PLANAR && c->geometry != RD_GEOM_TIP) return fail(RD_ERR_INVALID, "unknown geometry");
   if (c->capacity <= 0 || c->time_step <= 0.0) return fail(RD_ERR_INVALID, "capacity and time_step must be positive");
@@ -812,9 +1015,12 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
     sl.ch_off = e->ch_alloc.alloc(sl.ch_len, 32);
     if (sl.ch_off < 0) { sl.ch_len = 0; undo(); return fail(RD_ERR_CAPACITY, "MH chain pool full"); }
     int npt;
+    int P_ = 0, Q = 4;
     if (c->geometry == RD_GEOM_PLANAR) {
-      int P_ = c->quad_panels > 0 ? c->quad_panels : 16, Q = c->quad_order > 0 ? c->quad_order : 4;
+      Q = c->quad_order > 0 ? c->quad_order : 4;
       if (Q > 16) { undo(); return fail(RD_ERR_INVALID, "quad_order must be <= 16"); }
+      P_ = c->quad_panels > 0 ? c->quad_panels : supply_panels(p.em_Lx, p.em_Ly, p.emitter_type, p.ring_rmin, p.ring_thick, Q);
+      if ((long long)P_ * Q > 4096) { undo(); return fail(RD_ERR_INVALID, "quad_panels x quad_order must be <= 4096"); }
       p.quad_n = P_ * Q;
       npt = p.quad_n * p.quad_n;
     } else {
@@ -824,63 +1030,17 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
     sl.q_off = e->q_alloc.alloc(sl.q_len, 32);
     if (sl.q_off < 0) { sl.q_len = 0; undo(); return fail(RD_ERR_CAPACITY, "quadrature table full"); }
     p.q_off = (int)sl.q_off;
-    std::vector<double> hx(npt), hy(npt), hz(npt, 0.0), hw(npt);
-    if (c->geometry == RD_GEOM_PLANAR) {
-      int P_ = c->quad_panels > 0 ? c->quad_panels : 16, Q = c->quad_order > 0 ? c->quad_order : 4;
-      double gx[16], gw[16];
-      gauss_legendre(Q, gx, gw);
-      double A = p.em_Lx * p.em_Ly;
-      for (int iy = 0; iy < p.quad_n; ++iy) {
-        double uy = ((iy / Q) + 0.5 * (gx[iy % Q] + 1.0)) / P_, wy = 0.5 * gw[iy % Q] / P_;
-        for (int ix = 0; ix < p.quad_n; ++ix) {
-          double ux = ((ix / Q) + 0.5 * (gx[ix % Q] + 1.0)) / P_, wx = 0.5 * gw[ix % Q] / P_;
-          int k2 = iy * p.quad_n + ix;
-          if (p.emitter_type == 4) {   // (angle, radius) of the ring, area factor 2 pi w r (fe_v2:701-707)
-            const double angle = ux * 2.0 * e->k.pi, radius = p.ring_rmin + uy * p.ring_thick;
-            hx[k2] = radius * std::cos(angle);
-            hy[k2] = radius * std::sin(angle);
-            hw[k2] = (wx * wy) * (2.0 * e->k.pi * p.ring_thick * radius);
-          } else {
-            hx[k2] = p.em_x0 + ux * p.em_Lx;
-            hy[k2] = p.em_y0 + uy * p.em_Ly;
-            hw[k2] = (wx * wy) * A;
-          }
-        }
-      }
-    } else {
-      // 100 x 100 midpoint grid in (xi, phi) with the cell areas
-      // (Do_Field_Emission_Tip_OLDCODE :434-481, Tip_Area, xyz_corr)
-      const double pi = e->k.pi;
-      const int nr = 100;
-      double len_phi = 2.0 * pi / nr, len_xi = (p.max_xi - 1.0) / nr, e2 = p.eta_1 * p.eta_1;
-      auto fac = [&](double xi) { return xi * std::sqrt(xi * xi - e2) - e2 * std::log(xi + std::sqrt(xi * xi - e2)); };
-      for (int i = 1; i <= nr; ++i)
-        for (int j = 1; j <= nr; ++j) {
-          double xi_c = 1.0 + (i - 0.5) * len_xi, phi_c = (j - 0.5) * len_phi;
-          int k2 = (i - 1) * nr + (j - 1);
-          double xy = p.a_foci * std::sqrt((xi_c * xi_c - 1.0) * (1.0 - p.eta_1 * p.eta_1));
-          hx[k2] = xy * std::cos(phi_c);
-          hy[k2] = xy * std::sin(phi_c);
-          hz[k2] = (p.a_foci * xi_c) * p.eta_1 + p.shift_z;
-          double xi1 = 1.0 + (i - 1.0) * len_xi, xi2 = 1.0 + (i + 0.0) * len_xi;
-          double ph1 = (j - 1.0) * len_phi, ph2 = (j + 0.0) * len_phi;
-          hw[k2] = (((0.5 * (p.a_foci * p.a_foci)) * std::sqrt(1.0 - e2)) * (ph2 - ph1)) * (fac(xi2) - fac(xi1));
-        }
-    }
-    std::vector<float4> hpp(npt);
-    for (int k2 = 0; k2 < npt; ++k2) {   // the FP32-frame split of rd_device.cuh split_nm
-      double vx = (hx[k2] - p.org_x) * 1.0e9, vy = (hy[k2] - p.org_y) * 1.0e9;
-      float ax = (float)vx, ay = (float)vy;
-      hpp[k2] = make_float4(ax, (float)(vx - (double)ax), ay, (float)(vy - (double)ay));
-    }
-    CK(cudaMemcpyAsync(e->qpp + sl.q_off, hpp.data(), npt * sizeof(float4), cudaMemcpyHostToDevice, e->st));
-    CK(cudaMemcpyAsync(e->qx + sl.q_off, hx.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
-    CK(cudaMemcpyAsync(e->qy + sl.q_off, hy.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
-    CK(cudaMemcpyAsync(e->qz + sl.q_off, hz.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
-    CK(cudaMemcpyAsync(e->qw + sl.q_off, hw.data(), npt * sizeof(double), cudaMemcpyHostToDevice, e->st));
-    CK(cudaStreamSynchronize(e->st));
+    // the grid is filled on the device: nothing but this description crosses the bus
+    QuadSpec qs{};
+    qs.geometry = p.geometry; qs.emitter_type = p.emitter_type; qs.P = P_; qs.Q = Q;
+    qs.quad_n = p.quad_n; qs.q_off = (int)sl.q_off;
+    qs.x0 = p.em_x0; qs.y0 = p.em_y0; qs.Lx = p.em_Lx; qs.Ly = p.em_Ly;
+    qs.ring_rmin = p.ring_rmin; qs.ring_thick = p.ring_thick; qs.org_x = p.org_x; qs.org_y = p.org_y;
+    qs.a_foci = p.a_foci; qs.eta_1 = p.eta_1; qs.max_xi = p.max_xi; qs.shift_z = p.shift_z;
+    if (c->geometry == RD_GEOM_PLANAR) gauss_legendre(Q, qs.gx, qs.gw);
+    CK(rd_launch_quad_fill(us, qs, e->qx, e->qy, e->qz, e->qw, e->qpp));
   }
-  CK(cudaMemcpyAsync(e->work + sl.w_off, wv.data(), sl.w_len * sizeof(double), cudaMemcpyHostToDevice, e->st));
+  CK(upload(e, e->work + sl.w_off, wv.data(), sl.w_len * sizeof(double), us, deferred));
   // supply-target table per checkerboard cell or Voronoi site (the Gaussian model has none)
   std::vector<double> wt(3 * sl.w_len, 0.0);
   const long long cells = p.work_model == 1 ? sl.w_len : (p.work_model == 4 ? p.work_nx : 0);
@@ -890,19 +1050,27 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
     wt[3 * k2 + 1] = std::log(e->k.l_const / (phi * phi));
     wt[3 * k2 + 2] = e->k.l_const / (phi * phi);
   }
-  CK(cudaMemcpyAsync(e->wtab + 3 * sl.w_off, wt.data(), wt.size() * sizeof(double), cudaMemcpyHostToDevice, e->st));
+  CK(upload(e, e->wtab + 3 * sl.w_off, wt.data(), wt.size() * sizeof(double), us, deferred));
   DiodeDyn y{};
   y.MH_std = (c->geometry == RD_GEOM_TIP) ? 0.125 : 0.0125;   // fe_v2:58; tip 1.0 clamped to 0.125
   y.a_rate = (c->geometry == RD_GEOM_TIP) ? 0.5 : 1.0;
   y.first_dead = 0x7fffffff;
-  int choff = (int)sl.ch_off, qoff = (int)sl.q_off;
-  CK(cudaMemcpyAsync(e->dP + s, &p, sizeof p, cudaMemcpyHostToDevice, e->st));
-  CK(cudaMemcpyAsync(e->dD + s, &y, sizeof y, cudaMemcpyHostToDevice, e->st));
-  CK(cudaMemcpyAsync(e->d_choff + s, &choff, sizeof(int), cudaMemcpyHostToDevice, e->st));
-  CK(cudaMemcpyAsync(e->d_qoff + s, &qoff, sizeof(int), cudaMemcpyHostToDevice, e->st));
-  CK(cudaMemsetAsync(e->life + (size_t)s * RD_MAX_LIFE, 0, sizeof(int) * RD_MAX_LIFE, e->st));
-  CK(cudaMemsetAsync(e->pool.mask + p.off, 0, sizeof(int) * p.cap, e->st));
-  CK(cudaStreamSynchronize(e->st));
+  y.step_offset = step_offset;
+  DiodeParams pw = p;
+  if (deferred) pw.active = 0;   // activate_pending() sets it before the next step
+  e->act_P[s] = p;               // pinned: the source of the activation copy
+  e->act_P[s].active = 1;
+  e->act_D[s] = y;
+  e->act_choff[s] = (int)sl.ch_off;
+  e->act_qoff[s] = (int)sl.q_off;
+  CK(upload(e, e->dP + s, &pw, sizeof p, us, deferred));
+  CK(cudaMemcpyAsync(e->dD + s, &e->act_D[s], sizeof y, cudaMemcpyHostToDevice, us));
+  CK(cudaMemcpyAsync(e->d_choff + s, &e->act_choff[s], sizeof(int), cudaMemcpyHostToDevice, us));
+  CK(cudaMemcpyAsync(e->d_qoff + s, &e->act_qoff[s], sizeof(int), cudaMemcpyHostToDevice, us));
+  CK(cudaMemsetAsync(e->life + (size_t)s * RD_MAX_LIFE, 0, sizeof(int) * RD_MAX_LIFE, us));
+  CK(cudaMemsetAsync(e->pool.mask + p.off, 0, sizeof(int) * p.cap, us));
+  if (deferred) e->pending.push_back(s);
+  else CK(cudaStreamSynchronize(us));
   sl.used = true;
   sl.p = p;
   e->slots[s] = sl;
@@ -910,7 +1078,15 @@ int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
   return RD_OK;
 }
 
+int rd_diode_add(rd_engine* e, const rd_diode_config* c, int* diode) {
+  if (!e) return fail(RD_ERR_INVALID, "null argument");
+  int rc = flush_admissions(e);
+  if (rc) return rc;
+  return diode_add_impl(e, c, diode, e->st, false);
+}
+
 int rd_diode_remove(rd_engine* e, int d) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   SlotHost& sl = e->slots[d];
   DiodeParams p{};
@@ -934,8 +1110,27 @@ int rd_diode_count(rd_engine* e, int* active) {
   return RD_OK;
 }
 
+// Add_Particle for a slot being admitted (deferred, on sa): positions and
+// velocities staged through the admission arena, k_add_particles on sa.
+static int add_particles_deferred(rd_engine* e, int d, int n, const double* pos, const double* vel, int step,
+                                  int section) {
+  size_t off = 0;
+  if (n > 0) {
+    const size_t bytes = (vel ? 6 : 3) * sizeof(double) * (size_t)n;
+    CK(adm_take(e, bytes, &off));
+    std::memcpy(e->adm_h + off, pos, 3 * sizeof(double) * n);
+    if (vel) std::memcpy(e->adm_h + off + 3 * sizeof(double) * n, vel, 3 * sizeof(double) * n);
+    CK(cudaMemcpyAsync(e->adm_d + off, e->adm_h + off, bytes, cudaMemcpyHostToDevice, e->sa));
+  }
+  const double* dpos = (const double*)(e->adm_d + off);
+  CK(rd_launch_add_particles(e->sa, e->dP, e->dD, e->pool, d, n, dpos, vel ? dpos + 3LL * n : nullptr, nullptr,
+                             step, section));
+  return RD_OK;
+}
+
 int rd_add_particles(rd_engine* e, int d, int n, const double* pos, const double* vel,
                      const int* species, int step, int section) {
+  if (e) { int rc0 = flush_admissions(e); if (rc0) return rc0; }
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (n < 0 || (n > 0 && !pos)) return fail(RD_ERR_INVALID, "bad particle arrays");
   int rc = stage(e, 6LL * n, n);
@@ -965,6 +1160,7 @@ static int read_dyn(rd_engine* e, int d, DiodeDyn* y) {
 
 int rd_get_particles(rd_engine* e, int d, int cap, double* pos, double* vel, double* acc,
                      double* charge, int* id, int* section, int* n_out) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   DiodeDyn y;
   int rc = read_dyn(e, d, &y);
@@ -993,6 +1189,7 @@ int rd_get_particles(rd_engine* e, int d, int cap, double* pos, double* vel, dou
 
 int rd_set_particles(rd_engine* e, int d, int n, const double* pos, const double* vel,
                      const double* acc, const double* accp, const double* accp2) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   DiodeDyn y;
   int rc = read_dyn(e, d, &y);
@@ -1021,6 +1218,7 @@ int rd_set_particles(rd_engine* e, int d, int n, const double* pos, const double
 }
 
 int rd_accel(rd_engine* e, int d, double* acc3n) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_accel");
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   int rc = repack(e);
@@ -1034,6 +1232,7 @@ int rd_accel(rd_engine* e, int d, double* acc3n) {
 static int field_at_batch(rd_engine* e, int d, int M, const double* pos, double* field);
 
 int rd_field_at(rd_engine* e, int d, int M, const double* pos, double* field) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_field_at");
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (M < 0 || (M > 0 && (!pos || !field))) return fail(RD_ERR_INVALID, "bad point arrays");
@@ -1080,6 +1279,7 @@ static int field_at_batch(rd_engine* e, int d, int M, const double* pos, double*
 }
 
 int rd_time_accel(rd_engine* e, int reps, double* ms_per_eval) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!e || !ms_per_eval || reps <= 0) return fail(RD_ERR_INVALID, "bad argument");
   int rc = repack(e);
   if (rc) return rc;
@@ -1096,6 +1296,7 @@ int rd_time_accel(rd_engine* e, int reps, double* ms_per_eval) {
 }
 
 int rd_time_verlet(rd_engine* e, int reps, double* position_ms, double* velocity_ms) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_time_verlet");
   if (!e || !position_ms || !velocity_ms || reps <= 0) return fail(RD_ERR_INVALID, "bad argument");
   const int ns = e->nslots_hw();
@@ -1124,7 +1325,43 @@ int rd_time_verlet(rd_engine* e, int reps, double* position_ms, double* velocity
   return RD_OK;
 }
 
+int rd_time_remove(rd_engine* e, double* position_ms, double* remove_ms, long long* moved, long long* removed) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
+  NvtxRange nvtx_range("rd_time_remove");
+  if (!e || !position_ms || !remove_ms || !moved || !removed) return fail(RD_ERR_INVALID, "bad argument");
+  const int S = e->cfg.max_diodes;
+  float ms = 0.f;
+  CK(plan(e, PM_PART));
+  CK(cudaEventRecord(e->ev0, e->st));
+  CK(rd_launch_position(e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_PART], e->ph[PM_PART], e->evlog,
+                        e->d_step));
+  CK(cudaEventRecord(e->ev1, e->st));
+  CK(cudaEventSynchronize(e->ev1));
+  CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+  *position_ms = ms;
+  // survivors behind the first removed particle are the ones compaction moves
+  std::vector<DiodeDyn> dyn(S);
+  CK(cudaMemcpy(dyn.data(), e->dD, sizeof(DiodeDyn) * S, cudaMemcpyDeviceToHost));
+  *moved = 0;
+  *removed = 0;
+  for (int d = 0; d < S; ++d) {
+    if (!e->slots[d].used || dyn[d].n_remove == 0) continue;
+    *moved += (long long)dyn[d].n - dyn[d].first_dead - dyn[d].n_remove;
+    *removed += dyn[d].n_remove;
+  }
+  CK(plan(e, PM_PART1024));
+  CK(cudaEventRecord(e->ev0, e->st));
+  CK(rd_launch_compact(e->grid, e->nslots_hw(), e->st, e->dP, e->dD, e->pool, e->tmp, e->plan[PM_PART1024],
+                       e->ph[PM_PART1024], e->kept, e->life, e->d_step));
+  CK(cudaEventRecord(e->ev1, e->st));
+  CK(cudaEventSynchronize(e->ev1));
+  CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+  *remove_ms = ms;
+  return RD_OK;
+}
+
 int rd_time_field_at(rd_engine* e, int d, int M, const double* pos, int reps, double* ms_per_eval) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (M <= 0 || !pos || !ms_per_eval || reps <= 0) return fail(RD_ERR_INVALID, "bad argument");
   if (M > (e->max_items / 2) * RD_ITILE) return fail(RD_ERR_CAPACITY, "too many points for one evaluation");
@@ -1148,6 +1385,7 @@ int rd_time_field_at(rd_engine* e, int d, int M, const double* pos, int reps, do
 
 // ---- event log -------------------------------------------------------------------------
 int rd_events_take(rd_engine* e, int cap, rd_event* out, int* n_out, long long* n_lost) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!e || !n_out || !n_lost || cap < 0 || (cap > 0 && !out)) return fail(RD_ERR_INVALID, "bad argument");
   *n_out = 0;
   *n_lost = 0;
@@ -1191,14 +1429,18 @@ static int time_pair_passes(rd_engine* e, int reps, double* force_ms, double* mh
   *force_ms = ms / reps;
   *mh_ms = 0.0;
   if (s.emit_planar) {
-    const int prec = e->cfg.precision;
-    for (int r = -1; r < reps; ++r) {
-      if (r == 0) CK(cudaEventRecord(e->ev0, e->st));
-      CK(plan(e, PM_MH));
-      CK(rd_launch_mh_jump(prec, 1, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
-                           e->cs, e->d_choff, e->wtab, e->d_step, -1, e->partial, e->tickets, e->kscale,
-                           e->item_queue, 0, s.mh_planar == 1));
-    }
+    // dry jumps back to back on the part streams, forked and joined once, as a step runs its
+    // jumps: successive launches of a stream overlap the other streams' tails
+    const int parts = mh_parts_for(e, s), form = mh_form_for(e, s);
+    CK(plan(e, PM_MH));
+    if ((rc = mh_fork(e, parts, e->st)) || (rc = planar_mh_launch(e, s, -1, parts, form, e->st)) ||
+        (rc = mh_join(e, parts, e->st)))
+      return rc;
+    CK(cudaEventRecord(e->ev0, e->st));
+    if ((rc = mh_fork(e, parts, e->st))) return rc;
+    for (int r = 0; r < reps; ++r)
+      if ((rc = planar_mh_launch(e, s, -1, parts, form, e->st))) return rc;
+    if ((rc = mh_join(e, parts, e->st))) return rc;
     CK(cudaEventRecord(e->ev1, e->st));
     CK(cudaEventSynchronize(e->ev1));
     CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
@@ -1208,6 +1450,7 @@ static int time_pair_passes(rd_engine* e, int reps, double* force_ms, double* mh
 }
 
 int rd_autotune(rd_engine* e, rd_tune_result* out) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_autotune");
   if (!e || !out) return fail(RD_ERR_INVALID, "null argument");
   *out = rd_tune_result{};
@@ -1223,7 +1466,10 @@ int rd_autotune(rd_engine* e, rd_tune_result* out) {
   CK(cudaMemcpyAsync(e->tmp.az, e->pool.az, bytes, cudaMemcpyDeviceToDevice, e->st));
   const int jumps = std::max(signature(e).jumps, 1);
   const int saved_min = e->clen_min, saved_max = e->nch_max;
-  double best = 1e300, at_default = 0.0;
+  const int user_parts = e->mh_parts, user_form = e->mh_form;
+  e->mh_parts = 0;    // the chunking is searched at the default launch shape
+  e->mh_form = -1;
+  double best = 1e300, at_default = 0.0, best_fms = 0.0;
   int best_min = saved_min, best_max = saved_max;
   const int mins[] = {128, 256, 512, 1024, 2048};   // short chunks: more items for small systems
   const int maxs[] = {8, 16, 32};
@@ -1232,23 +1478,91 @@ int rd_autotune(rd_engine* e, rd_tune_result* out) {
       e->clen_min = a;
       e->nch_max = b;
       double fms = 0.0, mms = 0.0;
-      if ((rc = time_pair_passes(e, 2, &fms, &mms))) { e->clen_min = saved_min; e->nch_max = saved_max; return rc; }
+      if ((rc = time_pair_passes(e, 2, &fms, &mms))) {
+        e->clen_min = saved_min; e->nch_max = saved_max; e->mh_parts = user_parts; e->mh_form = user_form;
+        return rc;
+      }
       const double est = fms + jumps * mms;
       if (a == RD_CLEN_MIN && b == RD_NCH_MAX) at_default = est;
-      if (est < best) { best = est; best_min = a; best_max = b; }
+      if (est < best) { best = est; best_min = a; best_max = b; best_fms = fms; }
       out->candidates++;
     }
   e->clen_min = best_min;
   e->nch_max = best_max;
+  // the MH launch shape under the chosen chunking: plan parts (with two or more
+  // diodes running batched chains) and the FP32 thread form; both bit-identical
+  const Sig sg = signature(e);
+  const int saved_parts = user_parts, saved_form = user_form;
+  int best_parts = mh_parts_for(e, sg), best_form = mh_form_for(e, sg);
+  double best_mh_ms = 1e300;
+  if (sg.emit_planar) {
+    double& best_mh = best_mh_ms;
+    const int max_parts = sg.mh_planar > 1 ? RD_MH_PARTS_MAX : 1;
+    const int max_form = e->cfg.precision == RD_PREC_FP32C ? 1 : 0;
+    for (int parts = 1; parts <= max_parts; ++parts)
+      for (int form = 0; form <= max_form; ++form) {
+        e->mh_parts = parts;
+        e->mh_form = form;
+        double fms = 0.0, mms = 0.0;
+        if ((rc = time_pair_passes(e, 6, &fms, &mms))) { e->mh_parts = saved_parts; e->mh_form = saved_form; return rc; }
+        if (mms < best_mh) { best_mh = mms; best_parts = parts; best_form = form; }
+        out->candidates++;
+      }
+  }
+  e->mh_parts = best_parts;
+  e->mh_form = best_form;
+  if (sg.emit_planar) best = std::min(best, best_fms + jumps * best_mh_ms);
   CK(cudaMemcpyAsync(e->pool.ax, e->tmp.ax, bytes, cudaMemcpyDeviceToDevice, e->st));
   CK(cudaMemcpyAsync(e->pool.ay, e->tmp.ay, bytes, cudaMemcpyDeviceToDevice, e->st));
   CK(cudaMemcpyAsync(e->pool.az, e->tmp.az, bytes, cudaMemcpyDeviceToDevice, e->st));
   CK(cudaStreamSynchronize(e->st));
   out->chunk_min = best_min;
   out->chunk_count_max = best_max;
+  out->mh_parts = best_parts;
+  out->mh_form = best_form;
   out->ms_default = at_default;
   out->ms_chosen = best;
-  return RD_OK;   // the step graph is rebuilt at the next step (its signature holds the chunking)
+  return RD_OK;   // the step graph is rebuilt at the next step (its signature holds the choices)
+}
+
+int rd_supply_points(const rd_diode_config* c, long long* npts) {
+  if (!c || !npts) return fail(RD_ERR_INVALID, "null argument");
+  *npts = 0;
+  if (!c->emission) return RD_OK;
+  if (c->geometry == RD_GEOM_TIP) { *npts = 10000; return RD_OK; }
+  if (c->geometry != RD_GEOM_PLANAR) return fail(RD_ERR_INVALID, "unknown geometry");
+  const int Q = c->quad_order > 0 ? c->quad_order : 4;
+  int P = c->quad_panels;
+  if (P <= 0) {
+    const RdConst k = make_constants();
+    const int type = c->emitter_type > 0 ? c->emitter_type : 2;
+    double thick = 0.0, rmin = 0.0;
+    if (type == 4) {
+      thick = c->emitter_thickness > 0.0 ? c->emitter_thickness
+                                         : std::sqrt((k.q0 * c->gap) / (k.pi * k.eps0 * c->V_s));
+      rmin = c->emitter_dim[0] - thick;
+    }
+    P = supply_panels(c->emitter_dim[0], c->emitter_dim[1], type, rmin, thick, Q);
+  }
+  *npts = (long long)(P * Q) * (P * Q);
+  return RD_OK;
+}
+
+int rd_set_mh_launch(rd_engine* e, int parts, int form) {
+  if (!e) return fail(RD_ERR_INVALID, "null engine");
+  if (parts < 0 || parts > RD_MH_PARTS_MAX) return fail(RD_ERR_INVALID, "parts must be in [0, 4] (0: default)");
+  if (form < -1 || form > 1) return fail(RD_ERR_INVALID, "form must be -1 (default), 0 or 1");
+  e->mh_parts = parts;
+  e->mh_form = form;
+  return RD_OK;
+}
+
+int rd_get_mh_launch(rd_engine* e, int* parts, int* form) {
+  if (!e || !parts || !form) return fail(RD_ERR_INVALID, "null argument");
+  const Sig s = signature(e);
+  *parts = mh_parts_for(e, s);
+  *form = mh_form_for(e, s);
+  return RD_OK;
 }
 
 int rd_set_chunking(rd_engine* e, int chunk_min, int chunk_count_max) {
@@ -1269,6 +1583,7 @@ int rd_get_chunking(rd_engine* e, int* chunk_min, int* chunk_count_max) {
 }
 
 int rd_mark_remove(rd_engine* e, int d, int i, int why) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (why != RD_REMOVE_TOP && why != RD_REMOVE_BOT) return fail(RD_ERR_INVALID, "unknown removal flag");
   CK(rd_launch_mark(e->st, e->dP, e->dD, e->pool, d, i, why));
@@ -1277,6 +1592,7 @@ int rd_mark_remove(rd_engine* e, int d, int i, int why) {
 }
 
 int rd_do_emission(rd_engine* e, int step) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_do_emission");
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   CK(rd_launch_step_set(e->st, e->d_step, step));
@@ -1287,6 +1603,7 @@ int rd_do_emission(rd_engine* e, int step) {
 }
 
 int rd_update_position(rd_engine* e, int step) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_update_position");
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   CK(rd_launch_step_set(e->st, e->d_step, step));
@@ -1297,6 +1614,7 @@ int rd_update_position(rd_engine* e, int step) {
 }
 
 int rd_remove_particles(rd_engine* e, int step) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_remove_particles");
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   CK(rd_launch_step_set(e->st, e->d_step, step));
@@ -1307,6 +1625,7 @@ int rd_remove_particles(rd_engine* e, int step) {
 }
 
 int rd_run(rd_engine* e, int first_step, int nsteps) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_run");
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   if (nsteps < 0) return fail(RD_ERR_INVALID, "nsteps < 0");
@@ -1350,6 +1669,7 @@ static void fill_counters(const DiodeDyn& y, rd_counters* o) {
 }
 
 int rd_counters_get(rd_engine* e, int d, rd_counters* o) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (!o) return fail(RD_ERR_INVALID, "null argument");
   DiodeDyn y;
@@ -1360,6 +1680,7 @@ int rd_counters_get(rd_engine* e, int d, rd_counters* o) {
 }
 
 int rd_validate(rd_engine* e, int counts[RD_VALIDATE_KINDS], long long* total) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_validate");
   if (!e || !counts) return fail(RD_ERR_INVALID, "null argument");
   const int S = e->nslots_hw();
@@ -1412,6 +1733,7 @@ long long state_bytes(int n) {
 }  // namespace
 
 int rd_diode_state_size(rd_engine* e, int d, long long* bytes) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (!bytes) return fail(RD_ERR_INVALID, "null argument");
   DiodeDyn y;
@@ -1422,6 +1744,7 @@ int rd_diode_state_size(rd_engine* e, int d, long long* bytes) {
 }
 
 int rd_diode_save(rd_engine* e, int d, void* buf, long long cap, long long* written) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_diode_save");
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (!buf) return fail(RD_ERR_INVALID, "null buffer");
@@ -1453,6 +1776,7 @@ int rd_diode_save(rd_engine* e, int d, void* buf, long long cap, long long* writ
 }
 
 int rd_diode_load(rd_engine* e, int d, const void* buf, long long size) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_diode_load");
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (!buf || size < (long long)sizeof(StateHeader)) return fail(RD_ERR_INVALID, "not a diode state");
@@ -1484,6 +1808,7 @@ int rd_diode_load(rd_engine* e, int d, const void* buf, long long size) {
 }
 
 int rd_life_time(rd_engine* e, int d, int* hist) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!valid_diode(e, d)) return fail(RD_ERR_NOTFOUND, "unknown diode");
   if (!hist) return fail(RD_ERR_INVALID, "null argument");
   CK(cudaMemcpy(hist, e->life + (size_t)d * RD_MAX_LIFE, sizeof(int) * RD_MAX_LIFE, cudaMemcpyDeviceToHost));
@@ -1499,6 +1824,7 @@ int rd_last_run_stats(rd_engine* e, double* ms, int* kps) {
 
 
 int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   NvtxRange nvtx_range("rd_profile_step");
   if (!e || !out) return fail(RD_ERR_INVALID, "null argument");
   *out = rd_phase_times{};
@@ -1537,14 +1863,16 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
       out->mh_pair_evals += (long long)dyn[d].chains * dyn[d].n * sl.p.mh_jumps;
     }
     CK(plan(e, PM_MH));
+    if (s.emit_planar)
+      CK(rd_launch_mh_vacuum(prec, S, e->st, e->dP, e->dD, e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
     const int gmask = (s.emit_planar ? 1 : 0) | (s.emit_tip ? 2 : 0);
     CK(rd_launch_mh_jump(prec, gmask, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                          e->cs, e->d_choff, e->wtab, e->d_step, 0, e->partial, e->tickets, e->kscale, e->item_queue,
-                         0, s.mh_planar == 1));
+                         0, 1, mh_form_for(e, s)));
     CK(rd_launch_mh_init(prec, e->grid, e->st, e->dP, e->dD, e->pool, e->plan[PM_MH], e->ph[PM_MH],
                          e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
     CK(cudaEventRecord(ev[2], e->st));
-    int rcj = launch_mh_jumps(e, s);
+    int rcj = launch_mh_jumps(e, s, e->st);
     if (rcj) return rcj;
     out->mh_jump_launches = s.jumps;
     CK(cudaEventRecord(ev[3], e->st));
@@ -1630,6 +1958,7 @@ int rd_poll(rd_engine* e, long long id, rd_request_status* out) {
 }
 
 int rd_cancel(rd_engine* e, long long id) {
+  if (e) { const int rcf = flush_admissions(e); if (rcf) return rcf; }
   if (!e) return fail(RD_ERR_INVALID, "null engine");
   auto it = e->reqs.find(id);
   if (it == e->reqs.end()) return fail(RD_ERR_NOTFOUND, "unknown request");
@@ -1649,14 +1978,27 @@ int rd_cancel(rd_engine* e, long long id) {
   return RD_OK;
 }
 
-static int serve_admit(rd_engine* e, rd_serve_stats* st) {
+// Admits queued requests into free slots, FIFO, head of line waiting for
+// capacity.  Everything is issued on the admission stream sa and nothing waits
+// for the GPU: the slots become active at the next activate_pending(), so when
+// a step is running on the engine stream the uploads overlap it.  first_step:
+// the engine step at which the admitted diodes run their step 1.
+static int serve_admit(rd_engine* e, rd_serve_stats* st, int first_step) {
+  if (e->queue.empty()) return RD_OK;
+  bool any_free = false;
+  for (auto& sl : e->slots) if (!sl.used) { any_free = true; break; }
+  if (!any_free) return RD_OK;
+  // the previous batch's copies from the arena were waited for by the engine stream
+  // (activate_pending) and that stream was synchronised since: the arena is free
+  CK(cudaStreamSynchronize(e->sa));
+  e->adm_used = 0;
   while (!e->queue.empty()) {
     long long id = e->queue.front();
     rd_engine::Req& r = e->reqs[id];
     rd_diode_config cfg = r.cfg;
     if (!r.work.empty()) cfg.work = r.work.data();
     int slot = -1;
-    int rc = rd_diode_add(e, &cfg, &slot);
+    int rc = diode_add_impl(e, &cfg, &slot, e->sa, true, first_step - 1);
     if (rc == RD_ERR_CAPACITY) return RD_OK;   // head of line waits for capacity
     if (rc) {                                  // invalid request: drop it
       r.st.state = RD_REQ_CANCELLED;
@@ -1664,11 +2006,11 @@ static int serve_admit(rd_engine* e, rd_serve_stats* st) {
       e->queue.pop_front();
       continue;
     }
-    int off = e->gstep - 1;   // the diode's first step is 1
-    CK(cudaMemcpy(&e->dD[slot].step_offset, &off, sizeof(int), cudaMemcpyHostToDevice));
+    // the slot exists on the host now; its device slot stays inactive until activation
+    e->slots[slot].used = true;
     const int n = (int)(r.pos.size() / 3);
-    if (n > 0) {
-      rc = rd_add_particles(e, slot, n, r.pos.data(), r.vel.empty() ? nullptr : r.vel.data(), nullptr, 0, 1);
+    if (n > 0 || true) {
+      rc = add_particles_deferred(e, slot, n, r.pos.data(), r.vel.empty() ? nullptr : r.vel.data(), 0, 1);
       if (rc) return rc;
       st->h2d_bytes += (long long)(r.pos.size() + r.vel.size()) * sizeof(double);
     }
@@ -1693,8 +2035,11 @@ int rd_serve(rd_engine* e, int iterations, rd_serve_stats* out) {
   std::vector<DiodeDyn> dyn(S);
   std::vector<double> times;
   for (int it = 0; it < iterations; ++it) {
-    int rc = serve_admit(e, out);
-    if (rc) return rc;
+    int rc;
+    // with nothing running, admit now; otherwise the requests admitted while the
+    // previous step ran (overlapped with it) become active here
+    if (e->running.empty() && (rc = serve_admit(e, out, e->gstep))) return rc;
+    if ((rc = activate_pending(e))) return rc;
     if (e->running.empty()) break;
     if ((rc = ensure_graph(e))) return rc;
     CK(rd_launch_step_set(e->st, e->d_step, e->gstep));
@@ -1702,6 +2047,10 @@ int rd_serve(rd_engine* e, int iterations, rd_serve_stats* out) {
     CK(cudaGraphLaunch(e->graph, e->st));
     CK(cudaEventRecord(e->ev1, e->st));
     CK(cudaMemcpyAsync(dyn.data(), e->dD, sizeof(DiodeDyn) * S, cudaMemcpyDeviceToHost, e->st));
+    // while the step runs: admit queued requests into the slots free now, for the next step
+    std::vector<char> was_pending(S, 0);
+    if ((rc = serve_admit(e, out, e->gstep + 1))) return rc;
+    for (int sidx : e->pending) was_pending[sidx] = 1;
     CK(cudaStreamSynchronize(e->st));
     out->d2h_bytes += (long long)sizeof(DiodeDyn) * S;
     float ms = 0.f;
@@ -1712,6 +2061,7 @@ int rd_serve(rd_engine* e, int iterations, rd_serve_stats* out) {
     e->gstep++;
     std::vector<int> done;
     for (auto& kv : e->running) {
+      if (was_pending[kv.first]) continue;   // admitted during this step: not active yet
       const DiodeDyn& y = dyn[kv.first];
       rd_engine::Req& r = e->reqs[kv.second];
       out->electron_steps += y.electron_steps - r.st.counters.electron_steps;

@@ -19,6 +19,8 @@
 //    Do_Field_Emission_Tip_OLDCODE :417-534).  Random numbers are Philox
 //    streams keyed by the diode seed with counters (chain, iteration, step,
 //    purpose), so every chain is reproducible and independent of scheduling.
+#include <cooperative_groups.h>
+
 #include "rd_tiles.cuh"
 
 
@@ -178,10 +180,11 @@ __device__ __forceinline__ double supply_log_xy(const DiodeParams& p, const doub
 
 // ---- FP32 forms of the MH arithmetic (FP32-compensated planar chains) -----------------
 // The FP32 form keeps each chain as FP32 nm offsets from the emitter centre
-// and draws, proposes and tests in FP32; only the field finish and the state
-// handed to the emission test (x, y, F of accepted points) are FP64.  FP64 is
-// a small fraction of the FP32 rate on this part, and this arithmetic runs
-// once per chain per work item.
+// and draws and proposes in FP32; the field finish, the state handed to the
+// emission test (x, y, F of accepted points) and the accept / reject decision
+// are FP64 (mh_accept_one_f: an FP32 filter decides when it is certain, the
+// FP64 targets otherwise).  FP64 is a small fraction of the FP32 rate on this
+// part, and this arithmetic runs once per chain per work item.
 
 // A uniform float in (0, 1) from 24 bits of a Philox word.
 __device__ __forceinline__ float u01f(uint32_t w) {
@@ -738,7 +741,7 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
         const float fy = fminf(fmaf(v2, p.em_wy, -p.em_hy), p.em_hy);
         const double x = p.org_x + (double)fx * 1.0e-9, y = p.org_y + (double)fy * 1.0e-9;
         const double Fz = warp_field_planar_z0<PREC>(p, pool, n, x, y, kscale);
-        if (Fz < 0.0 && (float)Fz < 0.0f) {
+        if (Fz < 0.0) {
           ok = 1; F = Fz; X = x; Y = y;
           if (lane == 0) {
             cs.fx[k] = fx; cs.fy[k] = fy;
@@ -782,6 +785,19 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
 }
 
 // ---- MH jump iteration ---------------------------------------------------------------------
+// The MH_std update of one jump iteration from its acceptance counts
+// (MH_std_update :603-612, once per iteration after the warm-up jumps).
+__device__ __forceinline__ void mh_std_step(const DiodeParams& p, double* mh_std, double* a_rate, int it_idx,
+                                            int ndim_first, int A, int R) {
+  if (it_idx > ndim_first && A + R > 0) {
+    double rate = (double)A / (double)(A + R);
+    *a_rate = rate;
+    double s = *mh_std * exp(0.025 * (rate - 0.35));
+    if (s > p.mh_hi) s = p.mh_hi; else if (s < p.mh_lo) s = p.mh_lo;
+    *mh_std = s;
+  }
+}
+
 __device__ __forceinline__ void mh_counts_and_update(const DiodeParams& p, DiodeDyn& y, int tiles,
                                                      int it_idx, int ndim_first, int a, int r,
                                                      int* red_i) {
@@ -802,13 +818,7 @@ __device__ __forceinline__ void mh_counts_and_update(const DiodeParams& p, Diode
       __threadfence();
       int A = atomicExch(&y.mh_acc, 0), R = atomicExch(&y.mh_rej, 0);
       y.mh_done = 0;
-      if (it_idx > ndim_first && A + R > 0) {   // MH_std_update :603-612
-        double rate = (double)A / (double)(A + R);
-        y.a_rate = rate;
-        double s = y.MH_std * exp(0.025 * (rate - 0.35));
-        if (s > p.mh_hi) s = p.mh_hi; else if (s < p.mh_lo) s = p.mh_lo;
-        y.MH_std = s;
-      }
+      mh_std_step(p, &y.MH_std, &y.a_rate, it_idx, ndim_first, A, R);
     }
   }
   __syncthreads();
@@ -839,20 +849,63 @@ __device__ __forceinline__ int mh_accept_one(const DiodeParams& p, ChainState& c
   return a;
 }
 
+// The FP64 target Elec_Supply_log (src/mod_field_emission_v2.F90:589-595) of
+// an FP32 chain's point (FP32 nm offsets from the emitter centre), with the
+// work-function cell or site chosen exactly as supply_log_xy_f chooses it.
+__device__ __forceinline__ double supply_log_chain_d(const DiodeParams& p, const double* __restrict__ wtab,
+                                                     float x, float y, double F) {
+  if (p.work_model == 1) return supply_log_tab(p, wtab, work_cell_f(p, x, y), F);
+  const double X = p.org_x + (double)x * 1.0e-9, Y = p.org_y + (double)y * 1.0e-9;
+  const int cell = work_cell(p, X, Y);
+  if (cell >= 0) return supply_log_tab(p, wtab, cell, F);
+  return fn_supply_log(F, gaussian_work(p, p.work_data, X, Y), p.image_charge);
+}
+
+// Guard band of the FP32 acceptance filter.  The FP32 target differs from the
+// FP64 one by at most ~1e-5 (logf within 1 ulp of values below ~50, the
+// field rounded to a float, three float additions), the FP32 log u by at most
+// ~2e-5 (see mh_accept_one_f), so a margin of 1e-3 leaves a factor of ~30.
+#define RD_MH_GUARD 1.0e-3f
+
+// The FP64 form's accept test for a decision inside the guard band (rare; kept
+// out of line so that it does not cost the pair-sum loop registers).  o0, o1
+// are the Philox words of the FP64 form's uniform u (u01_words).
+__device__ __noinline__ bool mh_take_fp64(const DiodeParams& p, const double* __restrict__ wtab, float wx,
+                                          float wy, double F, float cx, float cy, double Fc, uint32_t o0,
+                                          uint32_t o1) {
+  const double snd = supply_log_chain_d(p, wtab, wx, wy, F);
+  const double scd = supply_log_chain_d(p, wtab, cx, cy, Fc);
+  return snd >= scd || log(u01_words(o0, o1)) <= snd - scd;
+}
+
 // mh_accept_one for the FP32 chains (proposal wx, wy in FP32 nm offsets).
+// The decision is the FP64 form's (:1400-1443): take the proposal iff
+// log u <= sn - sc, with the 53-bit uniform u of the FP64 form and the FP64
+// targets sn (proposal) and sc (current point).  FP32 estimates decide it
+// whenever they are further than RD_MH_GUARD from the threshold (the FP64
+// comparison must then agree); otherwise both targets and log u are
+// evaluated in FP64 -- a few in ten thousand decisions.  The FP32 estimate of
+// u is the leading Philox word o0 / 2^32 (u lies in [o0, o0 + 1) / 2^32), whose
+// log is within 1.6e-5 of log u for o0 >= 2^16; smaller words (one draw in
+// 65536) take the FP64 test.  Chains store the FP32 estimate of their target; the FP64 one is
+// recomputed from the stored point and field (cs.F, FP64) when needed.
 __device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState& cs, const double* wtab,
                                                int c, int k, int it_idx, uint32_t step, double F,
                                                float wx, float wy) {
   int a = 0;
-  const float Ff = (float)F;
-  if (F < 0.0 && Ff < 0.0f) {
-    const float sn = supply_log_xy_f(p, wtab, wx, wy, Ff);
-    const float sc = cs.fsup[k];
-    bool take = sn >= sc;
-    if (!take) {
-      float u1, u2;
-      rng2f(p.seed, (uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, &u1, &u2);
-      take = logf(u1) <= sn - sc;
+  if (F < 0.0) {
+    const float sn = supply_log_xy_f(p, wtab, wx, wy, (float)F);
+    const float df = sn - cs.fsup[k];
+    bool take;
+    if (isfinite(df) && df >= RD_MH_GUARD) {
+      take = true;                       // sn > sc in FP64 too, and log u <= 0
+    } else {
+      uint32_t o[4];
+      philox4x32((uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, (uint32_t)p.seed, (uint32_t)(p.seed >> 32), o);
+      const float lu = logf((float)o[0] * 2.3283064365386963e-10f);
+      if (o[0] >= 65536u && isfinite(df) && lu <= df - RD_MH_GUARD) take = true;
+      else if (o[0] >= 65536u && isfinite(df) && lu > df + RD_MH_GUARD) take = false;
+      else take = mh_take_fp64(p, wtab, wx, wy, F, cs.fx[k], cs.fy[k], cs.F[k], o[0], o[1]);   // guard band
     }
     if (take) {
       cs.fx[k] = wx; cs.fy[k] = wy; cs.fsup[k] = sn; cs.F[k] = F;
@@ -867,6 +920,84 @@ __device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState&
     cs.fgx[k] = g1; cs.fgy[k] = g2;
   }
   return a;
+}
+
+// Proposal of planar chain c (slot k) for a jump: round 0 of the uniform start
+// (init, :1321-1364), the current point (dry: autotuner timing), or the stored
+// Gaussian pair times the step size (sx, sy) plus the current point, reflected
+// at the emitter edges (check_limits_metro_rec :1466-1516).  FP32 chains: nm
+// offsets from the emitter centre, half widths hx, hy.
+__device__ __forceinline__ void mh_propose_f32(const DiodeParams& p, const ChainState& cs, int k, int c, int ok,
+                                               bool init, bool dry, uint32_t step, float sx, float sy, float hx,
+                                               float hy, float* px, float* py) {
+  float x = 0.0f, yv = 0.0f;
+  if (init && ok) {
+    float u1, u2;
+    rng2f(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+    x = fminf(fmaf(u1, p.em_wx, -hx), hx);
+    yv = fminf(fmaf(u2, p.em_wy, -hy), hy);
+  } else if (dry && ok) {
+    x = cs.fx[k]; yv = cs.fy[k];
+  } else if (ok) {
+    x = fmaf(cs.fgx[k], sx, cs.fx[k]);
+    yv = fmaf(cs.fgy[k], sy, cs.fy[k]);
+    if (x > hx) x = hx - (x - hx); else if (x < -hx) x = -hx - (x + hx);
+    if (yv > hy) yv = hy - (yv - hy); else if (yv < -hy) yv = -hy - (yv + hy);
+  }
+  *px = x; *py = yv;
+}
+
+__device__ __forceinline__ void mh_propose_f64(const DiodeParams& p, const ChainState& cs, int k, int c, int ok,
+                                               bool init, bool dry, uint32_t step, double sx, double sy,
+                                               double* px, double* py) {
+  double wx = p.em_x0, wy = p.em_y0;
+  if (init && ok) {
+    double u1, u2;
+    rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+    wx = u1 * p.em_Lx + p.em_x0;
+    wy = u2 * p.em_Ly + p.em_y0;
+  } else if (dry && ok) {
+    wx = cs.x[k]; wy = cs.y[k];
+  } else if (ok) {
+    double x = cs.gx[k] * sx + cs.x[k], yv = cs.gy[k] * sy + cs.y[k];
+    const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+    if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
+    if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
+    wx = x; wy = yv;
+  }
+  *px = wx; *py = wy;
+}
+
+// Round 0 of a chain's uniform start, given the field F at its first draw: a
+// favourable point (F < 0) makes the chain, with its target and the Gaussian
+// pair of jump 1; otherwise k_mh_init continues from round 1.
+__device__ __forceinline__ void mh_start_f32(const DiodeParams& p, ChainState& cs, const double* wtab, int k, int c,
+                                             uint32_t step, double F, float x, float y) {
+  if (F < 0.0 && p.init_rounds > 0) {
+    cs.ok[k] = 1; cs.F[k] = F;
+    cs.fx[k] = x; cs.fy[k] = y;
+    cs.x[k] = p.org_x + (double)x * 1.0e-9;
+    cs.y[k] = p.org_y + (double)y * 1.0e-9;
+    cs.fsup[k] = supply_log_xy_f(p, wtab, x, y, (float)F);
+    float g1, g2;
+    gauss2f(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
+    cs.fgx[k] = g1; cs.fgy[k] = g2;
+  } else {
+    cs.ok[k] = 0;
+  }
+}
+
+__device__ __forceinline__ void mh_start_f64(const DiodeParams& p, ChainState& cs, const double* wtab, int k, int c,
+                                             uint32_t step, double F, double x, double y) {
+  if (F < 0.0 && p.init_rounds > 0) {
+    cs.ok[k] = 1; cs.F[k] = F; cs.x[k] = x; cs.y[k] = y;
+    cs.sup[k] = supply_log_xy(p, wtab, x, y, F);
+    double g1, g2;
+    gauss2(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
+    cs.gx[k] = g1; cs.gy[k] = g2;
+  } else {
+    cs.ok[k] = 0;
+  }
 }
 
 // One Metropolis-Hastings jump iteration of the planar chains (it_idx >= 1),
@@ -885,16 +1016,17 @@ __device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState&
 // FP32: 32 threads, four chains each, at most 64 registers so that 32 CTAs
 // (the per-SM block limit) are resident: 32 warps instead of the 28 that
 // 72 registers allowed, +1.6 % on the served step; FP64: 128 threads, one
-// chain each.  LONE (FP32, a single emitting planar diode): 64 threads, two
-// chains each, so that a diode's few tiles spread over twice the warps; a
-// chain's sum is the same lane arithmetic in the same j order either way.
+// chain each.  LONE (FP32): 64 threads, two chains each, so that a diode's few
+// tiles spread over twice the warps (the default for a single emitting planar
+// diode; rd_autotune may pick it for any mix); a chain's sum is the same lane
+// arithmetic in the same j order either way.
 template <int PREC, int LONE>
 __global__ void __launch_bounds__(PREC == 1 ? (LONE ? 64 : 32) : RD_ITILE, PREC == 1 ? (LONE ? 16 : 32) : 1)
 k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
                  const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph, ChainState cs,
                  const int* __restrict__ ch_off, const double* __restrict__ wtab,
                  const int* __restrict__ step_ptr, int it_idx, double* __restrict__ partial,
-                 int* __restrict__ tickets, double kscale, int* __restrict__ queue, int part) {
+                 int* __restrict__ tickets, double kscale, int* __restrict__ queue, int part, int nparts) {
   __shared__ int red_i[2 * RD_ITILE];
   __shared__ int s_item;
   constexpr int CPT = PREC == 1 ? (LONE ? 2 : 4) : 1;
@@ -903,7 +1035,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
   const bool init = it_idx == 0;
   const bool dry = it_idx < 0;   // timing pass: field at the current points, nothing written
   int lo, hi;   // this launch's part of the plan (part_range)
-  part_range(plan, nd, total, part, RD_MH_PARTS, &lo, &hi);
+  part_range(plan, nd, total, part, nparts, &lo, &hi);
   for (int g = queue_first(lo, hi); g < hi; g = queue_next(queue, &s_item, lo, hi)) {
     ItemRef it = decode_item(plan, nd, g);
     const DiodeParams& p = P[it.d];
@@ -924,22 +1056,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
         const int c = it.i0 + tid + q * nt;
         kk[q] = ch_off[it.d] + c;
         ok[q] = (c < M) ? (init ? 1 : cs.ok[kk[q]]) : 0;
-        float x = 0.0f, yv = 0.0f;
-        if (init && ok[q]) {   // round 0 of the uniform start (:1321-1364)
-          float u1, u2;
-          rng2f(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
-          x = fminf(fmaf(u1, p.em_wx, -hx), hx);
-          yv = fminf(fmaf(u2, p.em_wy, -hy), hy);
-        } else if (dry && ok[q]) {
-          x = cs.fx[kk[q]]; yv = cs.fy[kk[q]];
-        } else if (ok[q]) {    // Gaussian step, reflected at the edges (:1466-1516)
-          const int k = kk[q];
-          x = fmaf(cs.fgx[k], sx, cs.fx[k]);
-          yv = fmaf(cs.fgy[k], sy, cs.fy[k]);
-          if (x > hx) x = hx - (x - hx); else if (x < -hx) x = -hx - (x + hx);
-          if (yv > hy) yv = hy - (yv - hy); else if (yv < -hy) yv = -hy - (yv + hy);
-        }
-        fwx[q] = x; fwy[q] = yv;
+        mh_propose_f32(p, cs, kk[q], c, ok[q], init, dry, step, sx, sy, hx, hy, &fwx[q], &fwy[q]);
       }
     } else {
       const double mhs = y.MH_std;
@@ -949,22 +1066,7 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
         const int c = it.i0 + tid + q * nt;
         kk[q] = ch_off[it.d] + c;
         ok[q] = (c < M) ? (init ? 1 : cs.ok[kk[q]]) : 0;
-        wx[q] = p.em_x0; wy[q] = p.em_y0;
-        if (init && ok[q]) {   // round 0 of the uniform start (:1321-1364)
-          double u1, u2;
-          rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
-          wx[q] = u1 * p.em_Lx + p.em_x0;
-          wy[q] = u2 * p.em_Ly + p.em_y0;
-        } else if (dry && ok[q]) {
-          wx[q] = cs.x[kk[q]]; wy[q] = cs.y[kk[q]];
-        } else if (ok[q]) {
-          const int k = kk[q];
-          double x = cs.gx[k] * sx + cs.x[k], yv = cs.gy[k] * sy + cs.y[k];
-          const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
-          if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
-          if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
-          wx[q] = x; wy[q] = yv;
-        }
+        mh_propose_f64(p, cs, kk[q], c, ok[q], init, dry, step, sx, sy, &wx[q], &wy[q]);
       }
     }
     double s[CPT];
@@ -994,30 +1096,8 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
         if (!ok[q]) continue;
         const int c = it.i0 + tid + q * nt, k = kk[q];
         const double F = z0_finish<PREC>(p, s[q], kscale);
-        if constexpr (PREC == 1) {
-          if (F < 0.0 && (float)F < 0.0f && p.init_rounds > 0) {
-            cs.ok[k] = 1; cs.F[k] = F;
-            cs.fx[k] = fwx[q]; cs.fy[k] = fwy[q];
-            cs.x[k] = p.org_x + (double)fwx[q] * 1.0e-9;
-            cs.y[k] = p.org_y + (double)fwy[q] * 1.0e-9;
-            cs.fsup[k] = supply_log_xy_f(p, wtab, fwx[q], fwy[q], (float)F);
-            float g1, g2;
-            gauss2f(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
-            cs.fgx[k] = g1; cs.fgy[k] = g2;
-          } else {
-            cs.ok[k] = 0;
-          }
-        } else {
-          if (F < 0.0 && p.init_rounds > 0) {
-            cs.ok[k] = 1; cs.F[k] = F; cs.x[k] = wx[q]; cs.y[k] = wy[q];
-            cs.sup[k] = supply_log_xy(p, wtab, wx[q], wy[q], F);
-            double g1, g2;
-            gauss2(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
-            cs.gx[k] = g1; cs.gy[k] = g2;
-          } else {
-            cs.ok[k] = 0;
-          }
-        }
+        if constexpr (PREC == 1) mh_start_f32(p, cs, wtab, k, c, step, F, fwx[q], fwy[q]);
+        else mh_start_f64(p, cs, wtab, k, c, step, F, wx[q], wy[q]);
       }
       continue;
     }
@@ -1037,6 +1117,115 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
   queue_leave(queue, lo, hi);
 }
 
+// The whole batched MH sampling of a planar diode with no particle in flight
+// (rd_mh_vacuum), in one launch: one cluster of RD_VAC_CTAS CTAs per diode
+// slot runs round 0 of the chains' start, the rounds k_mh_init would run, and
+// every jump.  With no charges the field at every point is z0_finish(p, 0), the
+// value the tiled kernels compute from their empty pair sums, and proposals,
+// starts and accept tests are the same device functions, so the chains evolve
+// bit for bit as in k_mh_jump_planar + k_mh_init.  After each jump the CTAs
+// reduce their acceptance counts, exchange them through distributed shared
+// memory across a cluster barrier and each apply the same MH_std update
+// (MH_std_update :603-612); jumps alternate between two count buffers, so a
+// CTA never overwrites counts another may still read.  Clusters of slots that
+// are not such diodes leave at once (the test is uniform over a cluster).
+template <int PREC>
+__global__ void __cluster_dims__(RD_VAC_CTAS, 1, 1) __launch_bounds__(RD_VAC_THREADS)
+k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainState cs,
+            const int* __restrict__ ch_off, const double* __restrict__ wtab, const int* __restrict__ step_ptr,
+            double kscale, int nslots) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  __shared__ int s_cnt[2][2];
+  __shared__ int s_red[2][RD_VAC_THREADS / 32];
+  __shared__ double s_mhs;
+  const int d = blockIdx.x / RD_VAC_CTAS;
+  if (d >= nslots) return;
+  const DiodeParams& p = P[d];
+  DiodeDyn& y = Dy[d];
+  if (!p.active || !rd_mh_vacuum(p, y) || y.chains <= 0) return;
+  const int rank = (int)cl.block_rank(), tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int M = y.chains, base = ch_off[d];
+  const int G = RD_VAC_CTAS * RD_VAC_THREADS, g0 = rank * RD_VAC_THREADS + tid;
+  const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
+  const double F = z0_finish<PREC>(p, 0.0, kscale);
+  const int ndim_first = (p.mh_jumps + 2) / 4;
+  double mhs = y.MH_std, arate = y.a_rate;
+  // the start: round 0; a chain that fails it fails every round (the field does not change)
+  int failed = 0;
+  for (int c = g0; c < M; c += G) {
+    const int k = base + c;
+    if constexpr (PREC == 1) {
+      float x, yv;
+      mh_propose_f32(p, cs, k, c, 1, true, false, step, 0.0f, 0.0f, p.em_hx, p.em_hy, &x, &yv);
+      mh_start_f32(p, cs, wtab, k, c, step, F, x, yv);
+    } else {
+      double x, yv;
+      mh_propose_f64(p, cs, k, c, 1, true, false, step, 0.0, 0.0, &x, &yv);
+      mh_start_f64(p, cs, wtab, k, c, step, F, x, yv);
+    }
+    if (!cs.ok[k]) {   // k_mh_init's record of a chain with no favourable start
+      cs.F[k] = 1.0; cs.sup[k] = -1.79769313486231570e308;
+      cs.x[k] = p.em_x0; cs.y[k] = p.em_y0;
+      failed++;
+    }
+  }
+  if (failed) atomicAdd(&y.chains_failed, failed);
+  for (int it = 1; it <= p.mh_jumps; ++it) {
+    int a = 0, r = 0;
+    if constexpr (PREC == 1) {
+      const float mf = (float)mhs;
+      const float sx = (it > ndim_first) ? p.em_wx * mf : p.em_wx * 0.10f;
+      const float sy = (it > ndim_first) ? p.em_wy * mf : p.em_wy * 0.10f;
+      for (int c = g0; c < M; c += G) {
+        const int k = base + c;
+        if (!cs.ok[k]) continue;
+        float x, yv;
+        mh_propose_f32(p, cs, k, c, 1, false, false, step, sx, sy, p.em_hx, p.em_hy, &x, &yv);
+        const int acc = mh_accept_one_f(p, cs, wtab, c, k, it, step, F, x, yv);
+        a += acc; r += 1 - acc;
+      }
+    } else {
+      const double sx = (it > ndim_first) ? p.em_Lx * mhs : p.em_Lx * 0.10;
+      const double sy = (it > ndim_first) ? p.em_Ly * mhs : p.em_Ly * 0.10;
+      for (int c = g0; c < M; c += G) {
+        const int k = base + c;
+        if (!cs.ok[k]) continue;
+        double x, yv;
+        mh_propose_f64(p, cs, k, c, 1, false, false, step, sx, sy, &x, &yv);
+        const int acc = mh_accept_one(p, cs, wtab, c, k, it, step, F, x, yv);
+        a += acc; r += 1 - acc;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      r += __shfl_xor_sync(0xffffffffu, r, o);
+    }
+    if (lane == 0) { s_red[0][w] = a; s_red[1][w] = r; }
+    __syncthreads();
+    const int par = it & 1;
+    if (tid == 0) {
+      int A = 0, R = 0;
+      for (int k = 0; k < RD_VAC_THREADS / 32; ++k) { A += s_red[0][k]; R += s_red[1][k]; }
+      s_cnt[par][0] = A; s_cnt[par][1] = R;
+    }
+    cl.sync();   // every CTA's counts of this jump are in place
+    if (tid == 0) {
+      int A = 0, R = 0;
+      for (int q = 0; q < RD_VAC_CTAS; ++q) {
+        const int* rc = cl.map_shared_rank(&s_cnt[par][0], q);
+        A += rc[0]; R += rc[1];
+      }
+      mh_std_step(p, &mhs, &arate, it, ndim_first, A, R);
+      s_mhs = mhs;
+    }
+    __syncthreads();
+    mhs = s_mhs;
+  }
+  if (rank == 0 && tid == 0) { y.MH_std = mhs; y.a_rate = arate; }
+  cl.sync();   // no CTA leaves while another may still read its counts
+}
+
 // Field sums of one j-tile at CPT tip proposals (upper role: the point's own
 // apex-sphere image, as tip_tile_split_f32<T_UPPER>); one shared load feeds all of the
 // thread's points.  The tip image term of the reference carries an extra
@@ -1054,13 +1243,15 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
 // known from the tile load): the charge multiply is dropped and the sign goes
 // into the accumulating FMA, which saves one of the ~27 FP32 operations of
 // each term pair.
-template <int CPT, bool ELEC>
+template <int CPT, bool ELEC, bool IC>
 __device__ __forceinline__ void tip_point_tiles_f32(const float4* __restrict__ sh, const float4* __restrict__ sl,
-                                                    int kmax, const float4* ih, const float4* iih, int ic,
+                                                    int kmax, const float4* ih, const float4* iih,
                                                     float (*td)[3], float (*te)[3]) {
+  constexpr bool ic = IC;   // image charges on: a template argument, no branch in the pair loop
   float dx_[CPT], dy_[CPT], dz_[CPT], ex_[CPT], ey_[CPT], ez_[CPT];
 #pragma unroll
   for (int q = 0; q < CPT; ++q) dx_[q] = dy_[q] = dz_[q] = ex_[q] = ey_[q] = ez_[q] = 0.f;
+#pragma unroll 2
   for (int k = 0; k < kmax; ++k) {
     const float4 h = sh[k], l = sl[k];
     const float qj = h.w;
@@ -1165,10 +1356,14 @@ k_mh_jump_tip(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool
         float td[CPT][3], te[CPT][3];
 #pragma unroll
         for (int q = 0; q < CPT; ++q) td[q][0] = td[q][1] = td[q][2] = te[q][0] = te[q][1] = te[q][2] = 0.f;
-        if (elec)
-          tip_point_tiles_f32<CPT, true>(sh, sl, min(RD_TILE, it.j1 - jt), ih, iih, p.image_charge, td, te);
-        else
-          tip_point_tiles_f32<CPT, false>(sh, sl, min(RD_TILE, it.j1 - jt), ih, iih, p.image_charge, td, te);
+        const int kmax = min(RD_TILE, it.j1 - jt);
+        if (p.image_charge) {
+          if (elec) tip_point_tiles_f32<CPT, true, true>(sh, sl, kmax, ih, iih, td, te);
+          else tip_point_tiles_f32<CPT, false, true>(sh, sl, kmax, ih, iih, td, te);
+        } else {
+          if (elec) tip_point_tiles_f32<CPT, true, false>(sh, sl, kmax, ih, iih, td, te);
+          else tip_point_tiles_f32<CPT, false, false>(sh, sl, kmax, ih, iih, td, te);
+        }
 #pragma unroll
         for (int q = 0; q < CPT; ++q) {
           accd[q].add(td[q][0], td[q][1], td[q][2]);
@@ -1709,6 +1904,25 @@ cudaError_t rd_launch_supply_reduce(int nslots, cudaStream_t st, const DiodePara
   return cudaGetLastError();
 }
 
+// Switches the step graph's conditional MH node on when the MH plan has work items.
+__global__ void k_mh_cond(cudaGraphConditionalHandle h, const PlanHeader* __restrict__ ph) {
+  cudaGraphSetConditional(h, ph->total_items > 0 ? 1u : 0u);
+}
+
+cudaError_t rd_launch_mh_cond(cudaStream_t st, cudaGraphConditionalHandle h, const PlanHeader* ph) {
+  k_mh_cond<<<1, 1, 0, st>>>(h, ph);
+  return cudaGetLastError();
+}
+
+cudaError_t rd_launch_mh_vacuum(int prec, int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
+                                const ChainState& cs, const int* ch_off, const double* wtab, const int* step_ptr,
+                                double kscale) {
+  const int grid = nslots * RD_VAC_CTAS;
+  if (prec == 1) k_mh_vacuum<1><<<grid, RD_VAC_THREADS, 0, st>>>(P, Dy, cs, ch_off, wtab, step_ptr, kscale, nslots);
+  else k_mh_vacuum<0><<<grid, RD_VAC_THREADS, 0, st>>>(P, Dy, cs, ch_off, wtab, step_ptr, kscale, nslots);
+  return cudaGetLastError();
+}
+
 cudaError_t rd_launch_mh_init(int prec, int grid, cudaStream_t st, const DiodeParams* P,
                               DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan,
                               const PlanHeader* ph, const ChainState& cs, const int* ch_off,
@@ -1723,13 +1937,13 @@ cudaError_t rd_launch_mh_jump(int prec, int geometry_mask, int grid, cudaStream_
                               const PlanEntry* plan, const PlanHeader* ph, const ChainState& cs,
                               const int* ch_off, const double* wtab, const int* step_ptr,
                               int it_idx, double* partial, int* tickets, double kscale, int* queue,
-                              int part, bool lone) {
-  // part (planar jumps): 0 all items, 1..RD_MH_PARTS one part of the plan (part_range);
-  // lone: the only emitting planar diode (FP32: the 64-thread form)
+                              int part, int nparts, int form) {
+  // part (planar jumps): 0 all items, 1..nparts one of nparts parts of the plan (part_range);
+  // form (FP32): 0 32 threads x 4 chains, 1 64 threads x 2 chains (bit-identical results)
   if (geometry_mask & 1) {
-    if (prec == 1 && lone) k_mh_jump_planar<1, 1><<<rd_grid(k_mh_jump_planar<1, 1>, 64, grid), 64, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part);
-    else if (prec == 1) k_mh_jump_planar<1, 0><<<rd_grid(k_mh_jump_planar<1, 0>, 32, grid), 32, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part);
-    else k_mh_jump_planar<0, 0><<<rd_grid(k_mh_jump_planar<0, 0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part);
+    if (prec == 1 && form == 1) k_mh_jump_planar<1, 1><<<rd_grid(k_mh_jump_planar<1, 1>, 64, grid), 64, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part, nparts);
+    else if (prec == 1) k_mh_jump_planar<1, 0><<<rd_grid(k_mh_jump_planar<1, 0>, 32, grid), 32, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part, nparts);
+    else k_mh_jump_planar<0, 0><<<rd_grid(k_mh_jump_planar<0, 0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, Dy, pool, plan, ph, cs, ch_off, wtab, step_ptr, it_idx, partial, tickets, kscale, queue, part, nparts);
   }
   if (geometry_mask & 2) {
     k_mh_propose<<<rd_grid(k_mh_propose, 256, grid), 256, 0, st>>>(P, Dy, plan, ph, cs, ch_off, step_ptr, it_idx,

@@ -22,8 +22,10 @@
 #define RD_TILE 128           // particles per shared-memory j-tile
 #define RD_ITILE 128          // i-particles (or points) per work item
 #define RD_TIP_CPT 2          // tip MH chains per thread (FP32 form; even)
-#define RD_MH_PARTS 2         // planar MH jump launches per jump, one stream each (1..4)
+#define RD_MH_PARTS 2         // planar MH jump launches per jump, one stream each (default)
+#define RD_MH_PARTS_MAX 4     // at most this many (rd_autotune / rd_set_mh_launch choose)
 #define RD_SUP_SPLIT 16       // blocks per diode in the supply reduction
+#define RD_SUP_NCH 4          // at most this many j-chunks per tile of planar supply points
 #define RD_EMIT_SPLIT 8       // blocks per diode in the emission accept test
 // j-chunking of pair sums: at least RD_CLEN_MIN particles per chunk, at most
 // RD_NCH_MAX chunks per i-tile
@@ -92,6 +94,17 @@ enum { PM_FORCE_PLANAR = 0, PM_FORCE_TIP = 1, PM_FIELD = 2, PM_SUPPLY_PLANAR = 3
        PM_SUPPLY_TIP = 4, PM_MH = 5, PM_FORCE_TTS = 6, PM_PART = 7, PM_PART1024 = 8, PM_COUNT = 9,
        PM_ALL_DIODES = 0x100 };
 
+// Supply quadrature grid of one diode, filled on the device (k_quad_fill):
+// planar, quad_n x quad_n Gauss-Legendre nodes (P panels of Q nodes per side)
+// over the emitter rectangle, or over (angle, radius) of a ring; tip, the
+// 100 x 100 midpoint grid in (xi, phi).
+struct QuadSpec {
+  int geometry, emitter_type, P, Q, quad_n, q_off;
+  double x0, y0, Lx, Ly, ring_rmin, ring_thick, org_x, org_y;
+  double a_foci, eta_1, max_xi, shift_z;
+  double gx[16], gw[16];
+};
+
 // Dynamic per-diode state (device resident, updated by kernels).
 struct DiodeDyn {
   int n;                 // particles in flight
@@ -113,6 +126,20 @@ struct DiodeDyn {
   double avg_part_vel[3], avg_elec_vel[3], avg_ion_vel[3], avg_mob;   // Average_Velocities
   int n_vel, n_elec_vel, n_ion_vel;   // particle counts at the velocity update (before removal)
 };
+
+// A planar diode whose batched MH chains sample the vacuum field: no particle
+// in flight when its chains start, so the field at every cathode point is the
+// vacuum field and no pair sum is needed.  k_mh_vacuum runs the start and all
+// jumps of such a diode's chains in one launch (one cluster of RD_VAC_CTAS
+// CTAs); the tiled jump kernels skip it (planner mode PM_MH).
+#define RD_VAC_CTAS 8
+#define RD_VAC_THREADS 256
+#define RD_VAC_MAX_CHAINS 8192
+#ifdef __CUDACC__
+__host__ __device__ inline bool rd_mh_vacuum(const DiodeParams& p, const DiodeDyn& y) {
+  return p.geometry == RD_G_PLANAR && p.emission && !p.mh_serial && y.n == 0 && y.chains <= RD_VAC_MAX_CHAINS;
+}
+#endif
 
 // Particle pool (device pointers).
 struct Pool {

@@ -77,7 +77,8 @@ __device__ __forceinline__ int plan_ni(const DiodeParams& p, const DiodeDyn& y, 
     case PM_FIELD: return npts[d];
     case PM_SUPPLY_PLANAR: return (p.emission && p.geometry == RD_G_PLANAR) ? p.quad_n * p.quad_n : 0;
     case PM_SUPPLY_TIP: return (p.emission && p.geometry == RD_G_TIP) ? 10000 : 0;
-    case PM_MH: return (p.emission && !p.mh_serial) ? y.chains : 0;   // serial diodes: k_mh_serial
+    // serial diodes: k_mh_serial; diodes with no particle in flight: k_mh_vacuum
+    case PM_MH: return (p.emission && !p.mh_serial && !rd_mh_vacuum(p, y)) ? y.chains : 0;
     default: return nj;
   }
 }
@@ -115,6 +116,8 @@ k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int n
   const int tsize = (mode == PM_PART1024) ? 1024 : RD_ITILE;
   const bool pair = ((mode & 0xff) <= PM_FORCE_TTS);
   const int clen_min = chunk_rule & 0xffff, nch_max = chunk_rule >> 16;   // see rd_chunk_rule
+  // the planar supply points are many tiles already: at most RD_SUP_NCH chunks per tile
+  const int nch_eff = (mode & 0xff) == PM_SUPPLY_PLANAR ? min(nch_max, RD_SUP_NCH) : nch_max;
   // grow the chunk length only if the items would not fit the scratch
   __shared__ int s_grow;
   if (tid == 0) s_grow = 0;
@@ -125,7 +128,7 @@ k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int n
     for (int d = tid; d < nslots; d += blockDim.x) {
       if (!P[d].active) continue;
       int tiles, nch, clen;
-      plan_split(plan_ni(P[d], Dy[d], mode, npts, d), Dy[d].n, tsize, pair, grow, clen_min, nch_max, &tiles,
+      plan_split(plan_ni(P[d], Dy[d], mode, npts, d), Dy[d].n, tsize, pair, grow, clen_min, nch_eff, &tiles,
                  &nch, &clen);
       cnt += (double)tiles * nch;
     }
@@ -152,7 +155,7 @@ k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int n
       nj = Dy[d].n;
       ni = plan_ni(P[d], Dy[d], mode, npts, d);
       if (mode == PM_MH) chains = ni;
-      plan_split(ni, nj, tsize, pair, grow, clen_min, nch_max, &tiles, &nch, &clen);
+      plan_split(ni, nj, tsize, pair, grow, clen_min, nch_eff, &tiles, &nch, &clen);
       items = tiles * nch;
     }
     int lane = tid & 31, w = tid >> 5;
@@ -633,6 +636,62 @@ cudaError_t rd_launch_add_particles(cudaStream_t st, const DiodeParams* P, Diode
     k_add_particles<<<blocks, 256, 0, st>>>(P, Dy, pool, d, cnt, pos, vel, species, step, section);
   }
   k_add_finish<<<1, 1, 0, st>>>(P, Dy, d, cnt);
+  return cudaGetLastError();
+}
+
+// Supply quadrature points of one diode with their weights (area included)
+// and their FP32-frame split (split_nm), one thread per point: planar nodes
+// of the composite Gauss-Legendre rule (Do_Surface_Integration_FE's
+// integrand, src/mod_field_emission_v2.F90:668-745, with the ring's
+// (angle, radius) map and 2 pi w r area factor, :701-707), or the tip's
+// 100 x 100 midpoint grid in (xi, phi) with the cell areas
+// (Do_Field_Emission_Tip_OLDCODE, src/mod_emission_tip.f90:434-481; Tip_Area).
+__global__ void __launch_bounds__(256)
+k_quad_fill(QuadSpec q, double* __restrict__ qx, double* __restrict__ qy, double* __restrict__ qz,
+            double* __restrict__ qw, float4* __restrict__ qpp) {
+  const int npt = q.geometry == RD_G_TIP ? 10000 : q.quad_n * q.quad_n;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= npt) return;
+  double x, y, z = 0.0, w;
+  if (q.geometry == RD_G_TIP) {
+    const int nr = 100, i = k / nr + 1, j = k % nr + 1;
+    const double pi = c_k.pi, len_phi = 2.0 * pi / nr, len_xi = (q.max_xi - 1.0) / nr, e2 = q.eta_1 * q.eta_1;
+    const double xi_c = 1.0 + (i - 0.5) * len_xi, phi_c = (j - 0.5) * len_phi;
+    const double xy = q.a_foci * sqrt((xi_c * xi_c - 1.0) * (1.0 - q.eta_1 * q.eta_1));
+    x = xy * cos(phi_c);
+    y = xy * sin(phi_c);
+    z = (q.a_foci * xi_c) * q.eta_1 + q.shift_z;
+    const double xi1 = 1.0 + (i - 1.0) * len_xi, xi2 = 1.0 + (i + 0.0) * len_xi;
+    const double ph1 = (j - 1.0) * len_phi, ph2 = (j + 0.0) * len_phi;
+    const double f2 = xi2 * sqrt(xi2 * xi2 - e2) - e2 * log(xi2 + sqrt(xi2 * xi2 - e2));
+    const double f1 = xi1 * sqrt(xi1 * xi1 - e2) - e2 * log(xi1 + sqrt(xi1 * xi1 - e2));
+    w = (((0.5 * (q.a_foci * q.a_foci)) * sqrt(1.0 - e2)) * (ph2 - ph1)) * (f2 - f1);
+  } else {
+    const int iy = k / q.quad_n, ix = k % q.quad_n, Q = q.Q;
+    const double uy = ((iy / Q) + 0.5 * (q.gx[iy % Q] + 1.0)) / q.P, wy = 0.5 * q.gw[iy % Q] / q.P;
+    const double ux = ((ix / Q) + 0.5 * (q.gx[ix % Q] + 1.0)) / q.P, wx = 0.5 * q.gw[ix % Q] / q.P;
+    if (q.emitter_type == 4) {
+      const double angle = ux * 2.0 * c_k.pi, radius = q.ring_rmin + uy * q.ring_thick;
+      x = radius * cos(angle);
+      y = radius * sin(angle);
+      w = (wx * wy) * (2.0 * c_k.pi * q.ring_thick * radius);
+    } else {
+      x = q.x0 + ux * q.Lx;
+      y = q.y0 + uy * q.Ly;
+      w = (wx * wy) * (q.Lx * q.Ly);
+    }
+  }
+  const int g = q.q_off + k;
+  qx[g] = x; qy[g] = y; qz[g] = z; qw[g] = w;
+  const double vx = (x - q.org_x) * 1.0e9, vy = (y - q.org_y) * 1.0e9;
+  const float ax = (float)vx, ay = (float)vy;
+  qpp[g] = make_float4(ax, (float)(vx - (double)ax), ay, (float)(vy - (double)ay));
+}
+
+cudaError_t rd_launch_quad_fill(cudaStream_t st, const QuadSpec& q, double* qx, double* qy, double* qz,
+                                double* qw, float4* qpp) {
+  const int npt = q.geometry == RD_G_TIP ? 10000 : q.quad_n * q.quad_n;
+  k_quad_fill<<<(npt + 255) / 256, 256, 0, st>>>(q, qx, qy, qz, qw, qpp);
   return cudaGetLastError();
 }
 

@@ -98,11 +98,11 @@ def _one_diode(rg, orc, phi, jumps, cap=8192):
               emitter_pos=(-side / 2, -side / 2), emitter_dim=(side, side), work=[[phi]], emission=True,
               mh_jumps=jumps, seed=20261203)
     eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=cap + 64, chain_capacity=cap + 64,
-                    quad_capacity=4096)
+                    quad_capacity=rg.supply_points(**kw) + 64)
     d = eng.add_diode(**kw)
     o = orc.OracleDiode(cap=cap, V_s=2.0e3, d=1000 * NM, time_step=0.25e-15, image_charge=True, N_ic_max=0)
     o.set_planar_emitter(-side / 2, -side / 2, side, side, [[phi]])
-    o.set_emission(True, seed=20261203, mh_jumps=jumps, max_chains=cap, quad_panels=16, quad_order=4)
+    o.set_emission(True, seed=20261203, mh_jumps=jumps, max_chains=cap)   # the default supply rule
     return eng, d, o
 
 

@@ -77,7 +77,7 @@ def test_largest_diode_alone_equals_128_mix(rg):
     reqs = [st.next() for _ in range(128)]
     big = max(range(128), key=lambda k: reqs[k]["capacity"])
     eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=128, particle_capacity=128 * 32768 + 4096,
-                    chain_capacity=128 * 32768 + 4096, quad_capacity=128 * 4096 + 4096)
+                    chain_capacity=128 * 32768 + 4096, quad_capacity=128 * bench.MAX_SUPPLY_POINTS + 4096)
     ds = []
     for r in reqs:
         d = eng.add_diode(**bench.diode_kwargs(r))
@@ -89,7 +89,7 @@ def test_largest_diode_alone_equals_128_mix(rg):
     eng.close()
     r = reqs[big]
     one = rg.Engine(precision=rg.PREC_FP32C, max_diodes=1, particle_capacity=r["capacity"] + 64,
-                    chain_capacity=r["capacity"] + 64, quad_capacity=4096)
+                    chain_capacity=r["capacity"] + 64, quad_capacity=bench.MAX_SUPPLY_POINTS + 64)
     d = one.add_diode(**bench.diode_kwargs(r))
     d.add_particles(bench.prefill(r), step=0)
     one.run(1, 1)

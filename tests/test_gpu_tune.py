@@ -1,9 +1,11 @@
-"""The pair-sum chunking and its autotuner (rd_autotune / rd_set_chunking).
-The chunking sets the j-chunk lengths of every pair sum; a result depends on
-it only in the last FP32 bits, so: tuning leaves the particle state exactly
-as it was, a run continued after tuning equals the same run continued under
-the chosen chunking set by hand, and a diode is bit-identical alone and in a
-mix under any one chunking."""
+"""The pair-sum chunking, the MH launch shape and their autotuner
+(rd_autotune / rd_set_chunking / rd_set_mh_launch).  The chunking sets the
+j-chunk lengths of every pair sum; a result depends on it only in the last
+FP32 bits, so: tuning leaves the particle state exactly as it was, a run
+continued after tuning equals the same run continued under the chosen
+chunking set by hand, and a diode is bit-identical alone and in a mix under
+any one chunking.  The MH launch shape (plan parts on streams, FP32 thread
+form) changes no bit at all."""
 import numpy as np
 import pytest
 
@@ -41,7 +43,9 @@ def test_autotune_keeps_state_and_matches_chosen_chunking(rg):
     e1.run(1, 3)
     before = _state(d1)
     t = e1.autotune()
-    assert t["candidates"] == 15
+    assert t["candidates"] == 15 + 4 * 2     # chunkings, then MH parts 1-4 x two thread forms
+    assert 1 <= t["mh_parts"] <= 4 and t["mh_form"] in (0, 1)
+    assert e1.get_mh_launch() == (t["mh_parts"], t["mh_form"])
     assert t["chunk_min"] in (128, 256, 512, 1024, 2048) and t["chunk_count_max"] in (8, 16, 32)
     assert 0 < t["ms_chosen"] <= t["ms_default"]
     assert e1.get_chunking() == (t["chunk_min"], t["chunk_count_max"])
@@ -74,3 +78,22 @@ def test_alone_equals_mix_under_a_chunking(rg, chunking):
         one.run(1, 4)
         _same([m], [d.particles()])
         one.close()
+
+
+def test_mh_launch_shapes_change_no_bit(rg):
+    """Every planar MH launch shape -- 1 to 4 launches per jump over parts of
+    the plan, 32 threads x 4 chains or 64 x 2 -- gives bit-identical states."""
+    reqs = make_requests(n=5, seed=13)
+    ref = None
+    for parts, form in ((0, -1), (1, 0), (2, 1), (3, 0), (4, 1), (4, 0)):
+        eng, ds = _engine(rg, reqs)
+        eng.set_mh_launch(parts, form)
+        eng.run(1, 3)
+        if parts:
+            assert eng.get_mh_launch() == (parts, form)
+        st = _state(ds)
+        eng.close()
+        if ref is None:
+            ref = st
+        else:
+            _same(ref, st)

@@ -1,0 +1,44 @@
+"""k_mh_vacuum: the batched MH sampling of a planar diode with no particle in
+flight -- the chains' start and all their jumps -- runs in one launch (one
+thread-block cluster per diode).  It must give exactly what the tiled jump
+kernels give.  A diode holding one atom (charge 0: every pair sum adds exact
+zeros, so its field is the vacuum field bit for bit) takes the tiled kernels;
+the same diode without it takes the vacuum kernel.  One step of each must
+agree in every emission counter and in every emitted electron's position, in
+both precisions.  (The FP64 form of the empty one-diode deck is also checked
+against the oracle chain for chain in test_gpu_config_parity.py.)
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NM = 1e-9
+
+
+def _step(rg, prec, atom, jumps):
+    eng = rg.Engine(precision=prec, max_diodes=2, particle_capacity=8192, chain_capacity=8192,
+                    quad_capacity=65536, event_capacity=1 << 15)
+    d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, time_step=0.25e-15, capacity=8000,
+                      emitter_pos=(-500 * NM, -500 * NM), emitter_dim=(1000 * NM, 1000 * NM),
+                      work=[[2.0, 2.3], [2.6, 2.1]], emission=True, mh_jumps=jumps, seed=99)
+    if atom:
+        d.add_particles(np.array([[400 * NM, 400 * NM, 900 * NM]]), species=[rg.ATOM], step=0)
+    eng.step(1)
+    c = d.counters()
+    ev, lost = eng.events_take()
+    assert lost == 0
+    sites = np.array(sorted(e["pos"][:2] for e in ev if e["kind"] == rg.EVENT_EMIT))
+    eng.close()
+    return c, sites
+
+
+@pytest.mark.parametrize("prec,jumps", [(1, 200), (1, 37), (0, 60)])
+def test_vacuum_kernel_equals_tiled_kernels(rg, prec, jumps):
+    empty, s_empty = _step(rg, prec, False, jumps)
+    atom, s_atom = _step(rg, prec, True, jumps)
+    assert 1000 < empty["chains"] <= 8192 and empty["emitted_step"] > 50
+    for key in ("N_sup", "chains", "chains_failed", "MH_std", "a_rate", "df_avg", "emitted_step", "residual"):
+        assert empty[key] == atom[key], key
+    assert empty["F_avg"] == atom["F_avg"]
+    np.testing.assert_array_equal(s_empty, s_atom)
