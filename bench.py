@@ -64,6 +64,12 @@ class RequestStream:
         return req
 
 
+# Supply quadrature points of the largest emitter of the stream (2000 nm side: 100
+# panels of 4 x 4 Gauss-Legendre nodes per side, nodes 5 nm apart), the per-diode
+# bound for the quadrature tables of the serving engines.
+MAX_SUPPLY_POINTS = 400 * 400
+
+
 def diode_kwargs(req, max_chains=0):
     s = req["side"]
     return dict(V_s=req["V_s"], gap=req["gap"], time_step=0.25e-15, image_charge=True, N_ic_max=0,
@@ -170,73 +176,115 @@ class L2Flush:
 
 
 # ---------------------------------------------------------------------------------
-def cpu_sample(stream_seed, budget_pairs=2.0e10, rank=0):
+def capacity_strata(reqs):
+    """The requests by capacity octave (256-512, ..., 16384-32768): {octave: [requests]}."""
+    out = {}
+    for r in reqs:
+        out.setdefault(min(6, int(math.log2(r["capacity"] / 256.0))), []).append(r)
+    return out
+
+
+def cpu_step_seconds(orc, r, steps, jumps=(1, 2)):
+    """Seconds of one full time step of request r (pre-filled) in the oracle's
+    OpenMP restatement: supply integral, MH chains, Beeman update with the
+    all-pair forces, removal (the diode is full, so the emission test adds
+    nothing).  The MH chains are timed at two short jump counts and
+    extrapolated linearly to the step's 200 jumps (a step's MH cost is a start
+    pass plus a fixed cost per jump), so that even the largest diodes take
+    seconds.  Returns (seconds, electrons in flight)."""
+    o = orc.OracleDiode(cap=r["capacity"], V_s=r["V_s"], d=r["gap"], time_step=0.25e-15,
+                        image_charge=True, N_ic_max=0)
+    s = r["side"]
+    o.set_planar_emitter(-s / 2, -s / 2, s, s, [[r["phi"]]])
+    o.set_emission(True, seed=r["seed"], mh_jumps=jumps[0], max_chains=r["capacity"])
+    o.add_many(prefill(r), step=0)
+    t0 = time.perf_counter()
+    n_sup = o.supply()
+    t_sup = time.perf_counter() - t0
+    M = int(min(max(math.floor(n_sup + 0.5), 0), r["capacity"]))
+    mh = []
+    for j in jumps:
+        o.s.mh_jumps = j
+        t0 = time.perf_counter()
+        o.mh_batch(1, M)
+        mh.append(time.perf_counter() - t0)
+    per_jump = max(0.0, (mh[1] - mh[0]) / (jumps[1] - jumps[0]))
+    start = max(0.0, mh[0] - jumps[0] * per_jump)
+    n = o.n
+    t0 = time.perf_counter()
+    o.verlet(1)
+    o.remove(1)
+    t_upd = time.perf_counter() - t0
+    return t_sup + start + 200 * per_jump + t_upd, n
+
+
+def cpu_sample(reqs_resident, rank=0):
     """The CPU restatement of the reference path (oracle, OpenMP, all host
-    threads) on a bounded sample: full time steps of the first requests of the
-    stream whose estimated cost fits the budget (the smallest diodes, which
-    favours the CPU).  Returns (electron-steps/s, sample description, cores)."""
+    threads) on a capacity-stratified sample of the served window's resident
+    set: per capacity octave, the resident request nearest the octave's median
+    capacity runs one full time step (cpu_step_seconds), and the octave's
+    electron-steps are charged at that request's per-electron time.  So the
+    sample's per-electron cost follows the resident set's capacity mix.
+    Returns (electron-steps/s, sample description, cores, seconds measured)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import orc
     orc.build()
-    st = RequestStream(stream_seed, rank=rank)
-    used, picked = 0.0, []
-    for _ in range(400):
-        r = st.next()
-        if r is None:
-            break
-        cost = 200.0 * r["capacity"] ** 2 + 4096.0 * r["capacity"] + r["capacity"] ** 2
-        if used + cost <= budget_pairs:
-            picked.append(r)
-            used += cost
-        if len(picked) >= 6:
-            break
-    e_steps, t_tot = 0, 0.0
-    for r in picked:
-        o = orc.OracleDiode(cap=r["capacity"], V_s=r["V_s"], d=r["gap"], time_step=0.25e-15,
-                            image_charge=True, N_ic_max=0)
-        s = r["side"]
-        o.set_planar_emitter(-s / 2, -s / 2, s, s, [[r["phi"]]])
-        o.set_emission(True, seed=r["seed"], mh_jumps=200, max_chains=r["capacity"],
-                       quad_panels=16, quad_order=4)
-        for p in prefill(r):
-            o.add(p, step=0)
-        t0 = time.perf_counter()
-        o.emission(1)
-        n = o.n
-        o.verlet(1)
-        o.remove(1)
-        t_tot += time.perf_counter() - t0
-        e_steps += n
+    strata = capacity_strata(reqs_resident)
+    tot_e, tot_t, t_meas, picked = 0.0, 0.0, 0.0, []
+    for k in sorted(strata):
+        group = sorted(strata[k], key=lambda q: q["capacity"])
+        rep = group[len(group) // 2]
+        w0 = time.perf_counter()
+        secs, n = cpu_step_seconds(orc, rep, 1)
+        t_meas += time.perf_counter() - w0
+        per_e = secs / max(n, 1)
+        e_group = sum(q["capacity"] for q in group)   # pre-filled to capacity
+        tot_e += e_group
+        tot_t += per_e * e_group
+        picked.append((rep["capacity"], len(group)))
     cores = orc.lib().orc_omp_threads()
-    desc = ("1 full time step of each of %d stream requests (capacities %s) with the "
-            "oracle's OpenMP C restatement" % (len(picked), [r["capacity"] for r in picked]))
-    return (e_steps / t_tot if t_tot > 0 else 0.0), desc, cores, t_tot
+    desc = ("capacity-stratified sample of the %d resident requests of the served window: per capacity "
+            "octave one request (capacity, requests in the octave) %s runs one full step with the "
+            "oracle's OpenMP C restatement, MH timed at 1 and 2 jumps and extrapolated to 200; the "
+            "octave's electron-steps are charged at its per-electron time" % (len(reqs_resident), picked))
+    return (tot_e / tot_t if tot_t > 0 else 0.0), desc, cores, t_meas
 
 
-def plain_fp64_sample(rg, requests, budget_s=25.0):
-    """The plain FP64 GPU form, one diode at a time (own engine, rd_run per
-    diode, chunking tuned per diode like the served engine's), on a sample of
-    the served requests."""
-    e_steps, dev_s, names = 0, 0.0, []
+def plain_fp64_all(rg, requests, budget_s=600.0):
+    """The plain FP64 GPU form, one diode at a time (own engine per diode), on
+    every resident request of the served window: one untimed step (graph
+    capture), the chunking tuner for systems below 4096 electrons (a lone small
+    system needs short chunks to fill 152 SMs; larger ones fill it at the
+    default chunking), then one step timed with CUDA events (rd_run).  The
+    requests are visited in a capacity-interleaved order, so that a budget cut
+    leaves a sample spread over the capacities.  Returns (electron-steps/s,
+    capacities covered, requests in all)."""
+    order = sorted(requests, key=lambda q: q["capacity"])
+    n = len(order)
+    bits = max(1, (n - 1).bit_length())
+    idx = sorted(range(1 << bits), key=lambda k: int(format(k, "0%db" % bits)[::-1], 2))
+    order = [order[k] for k in idx if k < n]
+    e_steps, dev_s, caps = 0, 0.0, []
     t_start = time.perf_counter()
-    for r in sorted(requests, key=lambda q: q["capacity"]):
+    for r in order:
         if time.perf_counter() - t_start > budget_s:
             break
+        kw = diode_kwargs(r)
         eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=1, particle_capacity=r["capacity"] + 64,
-                        chain_capacity=r["capacity"] + 64, quad_capacity=4096)
-        d = eng.add_diode(**diode_kwargs(r))
+                        chain_capacity=r["capacity"] + 64, quad_capacity=rg.supply_points(**kw) + 64)
+        d = eng.add_diode(**kw)
         d.add_particles(prefill(r), step=0)
-        eng.run(1, 1)                     # first step (graph capture) untimed
-        eng.autotune()                    # the same tuning the served engine gets
-        eng.run(2, 1)                     # graph rebuilt under the chosen chunking, untimed
+        eng.run(1, 1)
+        if r["capacity"] < 4096:
+            eng.autotune()
         n0 = d.counters()["electron_steps"]
-        eng.run(3, 1)
+        eng.run(2, 1)
         ms, _ = eng.last_run_stats()
         e_steps += d.counters()["electron_steps"] - n0
         dev_s += ms / 1e3
-        names.append(r["capacity"])
+        caps.append(r["capacity"])
         eng.close()
-    return (e_steps / dev_s if dev_s > 0 else 0.0), names
+    return (e_steps / dev_s if dev_s > 0 else 0.0), caps, n
 
 
 # ---------------------------------------------------------------------------------
@@ -260,46 +308,85 @@ def reduce_ranks(world, maxes, sums):
 MH_JUMP_DRAM_BYTES = 35.05e6
 
 
+# Serving-iteration time of the 128-slot mix, used only to pace the stream's
+# arrivals in the admission schedule below.
+STEP_S_EST = 0.245
+# The timed window starts at least this many serving iterations (~100 s) into the stream.
+WINDOW_AFTER = 400
+
+
+def fifo_schedule(reqs, S, step_s=STEP_S_EST):
+    """Admission and completion iteration of each request of the stream when S
+    slots serve it first come first served (rd_serve's order): a request is
+    admitted at the first iteration when a slot is free and it has arrived,
+    runs its steps, and frees its slot for the iteration after its last one.
+    Returns [(admit, done)] with done = admit + steps."""
+    import heapq
+    free = [0] * S
+    out = []
+    for r in reqs:
+        a = max(heapq.heappop(free), int(math.ceil(r["arrival"] / step_s)))
+        heapq.heappush(free, a + r["steps"])
+        out.append((a, a + r["steps"]))
+    return out
+
+
+def steady_window(reqs, S, lead):
+    """A timed window of the saturated server that holds continuous batching:
+    the first iteration T0 >= WINDOW_AFTER at which a resident request runs its
+    last step (so it retires at the end of timed iteration 1 and the queue head
+    is admitted at iteration 2).  Returns T0, the residents at T0 - lead as
+    (request, remaining steps from T0 - lead on) in admission order, and the
+    queue at that point (arrived, not admitted) in FIFO order."""
+    sched = fifo_schedule(reqs, S)
+    T0 = min(done - 1 for a, done in sched if done - 1 >= WINDOW_AFTER)
+    ts = T0 - lead
+    res = sorted([(a, r, done - ts) for r, (a, done) in zip(reqs, sched) if a <= ts < done], key=lambda x: x[0])
+    queue = [r for r, (a, done) in zip(reqs, sched) if a > ts and r["arrival"] <= ts * STEP_S_EST]
+    return T0, [(r, rem) for a, r, rem in res], queue
+
+
 def run_ours(args, rank, world):
     import rumdeed_gb300 as rg
     rg.build()
     S = args.slots
     eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=S, particle_capacity=S * 32768 + 4096,
-                    chain_capacity=S * 32768 + 4096, quad_capacity=S * 4096 + 4096)
+                    chain_capacity=S * 32768 + 4096, quad_capacity=S * MAX_SUPPLY_POINTS + 4096)
     stream = RequestStream(SEED, rank=rank)
-    pending = stream.next()
-    submitted = {}
-    flush = L2Flush()
-    t0 = time.perf_counter()
-
-    def submit_arrived():
-        nonlocal pending
-        now = time.perf_counter() - t0
-        h2d = 0
-        while pending is not None and pending["arrival"] <= now:
-            pos = prefill(pending)
-            rid = eng.submit(pending["steps"], pos=pos, **diode_kwargs(pending))
-            submitted[rid] = pending
-            h2d += pos.nbytes
-            pending = stream.next()
-        return h2d
-
-    # warm-up: W iterations and until the slots are full (saturated server)
-    it = 0
+    reqs = []
     while True:
-        submit_arrived()
-        st = eng.serve(1)
-        it += 1
-        if it >= args.warmup and (st["running"] >= S or pending is None):
+        r = stream.next()
+        if r is None:
             break
-        if it > 100000:
-            break
-    # the autotuner picks the pair-sum chunking for the resident mix; one more
-    # untimed iteration rebuilds the step graph under it
+        reqs.append(r)
+    # The saturated server's state at the window: the S resident requests with the steps
+    # they still have to run, and the queue behind them (stream order).  The untimed
+    # iterations before the window (warm-up, and one after the autotuner) are counted in.
+    lead = args.warmup + 1
+    T0, residents, queue = steady_window(reqs, S, lead)
+    queue_pre, queue_later = queue[:2 * S], queue[2 * S:]
+    submitted = {}
+
+    def submit(r, steps):
+        pos = prefill(r)
+        rid = eng.submit(steps, pos=pos, **diode_kwargs(r))
+        submitted[rid] = r
+        return pos.nbytes
+
+    for r, rem in residents:
+        submit(r, rem)
+    for r in queue_pre:
+        submit(r, r["steps"])
+    flush = L2Flush()
+    for _ in range(args.warmup):
+        eng.serve(1)
+    # the autotuner picks the pair-sum chunking and the MH launch shape for the resident
+    # mix; one more untimed iteration rebuilds the step graph under them
     tune = eng.autotune()
-    submit_arrived()
     eng.serve(1)
-    # timed region
+    # timed region: continuous batching on the saturated server.  The stream's later
+    # requests keep arriving (submitted at their arrival rate, behind the queue);
+    # residents retire and the queue head is admitted inside the window.
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     if world > 1:
         import torch.distributed as dist
@@ -307,10 +394,17 @@ def run_ours(args, rank, world):
     clocks.start()
     dev_ms, wall_s, e_steps, h2d, d2h, admitted, retired = 0.0, 0.0, 0, 0, 0, 0, 0
     step_ms = []
+    later = iter(queue_later)
+    nxt = next(later, None)
+    t_base = nxt["arrival"] if nxt is not None else 0.0
+    t0 = time.perf_counter()
     for k in range(args.steps):
         flush()
         w0 = time.perf_counter()
-        submit_arrived()
+        now = t_base + (w0 - t0)
+        while nxt is not None and nxt["arrival"] <= now:
+            h2d += submit(nxt, nxt["steps"])
+            nxt = next(later, None)
         st = eng.serve(1)
         wall_s += time.perf_counter() - w0
         dev_ms += st["device_ms"]
@@ -324,36 +418,42 @@ def run_ours(args, rank, world):
     running = st["running"]
     queued = st["queued"]
     _, kps = eng.last_run_stats()
-    # queueing delay of the requests admitted so far
+    # queueing delay of the requests admitted in the window (submitted before it)
     qd = []
-    for rid in list(submitted)[:2000]:
+    for rid in list(submitted):
         s = eng.poll(rid)
         if s["admit_s"] >= 0:
             qd.append(s["admit_s"] - s["submit_s"])
+    resident_ids = [rid for rid in submitted if eng.poll(rid)["state"] == rg.REQ_RUNNING]
+    resident = [submitted[rid] for rid in resident_ids]
+    capped = sum(eng.poll(rid)["counters"]["chains_capped"] for rid in resident_ids)
+    chains = sum(eng.poll(rid)["counters"]["chains"] for rid in resident_ids)
     # per-phase profile of one more step (dominant kernel: MH jump launches)
     prof = eng.profile_step(10 ** 6)
-    resident = [submitted[r] for r in list(submitted) if eng.poll(r)["state"] == rg.REQ_RUNNING]
 
     # End to end through the public API (rd_submit / rd_serve, host buffers): every
-    # request is cancelled, then the same resident requests are submitted again at
+    # request is cancelled, then the window's state -- the residents with the steps
+    # they had left when it began, and the queue behind them -- is submitted again at
     # once from host memory, as new simulations.  The wall clock covers the
     # submissions, their admission (host -> device uploads through the engine's
     # pinned stage) and K serving iterations, each reading the per-diode counters
-    # back to the host.
+    # back to the host, with the same retirement and admission as the window.
     for rid in list(submitted):
         if eng.poll(rid)["state"] in (rg.REQ_QUEUED, rg.REQ_RUNNING):
             eng.cancel(rid)
-    burst = sorted(resident, key=lambda q: q["index"])
-    burst_pos = [prefill(r) for r in burst]
-    e2e_steps, e2e_h2d, e2e_d2h = 0, 0, 0
+    _, res_t0, queue_t0 = steady_window(reqs, S, 0)
+    burst = [(r, rem, prefill(r)) for r, rem in res_t0] + [(r, r["steps"], prefill(r)) for r in queue_t0[:2 * S]]
+    e2e_steps, e2e_h2d, e2e_d2h, e2e_adm, e2e_ret = 0, 0, 0, 0, 0
     w0 = time.perf_counter()
-    for r, pos in zip(burst, burst_pos):
-        eng.submit(r["steps"], pos=pos, **diode_kwargs(r))
+    for r, steps, pos in burst:
+        eng.submit(steps, pos=pos, **diode_kwargs(r))
     for k in range(args.steps):
         st = eng.serve(1)
         e2e_steps += st["electron_steps"]
         e2e_h2d += st["h2d_bytes"]
         e2e_d2h += st["d2h_bytes"]
+        e2e_adm += st["admitted"]
+        e2e_ret += st["retired"]
     e2e_wall = time.perf_counter() - w0
     eng.close()
 
@@ -377,8 +477,8 @@ def run_ours(args, rank, world):
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
         peak_src = "nominal: 152 SMs x 128 lanes x 2 x 2.07 GHz"
     traffic = MH_JUMP_DRAM_BYTES
-    plain_v, plain_caps = plain_fp64_sample(rg, resident, budget_s=args.plain_budget)
-    cpu_v, cpu_desc, cores, cpu_t = cpu_sample(SEED, rank=rank)
+    plain_v, plain_caps, plain_n = plain_fp64_all(rg, resident, budget_s=args.plain_budget)
+    cpu_v, cpu_desc, cores, cpu_t = cpu_sample(resident, rank=rank)
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / max(args.steps, 1),
@@ -388,31 +488,41 @@ def run_ours(args, rank, world):
         "config": {"workload": WORKLOAD,
                    "slots": S, "precision": "fp32c", "parallelism": "replicas" if world > 1 else "1 GPU",
                    "chunking": {"chunk_min": tune["chunk_min"], "chunk_count_max": tune["chunk_count_max"],
-                                "tuned_ms": tune["ms_chosen"], "default_ms": tune["ms_default"]},
+                                "mh_parts": tune["mh_parts"], "mh_form": tune["mh_form"],
+                                "candidates": tune["candidates"],
+                                "tuned_ms": tune["ms_chosen"], "default_ms": tune["ms_default"],
+                                "fixed": "i-tile 128 (particles, points or chains per work item); force: 64 threads "
+                                         "x 2 particles (one image partner), 128 x 1 otherwise"},
                    "l2": "256 MB buffer written between timed iterations",
+                   "window": "the saturated server %d serving iterations into the stream (first-come-first-"
+                             "served slot schedule of the stream): the %d resident requests with the steps they "
+                             "have left, the queue behind them, later requests arriving at the stream's rate; "
+                             "a resident retires at the end of the first timed iteration" % (T0, S),
                    "resident_diodes": running, "queued_requests": queued,
-                   "admitted_in_timed": admitted, "retired_in_timed": retired},
+                   "admitted_in_timed": admitted, "retired_in_timed": retired,
+                   "chains_in_last_step": chains, "chains_capped_in_last_step": capped},
         "latency": {"step_ms_p50": float(np.percentile(step_ms, 50)),
                     "step_ms_p99": float(np.percentile(step_ms, 99)),
                     "step_ms_max": float(max(step_ms)),
                     "queueing_delay_s_p50": float(np.percentile(qd, 50)) if qd else None,
                     "queueing_delay_s_p99": float(np.percentile(qd, 99)) if qd else None,
-                    "simulation_latency": "no simulation completes inside the window: "
-                                          "projected = steps x step time (>= 500 steps); measured "
-                                          "with step counts / 100 by --case serve-latency"},
+                    "simulation_latency": "a simulation lasts minutes (500-20000 steps at ~0.25 s): "
+                                          "measured with step counts / 100 by --case serve-latency"},
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": e2e_h2d / max(args.steps, 1),
                 "d2h_bytes_per_step": e2e_d2h / max(args.steps, 1),
-                "window": "the %d resident requests submitted again from host memory at once, "
-                          "admitted (uploads through the pinned stage) and served %d iterations "
-                          "with counter read-back; wall clock; no L2 flush" % (len(burst), args.steps),
+                "window": "the window's state (%d resident requests with the steps they had left, %d queued) "
+                          "submitted again from host memory at once, admitted (uploads through the pinned "
+                          "stage) and served %d iterations with counter read-back, %d admitted and %d retired "
+                          "after the first; wall clock; no L2 flush"
+                          % (len(res_t0), len(burst) - len(res_t0), args.steps, e2e_adm - len(res_t0), e2e_ret),
                 "steady_state": {"value": e_all / wall_s if wall_s > 0 else 0.0,
                                  "h2d_bytes_per_step": h2d / max(args.steps, 1),
                                  "d2h_bytes_per_step": d2h / max(args.steps, 1),
                                  "window": "the timed serving iterations, wall clock"}},
         "plain_fp64_one_diode_at_a_time": {"value": plain_v, "unit": METRIC,
-                                           "sample_capacities": plain_caps,
+                                           "covered": "%d of the %d resident requests" % (len(plain_caps), plain_n),
                                            "served_over_plain": value / plain_v if plain_v else None},
-        "gpu_launches": 2 * args.steps * (kps + 1) + 2 * (admitted + len(burst)),
+        "gpu_launches": 2 * args.steps * (kps + 1) + 3 * (admitted + len(burst)),
         "roofline": {"bound": "fp32", "kernel": "k_mh_jump_planar<1>",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
@@ -435,12 +545,24 @@ def run_ours(args, rank, world):
 
 
 def run_reference(args, rank, world):
+    """The CPU restatement of the reference path (the Fortran reference cannot be
+    built here) on the served window's resident set, capacity-stratified
+    (cpu_sample): W + K repetitions, the median reported."""
     if rank != 0:
         return
+    reqs = []
+    st = RequestStream(SEED)
+    while True:
+        r = st.next()
+        if r is None:
+            break
+        reqs.append(r)
+    _, residents, _ = steady_window(reqs, args.slots, 0)
+    resident = [r for r, rem in residents]
     vals, t_all = [], 0.0
     desc, cores = "", 0
     for k in range(args.warmup + args.steps):
-        v, desc, cores, t = cpu_sample(SEED, budget_pairs=args.ref_budget, rank=0)
+        v, desc, cores, t = cpu_sample(resident, rank=0)
         if k >= args.warmup:
             vals.append(v)
             t_all += t
@@ -449,7 +571,8 @@ def run_reference(args, rank, world):
             "warmup": args.warmup, "ms_per_step": 1e3 * t_all / max(args.steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic request stream (seeded PCG64; no dataset involved)",
-            "config": {"workload": WORKLOAD + " (bounded CPU sample)"},
+            "config": {"workload": WORKLOAD, "slots": args.slots,
+                       "window": "the resident set of the served window (see the served line)"},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port",
                              "sample": desc + " (the Fortran reference cannot be built here: no "
@@ -555,7 +678,7 @@ def case_serve_latency(args):
     rg.build()
     S = args.slots
     eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=S, particle_capacity=S * 32768 + 4096,
-                    chain_capacity=S * 32768 + 4096, quad_capacity=S * 4096 + 4096)
+                    chain_capacity=S * 32768 + 4096, quad_capacity=S * MAX_SUPPLY_POINTS + 4096)
     stream = RequestStream(SEED)
     pending = stream.next()
     ids = []
@@ -644,6 +767,106 @@ def case_verlet(args):
     print(json.dumps(out), flush=True)
 
 
+def case_uncapped(args):
+    """The chain cap.  The served engine runs at most `capacity` MH chains per
+    diode and step (a step cannot add more electrons than the diode holds);
+    the reference runs a chain for every one of the step's N_round candidates
+    and lets Add_Particle drop what does not fit (src/mod_field_emission_v2.F90:
+    283-330, src/mod_pair.F90:37-44).  The headline window's resident set runs
+    W + K steps both ways: capped, then with each diode's chain bound raised to
+    twice the N_round of its first capped step (chains_capped then counts what
+    is still cut).  Reports emitted and dropped electrons, chains and
+    electron-steps/s of both."""
+    import rumdeed_gb300 as rg
+    rg.build()
+    reqs = []
+    st = RequestStream(SEED)
+    while True:
+        r = st.next()
+        if r is None:
+            break
+        reqs.append(r)
+    _, residents, _ = steady_window(reqs, args.slots, 0)
+    res = [r for r, rem in residents]
+
+    def run(bounds):
+        chcap = sum(bounds) + 4096
+        eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=len(res), particle_capacity=len(res) * 32768 + 4096,
+                        chain_capacity=chcap, quad_capacity=len(res) * MAX_SUPPLY_POINTS + 4096)
+        ds = []
+        for r, b in zip(res, bounds):
+            d = eng.add_diode(**diode_kwargs(r, max_chains=b))
+            d.add_particles(prefill(r), step=0)
+            ds.append(d)
+        eng.run(1, 1)
+        first = [d.counters() for d in ds]
+        c0 = [d.counters() for d in ds]
+        eng.run(2, args.warmup + args.steps - 1)
+        ms, _ = eng.last_run_stats()
+        c1 = [d.counters() for d in ds]
+        eng.close()
+        steps = args.warmup + args.steps - 1
+        return {"electron_steps_per_s": sum(b["electron_steps"] - a["electron_steps"] for a, b in zip(c0, c1))
+                / (ms / 1e3),
+                "ms_per_step": ms / steps, "emitted": sum(c["emitted_total"] for c in c1),
+                "dropped": sum(c["dropped_total"] for c in c1),
+                "chains_last_step": sum(c["chains"] for c in c1),
+                "chains_capped_last_step": sum(c["chains_capped"] for c in c1)}, first
+    capped, first = run([r["capacity"] for r in res])
+    n_round = [c["chains"] + c["chains_capped"] for c in first]
+    uncapped, _ = run([max(r["capacity"], 2 * n) for r, n in zip(res, n_round)])
+    print(json.dumps({"case": "uncapped", "diodes": len(res), "steps": args.warmup + args.steps,
+                      "n_round_first_step": sum(n_round),
+                      "diodes_capped_first_step": sum(1 for c in first if c["chains_capped"] > 0),
+                      "capped": capped, "uncapped": uncapped}), flush=True)
+
+
+def case_compact(args):
+    """Absorption and compaction at full size: 64 planar diodes of 262144
+    electrons (16.8 M), of which three in four sit just below the anode moving
+    up and cross it in the next position pass, the others (every fourth, so
+    the survivors are spread over each diode) at mid-gap at rest.  One position
+    pass marks the crossers; the removal that follows compacts each diode's
+    survivors stably (rd_time_remove, CUDA events).  Algorithmic bytes: the
+    survey's 2 x the moved survivors' state, 152 B of FP64 and int state per
+    particle read and written once; the implementation moves each survivor
+    twice (to the compaction pool and back) and rewrites its FP32 packs."""
+    import rumdeed_gb300 as rg
+    rg.build()
+    D, n = 64, max(1024, args.verlet_n // 64)
+
+    def fill(eng, D, n):
+        rng = np.random.default_rng(11)
+        for k in range(D):
+            d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, capacity=n, image_charge=True, N_ic_max=0)
+            keep = (np.arange(n) % 4) == 0
+            z = np.where(keep, 500 * NM, 999.9 * NM)
+            vz = np.where(keep, 0.0, 1.0e8)
+            d.add_particles(np.column_stack([rng.uniform(-500 * NM, 500 * NM, n), rng.uniform(-500 * NM, 500 * NM, n), z]),
+                            vel=np.column_stack([np.zeros(n), np.zeros(n), vz]), step=0)
+
+    warm = rg.Engine(precision=rg.PREC_FP32C, max_diodes=2, particle_capacity=2 * 4096 + 64, chain_capacity=64,
+                     quad_capacity=64)
+    fill(warm, 2, 4096)
+    warm.time_remove()   # loads the kernels
+    warm.close()
+    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=D, particle_capacity=D * (n + 64), chain_capacity=4096,
+                    quad_capacity=4096)
+    fill(eng, D, n)
+    pos_ms, rem_ms, moved, removed = eng.time_remove()
+    left = sum(d.counters()["n"] for d in eng.diodes.values())
+    eng.close()
+    alg = 2.0 * moved * 152
+    impl = moved * (4 * 152 + 64)
+    peak = hbm_peak_gbs()
+    print(json.dumps({"case": "compact", "diodes": D, "electrons": D * n, "removed": removed, "moved": moved,
+                      "survivors": left, "position_ms": pos_ms, "remove_ms": rem_ms,
+                      "algorithmic_GBs": alg / (rem_ms / 1e3) / 1e9, "implementation_GBs": impl / (rem_ms / 1e3) / 1e9,
+                      "hbm_peak_GBs": peak, "frac_algorithmic": alg / (rem_ms / 1e3) / 1e9 / peak if peak else None,
+                      "bytes": {"algorithmic_per_moved": 2 * 152, "implementation_per_moved": 4 * 152 + 64}}),
+          flush=True)
+
+
 def case_burst(args):
     """The first S requests of the serving stream admitted at once (no arrival
     pacing), then W + K serving iterations: the serving workload with a fixed
@@ -658,7 +881,7 @@ def case_burst(args):
     except Exception:
         pass
     eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=S, particle_capacity=S * 32768 + 4096,
-                    chain_capacity=S * 32768 + 4096, quad_capacity=S * 4096 + 4096)
+                    chain_capacity=S * 32768 + 4096, quad_capacity=S * MAX_SUPPLY_POINTS + 4096)
     stream = RequestStream(SEED)
     reqs = [stream.next() for _ in range(S)]
     for r in reqs:
@@ -686,7 +909,7 @@ def case_mh_small(args):
     import rumdeed_gb300 as rg
     rg.build()
     eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=4, particle_capacity=4 * 8192,
-                    chain_capacity=4 * 8192, quad_capacity=4 * 4096)
+                    chain_capacity=4 * 8192, quad_capacity=4 * 65536)
     rng = np.random.default_rng(1)
     n, side = 6000, 1000 * NM
     for k in range(4):
@@ -710,7 +933,7 @@ def case_one_diode(args):
     side = 1000 * NM
     prec = rg.PREC_FP64 if args.precision == "fp64" else rg.PREC_FP32C
     eng = rg.Engine(precision=prec, max_diodes=1, particle_capacity=20064, chain_capacity=20064,
-                    quad_capacity=4096)
+                    quad_capacity=65536)
     d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, time_step=0.25e-15, image_charge=True, N_ic_max=0,
                       capacity=20000, emitter_pos=(-side / 2, -side / 2), emitter_dim=(side, side),
                       emission=True, seed=SEED, work=[[args.phi]], mh_jumps=args.jumps)
@@ -745,7 +968,7 @@ def case_plain(args):
             gpu = {}
             for prec, tag in ((rg.PREC_FP64, "fp64"), (rg.PREC_FP32C, "fp32c")):
                 eng = rg.Engine(precision=prec, max_diodes=1, particle_capacity=20064,
-                                chain_capacity=20064, quad_capacity=4096)
+                                chain_capacity=20064, quad_capacity=65536)
                 d = eng.add_diode(work=[[phi]], mh_jumps=jumps, **kw)
                 eng.run(1, args.warmup)
                 tune = eng.autotune()   # a lone diode needs short chunks to fill the GPU
@@ -759,7 +982,7 @@ def case_plain(args):
             o = orc.OracleDiode(cap=20000, V_s=2.0e3, d=1000 * NM, time_step=0.25e-15, image_charge=True,
                                 N_ic_max=0)
             o.set_planar_emitter(-side / 2, -side / 2, side, side, [[phi]])
-            o.set_emission(True, seed=SEED, mh_jumps=jumps, max_chains=20000, quad_panels=16, quad_order=4)
+            o.set_emission(True, seed=SEED, mh_jumps=jumps, max_chains=20000)   # the default supply rule
             cpu_steps, t0 = 0, time.perf_counter()
             while cpu_steps < 3 and time.perf_counter() - t0 < 20.0:
                 o.step(cpu_steps + 1)
@@ -819,11 +1042,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--slots", type=int, default=128)
-    ap.add_argument("--plain-budget", type=float, default=20.0)
-    ap.add_argument("--ref-budget", type=float, default=1.0e10)
+    ap.add_argument("--plain-budget", type=float, default=600.0,
+                    help="seconds for the plain FP64 one-diode-at-a-time leg over the resident set")
     ap.add_argument("--case", default="serve",
                     choices=["serve", "micro", "burst", "mh-small", "plain", "tips", "serve-latency", "verlet",
-                             "one-diode"],
+                             "one-diode", "uncapped", "compact"],
                     help="serve: the headline serving benchmark; the others are secondary workloads")
     ap.add_argument("--sizes", default="4096,65536,262144", help="micro: electron counts")
     ap.add_argument("--nics", default="0,7,8", help="micro: N_ic_max values (K = 8 mirror terms read "
@@ -853,7 +1076,7 @@ def main():
         if rank == 0:
             {"micro": case_micro, "burst": case_burst, "mh-small": case_mh_small, "plain": case_plain,
              "serve-latency": case_serve_latency, "verlet": case_verlet, "one-diode": case_one_diode,
-             "tips": case_tips}[args.case](args)
+             "tips": case_tips, "uncapped": case_uncapped, "compact": case_compact}[args.case](args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
