@@ -1251,7 +1251,8 @@ __device__ __forceinline__ void tip_point_tiles_f32(const float4* __restrict__ s
   float dx_[CPT], dy_[CPT], dz_[CPT], ex_[CPT], ey_[CPT], ez_[CPT];
 #pragma unroll
   for (int q = 0; q < CPT; ++q) dx_[q] = dy_[q] = dz_[q] = ex_[q] = ey_[q] = ez_[q] = 0.f;
-#pragma unroll 2
+  constexpr int kUnroll = RD_TIP_UNROLL;
+#pragma unroll kUnroll
   for (int k = 0; k < kmax; ++k) {
     const float4 h = sh[k], l = sl[k];
     const float qj = h.w;

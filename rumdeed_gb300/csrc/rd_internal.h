@@ -21,7 +21,12 @@
 
 #define RD_TILE 128           // particles per shared-memory j-tile
 #define RD_ITILE 128          // i-particles (or points) per work item
+#ifndef RD_TIP_CPT
 #define RD_TIP_CPT 2          // tip MH chains per thread (FP32 form; even)
+#endif
+#ifndef RD_TIP_UNROLL
+#define RD_TIP_UNROLL 2       // j-loop unroll of the FP32 tip MH tile
+#endif
 #define RD_MH_PARTS 2         // planar MH jump launches per jump, one stream each (default)
 #define RD_MH_PARTS_MAX 4     // at most this many (rd_autotune / rd_set_mh_launch choose)
 #define RD_SUP_SPLIT 16       // blocks per diode in the supply reduction
