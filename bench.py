@@ -537,6 +537,8 @@ def run_ours(args, rank, world):
         "phase_ms": {k: prof[k] for k in ("supply_ms", "mh_init_ms", "mh_jumps_ms", "emit_ms",
                                           "position_ms", "force_ms", "velocity_ms", "compact_ms",
                                           "total_ms")},
+        "supply_TFLOPs": (20.0 * prof["supply_pair_evals"] / (prof["supply_ms"] / 1e3) / 1e12
+                          if prof["supply_ms"] > 0 else None),
         "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cores, "kind": "port",
                          "sample": cpu_desc, "seconds": cpu_t},
         "clocks": clk,
@@ -937,15 +939,22 @@ def case_one_diode(args):
     d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, time_step=0.25e-15, image_charge=True, N_ic_max=0,
                       capacity=20000, emitter_pos=(-side / 2, -side / 2), emitter_dim=(side, side),
                       emission=True, seed=SEED, work=[[args.phi]], mh_jumps=args.jumps)
-    eng.run(1, args.warmup)
-    eng.run(args.warmup + 1, args.steps)
-    ms, kps = eng.last_run_stats()
+    if args.uncaptured:
+        # every step phase by phase from the host (rd_profile_step): plain stream launches, which a
+        # profiler lists one by one (the step graph of a lone diode holds a conditional node)
+        for k in range(args.warmup + args.steps):
+            p = eng.profile_step(k + 1)
+        ms, kps = p["total_ms"] * args.steps, 0
+    else:
+        eng.run(1, args.warmup)
+        eng.run(args.warmup + 1, args.steps)
+        ms, kps = eng.last_run_stats()
     c = d.counters()
     eng.close()
     print(json.dumps({"case": "one-diode", "precision": args.precision, "work_function_eV": args.phi,
                       "mh_jumps": args.jumps, "steps": args.steps, "ms_per_step": ms / args.steps,
-                      "steps_per_s": args.steps / (ms / 1e3), "kernels_per_step": kps, "in_flight": c["n"]}),
-          flush=True)
+                      "steps_per_s": args.steps / (ms / 1e3), "kernels_per_step": kps, "in_flight": c["n"],
+                      "uncaptured": bool(args.uncaptured)}), flush=True)
 
 
 def case_plain(args):
@@ -1059,6 +1068,8 @@ def main():
     ap.add_argument("--phi", type=float, default=4.7, help="one-diode: work function (eV)")
     ap.add_argument("--jumps", type=int, default=100, help="one-diode: MH jumps per step")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"], help="one-diode: engine precision")
+    ap.add_argument("--uncaptured", action="store_true",
+                    help="one-diode: run the steps phase by phase (rd_profile_step) instead of the step graph")
     ap.add_argument("--validate-every", type=int, default=0,
                     help="serve-latency: run rd_validate every this many iterations (0: never)")
     ap.add_argument("--fp64-budget", type=float, default=2.0e11,

@@ -69,6 +69,7 @@ class Diode(C.Structure):
         ("atom_time_interval", C.c_int), ("ramo_current_ion", C.c_double),
         ("avg_part_vel", C.c_double * 3), ("avg_ion_vel", C.c_double * 3), ("avg_mob", C.c_double),
         ("n_part_vel", C.c_int), ("n_elec_vel", C.c_int), ("n_ion_vel", C.c_int),
+        ("F_avg_x", C.c_double), ("F_avg_y", C.c_double),
     ]
 
 

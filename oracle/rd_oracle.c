@@ -971,7 +971,8 @@ double orc_supply_integral_planar(orc_diode* s) {
   double A = s->em_dim[0] * s->em_dim[1];
   int npt = P * Q;
   double* val = (double*)calloc((size_t)npt * npt, sizeof(double));
-  double* fz = (double*)calloc((size_t)npt * npt, sizeof(double));
+  double* fz = (double*)calloc((size_t)npt * 3 * npt, sizeof(double));   /* z, then x, y */
+  double* fxy = fz + (size_t)npt * npt;
 #pragma omp parallel for schedule(dynamic, 8)
   for (int k = 0; k < npt * npt; ++k) {
     int iy = k / npt, ix = k % npt;
@@ -990,17 +991,23 @@ double orc_supply_integral_planar(orc_diode* s) {
     double f[3];
     orc_field_at(s, p, f, 1);
     fz[k] = f[2];
+    fxy[2 * (size_t)k] = f[0];
+    fxy[2 * (size_t)k + 1] = f[1];
     if (f[2] < 0.0) {
       double phi = work_at(s, p[0], p[1], NULL);
       val[k] = (wx * wy) * (Ak * orc_elec_supply_v2(f[2], phi, s->image_charge, s->time_step));
     }
   }
-  nsum tot = {0, 0}, ftot = {0, 0};
+  nsum tot = {0, 0}, ftot = {0, 0}, fxt = {0, 0}, fyt = {0, 0};
   for (int k = 0; k < npt * npt; ++k) {
     if (val[k] != 0.0) nadd(&tot, val[k]);
     nadd(&ftot, fz[k]);
+    nadd(&fxt, fxy[2 * (size_t)k]);
+    nadd(&fyt, fxy[2 * (size_t)k + 1]);
   }
   s->F_avg_z = nval(&ftot) / (double)(npt * npt);   /* F_avg, fe_v2:644-651 */
+  s->F_avg_x = nval(&fxt) / (double)(npt * npt);
+  s->F_avg_y = nval(&fyt) / (double)(npt * npt);
   free(val); free(fz);
   return nval(&tot);
 }
@@ -1525,6 +1532,7 @@ int orc_do_emission(orc_diode* s, int step) {
   if (!s->emission) { s->emitted_step = 0; return 0; }
   if (step <= s->emit_delay) {   /* emitters_delay(i) < step, fe_v2:181 */
     s->emitted_step = 0; s->N_sup = 0.0; s->last_chains = 0; s->F_avg_z = 0.0; s->df_avg = 0.0;
+    s->F_avg_x = 0.0; s->F_avg_y = 0.0;
     return 0;
   }
   return s->geometry == ORC_TIP ? orc_do_emission_tip(s, step) : orc_do_emission_planar(s, step);

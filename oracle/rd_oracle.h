@@ -109,6 +109,7 @@ typedef struct {
    * particle counts it divides by (before removal); avg_elec_vel is above */
   double avg_part_vel[3], avg_ion_vel[3], avg_mob;
   int n_part_vel, n_elec_vel, n_ion_vel;
+  double F_avg_x, F_avg_y;  /* field.dt: mean lateral field of the supply points (0 with image charges) */
 } orc_diode;
 
 /* Create / destroy.  Geometry parameters follow Init_Field_Emission_v2

@@ -359,6 +359,7 @@ static bool valid_chunking(int clen_min, int nch_max) {
 
 struct Sig {
   bool planar = false, tip = false, emit_planar = false, emit_tip = false, nic = false;
+  bool emit_lat = false;      // some emitting planar diode has no image charges (PM_SUPPLY_LAT)
   bool emit_serial = false;   // some planar diode uses the serial MH sampler
   bool tts = false;           // some diode uses the two-time-step integrator
   int jumps = 0;
@@ -374,6 +375,7 @@ static Sig signature(const rd_engine* e) {
     if (p.tts > 0) s.tts = true;
     if (p.emission) {
       if (p.geometry == RD_G_TIP) s.emit_tip = true; else s.emit_planar = true;
+      if (p.geometry != RD_G_TIP && !p.image_charge) s.emit_lat = true;
       if (p.geometry != RD_G_TIP && p.mh_serial) s.emit_serial = true;
       if (p.geometry != RD_G_TIP && !p.mh_serial) s.mh_planar++;
       s.jumps = std::max(s.jumps, p.mh_jumps);
@@ -459,18 +461,23 @@ static int launch_mh_tiled(rd_engine* e, const Sig& s, cudaStream_t main) {
   return launch_mh_jumps(e, s, main);
 }
 
-// Inside a stream capture: the tiled MH chains as the body of a conditional
-// (IF) graph node, which a one-thread kernel switches on only when the MH plan
-// has work items.  A step whose emitting diodes all sample the vacuum field
-// (k_mh_vacuum) -- or that has no chain at all -- then skips the start and
-// jump launches entirely.  The body is captured on stream e->sbody.
+// Inside a stream capture, for a lone emitting planar diode: the tiled MH
+// chains as the body of a conditional (IF) graph node, which a one-thread
+// kernel switches on only when the MH plan has work items.  A step whose diode
+// samples the vacuum field (k_mh_vacuum) -- or has no chain at all -- then
+// skips the start and jump launches entirely.  The body is captured on stream
+// e->sbody.
 static int launch_mh_tiled_if(rd_engine* e, const Sig& s) {
   cudaStreamCaptureStatus cst;
   cudaGraph_t cap = nullptr;
   const cudaGraphNode_t* deps = nullptr;
   size_t ndeps = 0;
   CK(cudaStreamGetCaptureInfo(e->st, &cst, nullptr, &cap, nullptr, nullptr, nullptr));
-  if (cst != cudaStreamCaptureStatusActive) return launch_mh_tiled(e, s, e->st);
+  // Only a lone emitting planar diode (the one-diode deck) gains: with two or more, every
+  // one would have to be empty.  Elsewhere the plain launches are kept, which also keeps
+  // the step graph's kernels visible one by one to a profiler (ncu does not profile the
+  // kernel nodes of a graph that holds a conditional node).
+  if (cst != cudaStreamCaptureStatusActive || s.mh_planar > 1 || s.emit_tip) return launch_mh_tiled(e, s, e->st);
   cudaGraphConditionalHandle h;
   CK(cudaGraphConditionalHandleCreate(&h, cap, 0, cudaGraphCondAssignDefault));
   CK(rd_launch_mh_cond(e->st, h, e->ph[PM_MH]));
@@ -504,6 +511,13 @@ static int launch_emission(rd_engine* e) {
     CK(rd_launch_z0_points(prec, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_PLANAR],
                            e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qpp, e->qF, e->partial, e->tickets,
                            e->kscale, e->item_queue + 6));
+    e->kernels_in_step++;
+  }
+  if (s.emit_lat) {   // planar diodes without image charges: all three components at the points
+    CK(plan(e, PM_SUPPLY_LAT));
+    PointSet lp{e->qx, e->qy, e->qz, e->qfx, e->qfy, e->qF, e->d_qoff};
+    CK(rd_launch_field_points(prec, RD_G_PLANAR, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_LAT],
+                              e->ph[PM_SUPPLY_LAT], lp, e->partial, e->tickets, e->kscale));
     e->kernels_in_step++;
   }
   if (s.emit_tip) {
@@ -601,8 +615,8 @@ static int launch_step_body(rd_engine* e) {
 static std::string sig_string(rd_engine* e) {
   Sig s = signature(e);
   char b[128];
-  snprintf(b, sizeof b, "%d%d%d%d%d%d%d%d:%d:%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
-           s.emit_serial, s.tts, s.mh_planar > 1 ? 2 : s.mh_planar, s.jumps, e->clen_min, e->nch_max,
+  snprintf(b, sizeof b, "%d%d%d%d%d%d%d%d%d:%d:%d:%d:%d:%d", s.planar, s.tip, s.emit_planar, s.emit_tip, s.nic,
+           s.emit_serial, s.tts, s.mh_planar > 1 ? 2 : s.mh_planar, s.emit_lat, s.jumps, e->clen_min, e->nch_max,
            mh_parts_for(e, s), mh_form_for(e, s));
   return b;
 }
@@ -749,7 +763,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
       e->dalloc(&e->d_npts, S) || e->dalloc(&e->d_zero_off, S) ||
       e->dalloc(&e->partial, (size_t)e->max_items * 3 * RD_ITILE) ||
       e->dalloc(&e->tickets, e->max_items) || e->dalloc(&e->kept, e->max_items) ||
-      e->dalloc(&e->sup_part, (size_t)S * RD_SUP_SPLIT * 2) ||
+      e->dalloc(&e->sup_part, (size_t)S * RD_SUP_SPLIT * 4) ||
       e->dalloc(&e->item_queue, 8 + 2 * RD_MH_PARTS_MAX) ||
       (cfg->event_capacity > 0 && (e->dalloc(&e->evlog.buf, (size_t)cfg->event_capacity) ||
                                    e->dalloc(&e->evlog.count, 1))) ||
@@ -1654,7 +1668,8 @@ static void fill_counters(const DiodeDyn& y, rd_counters* o) {
   o->electron_steps = y.electron_steps; o->steps_done = y.steps_done;
   o->ramo_current = y.ramo_current; o->N_sup = y.N_sup; o->MH_std = y.MH_std;
   o->a_rate = y.a_rate; o->residual = y.residual;
-  o->F_avg[0] = 0.0; o->F_avg[1] = 0.0; o->F_avg[2] = y.F_avg_z;   // x, y cancel at the cathode
+  // with image charges the lateral components cancel at the cathode exactly (0)
+  o->F_avg[0] = y.F_avg_x; o->F_avg[1] = y.F_avg_y; o->F_avg[2] = y.F_avg_z;
   o->df_avg = y.df_avg;
   o->ramo_current_ion = y.ramo_ion;
   for (int c = 0; c < 3; ++c) {
@@ -1843,6 +1858,12 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
       CK(plan(e, PM_SUPPLY_PLANAR));
       CK(rd_launch_z0_points(prec, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_PLANAR],
                              e->ph[PM_SUPPLY_PLANAR], e->qx, e->qy, e->qpp, e->qF, e->partial, e->tickets, e->kscale, e->item_queue + 6));
+    }
+    if (s.emit_lat) {
+      CK(plan(e, PM_SUPPLY_LAT));
+      PointSet lp{e->qx, e->qy, e->qz, e->qfx, e->qfy, e->qF, e->d_qoff};
+      CK(rd_launch_field_points(prec, RD_G_PLANAR, e->grid, e->st, e->dP, e->pool, e->plan[PM_SUPPLY_LAT],
+                                e->ph[PM_SUPPLY_LAT], lp, e->partial, e->tickets, e->kscale));
     }
     if (s.emit_tip) {
       CK(plan(e, PM_SUPPLY_TIP));

@@ -463,9 +463,11 @@ __device__ __forceinline__ double z0_finish(const DiodeParams& p, double s, doub
 }
 
 // F_z at the supply quadrature points (qpp holds their FP32-frame split).
-// FP32: 64 threads, two points each; FP64: 128 threads, one point each.
+// FP32: 32 threads, four points each (the MH jump's form: one shared load feeds
+// four points, and a point's sum is the same lane arithmetic in the same j
+// order in any form); FP64: 128 threads, one point each.
 template <int PREC>
-__global__ void __launch_bounds__(RD_ITILE)
+__global__ void __launch_bounds__(PREC == 1 ? 32 : RD_ITILE, PREC == 1 ? 32 : 1)
 k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __restrict__ plan,
             const PlanHeader* __restrict__ ph, const double* __restrict__ qx,
             const double* __restrict__ qy, const float4* __restrict__ qpp, double* __restrict__ qF,
@@ -473,7 +475,7 @@ k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __res
   __shared__ int s_item;
   __shared__ float4 sh[RD_TILE], sl[RD_TILE];
   __shared__ rd_d4 sj[RD_TILE];
-  constexpr int CPT = PREC == 1 ? 2 : 1;
+  constexpr int CPT = PREC == 1 ? 4 : 1;
   const int nt = blockDim.x;
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
@@ -481,11 +483,15 @@ k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __res
     const DiodeParams& p = P[it.d];
     const int m = plan[it.d].n_i, qo = p.q_off;
     double s[CPT];
-    if (PREC == 1) {
-      const int i0 = it.i0 + tid, i1 = it.i0 + nt + tid;
+    if constexpr (PREC == 1) {
       const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-      const float4 pts[2] = {i0 < m ? qpp[qo + i0] : z4, i1 < m ? qpp[qo + i1] : z4};
-      z0_item_sumN<2>(p, pool, it, pts, s);
+      float4 pts[CPT];
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) {
+        const int i = it.i0 + tid + q * nt;
+        pts[q] = i < m ? qpp[qo + i] : z4;
+      }
+      z0_item_sumN<CPT>(p, pool, it, pts, s);
     } else {
       const int i = it.i0 + tid;
       const bool valid = i < m;
@@ -550,10 +556,14 @@ k_supply_reduce(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
   const int npt = (p.geometry == RD_G_TIP) ? 10000 : p.quad_n * p.quad_n;
   const int per = (npt + RD_SUP_SPLIT - 1) / RD_SUP_SPLIT;
   const int k0 = b * per, k1 = min(npt, k0 + per);
-  double acc = 0.0, fsum = 0.0;
+  // planar diodes without image charges carry all three field components (PM_SUPPLY_LAT):
+  // their lateral mean goes to field.dt too
+  const bool lat = p.geometry == RD_G_PLANAR && !p.image_charge;
+  double acc = 0.0, fsum = 0.0, fxs = 0.0, fys = 0.0;
   for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
     double F = qF[p.q_off + k];
     fsum += F;
+    if (lat) { fxs += qfx[p.q_off + k]; fys += qfy[p.q_off + k]; }
     if (p.geometry == RD_G_TIP) {   // Field_normal :105-112
       double nx, ny, nz;
       tip_normal(p, qx[p.q_off + k], qy[p.q_off + k], &nx, &ny, &nz);
@@ -571,9 +581,11 @@ k_supply_reduce(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
   }
   const double N_sup = block_sum(acc, red);
   const double F_sum = block_sum(fsum, red);
+  const double Fx_sum = lat ? block_sum(fxs, red) : 0.0;   // block-uniform condition
+  const double Fy_sum = lat ? block_sum(fys, red) : 0.0;
   if (threadIdx.x == 0) {
-    sup_part[((size_t)d * RD_SUP_SPLIT + b) * 2] = N_sup;
-    sup_part[((size_t)d * RD_SUP_SPLIT + b) * 2 + 1] = F_sum;
+    double* o = sup_part + ((size_t)d * RD_SUP_SPLIT + b) * 4;
+    o[0] = N_sup; o[1] = F_sum; o[2] = Fx_sum; o[3] = Fy_sum;
   }
 }
 
@@ -587,17 +599,19 @@ __global__ void k_supply_finish(const DiodeParams* __restrict__ P, DiodeDyn* __r
   if (!supply_live(p, y, step_ptr)) {   // the emitter is not on yet (:181)
     y.N_sup = 0.0; y.chains = y.chains_capped = y.chains_failed = 0;
     y.mh_acc = y.mh_rej = y.mh_done = 0;
-    y.F_avg_z = 0.0; y.df_avg = 0.0;
+    y.F_avg_z = 0.0; y.F_avg_x = 0.0; y.F_avg_y = 0.0; y.df_avg = 0.0;
     return;
   }
   const int npt = (p.geometry == RD_G_TIP) ? 10000 : p.quad_n * p.quad_n;
-  double N_sup = 0.0, F_sum = 0.0;
+  double N_sup = 0.0, F_sum = 0.0, Fx_sum = 0.0, Fy_sum = 0.0;
   for (int b = 0; b < RD_SUP_SPLIT; ++b) {
-    N_sup += sup_part[((size_t)d * RD_SUP_SPLIT + b) * 2];
-    F_sum += sup_part[((size_t)d * RD_SUP_SPLIT + b) * 2 + 1];
+    const double* o = sup_part + ((size_t)d * RD_SUP_SPLIT + b) * 4;
+    N_sup += o[0]; F_sum += o[1]; Fx_sum += o[2]; Fy_sum += o[3];
   }
   y.N_sup = N_sup;
   y.F_avg_z = p.geometry == RD_G_TIP ? 0.0 : F_sum / npt;   // F_avg, :644-651 (planar)
+  y.F_avg_x = p.geometry == RD_G_TIP ? 0.0 : Fx_sum / npt;
+  y.F_avg_y = p.geometry == RD_G_TIP ? 0.0 : Fy_sum / npt;
   long nr;
   if (p.geometry == RD_G_TIP) {
     nr = nint_d(N_sup);
@@ -1121,14 +1135,17 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
 // (rd_mh_vacuum), in one launch: one cluster of RD_VAC_CTAS CTAs per diode
 // slot runs round 0 of the chains' start, the rounds k_mh_init would run, and
 // every jump.  With no charges the field at every point is z0_finish(p, 0), the
-// value the tiled kernels compute from their empty pair sums, and proposals,
-// starts and accept tests are the same device functions, so the chains evolve
-// bit for bit as in k_mh_jump_planar + k_mh_init.  After each jump the CTAs
-// reduce their acceptance counts, exchange them through distributed shared
-// memory across a cluster barrier and each apply the same MH_std update
-// (MH_std_update :603-612); jumps alternate between two count buffers, so a
-// CTA never overwrites counts another may still read.  Clusters of slots that
-// are not such diodes leave at once (the test is uniform over a cluster).
+// value the tiled kernels compute from their empty pair sums.  Each thread
+// keeps its RD_VAC_CPT chains in registers for the whole sampling and writes
+// them back at the end; the proposal, start and accept arithmetic is that of
+// mh_propose_*, mh_start_* and mh_accept_one(_f) step for step (the tiled path
+// keeps the same state in memory), so the chains evolve bit for bit as in
+// k_mh_jump_planar + k_mh_init.  After each jump the CTAs reduce their
+// acceptance counts, exchange them through distributed shared memory across a
+// cluster barrier and each apply the same MH_std update (MH_std_update
+// :603-612); jumps alternate between two count buffers, so a CTA never
+// overwrites counts another may still read.  Clusters of slots that are not
+// such diodes leave at once (the test is uniform over a cluster).
 template <int PREC>
 __global__ void __cluster_dims__(RD_VAC_CTAS, 1, 1) __launch_bounds__(RD_VAC_THREADS)
 k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainState cs,
@@ -1139,36 +1156,70 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
   __shared__ int s_cnt[2][2];
   __shared__ int s_red[2][RD_VAC_THREADS / 32];
   __shared__ double s_mhs;
+  // the diode's parameters and supply-target table in shared memory for the whole
+  // sampling: global data would be fetched again after every cluster barrier
+  __shared__ DiodeParams sp;
+  __shared__ double swt[3 * RD_VAC_WTAB];
   const int d = blockIdx.x / RD_VAC_CTAS;
   if (d >= nslots) return;
-  const DiodeParams& p = P[d];
   DiodeDyn& y = Dy[d];
-  if (!p.active || !rd_mh_vacuum(p, y) || y.chains <= 0) return;
+  if (!P[d].active || !rd_mh_vacuum(P[d], y) || y.chains <= 0) return;
   const int rank = (int)cl.block_rank(), tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  {
+    const int* src = reinterpret_cast<const int*>(P + d);
+    int* dst = reinterpret_cast<int*>(&sp);
+    for (int k = tid; k < (int)(sizeof(DiodeParams) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+  }
+  __syncthreads();
+  const int cells = sp.work_model == 1 ? sp.work_nx * sp.work_ny : (sp.work_model == 4 ? sp.work_nx : 0);
+  const bool wsh = cells <= RD_VAC_WTAB;   // the table's values are the same wherever they are read
+  if (wsh)
+    for (int k = tid; k < 3 * cells; k += blockDim.x) swt[k] = wtab[3 * sp.work_off + k];
+  __syncthreads();
+  if (wsh && tid == 0) sp.work_off = 0;   // entries now at swt[3 * cell]
+  __syncthreads();
+  if (wsh) wtab = swt;
+  const DiodeParams& p = sp;
   const int M = y.chains, base = ch_off[d];
   const int G = RD_VAC_CTAS * RD_VAC_THREADS, g0 = rank * RD_VAC_THREADS + tid;
   const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
   const double F = z0_finish<PREC>(p, 0.0, kscale);
   const int ndim_first = (p.mh_jumps + 2) / 4;
   double mhs = y.MH_std, arate = y.a_rate;
+  // chain state in registers: FP32 chains (nm offsets) or FP64 chains (m)
+  int ok[RD_VAC_CPT];
+  float fx[RD_VAC_CPT], fy[RD_VAC_CPT], fsup[RD_VAC_CPT], fgx[RD_VAC_CPT], fgy[RD_VAC_CPT];
+  double dx[RD_VAC_CPT], dy[RD_VAC_CPT], dsup[RD_VAC_CPT], dgx[RD_VAC_CPT], dgy[RD_VAC_CPT], Fc[RD_VAC_CPT];
   // the start: round 0; a chain that fails it fails every round (the field does not change)
   int failed = 0;
-  for (int c = g0; c < M; c += G) {
-    const int k = base + c;
-    if constexpr (PREC == 1) {
-      float x, yv;
-      mh_propose_f32(p, cs, k, c, 1, true, false, step, 0.0f, 0.0f, p.em_hx, p.em_hy, &x, &yv);
-      mh_start_f32(p, cs, wtab, k, c, step, F, x, yv);
-    } else {
-      double x, yv;
-      mh_propose_f64(p, cs, k, c, 1, true, false, step, 0.0, 0.0, &x, &yv);
-      mh_start_f64(p, cs, wtab, k, c, step, F, x, yv);
+#pragma unroll
+  for (int q = 0; q < RD_VAC_CPT; ++q) {
+    const int c = g0 + q * G;
+    ok[q] = 0;
+    fx[q] = fy[q] = fsup[q] = fgx[q] = fgy[q] = 0.0f;
+    dx[q] = dy[q] = dsup[q] = dgx[q] = dgy[q] = 0.0; Fc[q] = F;
+    if (c >= M) continue;
+    if constexpr (PREC == 1) {   // mh_propose_f32 (init) + mh_start_f32
+      float u1, u2;
+      rng2f(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+      const float x = fminf(fmaf(u1, p.em_wx, -p.em_hx), p.em_hx);
+      const float yv = fminf(fmaf(u2, p.em_wy, -p.em_hy), p.em_hy);
+      if (F < 0.0 && p.init_rounds > 0) {
+        ok[q] = 1; fx[q] = x; fy[q] = yv;
+        fsup[q] = supply_log_xy_f(p, wtab, x, yv, (float)F);
+        gauss2f(p.seed, (uint32_t)c, 1u, step, &fgx[q], &fgy[q]);
+      }
+    } else {                     // mh_propose_f64 (init) + mh_start_f64
+      double u1, u2;
+      rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+      const double x = u1 * p.em_Lx + p.em_x0, yv = u2 * p.em_Ly + p.em_y0;
+      if (F < 0.0 && p.init_rounds > 0) {
+        ok[q] = 1; dx[q] = x; dy[q] = yv;
+        dsup[q] = supply_log_xy(p, wtab, x, yv, F);
+        gauss2(p.seed, (uint32_t)c, 1u, step, &dgx[q], &dgy[q]);
+      }
     }
-    if (!cs.ok[k]) {   // k_mh_init's record of a chain with no favourable start
-      cs.F[k] = 1.0; cs.sup[k] = -1.79769313486231570e308;
-      cs.x[k] = p.em_x0; cs.y[k] = p.em_y0;
-      failed++;
-    }
+    if (!ok[q]) failed++;
   }
   if (failed) atomicAdd(&y.chains_failed, failed);
   for (int it = 1; it <= p.mh_jumps; ++it) {
@@ -1177,23 +1228,63 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
       const float mf = (float)mhs;
       const float sx = (it > ndim_first) ? p.em_wx * mf : p.em_wx * 0.10f;
       const float sy = (it > ndim_first) ? p.em_wy * mf : p.em_wy * 0.10f;
-      for (int c = g0; c < M; c += G) {
-        const int k = base + c;
-        if (!cs.ok[k]) continue;
-        float x, yv;
-        mh_propose_f32(p, cs, k, c, 1, false, false, step, sx, sy, p.em_hx, p.em_hy, &x, &yv);
-        const int acc = mh_accept_one_f(p, cs, wtab, c, k, it, step, F, x, yv);
+      const float hx = p.em_hx, hy = p.em_hy;
+#pragma unroll
+      for (int q = 0; q < RD_VAC_CPT; ++q) {
+        if (!ok[q]) continue;
+        const int c = g0 + q * G;
+        // mh_propose_f32
+        float x = fmaf(fgx[q], sx, fx[q]);
+        float yv = fmaf(fgy[q], sy, fy[q]);
+        if (x > hx) x = hx - (x - hx); else if (x < -hx) x = -hx - (x + hx);
+        if (yv > hy) yv = hy - (yv - hy); else if (yv < -hy) yv = -hy - (yv + hy);
+        // mh_accept_one_f
+        int acc = 0;
+        if (F < 0.0) {
+          const float sn = supply_log_xy_f(p, wtab, x, yv, (float)F);
+          const float df = sn - fsup[q];
+          bool take;
+          if (isfinite(df) && df >= RD_MH_GUARD) {
+            take = true;
+          } else {
+            uint32_t o[4];
+            philox4x32((uint32_t)c, (uint32_t)it, step, RNG_ACCEPT, (uint32_t)p.seed, (uint32_t)(p.seed >> 32), o);
+            const float lu = logf((float)o[0] * 2.3283064365386963e-10f);
+            if (o[0] >= 65536u && isfinite(df) && lu <= df - RD_MH_GUARD) take = true;
+            else if (o[0] >= 65536u && isfinite(df) && lu > df + RD_MH_GUARD) take = false;
+            else take = mh_take_fp64(p, wtab, x, yv, F, fx[q], fy[q], Fc[q], o[0], o[1]);
+          }
+          if (take) { fx[q] = x; fy[q] = yv; fsup[q] = sn; Fc[q] = F; acc = 1; }
+        }
+        if (it < p.mh_jumps) gauss2f(p.seed, (uint32_t)c, (uint32_t)(it + 1), step, &fgx[q], &fgy[q]);
         a += acc; r += 1 - acc;
       }
     } else {
       const double sx = (it > ndim_first) ? p.em_Lx * mhs : p.em_Lx * 0.10;
       const double sy = (it > ndim_first) ? p.em_Ly * mhs : p.em_Ly * 0.10;
-      for (int c = g0; c < M; c += G) {
-        const int k = base + c;
-        if (!cs.ok[k]) continue;
-        double x, yv;
-        mh_propose_f64(p, cs, k, c, 1, false, false, step, sx, sy, &x, &yv);
-        const int acc = mh_accept_one(p, cs, wtab, c, k, it, step, F, x, yv);
+      const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+#pragma unroll
+      for (int q = 0; q < RD_VAC_CPT; ++q) {
+        if (!ok[q]) continue;
+        const int c = g0 + q * G;
+        // mh_propose_f64
+        double x = dgx[q] * sx + dx[q], yv = dgy[q] * sy + dy[q];
+        if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
+        if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
+        // mh_accept_one
+        int acc = 0;
+        if (F < 0.0) {
+          const double sn = supply_log_xy(p, wtab, x, yv, F);
+          const double sc = dsup[q];
+          bool take = sn >= sc;
+          if (!take) {
+            double u1, u2;
+            rng2(p.seed, (uint32_t)c, (uint32_t)it, step, RNG_ACCEPT, &u1, &u2);
+            take = log(u1) <= sn - sc;
+          }
+          if (take) { dx[q] = x; dy[q] = yv; dsup[q] = sn; Fc[q] = F; acc = 1; }
+        }
+        if (it < p.mh_jumps) gauss2(p.seed, (uint32_t)c, (uint32_t)(it + 1), step, &dgx[q], &dgy[q]);
         a += acc; r += 1 - acc;
       }
     }
@@ -1204,23 +1295,53 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
     if (lane == 0) { s_red[0][w] = a; s_red[1][w] = r; }
     __syncthreads();
     const int par = it & 1;
-    if (tid == 0) {
-      int A = 0, R = 0;
-      for (int k = 0; k < RD_VAC_THREADS / 32; ++k) { A += s_red[0][k]; R += s_red[1][k]; }
-      s_cnt[par][0] = A; s_cnt[par][1] = R;
+    if (w == 0) {   // this CTA's counts
+      int A = lane < RD_VAC_THREADS / 32 ? s_red[0][lane] : 0, R = lane < RD_VAC_THREADS / 32 ? s_red[1][lane] : 0;
+      for (int o = 16; o > 0; o >>= 1) {
+        A += __shfl_xor_sync(0xffffffffu, A, o);
+        R += __shfl_xor_sync(0xffffffffu, R, o);
+      }
+      if (lane == 0) { s_cnt[par][0] = A; s_cnt[par][1] = R; }
     }
     cl.sync();   // every CTA's counts of this jump are in place
-    if (tid == 0) {
+    if (w == 0) {   // the cluster's counts: lane q reads CTA q's
       int A = 0, R = 0;
-      for (int q = 0; q < RD_VAC_CTAS; ++q) {
-        const int* rc = cl.map_shared_rank(&s_cnt[par][0], q);
-        A += rc[0]; R += rc[1];
+      if (lane < RD_VAC_CTAS) {
+        const int* rc = cl.map_shared_rank(&s_cnt[par][0], lane);
+        A = rc[0]; R = rc[1];
       }
-      mh_std_step(p, &mhs, &arate, it, ndim_first, A, R);
-      s_mhs = mhs;
+      for (int o = 16; o > 0; o >>= 1) {
+        A += __shfl_xor_sync(0xffffffffu, A, o);
+        R += __shfl_xor_sync(0xffffffffu, R, o);
+      }
+      if (lane == 0) {
+        mh_std_step(p, &mhs, &arate, it, ndim_first, A, R);
+        s_mhs = mhs;
+      }
     }
     __syncthreads();
     mhs = s_mhs;
+  }
+  // the chains back to memory, as the tiled path leaves them
+#pragma unroll
+  for (int q = 0; q < RD_VAC_CPT; ++q) {
+    const int c = g0 + q * G;
+    if (c >= M) continue;
+    const int k = base + c;
+    cs.ok[k] = ok[q];
+    if (!ok[q]) {   // k_mh_init's record of a chain with no favourable start
+      cs.F[k] = 1.0; cs.sup[k] = -1.79769313486231570e308;
+      cs.x[k] = p.em_x0; cs.y[k] = p.em_y0;
+      continue;
+    }
+    cs.F[k] = Fc[q];
+    if constexpr (PREC == 1) {
+      cs.fx[k] = fx[q]; cs.fy[k] = fy[q]; cs.fsup[k] = fsup[q]; cs.fgx[k] = fgx[q]; cs.fgy[k] = fgy[q];
+      cs.x[k] = p.org_x + (double)fx[q] * 1.0e-9;
+      cs.y[k] = p.org_y + (double)fy[q] * 1.0e-9;
+    } else {
+      cs.x[k] = dx[q]; cs.y[k] = dy[q]; cs.sup[k] = dsup[q]; cs.gx[k] = dgx[q]; cs.gy[k] = dgy[q];
+    }
   }
   if (rank == 0 && tid == 0) { y.MH_std = mhs; y.a_rate = arate; }
   cl.sync();   // no CTA leaves while another may still read its counts
@@ -1890,7 +2011,7 @@ cudaError_t rd_launch_z0_points(int prec, int grid, cudaStream_t st, const Diode
                                 const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
                                 const double* qx, const double* qy, const float4* qpp, double* qF,
                                 double* partial, int* tickets, double kscale, int* queue) {
-  if (prec == 1) k_z0_points<1><<<rd_grid(k_z0_points<1>, 64, grid), 64, 0, st>>>(P, pool, plan, ph, qx, qy, qpp, qF, partial, tickets, kscale, queue);
+  if (prec == 1) k_z0_points<1><<<rd_grid(k_z0_points<1>, 32, grid), 32, 0, st>>>(P, pool, plan, ph, qx, qy, qpp, qF, partial, tickets, kscale, queue);
   else k_z0_points<0><<<rd_grid(k_z0_points<0>, RD_ITILE, grid), RD_ITILE, 0, st>>>(P, pool, plan, ph, qx, qy, qpp, qF, partial, tickets, kscale, queue);
   return cudaGetLastError();
 }

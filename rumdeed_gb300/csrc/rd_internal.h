@@ -25,11 +25,11 @@
 #define RD_TIP_CPT 2          // tip MH chains per thread (FP32 form; even)
 #endif
 #ifndef RD_TIP_UNROLL
-#define RD_TIP_UNROLL 2       // j-loop unroll of the FP32 tip MH tile
+#define RD_TIP_UNROLL 4       // j-loop unroll of the FP32 tip MH tile
 #endif
 #define RD_MH_PARTS 2         // planar MH jump launches per jump, one stream each (default)
 #define RD_MH_PARTS_MAX 4     // at most this many (rd_autotune / rd_set_mh_launch choose)
-#define RD_SUP_SPLIT 16       // blocks per diode in the supply reduction
+#define RD_SUP_SPLIT 64       // blocks per diode in the supply reduction
 #define RD_SUP_NCH 4          // at most this many j-chunks per tile of planar supply points
 #define RD_EMIT_SPLIT 8       // blocks per diode in the emission accept test
 // j-chunking of pair sums: at least RD_CLEN_MIN particles per chunk, at most
@@ -91,13 +91,16 @@ struct DiodeParams {
 };
 
 // Planner modes (k_plan): which i-set of each diode a pair-sum plan covers.
-// Modes up to PM_FORCE_TTS are pair sums (tiles x j-chunks), the two PM_PART
-// modes per-particle index spaces.  PM_ALL_DIODES added to PM_FORCE_PLANAR or
+// Modes up to PM_SUPPLY_LAT are pair sums (tiles x j-chunks), the two PM_PART
+// modes per-particle index spaces.  PM_SUPPLY_PLANAR: the supply points of
+// planar diodes with image charges (F_z only: the lateral components cancel
+// at the cathode); PM_SUPPLY_LAT: those of planar diodes without (all three
+// components, for the mean field of field.dt).  PM_ALL_DIODES added to PM_FORCE_PLANAR or
 // PM_FORCE_TIP also covers the two-time-step diodes (the plain
 // Calculate_Acceleration_Particles pass, which ignores two_time_step).
 enum { PM_FORCE_PLANAR = 0, PM_FORCE_TIP = 1, PM_FIELD = 2, PM_SUPPLY_PLANAR = 3,
-       PM_SUPPLY_TIP = 4, PM_MH = 5, PM_FORCE_TTS = 6, PM_PART = 7, PM_PART1024 = 8, PM_COUNT = 9,
-       PM_ALL_DIODES = 0x100 };
+       PM_SUPPLY_TIP = 4, PM_MH = 5, PM_FORCE_TTS = 6, PM_SUPPLY_LAT = 7, PM_PART = 8, PM_PART1024 = 9,
+       PM_COUNT = 10, PM_ALL_DIODES = 0x100 };
 
 // Supply quadrature grid of one diode, filled on the device (k_quad_fill):
 // planar, quad_n x quad_n Gauss-Legendre nodes (P panels of Q nodes per side)
@@ -128,6 +131,7 @@ struct DiodeDyn {
   double ramo_current, ramo_ion;   // ramo_current(species_elec), ramo_current(species_ion)
   double MH_std, a_rate, residual, N_sup;
   double F_avg_z, df_avg;   // field.dt quantities of the last emission
+  double F_avg_x, F_avg_y;  // lateral mean field (planar diodes without image charges; 0 otherwise)
   double avg_part_vel[3], avg_elec_vel[3], avg_ion_vel[3], avg_mob;   // Average_Velocities
   int n_vel, n_elec_vel, n_ion_vel;   // particle counts at the velocity update (before removal)
 };
@@ -138,8 +142,10 @@ struct DiodeDyn {
 // jumps of such a diode's chains in one launch (one cluster of RD_VAC_CTAS
 // CTAs); the tiled jump kernels skip it (planner mode PM_MH).
 #define RD_VAC_CTAS 8
-#define RD_VAC_THREADS 256
-#define RD_VAC_MAX_CHAINS 8192
+#define RD_VAC_THREADS 512
+#define RD_VAC_CPT 2          // chains per thread, kept in registers
+#define RD_VAC_MAX_CHAINS (RD_VAC_CTAS * RD_VAC_THREADS * RD_VAC_CPT)
+#define RD_VAC_WTAB 512       // supply-target table entries staged in shared memory
 #ifdef __CUDACC__
 __host__ __device__ inline bool rd_mh_vacuum(const DiodeParams& p, const DiodeDyn& y) {
   return p.geometry == RD_G_PLANAR && p.emission && !p.mh_serial && y.n == 0 && y.chains <= RD_VAC_MAX_CHAINS;

@@ -20,20 +20,47 @@
 
 namespace {
 
-__device__ __forceinline__ void mark_remove(const DiodeParams& p, DiodeDyn& y, Pool& pool, int i,
-                                            int gi, int why, const EventLog& ev, int d, int step) {
-  if (!pool.mask[gi]) return;
+// Marks particle gi removed (mask off, charge zeroed, absorption record) and
+// returns its contribution to the diode's removal counters: bit 0 removed,
+// bit 1 an electron, bit 2 at the anode.  The caller adds the counters up
+// (warp-aggregated in k_position, where a whole crossing front is removed at
+// once; directly by mark_remove).
+__device__ __forceinline__ int mark_remove_flags(const DiodeParams& p, Pool& pool, int gi, int why,
+                                                 const EventLog& ev, int d, int step) {
+  if (!pool.mask[gi]) return 0;
   pool.mask[gi] = 0;
   pool.q[gi] = 0.0;   // a marked particle no longer acts on others (:206-207)
+  if (pool.species[gi] != 1) return 1;
+  // density_absorb_{top,bot}.bin record (:241-257)
+  log_event(ev, pool.x[gi], pool.y[gi], pool.z[gi], pool.vx[gi], pool.vy[gi], pool.vz[gi], d,
+            why == 1 ? RD_EVENT_ABSORB_TOP : RD_EVENT_ABSORB_BOT, pool.section[gi], pool.id[gi], 1, step);
+  return why == 1 ? 7 : 3;
+}
+
+// Removal counters of one warp's marks (flags as mark_remove_flags returns;
+// every lane of the warp calls it, all for the same diode).
+__device__ __forceinline__ void count_removals_warp(DiodeDyn& y, int flags, int i) {
+  const unsigned rem = __ballot_sync(0xffffffffu, flags & 1);
+  if (!rem) return;
+  const unsigned top = __ballot_sync(0xffffffffu, flags == 7);
+  const unsigned bot = __ballot_sync(0xffffffffu, flags == 3);
+  const int imin = __reduce_min_sync(0xffffffffu, (flags & 1) ? i : 0x7fffffff);
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&y.n_remove, __popc(rem));
+    atomicMin(&y.first_dead, imin);
+    if (top) atomicAdd(&y.n_remove_top, __popc(top));
+    if (bot) atomicAdd(&y.n_remove_bot, __popc(bot));
+  }
+}
+
+__device__ __forceinline__ void mark_remove(const DiodeParams& p, DiodeDyn& y, Pool& pool, int i,
+                                            int gi, int why, const EventLog& ev, int d, int step) {
+  const int f = mark_remove_flags(p, pool, gi, why, ev, d, step);
+  if (!f) return;
   atomicAdd(&y.n_remove, 1);
   atomicMin(&y.first_dead, i);
-  if (pool.species[gi] == 1) {
-    if (why == 1) atomicAdd(&y.n_remove_top, 1);
-    else atomicAdd(&y.n_remove_bot, 1);
-    // density_absorb_{top,bot}.bin record (:241-257)
-    log_event(ev, pool.x[gi], pool.y[gi], pool.z[gi], pool.vx[gi], pool.vy[gi], pool.vz[gi], d,
-              why == 1 ? RD_EVENT_ABSORB_TOP : RD_EVENT_ABSORB_BOT, pool.section[gi], pool.id[gi], 1, step);
-  }
+  if (f == 7) atomicAdd(&y.n_remove_top, 1);
+  else if (f == 3) atomicAdd(&y.n_remove_bot, 1);
 }
 
 __device__ __forceinline__ void pack_one(const DiodeParams& p, const Pool& pool, int gi) {
@@ -75,7 +102,10 @@ __device__ __forceinline__ int plan_ni(const DiodeParams& p, const DiodeDyn& y, 
     case PM_FORCE_TIP: return (p.geometry == RD_G_TIP && std_force) ? nj : 0;
     case PM_FORCE_TTS: return p.tts > 0 ? nj : 0;
     case PM_FIELD: return npts[d];
-    case PM_SUPPLY_PLANAR: return (p.emission && p.geometry == RD_G_PLANAR) ? p.quad_n * p.quad_n : 0;
+    case PM_SUPPLY_PLANAR:
+      return (p.emission && p.geometry == RD_G_PLANAR && p.image_charge) ? p.quad_n * p.quad_n : 0;
+    case PM_SUPPLY_LAT:
+      return (p.emission && p.geometry == RD_G_PLANAR && !p.image_charge) ? p.quad_n * p.quad_n : 0;
     case PM_SUPPLY_TIP: return (p.emission && p.geometry == RD_G_TIP) ? 10000 : 0;
     // serial diodes: k_mh_serial; diodes with no particle in flight: k_mh_vacuum
     case PM_MH: return (p.emission && !p.mh_serial && !rd_mh_vacuum(p, y)) ? y.chains : 0;
@@ -114,10 +144,11 @@ k_plan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, int n
   __shared__ int s_run_items, s_run_chains;
   const int tid = threadIdx.x;
   const int tsize = (mode == PM_PART1024) ? 1024 : RD_ITILE;
-  const bool pair = ((mode & 0xff) <= PM_FORCE_TTS);
+  const bool pair = ((mode & 0xff) <= PM_SUPPLY_LAT);
   const int clen_min = chunk_rule & 0xffff, nch_max = chunk_rule >> 16;   // see rd_chunk_rule
   // the planar supply points are many tiles already: at most RD_SUP_NCH chunks per tile
-  const int nch_eff = (mode & 0xff) == PM_SUPPLY_PLANAR ? min(nch_max, RD_SUP_NCH) : nch_max;
+  const int nch_eff = ((mode & 0xff) == PM_SUPPLY_PLANAR || (mode & 0xff) == PM_SUPPLY_LAT)
+                          ? min(nch_max, RD_SUP_NCH) : nch_max;
   // grow the chunk length only if the items would not fit the scratch
   __shared__ int s_grow;
   if (tid == 0) s_grow = 0;
@@ -212,7 +243,9 @@ k_position(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool po
            const int* __restrict__ step_ptr) {
   for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
     int d, i;
-    if (!part_index(plan, ph, g, &d, &i)) continue;
+    const bool valid = part_index(plan, ph, g, &d, &i);   // d is the item's diode on every lane
+    int rm = 0;   // this lane's removal (mark_remove_flags)
+    if (valid) {
     const DiodeParams& p = P[d];
     const int gi = p.off + i;
     const int sp = pool.species[gi];
@@ -249,11 +282,13 @@ k_position(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool po
           log_event(ev, x, y, z, pool.vx[gi], pool.vy[gi], pool.vz[gi], d, RD_EVENT_PLANE + k,
                     pool.section[gi], pool.id[gi], pool.species[gi], step);
       }
-      if (z < 0.0) mark_remove(p, yy, pool, i, gi, 2, ev, d, step);
-      else if (z > p.d) mark_remove(p, yy, pool, i, gi, 1, ev, d, step);
-      if (p.geometry == RD_G_TIP && tip_eta(p, x, y, z) < p.eta_1) mark_remove(p, yy, pool, i, gi, 2, ev, d, step);
+      if (z < 0.0) rm = mark_remove_flags(p, pool, gi, 2, ev, d, step);
+      else if (z > p.d) rm = mark_remove_flags(p, pool, gi, 1, ev, d, step);
+      if (p.geometry == RD_G_TIP && tip_eta(p, x, y, z) < p.eta_1) rm |= mark_remove_flags(p, pool, gi, 2, ev, d, step);
     }
     pack_one(p, pool, gi);
+    }
+    count_removals_warp(Dy[d], rm, i);
   }
 }
 
@@ -472,6 +507,7 @@ k_compact_scatter(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict_
     int pre = 0;
     for (int q = 0; q < w; ++q) pre += wsum[q];
     pre += __popc(bal & ((1u << lane) - 1));
+    int bin = -1;   // life-time bin of a removed electron (record_lifetime :1135-1160)
     if (i < n && i >= y.first_dead) {
       if (m) {
         move_particle(pool, tmp, p.off + i, p.off + before + pre);
@@ -479,9 +515,13 @@ k_compact_scatter(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict_
         int lt = step - pool.step0[p.off + i];
         if (lt <= 0) lt = 1;
         if (lt > RD_MAX_LIFE) lt = RD_MAX_LIFE;
-        if (pool.species[p.off + i] == 1) atomicAdd(&life[(size_t)it.d * RD_MAX_LIFE + lt - 1], 1);
+        if (pool.species[p.off + i] == 1) bin = lt - 1;
       }
     }
+    // one atomic per distinct bin of the warp: electrons removed together mostly share one
+    const unsigned peers = __match_any_sync(0xffffffffu, bin);
+    if (bin >= 0 && lane == __ffs(peers) - 1)
+      atomicAdd(&life[(size_t)it.d * RD_MAX_LIFE + bin], __popc(peers));
     __syncthreads();
   }
 }

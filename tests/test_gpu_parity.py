@@ -700,3 +700,37 @@ def test_fp32c_mixed_electron_and_ion_tiles(rg, orc, nic):
                                       np.zeros(50)])])
     assert nrel(dio.calc_field_at_batch(pts), o.field_at(pts)) <= TOL32
     eng.close()
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-12), (1, 1e-5)])
+def test_emission_without_image_charges_and_lateral_field(rg, orc, prec, tol):
+    """A planar diode without image charges: its supply points carry all three
+    field components, so field.dt's mean field F_avg (Do_Surface_Integration_FE,
+    src/mod_field_emission_v2.F90:644-651) has lateral parts; with image charges
+    they cancel at the cathode.  Against the oracle: N_sup, the chain count
+    and F_avg (relative to |F_avg_z|); in FP64 also the emitted electrons."""
+    rng = np.random.default_rng(31)
+    d, V, n0 = 500 * NM, 1.0e3, 150
+    pos = np.column_stack([rng.uniform(-60 * NM, 60 * NM, n0), rng.uniform(-60 * NM, 60 * NM, n0),
+                           rng.uniform(2 * NM, 490 * NM, n0)])
+    eng = rg.Engine(precision=prec, max_diodes=2, particle_capacity=8192, chain_capacity=4096)
+    dio = eng.add_diode(V_s=V, gap=d, capacity=4096, image_charge=False, emitter_pos=(-50 * NM, -50 * NM),
+                        emitter_dim=(100 * NM, 100 * NM), work=[[2.0]], emission=True, mh_jumps=40,
+                        max_chains=300, quad_panels=8, quad_order=4, seed=31)
+    dio.add_particles(pos)
+    o = orc.OracleDiode(cap=4096, V_s=V, d=d, image_charge=False)
+    o.set_planar_emitter(-50 * NM, -50 * NM, 100 * NM, 100 * NM, [[2.0]])
+    o.set_emission(True, seed=31, mh_jumps=40, max_chains=300, quad_panels=8, quad_order=4)
+    for p in pos:
+        o.add(p)
+    eng.do_emission(1)
+    o.emission(1)
+    c = dio.counters()
+    assert c["N_sup"] == pytest.approx(o.s.N_sup, rel=tol)
+    ref = np.array([o.s.F_avg_x, o.s.F_avg_y, o.s.F_avg_z])
+    assert abs(ref[0]) + abs(ref[1]) > 1e-6 * abs(ref[2])          # the lateral mean is there
+    assert np.max(np.abs(np.array(c["F_avg"]) - ref)) <= tol * abs(ref[2]), (c["F_avg"], ref)
+    if prec == 0:
+        assert c["chains"] == o.s.last_chains and c["emitted_step"] == o.s.emitted_step
+        np.testing.assert_array_equal(dio.particles()["id"], o.iarr("id"))
+    eng.close()
