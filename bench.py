@@ -465,8 +465,9 @@ def run_ours(args, rank, world):
     if rank != 0:
         return
     # dominant kernel roofline (FP32 pipe; 20 flops per Coulomb-like term).  The unit is one
-    # MH jump: the two concurrent launches of k_mh_jump_planar<1> (one per half of the plan,
-    # on two streams), timed together by CUDA events that bracket the fork and the join.
+    # MH jump: the mh_parts concurrent launches of k_mh_jump_planar<1> (one per part of the
+    # plan, on their own streams), timed together by CUDA events that bracket the fork and
+    # the join.
     jumps = max(prof["mh_jump_launches"], 1)
     avg_ms = prof["mh_jumps_ms"] / jumps
     flops_per_jump = 20.0 * prof["mh_pair_evals"] / jumps
@@ -476,7 +477,8 @@ def run_ours(args, rank, world):
     if peak is None:
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
         peak_src = "nominal: 152 SMs x 128 lanes x 2 x 2.07 GHz"
-    traffic = MH_JUMP_DRAM_BYTES
+    # the ncu figure was taken on the 128-slot resident set; other mixes report none
+    traffic = MH_JUMP_DRAM_BYTES if args.slots == 128 else None
     plain_v, plain_caps, plain_n = plain_fp64_all(rg, resident, budget_s=args.plain_budget)
     cpu_v, cpu_desc, cores, cpu_t = cpu_sample(resident, rank=rank)
     line = {
@@ -527,11 +529,11 @@ def run_ours(args, rank, world):
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_source": peak_src,
-                     "unit_of_work": "one MH jump of every chain: the two concurrent launches "
-                                     "(halves of the plan) of k_mh_jump_planar<1>",
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the two "
-                                       "launches of a jump on the burst case (the same 128 resident "
-                                       "requests)",
+                     "unit_of_work": "one MH jump of every chain: the %d concurrent launches "
+                                     "(parts of the plan) of k_mh_jump_planar<1>" % tune["mh_parts"],
+                     "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
+                                        "launches of a jump on the burst case (the same 128 resident "
+                                        "requests)" if traffic else "not captured for this mix"),
                      "flops_convention": "20 flops per Coulomb-like term (Nyland et al.); "
                                          "1 term per (chain, particle) at the cathode"},
         "phase_ms": {k: prof[k] for k in ("supply_ms", "mh_init_ms", "mh_jumps_ms", "emit_ms",

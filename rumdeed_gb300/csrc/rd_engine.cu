@@ -757,6 +757,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
       e->dalloc(&e->qw, qcap) || e->dalloc(&e->qF, qcap) || e->dalloc(&e->qfx, qcap) ||
       e->dalloc(&e->qfy, qcap) || e->dalloc(&e->qpp, qcap) || e->dalloc(&e->cs.gx, chcap) || e->dalloc(&e->cs.gy, chcap) ||
       e->dalloc(&e->cs.fx, chcap) || e->dalloc(&e->cs.fy, chcap) || e->dalloc(&e->cs.fsup, chcap) ||
+      e->dalloc(&e->cs.fF, chcap) ||
       e->dalloc(&e->cs.fgx, chcap) || e->dalloc(&e->cs.fgy, chcap) ||
       e->dalloc(&e->cs.pph, chcap) || e->dalloc(&e->cs.pih, chcap) ||
       e->dalloc(&e->d_choff, S) || e->dalloc(&e->d_qoff, S) ||

@@ -231,34 +231,50 @@ __device__ __forceinline__ int work_cell_f(const DiodeParams& p, float x, float 
   return (yi - 1) * nx + (xi - 1);
 }
 
-// supply_log_tab in FP32 from the table entry (log phi, log(l_const/phi^2),
-// l_const/phi^2) (F < 0 as a float).
-__device__ __forceinline__ float supply_log_entry_f(const DiodeParams& p, float t0, float t1, float t2, float F) {
-  const float LF = logf(-F);
-  if (!p.image_charge) return 2.0f * LF - t0;
-  float l = t2 * (-F), ll = t1 + LF;
-  if (l > 1.0f) { l = 1.0f; ll = 0.0f; }
-  const float ty = 1.0f + l * ((1.0f / 9.0f) - (1.0f / 18.0f) * ll);
-  return (2.0f * LF - 2.0f * logf(ty)) - t0;
+// The FP32 chains compare targets by their parts.  Elec_Supply_log
+// (src/mod_field_emission_v2.F90:589-595) is
+//   s = 2 log(-F) - rho,   rho = 2 log t_y + log phi,
+//   t_y = 1 + l (1/9 - log(l) / 18),  l = min(l_const / phi^2 (-F), 1)
+// (t_y = 1 without image charges), and two targets differ by
+//   d = s_n - s_c = 2 log(F_n / F_c) - (rho_n - rho_c),
+// which the FP32 form evaluates without cancelling two values near 40
+// (mh_accept_one_f).  A chain keeps rho and its field as floats.  2 log t_y
+// lies in [0, 0.212] and is formed as 2 log1p(l (1/9 - log(l) / 18)).
+__device__ __forceinline__ float rho_entry_f(const DiodeParams& p, float t0, float t2, float F) {
+  if (!p.image_charge) return t0;
+  const float l = t2 * (-F);
+  float tau = 0.0f;                          // l below 1e-30: t_y - 1 < 4e-30
+  if (l > 1.0f) tau = 1.0f / 9.0f;
+  else if (l > 1.0e-30f) tau = l * ((1.0f / 9.0f) - (1.0f / 18.0f) * logf(l));
+  return fmaf(2.0f, log1pf(tau), t0);
 }
 
-// supply_log_tab in FP32 (F < 0 as a float).
-__device__ __forceinline__ float supply_log_f(const DiodeParams& p, const double* __restrict__ wtab,
-                                              int cell, float F) {
-  const double* t = wtab + 3 * (p.work_off + cell);
-  return supply_log_entry_f(p, (float)t[0], (float)t[1], (float)t[2], F);
+// Work-function cell or site of an FP32 chain's point (FP32 nm offsets from
+// the emitter centre); -1 for the Gaussian model, whose phi varies within any
+// cell.  It is the cell supply_log_chain_d takes.
+__device__ __forceinline__ int chain_cell_f(const DiodeParams& p, float x, float y) {
+  if (p.work_model == 1) return work_cell_f(p, x, y);
+  return work_cell(p, p.org_x + (double)x * 1.0e-9, p.org_y + (double)y * 1.0e-9);
 }
 
-// The FP32 chains' target at (x, y) given as FP32 nm offsets, any model.
-__device__ __forceinline__ float supply_log_xy_f(const DiodeParams& p, const double* __restrict__ wtab,
-                                                 float x, float y, float F) {
-  if (p.work_model == 1) return supply_log_f(p, wtab, work_cell_f(p, x, y), F);
-  const double X = p.org_x + (double)x * 1.0e-9, Y = p.org_y + (double)y * 1.0e-9;
-  const int cell = work_cell(p, X, Y);
-  if (cell >= 0) return supply_log_f(p, wtab, cell, F);
-  const double phi = gaussian_work(p, p.work_data, X, Y);
-  const double l2 = c_k.l_const / (phi * phi);
-  return supply_log_entry_f(p, (float)log(phi), (float)log(l2), (float)l2, F);
+// log phi and l_const / phi^2 as floats at an FP32 chain's point of cell `cell`.
+__device__ __forceinline__ void work_entry_f(const DiodeParams& p, const double* __restrict__ wtab, int cell,
+                                             float x, float y, float* t0, float* t2) {
+  if (cell >= 0) {
+    const double* t = wtab + 3 * (p.work_off + cell);
+    *t0 = (float)t[0]; *t2 = (float)t[2];
+    return;
+  }
+  const double phi = gaussian_work(p, p.work_data, p.org_x + (double)x * 1.0e-9, p.org_y + (double)y * 1.0e-9);
+  *t0 = (float)log(phi); *t2 = (float)(c_k.l_const / (phi * phi));
+}
+
+// rho of an FP32 chain's point for the field F < 0 (as a float).
+__device__ __forceinline__ float rho_xy_f(const DiodeParams& p, const double* __restrict__ wtab, float x,
+                                          float y, float F) {
+  float t0, t2;
+  work_entry_f(p, wtab, chain_cell_f(p, x, y), x, y, &t0, &t2);
+  return rho_entry_f(p, t0, t2, F);
 }
 
 // ---- cathode z = 0 field, planar ----------------------------------------------------
@@ -759,7 +775,9 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
           ok = 1; F = Fz; X = x; Y = y;
           if (lane == 0) {
             cs.fx[k] = fx; cs.fy[k] = fy;
-            cs.fsup[k] = supply_log_xy_f(p, wtab, fx, fy, (float)Fz);
+            const float Ff = (float)Fz;
+            cs.fsup[k] = rho_xy_f(p, wtab, fx, fy, Ff);
+            cs.fF[k] = Ff;
           }
         }
       } else {
@@ -865,7 +883,7 @@ __device__ __forceinline__ int mh_accept_one(const DiodeParams& p, ChainState& c
 
 // The FP64 target Elec_Supply_log (src/mod_field_emission_v2.F90:589-595) of
 // an FP32 chain's point (FP32 nm offsets from the emitter centre), with the
-// work-function cell or site chosen exactly as supply_log_xy_f chooses it.
+// work-function cell or site chosen exactly as chain_cell_f chooses it.
 __device__ __forceinline__ double supply_log_chain_d(const DiodeParams& p, const double* __restrict__ wtab,
                                                      float x, float y, double F) {
   if (p.work_model == 1) return supply_log_tab(p, wtab, work_cell_f(p, x, y), F);
@@ -875,15 +893,10 @@ __device__ __forceinline__ double supply_log_chain_d(const DiodeParams& p, const
   return fn_supply_log(F, gaussian_work(p, p.work_data, X, Y), p.image_charge);
 }
 
-// Guard band of the FP32 acceptance filter.  The FP32 target differs from the
-// FP64 one by at most ~1e-5 (logf within 1 ulp of values below ~50, the
-// field rounded to a float, three float additions), the FP32 log u by at most
-// ~2e-5 (see mh_accept_one_f), so a margin of 1e-3 leaves a factor of ~30.
-#define RD_MH_GUARD 1.0e-3f
-
-// The FP64 form's accept test for a decision inside the guard band (rare; kept
-// out of line so that it does not cost the pair-sum loop registers).  o0, o1
-// are the Philox words of the FP64 form's uniform u (u01_words).
+// The FP64 form's accept test for a decision the FP32 filter leaves open
+// (rare; kept out of line so that it does not cost the pair-sum loop
+// registers).  o0, o1 are the Philox words of the FP64 form's uniform u
+// (u01_words).
 __device__ __noinline__ bool mh_take_fp64(const DiodeParams& p, const double* __restrict__ wtab, float wx,
                                           float wy, double F, float cx, float cy, double Fc, uint32_t o0,
                                           uint32_t o1) {
@@ -892,37 +905,63 @@ __device__ __noinline__ bool mh_take_fp64(const DiodeParams& p, const double* __
   return snd >= scd || log(u01_words(o0, o1)) <= snd - scd;
 }
 
-// mh_accept_one for the FP32 chains (proposal wx, wy in FP32 nm offsets).
-// The decision is the FP64 form's (:1400-1443): take the proposal iff
-// log u <= sn - sc, with the 53-bit uniform u of the FP64 form and the FP64
-// targets sn (proposal) and sc (current point).  FP32 estimates decide it
-// whenever they are further than RD_MH_GUARD from the threshold (the FP64
-// comparison must then agree); otherwise both targets and log u are
-// evaluated in FP64 -- a few in ten thousand decisions.  The FP32 estimate of
-// u is the leading Philox word o0 / 2^32 (u lies in [o0, o0 + 1) / 2^32), whose
-// log is within 1.6e-5 of log u for o0 >= 2^16; smaller words (one draw in
-// 65536) take the FP64 test.  Chains store the FP32 estimate of their target; the FP64 one is
-// recomputed from the stored point and field (cs.F, FP64) when needed.
+// Guard of the FP32 acceptance filter: ten times a bound on how far its
+// estimates of d = s_n - s_c and of log u can lie from the FP64 form's values.
+// With e = 2^-24: 2 log(F_n / F_c) from the fields rounded to floats and one
+// division is within 6.2e + 2e |.| of its value; each rho within
+// 1.95e + 2e |rho| (logf and log1pf within 1 ulp, the table entries rounded to
+// floats, t_y - 1 <= 1/9 with |l d(t_y)/dl| <= 1/18); log u within
+// 2.01e + 2e |log u| (the 53-bit u rounded to a float); three sums rounded.
+// In all |error| <= 12.2e + 5e S with S = |2 log(F_n / F_c)| + |rho_n| +
+// |rho_c| (+ |log u| once it is formed): 7.3e-7 + 3.0e-7 S.  The FP64 values'
+// own rounding (~1e-13) does not matter at this scale.
+__device__ __forceinline__ float mh_guard(float S) { return 8.0e-6f + 4.0e-6f * S; }
+
+// The accept / reject decision of an FP32 chain (:1400-1443) as the FP64 form
+// takes it: take the proposal (wx, wy; field F, Ff = (float)F; rho_n) iff
+// s_n >= s_c or log u <= s_n - s_c, with the FP64 targets and the 53-bit
+// uniform u of the FP64 form; the chain is at (cx, cy) with field Fc (Fcf its
+// float) and rho_c.  The FP32 estimates decide whenever they lie further than
+// mh_guard from the threshold, where the FP64 comparison must agree; inside
+// the guard the FP64 test runs (about one decision in 10^5).  Equal fields
+// and one work-function cell give equal FP64 targets, hence s_n >= s_c.
+__device__ __forceinline__ bool mh_decide_f(const DiodeParams& p, const double* __restrict__ wtab, int c,
+                                            int it_idx, uint32_t step, double F, float Ff, float rn, float wx,
+                                            float wy, float cx, float cy, double Fc, float Fcf, float rc) {
+  const float l2 = 2.0f * logf(Ff / Fcf);
+  const float df = l2 - (rn - rc);
+  const float S = fabsf(l2) + fabsf(rn) + fabsf(rc);
+  if (isfinite(df) && df >= mh_guard(S)) return true;   // s_n > s_c in FP64 too
+  if (df == 0.0f && __double_as_longlong(F) == __double_as_longlong(Fc)) {
+    const int cn = chain_cell_f(p, wx, wy);
+    if (cn >= 0 && cn == chain_cell_f(p, cx, cy)) return true;
+  }
+  uint32_t o[4];
+  philox4x32((uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, (uint32_t)p.seed, (uint32_t)(p.seed >> 32), o);
+  // u = o0 / 2^32 + (o1 >> 11) / 2^53 exactly (u01_words); the float carries two roundings
+  const float lu = logf(fmaf((float)(o[1] >> 11), 1.1102230246251565e-16f, (float)o[0] * 2.3283064365386963e-10f));
+  if (isfinite(df)) {
+    const float g = mh_guard(S + fabsf(lu));
+    if (lu <= df - g) return true;
+    if (lu > df + g) return false;
+  }
+  return mh_take_fp64(p, wtab, wx, wy, F, cx, cy, Fc, o[0], o[1]);
+}
+
+// mh_accept_one for the FP32 chains (proposal wx, wy in FP32 nm offsets), the
+// decision by mh_decide_f.  Chains store their point, rho and field as floats
+// and the field in FP64 (cs.F), from which mh_take_fp64 recomputes the FP64
+// target when it is needed.
 __device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState& cs, const double* wtab,
                                                int c, int k, int it_idx, uint32_t step, double F,
                                                float wx, float wy) {
   int a = 0;
   if (F < 0.0) {
-    const float sn = supply_log_xy_f(p, wtab, wx, wy, (float)F);
-    const float df = sn - cs.fsup[k];
-    bool take;
-    if (isfinite(df) && df >= RD_MH_GUARD) {
-      take = true;                       // sn > sc in FP64 too, and log u <= 0
-    } else {
-      uint32_t o[4];
-      philox4x32((uint32_t)c, (uint32_t)it_idx, step, RNG_ACCEPT, (uint32_t)p.seed, (uint32_t)(p.seed >> 32), o);
-      const float lu = logf((float)o[0] * 2.3283064365386963e-10f);
-      if (o[0] >= 65536u && isfinite(df) && lu <= df - RD_MH_GUARD) take = true;
-      else if (o[0] >= 65536u && isfinite(df) && lu > df + RD_MH_GUARD) take = false;
-      else take = mh_take_fp64(p, wtab, wx, wy, F, cs.fx[k], cs.fy[k], cs.F[k], o[0], o[1]);   // guard band
-    }
-    if (take) {
-      cs.fx[k] = wx; cs.fy[k] = wy; cs.fsup[k] = sn; cs.F[k] = F;
+    const float Ff = (float)F;
+    const float rn = rho_xy_f(p, wtab, wx, wy, Ff);
+    if (mh_decide_f(p, wtab, c, it_idx, step, F, Ff, rn, wx, wy, cs.fx[k], cs.fy[k], cs.F[k], cs.fF[k],
+                    cs.fsup[k])) {
+      cs.fx[k] = wx; cs.fy[k] = wy; cs.fsup[k] = rn; cs.fF[k] = Ff; cs.F[k] = F;
       cs.x[k] = p.org_x + (double)wx * 1.0e-9;
       cs.y[k] = p.org_y + (double)wy * 1.0e-9;
       a = 1;
@@ -992,7 +1031,9 @@ __device__ __forceinline__ void mh_start_f32(const DiodeParams& p, ChainState& c
     cs.fx[k] = x; cs.fy[k] = y;
     cs.x[k] = p.org_x + (double)x * 1.0e-9;
     cs.y[k] = p.org_y + (double)y * 1.0e-9;
-    cs.fsup[k] = supply_log_xy_f(p, wtab, x, y, (float)F);
+    const float Ff = (float)F;
+    cs.fsup[k] = rho_xy_f(p, wtab, x, y, Ff);
+    cs.fF[k] = Ff;
     float g1, g2;
     gauss2f(p.seed, (uint32_t)c, 1u, step, &g1, &g2);
     cs.fgx[k] = g1; cs.fgy[k] = g2;
@@ -1140,7 +1181,10 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
 // them back at the end; the proposal, start and accept arithmetic is that of
 // mh_propose_*, mh_start_* and mh_accept_one(_f) step for step (the tiled path
 // keeps the same state in memory), so the chains evolve bit for bit as in
-// k_mh_jump_planar + k_mh_init.  After each jump the CTAs reduce their
+// k_mh_jump_planar + k_mh_init.  One field everywhere makes the FP64 targets of
+// two points of one work-function cell equal, so such a proposal is taken
+// (s_n >= s_c) without a draw, as the FP64 form takes it; a uniform work
+// function makes every jump such.  After each jump the CTAs reduce their
 // acceptance counts, exchange them through distributed shared memory across a
 // cluster barrier and each apply the same MH_std update (MH_std_update
 // :603-612); jumps alternate between two count buffers, so a CTA never
@@ -1153,13 +1197,15 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
             double kscale, int nslots) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
-  __shared__ int s_cnt[2][2];
-  __shared__ int s_red[2][RD_VAC_THREADS / 32];
+  constexpr int NW = RD_VAC_THREADS / 32;
+  __shared__ unsigned s_cnt[2];          // this CTA's counts of a jump: (rejected << 16) | accepted
+  __shared__ unsigned s_red[NW];
   __shared__ double s_mhs;
   // the diode's parameters and supply-target table in shared memory for the whole
   // sampling: global data would be fetched again after every cluster barrier
   __shared__ DiodeParams sp;
   __shared__ double swt[3 * RD_VAC_WTAB];
+  __shared__ float2 swf[RD_VAC_WTAB];   // (log phi, l_const / phi^2) as floats
   const int d = blockIdx.x / RD_VAC_CTAS;
   if (d >= nslots) return;
   DiodeDyn& y = Dy[d];
@@ -1174,7 +1220,11 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
   const int cells = sp.work_model == 1 ? sp.work_nx * sp.work_ny : (sp.work_model == 4 ? sp.work_nx : 0);
   const bool wsh = cells <= RD_VAC_WTAB;   // the table's values are the same wherever they are read
   if (wsh)
-    for (int k = tid; k < 3 * cells; k += blockDim.x) swt[k] = wtab[3 * sp.work_off + k];
+    for (int k = tid; k < cells; k += blockDim.x) {
+      const double* t = wtab + 3 * (sp.work_off + k);
+      swt[3 * k] = t[0]; swt[3 * k + 1] = t[1]; swt[3 * k + 2] = t[2];
+      swf[k] = make_float2((float)t[0], (float)t[2]);
+    }
   __syncthreads();
   if (wsh && tid == 0) sp.work_off = 0;   // entries now at swt[3 * cell]
   __syncthreads();
@@ -1184,36 +1234,46 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
   const int G = RD_VAC_CTAS * RD_VAC_THREADS, g0 = rank * RD_VAC_THREADS + tid;
   const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
   const double F = z0_finish<PREC>(p, 0.0, kscale);
+  const float Ff = (float)F;
+  const bool start_ok = F < 0.0 && p.init_rounds > 0;
   const int ndim_first = (p.mh_jumps + 2) / 4;
   double mhs = y.MH_std, arate = y.a_rate;
+  // the FP32 chains' rho at (x, y) of cell `cell`, from the staged float table
+  auto rho_at = [&](int cell, float x, float yv) -> float {
+    float t0, t2;
+    if (wsh && cell >= 0) { const float2 e = swf[cell]; t0 = e.x; t2 = e.y; }
+    else work_entry_f(p, wtab, cell, x, yv, &t0, &t2);
+    return rho_entry_f(p, t0, t2, Ff);
+  };
   // chain state in registers: FP32 chains (nm offsets) or FP64 chains (m)
-  int ok[RD_VAC_CPT];
-  float fx[RD_VAC_CPT], fy[RD_VAC_CPT], fsup[RD_VAC_CPT], fgx[RD_VAC_CPT], fgy[RD_VAC_CPT];
-  double dx[RD_VAC_CPT], dy[RD_VAC_CPT], dsup[RD_VAC_CPT], dgx[RD_VAC_CPT], dgy[RD_VAC_CPT], Fc[RD_VAC_CPT];
+  int ok[RD_VAC_CPT], cc[RD_VAC_CPT];
+  float fx[RD_VAC_CPT], fy[RD_VAC_CPT], rc[RD_VAC_CPT], fgx[RD_VAC_CPT], fgy[RD_VAC_CPT];
+  double dx[RD_VAC_CPT], dy[RD_VAC_CPT], dsup[RD_VAC_CPT], dgx[RD_VAC_CPT], dgy[RD_VAC_CPT];
   // the start: round 0; a chain that fails it fails every round (the field does not change)
   int failed = 0;
 #pragma unroll
   for (int q = 0; q < RD_VAC_CPT; ++q) {
     const int c = g0 + q * G;
-    ok[q] = 0;
-    fx[q] = fy[q] = fsup[q] = fgx[q] = fgy[q] = 0.0f;
-    dx[q] = dy[q] = dsup[q] = dgx[q] = dgy[q] = 0.0; Fc[q] = F;
+    ok[q] = 0; cc[q] = -1;
+    fx[q] = fy[q] = rc[q] = fgx[q] = fgy[q] = 0.0f;
+    dx[q] = dy[q] = dsup[q] = dgx[q] = dgy[q] = 0.0;
     if (c >= M) continue;
     if constexpr (PREC == 1) {   // mh_propose_f32 (init) + mh_start_f32
       float u1, u2;
       rng2f(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
       const float x = fminf(fmaf(u1, p.em_wx, -p.em_hx), p.em_hx);
       const float yv = fminf(fmaf(u2, p.em_wy, -p.em_hy), p.em_hy);
-      if (F < 0.0 && p.init_rounds > 0) {
+      if (start_ok) {
         ok[q] = 1; fx[q] = x; fy[q] = yv;
-        fsup[q] = supply_log_xy_f(p, wtab, x, yv, (float)F);
+        cc[q] = chain_cell_f(p, x, yv);
+        rc[q] = rho_at(cc[q], x, yv);
         gauss2f(p.seed, (uint32_t)c, 1u, step, &fgx[q], &fgy[q]);
       }
     } else {                     // mh_propose_f64 (init) + mh_start_f64
       double u1, u2;
       rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
       const double x = u1 * p.em_Lx + p.em_x0, yv = u2 * p.em_Ly + p.em_y0;
-      if (F < 0.0 && p.init_rounds > 0) {
+      if (start_ok) {
         ok[q] = 1; dx[q] = x; dy[q] = yv;
         dsup[q] = supply_log_xy(p, wtab, x, yv, F);
         gauss2(p.seed, (uint32_t)c, 1u, step, &dgx[q], &dgy[q]);
@@ -1223,7 +1283,7 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
   }
   if (failed) atomicAdd(&y.chains_failed, failed);
   for (int it = 1; it <= p.mh_jumps; ++it) {
-    int a = 0, r = 0;
+    unsigned cnt = 0;   // (rejected << 16) | accepted over this thread's chains
     if constexpr (PREC == 1) {
       const float mf = (float)mhs;
       const float sx = (it > ndim_first) ? p.em_wx * mf : p.em_wx * 0.10f;
@@ -1231,7 +1291,7 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
       const float hx = p.em_hx, hy = p.em_hy;
 #pragma unroll
       for (int q = 0; q < RD_VAC_CPT; ++q) {
-        if (!ok[q]) continue;
+        if (!ok[q]) continue;   // an ok chain has F < 0
         const int c = g0 + q * G;
         // mh_propose_f32
         float x = fmaf(fgx[q], sx, fx[q]);
@@ -1239,25 +1299,16 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
         if (x > hx) x = hx - (x - hx); else if (x < -hx) x = -hx - (x + hx);
         if (yv > hy) yv = hy - (yv - hy); else if (yv < -hy) yv = -hy - (yv + hy);
         // mh_accept_one_f
-        int acc = 0;
-        if (F < 0.0) {
-          const float sn = supply_log_xy_f(p, wtab, x, yv, (float)F);
-          const float df = sn - fsup[q];
-          bool take;
-          if (isfinite(df) && df >= RD_MH_GUARD) {
-            take = true;
-          } else {
-            uint32_t o[4];
-            philox4x32((uint32_t)c, (uint32_t)it, step, RNG_ACCEPT, (uint32_t)p.seed, (uint32_t)(p.seed >> 32), o);
-            const float lu = logf((float)o[0] * 2.3283064365386963e-10f);
-            if (o[0] >= 65536u && isfinite(df) && lu <= df - RD_MH_GUARD) take = true;
-            else if (o[0] >= 65536u && isfinite(df) && lu > df + RD_MH_GUARD) take = false;
-            else take = mh_take_fp64(p, wtab, x, yv, F, fx[q], fy[q], Fc[q], o[0], o[1]);
-          }
-          if (take) { fx[q] = x; fy[q] = yv; fsup[q] = sn; Fc[q] = F; acc = 1; }
+        const int cn = chain_cell_f(p, x, yv);
+        bool take = cn >= 0 && cn == cc[q];   // equal FP64 targets
+        float rn = rc[q];
+        if (!take) {
+          rn = rho_at(cn, x, yv);
+          take = mh_decide_f(p, wtab, c, it, step, F, Ff, rn, x, yv, fx[q], fy[q], F, Ff, rc[q]);
         }
+        if (take) { fx[q] = x; fy[q] = yv; rc[q] = rn; cc[q] = cn; cnt += 1u; }
+        else cnt += 1u << 16;
         if (it < p.mh_jumps) gauss2f(p.seed, (uint32_t)c, (uint32_t)(it + 1), step, &fgx[q], &fgy[q]);
-        a += acc; r += 1 - acc;
       }
     } else {
       const double sx = (it > ndim_first) ? p.em_Lx * mhs : p.em_Lx * 0.10;
@@ -1272,50 +1323,33 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
         if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
         if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
         // mh_accept_one
-        int acc = 0;
-        if (F < 0.0) {
-          const double sn = supply_log_xy(p, wtab, x, yv, F);
-          const double sc = dsup[q];
-          bool take = sn >= sc;
-          if (!take) {
-            double u1, u2;
-            rng2(p.seed, (uint32_t)c, (uint32_t)it, step, RNG_ACCEPT, &u1, &u2);
-            take = log(u1) <= sn - sc;
-          }
-          if (take) { dx[q] = x; dy[q] = yv; dsup[q] = sn; Fc[q] = F; acc = 1; }
+        const double sn = supply_log_xy(p, wtab, x, yv, F);
+        const double sc = dsup[q];
+        bool take = sn >= sc;
+        if (!take) {
+          double u1, u2;
+          rng2(p.seed, (uint32_t)c, (uint32_t)it, step, RNG_ACCEPT, &u1, &u2);
+          take = log(u1) <= sn - sc;
         }
+        if (take) { dx[q] = x; dy[q] = yv; dsup[q] = sn; cnt += 1u; }
+        else cnt += 1u << 16;
         if (it < p.mh_jumps) gauss2(p.seed, (uint32_t)c, (uint32_t)(it + 1), step, &dgx[q], &dgy[q]);
-        a += acc; r += 1 - acc;
       }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_xor_sync(0xffffffffu, a, o);
-      r += __shfl_xor_sync(0xffffffffu, r, o);
-    }
-    if (lane == 0) { s_red[0][w] = a; s_red[1][w] = r; }
+    // at most RD_VAC_MAX_CHAINS = 8192 chains: each half of the packed sum stays below 2^16
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    if (lane == 0) s_red[w] = cnt;
     __syncthreads();
     const int par = it & 1;
     if (w == 0) {   // this CTA's counts
-      int A = lane < RD_VAC_THREADS / 32 ? s_red[0][lane] : 0, R = lane < RD_VAC_THREADS / 32 ? s_red[1][lane] : 0;
-      for (int o = 16; o > 0; o >>= 1) {
-        A += __shfl_xor_sync(0xffffffffu, A, o);
-        R += __shfl_xor_sync(0xffffffffu, R, o);
-      }
-      if (lane == 0) { s_cnt[par][0] = A; s_cnt[par][1] = R; }
+      unsigned v = __reduce_add_sync(0xffffffffu, lane < NW ? s_red[lane] : 0u);
+      if (lane == 0) s_cnt[par] = v;
     }
     cl.sync();   // every CTA's counts of this jump are in place
     if (w == 0) {   // the cluster's counts: lane q reads CTA q's
-      int A = 0, R = 0;
-      if (lane < RD_VAC_CTAS) {
-        const int* rc = cl.map_shared_rank(&s_cnt[par][0], lane);
-        A = rc[0]; R = rc[1];
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        A += __shfl_xor_sync(0xffffffffu, A, o);
-        R += __shfl_xor_sync(0xffffffffu, R, o);
-      }
+      const unsigned v = __reduce_add_sync(0xffffffffu, lane < RD_VAC_CTAS ? *cl.map_shared_rank(&s_cnt[par], lane) : 0u);
       if (lane == 0) {
-        mh_std_step(p, &mhs, &arate, it, ndim_first, A, R);
+        mh_std_step(p, &mhs, &arate, it, ndim_first, (int)(v & 0xffffu), (int)(v >> 16));
         s_mhs = mhs;
       }
     }
@@ -1334,9 +1368,10 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
       cs.x[k] = p.em_x0; cs.y[k] = p.em_y0;
       continue;
     }
-    cs.F[k] = Fc[q];
+    cs.F[k] = F;
     if constexpr (PREC == 1) {
-      cs.fx[k] = fx[q]; cs.fy[k] = fy[q]; cs.fsup[k] = fsup[q]; cs.fgx[k] = fgx[q]; cs.fgy[k] = fgy[q];
+      cs.fx[k] = fx[q]; cs.fy[k] = fy[q]; cs.fsup[k] = rc[q]; cs.fF[k] = Ff;
+      cs.fgx[k] = fgx[q]; cs.fgy[k] = fgy[q];
       cs.x[k] = p.org_x + (double)fx[q] * 1.0e-9;
       cs.y[k] = p.org_y + (double)fy[q] * 1.0e-9;
     } else {

@@ -195,8 +195,9 @@ struct ChainState {
   int *em;               // emits this step (k_emit_test)
   double *gx, *gy;       // planar: Gaussian pair of the next proposal
   // FP32-compensated planar chains: position as FP32 nm offsets from the
-  // emitter centre (the chain lives on that grid), log target, Gaussian pair
-  float *fx, *fy, *fsup, *fgx, *fgy;
+  // emitter centre (the chain lives on that grid), the target's rho and the
+  // field as floats (mh_decide_f), Gaussian pair
+  float *fx, *fy, *fsup, *fF, *fgx, *fgy;
   // FP32-compensated tip chains: the proposal packed once per jump for the
   // field tiles (the point on the FP32 nm grid and the high words of its
   // apex-sphere image)
