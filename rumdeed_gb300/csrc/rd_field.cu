@@ -819,14 +819,21 @@ __global__ void k_mh_init(const DiodeParams* __restrict__ P, DiodeDyn* __restric
 // ---- MH jump iteration ---------------------------------------------------------------------
 // The MH_std update of one jump iteration from its acceptance counts
 // (MH_std_update :603-612, once per iteration after the warm-up jumps).
+// MH_std_update (:603-612) in parts: the factor of a jump with A accepted and
+// R rejected proposals (A + R > 0), and the clamped product.
+__device__ __forceinline__ double mh_std_gain(int A, int R, double* rate) {
+  *rate = (double)A / (double)(A + R);
+  return exp(0.025 * (*rate - 0.35));
+}
+__device__ __forceinline__ double mh_std_clamp(const DiodeParams& p, double s) {
+  if (s > p.mh_hi) s = p.mh_hi; else if (s < p.mh_lo) s = p.mh_lo;
+  return s;
+}
 __device__ __forceinline__ void mh_std_step(const DiodeParams& p, double* mh_std, double* a_rate, int it_idx,
                                             int ndim_first, int A, int R) {
   if (it_idx > ndim_first && A + R > 0) {
-    double rate = (double)A / (double)(A + R);
-    *a_rate = rate;
-    double s = *mh_std * exp(0.025 * (rate - 0.35));
-    if (s > p.mh_hi) s = p.mh_hi; else if (s < p.mh_lo) s = p.mh_lo;
-    *mh_std = s;
+    const double g = mh_std_gain(A, R, a_rate);
+    *mh_std = mh_std_clamp(p, *mh_std * g);
   }
 }
 
@@ -1172,6 +1179,14 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
   queue_leave(queue, lo, hi);
 }
 
+// mh_decide_f for a vacuum-field chain (F_n = F_c), out of line: k_mh_vacuum
+// reaches it only for a proposal into another work-function cell.
+__device__ __noinline__ bool mh_decide_vac(const DiodeParams& p, const double* __restrict__ wtab, int c, int it_idx,
+                                           uint32_t step, double F, float Ff, float rn, float wx, float wy, float cx,
+                                           float cy, float rc) {
+  return mh_decide_f(p, wtab, c, it_idx, step, F, Ff, rn, wx, wy, cx, cy, F, Ff, rc);
+}
+
 // The whole batched MH sampling of a planar diode with no particle in flight
 // (rd_mh_vacuum), in one launch: one cluster of RD_VAC_CTAS CTAs per diode
 // slot runs round 0 of the chains' start, the rounds k_mh_init would run, and
@@ -1201,6 +1216,7 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
   __shared__ unsigned s_cnt[2];          // this CTA's counts of a jump: (rejected << 16) | accepted
   __shared__ unsigned s_red[NW];
   __shared__ double s_mhs;
+  __shared__ float s_mhf;
   // the diode's parameters and supply-target table in shared memory for the whole
   // sampling: global data would be fetched again after every cluster barrier
   __shared__ DiodeParams sp;
@@ -1226,6 +1242,13 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
       swf[k] = make_float2((float)t[0], (float)t[2]);
     }
   __syncthreads();
+  // a uniform work function: every cell's entry the same (bit for bit)
+  int differs = 0;
+  if (wsh)
+    for (int k = tid; k < cells; k += blockDim.x)
+      for (int e = 0; e < 3; ++e)
+        differs |= __double_as_longlong(swt[3 * k + e]) != __double_as_longlong(swt[e]);
+  const bool uniform = __syncthreads_or(differs) == 0 && wsh && cells >= 1 && sp.mh_jumps <= RD_VAC_MAXJ;
   if (wsh && tid == 0) sp.work_off = 0;   // entries now at swt[3 * cell]
   __syncthreads();
   if (wsh) wtab = swt;
@@ -1238,6 +1261,7 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
   const bool start_ok = F < 0.0 && p.init_rounds > 0;
   const int ndim_first = (p.mh_jumps + 2) / 4;
   double mhs = y.MH_std, arate = y.a_rate;
+  float mhf = (float)mhs;
   // the FP32 chains' rho at (x, y) of cell `cell`, from the staged float table
   auto rho_at = [&](int cell, float x, float yv) -> float {
     float t0, t2;
@@ -1282,10 +1306,63 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
     if (!ok[q]) failed++;
   }
   if (failed) atomicAdd(&y.chains_failed, failed);
-  for (int it = 1; it <= p.mh_jumps; ++it) {
+  if (uniform) {
+    // One field and one target everywhere: every proposal of a started chain is
+    // taken (s_n >= s_c), so each jump's counts are (T, 0) for the T = M chains
+    // that started (none when the field is not favourable) and the MH_std
+    // schedule is known before the first jump.  Thread 0 forms it with
+    // mh_std_gain / mh_std_clamp, as mh_std_step does jump by jump; the chains
+    // then walk without a barrier.
+    __shared__ double s_seq[RD_VAC_MAXJ + 1];   // the step-size factor of each jump
+    __shared__ float s_seqf[RD_VAC_MAXJ + 1];   // the same for the FP32 chains
+    __shared__ double s_end[2];
+    if (tid == 0) {
+      const int T = start_ok ? M : 0;
+      double m = mhs, ar = arate, rate = 0.0, g = 0.0;
+      if (T > 0) g = mh_std_gain(T, 0, &rate);
+      for (int it = 1; it <= p.mh_jumps; ++it) {
+        s_seq[it] = (it > ndim_first) ? m : 0.10;
+        s_seqf[it] = (it > ndim_first) ? (float)m : 0.10f;
+        if (it > ndim_first && T > 0) { ar = rate; m = mh_std_clamp(p, m * g); }
+      }
+      s_end[0] = m; s_end[1] = ar;
+    }
+    __syncthreads();
+    for (int it = 1; it <= p.mh_jumps; ++it) {
+      if constexpr (PREC == 1) {
+        const float mf = s_seqf[it];
+        const float sx = p.em_wx * mf, sy = p.em_wy * mf;
+        const float hx = p.em_hx, hy = p.em_hy;
+#pragma unroll
+        for (int q = 0; q < RD_VAC_CPT; ++q) {
+          if (!ok[q]) continue;
+          float x = fmaf(fgx[q], sx, fx[q]);
+          float yv = fmaf(fgy[q], sy, fy[q]);
+          if (x > hx) x = hx - (x - hx); else if (x < -hx) x = -hx - (x + hx);
+          if (yv > hy) yv = hy - (yv - hy); else if (yv < -hy) yv = -hy - (yv + hy);
+          fx[q] = x; fy[q] = yv;
+          if (it < p.mh_jumps) gauss2f(p.seed, (uint32_t)(g0 + q * G), (uint32_t)(it + 1), step, &fgx[q], &fgy[q]);
+        }
+      } else {
+        const double sx = p.em_Lx * s_seq[it], sy = p.em_Ly * s_seq[it];
+        const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+#pragma unroll
+        for (int q = 0; q < RD_VAC_CPT; ++q) {
+          if (!ok[q]) continue;
+          double x = dgx[q] * sx + dx[q], yv = dgy[q] * sy + dy[q];
+          if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
+          if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
+          dx[q] = x; dy[q] = yv;
+          if (it < p.mh_jumps) gauss2(p.seed, (uint32_t)(g0 + q * G), (uint32_t)(it + 1), step, &dgx[q], &dgy[q]);
+        }
+      }
+    }
+    mhs = s_end[0]; arate = s_end[1];
+  }
+  for (int it = 1; !uniform && it <= p.mh_jumps; ++it) {
     unsigned cnt = 0;   // (rejected << 16) | accepted over this thread's chains
     if constexpr (PREC == 1) {
-      const float mf = (float)mhs;
+      const float mf = mhf;
       const float sx = (it > ndim_first) ? p.em_wx * mf : p.em_wx * 0.10f;
       const float sy = (it > ndim_first) ? p.em_wy * mf : p.em_wy * 0.10f;
       const float hx = p.em_hx, hy = p.em_hy;
@@ -1304,7 +1381,7 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
         float rn = rc[q];
         if (!take) {
           rn = rho_at(cn, x, yv);
-          take = mh_decide_f(p, wtab, c, it, step, F, Ff, rn, x, yv, fx[q], fy[q], F, Ff, rc[q]);
+          take = mh_decide_vac(p, wtab, c, it, step, F, Ff, rn, x, yv, fx[q], fy[q], rc[q]);
         }
         if (take) { fx[q] = x; fy[q] = yv; rc[q] = rn; cc[q] = cn; cnt += 1u; }
         else cnt += 1u << 16;
@@ -1350,11 +1427,11 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
       const unsigned v = __reduce_add_sync(0xffffffffu, lane < RD_VAC_CTAS ? *cl.map_shared_rank(&s_cnt[par], lane) : 0u);
       if (lane == 0) {
         mh_std_step(p, &mhs, &arate, it, ndim_first, (int)(v & 0xffffu), (int)(v >> 16));
-        s_mhs = mhs;
+        s_mhs = mhs; s_mhf = (float)mhs;
       }
     }
     __syncthreads();
-    mhs = s_mhs;
+    mhs = s_mhs; mhf = s_mhf;
   }
   // the chains back to memory, as the tiled path leaves them
 #pragma unroll

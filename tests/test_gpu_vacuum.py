@@ -7,6 +7,11 @@ the same diode without it takes the vacuum kernel.  One step of each must
 agree in every emission counter and in every emitted electron's position, in
 both precisions.  (The FP64 form of the empty one-diode deck is also checked
 against the oracle chain for chain in test_gpu_config_parity.py.)
+
+A uniform work function (one cell, or cells that all hold the same value)
+makes every target equal, so every proposal is taken and the kernel walks the
+chains without a barrier per jump; a checkerboard of different values takes
+the jump-by-jump path with the cluster-wide acceptance counts.
 """
 import numpy as np
 import pytest
@@ -16,12 +21,17 @@ pytestmark = pytest.mark.gpu
 NM = 1e-9
 
 
-def _step(rg, prec, atom, jumps):
+CHECKER = [[2.0, 2.3], [2.6, 2.1]]
+UNIFORM = [[2.2]]
+UNIFORM4 = [[2.2, 2.2], [2.2, 2.2]]
+
+
+def _step(rg, prec, atom, jumps, work):
     eng = rg.Engine(precision=prec, max_diodes=2, particle_capacity=8192, chain_capacity=8192,
                     quad_capacity=65536, event_capacity=1 << 15)
     d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, time_step=0.25e-15, capacity=8000,
                       emitter_pos=(-500 * NM, -500 * NM), emitter_dim=(1000 * NM, 1000 * NM),
-                      work=[[2.0, 2.3], [2.6, 2.1]], emission=True, mh_jumps=jumps, seed=99)
+                      work=work, emission=True, mh_jumps=jumps, seed=99)
     if atom:
         d.add_particles(np.array([[400 * NM, 400 * NM, 900 * NM]]), species=[rg.ATOM], step=0)
     eng.step(1)
@@ -33,10 +43,11 @@ def _step(rg, prec, atom, jumps):
     return c, sites
 
 
-@pytest.mark.parametrize("prec,jumps", [(1, 200), (1, 37), (0, 60)])
-def test_vacuum_kernel_equals_tiled_kernels(rg, prec, jumps):
-    empty, s_empty = _step(rg, prec, False, jumps)
-    atom, s_atom = _step(rg, prec, True, jumps)
+@pytest.mark.parametrize("prec,jumps,work", [(1, 200, CHECKER), (1, 37, CHECKER), (0, 60, CHECKER),
+                                             (1, 200, UNIFORM), (1, 100, UNIFORM4), (0, 60, UNIFORM)])
+def test_vacuum_kernel_equals_tiled_kernels(rg, prec, jumps, work):
+    empty, s_empty = _step(rg, prec, False, jumps, work)
+    atom, s_atom = _step(rg, prec, True, jumps, work)
     assert 1000 < empty["chains"] <= 8192 and empty["emitted_step"] > 50
     for key in ("N_sup", "chains", "chains_failed", "MH_std", "a_rate", "df_avg", "emitted_step", "residual"):
         assert empty[key] == atom[key], key
