@@ -930,8 +930,9 @@ def case_one_diode(args):
     """One planar diode of the reference's one-diode configuration (1 um gap,
     2 kV, 1000 x 1000 nm emitter, dt 0.25 fs, one image term) at work function
     --phi and --jumps MH jumps per step, in --precision; no CPU leg and no
-    tuner, so that a profiler sees only the engine's own launches.  Prints
-    device ms per step and the kernels per step."""
+    tuner (--chunk-min / --chunk-count set the chunking by hand), so that a
+    profiler sees only the engine's own launches.  Prints device ms per step
+    and the kernels per step."""
     import rumdeed_gb300 as rg
     rg.build()
     side = 1000 * NM
@@ -941,6 +942,8 @@ def case_one_diode(args):
     d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, time_step=0.25e-15, image_charge=True, N_ic_max=0,
                       capacity=20000, emitter_pos=(-side / 2, -side / 2), emitter_dim=(side, side),
                       emission=True, seed=SEED, work=[[args.phi]], mh_jumps=args.jumps)
+    if args.chunk_min or args.chunk_count:
+        eng.set_chunking(args.chunk_min, args.chunk_count)
     if args.uncaptured:
         # every step phase by phase from the host (rd_profile_step): plain stream launches, which a
         # profiler lists one by one (the step graph of a lone diode holds a conditional node)
@@ -1070,6 +1073,8 @@ def main():
     ap.add_argument("--phi", type=float, default=4.7, help="one-diode: work function (eV)")
     ap.add_argument("--jumps", type=int, default=100, help="one-diode: MH jumps per step")
     ap.add_argument("--precision", default="fp32c", choices=["fp32c", "fp64"], help="one-diode: engine precision")
+    ap.add_argument("--chunk-min", type=int, default=0, help="one-diode: j-chunk length (0: the default)")
+    ap.add_argument("--chunk-count", type=int, default=0, help="one-diode: j-chunks per tile at most (0: the default)")
     ap.add_argument("--uncaptured", action="store_true",
                     help="one-diode: run the steps phase by phase (rd_profile_step) instead of the step graph")
     ap.add_argument("--validate-every", type=int, default=0,

@@ -253,3 +253,15 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float v) {
   hi = s;
   lo += err;
 }
+
+// (hi, lo) += (h, l) for float pairs: the two-sum of the high parts, the low
+// parts and its error added, then renormalised (fast two-sum), so that
+// lo stays below an ulp of hi.  Sums of chunk partials in chunk order.
+__device__ __forceinline__ void pair_add(float& hi, float& lo, float h, float l) {
+  const float s = hi + h;
+  const float bp = s - hi;
+  const float err = (hi - (s - bp)) + (h - bp);
+  const float t = (lo + l) + err;
+  hi = s + t;
+  lo = t - (hi - s);
+}

@@ -359,7 +359,7 @@ __device__ __forceinline__ void z0_tile_x2(const float4* __restrict__ s0, const 
 // two-sum and returned as doubles; z0_finish turns them into V/m.
 template <int CPT>
 __device__ __forceinline__ void z0_item_sumN(const DiodeParams& p, const Pool& pool, const ItemRef& it,
-                                             const float4* pts, double* out) {
+                                             const float4* pts, float* out_hi, float* out_lo) {
   constexpr int NP = CPT / 2;
   __shared__ float4 sp[3][RD_TILE];
   float4* sh = sp[0];   // nic > 0: raw packs
@@ -406,7 +406,7 @@ __device__ __forceinline__ void z0_item_sumN(const DiodeParams& p, const Pool& p
     for (int i = 0; i < CPT; ++i) two_sum_acc(hi[i], lo[i], t[i]);
   }
 #pragma unroll
-  for (int i = 0; i < CPT; ++i) out[i] = (double)hi[i] + (double)lo[i];
+  for (int i = 0; i < CPT; ++i) { out_hi[i] = hi[i]; out_lo[i] = lo[i]; }
 }
 
 __device__ __forceinline__ double z0_tile_f64(const rd_d4* __restrict__ sj, int kmax, double px,
@@ -478,6 +478,32 @@ __device__ __forceinline__ double z0_finish(const DiodeParams& p, double s, doub
   return p.E_z + f * c_k.div_fac_c * s;
 }
 
+// Chunk partials of FP32 pair sums: a chunk of a tile with more than one
+// stores its (hi, lo) pairs in the partial scratch (8 bytes per sum, as the
+// FP64 partials); the tile's last chunk (tile_ticket) adds them in chunk order
+// with pair_add and returns true, the others return false.  Float pairs keep
+// ~44 bits, far below the FP32 tiles' own rounding, and their sum costs no
+// FP64 operation.
+template <int CPT>
+__device__ __forceinline__ bool pair_partials(double* partial, int* tickets, const ItemRef& it, int g, int tid,
+                                              int nt, float* hi, float* lo) {
+  if (it.nch <= 1) return true;
+  float2* pf = reinterpret_cast<float2*>(partial);
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) pf[(size_t)g * RD_ITILE + tid + q * nt] = make_float2(hi[q], lo[q]);
+  if (!tile_ticket(tickets, it)) return false;
+#pragma unroll
+  for (int q = 0; q < CPT; ++q) {
+    float H = 0.0f, L = 0.0f;
+    for (int c = 0; c < it.nch; ++c) {
+      const float2 v = __ldcg(pf + (size_t)(it.base + c) * RD_ITILE + tid + q * nt);
+      pair_add(H, L, v.x, v.y);
+    }
+    hi[q] = H; lo[q] = L;
+  }
+  return true;
+}
+
 // F_z at the supply quadrature points (qpp holds their FP32-frame split).
 // FP32: 32 threads, four points each (the MH jump's form: one shared load feeds
 // four points, and a point's sum is the same lane arithmetic in the same j
@@ -507,19 +533,21 @@ k_z0_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __res
         const int i = it.i0 + tid + q * nt;
         pts[q] = i < m ? qpp[qo + i] : z4;
       }
-      z0_item_sumN<CPT>(p, pool, it, pts, s);
+      float hi[CPT], lo[CPT];
+      z0_item_sumN<CPT>(p, pool, it, pts, hi, lo);
+      if (!pair_partials<CPT>(partial, tickets, it, g, tid, nt, hi, lo)) continue;
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) s[q] = (double)hi[q] + (double)lo[q];
     } else {
       const int i = it.i0 + tid;
       const bool valid = i < m;
       s[0] = z0_item_sum<PREC>(p, pool, it, valid ? qx[qo + i] : p.em_x0, valid ? qy[qo + i] : p.em_y0,
                                make_float4(0.f, 0.f, 0.f, 0.f), sh, sl, sj);
-    }
-    if (it.nch > 1) {
-      for (int q = 0; q < CPT; ++q) partial[(size_t)g * RD_ITILE + tid + q * nt] = s[q];
-      if (!tile_ticket(tickets, it)) continue;
-      for (int q = 0; q < CPT; ++q) {
-        s[q] = 0.0;
-        for (int c = 0; c < it.nch; ++c) s[q] += __ldcg(partial + (size_t)(it.base + c) * RD_ITILE + tid + q * nt);
+      if (it.nch > 1) {
+        partial[(size_t)g * RD_ITILE + tid] = s[0];
+        if (!tile_ticket(tickets, it)) continue;
+        s[0] = 0.0;
+        for (int c = 0; c < it.nch; ++c) s[0] += __ldcg(partial + (size_t)(it.base + c) * RD_ITILE + tid);
       }
     }
     for (int q = 0; q < CPT; ++q) {
@@ -958,19 +986,19 @@ __device__ __forceinline__ bool mh_decide_f(const DiodeParams& p, const double* 
 // mh_accept_one for the FP32 chains (proposal wx, wy in FP32 nm offsets), the
 // decision by mh_decide_f.  Chains store their point, rho and field as floats
 // and the field in FP64 (cs.F), from which mh_take_fp64 recomputes the FP64
-// target when it is needed.
+// target when it is needed.  The point in FP64 metres (cs.x, cs.y), which only
+// the emission test reads, is formed once, at the last jump.
 __device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState& cs, const double* wtab,
                                                int c, int k, int it_idx, uint32_t step, double F,
                                                float wx, float wy) {
   int a = 0;
+  float cx = cs.fx[k], cy = cs.fy[k];
   if (F < 0.0) {
     const float Ff = (float)F;
     const float rn = rho_xy_f(p, wtab, wx, wy, Ff);
-    if (mh_decide_f(p, wtab, c, it_idx, step, F, Ff, rn, wx, wy, cs.fx[k], cs.fy[k], cs.F[k], cs.fF[k],
-                    cs.fsup[k])) {
+    if (mh_decide_f(p, wtab, c, it_idx, step, F, Ff, rn, wx, wy, cx, cy, cs.F[k], cs.fF[k], cs.fsup[k])) {
       cs.fx[k] = wx; cs.fy[k] = wy; cs.fsup[k] = rn; cs.fF[k] = Ff; cs.F[k] = F;
-      cs.x[k] = p.org_x + (double)wx * 1.0e-9;
-      cs.y[k] = p.org_y + (double)wy * 1.0e-9;
+      cx = wx; cy = wy;
       a = 1;
     }
   }
@@ -978,6 +1006,9 @@ __device__ __forceinline__ int mh_accept_one_f(const DiodeParams& p, ChainState&
     float g1, g2;
     gauss2f(p.seed, (uint32_t)c, (uint32_t)(it_idx + 1), step, &g1, &g2);
     cs.fgx[k] = g1; cs.fgy[k] = g2;
+  } else {
+    cs.x[k] = p.org_x + (double)cx * 1.0e-9;
+    cs.y[k] = p.org_y + (double)cy * 1.0e-9;
   }
   return a;
 }
@@ -1136,19 +1167,20 @@ k_mh_jump_planar(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, P
       float4 pts[CPT];
 #pragma unroll
       for (int q = 0; q < CPT; ++q) pts[q] = make_float4(fwx[q], 0.f, fwy[q], 0.f);
-      z0_item_sumN<CPT>(p, pool, it, pts, s);
+      float hi[CPT], lo[CPT];
+      z0_item_sumN<CPT>(p, pool, it, pts, hi, lo);
+      if (!pair_partials<CPT>(partial, tickets, it, g, tid, nt, hi, lo)) continue;
+#pragma unroll
+      for (int q = 0; q < CPT; ++q) s[q] = (double)hi[q] + (double)lo[q];
     } else {
       __shared__ float4 sh[RD_TILE], sl[RD_TILE];
       __shared__ rd_d4 sj[RD_TILE];
       s[0] = z0_item_sum<PREC>(p, pool, it, wx[0], wy[0], make_float4(0.f, 0.f, 0.f, 0.f), sh, sl, sj);
-    }
-    if (it.nch > 1) {
-      for (int q = 0; q < CPT; ++q) partial[(size_t)g * RD_ITILE + tid + q * nt] = s[q];
-      if (!tile_ticket(tickets, it)) continue;
-      for (int q = 0; q < CPT; ++q) {
-        s[q] = 0.0;
-        for (int cc = 0; cc < it.nch; ++cc)
-          s[q] += __ldcg(partial + (size_t)(it.base + cc) * RD_ITILE + tid + q * nt);
+      if (it.nch > 1) {
+        partial[(size_t)g * RD_ITILE + tid] = s[0];
+        if (!tile_ticket(tickets, it)) continue;
+        s[0] = 0.0;
+        for (int cc = 0; cc < it.nch; ++cc) s[0] += __ldcg(partial + (size_t)(it.base + cc) * RD_ITILE + tid);
       }
     }
     // epilogue of the completed tile
