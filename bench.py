@@ -827,23 +827,31 @@ def case_uncapped(args):
 
 def case_compact(args):
     """Absorption and compaction at full size: 64 planar diodes of 262144
-    electrons (16.8 M), of which three in four sit just below the anode moving
-    up and cross it in the next position pass, the others (every fourth, so
-    the survivors are spread over each diode) at mid-gap at rest.  One position
-    pass marks the crossers; the removal that follows compacts each diode's
-    survivors stably (rd_time_remove, CUDA events).  Algorithmic bytes: the
-    survey's 2 x the moved survivors' state, 152 B of FP64 and int state per
-    particle read and written once; the implementation moves each survivor
-    twice (to the compaction pool and back) and rewrites its FP32 packs."""
+    electrons (16.8 M).  Two removal patterns: (a) three in four sit just below
+    the anode moving up and cross it in the next position pass, the others
+    (every fourth, so the survivors are spread over each diode) at mid-gap at
+    rest; (b) 1 % of the electrons at random indices cross, the scattered
+    removals of the reference's own compaction benchmark (Util/bench_compact.f90,
+    1e6 particles with 1e4 removals).  One position pass marks the crossers;
+    the removal that follows compacts each diode's survivors stably in place
+    (rd_time_remove, CUDA events).  Algorithmic bytes: the survey's 2 x the
+    moved survivors' state, 152 B of FP64 and int state per particle read and
+    written once; the implementation also writes each moved survivor's 64 B of
+    FP32 packs and reads and rewrites the 4 B removal mask of every particle
+    behind the first removed one."""
     import rumdeed_gb300 as rg
     rg.build()
     D, n = 64, max(1024, args.verlet_n // 64)
 
-    def fill(eng, D, n):
+    def fill(eng, D, n, pattern):
         rng = np.random.default_rng(11)
         for k in range(D):
             d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, capacity=n, image_charge=True, N_ic_max=0)
-            keep = (np.arange(n) % 4) == 0
+            if pattern == "three_in_four":
+                keep = (np.arange(n) % 4) == 0
+            else:
+                keep = np.ones(n, dtype=bool)
+                keep[rng.choice(n, n // 100, replace=False)] = False
             z = np.where(keep, 500 * NM, 999.9 * NM)
             vz = np.where(keep, 0.0, 1.0e8)
             d.add_particles(np.column_stack([rng.uniform(-500 * NM, 500 * NM, n), rng.uniform(-500 * NM, 500 * NM, n), z]),
@@ -851,24 +859,26 @@ def case_compact(args):
 
     warm = rg.Engine(precision=rg.PREC_FP32C, max_diodes=2, particle_capacity=2 * 4096 + 64, chain_capacity=64,
                      quad_capacity=64)
-    fill(warm, 2, 4096)
+    fill(warm, 2, 4096, "three_in_four")
     warm.time_remove()   # loads the kernels
     warm.close()
-    eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=D, particle_capacity=D * (n + 64), chain_capacity=4096,
-                    quad_capacity=4096)
-    fill(eng, D, n)
-    pos_ms, rem_ms, moved, removed = eng.time_remove()
-    left = sum(d.counters()["n"] for d in eng.diodes.values())
-    eng.close()
-    alg = 2.0 * moved * 152
-    impl = moved * (4 * 152 + 64)
     peak = hbm_peak_gbs()
-    print(json.dumps({"case": "compact", "diodes": D, "electrons": D * n, "removed": removed, "moved": moved,
-                      "survivors": left, "position_ms": pos_ms, "remove_ms": rem_ms,
-                      "algorithmic_GBs": alg / (rem_ms / 1e3) / 1e9, "implementation_GBs": impl / (rem_ms / 1e3) / 1e9,
-                      "hbm_peak_GBs": peak, "frac_algorithmic": alg / (rem_ms / 1e3) / 1e9 / peak if peak else None,
-                      "bytes": {"algorithmic_per_moved": 2 * 152, "implementation_per_moved": 4 * 152 + 64}}),
-          flush=True)
+    for pattern in ("three_in_four", "scattered_1pct"):
+        eng = rg.Engine(precision=rg.PREC_FP32C, max_diodes=D, particle_capacity=D * (n + 64), chain_capacity=4096,
+                        quad_capacity=4096)
+        fill(eng, D, n, pattern)
+        pos_ms, rem_ms, moved, removed = eng.time_remove()
+        left = sum(d.counters()["n"] for d in eng.diodes.values())
+        eng.close()
+        alg = 2.0 * moved * 152
+        impl = moved * (2 * 152 + 64)
+        print(json.dumps({"case": "compact", "pattern": pattern, "diodes": D, "electrons": D * n, "removed": removed,
+                          "moved": moved, "survivors": left, "position_ms": pos_ms, "remove_ms": rem_ms,
+                          "algorithmic_GBs": alg / (rem_ms / 1e3) / 1e9,
+                          "implementation_GBs": impl / (rem_ms / 1e3) / 1e9,
+                          "hbm_peak_GBs": peak, "frac_algorithmic": alg / (rem_ms / 1e3) / 1e9 / peak if peak else None,
+                          "bytes": {"algorithmic_per_moved": 2 * 152, "implementation_per_moved": 2 * 152 + 64}}),
+              flush=True)
 
 
 def case_burst(args):

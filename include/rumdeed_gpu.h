@@ -192,7 +192,12 @@ int rd_mark_remove(rd_engine* e, int diode, int index, int why);
  *   rd_update_position Update_Position (Velocity_Verlet, mod_verlet.F90:123-162)
  *   rd_remove_particles Remove_Particles (mod_pair.F90:352-562)
  *   rd_step            the three in order, as one captured CUDA graph
- *   rd_run             nsteps consecutive rd_step calls, steps first..first+nsteps-1 */
+ *   rd_run             nsteps consecutive rd_step calls, steps first..first+nsteps-1
+ * The compaction works in place: each 1024-particle tile waits, with a bounded
+ * number of polls, until the earlier tiles it overwrites have read their
+ * particles.  Those waits always end in a working run; if one ever gave up,
+ * rd_remove_particles, rd_run, rd_serve, rd_profile_step and rd_time_remove
+ * return RD_ERR_STATE, and the particle state is no longer valid. */
 int rd_do_emission(rd_engine* e, int step);
 int rd_update_position(rd_engine* e, int step);
 int rd_remove_particles(rd_engine* e, int step);

@@ -18,7 +18,7 @@ LIB = os.path.join(OUT_DIR, "librumdeed_gb300.so")
 DRIVER_SRC = os.path.join(HERE, "driver", "rd_main.cpp")
 DRIVER = os.path.join(OUT_DIR, "rd_main")
 SOURCES = ["rd_force.cu", "rd_field.cu", "rd_step.cu", "rd_engine.cu", "rd_noalloc.cu"]
-HEADERS = ["rd_internal.h", "rd_device.cuh", "rd_pair.cuh", "rd_tiles.cuh"]
+HEADERS = ["rd_internal.h", "rd_device.cuh", "rd_pair.cuh", "rd_tiles.cuh", "rd_split.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-ftz=true", "-Xcompiler", "-fPIC,-ffp-contract=off",
          "-I", os.path.join(HERE, "..", "include")]

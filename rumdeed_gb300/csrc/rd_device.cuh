@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "rd_internal.h"
+#include "rd_split.h"
 
 // Each translation unit holds its own copy of the constants (no relocatable
 // device code); rd_upload_constants_<unit>() fills it at engine creation.
@@ -224,12 +225,10 @@ __device__ __forceinline__ void vacuum_field(const DiodeParams& P, double x, dou
 }
 
 // ---- FP32 frame ---------------------------------------------------------------
-// Position in nm split into a high float and the float of the remainder.
+// Position in nm split into a high float and the float of the remainder
+// (hi = (float)v, lo = (float)(v - hi); formed from the bits, rd_split.h).
 __device__ __forceinline__ void split_nm(double v_m, double origin_m, float* hi, float* lo) {
-  double v = (v_m - origin_m) * 1.0e9;
-  float h = (float)v;
-  *hi = h;
-  *lo = (float)(v - (double)h);
+  rd_split_exact((v_m - origin_m) * 1.0e9, hi, lo);
 }
 
 // Append one record to the event log (no-op without a log).

@@ -86,9 +86,8 @@ cudaError_t rd_launch_force_tts(int grid, cudaStream_t st, const DiodeParams* P,
                                 const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
                                 double* partial, int* tickets, int* queue, const int* step_ptr);
 cudaError_t rd_launch_compact(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
-                              DiodeDyn* Dy, const Pool& pool, const Pool& tmp,
-                              const PlanEntry* plan, const PlanHeader* ph, int* kept, int* life,
-                              const int* step_ptr);
+                              DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
+                              int* cnt, int* pre, int* flag, int* cq, int* life, const int* step_ptr);
 cudaError_t rd_launch_step_set(cudaStream_t st, int* step_ptr, int step);
 cudaError_t rd_launch_step_inc(cudaStream_t st, int* step_ptr);
 cudaError_t rd_launch_add_particles(cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
@@ -232,7 +231,8 @@ struct rd_engine {
   // device memory
   DiodeParams* dP = nullptr;
   DiodeDyn* dD = nullptr;
-  Pool pool{}, tmp{};
+  Pool pool{};
+  double *save_ax = nullptr, *save_ay = nullptr, *save_az = nullptr;   // accelerations kept across rd_autotune
   std::vector<void*> allocs;
   double* work = nullptr;
   double* wtab = nullptr;   // per work cell: log phi, log(l_const/phi^2), l_const/phi^2
@@ -249,7 +249,9 @@ struct rd_engine {
                                // MH (part 0 / 1), [2..3] tip MH, [4..5] force, [6..7] supply,
                                // [6 + 2p .. 7 + 2p] planar MH part p >= 2 (8 + 2 RD_MH_PARTS_MAX)
   EventLog evlog{nullptr, nullptr, 0};   // emission / absorption records (rd_events_take)
-  int* kept = nullptr;
+  int *ccnt = nullptr, *cpre = nullptr, *cflag = nullptr;   // compaction: per 256-particle unit survivors,
+                                                            // first destinations and load flags
+  int* cq = nullptr;      // compaction: [0] tile counter, [1] blocks left, [2] waits that gave up
   double* ramo = nullptr;   // velocity-pass item partials (10 per 128-particle item)
   int* life = nullptr;
   int* d_step = nullptr;
@@ -591,10 +593,21 @@ static int launch_update_position(rd_engine* e) {
   return RD_OK;
 }
 
+// Waits of the in-place compaction (k_compact_move) that gave up: each is a
+// tile that stored nothing, so the particle state is no longer valid.  Read
+// after the engine stream has drained.
+static int compaction_check(rd_engine* e) {
+  int bad = 0;
+  CK(cudaMemcpyAsync(&bad, e->cq + 2, sizeof(int), cudaMemcpyDeviceToHost, e->st));
+  CK(cudaStreamSynchronize(e->st));
+  if (bad) return fail(RD_ERR_STATE, "compaction: a wait on an earlier tile gave up; the particle state is not valid");
+  return RD_OK;
+}
+
 static int launch_remove(rd_engine* e) {
   CK(plan(e, PM_PART1024));
-  CK(rd_launch_compact(e->grid, e->nslots_hw(), e->st, e->dP, e->dD, e->pool, e->tmp,
-                       e->plan[PM_PART1024], e->ph[PM_PART1024], e->kept, e->life, e->d_step));
+  CK(rd_launch_compact(e->grid, e->nslots_hw(), e->st, e->dP, e->dD, e->pool, e->plan[PM_PART1024],
+                       e->ph[PM_PART1024], e->ccnt, e->cpre, e->cflag, e->cq, e->life, e->d_step));
   e->kernels_in_step += 4;
   return RD_OK;
 }
@@ -751,7 +764,11 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   e->max_items = (int)std::min<long long>(
       1 << 26, std::max((long long)RD_NCH_MAX * (std::max(cap, chcap) / RD_ITILE + 4LL * S),
                         (long long)RD_SUP_NCH * (qcap / RD_ITILE + 4LL * S)) + 65536);
-  if ((rc = alloc_pool(e, e->pool, cap)) || (rc = alloc_pool(e, e->tmp, cap))) return bail(rc);
+  // compaction units: four per 1024-particle tile, at most capacity/1024 + slots tiles
+  const size_t cunits = 4 * ((size_t)cap / 1024 + (size_t)S + 1);
+  if ((rc = alloc_pool(e, e->pool, cap))) return bail(rc);
+  if (e->dalloc(&e->save_ax, cap) || e->dalloc(&e->save_ay, cap) || e->dalloc(&e->save_az, cap))
+    return bail(fail(RD_ERR_NOMEM, "device allocation failed"));
   if (e->dalloc(&e->dP, S) || e->dalloc(&e->dD, S) || e->dalloc(&e->work, (size_t)S * 4 + 4096) || e->dalloc(&e->wtab, 3 * ((size_t)S * 4 + 4096)) ||
       e->dalloc(&e->qx, qcap) || e->dalloc(&e->qy, qcap) || e->dalloc(&e->qz, qcap) ||
       e->dalloc(&e->qw, qcap) || e->dalloc(&e->qF, qcap) || e->dalloc(&e->qfx, qcap) ||
@@ -763,7 +780,9 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
       e->dalloc(&e->d_choff, S) || e->dalloc(&e->d_qoff, S) ||
       e->dalloc(&e->d_npts, S) || e->dalloc(&e->d_zero_off, S) ||
       e->dalloc(&e->partial, (size_t)e->max_items * 3 * RD_ITILE) ||
-      e->dalloc(&e->tickets, e->max_items) || e->dalloc(&e->kept, e->max_items) ||
+      e->dalloc(&e->tickets, e->max_items) ||
+      e->dalloc(&e->ccnt, cunits) || e->dalloc(&e->cpre, cunits) || e->dalloc(&e->cflag, cunits) ||
+      e->dalloc(&e->cq, 4) ||
       e->dalloc(&e->sup_part, (size_t)S * RD_SUP_SPLIT * 4) ||
       e->dalloc(&e->item_queue, 8 + 2 * RD_MH_PARTS_MAX) ||
       (cfg->event_capacity > 0 && (e->dalloc(&e->evlog.buf, (size_t)cfg->event_capacity) ||
@@ -782,6 +801,7 @@ int rd_engine_create(const rd_engine_config* cfg, rd_engine** out) {
   cudaMemsetAsync(e->dP, 0, sizeof(DiodeParams) * S, e->st);
   cudaMemsetAsync(e->dD, 0, sizeof(DiodeDyn) * S, e->st);
   cudaMemsetAsync(e->tickets, 0, sizeof(int) * e->max_items, e->st);
+  cudaMemsetAsync(e->cq, 0, sizeof(int) * 4, e->st);
   cudaMemsetAsync(e->item_queue, 0, sizeof(int) * (8 + 2 * RD_MH_PARTS_MAX), e->st);
   if (e->evlog.count) cudaMemsetAsync(e->evlog.count, 0, sizeof(int), e->st);
   e->evlog.cap = cfg->event_capacity > 0 ? cfg->event_capacity : 0;
@@ -1366,13 +1386,13 @@ int rd_time_remove(rd_engine* e, double* position_ms, double* remove_ms, long lo
   }
   CK(plan(e, PM_PART1024));
   CK(cudaEventRecord(e->ev0, e->st));
-  CK(rd_launch_compact(e->grid, e->nslots_hw(), e->st, e->dP, e->dD, e->pool, e->tmp, e->plan[PM_PART1024],
-                       e->ph[PM_PART1024], e->kept, e->life, e->d_step));
+  CK(rd_launch_compact(e->grid, e->nslots_hw(), e->st, e->dP, e->dD, e->pool, e->plan[PM_PART1024],
+                       e->ph[PM_PART1024], e->ccnt, e->cpre, e->cflag, e->cq, e->life, e->d_step));
   CK(cudaEventRecord(e->ev1, e->st));
   CK(cudaEventSynchronize(e->ev1));
   CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
   *remove_ms = ms;
-  return RD_OK;
+  return compaction_check(e);
 }
 
 int rd_time_field_at(rd_engine* e, int d, int M, const double* pos, int reps, double* ms_per_eval) {
@@ -1476,9 +1496,9 @@ int rd_autotune(rd_engine* e, rd_tune_result* out) {
   if (rc) return rc;
   // the force passes overwrite the current accelerations: keep them in the compaction pool
   const size_t bytes = sizeof(double) * (size_t)e->cfg.particle_capacity;
-  CK(cudaMemcpyAsync(e->tmp.ax, e->pool.ax, bytes, cudaMemcpyDeviceToDevice, e->st));
-  CK(cudaMemcpyAsync(e->tmp.ay, e->pool.ay, bytes, cudaMemcpyDeviceToDevice, e->st));
-  CK(cudaMemcpyAsync(e->tmp.az, e->pool.az, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaMemcpyAsync(e->save_ax, e->pool.ax, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaMemcpyAsync(e->save_ay, e->pool.ay, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaMemcpyAsync(e->save_az, e->pool.az, bytes, cudaMemcpyDeviceToDevice, e->st));
   const int jumps = std::max(signature(e).jumps, 1);
   const int saved_min = e->clen_min, saved_max = e->nch_max;
   const int user_parts = e->mh_parts, user_form = e->mh_form;
@@ -1527,9 +1547,9 @@ int rd_autotune(rd_engine* e, rd_tune_result* out) {
   e->mh_parts = best_parts;
   e->mh_form = best_form;
   if (sg.emit_planar) best = std::min(best, best_fms + jumps * best_mh_ms);
-  CK(cudaMemcpyAsync(e->pool.ax, e->tmp.ax, bytes, cudaMemcpyDeviceToDevice, e->st));
-  CK(cudaMemcpyAsync(e->pool.ay, e->tmp.ay, bytes, cudaMemcpyDeviceToDevice, e->st));
-  CK(cudaMemcpyAsync(e->pool.az, e->tmp.az, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaMemcpyAsync(e->pool.ax, e->save_ax, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaMemcpyAsync(e->pool.ay, e->save_ay, bytes, cudaMemcpyDeviceToDevice, e->st));
+  CK(cudaMemcpyAsync(e->pool.az, e->save_az, bytes, cudaMemcpyDeviceToDevice, e->st));
   CK(cudaStreamSynchronize(e->st));
   out->chunk_min = best_min;
   out->chunk_count_max = best_max;
@@ -1636,7 +1656,7 @@ int rd_remove_particles(rd_engine* e, int step) {
   int rc = launch_remove(e);
   if (rc) return rc;
   CK(cudaStreamSynchronize(e->st));
-  return RD_OK;
+  return compaction_check(e);
 }
 
 int rd_run(rd_engine* e, int first_step, int nsteps) {
@@ -1654,7 +1674,7 @@ int rd_run(rd_engine* e, int first_step, int nsteps) {
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
   e->last_ms = ms;
-  return RD_OK;
+  return compaction_check(e);
 }
 
 int rd_step(rd_engine* e, int step) { return rd_run(e, step, 1); }
@@ -1933,7 +1953,7 @@ int rd_profile_step(rd_engine* e, int step, rd_phase_times* out) {
   float tot;
   CK(cudaEventElapsedTime(&tot, ev[0], ev[8]));
   out->total_ms = tot;
-  return RD_OK;
+  return compaction_check(e);
 }
 
 // ---- serving --------------------------------------------------------------------------
@@ -2074,6 +2094,7 @@ int rd_serve(rd_engine* e, int iterations, rd_serve_stats* out) {
     if ((rc = serve_admit(e, out, e->gstep + 1))) return rc;
     for (int sidx : e->pending) was_pending[sidx] = 1;
     CK(cudaStreamSynchronize(e->st));
+    if ((rc = compaction_check(e))) return rc;
     out->d2h_bytes += (long long)sizeof(DiodeDyn) * S;
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));

@@ -39,6 +39,7 @@
 // the planner's chunk rule argument: clen_min | nch_max << 16
 inline int rd_chunk_rule(int clen_min, int nch_max) { return clen_min | (nch_max << 16); }
 #define RD_MAX_LIFE 1000
+#define RD_COMPACT_SPIN (1 << 22)   // polls (64 ns sleeps) of a compaction tile waiting on an earlier one
 #define RD_MAX_WORK 4096      // max checkerboard cells per diode (64x64)
 
 enum { RD_G_PLANAR = 1, RD_G_TIP = 2 };

@@ -63,18 +63,20 @@ __device__ __forceinline__ void mark_remove(const DiodeParams& p, DiodeDyn& y, P
   else if (f == 3) atomicAdd(&y.n_remove_bot, 1);
 }
 
-__device__ __forceinline__ void pack_one(const DiodeParams& p, const Pool& pool, int gi) {
-  double x = pool.x[gi], y = pool.y[gi], z = pool.z[gi];
+// FP32 packs of particle gi from its position and charge (the caller's values
+// of pool.x/y/z/q at gi).
+__device__ __forceinline__ void pack_vals(const DiodeParams& p, const Pool& pool, int gi, double x, double y,
+                                          double z, double q) {
   float4 h, l;
   split_nm(x, p.org_x, &h.x, &l.x);
   split_nm(y, p.org_y, &h.y, &l.y);
   split_nm(z, 0.0, &h.z, &l.z);
-  h.w = (float)(pool.q[gi] * c_k.q0_inv);   // exact for charges that are multiples of q0
+  h.w = (float)(q * c_k.q0_inv);   // exact for charges that are multiples of q0
   l.w = (float)((p.d - z) * 1.0e9);
   pool.pk_hi[gi] = h;
   pool.pk_lo[gi] = l;
   if (p.geometry == RD_G_PLANAR) {
-    const float zf = (float)(z * 1.0e9), qf = h.w;
+    const float zf = h.z, qf = h.w;   // h.z is (float)(z 1e9): the split's origin is 0
     pool.zk_hi[gi] = make_float4(h.x, h.y, fmaxf(zf * zf, 1e-20f), qf * zf);
     pool.zk_lo[gi] = make_float4(l.x, l.y, zf, qf);
   }
@@ -90,6 +92,10 @@ __device__ __forceinline__ void pack_one(const DiodeParams& p, const Pool& pool,
     pool.ip_hi[gi] = a;
     pool.ip_lo[gi] = b;
   }
+}
+
+__device__ __forceinline__ void pack_one(const DiodeParams& p, const Pool& pool, int gi) {
+  pack_vals(p, pool, gi, pool.x[gi], pool.y[gi], pool.z[gi], pool.q[gi]);
 }
 
 // ---- planner --------------------------------------------------------------------
@@ -446,12 +452,31 @@ k_ramo(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, const PlanE
 }
 
 // ---- compaction ------------------------------------------------------------------------
+// Stable compaction in place over 256-particle units (four per 1024-particle
+// tile of the PM_PART1024 plan; unit u = 4 x item + quarter):
+//  * k_compact_count: survivors per unit (cnt[u]), and the units' load flags
+//    cleared.
+//  * k_compact_scan: per diode, the survivors of the diode's earlier units
+//    (pre[u], an exclusive scan in unit order): the unit's first destination.
+//  * k_compact_move: units taken in increasing order from a counter.  A unit
+//    loads its moving survivors (those behind the diode's first removed
+//    particle) into registers, records the life times of its removed
+//    electrons and raises its load flag; then it waits until every earlier
+//    unit whose particles its destinations overwrite has raised its flag,
+//    and stores.  Destinations never lie behind a survivor's own index, so
+//    only earlier units are overwritten; those were taken before this one and
+//    are running or done, and their loads do not wait, so every wait ends.
+//    Each wait is still bounded (RD_COMPACT_SPIN polls): a wait that gives up
+//    counts in cq[2] (rd_run reports it) and the unit stores nothing.
+// Each moved survivor is read once and written once (152 B of state each
+// way) and its FP32 packs are written from the loaded values.
 __global__ void __launch_bounds__(1024)
 k_compact_count(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
                 const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
-                int* __restrict__ kept) {
+                int* __restrict__ cnt, int* __restrict__ flag) {
   __shared__ int wsum[32];
   for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
+    if (threadIdx.x < 4) flag[4 * g + threadIdx.x] = 0;
     ItemRef it = decode_item(plan, ph->n_diodes, g);
     const DiodeParams& p = P[it.d];
     if (Dy[it.d].n_remove == 0) continue;   // block-uniform
@@ -461,87 +486,161 @@ k_compact_count(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ 
     int c = __popc(__ballot_sync(0xffffffffu, m));
     if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 4) {   // unit q: warps 8q .. 8q + 7
       int t = 0;
-      for (int q = 0; q < 32; ++q) t += wsum[q];
-      kept[g] = t;
+      for (int k = 0; k < 8; ++k) t += wsum[8 * threadIdx.x + k];
+      cnt[4 * g + threadIdx.x] = t;
     }
     __syncthreads();
   }
 }
 
-__device__ __forceinline__ void move_particle(const Pool& a, const Pool& b, int src, int dst) {
-  b.x[dst] = a.x[src]; b.y[dst] = a.y[src]; b.z[dst] = a.z[src];
-  b.vx[dst] = a.vx[src]; b.vy[dst] = a.vy[src]; b.vz[dst] = a.vz[src];
-  b.ax[dst] = a.ax[src]; b.ay[dst] = a.ay[src]; b.az[dst] = a.az[src];
-  b.bx[dst] = a.bx[src]; b.by[dst] = a.by[src]; b.bz[dst] = a.bz[src];
-  b.cx[dst] = a.cx[src]; b.cy[dst] = a.cy[src]; b.cz[dst] = a.cz[src];
-  b.q[dst] = a.q[src]; b.m[dst] = a.m[src];
-  b.species[dst] = a.species[src]; b.id[dst] = a.id[src];
-  b.step0[dst] = a.step0[src]; b.section[dst] = a.section[src];
+// One block per diode slot with removals: pre[u] = sum of cnt over the
+// diode's earlier units, in chunks of 1024 units with a carry.
+__global__ void __launch_bounds__(1024)
+k_compact_scan(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy,
+               const PlanEntry* __restrict__ plan, const int* __restrict__ cnt, int* __restrict__ pre) {
+  __shared__ int wsum[32];
+  const int d = blockIdx.x;
+  if (!P[d].active || Dy[d].n_remove == 0) return;
+  const int base = 4 * plan[d].item_off, units = 4 * plan[d].tiles;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int carry = 0;
+  for (int c0 = 0; c0 < units; c0 += 1024) {
+    const int u = c0 + threadIdx.x;
+    const int v = u < units ? cnt[base + u] : 0;
+    int x = v;   // inclusive scan in the warp
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      int t = wsum[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      wsum[lane] = t;   // inclusive over the warps
+    }
+    __syncthreads();
+    const int excl = carry + (w > 0 ? wsum[w - 1] : 0) + x - v;
+    if (u < units) pre[base + u] = excl;
+    carry += wsum[31];
+    __syncthreads();
+  }
 }
 
-__global__ void __launch_bounds__(1024)
-k_compact_scatter(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
-                  Pool tmp, const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
-                  const int* __restrict__ kept, int* __restrict__ life, const int* __restrict__ step_ptr) {
-  __shared__ int wsum[32];
-  for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
+struct MovedParticle {
+  double x, y, z, vx, vy, vz, ax, ay, az, bx, by, bz, cx, cy, cz, q, m;
+  int species, id, step0, section;
+};
+
+__device__ __forceinline__ void load_particle(const Pool& a, int i, MovedParticle& r) {
+  r.x = a.x[i]; r.y = a.y[i]; r.z = a.z[i];
+  r.vx = a.vx[i]; r.vy = a.vy[i]; r.vz = a.vz[i];
+  r.ax = a.ax[i]; r.ay = a.ay[i]; r.az = a.az[i];
+  r.bx = a.bx[i]; r.by = a.by[i]; r.bz = a.bz[i];
+  r.cx = a.cx[i]; r.cy = a.cy[i]; r.cz = a.cz[i];
+  r.q = a.q[i]; r.m = a.m[i];
+  r.species = a.species[i]; r.id = a.id[i]; r.step0 = a.step0[i]; r.section = a.section[i];
+}
+
+__device__ __forceinline__ void store_particle(const Pool& b, int i, const MovedParticle& r) {
+  b.x[i] = r.x; b.y[i] = r.y; b.z[i] = r.z;
+  b.vx[i] = r.vx; b.vy[i] = r.vy; b.vz[i] = r.vz;
+  b.ax[i] = r.ax; b.ay[i] = r.ay; b.az[i] = r.az;
+  b.bx[i] = r.bx; b.by[i] = r.by; b.bz[i] = r.bz;
+  b.cx[i] = r.cx; b.cy[i] = r.cy; b.cz[i] = r.cz;
+  b.q[i] = r.q; b.m[i] = r.m;
+  b.species[i] = r.species; b.id[i] = r.id; b.step0[i] = r.step0; b.section[i] = r.section;
+}
+
+__global__ void __launch_bounds__(256, 4)
+k_compact_move(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
+               const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
+               const int* __restrict__ cnt, const int* __restrict__ pre, int* __restrict__ flag,
+               int* __restrict__ cq, int* __restrict__ life, const int* __restrict__ step_ptr) {
+  __shared__ int wsum[8], s_unit, s_ok;
+  const int total = 4 * ph->total_items, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_unit = atomicAdd(&cq[0], 1);   // units in increasing order
+    __syncthreads();
+    const int u = s_unit;
+    if (u >= total) break;
+    const int g = u >> 2;
     ItemRef it = decode_item(plan, ph->n_diodes, g);
     const DiodeParams& p = P[it.d];
     const DiodeDyn& y = Dy[it.d];
-    if (y.n_remove == 0) continue;
-    const int step = *step_ptr - y.step_offset;
-    const int n = plan[it.d].n_i;
-    const int b = it.tile, i0 = it.i0;
-    if (i0 + 1024 <= y.first_dead) continue;   // nothing moves in this block
-    const bool record = (n - y.n_remove) > 0;  // the reference skips the all-removed case
-    int before = 0;
-    const int tb0 = plan[it.d].item_off;
-    for (int q = 0; q < b; ++q) before += kept[tb0 + q];
-    const int i = i0 + threadIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int m = (i < n) ? pool.mask[p.off + i] : 0;
-    unsigned bal = __ballot_sync(0xffffffffu, m);
+    const int n = plan[it.d].n_i, i0 = it.i0 + 256 * (u & 3), tb0 = plan[it.d].item_off;
+    const int fd = y.first_dead;
+    if (y.n_remove == 0 || i0 >= n || i0 + 256 <= fd) {   // nothing of this unit moves or is overwritten
+      if (threadIdx.x == 0) atomicExch(&flag[u], 1);
+      continue;
+    }
+    const int before = pre[u];
+    const int i = i0 + threadIdx.x;
+    const int m = (i < n) ? pool.mask[p.off + i] : 0;
+    const unsigned bal = __ballot_sync(0xffffffffu, m);
     if (lane == 0) wsum[w] = __popc(bal);
     __syncthreads();
-    int pre = 0;
-    for (int q = 0; q < w; ++q) pre += wsum[q];
-    pre += __popc(bal & ((1u << lane) - 1));
+    int pos = 0;
+    for (int q = 0; q < w; ++q) pos += wsum[q];
+    pos += __popc(bal & ((1u << lane) - 1));
+    const bool moves = i < n && i >= fd && m;
+    MovedParticle r;
+    if (moves) load_particle(pool, p.off + i, r);
     int bin = -1;   // life-time bin of a removed electron (record_lifetime :1135-1160)
-    if (i < n && i >= y.first_dead) {
-      if (m) {
-        move_particle(pool, tmp, p.off + i, p.off + before + pre);
-      } else if (record) {
-        int lt = step - pool.step0[p.off + i];
-        if (lt <= 0) lt = 1;
-        if (lt > RD_MAX_LIFE) lt = RD_MAX_LIFE;
-        if (pool.species[p.off + i] == 1) bin = lt - 1;
-      }
+    if (i < n && i >= fd && !m && (n - y.n_remove) > 0) {   // the reference skips the all-removed case
+      int lt = (*step_ptr - y.step_offset) - pool.step0[p.off + i];
+      if (lt <= 0) lt = 1;
+      if (lt > RD_MAX_LIFE) lt = RD_MAX_LIFE;
+      if (pool.species[p.off + i] == 1) bin = lt - 1;
     }
     // one atomic per distinct bin of the warp: electrons removed together mostly share one
     const unsigned peers = __match_any_sync(0xffffffffu, bin);
     if (bin >= 0 && lane == __ffs(peers) - 1)
       atomicAdd(&life[(size_t)it.d * RD_MAX_LIFE + bin], __popc(peers));
+    if (i < n) pool.mask[p.off + i] = 1;
+    __threadfence();   // this thread's loads are complete before the flag is raised
     __syncthreads();
+    if (threadIdx.x == 0) atomicExch(&flag[u], 1);
+    // earlier units holding positions of [before, before + cnt): the destinations
+    // (each below its survivor's own index, so in this unit or an earlier one)
+    const int ku = cnt[u], own = (u - 4 * tb0);
+    const int t_lo = before >> 8, t_hi = ku > 0 ? min(own - 1, (before + ku - 1) >> 8) : -1;
+    if (w == 0) {
+      int ok = 1;
+      for (int t = t_lo + lane; t <= t_hi; t += 32) {
+        const volatile int* f = flag + 4 * tb0 + t;
+        int spins = 0;
+        while (*f == 0 && spins < RD_COMPACT_SPIN) { __nanosleep(64); ++spins; }
+        if (*f == 0) ok = 0;
+      }
+      ok = __all_sync(0xffffffffu, ok);
+      if (lane == 0) {
+        if (!ok) atomicAdd(&cq[2], 1);
+        s_ok = ok;
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (!s_ok) continue;
+    if (moves) {
+      const int dst = p.off + before + pos;
+      store_particle(pool, dst, r);
+      pack_vals(p, pool, dst, r.x, r.y, r.z, r.q);
+    }
   }
-}
-
-__global__ void __launch_bounds__(1024)
-k_compact_copy(const DiodeParams* __restrict__ P, const DiodeDyn* __restrict__ Dy, Pool pool,
-               Pool tmp, const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph) {
-  for (int g = blockIdx.x; g < ph->total_items; g += gridDim.x) {
-    ItemRef it = decode_item(plan, ph->n_diodes, g);
-    const DiodeParams& p = P[it.d];
-    const DiodeDyn& y = Dy[it.d];
-    if (y.n_remove == 0) continue;
-    const int n = plan[it.d].n_i, n_new = n - y.n_remove;
-    const int i = it.i0 + threadIdx.x;
-    if (i >= n) continue;
-    const int gi = p.off + i;
-    pool.mask[gi] = 1;
-    if (i >= y.first_dead && i < n_new) {
-      move_particle(tmp, pool, gi, gi);
-      pack_one(p, pool, gi);
+  // the last block to leave resets the unit counter for the next launch
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&cq[1], 1) == (int)gridDim.x - 1) {
+      cq[0] = 0;
+      cq[1] = 0;
+      __threadfence();
     }
   }
 }
@@ -599,12 +698,12 @@ cudaError_t rd_launch_velocity(int grid, int nslots, cudaStream_t st, const Diod
   return cudaGetLastError();
 }
 cudaError_t rd_launch_compact(int grid, int nslots, cudaStream_t st, const DiodeParams* P,
-                              DiodeDyn* Dy, const Pool& pool, const Pool& tmp,
-                              const PlanEntry* plan, const PlanHeader* ph, int* kept, int* life,
-                              const int* step_ptr) {
-  k_compact_count<<<rd_grid(k_compact_count, 1024, grid), 1024, 0, st>>>(P, Dy, pool, plan, ph, kept);
-  k_compact_scatter<<<rd_grid(k_compact_scatter, 1024, grid), 1024, 0, st>>>(P, Dy, pool, tmp, plan, ph, kept, life, step_ptr);
-  k_compact_copy<<<rd_grid(k_compact_copy, 1024, grid), 1024, 0, st>>>(P, Dy, pool, tmp, plan, ph);
+                              DiodeDyn* Dy, const Pool& pool, const PlanEntry* plan, const PlanHeader* ph,
+                              int* cnt, int* pre, int* flag, int* cq, int* life, const int* step_ptr) {
+  k_compact_count<<<rd_grid(k_compact_count, 1024, grid), 1024, 0, st>>>(P, Dy, pool, plan, ph, cnt, flag);
+  if (nslots > 0) k_compact_scan<<<nslots, 1024, 0, st>>>(P, Dy, plan, cnt, pre);
+  k_compact_move<<<rd_grid(k_compact_move, 256, grid), 256, 0, st>>>(P, Dy, pool, plan, ph, cnt, pre, flag, cq,
+                                                                     life, step_ptr);
   k_compact_finish<<<(nslots + 127) / 128, 128, 0, st>>>(P, Dy, nslots);
   return cudaGetLastError();
 }

@@ -183,6 +183,53 @@ def test_removal_compaction_gpu(rg, orc):
     eng.close()
 
 
+def test_inplace_compaction_many_tiles(rg):
+    """The in-place compaction over many 1024-particle tiles: a diode losing three
+    in four (survivors written over many earlier tiles, whose loads each tile waits
+    for), one with 1 % scattered removals (Util/bench_compact.f90's scenario), one
+    with none and one losing all, compacted twice in a row (the tile counter and the
+    load flags reset between launches).  Survivors keep creation order with their
+    state, as compact_array does (src/mod_pair.F90:1180-1223)."""
+    eng = rg.Engine(precision=rg.PREC_FP64, max_diodes=4, particle_capacity=100000)
+    rng = np.random.default_rng(31)
+    sizes = [24000, 30000, 5000, 6000]
+    dios, data, alive = [], [], []
+    for n in sizes:
+        d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, capacity=n, image_charge=False)
+        R = np.column_stack([rng.uniform(-500, 500, n), rng.uniform(-500, 500, n), rng.uniform(1, 999, n)]) * NM
+        V = rng.normal(0.0, 1.0e5, (n, 3))
+        d.add_particles(R, V, species=np.where(np.arange(n) % 5 == 2, 2, 1), step=1)
+        dios.append(d)
+        data.append((R, V))
+        alive.append(np.arange(n))
+    for rnd in range(2):
+        dead = [alive[0][(np.arange(len(alive[0])) % 4) != 0],
+                np.sort(rng.choice(alive[1], len(alive[1]) // 100, replace=False)),
+                np.array([], dtype=int),
+                alive[3] if rnd == 0 else np.array([], dtype=int)]
+        for d, k, dd in zip(dios, alive, dead):
+            pos_of = {int(v): j for j, v in enumerate(k)}
+            for i in dd:
+                d.mark_particles_remove(pos_of[int(i)], rg.REMOVE_TOP)
+        eng.remove_particles(5 + rnd)
+        alive = [np.setdiff1d(k, dd) for k, dd in zip(alive, dead)]
+        for d, k, (R, V) in zip(dios, alive, data):
+            assert d.n == len(k)
+            p = d.particles()
+            np.testing.assert_array_equal(p["id"][:len(k)], k)
+            np.testing.assert_array_equal(p["pos"][:len(k)], R[k])
+            np.testing.assert_array_equal(p["vel"][:len(k)], V[k])
+        assert sum(eng.validate().values()) == 0
+    for d, n, k in zip(dios, sizes, alive):
+        removed = np.setdiff1d(np.arange(n), k)
+        n_elec = int(np.sum((removed % 5) != 2))
+        # the reference records no life times when a diode loses every particle
+        expect = 0 if d is dios[3] else n_elec
+        assert int(d.life_time().sum()) == expect
+        assert d.counters()["absorbed_top_total"] == n_elec
+    eng.close()
+
+
 def _emission_pair(rg, orc, prec, seed=77, n0=150, work=2.0, jumps=40, chains=300):
     rng = np.random.default_rng(seed)
     d, V = 500 * NM, 1.0e3
