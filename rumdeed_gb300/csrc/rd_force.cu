@@ -24,68 +24,63 @@
 namespace {
 
 // ---- planar, FP32 compensated, one image partner (N_ic_max = 0) -----------------
-// Two i-particles per thread (64 threads per 128-particle tile), in the .x and
-// .y lanes of packed FP32x2 arithmetic, so one shared-memory load of a
-// j-particle feeds both pairs and each step for the two pairs is one packed
-// instruction (rsqrt stays per lane).  The j data sit in shared memory
-// duplicated and negated: s0 = (-x_hi, -x_hi, -x_lo, -x_lo), s1 and s2 the same
-// for y and z, sq the charges.  Per pair: the Coulomb term and the n = 0 image
-// partner at -z_j, whose height difference is z_i + z_j = 2 z_i - dz (2 z_i as
-// one float: relative error 6e-8); the image height is formed negated
-// (dz - 2 z_i), which rounds to exactly the negation.  The 1e-20 nm^2 floor
-// inside dxy^2 keeps the self pair and coincident pairs finite (their q or d
-// is zero).  Each lane does the operations of the scalar pair in the same
-// order: differences and sums as there, a - b as a + (-b) or fma(b, -1, a).
+// Two i-particles per thread (64 threads per 128-particle tile), so one
+// shared-memory load of a j-particle feeds two pairs.  Per pair: the Coulomb
+// term and the n = 0 image partner at -z_j, whose height difference is
+// z_i + z_j = 2 z_i - dz (2 z_i as one float: relative error 6e-8).  The
+// 1e-20 nm^2 floor inside dxy^2 keeps the self pair and coincident pairs
+// finite (their q or d is zero).
 // ELEC (off-diagonal tiles whose charges are all -1, the electrons' q/q0):
 // the charge multiplies are dropped and the sign folded into the sums.
-// DIAG: the diagonal tile, where a particle's own term has q = 0.
 template <bool IC, bool DIAG, bool ELEC = false>
-__device__ __forceinline__ void planar_tile2_nic0(const float4* __restrict__ s0, const float4* __restrict__ s1,
-                                                  const float4* __restrict__ s2, const float* __restrict__ sq,
-                                                  int kmax, const float2 (&H)[3], const float2 (&L)[3],
-                                                  float2 ntz, int self_a, int self_b, float2 (&t)[3]) {
-  const float2 eps = make_float2(1e-20f, 1e-20f), neg1 = make_float2(-1.f, -1.f);
-  float2 ax = make_float2(0.f, 0.f), ay = ax, az = ax;
+__device__ __forceinline__ void planar_tile2_nic0(const float4* __restrict__ sh, const float4* __restrict__ sl,
+                                                  int kmax, float4 ah, float4 al, float atz, float4 bh,
+                                                  float4 bl, float btz, int self_a, int self_b,
+                                                  float3& ta, float3& tb) {
+  float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
 #pragma unroll 2
   for (int k = 0; k < kmax; ++k) {
-    const float4 a = s0[k], b = s1[k], c = s2[k];
-    float2 q2 = make_float2(1.f, 1.f);
-    if (!ELEC) {
-      const float q = sq[k];
-      q2 = make_float2((DIAG && k == self_a) ? 0.f : q, (DIAG && k == self_b) ? 0.f : q);
+    const float4 h = sh[k], l = sl[k];
+    const float qa = ELEC ? 1.f : ((DIAG && k == self_a) ? 0.f : h.w);
+    const float qb = ELEC ? 1.f : ((DIAG && k == self_b) ? 0.f : h.w);
+    {
+      const float dx = (ah.x - h.x) + (al.x - l.x), dy = (ah.y - h.y) + (al.y - l.y);
+      const float dz = (ah.z - h.z) + (al.z - l.z);
+      const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, 1e-20f));
+      const float inv = rsqrtf(fmaf(dz, dz, dxy2));
+      const float s = qa * ((inv * inv) * inv);
+      if (IC) {
+        const float zs = atz - dz;
+        const float ri = rsqrtf(fmaf(zs, zs, dxy2));
+        const float si = qa * ((ri * ri) * ri);
+        const float t = s - si;
+        ax = fmaf(t, dx, ax); ay = fmaf(t, dy, ay);
+        az = fmaf(s, dz, fmaf(-si, zs, az));
+      } else {
+        ax = fmaf(s, dx, ax); ay = fmaf(s, dy, ay); az = fmaf(s, dz, az);
+      }
     }
-    const float2 dx = __fadd2_rn(__fadd2_rn(H[0], make_float2(a.x, a.y)), __fadd2_rn(L[0], make_float2(a.z, a.w)));
-    const float2 dy = __fadd2_rn(__fadd2_rn(H[1], make_float2(b.x, b.y)), __fadd2_rn(L[1], make_float2(b.z, b.w)));
-    const float2 dz = __fadd2_rn(__fadd2_rn(H[2], make_float2(c.x, c.y)), __fadd2_rn(L[2], make_float2(c.z, c.w)));
-    const float2 dxy2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, eps));
-    const float2 r2 = __ffma2_rn(dz, dz, dxy2);
-    float2 inv;
-    inv.x = rsqrtf(r2.x);
-    inv.y = rsqrtf(r2.y);
-    float2 s = __fmul2_rn(__fmul2_rn(inv, inv), inv);
-    if (!ELEC) s = __fmul2_rn(q2, s);
-    if (IC) {
-      const float2 zsn = __fadd2_rn(dz, ntz);   // -(z_i + z_j) = -(2 z_i - dz)
-      const float2 e2 = __ffma2_rn(zsn, zsn, dxy2);
-      float2 ri;
-      ri.x = rsqrtf(e2.x);
-      ri.y = rsqrtf(e2.y);
-      float2 si = __fmul2_rn(__fmul2_rn(ri, ri), ri);
-      if (!ELEC) si = __fmul2_rn(q2, si);
-      const float2 tt = __ffma2_rn(si, neg1, s);   // s - si
-      ax = __ffma2_rn(tt, dx, ax);
-      ay = __ffma2_rn(tt, dy, ay);
-      az = __ffma2_rn(s, dz, __ffma2_rn(si, zsn, az));
-    } else {
-      ax = __ffma2_rn(s, dx, ax);
-      ay = __ffma2_rn(s, dy, ay);
-      az = __ffma2_rn(s, dz, az);
+    {
+      const float dx = (bh.x - h.x) + (bl.x - l.x), dy = (bh.y - h.y) + (bl.y - l.y);
+      const float dz = (bh.z - h.z) + (bl.z - l.z);
+      const float dxy2 = fmaf(dx, dx, fmaf(dy, dy, 1e-20f));
+      const float inv = rsqrtf(fmaf(dz, dz, dxy2));
+      const float s = qb * ((inv * inv) * inv);
+      if (IC) {
+        const float zs = btz - dz;
+        const float ri = rsqrtf(fmaf(zs, zs, dxy2));
+        const float si = qb * ((ri * ri) * ri);
+        const float t = s - si;
+        bx = fmaf(t, dx, bx); by = fmaf(t, dy, by);
+        bz = fmaf(s, dz, fmaf(-si, zs, bz));
+      } else {
+        bx = fmaf(s, dx, bx); by = fmaf(s, dy, by); bz = fmaf(s, dz, bz);
+      }
     }
   }
-  if (ELEC) {
-    ax = __fmul2_rn(ax, neg1); ay = __fmul2_rn(ay, neg1); az = __fmul2_rn(az, neg1);
-  }
-  t[0] = ax; t[1] = ay; t[2] = az;
+  if (ELEC) { ax = -ax; ay = -ay; az = -az; bx = -bx; by = -by; bz = -bz; }
+  ta.x += ax; ta.y += ay; ta.z += az;
+  tb.x += bx; tb.y += by; tb.z += bz;
 }
 
 __global__ void __launch_bounds__(64)
@@ -93,8 +88,7 @@ k_force_planar_f32_nic0(const DiodeParams* __restrict__ P, Pool pool,
                         const PlanEntry* __restrict__ plan, const PlanHeader* __restrict__ ph,
                         double* __restrict__ partial, int* __restrict__ tickets, double kscale, int* __restrict__ queue) {
   __shared__ int s_item;
-  __shared__ float4 sx2[3][RD_TILE];   // (-x_hi, -x_hi, -x_lo, -x_lo), the same for y and z
-  __shared__ float sq[RD_TILE];
+  __shared__ float4 sh[RD_TILE], sl[RD_TILE];
   const int total = ph->total_items, nd = ph->n_diodes;
   const int tid = threadIdx.x, nt = 64;
   for (int g = queue_first(0, total); g < total; g = queue_next(queue, &s_item, 0, total)) {
@@ -105,9 +99,7 @@ k_force_planar_f32_nic0(const DiodeParams* __restrict__ P, Pool pool,
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 ah = ia < n ? pool.pk_hi[off + ia] : z4, al = ia < n ? pool.pk_lo[off + ia] : z4;
     const float4 bh = ib < n ? pool.pk_hi[off + ib] : z4, bl = ib < n ? pool.pk_lo[off + ib] : z4;
-    const float2 H[3] = {make_float2(ah.x, bh.x), make_float2(ah.y, bh.y), make_float2(ah.z, bh.z)};
-    const float2 L[3] = {make_float2(al.x, bl.x), make_float2(al.y, bl.y), make_float2(al.z, bl.z)};
-    const float2 ntz = make_float2(-(2.f * (ah.z + al.z)), -(2.f * (bh.z + bl.z)));
+    const float atz = 2.f * (ah.z + al.z), btz = 2.f * (bh.z + bl.z);
     const bool ic = p.image_charge != 0;
     F32Acc A, B;
     A.zero(); B.zero();
@@ -117,28 +109,25 @@ k_force_planar_f32_nic0(const DiodeParams* __restrict__ P, Pool pool,
       for (int q = tid; q < RD_TILE; q += nt) {
         const int j = jt + q;
         if (j < it.j1) {
-          const float4 h = pool.pk_hi[off + j], l = pool.pk_lo[off + j];
-          sx2[0][q] = make_float4(-h.x, -h.x, -l.x, -l.x);
-          sx2[1][q] = make_float4(-h.y, -h.y, -l.y, -l.y);
-          sx2[2][q] = make_float4(-h.z, -h.z, -l.z, -l.z);
-          sq[q] = h.w;
-          elec &= (h.w == -1.0f);
+          const float4 hj = pool.pk_hi[off + j];
+          sh[q] = hj; sl[q] = pool.pk_lo[off + j];
+          elec &= (hj.w == -1.0f);
         }
       }
       elec = __syncthreads_and(elec);
       const int kmax = min(RD_TILE, it.j1 - jt);
-      float2 t[3];
+      float3 ta = make_float3(0.f, 0.f, 0.f), tb = ta;
       const bool diag = (jt == it.i0);
       if (ic) {
-        if (diag) planar_tile2_nic0<true, true>(sx2[0], sx2[1], sx2[2], sq, kmax, H, L, ntz, tid, nt + tid, t);
-        else if (elec) planar_tile2_nic0<true, false, true>(sx2[0], sx2[1], sx2[2], sq, kmax, H, L, ntz, -1, -1, t);
-        else planar_tile2_nic0<true, false>(sx2[0], sx2[1], sx2[2], sq, kmax, H, L, ntz, -1, -1, t);
+        if (diag) planar_tile2_nic0<true, true>(sh, sl, kmax, ah, al, atz, bh, bl, btz, tid, nt + tid, ta, tb);
+        else if (elec) planar_tile2_nic0<true, false, true>(sh, sl, kmax, ah, al, atz, bh, bl, btz, -1, -1, ta, tb);
+        else planar_tile2_nic0<true, false>(sh, sl, kmax, ah, al, atz, bh, bl, btz, -1, -1, ta, tb);
       } else {
-        if (diag) planar_tile2_nic0<false, true>(sx2[0], sx2[1], sx2[2], sq, kmax, H, L, ntz, tid, nt + tid, t);
-        else planar_tile2_nic0<false, false>(sx2[0], sx2[1], sx2[2], sq, kmax, H, L, ntz, -1, -1, t);
+        if (diag) planar_tile2_nic0<false, true>(sh, sl, kmax, ah, al, atz, bh, bl, btz, tid, nt + tid, ta, tb);
+        else planar_tile2_nic0<false, false>(sh, sl, kmax, ah, al, atz, bh, bl, btz, -1, -1, ta, tb);
       }
-      A.add(t[0].x, t[1].x, t[2].x);
-      B.add(t[0].y, t[1].y, t[2].y);
+      A.add(ta.x, ta.y, ta.z);
+      B.add(tb.x, tb.y, tb.z);
     }
     double f[2][3] = {{(double)A.hx + (double)A.lx, (double)A.hy + (double)A.ly, (double)A.hz + (double)A.lz},
                       {(double)B.hx + (double)B.lx, (double)B.hy + (double)B.ly, (double)B.hz + (double)B.lz}};
