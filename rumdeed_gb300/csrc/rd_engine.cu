@@ -535,7 +535,7 @@ static int launch_emission(rd_engine* e) {
   CK(plan(e, PM_MH));
   if (s.emit_planar) {   // diodes with no particle in flight: all their MH sampling in one launch
     CK(rd_launch_mh_vacuum(prec, ns, e->st, e->dP, e->dD, e->cs, e->d_choff, e->wtab, e->d_step, e->kscale));
-    e->kernels_in_step++;
+    e->kernels_in_step += 2;   // uniform work functions, and the others
   }
   int rc = launch_mh_tiled_if(e, s);
   if (rc) return rc;

@@ -20,6 +20,7 @@
 //    streams keyed by the diode seed with counters (chain, iteration, step,
 //    purpose), so every chain is reproducible and independent of scheduling.
 #include <cooperative_groups.h>
+#include <type_traits>
 
 #include "rd_tiles.cuh"
 
@@ -51,7 +52,7 @@ __global__ void __launch_bounds__(RD_ITILE)
 k_field_points(const DiodeParams* __restrict__ P, Pool pool, const PlanEntry* __restrict__ plan,
                const PlanHeader* __restrict__ ph, PointSet pts, double* __restrict__ partial,
                int* __restrict__ tickets, double kscale) {
-  __shared__ float4 sh[RD_TILE], sl[RD_TILE], sih[RD_TILE], sil[RD_TILE];
+  __shared__ float4 sh[RD_TILE], sl[RD_TILE], sih[RD_TILE];
   __shared__ rd_d4 sj[RD_TILE];
   const int total = ph->total_items, nd = ph->n_diodes, tid = threadIdx.x;
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
@@ -1231,7 +1232,8 @@ __device__ __noinline__ bool mh_decide_vac(const DiodeParams& p, const double* _
 // k_mh_jump_planar + k_mh_init.  One field everywhere makes the FP64 targets of
 // two points of one work-function cell equal, so such a proposal is taken
 // (s_n >= s_c) without a draw, as the FP64 form takes it; a uniform work
-// function makes every jump such.  After each jump the CTAs reduce their
+// function makes every jump such, and k_mh_vacuum_uniform samples those
+// diodes instead (this kernel leaves them).  After each jump the CTAs reduce their
 // acceptance counts, exchange them through distributed shared memory across a
 // cluster barrier and each apply the same MH_std update (MH_std_update
 // :603-612); jumps alternate between two count buffers, so a CTA never
@@ -1281,6 +1283,7 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
       for (int e = 0; e < 3; ++e)
         differs |= __double_as_longlong(swt[3 * k + e]) != __double_as_longlong(swt[e]);
   const bool uniform = __syncthreads_or(differs) == 0 && wsh && cells >= 1 && sp.mh_jumps <= RD_VAC_MAXJ;
+  if (uniform) return;   // k_mh_vacuum_uniform samples it (the test is uniform over the cluster)
   if (wsh && tid == 0) sp.work_off = 0;   // entries now at swt[3 * cell]
   __syncthreads();
   if (wsh) wtab = swt;
@@ -1338,60 +1341,7 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
     if (!ok[q]) failed++;
   }
   if (failed) atomicAdd(&y.chains_failed, failed);
-  if (uniform) {
-    // One field and one target everywhere: every proposal of a started chain is
-    // taken (s_n >= s_c), so each jump's counts are (T, 0) for the T = M chains
-    // that started (none when the field is not favourable) and the MH_std
-    // schedule is known before the first jump.  Thread 0 forms it with
-    // mh_std_gain / mh_std_clamp, as mh_std_step does jump by jump; the chains
-    // then walk without a barrier.
-    __shared__ double s_seq[RD_VAC_MAXJ + 1];   // the step-size factor of each jump
-    __shared__ float s_seqf[RD_VAC_MAXJ + 1];   // the same for the FP32 chains
-    __shared__ double s_end[2];
-    if (tid == 0) {
-      const int T = start_ok ? M : 0;
-      double m = mhs, ar = arate, rate = 0.0, g = 0.0;
-      if (T > 0) g = mh_std_gain(T, 0, &rate);
-      for (int it = 1; it <= p.mh_jumps; ++it) {
-        s_seq[it] = (it > ndim_first) ? m : 0.10;
-        s_seqf[it] = (it > ndim_first) ? (float)m : 0.10f;
-        if (it > ndim_first && T > 0) { ar = rate; m = mh_std_clamp(p, m * g); }
-      }
-      s_end[0] = m; s_end[1] = ar;
-    }
-    __syncthreads();
-    for (int it = 1; it <= p.mh_jumps; ++it) {
-      if constexpr (PREC == 1) {
-        const float mf = s_seqf[it];
-        const float sx = p.em_wx * mf, sy = p.em_wy * mf;
-        const float hx = p.em_hx, hy = p.em_hy;
-#pragma unroll
-        for (int q = 0; q < RD_VAC_CPT; ++q) {
-          if (!ok[q]) continue;
-          float x = fmaf(fgx[q], sx, fx[q]);
-          float yv = fmaf(fgy[q], sy, fy[q]);
-          if (x > hx) x = hx - (x - hx); else if (x < -hx) x = -hx - (x + hx);
-          if (yv > hy) yv = hy - (yv - hy); else if (yv < -hy) yv = -hy - (yv + hy);
-          fx[q] = x; fy[q] = yv;
-          if (it < p.mh_jumps) gauss2f(p.seed, (uint32_t)(g0 + q * G), (uint32_t)(it + 1), step, &fgx[q], &fgy[q]);
-        }
-      } else {
-        const double sx = p.em_Lx * s_seq[it], sy = p.em_Ly * s_seq[it];
-        const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
-#pragma unroll
-        for (int q = 0; q < RD_VAC_CPT; ++q) {
-          if (!ok[q]) continue;
-          double x = dgx[q] * sx + dx[q], yv = dgy[q] * sy + dy[q];
-          if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
-          if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
-          dx[q] = x; dy[q] = yv;
-          if (it < p.mh_jumps) gauss2(p.seed, (uint32_t)(g0 + q * G), (uint32_t)(it + 1), step, &dgx[q], &dgy[q]);
-        }
-      }
-    }
-    mhs = s_end[0]; arate = s_end[1];
-  }
-  for (int it = 1; !uniform && it <= p.mh_jumps; ++it) {
+  for (int it = 1; it <= p.mh_jumps; ++it) {
     unsigned cnt = 0;   // (rejected << 16) | accepted over this thread's chains
     if constexpr (PREC == 1) {
       const float mf = mhf;
@@ -1489,6 +1439,182 @@ k_mh_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainS
   }
   if (rank == 0 && tid == 0) { y.MH_std = mhs; y.a_rate = arate; }
   cl.sync();   // no CTA leaves while another may still read its counts
+}
+
+// The batched MH sampling of a vacuum-field diode (rd_mh_vacuum) whose work
+// function is uniform (every cell's supply-target entry the same, bit for bit).
+// One field and one target everywhere: every proposal of a started chain is
+// taken (s_n >= s_c), so each jump's counts are (T, 0) for the T = M chains
+// that started (none when the field is not favourable) and the MH_std schedule
+// is known before the first jump.  A chain's walk then needs only its Gaussian
+// pairs, whose Philox counters (chain, jump, step) make them independent: the
+// RD_VU_THREADS threads of a block draw them for its RD_VU_CHAINS chains, a
+// chunk of RD_VU_JCHUNK jumps at a time, into shared memory, and each chain
+// walks the chunk in one lane of warp 1.  Thread 0 forms the schedule with
+// mh_std_gain / mh_std_clamp meanwhile, as mh_std_step does jump by jump; once
+// the clamped step size stops changing, every later jump takes it.  Blocks
+// (x: group of chains, y: diode slot) spread a diode's chains over the GPU.
+// The start, the draws and the step arithmetic are those of k_mh_vacuum (and
+// of mh_propose_* / mh_start_* on the tiled path), in the same order, so the
+// chains end bit for bit as there.  The last block of a diode to finish writes
+// MH_std and a_rate (a ticket on mh_done, which is 0 between jumps), after
+// every block has read the old values.
+template <int PREC>
+__global__ void __launch_bounds__(RD_VU_THREADS)
+k_mh_vacuum_uniform(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, ChainState cs,
+                    const int* __restrict__ ch_off, const double* __restrict__ wtab,
+                    const int* __restrict__ step_ptr, double kscale) {
+  using Real = typename std::conditional<PREC == 1, float, double>::type;
+  __shared__ DiodeParams sp;
+  __shared__ double s_seq[RD_VAC_MAXJ + 1];   // the step-size factor of each jump
+  __shared__ float s_seqf[RD_VAC_MAXJ + 1];   // the same for the FP32 chains
+  __shared__ double s_end[2];
+  __shared__ Real s_g[RD_VU_JCHUNK][RD_VU_CHAINS][2];   // Gaussian pairs of a chunk of jumps
+  __shared__ int s_last;
+  const int d = blockIdx.y, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  DiodeDyn& y = Dy[d];
+  if (!P[d].active || !rd_mh_vacuum(P[d], y) || y.chains <= 0) return;
+  const int M = y.chains, c0 = blockIdx.x * RD_VU_CHAINS;
+  if (c0 >= M) return;
+  {
+    const int* src = reinterpret_cast<const int*>(P + d);
+    int* dst = reinterpret_cast<int*>(&sp);
+    for (int k = tid; k < (int)(sizeof(DiodeParams) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+  }
+  __syncthreads();
+  const DiodeParams& p = sp;
+  // the test of k_mh_vacuum: every entry of the diode's table equal to the first
+  const int cells = p.work_model == 1 ? p.work_nx * p.work_ny : (p.work_model == 4 ? p.work_nx : 0);
+  const bool wsh = cells <= RD_VAC_WTAB;
+  int differs = 0;
+  if (wsh)
+    for (int k = tid; k < cells; k += blockDim.x)
+      for (int e = 0; e < 3; ++e)
+        differs |= __double_as_longlong(wtab[3 * (p.work_off + k) + e]) !=
+                   __double_as_longlong(wtab[3 * p.work_off + e]);
+  if (!(__syncthreads_or(differs) == 0 && wsh && cells >= 1 && p.mh_jumps <= RD_VAC_MAXJ)) return;
+  const int J = p.mh_jumps, base = ch_off[d];
+  const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
+  const double F = z0_finish<PREC>(p, 0.0, kscale);
+  const float Ff = (float)F;
+  const bool start_ok = F < 0.0 && p.init_rounds > 0;
+  const int ndim_first = (J + 2) / 4;
+  const int nc = min(RD_VU_CHAINS, M - c0);   // chains of this block
+  if (tid == 0) {   // the schedule
+    const int T = start_ok ? M : 0;
+    double m = y.MH_std, ar = y.a_rate, rate = 0.0, g = 0.0;
+    if (T > 0) g = mh_std_gain(T, 0, &rate);
+    for (int it = 1; it <= J; ++it) {
+      if (it > ndim_first && T > 0) {
+        s_seq[it] = m; s_seqf[it] = (float)m;
+        ar = rate;
+        const double nx = mh_std_clamp(p, m * g);
+        if (nx == m) {   // a fixed point: every later jump takes the same step size
+          const float mf = (float)m;
+          for (int k = it + 1; k <= J; ++k) { s_seq[k] = m; s_seqf[k] = mf; }
+          break;
+        }
+        m = nx;
+      } else {
+        s_seq[it] = (it > ndim_first) ? m : 0.10;
+        s_seqf[it] = (it > ndim_first) ? (float)m : 0.10f;
+      }
+    }
+    s_end[0] = m; s_end[1] = ar;
+  }
+  // the start (round 0) of the block's chains, one per lane of warp 1
+  const int c = c0 + lane;
+  const bool mine = w == 1 && lane < nc;
+  Real px = 0, py = 0, gx = 0, gy = 0;
+  float rc = 0.0f;
+  double dsup = 0.0;
+  if (mine && start_ok) {
+    if constexpr (PREC == 1) {   // mh_propose_f32 (init) + mh_start_f32
+      float u1, u2;
+      rng2f(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+      px = fminf(fmaf(u1, p.em_wx, -p.em_hx), p.em_hx);
+      py = fminf(fmaf(u2, p.em_wy, -p.em_hy), p.em_hy);
+      rc = rho_xy_f(p, wtab, px, py, Ff);
+    } else {                     // mh_propose_f64 (init) + mh_start_f64
+      double u1, u2;
+      rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+      px = u1 * p.em_Lx + p.em_x0;
+      py = u2 * p.em_Ly + p.em_y0;
+      dsup = supply_log_xy(p, wtab, px, py, F);
+    }
+    if (J == 0) {   // the start's draw is the chain's last
+      if constexpr (PREC == 1) gauss2f(p.seed, (uint32_t)c, 1u, step, &gx, &gy);
+      else gauss2(p.seed, (uint32_t)c, 1u, step, &gx, &gy);
+    }
+  }
+  if (start_ok) {
+    for (int j0 = 1; j0 <= J; j0 += RD_VU_JCHUNK) {
+      const int nj = min(RD_VU_JCHUNK, J - j0 + 1);
+      __syncthreads();   // the previous chunk's walk is done with s_g
+      // the Gaussian pair of jump it is the draw with counter it (the start's for jump 1)
+      for (int k = tid - (j0 == 1 ? 32 : 0); k < nj * nc; k += blockDim.x - (j0 == 1 ? 32 : 0)) {
+        if (k < 0) break;   // thread 0's warp forms the schedule during the first chunk
+        const int jj = k / nc, q = k - jj * nc;
+        Real a, b;
+        if constexpr (PREC == 1) gauss2f(p.seed, (uint32_t)(c0 + q), (uint32_t)(j0 + jj), step, &a, &b);
+        else gauss2(p.seed, (uint32_t)(c0 + q), (uint32_t)(j0 + jj), step, &a, &b);
+        s_g[jj][q][0] = a; s_g[jj][q][1] = b;
+      }
+      __syncthreads();
+      if (mine) {
+        for (int jj = 0; jj < nj; ++jj) {
+          const int it = j0 + jj;
+          gx = s_g[jj][lane][0]; gy = s_g[jj][lane][1];
+          if constexpr (PREC == 1) {
+            const float mf = s_seqf[it];
+            const float sx = p.em_wx * mf, sy = p.em_wy * mf, hx = p.em_hx, hy = p.em_hy;
+            float x = fmaf(gx, sx, px), yv = fmaf(gy, sy, py);
+            if (x > hx) x = hx - (x - hx); else if (x < -hx) x = -hx - (x + hx);
+            if (yv > hy) yv = hy - (yv - hy); else if (yv < -hy) yv = -hy - (yv + hy);
+            px = x; py = yv;
+          } else {
+            const double sx = p.em_Lx * s_seq[it], sy = p.em_Ly * s_seq[it];
+            const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+            double x = gx * sx + px, yv = gy * sy + py;
+            if (x > hx) x = hx - (x - hx); else if (x < p.em_x0) x = (p.em_x0 - x) + p.em_x0;
+            if (yv > hy) yv = hy - (yv - hy); else if (yv < p.em_y0) yv = (p.em_y0 - yv) + p.em_y0;
+            px = x; py = yv;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();   // the schedule's end values
+  // the chains back to memory, as k_mh_vacuum leaves them
+  if (mine) {
+    const int k = base + c;
+    cs.ok[k] = start_ok ? 1 : 0;
+    if (!start_ok) {   // k_mh_init's record of a chain with no favourable start
+      cs.F[k] = 1.0; cs.sup[k] = -1.79769313486231570e308;
+      cs.x[k] = p.em_x0; cs.y[k] = p.em_y0;
+    } else {
+      cs.F[k] = F;
+      if constexpr (PREC == 1) {
+        cs.fx[k] = px; cs.fy[k] = py; cs.fsup[k] = rc; cs.fF[k] = Ff;
+        cs.fgx[k] = gx; cs.fgy[k] = gy;
+        cs.x[k] = p.org_x + (double)px * 1.0e-9;
+        cs.y[k] = p.org_y + (double)py * 1.0e-9;
+      } else {
+        cs.x[k] = px; cs.y[k] = py; cs.sup[k] = dsup; cs.gx[k] = gx; cs.gy[k] = gy;
+      }
+    }
+  }
+  if (tid == 0) {
+    if (!start_ok) atomicAdd(&y.chains_failed, nc);
+    __threadfence();
+    const int nblk = (M + RD_VU_CHAINS - 1) / RD_VU_CHAINS;
+    s_last = atomicAdd(&y.mh_done, 1) == nblk - 1;
+    if (s_last) {   // every block of the diode has read MH_std and a_rate
+      y.mh_done = 0;
+      y.MH_std = s_end[0];
+      y.a_rate = s_end[1];
+    }
+  }
 }
 
 // Field sums of one j-tile at CPT tip proposals (upper role: the point's own
@@ -2184,8 +2310,14 @@ cudaError_t rd_launch_mh_vacuum(int prec, int nslots, cudaStream_t st, const Dio
                                 const ChainState& cs, const int* ch_off, const double* wtab, const int* step_ptr,
                                 double kscale) {
   const int grid = nslots * RD_VAC_CTAS;
-  if (prec == 1) k_mh_vacuum<1><<<grid, RD_VAC_THREADS, 0, st>>>(P, Dy, cs, ch_off, wtab, step_ptr, kscale, nslots);
-  else k_mh_vacuum<0><<<grid, RD_VAC_THREADS, 0, st>>>(P, Dy, cs, ch_off, wtab, step_ptr, kscale, nslots);
+  const dim3 ugrid(RD_VAC_MAX_CHAINS / RD_VU_CHAINS, nslots);
+  if (prec == 1) {
+    k_mh_vacuum_uniform<1><<<ugrid, RD_VU_THREADS, 0, st>>>(P, Dy, cs, ch_off, wtab, step_ptr, kscale);
+    k_mh_vacuum<1><<<grid, RD_VAC_THREADS, 0, st>>>(P, Dy, cs, ch_off, wtab, step_ptr, kscale, nslots);
+  } else {
+    k_mh_vacuum_uniform<0><<<ugrid, RD_VU_THREADS, 0, st>>>(P, Dy, cs, ch_off, wtab, step_ptr, kscale);
+    k_mh_vacuum<0><<<grid, RD_VAC_THREADS, 0, st>>>(P, Dy, cs, ch_off, wtab, step_ptr, kscale, nslots);
+  }
   return cudaGetLastError();
 }
 

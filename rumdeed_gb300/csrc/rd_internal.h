@@ -148,6 +148,9 @@ struct DiodeDyn {
 #define RD_VAC_MAX_CHAINS (RD_VAC_CTAS * RD_VAC_THREADS * RD_VAC_CPT)
 #define RD_VAC_WTAB 512       // supply-target table entries staged in shared memory
 #define RD_VAC_MAXJ 1024      // jumps whose step-size schedule a uniform work function precomputes
+#define RD_VU_CHAINS 32       // chains per block of k_mh_vacuum_uniform (one lane each)
+#define RD_VU_THREADS 128     // its threads (all draw the Gaussian pairs)
+#define RD_VU_JCHUNK 64       // jumps whose Gaussian pairs a block holds at once
 #ifdef __CUDACC__
 __host__ __device__ inline bool rd_mh_vacuum(const DiodeParams& p, const DiodeDyn& y) {
   return p.geometry == RD_G_PLANAR && p.emission && !p.mh_serial && y.n == 0 && y.chains <= RD_VAC_MAX_CHAINS;

@@ -53,3 +53,41 @@ def test_vacuum_kernel_equals_tiled_kernels(rg, prec, jumps, work):
         assert empty[key] == atom[key], key
     assert empty["F_avg"] == atom["F_avg"]
     np.testing.assert_array_equal(s_empty, s_atom)
+
+
+def _engine_of_two(rg, prec, atom, jumps, work, steps):
+    eng = rg.Engine(precision=prec, max_diodes=2, particle_capacity=20000, chain_capacity=20000,
+                    quad_capacity=131072, event_capacity=1 << 16)
+    ds = []
+    for seed in (5, 6):
+        d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, time_step=0.25e-15, capacity=9000,
+                          emitter_pos=(-500 * NM, -500 * NM), emitter_dim=(1000 * NM, 1000 * NM),
+                          work=work, emission=True, mh_jumps=jumps, seed=seed)
+        if atom:
+            d.add_particles(np.array([[400 * NM, 400 * NM, 900 * NM]]), species=[rg.ATOM], step=0)
+        ds.append(d)
+    out = []
+    for s in range(1, steps + 1):
+        eng.step(s)
+        ev, lost = eng.events_take()
+        assert lost == 0
+        out.append([(d.counters(), sorted(tuple(e["pos"][:2]) for e in ev
+                                          if e["kind"] == rg.EVENT_EMIT and e["diode"] == d.index)) for d in ds])
+    eng.close()
+    return out
+
+
+@pytest.mark.parametrize("prec,work,steps", [(1, [[4.7]], 6), (0, [[4.7]], 3), (1, UNIFORM, 1)])
+def test_vacuum_uniform_two_diodes_over_steps(rg, prec, work, steps):
+    """Two vacuum-field diodes in one engine (the uniform kernel's second grid row),
+    over several steps: at 4.7 eV nothing is emitted, so the diodes stay empty and
+    MH_std climbs to its clamp, where the schedule takes its fixed point; at 2.2 eV
+    one step emits.  Every counter and emission site equals the tiled kernels'."""
+    empty = _engine_of_two(rg, prec, False, 100, work, steps)
+    atom = _engine_of_two(rg, prec, True, 100, work, steps)
+    for se, sa in zip(empty, atom):
+        for (ce, ee), (ca, ea) in zip(se, sa):
+            for key in ("N_sup", "chains", "chains_failed", "MH_std", "a_rate", "df_avg", "emitted_step"):
+                assert ce[key] == ca[key], key
+            assert ee == ea
+    assert empty[-1][0][0]["MH_std"] != empty[0][0][0]["MH_std"] or steps == 1
