@@ -2104,6 +2104,11 @@ k_mh_serial(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool p
   const DiodeParams& p = P[d];
   if (!p.active || !p.emission || !p.mh_serial || p.geometry != RD_G_PLANAR) return;
   DiodeDyn& y = Dy[d];
+  if (y.ser_done) {   // k_mh_serial_vacuum sampled this step's chains
+    __syncthreads();
+    if (threadIdx.x == 0) y.ser_done = 0;
+    return;
+  }
   const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
   const int M = y.chains, n0 = y.n, id0 = y.nrID;
   const int ndim = p.mh_jumps, ndim_first = (ndim + 2) / 4;
@@ -2360,11 +2365,162 @@ cudaError_t rd_launch_emit(int nslots, cudaStream_t st, const DiodeParams* P, Di
   return cudaGetLastError();
 }
 
+namespace {
+// The serial sampler (k_mh_serial) on a planar rectangle-emitter diode with no
+// particle in flight and a uniform work function, run speculatively in parallel.
+// Chains depend on each other only through the electrons earlier chains emit
+// in the step and through MH_std, which each chain updates once from its own
+// acceptance rate.  With no particle in flight the field at every point is the
+// vacuum field, and with a uniform work function every target is the same, so
+// until a chain emits every proposal is taken: each chain's acceptance rate is
+// 1, MH_std after chain c is known without running it (clamped to a fixed
+// point after a few chains), the start of every chain is its round-0 draw, and
+// its walk needs only its Gaussian pairs.  Blocks (x: group of RD_VU_CHAINS
+// chains, y: diode slot) draw the pairs of all (chain, jump) into shared memory
+// and walk each chain in one lane, as k_mh_vacuum_uniform does, with the
+// chain's own step size; then each chain takes its emission draw.  If no chain
+// of the diode emits (escape probabilities of ~1e-13 at 4.7 eV), the last
+// block to finish writes the step's results, exactly those k_mh_serial would
+// write but the escape-probability sum, which is M e (e the one escape
+// probability; k_mh_serial adds e M times, equal to within 2e-13), and sets
+// ser_done, so k_mh_serial leaves the diode.  If any chain emits, nothing is
+// written and k_mh_serial samples the diode from its first chain as usual.
+template <int PREC>
+__global__ void __launch_bounds__(RD_VU_THREADS)
+k_mh_serial_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, const double* __restrict__ work,
+                   const double* __restrict__ wtab, const int* __restrict__ step_ptr, double kscale) {
+  __shared__ DiodeParams sp;
+  __shared__ double s_mhs[RD_VU_CHAINS];           // MH_std each chain of the block walks with
+  __shared__ double s_end;                          // MH_std after the diode's last chain
+  __shared__ double s_g[RD_VU_JCHUNK][RD_VU_CHAINS][2];
+  const int d = blockIdx.y, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const DiodeParams& pg = P[d];
+  if (!pg.active || !pg.emission || !pg.mh_serial || pg.geometry != RD_G_PLANAR || pg.emitter_type == 4) return;
+  DiodeDyn& y = Dy[d];
+  if (y.n != 0 || y.chains <= 0 || y.chains > RD_VAC_MAX_CHAINS) return;   // the grid covers this many
+  const int M = y.chains, c0 = blockIdx.x * RD_VU_CHAINS;
+  if (c0 >= M) return;
+  {
+    const int* src = reinterpret_cast<const int*>(P + d);
+    int* dst = reinterpret_cast<int*>(&sp);
+    for (int k = tid; k < (int)(sizeof(DiodeParams) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+  }
+  __syncthreads();
+  const DiodeParams& p = sp;
+  const int cells = p.work_model == 1 ? p.work_nx * p.work_ny : (p.work_model == 4 ? p.work_nx : 0);
+  int differs = 0;
+  for (int k = tid; k < cells; k += blockDim.x)
+    for (int e = 0; e < 3; ++e)
+      differs |= __double_as_longlong(wtab[3 * (p.work_off + k) + e]) !=
+                 __double_as_longlong(wtab[3 * p.work_off + e]);
+  if (!(__syncthreads_or(differs) == 0 && cells >= 1)) return;
+  const int J = p.mh_jumps, ndim_first = (J + 2) / 4;
+  const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
+  const double F = z0_finish<PREC>(p, 0.0, kscale);   // what block_field_z0 gives with no particle
+  const bool found = F < 0.0 && p.init_rounds > 0;     // every chain starts at its round-0 draw, or none does
+  const bool updates = found && J > ndim_first;        // each chain updates MH_std once, at rate 1
+  const int nc = min(RD_VU_CHAINS, M - c0);
+  if (tid == 0) {   // MH_std of chains c0 .. c0 + nc - 1, and after chain M - 1
+    const double ar = (double)(J - ndim_first) / (double)(J - ndim_first);   // 1, formed as k_mh_serial forms it
+    const double g = exp(0.025 * (ar - 0.35));          // k_mh_serial's factor at that rate
+    double m = y.MH_std;
+    bool fixed = !updates;
+    for (int c = 0; c < M; ++c) {
+      if (c >= c0 && c < c0 + nc) s_mhs[c - c0] = m;
+      if (fixed) {   // every later chain walks with m
+        for (int k = max(c + 1, c0); k < c0 + nc; ++k) s_mhs[k - c0] = m;
+        break;
+      }
+      double nx = m * g;
+      if (nx > p.mh_hi) nx = p.mh_hi; else if (nx < p.mh_lo) nx = p.mh_lo;
+      fixed = nx == m;
+      m = nx;
+    }
+    s_end = m;
+  }
+  const int c = c0 + lane;
+  const bool mine = w == 1 && lane < nc;
+  double cx = p.em_x0, cy = p.em_y0;
+  if (mine && found) {
+    double u1, u2;
+    rng2(p.seed, (uint32_t)c, 0u, step, RNG_INIT, &u1, &u2);
+    cx = u1 * p.em_Lx + p.em_x0;
+    cy = u2 * p.em_Ly + p.em_y0;
+  }
+  if (found) {
+    for (int j0 = 1; j0 <= J; j0 += RD_VU_JCHUNK) {
+      const int nj = min(RD_VU_JCHUNK, J - j0 + 1);
+      __syncthreads();   // the previous chunk's walk is done with s_g, s_mhs is in place
+      for (int k = tid - (j0 == 1 ? 32 : 0); k < nj * nc; k += blockDim.x - (j0 == 1 ? 32 : 0)) {
+        if (k < 0) break;   // thread 0's warp forms the MH_std sequence during the first chunk
+        const int jj = k / nc, q = k - jj * nc;
+        double a, b;
+        gauss2(p.seed, (uint32_t)(c0 + q), (uint32_t)(j0 + jj), step, &a, &b);
+        s_g[jj][q][0] = a; s_g[jj][q][1] = b;
+      }
+      __syncthreads();
+      if (mine) {
+        const double mhs = s_mhs[lane];
+        const double hx = p.em_x0 + p.em_Lx, hy = p.em_y0 + p.em_Ly;
+        for (int jj = 0; jj < nj; ++jj) {   // k_mh_serial's rectangle step; every proposal taken
+          const int i = j0 + jj;
+          double sx = p.em_Lx * 0.10, sy = p.em_Ly * 0.10;
+          if (i > ndim_first) { sx = p.em_Lx * mhs; sy = p.em_Ly * mhs; }
+          double wx = s_g[jj][lane][0] * sx + cx;
+          double wy = s_g[jj][lane][1] * sy + cy;
+          if (wx > hx) wx = hx - (wx - hx); else if (wx < p.em_x0) wx = (p.em_x0 - wx) + p.em_x0;
+          if (wy > hy) wy = hy - (wy - hy); else if (wy < p.em_y0) wy = (p.em_y0 - wy) + p.em_y0;
+          cx = wx; cy = wy;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // each chain's emission draw against its escape probability
+  int emits = 0;
+  double D = -1.79769313486231570e308;
+  if (found) D = fn_escape_log(F, work_at(p, work, p.em_x0, p.em_y0, nullptr), p.image_charge);
+  if (mine) {
+    double Dc = found ? fn_escape_log(F, work_at(p, work, cx, cy, nullptr), p.image_charge) : D;
+    double u1, u2;
+    rng2(p.seed, (uint32_t)c, 0u, step, RNG_EMIT, &u1, &u2);
+    emits = log(u1) <= Dc;
+  }
+  emits = __syncthreads_or(emits);
+  if (tid == 0) {
+    if (emits) atomicOr(&y.ser_emit, 1);
+    __threadfence();
+    const int nblk = (M + RD_VU_CHAINS - 1) / RD_VU_CHAINS;
+    if (atomicAdd(&y.ser_ticket, 1) == nblk - 1) {   // every block of the diode is done
+      __threadfence();
+      if (atomicAdd(&y.ser_emit, 0) == 0) {   // no chain emitted: the step's results, as k_mh_serial
+        y.emitted_step = 0;
+        y.dropped_step = 0;
+        y.chains_failed = found ? 0 : M;
+        y.MH_std = s_end;
+        if (updates) y.a_rate = 1.0;
+        const double df_sum = found ? (double)M * exp(D) : 0.0;
+        y.df_avg = y.N_sup > 0.0 ? df_sum / y.N_sup : 0.0;
+        y.ser_done = 1;
+      }
+      y.ser_ticket = 0;
+      y.ser_emit = 0;
+    }
+  }
+}
+}  // namespace
+
 cudaError_t rd_launch_mh_serial(int prec, int nslots, cudaStream_t st, const DiodeParams* P, DiodeDyn* Dy,
                                 const Pool& pool, const double* work, const double* wtab,
                                 const int* step_ptr, double kscale, const EventLog& ev) {
-  if (prec == 1) k_mh_serial<1><<<nslots, 256, 0, st>>>(P, Dy, pool, work, wtab, step_ptr, kscale, ev);
-  else k_mh_serial<0><<<nslots, 256, 0, st>>>(P, Dy, pool, work, wtab, step_ptr, kscale, ev);
+  const dim3 vgrid(RD_VAC_MAX_CHAINS / RD_VU_CHAINS, nslots);
+  if (prec == 1) {
+    k_mh_serial_vacuum<1><<<vgrid, RD_VU_THREADS, 0, st>>>(P, Dy, work, wtab, step_ptr, kscale);
+    k_mh_serial<1><<<nslots, 256, 0, st>>>(P, Dy, pool, work, wtab, step_ptr, kscale, ev);
+  } else {
+    k_mh_serial_vacuum<0><<<vgrid, RD_VU_THREADS, 0, st>>>(P, Dy, work, wtab, step_ptr, kscale);
+    k_mh_serial<0><<<nslots, 256, 0, st>>>(P, Dy, pool, work, wtab, step_ptr, kscale, ev);
+  }
   return cudaGetLastError();
 }
 

@@ -123,6 +123,7 @@ struct DiodeDyn {
   int emitted_step, dropped_step;
   int chains, chains_failed, chains_capped;
   int mh_acc, mh_rej, mh_done;   // per-jump counters (reset by the last arriver)
+  int ser_ticket, ser_emit, ser_done;   // serial sampler, speculative vacuum pass (k_mh_serial_vacuum)
   int sup_done;
   int absorbed_top_step, absorbed_bot_step;
   int step_offset;       // this diode's step = engine step - step_offset

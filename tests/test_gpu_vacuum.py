@@ -91,3 +91,49 @@ def test_vacuum_uniform_two_diodes_over_steps(rg, prec, work, steps):
                 assert ce[key] == ca[key], key
             assert ee == ea
     assert empty[-1][0][0]["MH_std"] != empty[0][0][0]["MH_std"] or steps == 1
+
+
+def _serial_pair(rg, prec, atom, jumps, work, steps):
+    eng = rg.Engine(precision=prec, max_diodes=2, particle_capacity=20000, chain_capacity=20000,
+                    quad_capacity=131072, event_capacity=1 << 16)
+    ds = []
+    for seed in (11, 12):
+        d = eng.add_diode(V_s=2.0e3, gap=1000 * NM, time_step=0.25e-15, capacity=9000,
+                          emitter_pos=(-500 * NM, -500 * NM), emitter_dim=(1000 * NM, 1000 * NM),
+                          work=work, emission=True, mh_jumps=jumps, seed=seed, mh_serial=True)
+        if atom:
+            d.add_particles(np.array([[400 * NM, 400 * NM, 900 * NM]]), species=[rg.ATOM], step=0)
+        ds.append(d)
+    out = []
+    for s in range(1, steps + 1):
+        eng.step(s)
+        ev, lost = eng.events_take()
+        assert lost == 0
+        out.append([(d.counters(), sorted(tuple(e["pos"][:2]) for e in ev
+                                          if e["kind"] == rg.EVENT_EMIT and e["diode"] == d.index)) for d in ds])
+    eng.close()
+    return out
+
+
+@pytest.mark.parametrize("prec,work,steps", [(1, [[4.7]], 3), (0, [[4.7]], 2), (1, UNIFORM4, 1), (0, UNIFORM, 1)])
+def test_serial_sampler_vacuum_pass_equals_serial_kernel(rg, prec, work, steps):
+    """The serial sampler (mh_batch = .false.) on empty diodes with a uniform work
+    function: the speculative parallel pass (k_mh_serial_vacuum) against the serial
+    kernel itself, which a zero-charge atom forces (its field is the vacuum field bit
+    for bit).  At 4.7 eV no chain emits and the parallel pass gives the step's
+    results: every counter equals the serial kernel's, the escape-probability mean
+    to 1e-12 (M e against e added M times).  At 2.2 eV chains emit, the pass writes
+    nothing and the serial kernel samples the diode: every counter and emission
+    site equal."""
+    fast = _serial_pair(rg, prec, False, 100, work, steps)
+    slow = _serial_pair(rg, prec, True, 100, work, steps)
+    for sf, ss in zip(fast, slow):
+        for (cf, ef), (cs, es) in zip(sf, ss):
+            for key in ("N_sup", "chains", "chains_failed", "MH_std", "a_rate", "emitted_step", "dropped_step"):
+                assert cf[key] == cs[key], key
+            assert cf["df_avg"] == pytest.approx(cs["df_avg"], rel=1e-12, abs=1e-300)
+            assert ef == es
+    if work == [[4.7]]:
+        assert all(c["emitted_step"] == 0 for s in fast for c, _ in s)
+    else:
+        assert sum(c["emitted_step"] for s in fast for c, _ in s) > 0
