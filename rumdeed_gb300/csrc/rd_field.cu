@@ -2380,11 +2380,11 @@ namespace {
 // and walk each chain in one lane, as k_mh_vacuum_uniform does, with the
 // chain's own step size; then each chain takes its emission draw.  If no chain
 // of the diode emits (escape probabilities of ~1e-13 at 4.7 eV), the last
-// block to finish writes the step's results, exactly those k_mh_serial would
-// write but the escape-probability sum, which is M e (e the one escape
-// probability; k_mh_serial adds e M times, equal to within 2e-13), and sets
-// ser_done, so k_mh_serial leaves the diode.  If any chain emits, nothing is
-// written and k_mh_serial samples the diode from its first chain as usual.
+// block to finish writes the step's results, bit for bit those k_mh_serial
+// would write (the escape-probability sum, e added M times in order, by
+// rd_repeat_sum), and sets ser_done, so k_mh_serial leaves the diode.  If any
+// chain emits, nothing is written and k_mh_serial samples the diode from its
+// first chain as usual.
 template <int PREC>
 __global__ void __launch_bounds__(RD_VU_THREADS)
 k_mh_serial_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, const double* __restrict__ work,
@@ -2499,7 +2499,7 @@ k_mh_serial_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy,
         y.chains_failed = found ? 0 : M;
         y.MH_std = s_end;
         if (updates) y.a_rate = 1.0;
-        const double df_sum = found ? (double)M * exp(D) : 0.0;
+        const double df_sum = found ? rd_repeat_sum(exp(D), M) : 0.0;   // exp(D) added M times, as k_mh_serial adds it
         y.df_avg = y.N_sup > 0.0 ? df_sum / y.N_sup : 0.0;
         y.ser_done = 1;
       }

@@ -1,8 +1,9 @@
-// Host check of rd_split_exact against the FP64 form it replaces:
-//   hi = (float)v;  lo = (float)(v - (double)hi);
-// on random doubles over the magnitudes positions take in nm (and far
-// outside), on rounding ties and carries, and on the edges of the fast
-// range.  Prints the number of values checked and of bit mismatches.
+// Host check of rd_split.h against the FP64 forms it replaces: rd_split_exact
+// against  hi = (float)v;  lo = (float)(v - (double)hi);  on random doubles
+// over the magnitudes positions take in nm (and far outside), on rounding
+// ties and carries, and on the edges of the fast range; rd_repeat_sum against
+// the loop  s += e  (M terms) on random magnitudes, tie-prone values and
+// small M.  Prints the numbers checked and of bit mismatches.
 #include <cstdio>
 #include <cstdlib>
 #include <cmath>
@@ -55,6 +56,35 @@ int main(int argc, char** argv) {
         }
   check(0.0);
   check(-0.0);
-  printf("checked %lld mismatches %lld\n", checked, bad);
-  return bad != 0;
+  // rd_repeat_sum against the loop s += e, M terms
+  long long rchecked = 0, rbad = 0;
+  auto rcheck = [&](double e, int M) {
+    double s = 0.0;
+    for (int k = 0; k < M; ++k) s += e;
+    const double r = rd_repeat_sum(e, M);
+    ++rchecked;
+    uint64_t a, b;
+    memcpy(&a, &s, 8); memcpy(&b, &r, 8);
+    if (a != b) {
+      if (rbad < 10) printf("repeat-sum mismatch e=%.17g M=%d: %.17g vs %.17g\n", e, M, s, r);
+      ++rbad;
+    }
+  };
+  std::uniform_int_distribution<int> um(0, 9000);
+  for (long long k = 0; k < n / 200; ++k) {   // escape probabilities and any other magnitude
+    const double e = std::pow(10.0, -300.0 + 600.0 * u(rng));
+    rcheck(e, um(rng));
+  }
+  for (long long k = 0; k < n / 200; ++k) {   // low significand bits only: ties and carries in the binades
+    const uint64_t mant = (rng() & 0xffffull) | ((rng() & 1) ? (0xfffffull << 32) : 0);
+    rcheck(from_bits(((uint64_t)(1023 - 40 + (int)(rng() % 80)) << 52) | mant), um(rng));
+  }
+  for (int sh = 1; sh <= 14; ++sh)   // exact ties: the bits below a binade's ulp are one half
+    for (int M = 2; M <= 9000; M += 997)
+      rcheck(from_bits(((uint64_t)1000 << 52) | (1ull << (sh - 1))), M);
+  for (int M = 0; M <= 70; ++M) {
+    rcheck(1.0, M); rcheck(0.1, M); rcheck(3.0e-13, M); rcheck(0.0, M); rcheck(1.5, M);
+  }
+  printf("checked %lld mismatches %lld repeat-sums %lld mismatches %lld\n", checked, bad, rchecked, rbad);
+  return (bad != 0) || (rbad != 0);
 }
