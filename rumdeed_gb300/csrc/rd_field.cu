@@ -2055,11 +2055,12 @@ k_emit(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool, 
 }  // namespace
 
 // ---- serial MH sampler (mh_batch = .false.) ---------------------------------------------
-// F_z at one cathode point from the diode's first n particles, summed by the
-// whole block (every thread gets the total).
+// The pair sum of F_z at one cathode point over the diode's first n
+// particles, summed by the whole block (every thread gets the total, before
+// z0_finish).
 template <int PREC>
-__device__ double block_field_z0(const DiodeParams& p, const Pool& pool, int n, double px, double py,
-                                 double kscale, double* red) {
+__device__ double block_field_sum(const DiodeParams& p, const Pool& pool, int n, double px, double py,
+                                  double* red) {
   const int tid = threadIdx.x, nt = blockDim.x, off = p.off;
   const int nic = p.image_charge ? p.N_ic_max : 0;
   double s;
@@ -2080,7 +2081,7 @@ __device__ double block_field_z0(const DiodeParams& p, const Pool& pool, int n, 
       s += z0_tile_f64(&pj, 1, px, py, nic, p.d, c_k.L2);
     }
   }
-  return z0_finish<PREC>(p, block_sum(s, red), kscale);
+  return block_sum(s, red);
 }
 
 // The serial branch of Do_Field_Emission_Planar_rectangle (:322-333, 338-383)
@@ -2092,14 +2093,22 @@ __device__ double block_field_z0(const DiodeParams& p, const Pool& pool, int n, 
 // with 10 % of the emitter as the step, then MH_std), updates MH_std once from
 // its own acceptance rate after the warm-up, and its electron, if the escape
 // test passes, is added before the next chain starts, so later chains see it.
-// Same Philox counters as the batched sampler; every thread follows the same
-// control flow (the field sum is block-reduced and broadcast).
+// Same Philox counters as the batched sampler.  The whole block sums the field
+// at each point (block_field_sum); thread 0 alone holds the chain and does the
+// rest (draws, proposals, targets, decisions: FP64 work, which every warp
+// would otherwise repeat on the part's narrow FP64 pipe) and hands the block
+// the next point through shared memory.
 template <int PREC>
 __global__ void __launch_bounds__(256)
 k_mh_serial(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool pool,
             const double* __restrict__ work, const double* __restrict__ wtab,
             const int* __restrict__ step_ptr, double kscale, EventLog ev) {
   __shared__ double red[256];
+  // thread 0 -> block, one slot per jump parity (a slot is rewritten only after a
+  // barrier that every reader of its last value has passed)
+  __shared__ double s_pt[2][2];   // the point whose field the block sums next
+  __shared__ int s_sum[2];        // the block sums a field this jump (a ring proposal off the ring: no)
+  __shared__ int s_found, s_add, s_stop;   // the chain started; a particle was added; the chains stop
   const int d = blockIdx.x;
   const DiodeParams& p = P[d];
   if (!p.active || !p.emission || !p.mh_serial || p.geometry != RD_G_PLANAR) return;
@@ -2109,10 +2118,13 @@ k_mh_serial(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool p
     if (threadIdx.x == 0) y.ser_done = 0;
     return;
   }
+  const bool t0 = threadIdx.x == 0;
   const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
   const int M = y.chains, n0 = y.n, id0 = y.nrID;
   const int ndim = p.mh_jumps, ndim_first = (ndim + 2) / 4;
-  int n = n0, emitted = 0, dropped = 0, failed = 0;
+  int n = n0;   // particles the field sums see (every thread)
+  // thread 0's state
+  int emitted = 0, dropped = 0, failed = 0;
   double mhs = y.MH_std, a_rate = y.a_rate, df_sum = 0.0;
   const bool ring = p.emitter_type == 4;
   const double twopi = 2.0 * c_k.pi, rmin = p.ring_rmin, rmax = p.ring_rmin + p.ring_thick;
@@ -2120,44 +2132,68 @@ k_mh_serial(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool p
     double cx = p.em_x0, cy = p.em_y0, F = 1.0;
     double ca = 0.0, cr = rmin;   // ring: (angle, radius) of the chain (Metropolis_Hastings_ring_J)
     bool found = false;
-    for (int r = 0; r < p.init_rounds && !found; ++r) {
-      double u1, u2;
-      rng2(p.seed, (uint32_t)c, (uint32_t)r, step, RNG_INIT, &u1, &u2);
-      if (ring) {
-        ca = u1 * twopi;
-        cr = rmin + u2 * p.ring_thick;
-        cx = cr * cos(ca);
-        cy = cr * sin(ca);
-      } else {
-        cx = u1 * p.em_Lx + p.em_x0;
-        cy = u2 * p.em_Ly + p.em_y0;
+    if (t0) s_found = 0;
+    for (int r = 0; r < p.init_rounds; ++r) {
+      if (t0) {
+        double u1, u2;
+        rng2(p.seed, (uint32_t)c, (uint32_t)r, step, RNG_INIT, &u1, &u2);
+        if (ring) {
+          ca = u1 * twopi;
+          cr = rmin + u2 * p.ring_thick;
+          cx = cr * cos(ca);
+          cy = cr * sin(ca);
+        } else {
+          cx = u1 * p.em_Lx + p.em_x0;
+          cy = u2 * p.em_Ly + p.em_y0;
+        }
+        s_pt[0][0] = cx; s_pt[0][1] = cy;
       }
-      F = block_field_z0<PREC>(p, pool, n, cx, cy, kscale, red);
-      found = F < 0.0;
+      __syncthreads();
+      const double sum = block_field_sum<PREC>(p, pool, n, s_pt[0][0], s_pt[0][1], red);
+      if (t0) {
+        F = z0_finish<PREC>(p, sum, kscale);
+        found = F < 0.0;
+        s_found = found;
+      }
+      __syncthreads();
+      if (s_found) break;
     }
+    __syncthreads();   // s_found final (also with no start rounds)
     double D = -1.79769313486231570e308, Fout = 1.0;
-    if (!found) {
-      cx = ring ? rmin : p.em_x0;
-      cy = ring ? 0.0 : p.em_y0;
-      ++failed;
-    } else {
-      Fout = F;
-      // ring: log(radius) is the Jacobian of the (angle, radius) parametrisation (:1592-1596)
-      double sup_cur = supply_log_xy(p, wtab, cx, cy, F) + (ring ? log(cr) : 0.0);
-      int ja = 0, jr = 0;
-      double sx = (ring ? twopi : p.em_Lx) * 0.10, sy = (ring ? p.ring_thick : p.em_Ly) * 0.10;
-      for (int i = 1; i <= ndim; ++i) {
+    double sup_cur = 0.0, sx = 0.0, sy = 0.0;
+    int ja = 0, jr = 0;
+    if (t0) {
+      if (!found) {
+        cx = ring ? rmin : p.em_x0;
+        cy = ring ? 0.0 : p.em_y0;
+        ++failed;
+      } else {
+        Fout = F;
+        // ring: log(radius) is the Jacobian of the (angle, radius) parametrisation (:1592-1596)
+        sup_cur = supply_log_xy(p, wtab, cx, cy, F) + (ring ? log(cr) : 0.0);
+        sx = (ring ? twopi : p.em_Lx) * 0.10;
+        sy = (ring ? p.ring_thick : p.em_Ly) * 0.10;
+      }
+    }
+    const bool walk = s_found != 0;   // every thread: the chain found a start
+    for (int i = 1; walk && i <= ndim; ++i) {
+      double wx = 0.0, wy = 0.0, na = 0.0, nr = 0.0;
+      if (t0) {
         if (i > ndim_first) { sx = (ring ? twopi : p.em_Lx) * mhs; sy = (ring ? p.ring_thick : p.em_Ly) * mhs; }
         double g1, g2;
         gauss2(p.seed, (uint32_t)c, (uint32_t)i, step, &g1, &g2);
-        double wx, wy, na = 0.0, nr = 0.0;
+        int sum_it = 1;
         if (ring) {   // angle wrapped (Fortran MODULO), radius outside the ring rejected
           const double a = g1 * sx + ca;
           na = a - floor(a / twopi) * twopi;
           nr = g2 * sy + cr;
-          if (nr < rmin || nr > rmax) { if (i > ndim_first) ++jr; continue; }
-          wx = nr * cos(na);
-          wy = nr * sin(na);
+          if (nr < rmin || nr > rmax) {
+            if (i > ndim_first) ++jr;
+            sum_it = 0;
+          } else {
+            wx = nr * cos(na);
+            wy = nr * sin(na);
+          }
         } else {
           wx = g1 * sx + cx;
           wy = g2 * sy + cy;
@@ -2165,76 +2201,98 @@ k_mh_serial(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy, Pool p
           if (wx > hx) wx = hx - (wx - hx); else if (wx < p.em_x0) wx = (p.em_x0 - wx) + p.em_x0;
           if (wy > hy) wy = hy - (wy - hy); else if (wy < p.em_y0) wy = (p.em_y0 - wy) + p.em_y0;
         }
-        const double Fw = block_field_z0<PREC>(p, pool, n, wx, wy, kscale, red);
-        if (Fw >= 0.0) { if (i > ndim_first) ++jr; continue; }
-        const double sn = supply_log_xy(p, wtab, wx, wy, Fw) + (ring ? log(nr) : 0.0);
-        bool take = sn >= sup_cur;
-        if (!take) {
-          double u1, u2;
-          rng2(p.seed, (uint32_t)c, (uint32_t)i, step, RNG_ACCEPT, &u1, &u2);
-          take = log(u1) <= sn - sup_cur;
-        }
-        if (take) {
-          cx = wx; cy = wy; sup_cur = sn; Fout = Fw; ca = na; cr = nr;
-          if (i > ndim_first) ++ja;
-        } else if (i > ndim_first) {
-          ++jr;
+        s_pt[i & 1][0] = wx; s_pt[i & 1][1] = wy;
+        s_sum[i & 1] = sum_it;
+      }
+      __syncthreads();
+      if (!s_sum[i & 1]) continue;   // block-uniform: a ring proposal off the ring, no field needed
+      const double sum = block_field_sum<PREC>(p, pool, n, s_pt[i & 1][0], s_pt[i & 1][1], red);
+      if (t0) {
+        const double Fw = z0_finish<PREC>(p, sum, kscale);
+        if (Fw >= 0.0) {
+          if (i > ndim_first) ++jr;
+        } else {
+          const double sn = supply_log_xy(p, wtab, wx, wy, Fw) + (ring ? log(nr) : 0.0);
+          bool take = sn >= sup_cur;
+          if (!take) {
+            double u1, u2;
+            rng2(p.seed, (uint32_t)c, (uint32_t)i, step, RNG_ACCEPT, &u1, &u2);
+            take = log(u1) <= sn - sup_cur;
+          }
+          if (take) {
+            cx = wx; cy = wy; sup_cur = sn; Fout = Fw; ca = na; cr = nr;
+            if (i > ndim_first) ++ja;
+          } else if (i > ndim_first) {
+            ++jr;
+          }
         }
       }
-      if (ja + jr > 0) {   // MH_std_update once per chain (:1251-1254, :603-612)
-        a_rate = (double)ja / (double)(jr + ja);
-        mhs = mhs * exp(0.025 * (a_rate - 0.35));
-        if (mhs > p.mh_hi) mhs = p.mh_hi; else if (mhs < p.mh_lo) mhs = p.mh_lo;
-      }
-      D = fn_escape_log(Fout, work_at(p, work, cx, cy, nullptr), p.image_charge);
     }
-    if (Fout >= 0.0) {
-      D = -1.79769313486231570e308;
-      if (ring) break;   // the ring emitter's loop stops at an unfavourable chain (:447-455)
-    }
-    df_sum += exp(D);
-    double u1, u2;
-    rng2(p.seed, (uint32_t)c, 0u, step, RNG_EMIT, &u1, &u2);
-    if (log(u1) <= D) {
-      if (n < p.cap) {   // Add_Particle (src/mod_pair.F90:29-159), visible to the next chains
-        if (threadIdx.x == 0) {
-          const int gi = p.off + n;
-          const double X = cx, Y = cy, Z = 1.0 * c_k.length_scale;
-          int sec = 1;
-          work_at(p, work, X, Y, &sec);
-          double ex, ey, ez;
-          vacuum_field(p, X, Y, Z, &ex, &ey, &ez);
-          const double qm = (-1.0 * c_k.q0) / (1.0 * c_k.m0);
-          pool.x[gi] = X; pool.y[gi] = Y; pool.z[gi] = Z;
-          pool.vx[gi] = 0.0; pool.vy[gi] = 0.0; pool.vz[gi] = 0.0;
-          pool.ax[gi] = pool.bx[gi] = pool.cx[gi] = qm * ex;
-          pool.ay[gi] = pool.by[gi] = pool.cy[gi] = qm * ey;
-          pool.az[gi] = pool.bz[gi] = pool.cz[gi] = qm * ez;
-          pool.q[gi] = -1.0 * c_k.q0;
-          pool.m[gi] = 1.0 * c_k.m0;
-          pool.species[gi] = 1;
-          pool.id[gi] = id0 + emitted;
-          pool.step0[gi] = (int)step;
-          pool.section[gi] = sec;
-          pool.mask[gi] = 1;
-          float4 h, l;   // its cathode pack, for the FP32 field sums of the next chains
-          split_nm(X, p.org_x, &h.x, &l.x);
-          split_nm(Y, p.org_y, &h.y, &l.y);
-          const float zf = (float)(Z * 1.0e9), qf = -1.0f;
-          pool.zk_hi[gi] = make_float4(h.x, h.y, fmaxf(zf * zf, 1e-20f), qf * zf);
-          pool.zk_lo[gi] = make_float4(l.x, l.y, zf, qf);
-          log_event(ev, X, Y, Z, 0.0, 0.0, 0.0, d, RD_EVENT_EMIT, sec, id0 + emitted, 1, (int)step);
+    // the chain's end: MH_std, the escape test and its electron (thread 0)
+    if (t0) {
+      s_add = 0;
+      s_stop = 0;
+      if (found) {
+        if (ja + jr > 0) {   // MH_std_update once per chain (:1251-1254, :603-612)
+          a_rate = (double)ja / (double)(jr + ja);
+          mhs = mhs * exp(0.025 * (a_rate - 0.35));
+          if (mhs > p.mh_hi) mhs = p.mh_hi; else if (mhs < p.mh_lo) mhs = p.mh_lo;
         }
-        __threadfence_block();
-        __syncthreads();
-        ++n;
-        ++emitted;
+        D = fn_escape_log(Fout, work_at(p, work, cx, cy, nullptr), p.image_charge);
+      }
+      bool stop = false;
+      if (Fout >= 0.0) {
+        D = -1.79769313486231570e308;
+        stop = ring;   // the ring emitter's loop stops at an unfavourable chain (:447-455)
+      }
+      if (stop) {
+        s_stop = 1;
       } else {
-        ++dropped;
+        df_sum += exp(D);
+        double u1, u2;
+        rng2(p.seed, (uint32_t)c, 0u, step, RNG_EMIT, &u1, &u2);
+        if (log(u1) <= D) {
+          if (n < p.cap) {   // Add_Particle (src/mod_pair.F90:29-159), visible to the next chains
+            const int gi = p.off + n;
+            const double X = cx, Y = cy, Z = 1.0 * c_k.length_scale;
+            int sec = 1;
+            work_at(p, work, X, Y, &sec);
+            double ex, ey, ez;
+            vacuum_field(p, X, Y, Z, &ex, &ey, &ez);
+            const double qm = (-1.0 * c_k.q0) / (1.0 * c_k.m0);
+            pool.x[gi] = X; pool.y[gi] = Y; pool.z[gi] = Z;
+            pool.vx[gi] = 0.0; pool.vy[gi] = 0.0; pool.vz[gi] = 0.0;
+            pool.ax[gi] = pool.bx[gi] = pool.cx[gi] = qm * ex;
+            pool.ay[gi] = pool.by[gi] = pool.cy[gi] = qm * ey;
+            pool.az[gi] = pool.bz[gi] = pool.cz[gi] = qm * ez;
+            pool.q[gi] = -1.0 * c_k.q0;
+            pool.m[gi] = 1.0 * c_k.m0;
+            pool.species[gi] = 1;
+            pool.id[gi] = id0 + emitted;
+            pool.step0[gi] = (int)step;
+            pool.section[gi] = sec;
+            pool.mask[gi] = 1;
+            float4 h, l;   // its cathode pack, for the FP32 field sums of the next chains
+            split_nm(X, p.org_x, &h.x, &l.x);
+            split_nm(Y, p.org_y, &h.y, &l.y);
+            const float zf = (float)(Z * 1.0e9), qf = -1.0f;
+            pool.zk_hi[gi] = make_float4(h.x, h.y, fmaxf(zf * zf, 1e-20f), qf * zf);
+            pool.zk_lo[gi] = make_float4(l.x, l.y, zf, qf);
+            log_event(ev, X, Y, Z, 0.0, 0.0, 0.0, d, RD_EVENT_EMIT, sec, id0 + emitted, 1, (int)step);
+            ++emitted;
+            s_add = 1;
+            __threadfence_block();
+          } else {
+            ++dropped;
+          }
+        }
       }
     }
+    __syncthreads();
+    if (s_stop) break;
+    if (s_add) ++n;
   }
-  if (threadIdx.x == 0) {
+  if (t0) {
     y.n = n;
     y.nrID = id0 + emitted;
     y.emitted_step = emitted;
