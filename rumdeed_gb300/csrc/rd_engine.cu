@@ -544,7 +544,7 @@ static int launch_emission(rd_engine* e) {
   if (s.emit_serial) {   // serial MH diodes: chains one after another, one block per diode
     CK(rd_launch_mh_serial(prec, ns, e->st, e->dP, e->dD, e->pool, e->work, e->wtab, e->d_step, e->kscale,
                            e->evlog));
-    e->kernels_in_step++;
+    e->kernels_in_step += 2;   // the parallel pass for empty diodes, and the serial kernel
   }
   return RD_OK;
 }
