@@ -2474,7 +2474,7 @@ k_mh_serial_vacuum(const DiodeParams* __restrict__ P, DiodeDyn* __restrict__ Dy,
   if (!(__syncthreads_or(differs) == 0 && cells >= 1)) return;
   const int J = p.mh_jumps, ndim_first = (J + 2) / 4;
   const uint32_t step = (uint32_t)(*step_ptr - y.step_offset);
-  const double F = z0_finish<PREC>(p, 0.0, kscale);   // what block_field_z0 gives with no particle
+  const double F = z0_finish<PREC>(p, 0.0, kscale);   // k_mh_serial's field with no particle: z0_finish of a zero sum
   const bool found = F < 0.0 && p.init_rounds > 0;     // every chain starts at its round-0 draw, or none does
   const bool updates = found && J > ndim_first;        // each chain updates MH_std once, at rate 1
   const int nc = min(RD_VU_CHAINS, M - c0);
